@@ -1,0 +1,362 @@
+#!/usr/bin/env python3
+"""Walker-step benchmark (one JSON line on rank 0).
+
+Default workload: weighted DeepWalk (static alias sampling), walk length 80,
+4,194,304 walkers (one per vertex) on a seeded R-MAT scale-22 graph (edge
+factor 16, a/b/c = 0.57/0.19/0.19, undirected, lognormal(0,1) float32
+weights); every step rebuilds the alias tables on the GPU and walks all
+walkers (the reference includes the alias build in its timings).
+
+value : walker-steps/s with the graph resident in HBM and paths written to HBM
+        (kk_walk_device), device time from CUDA events on the engine's stream.
+e2e   : the same walk through the public C-ABI call kk_walk_into: the start-vertex
+        list is copied host->device and every path is copied device->host into
+        pinned host memory, inside the timed region.
+roofline: the walk kernel's bytes touched per walker-step at 32-byte sector
+        granularity (sampling part only) over its CUDA-event duration, against
+        the measured HBM copy bandwidth.
+cpu_baseline / --impl reference: the CPU restatement of the reference's path
+        (oracle/kk_oracle.c, pinned bit-for-bit to the reference) on all host
+        cores, over a bounded sample of the same workload.
+
+Multi-GPU (torchrun): weak scaling, each rank walks its own walker-id range on
+its own replica of the graph; no collective on the data path.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "deepwalk-s22": dict(app="deepwalk", scale=22, weights=2, types=0, walk_length=80,
+                         desc="weighted DeepWalk (alias sampling, alias build included), len 80, one walker per vertex, "
+                              "R-MAT scale 22 ef16 lognormal(0,1) weights"),
+    "node2vec-s16": dict(app="node2vec", scale=16, weights=1, types=0, walk_length=80, p=2.0, q=0.5,
+                         desc="node2vec p=2 q=0.5 len 80, 65,536 walkers, R-MAT scale 16 ef16 uniform[1,5) weights"),
+    "ppr-s24": dict(app="ppr", scale=24, weights=0, types=0, terminate_prob=1.0 / 80,
+                    desc="PPR terminate 1/80, unweighted, one walker per vertex, R-MAT scale 24 ef16"),
+    "metapath-s22": dict(app="metapath", scale=22, weights=1, types=5, walk_length=80,
+                         schemes=[[1, 2, 4, 8], [2, 8, 2, 16], [4, 1, 16, 4]], scheme_round_robin=True,
+                         desc="metapath len 80, 3 schemes of 4 one-hot type masks round robin, R-MAT scale 22 ef16, "
+                              "5 edge types, uniform[1,5) weights"),
+    "node2vec-s24": dict(app="node2vec", scale=24, weights=1, types=0, walk_length=80, p=2.0, q=0.5,
+                         desc="node2vec p=2 q=0.5 len 80, one walker per vertex, R-MAT scale 24 ef16 uniform[1,5)"),
+}
+
+# Bytes touched per walker-step by the walk kernel, at 32 B sector granularity:
+# int64 offset pair 16 B spans 1.25 sectors on average (40 B); a 16 B-aligned
+# alias bucket is one sector (32 B); the chosen neighbour id one sector (32 B);
+# the 4 B path write is coalesced by L2 into full sectors (4 B).
+B_STEP = {"deepwalk": 40 + 32 + 32 + 4, "ppr": 40 + 32 + 4}
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce(world, value, op):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def walk_kwargs(wl):
+    kw = {}
+    for k in ("walk_length", "terminate_prob", "p", "q", "schemes", "scheme_round_robin"):
+        if k in wl:
+            kw[k] = wl[k]
+    return kw
+
+
+def cpu_sample(g, wl, walkers, threads, seed, target_steps=2_000_000, chunks=16):
+    """Times the oracle (CPU restatement) on a bounded sample of the workload.
+
+    Alias tables (weighted) are built once for the whole graph and their time
+    is charged per walker (t_alias * sample/walkers); the walk runs `chunks`
+    contiguous walker-id ranges spread over the id space.
+    """
+    from oracle import pyoracle
+    csr = pyoracle.CSR(g["V"], g["off"], g["nbr"], g.get("w"), g.get("type"))
+    weighted = g.get("w") is not None
+    per_walker = max(1, wl.get("walk_length", 80))
+    sample = max(chunks * 64, min(walkers, target_steps // per_walker))
+    chunk = max(1, sample // chunks)
+    kw = walk_kwargs(wl)
+    t_alias = 0.0
+    if weighted:
+        t0 = time.perf_counter()
+        pyoracle.alias_build(csr, threads=threads)
+        t_alias = time.perf_counter() - t0
+    steps = 0
+    t_walk = 0.0
+    n_done = 0
+    for c in range(chunks):
+        begin = (walkers // chunks) * c
+        prm = pyoracle.make_params(wl["app"], seed=seed, walker_begin=begin, walker_num=chunk, weighted=weighted, **kw)
+        _, _, st = pyoracle.walk(csr, prm, cap=1, threads=threads, with_paths=False)
+        _, tw = pyoracle.last_timing()
+        steps += st
+        t_walk += tw
+        n_done += chunk
+    t_total = t_walk + t_alias * (n_done / walkers)
+    return {
+        "value": steps / t_total, "unit": "walker-steps/s", "cores": threads, "kind": "port",
+        "sample": "%d walkers in %d id ranges spread over %d (%d steps, %.2f s walking); alias build over the "
+                  "full graph %.2f s charged pro rata" % (n_done, chunks, walkers, steps, t_walk, t_alias),
+    }
+
+
+def run_reference(args, wl, world, rank, local):
+    """The reference's CPU path (its C restatement, pinned to the reference) on all host cores."""
+    if rank != 0:
+        return
+    from oracle import pyoracle
+    pyoracle.build()
+    g = pyoracle.rmat_graph(wl["scale"], 16, seed=wl["scale"], weights=wl["weights"], types=wl["types"])
+    walkers = g["V"] if wl["app"] != "node2vec" or wl["scale"] != 16 else 65536
+    threads = os.cpu_count() or 1
+    vals = []
+    for _ in range(args.warmup):
+        cpu_sample(g, wl, walkers, threads, seed=1, target_steps=500_000, chunks=4)
+    for _ in range(args.steps):
+        vals.append(cpu_sample(g, wl, walkers, threads, seed=1))
+    value = statistics.median(v["value"] for v in vals)
+    line = {
+        "impl": "reference", "metric": "walker-steps/s", "value": value, "unit": "walker-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded R-MAT)",
+        "config": {"workload": args.workload, "desc": wl["desc"], "walkers": walkers},
+        "cpu_baseline": dict(vals[-1], value=value),
+        "e2e": {"value": value, "unit": "walker-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, wl, world, rank, local):
+    import numpy as np
+    import torch
+
+    import knightking_gb300 as kk
+
+    torch.cuda.set_device(local)
+    engine = kk.WalkEngine(local)
+    engine.generate_rmat(wl["scale"], 16, seed=wl["scale"], weights=wl["weights"], types=wl["types"])
+    V, E, _, _ = engine.info()
+    walkers = V if not (wl["app"] == "node2vec" and wl["scale"] == 16) else 65536
+    walker_begin = rank * walkers
+    kw = walk_kwargs(wl)
+    stream = torch.cuda.Stream()
+    engine.set_stream(stream.cuda_stream)
+    app = wl["app"]
+
+    def step():
+        steps, _, _, _ = engine.walk_device(app, walkers, paths=False, seed=1, walker_begin=walker_begin, **kw)
+        return steps
+
+    for _ in range(args.warmup):
+        step()
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    total_steps = 0
+    walk_ms = []
+    alias_ms = []
+    with ClockSampler(local) as clocks:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            total_steps += step()
+            a, w = engine.last_timing()
+            alias_ms.append(a)
+            walk_ms.append(w)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    barrier(world)
+    elapsed_ms = allreduce(world, elapsed_ms, "max")
+    all_steps = allreduce(world, float(total_steps), "sum")
+    value = all_steps / (elapsed_ms / 1e3)
+
+    # ---- e2e: public C-ABI call with host buffers and copies in the timed region ----
+    start = np.arange(walkers, dtype=np.uint32) % np.uint32(V)
+    cap_per = (wl.get("walk_length", 0) + 1) if "walk_length" in wl else 0
+    if cap_per == 0:
+        cap_vertices = int(total_steps // args.steps) + walkers + 1024
+    else:
+        cap_vertices = walkers * cap_per
+    h_len = torch.empty(walkers, dtype=torch.int32, pin_memory=True)
+    h_off = torch.empty(walkers, dtype=torch.int64, pin_memory=True)
+    h_vert = torch.empty(cap_vertices, dtype=torch.int32, pin_memory=True)
+    e2e_steps = 0
+    e2e_runs = max(1, min(args.steps, 3))
+    engine.walk_into(app, walkers, h_len.data_ptr(), h_off.data_ptr(), h_vert.data_ptr(), cap_vertices, seed=1,
+                     walker_begin=walker_begin, start=start, **kw)
+    barrier(world)
+    t0 = time.perf_counter()
+    d2h = 0
+    for _ in range(e2e_runs):
+        st = engine.walk_into(app, walkers, h_len.data_ptr(), h_off.data_ptr(), h_vert.data_ptr(), cap_vertices,
+                              seed=1, walker_begin=walker_begin, start=start, **kw)
+        e2e_steps += st
+        d2h += walkers * 4 + walkers * 8 + (st + walkers) * 4
+    e2e_s = time.perf_counter() - t0
+    e2e_s = allreduce(world, e2e_s, "max")
+    e2e_value = allreduce(world, float(e2e_steps), "sum") / e2e_s
+
+    # ---- roofline of the walk kernel ----
+    peak, peak_kind = load_peaks()
+    steps_per_launch = total_steps / args.steps
+    b_step = B_STEP.get(app)
+    mean_walk_ms = statistics.mean(walk_ms)
+    roof = None
+    if b_step is not None:
+        achieved = steps_per_launch * b_step / (mean_walk_ms / 1e3) / 1e9
+        traffic = None
+        tf = os.path.join(ROOT, "profiles", "traffic_%s.json" % args.workload)
+        if os.path.exists(tf):
+            with open(tf) as f:
+                traffic = json.load(f)["dram_bytes_per_step"] * steps_per_launch
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "peak_kind": peak_kind, "bytes_per_step": b_step,
+                "kernel": "walk_first_order_kernel" if app != "node2vec" else "walk_second_order_kernel",
+                "kernel_ms": mean_walk_ms, "alias_build_ms": statistics.mean(alias_ms)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        g = engine.download_graph()
+        cpu = cpu_sample(g, wl, walkers, os.cpu_count() or 1, seed=1)
+
+    if rank == 0:
+        line = {
+            "metric": "walker-steps/s", "value": value, "unit": "walker-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded R-MAT generated on the GPU)",
+            "config": {"workload": args.workload, "desc": wl["desc"], "vertices": V, "edges": E,
+                       "walkers_per_gpu": walkers, "walker_steps_per_step": steps_per_launch,
+                       "l2": "inputs larger than L2 (graph + alias tables > 129 MB)", "parallelism": "replicas"},
+            "e2e": {"value": e2e_value, "unit": "walker-steps/s", "h2d_bytes_per_step": walkers * 4 + 256,
+                    "d2h_bytes_per_step": d2h // e2e_runs},
+            "gpu_launches": 2 * args.steps if wl["weights"] else args.steps,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    engine.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="deepwalk-s22", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    wl = WORKLOADS[args.workload]
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, wl, world, rank, local)
+    else:
+        run_ours(args, wl, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

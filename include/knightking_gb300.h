@@ -1,0 +1,183 @@
+/*
+ * knightking_gb300: C-ABI of the GB300 walker-step engine.
+ *
+ * Drop-in replacement, on one GPU, for KnightKing's WalkEngine::random_walk()
+ * path (include/walk.hpp:423-436 of the reference) and the graph/path plumbing
+ * around it.  Plain C types only; every call returns a kk_status and never
+ * throws.  Paths are bit-identical to the reference's sampler fed the same
+ * counter-based Philox stream (see KK_RNG_* below).
+ *
+ * Threading: one engine is driven by one host thread at a time.
+ */
+#ifndef KNIGHTKING_GB300_H
+#define KNIGHTKING_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference asserts or exits instead) ------------- */
+typedef int kk_status;
+#define KK_OK 0
+#define KK_ERR_INVALID_CONFIG 1 /* include/walk.hpp:251-261 asserts, bad sizes */
+#define KK_ERR_OOM 2
+#define KK_ERR_IO 3           /* include/storage.hpp:39 assert, include/graph.hpp:427 exit */
+#define KK_ERR_TRIAL_LIMIT 4  /* a walker exceeded the rejection-trial cap */
+#define KK_ERR_TIMEOUT 5
+#define KK_ERR_CUDA 6
+#define KK_ERR_NO_GRAPH 7
+#define KK_ERR_PATH_CAPACITY 8
+
+/* ---- edge kinds of the binary edge-list file (include/type.hpp:43-85) --- */
+#define KK_EDGE_UNWEIGHTED 0   /* Edge<EmptyData>:          {u32 src, u32 dst}           8 B */
+#define KK_EDGE_F32 1          /* Edge<real_t>:             {u32 src, u32 dst, f32 w}   12 B */
+#define KK_EDGE_META 2         /* Edge<UnweightedMetaData>: {u32 src, u32 dst, i32 type} 12 B */
+#define KK_EDGE_META_F32 3     /* Edge<WeightedMetaData>:   {src, dst, f32 w, i32 type}  16 B */
+
+/* ---- built-in apps (the reference's src/apps functors) ------------------ */
+#define KK_APP_DEEPWALK 0  /* src/apps/deepwalk.hpp:30-47 */
+#define KK_APP_PPR 1       /* src/apps/ppr.hpp:30-64 */
+#define KK_APP_NODE2VEC 2  /* src/apps/node2vec.hpp:108-202 */
+#define KK_APP_METAPATH 3  /* src/apps/metapath.hpp:70-128 */
+
+#define KK_MAX_SCHEMES 16
+#define KK_MAX_SCHEME_LEN 16
+
+/* Random stream: Philox4x32-10, key = seed, counter = (walker id, step,
+ * draw >> 2, stream), word draw & 3.  Streams: */
+#define KK_RNG_STREAM_WALK 0
+#define KK_RNG_STREAM_INIT_STATE 1
+#define KK_RNG_STREAM_INIT_DIST 2
+
+typedef struct kk_engine kk_engine;
+
+/* Options of one random_walk() call: the union of WalkConfig
+ * (include/walk.hpp:105-145), WalkerConfig (:147-193) and the apps' confs. */
+typedef struct
+{
+    int app;          /* KK_APP_* */
+    int weighted;     /* static component = edge weight (alias sampling) */
+    uint64_t seed;    /* Philox key */
+    uint32_t walker_num;
+    uint32_t walker_begin;   /* first walker id (ids are walker_begin + i) */
+    uint32_t walk_length;    /* DeepWalk / node2vec / metapath */
+    float terminate_prob;    /* PPR (extension = 1 - terminate_prob) */
+    float p, q;              /* node2vec */
+    int n_schemes;           /* metapath: schemes as per-state edge-type masks */
+    int scheme_len[KK_MAX_SCHEMES];
+    uint8_t scheme_mask[KK_MAX_SCHEMES][KK_MAX_SCHEME_LEN];
+    int scheme_round_robin;  /* 0: scheme = gen(n_schemes) on stream 1 (metapath.hpp:91-95); 1: id % n */
+    const uint32_t *start;   /* optional host start-vertex list (ppr.hpp:37-51); NULL: id % V */
+    uint32_t n_start;
+    double rate;             /* WalkConfig::set_walk_rate (-r), epochs of walker_num*rate walkers; 0 = 1 */
+} kk_walk_opts;
+
+/* Paths of one call, host memory, in walker-id order.  Walker i (id
+ * walker_begin + i) has length[i] vertices at vertices[offset[i]...]. */
+typedef struct
+{
+    uint32_t walker_num;
+    uint32_t walker_begin;
+    uint32_t epoch_walkers;  /* walkers per epoch of the call (walker_num when rate = 1) */
+    uint64_t total_steps;    /* sum(length) - walker_num: walker-steps taken */
+    uint32_t *length;
+    uint64_t *offset;
+    uint32_t *vertices;
+} kk_paths;
+
+/* ---- engine ------------------------------------------------------------- */
+
+/* WalkEngine() (include/walk.hpp:378-381): binds CUDA device `device`. */
+kk_status kk_engine_create(kk_engine **out, int device);
+void kk_engine_destroy(kk_engine *e);
+/* Runs the engine's work on `stream` (a cudaStream_t; NULL restores the
+ * engine's own stream), so a caller can order and time it with its events. */
+kk_status kk_engine_set_stream(kk_engine *e, void *stream);
+/* Message of the last failed call on this engine ("" if none). */
+const char *kk_last_error(const kk_engine *e);
+/* Message for a status code. */
+const char *kk_status_string(kk_status s);
+
+/* ---- graph (GraphEngine::load_graph, include/graph.hpp:408-530) --------- */
+
+/* Reads the reference's binary edge-list file (include/storage.hpp:35-55),
+ * optionally mirrors every edge (--make-undirected, include/graph.hpp:430-443),
+ * and builds the CSR in HBM with file order kept per source
+ * (include/graph.hpp:309-330). */
+kk_status kk_graph_load_binary(kk_engine *e, uint32_t v_num, const char *path, int edge_kind, int make_undirected);
+
+/* Uploads a host CSR: off[V+1] int64, nbr[E], w[E] (nullable), type[E] (nullable). */
+kk_status kk_graph_load_arrays(kk_engine *e, uint32_t v_num, uint64_t e_num, const int64_t *off,
+                               const uint32_t *nbr, const float *w, const uint8_t *type);
+
+/* Seeded R-MAT graph generated in HBM: edge_factor*2^scale draws with quadrant
+ * probabilities a, b, c; self-loops dropped, pairs deduplicated and mirrored,
+ * adjacency sorted.  weights: 0 none, 1 uniform [1,5), 2 lognormal(0,1);
+ * types: number of edge types (0 = none). */
+kk_status kk_graph_generate_rmat(kk_engine *e, uint32_t scale, uint32_t edge_factor, double a, double b, double c,
+                                 uint64_t seed, int weights, int types);
+
+kk_status kk_graph_info(const kk_engine *e, uint32_t *v_num, uint64_t *e_num, int *has_weights, int *has_types);
+
+/* Copies the device CSR to host arrays (any pointer may be NULL). */
+kk_status kk_graph_download(kk_engine *e, int64_t *off, uint32_t *nbr, float *w, uint8_t *type);
+
+/* node2vec needs each adjacency sorted by neighbour (src/apps/node2vec.hpp:122-125);
+ * kk_walk sorts on demand, this does it eagerly.  In place, on the device. */
+kk_status kk_graph_sort_adjacency(kk_engine *e);
+
+/* ---- alias tables (init_alias_tables, include/walk.hpp:538-652) --------- */
+
+/* Builds the alias tables of the static component w on the GPU and copies
+ * them out: bucket j of vertex v at off[v]+j holds (p, p_idx, q_idx) with
+ * indices local to v's adjacency (q_idx = 0xffffffff: no alias), and sum[v]
+ * the sequential float sum of v's weights.  Outputs are host arrays. */
+kk_status kk_alias_build(kk_engine *e, float *p, uint32_t *p_idx, uint32_t *q_idx, float *sum);
+
+/* ---- walks (WalkEngine::random_walk, include/walk.hpp:423-436) ---------- */
+
+/* Runs one walk job and returns its paths in host memory (free with
+ * kk_paths_free).  Epochs (opts->rate < 1) run one after the other. */
+kk_status kk_walk(kk_engine *e, const kk_walk_opts *opts, kk_paths **out);
+
+/* The apps' entry points: set opts->app and call kk_walk. */
+kk_status kk_walk_deepwalk(kk_engine *e, const kk_walk_opts *opts, kk_paths **out); /* deepwalk.hpp:30-47 */
+kk_status kk_walk_ppr(kk_engine *e, const kk_walk_opts *opts, kk_paths **out);      /* ppr.hpp:30-64 */
+kk_status kk_walk_node2vec(kk_engine *e, const kk_walk_opts *opts, kk_paths **out); /* node2vec.hpp:108-202 */
+kk_status kk_walk_metapath(kk_engine *e, const kk_walk_opts *opts, kk_paths **out); /* metapath.hpp:70-128 */
+
+/* Same walk into caller-owned host buffers (pinned memory gives full copy
+ * bandwidth): h_length[walker_num], h_offset[walker_num], and h_vertices with
+ * room for vertices_capacity vertices (KK_ERR_PATH_CAPACITY if too small).
+ * The output is PathSet-equivalent (include/path.hpp:46-84) in walker-id order. */
+kk_status kk_walk_into(kk_engine *e, const kk_walk_opts *opts, uint32_t *h_length, uint64_t *h_offset,
+                       uint32_t *h_vertices, uint64_t vertices_capacity, uint64_t *total_steps);
+
+/* Same walk with paths left in HBM (no host copy): for callers that consume
+ * paths on the GPU.  The buffers stay valid until the next walk call on this
+ * engine.  *d_length / *d_offset / *d_vertices are device pointers. */
+kk_status kk_walk_device(kk_engine *e, const kk_walk_opts *opts, uint64_t *total_steps, const uint32_t **d_length,
+                         const uint64_t **d_offset, const uint32_t **d_vertices);
+
+/* Milliseconds of the alias build and of the walk kernels of the last walk
+ * call, from CUDA events on the engine's stream. */
+kk_status kk_last_walk_timing(const kk_engine *e, float *alias_ms, float *walk_ms);
+
+void kk_paths_free(kk_paths *p);
+
+/* PathSet::dump text format (include/path.hpp:85-109): one line per walker,
+ * "id length" when with_head, then " v" per vertex.  Epoch by epoch
+ * (include/walk.hpp:804-844), walkers are written in the reference's segment
+ * order for seg_num worker threads: segment t of an epoch starting at walker b
+ * holds walkers b + t, b + t + seg_num, ... (include/path.hpp:383-441);
+ * seg_num = 1 writes walker-id order.  mode is "w" or "a". */
+kk_status kk_paths_dump(const kk_paths *p, const char *path, const char *mode, int with_head, int seg_num);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,262 @@
+/*
+ * Built-in apps: the reference's src/apps functors as __device__ functors.
+ * Each functor restates one lambda of the reference, with its arithmetic.
+ */
+#pragma once
+
+#include "walk.cuh"
+
+namespace kk
+{
+namespace apps
+{
+
+/* ---- shared ---------------------------------------------------------------- */
+
+/* walker.step >= walk_length ? 0 : 1 (deepwalk.hpp:36-38, node2vec.hpp:145-148) */
+template <typename S>
+struct FixedLengthExt
+{
+    step_t walk_length;
+    __device__ __forceinline__ real_t operator()(const Walker<S> &w, vertex_id_t) const
+    {
+        return w.step >= walk_length ? 0.0f : 1.0f;
+    }
+};
+
+/* get_trivial_static_comp for weighted graphs: the edge weight (static_comp.hpp:36-42) */
+struct WeightStatic
+{
+    const float *w;
+    __device__ __forceinline__ real_t operator()(vertex_id_t, const AdjUnit &e) const { return w[e.index]; }
+};
+
+struct ConstBound
+{
+    real_t value;
+    __device__ __forceinline__ real_t operator()(vertex_id_t, const AdjList &) const { return value; }
+};
+
+/* ---- PPR (ppr.hpp:30-64) -------------------------------------------------- */
+
+/* extension = 1 - terminate_prob, computed in float (ppr.hpp:35) */
+struct ConstantExt
+{
+    real_t ext;
+    __device__ __forceinline__ real_t operator()(const Walker<EmptyData> &, vertex_id_t) const { return ext; }
+};
+
+/* ---- node2vec (node2vec.hpp:30-202) --------------------------------------- */
+
+struct Node2vecState
+{
+    vertex_id_t previous_vertex;
+};
+
+/* std::lower_bound over a sorted adjacency; returns a local index (deg if none). */
+__device__ __forceinline__ uint32_t lower_bound_adj(const uint32_t *nbr, edge_id_t b, uint32_t deg, vertex_id_t x)
+{
+    uint32_t lo = 0, hi = deg;
+    while (lo < hi)
+    {
+        uint32_t mid = lo + ((hi - lo) >> 1);
+        if (nbr[b + mid] < x)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+/* update: previous_vertex = current (node2vec.hpp:129-136) */
+struct Node2vecUpdate
+{
+    __device__ __forceinline__ void operator()(Walker<Node2vecState> &w, vertex_id_t cur, const AdjUnit &) const
+    {
+        w.data.previous_vertex = cur;
+    }
+};
+
+/* post_query: from step 1 on, ask the previous vertex about the candidate (node2vec.hpp:150-158) */
+struct Node2vecPostQuery
+{
+    __device__ __forceinline__ bool operator()(const Walker<Node2vecState> &w, vertex_id_t, const AdjUnit &cand,
+                                               vertex_id_t &target, vertex_id_t &query) const
+    {
+        if (w.step == 0)
+            return false;
+        target = w.data.previous_vertex;
+        query = cand.neighbour;
+        return true;
+    }
+};
+
+/* respond_query: std::binary_search of the candidate in N(previous) (node2vec.hpp:159-166) */
+struct Node2vecRespond
+{
+    const uint32_t *nbr;
+    __device__ __forceinline__ void operator()(vertex_id_t, const vertex_id_t &query, const AdjList &adj,
+                                               bool &resp) const
+    {
+        uint32_t deg = adj.degree();
+        uint32_t i = lower_bound_adj(nbr, adj.begin, deg, query);
+        resp = i < deg && nbr[adj.begin + i] == query;
+    }
+};
+
+/* dynamic_comp (node2vec.hpp:167-185): ub at step 0, 1/p back to the previous
+ * vertex, 1 to a common neighbour, 1/q otherwise (float divisions of the
+ * float parameters). */
+struct Node2vecDyn
+{
+    real_t upperbound, inv_p, inv_q;
+    __device__ __forceinline__ real_t operator()(const Walker<Node2vecState> &w, const bool &resp, vertex_id_t,
+                                                 const AdjUnit &e) const
+    {
+        if (w.step == 0)
+            return upperbound;
+        if (w.data.previous_vertex == e.neighbour)
+            return inv_p;
+        if (resp)
+            return 1.0f;
+        return inv_q;
+    }
+};
+
+/* outlier_upperbound (node2vec.hpp:47-83): area overflow (unweighted) or
+ * overflow * w(return edge) (weighted), one outlier.  Where the previous
+ * vertex is not a neighbour (directed graphs) the reference reads past the
+ * adjacency; here the area is empty. */
+template <bool Weighted>
+struct Node2vecOutlierUB
+{
+    const uint32_t *nbr;
+    const float *w;
+    real_t overflow;
+    __device__ __forceinline__ void operator()(const Walker<Node2vecState> &wk, vertex_id_t, const AdjList &adj,
+                                               real_t &area, vertex_id_t &num) const
+    {
+        if constexpr (Weighted)
+        {
+            uint32_t deg = adj.degree();
+            uint32_t i = lower_bound_adj(nbr, adj.begin, deg, wk.data.previous_vertex);
+            area = i < deg ? fmul(w[adj.begin + i], overflow) : 0.0f;
+        }
+        else
+        {
+            area = overflow;
+        }
+        num = 1;
+    }
+};
+
+/* outlier_search: the return edge, std::lower_bound(N(v), previous) (node2vec.hpp:85-102) */
+struct Node2vecOutlierSearch
+{
+    const uint32_t *nbr;
+    __device__ __forceinline__ bool operator()(const Walker<Node2vecState> &wk, vertex_id_t, const AdjList &adj,
+                                               vertex_id_t, AdjUnit &out) const
+    {
+        uint32_t deg = adj.degree();
+        uint32_t i = lower_bound_adj(nbr, adj.begin, deg, wk.data.previous_vertex);
+        if (i >= deg)
+            return false;
+        out = AdjUnit{nbr[adj.begin + i], adj.begin + i};
+        return true;
+    }
+};
+
+/* Host-side constants, double then float as node2vec.hpp:126-139 computes them. */
+struct Node2vecConstants
+{
+    float upperbound, lowerbound, overflow, inv_p, inv_q;
+    bool outlier;
+    static Node2vecConstants make(float p, float q)
+    {
+        Node2vecConstants c;
+        double ip = 1.0 / (double)p, iq = 1.0 / (double)q;
+        c.upperbound = (float)(iq > 1.0 ? iq : 1.0);
+        double m = iq < 1.0 ? iq : 1.0;
+        c.lowerbound = (float)(ip < m ? ip : m);
+        c.overflow = (float)(ip - (double)c.upperbound);
+        c.inv_p = 1.0f / p;
+        c.inv_q = 1.0f / q;
+        c.outlier = c.overflow > 0.0f;
+        return c;
+    }
+};
+
+/* ---- metapath (metapath.hpp:32-128, metascheme.hpp:36-54) ------------------ */
+
+struct MetapathState
+{
+    int scheme_id;
+    int state;
+};
+
+struct MetaSchemes
+{
+    uint8_t mask[16][16]; /* scheme x state -> allowed edge types (bit t) */
+    uint8_t len[16];
+    uint32_t n;
+};
+
+/* extension: 0 at the length or when no out-edge has an allowed type (metapath.hpp:102-105) */
+struct MetapathExt
+{
+    const uint8_t *vertex_mask;
+    step_t walk_length;
+    MetaSchemes sc;
+    __device__ __forceinline__ real_t operator()(const Walker<MetapathState> &w, vertex_id_t v) const
+    {
+        return (w.step >= walk_length || !(vertex_mask[v] & sc.mask[w.data.scheme_id][w.data.state])) ? 0.0f : 1.0f;
+    }
+};
+
+/* dynamic_comp: 1 if the edge's type is allowed in the current state, else 0 (metapath.hpp:107-116) */
+struct MetapathDyn
+{
+    const uint8_t *type;
+    MetaSchemes sc;
+    __device__ __forceinline__ real_t operator()(const Walker<MetapathState> &w, vertex_id_t, const AdjUnit &e) const
+    {
+        return ((sc.mask[w.data.scheme_id][w.data.state] >> type[e.index]) & 1u) ? 1.0f : 0.0f;
+    }
+};
+
+/* init_state: scheme = gen(#schemes) (metapath.hpp:91-95) or round robin; state 0 */
+struct MetapathInitState
+{
+    uint32_t n;
+    int round_robin;
+    __device__ __forceinline__ void operator()(Walker<MetapathState> &w, vertex_id_t, Sampler &rng) const
+    {
+        w.data.scheme_id = round_robin ? (int)(w.id % n) : (int)rng.gen(n);
+        w.data.state = 0;
+    }
+};
+
+/* update: state = (state + 1) % len(scheme) (metapath.hpp:96-99) */
+struct MetapathUpdate
+{
+    MetaSchemes sc;
+    __device__ __forceinline__ void operator()(Walker<MetapathState> &w, vertex_id_t, const AdjUnit &) const
+    {
+        w.data.state = (w.data.state + 1) % (int)sc.len[w.data.scheme_id];
+    }
+};
+
+/* vertex_masks (metapath.hpp:77-88): OR of 1 << type over the out-edges */
+static __global__ void metapath_vertex_mask_kernel(GraphView g, uint8_t *vmask)
+{
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += gridDim.x * blockDim.x)
+    {
+        uint8_t m = 0;
+        for (int64_t e = g.off[v]; e < g.off[v + 1]; e++)
+            m |= (uint8_t)(1u << g.type[e]);
+        vmask[v] = m;
+    }
+}
+
+} // namespace apps
+} // namespace kk

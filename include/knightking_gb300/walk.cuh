@@ -1,0 +1,597 @@
+/*
+ * knightking_gb300 walk engine: configuration types and sm_103a kernels.
+ *
+ * The reference's plugin API (include/walk.hpp:105-363) with its hooks as
+ * templated __device__ functors instead of std::function members.  A hook left
+ * as NoHook is the reference's nullptr.  Hook signatures:
+ *
+ *   extension_comp     real_t (const Walker<S>&, vertex_id_t)
+ *   static_comp        real_t (vertex_id_t, const AdjUnit&)
+ *   dynamic_comp       real_t (const Walker<S>&, vertex_id_t, const AdjUnit&)          first order
+ *                      real_t (const Walker<S>&, const R&, vertex_id_t, const AdjUnit&) second order
+ *   dcomp_upperbound   real_t (vertex_id_t, const AdjList&)   (pure: called per use)
+ *   dcomp_lowerbound   real_t (vertex_id_t, const AdjList&)   (pure: called per use)
+ *   outlier_upperbound void   (const Walker<S>&, vertex_id_t, const AdjList&, real_t& area, vertex_id_t& num)
+ *   outlier_search     bool   (const Walker<S>&, vertex_id_t, const AdjList&, vertex_id_t idx, AdjUnit& out)
+ *                             (false = the reference's nullptr)
+ *   post_query         bool   (const Walker<S>&, vertex_id_t cur, const AdjUnit& cand, vertex_id_t& target, Q&)
+ *                             (true = a query to `target` is posted; the reference's emit)
+ *   respond_query      void   (vertex_id_t target, const Q&, const AdjList& target_adj, R&)
+ *   walker_init_dist   vertex_id_t (walker_id_t, Sampler&)            draws on stream 2
+ *   walker_init_state  void   (Walker<S>&, vertex_id_t, Sampler&)     draws on stream 1
+ *   walker_update_state void  (Walker<S>&, vertex_id_t cur, const AdjUnit& taken)
+ *
+ * Walker state starts value-initialised (all zero) before walker_init_state.
+ */
+#pragma once
+
+#include "device.cuh"
+
+namespace kk
+{
+
+/* ---- configuration types -------------------------------------------------- */
+
+/* WalkerConfig (include/walk.hpp:147-193). */
+template <typename S, typename InitDist = NoHook, typename InitState = NoHook, typename Update = NoHook>
+struct WalkerConfig
+{
+    typedef S state_type;
+    walker_id_t walker_num;
+    InitDist walker_init_dist;
+    InitState walker_init_state;
+    Update walker_update_state;
+};
+
+/* TransitionConfig (include/walk.hpp:195-271); validity rules of :251-261. */
+template <typename S, typename Ext, typename Static = NoHook, typename Dyn = NoHook, typename UB = NoHook,
+          typename LB = NoHook, typename OutUB = NoHook, typename OutSearch = NoHook>
+struct TransitionConfig
+{
+    static constexpr int order = 1;
+    typedef S state_type;
+    typedef EmptyData query_type;
+    typedef EmptyData response_type;
+    static constexpr bool has_static = is_hook<Static>();
+    static constexpr bool has_dynamic = is_hook<Dyn>();
+    static constexpr bool has_lowerbound = is_hook<LB>();
+    static constexpr bool has_outlier = is_hook<OutUB>();
+    static_assert(is_hook<Ext>(), "extension_comp is required");
+    static_assert(is_hook<Dyn>() || (!is_hook<UB>() && !is_hook<LB>() && !is_hook<OutUB>() && !is_hook<OutSearch>()),
+                  "bounds and outlier hooks need a dynamic_comp");
+    static_assert(!is_hook<Dyn>() || is_hook<UB>(), "dynamic_comp needs dcomp_upperbound");
+    static_assert(is_hook<OutUB>() == is_hook<OutSearch>(), "outlier_upperbound and outlier_search go together");
+
+    Ext extension_comp;
+    Static static_comp;
+    Dyn dynamic_comp;
+    UB dcomp_upperbound;
+    LB dcomp_lowerbound;
+    OutUB outlier_upperbound;
+    OutSearch outlier_search;
+};
+
+/* SecondOrderTransitionConfig (include/walk.hpp:273-363); rules of :339-351. */
+template <typename S, typename Q, typename R, typename Ext, typename Static, typename PostQuery, typename Respond,
+          typename Dyn, typename UB, typename LB = NoHook, typename OutUB = NoHook, typename OutSearch = NoHook>
+struct SecondOrderTransitionConfig
+{
+    static constexpr int order = 2;
+    typedef S state_type;
+    typedef Q query_type;
+    typedef R response_type;
+    static constexpr bool has_static = is_hook<Static>();
+    static constexpr bool has_dynamic = true;
+    static constexpr bool has_lowerbound = is_hook<LB>();
+    static constexpr bool has_outlier = is_hook<OutUB>();
+    static_assert(is_hook<Ext>(), "extension_comp is required");
+    static_assert(is_hook<PostQuery>() && is_hook<Respond>(), "post_query and respond_query are required");
+    static_assert(is_hook<Dyn>() && is_hook<UB>(), "second order needs dynamic_comp and dcomp_upperbound");
+    static_assert(is_hook<OutUB>() == is_hook<OutSearch>(), "outlier_upperbound and outlier_search go together");
+
+    Ext extension_comp;
+    Static static_comp;
+    PostQuery post_query;
+    Respond respond_query;
+    Dyn dynamic_comp;
+    UB dcomp_upperbound;
+    LB dcomp_lowerbound;
+    OutUB outlier_upperbound;
+    OutSearch outlier_search;
+};
+
+/* One alias bucket (AliasBucket, include/walk.hpp:52-57), 16 B aligned so a
+ * bucket is one vector load and never straddles a 32 B sector.  p_idx/q_idx
+ * are indices local to the vertex's adjacency; q_idx == kNone is the
+ * reference's q_ptr == nullptr. */
+struct __align__(16) AliasBucket
+{
+    float p;
+    uint32_t p_idx;
+    uint32_t q_idx;
+    uint32_t pad;
+};
+
+/* ---- alias-table build (init_alias_tables, include/walk.hpp:538-652) -------
+ *
+ * Per vertex, exactly the reference's order: prob[e] = static_comp in CSR
+ * order with a sequential float sum; ave = sum / deg; edges below ave go to
+ * the p queue, the rest to the q queue, both in edge order; then FIFO pairing:
+ * pop p, pop q, bucket = (prob[p]/ave, p, q), prob[q] -= ave - prob[p], q goes
+ * to the p or q tail by the same test; leftovers get p = 1 and no alias.
+ *
+ * Each queue entry carries (index, current prob): an index sits in at most one
+ * queue at a time and its prob only changes when it is popped from q, so the
+ * entry's value is always the reference's prob[index].  Both queues are linear
+ * arrays of deg entries (the q tail never passes deg: q_tail = B + I - C <= deg
+ * for B initial bigs, I pairings and C conversions, since I <= S + C).  Scratch:
+ * 2*deg (uint32 index, float prob) entries per vertex at 2*off[v]. */
+template <typename TC>
+__device__ __forceinline__ void alias_build_vertex(const GraphView &g, const TC &tc, uint32_t v, AliasBucket *out,
+                                                   float *sum_out, uint2 *scratch)
+{
+    int64_t e0 = g.off[v];
+    uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
+    if (deg == 0)
+    {
+        return;
+    }
+    float sum = 0.0f;
+    for (uint32_t e = 0; e < deg; e++)
+    {
+        sum = fadd(sum, tc.static_comp(v, AdjUnit{g.nbr[e0 + e], (edge_id_t)(e0 + e)}));
+    }
+    if (sum_out != nullptr)
+    {
+        sum_out[v] = sum;
+    }
+    float ave = fdiv(sum, u2f(deg));
+    uint2 *P = scratch + 2 * e0;
+    uint2 *Q = P + deg;
+    uint32_t pt = 0, qt = 0;
+    for (uint32_t e = 0; e < deg; e++)
+    {
+        float x = tc.static_comp(v, AdjUnit{g.nbr[e0 + e], (edge_id_t)(e0 + e)});
+        uint2 entry = make_uint2(e, __float_as_uint(x));
+        if (x < ave)
+            P[pt++] = entry;
+        else
+            Q[qt++] = entry;
+    }
+    uint32_t ph = 0, qh = 0;
+    AliasBucket *b = out + e0;
+    while (pt != ph)
+    {
+        uint2 pe = P[ph++];
+        float pv = __uint_as_float(pe.y);
+        AliasBucket nb;
+        nb.pad = 0;
+        nb.p_idx = pe.x;
+        if (qt != qh)
+        {
+            uint2 qe = Q[qh++];
+            float qv = __uint_as_float(qe.y);
+            nb.p = fdiv(pv, ave);
+            nb.q_idx = qe.x;
+            float diff = fsub(ave, pv);
+            qv = fsub(qv, diff);
+            uint2 ne = make_uint2(qe.x, __float_as_uint(qv));
+            if (qv < ave)
+                P[pt++] = ne;
+            else
+                Q[qt++] = ne;
+        }
+        else
+        {
+            nb.p = 1.0f;
+            nb.q_idx = kNone;
+        }
+        *b++ = nb;
+    }
+    while (qt != qh)
+    {
+        uint2 qe = Q[qh++];
+        AliasBucket nb;
+        nb.p = 1.0f;
+        nb.p_idx = qe.x;
+        nb.q_idx = kNone;
+        nb.pad = 0;
+        *b++ = nb;
+    }
+}
+
+template <typename TC>
+__global__ void __launch_bounds__(128) alias_build_kernel(GraphView g, TC tc, AliasBucket *out, float *sum_out,
+                                                          uint2 *scratch)
+{
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += gridDim.x * blockDim.x)
+    {
+        alias_build_vertex(g, tc, v, out, sum_out, scratch);
+    }
+}
+
+/* regular_area (include/walk.hpp:750-781): sum * ub with a static component,
+ * deg * ub without. */
+template <typename TC>
+__global__ void regular_area_kernel(GraphView g, TC tc, const float *sum, float *ra)
+{
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += gridDim.x * blockDim.x)
+    {
+        AdjList adj{(edge_id_t)g.off[v], (edge_id_t)g.off[v + 1]};
+        float ub = tc.dcomp_upperbound(v, adj);
+        if (TC::has_static)
+            ra[v] = fmul(sum[v], ub);
+        else
+            ra[v] = fmul(u2f(adj.degree()), ub);
+    }
+}
+
+/* ---- walk kernels -------------------------------------------------------- */
+
+#define KK_STATUS_OK 0
+#define KK_STATUS_TRIAL_LIMIT 4
+#define KK_STATUS_PATH_CAPACITY 8
+
+struct WalkLaunch
+{
+    uint64_t seed;
+    walker_id_t walker_begin;
+    uint32_t walker_num;
+    const uint64_t *path_off; /* per-walker path offsets (walker_num+1), or nullptr: i * cap */
+    uint32_t cap;             /* fixed path capacity (vertices) when path_off is nullptr */
+    uint32_t *path;           /* nullptr: lengths only */
+    uint32_t *length;
+    const uint32_t *start;    /* optional start-vertex list, start[id % n_start] */
+    uint32_t n_start;
+    unsigned long long *total_steps;
+    int *status;
+    uint32_t trial_limit;
+};
+
+template <typename S, typename WC>
+__device__ __forceinline__ vertex_id_t walker_start(const GraphView &g, const WC &wc, const WalkLaunch &L,
+                                                    Walker<S> &w, Sampler &rng)
+{
+    vertex_id_t v;
+    if constexpr (is_hook<decltype(wc.walker_init_dist)>())
+    {
+        rng.enter(w.id, 0, 2);
+        v = wc.walker_init_dist(w.id, rng);
+    }
+    else if (L.start != nullptr)
+    {
+        v = L.start[w.id % L.n_start];
+    }
+    else
+    {
+        v = w.id % g.V;
+    }
+    if constexpr (is_hook<decltype(wc.walker_init_state)>())
+    {
+        rng.enter(w.id, 0, 1);
+        wc.walker_init_state(w, v, rng);
+    }
+    return v;
+}
+
+/* Candidate pick: uniform (include/walk.hpp:1016-1018) or alias
+ * (:1020-1028; the coin is drawn only when the bucket has an alias). */
+template <typename TC>
+__device__ __forceinline__ uint32_t pick_candidate(const AliasBucket *alias, int64_t e0, uint32_t deg, Sampler &rng)
+{
+    if constexpr (TC::has_static)
+    {
+        AliasBucket b = alias[e0 + rng.gen(deg)];
+        if (b.q_idx == kNone || rng.gen_float(1.0f) < b.p)
+            return b.p_idx;
+        return b.q_idx;
+    }
+    else
+    {
+        return rng.gen(deg);
+    }
+}
+
+__device__ __forceinline__ void flush_steps(unsigned long long *total, unsigned long long mine)
+{
+    for (int o = 16; o > 0; o >>= 1)
+        mine += __shfl_down_sync(0xffffffffu, mine, o);
+    if ((threadIdx.x & 31) == 0 && mine != 0)
+        atomicAdd(total, mine);
+}
+
+/* First-order walk (include/walk.hpp:946-1067): one thread per walker, the
+ * walker's state in registers for its whole walk. */
+template <typename S, typename WC, typename TC>
+__global__ void __launch_bounds__(256) walk_first_order_kernel(GraphView g, WC wc, TC tc, const AliasBucket *alias,
+                                                               const float *ra, WalkLaunch L)
+{
+    unsigned long long my_steps = 0;
+    uint32_t n_iter = (L.walker_num + gridDim.x * blockDim.x - 1) / (gridDim.x * blockDim.x);
+    for (uint32_t it = 0; it < n_iter; it++)
+    {
+        uint32_t i = (it * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
+        if (i < L.walker_num)
+        {
+            Sampler rng;
+            rng.init(L.seed);
+            Walker<S> w;
+            w.id = L.walker_begin + i;
+            w.step = 0;
+            w.data = S{};
+            vertex_id_t v = walker_start<S>(g, wc, L, w, rng);
+            uint64_t pbase = L.path_off ? L.path_off[i] : (uint64_t)i * L.cap;
+            uint32_t cap = L.path_off ? (uint32_t)(L.path_off[i + 1] - pbase) : L.cap;
+            uint32_t *out = L.path ? L.path + pbase : nullptr;
+            if (out)
+                out[0] = v;
+            uint32_t len = 1;
+            for (;;)
+            {
+                int64_t e0 = g.off[v];
+                uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
+                if (deg == 0)
+                    break;
+                rng.enter(w.id, w.step, 0);
+                real_t ext = tc.extension_comp(w, v);
+                if (ext == 0.0f || (ext < 1.0f && rng.gen_float(1.0f) > ext))
+                    break;
+                AdjList adj{(edge_id_t)e0, (edge_id_t)(e0 + deg)};
+                uint32_t ac = kNone;
+                vertex_id_t nv = 0;
+                uint32_t trials = 0;
+                while (ac == kNone)
+                {
+                    if (++trials > L.trial_limit)
+                    {
+                        atomicExch(L.status, KK_STATUS_TRIAL_LIMIT);
+                        break;
+                    }
+                    if constexpr (TC::has_outlier)
+                    {
+                        real_t ob = 0.0f;
+                        vertex_id_t on = 0;
+                        tc.outlier_upperbound(w, v, adj, ob, on);
+                        if (ob > 0.0f && on > 0)
+                        {
+                            float rav = ra[v];
+                            float r = fsub(rng.gen_float(fadd(fmul(ob, u2f(on)), rav)), rav);
+                            if (r > 0.0f)
+                            {
+                                uint32_t oi = (uint32_t)fdiv(r, ob);
+                                if (oi + 1 > on)
+                                    oi = on - 1;
+                                AdjUnit cu;
+                                if (tc.outlier_search(w, v, adj, oi, cu))
+                                {
+                                    float sc = 1.0f;
+                                    if constexpr (TC::has_static)
+                                        sc = tc.static_comp(v, cu);
+                                    float r2 = fadd(fdiv(fsub(r, fmul(u2f(oi), ob)), sc), tc.dcomp_upperbound(v, adj));
+                                    if (r2 <= tc.dynamic_comp(w, v, cu))
+                                    {
+                                        ac = (uint32_t)(cu.index - (edge_id_t)e0);
+                                        nv = cu.neighbour;
+                                    }
+                                }
+                                continue;
+                            }
+                        }
+                    }
+                    uint32_t cand = pick_candidate<TC>(alias, e0, deg, rng);
+                    vertex_id_t cn = g.nbr[e0 + cand];
+                    if constexpr (TC::has_dynamic)
+                    {
+                        float dart = rng.gen_float(tc.dcomp_upperbound(v, adj));
+                        bool acc = false;
+                        if constexpr (TC::has_lowerbound)
+                            acc = dart <= tc.dcomp_lowerbound(v, adj);
+                        if (!acc)
+                            acc = dart <= tc.dynamic_comp(w, v, AdjUnit{cn, (edge_id_t)(e0 + cand)});
+                        if (acc)
+                        {
+                            ac = cand;
+                            nv = cn;
+                        }
+                    }
+                    else
+                    {
+                        ac = cand;
+                        nv = cn;
+                    }
+                }
+                if (ac == kNone)
+                    break; /* trial limit */
+                w.step++;
+                if constexpr (is_hook<decltype(wc.walker_update_state)>())
+                    wc.walker_update_state(w, v, AdjUnit{nv, (edge_id_t)(e0 + ac)});
+                if (out)
+                {
+                    if (len >= cap)
+                    {
+                        atomicExch(L.status, KK_STATUS_PATH_CAPACITY);
+                        break;
+                    }
+                    out[len] = nv;
+                }
+                len++;
+                v = nv;
+            }
+            L.length[i] = len;
+            my_steps += len - 1;
+        }
+    }
+    flush_steps(L.total_steps, my_steps);
+}
+
+/* Second-order walk (include/walk.hpp:1082-1381).  The reference's three
+ * supersteps per trial (candidate + query, response, accept) run inline per
+ * walker: each pass of the trial loop re-evaluates the extension (and its draw)
+ * as the reference does at the start of every superstep (:1167-1172); a
+ * lower-bound pre-accept takes the step at once (:1226-1257); an outlier
+ * search that returns no edge retries without a new extension test
+ * (:1176-1258). */
+template <typename S, typename WC, typename TC>
+__global__ void __launch_bounds__(256) walk_second_order_kernel(GraphView g, WC wc, TC tc, const AliasBucket *alias,
+                                                                const float *ra, WalkLaunch L)
+{
+    typedef typename TC::query_type Q;
+    typedef typename TC::response_type R;
+    unsigned long long my_steps = 0;
+    uint32_t n_iter = (L.walker_num + gridDim.x * blockDim.x - 1) / (gridDim.x * blockDim.x);
+    for (uint32_t it = 0; it < n_iter; it++)
+    {
+        uint32_t i = (it * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
+        if (i < L.walker_num)
+        {
+            Sampler rng;
+            rng.init(L.seed);
+            Walker<S> w;
+            w.id = L.walker_begin + i;
+            w.step = 0;
+            w.data = S{};
+            vertex_id_t v = walker_start<S>(g, wc, L, w, rng);
+            uint64_t pbase = L.path_off ? L.path_off[i] : (uint64_t)i * L.cap;
+            uint32_t cap = L.path_off ? (uint32_t)(L.path_off[i + 1] - pbase) : L.cap;
+            uint32_t *out = L.path ? L.path + pbase : nullptr;
+            if (out)
+                out[0] = v;
+            uint32_t len = 1;
+            for (;;)
+            {
+                int64_t e0 = g.off[v];
+                uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
+                if (deg == 0)
+                    break;
+                rng.enter(w.id, w.step, 0);
+                AdjList adj{(edge_id_t)e0, (edge_id_t)(e0 + deg)};
+                uint32_t ac = kNone;
+                vertex_id_t nv = 0;
+                bool stop = false;
+                uint32_t trials = 0;
+                for (;;)
+                {
+                    real_t ext = tc.extension_comp(w, v);
+                    if (ext == 0.0f || (ext < 1.0f && rng.gen_float(1.0f) > ext))
+                    {
+                        stop = true;
+                        break;
+                    }
+                    AdjUnit cu{0, 0};
+                    float randval = 0.0f;
+                    bool accepted = false;
+                    for (;;)
+                    {
+                        if (++trials > L.trial_limit)
+                        {
+                            atomicExch(L.status, KK_STATUS_TRIAL_LIMIT);
+                            stop = true;
+                            break;
+                        }
+                        bool in_app = false;
+                        if constexpr (TC::has_outlier)
+                        {
+                            real_t ob = 0.0f;
+                            vertex_id_t on = 0;
+                            tc.outlier_upperbound(w, v, adj, ob, on);
+                            if (ob > 0.0f && on > 0)
+                            {
+                                float rav = ra[v];
+                                float r = fsub(rng.gen_float(fadd(fmul(ob, u2f(on)), rav)), rav);
+                                if (r > 0.0f)
+                                {
+                                    in_app = true;
+                                    uint32_t oi = (uint32_t)fdiv(r, ob);
+                                    if (oi + 1 > on)
+                                        oi = on - 1;
+                                    if (tc.outlier_search(w, v, adj, oi, cu))
+                                    {
+                                        float sc = 1.0f;
+                                        if constexpr (TC::has_static)
+                                            sc = tc.static_comp(v, cu);
+                                        randval = fadd(fdiv(fsub(r, fmul(u2f(oi), ob)), sc), tc.dcomp_upperbound(v, adj));
+                                        break;
+                                    }
+                                }
+                            }
+                        }
+                        if (!in_app)
+                        {
+                            uint32_t cand = pick_candidate<TC>(alias, e0, deg, rng);
+                            cu = AdjUnit{g.nbr[e0 + cand], (edge_id_t)(e0 + cand)};
+                            randval = rng.gen_float(tc.dcomp_upperbound(v, adj));
+                            if constexpr (TC::has_lowerbound)
+                                accepted = randval <= tc.dcomp_lowerbound(v, adj);
+                            break;
+                        }
+                    }
+                    if (stop)
+                        break;
+                    if (!accepted)
+                    {
+                        R resp{};
+                        Q query{};
+                        vertex_id_t target = 0;
+                        if (tc.post_query(w, v, cu, target, query))
+                        {
+                            AdjList tadj{(edge_id_t)g.off[target], (edge_id_t)g.off[target + 1]};
+                            tc.respond_query(target, query, tadj, resp);
+                        }
+                        accepted = randval <= tc.dynamic_comp(w, resp, v, cu);
+                    }
+                    if (accepted)
+                    {
+                        ac = (uint32_t)(cu.index - (edge_id_t)e0);
+                        nv = cu.neighbour;
+                        break;
+                    }
+                }
+                if (stop)
+                    break;
+                w.step++;
+                if constexpr (is_hook<decltype(wc.walker_update_state)>())
+                    wc.walker_update_state(w, v, AdjUnit{nv, (edge_id_t)(e0 + ac)});
+                if (out)
+                {
+                    if (len >= cap)
+                    {
+                        atomicExch(L.status, KK_STATUS_PATH_CAPACITY);
+                        break;
+                    }
+                    out[len] = nv;
+                }
+                len++;
+                v = nv;
+            }
+            L.length[i] = len;
+            my_steps += len - 1;
+        }
+    }
+    flush_steps(L.total_steps, my_steps);
+}
+
+/* Upper bound on each walker's path length when the extension is a constant
+ * probability ext in (0,1) (PPR, src/apps/ppr.hpp:55-58): the walk cannot pass
+ * the first step whose first draw (the extension draw, draw 0) says stop.
+ * cap[i] = that step + 1 vertices; fails when no stop comes within max_steps. */
+static __global__ void constant_extension_bound_kernel(uint64_t seed, walker_id_t walker_begin, uint32_t walker_num, float ext,
+                                                uint32_t max_steps, uint64_t *cap_out, int *status)
+{
+    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < walker_num; i += gridDim.x * blockDim.x)
+    {
+        walker_id_t id = walker_begin + i;
+        uint32_t s = 0;
+        for (; s < max_steps; s++)
+        {
+            uint4 b = philox4x32_10(make_uint4(id, s, 0, 0), k0, k1);
+            if (map_gen_float(b.x, 1.0f) > ext)
+                break;
+        }
+        if (s == max_steps)
+            atomicExch(status, KK_STATUS_PATH_CAPACITY);
+        cap_out[i] = (uint64_t)s + 1;
+    }
+}
+
+} // namespace kk

@@ -1,0 +1,605 @@
+/*
+ * C-ABI of the walker-step engine (include/knightking_gb300.h).
+ *
+ * random_walk() (include/walk.hpp:698-878) on one GPU: per epoch of
+ * walker_num*rate walkers (:804-844) the app's kernels run on the engine's
+ * stream and the epoch's paths are compacted on the device and copied out;
+ * the reference's footprint shuffle and assembly (include/path.hpp:164-477)
+ * reduce to that compaction because each walker writes its own path slot.
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <cub/cub.cuh>
+#include <string>
+#include <vector>
+
+#include "engine.cuh"
+
+void kk_engine::free_graph()
+{
+    if (d_off)
+        cudaFree(d_off);
+    if (d_nbr)
+        cudaFree(d_nbr);
+    if (d_w)
+        cudaFree(d_w);
+    if (d_type)
+        cudaFree(d_type);
+    d_off = nullptr;
+    d_nbr = nullptr;
+    d_w = nullptr;
+    d_type = nullptr;
+    has_graph = false;
+    V = 0;
+    E = 0;
+    sorted = -1;
+}
+
+namespace kk
+{
+void graph_upload(kk_engine *e, uint32_t V, uint64_t E, const int64_t *off, const uint32_t *nbr, const float *w,
+                  const uint8_t *type);
+void graph_load_arrays(kk_engine *e, uint32_t V, uint64_t E, const int64_t *off, const uint32_t *nbr, const float *w,
+                       const uint8_t *type);
+void graph_load_binary(kk_engine *e, uint32_t V, const char *path, int kind, int undirected);
+void graph_generate_rmat(kk_engine *e, uint32_t scale, uint32_t ef, double a, double b, double c, uint64_t seed,
+                         int weights, int types);
+
+namespace
+{
+
+/* One warp per walker copies its path into the packed output. */
+__global__ void compact_paths_kernel(uint32_t n, const uint32_t *length, const uint64_t *src_off, uint32_t cap,
+                                     const uint32_t *path, const uint64_t *dst_off, uint32_t *out)
+{
+    uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t lane = threadIdx.x & 31;
+    uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t i = warp; i < n; i += nwarps)
+    {
+        uint64_t s = src_off ? src_off[i] : (uint64_t)i * cap;
+        uint64_t d = dst_off[i];
+        uint32_t len = length[i];
+        for (uint32_t k = lane; k < len; k += 32)
+            out[d + k] = path[s + k];
+    }
+}
+
+__global__ void length_to_u64_kernel(const uint32_t *len, uint64_t *out, uint32_t n)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += gridDim.x * blockDim.x)
+        out[i] = i < n ? len[i] : 0;
+}
+
+__global__ void cast_alias_kernel(const AliasBucket *b, uint64_t n, float *p, uint32_t *pi, uint32_t *qi)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    {
+        AliasBucket x = b[i];
+        p[i] = x.p;
+        pi[i] = x.p_idx;
+        qi[i] = x.q_idx;
+    }
+}
+
+template <typename F>
+kk_status guard(kk_engine *e, F f)
+{
+    try
+    {
+        if (e)
+            e->err.clear();
+        f();
+        return KK_OK;
+    }
+    catch (const Error &x)
+    {
+        if (e)
+            e->err = x.msg;
+        return x.status;
+    }
+    catch (const std::bad_alloc &)
+    {
+        if (e)
+            e->err = "host allocation failed";
+        return KK_ERR_OOM;
+    }
+    catch (const std::exception &x)
+    {
+        if (e)
+            e->err = x.what();
+        return KK_ERR_CUDA;
+    }
+}
+
+void validate_opts(kk_engine *e, const kk_walk_opts *o)
+{
+    if (o == nullptr)
+        fail(KK_ERR_INVALID_CONFIG, "opts is NULL");
+    require_graph(e);
+    if (o->app < KK_APP_DEEPWALK || o->app > KK_APP_METAPATH)
+        fail(KK_ERR_INVALID_CONFIG, "unknown app");
+    if (o->weighted && e->d_w == nullptr)
+        fail(KK_ERR_INVALID_CONFIG, "weighted walk on a graph without weights");
+    if (o->rate < 0.0 || o->rate > 1.0)
+        fail(KK_ERR_INVALID_CONFIG, "rate must be in (0, 1]");
+    if (o->start != nullptr && o->n_start == 0)
+        fail(KK_ERR_INVALID_CONFIG, "start list with n_start == 0");
+    if ((uint64_t)o->walker_begin + o->walker_num > 0x100000000ULL)
+        fail(KK_ERR_INVALID_CONFIG, "walker ids exceed 32 bits");
+    if (o->walk_length >= 0xfffffff0u)
+        fail(KK_ERR_INVALID_CONFIG, "walk_length too large");
+}
+
+/* Walkers per epoch: walker_num * rate, at least 1 (include/walk.hpp:706-709). */
+uint32_t epoch_walkers(const kk_walk_opts *o)
+{
+    if (o->walker_num == 0)
+        return 0;
+    double rate = o->rate == 0.0 ? 1.0 : o->rate;
+    uint32_t per = (uint32_t)((double)o->walker_num * rate);
+    if (per == 0)
+        per = 1;
+    if (per > o->walker_num)
+        per = o->walker_num;
+    return per;
+}
+
+const uint32_t *upload_start(kk_engine *e, const kk_walk_opts *o)
+{
+    if (o->start == nullptr)
+        return nullptr;
+    for (uint32_t i = 0; i < o->n_start; i++)
+        if (o->start[i] >= e->V)
+            fail(KK_ERR_INVALID_CONFIG, "start vertex >= v_num");
+    uint32_t *d = e->start.as<uint32_t>(o->n_start);
+    KK_CUDA_CHECK(cudaMemcpyAsync(d, o->start, (size_t)o->n_start * 4, cudaMemcpyHostToDevice, e->stream));
+    return d;
+}
+
+void run_epoch(kk_engine *e, const kk_walk_opts *o, const uint32_t *d_start, uint32_t begin, uint32_t num,
+               bool want_paths, WalkResult &res)
+{
+    RunSpec rs;
+    rs.seed = o->seed;
+    rs.walker_begin = begin;
+    rs.walker_num = num;
+    rs.d_start = d_start;
+    rs.n_start = o->n_start;
+    rs.want_paths = want_paths;
+    if (o->app == KK_APP_NODE2VEC)
+        run_app_node2vec(e, *o, rs, res);
+    else
+        run_app_first_order(e, *o, rs, res);
+}
+
+/* Compacts an epoch's paths on the device: packed vertices + per-walker offsets. */
+uint64_t pack_paths(kk_engine *e, const WalkResult &r, uint64_t **d_off_out, uint32_t **d_verts_out)
+{
+    uint32_t n = r.walker_num;
+    uint64_t *lens64 = e->caps.as<uint64_t>((uint64_t)n + 1);
+    uint64_t *off = e->packed_off.as<uint64_t>((uint64_t)n + 1);
+    length_to_u64_kernel<<<grid_for(e, (uint64_t)n + 1, 256), 256, 0, e->stream>>>(r.length, lens64, n);
+    exclusive_scan_u64(e, lens64, off, (uint64_t)n + 1);
+    uint64_t total = r.total_steps + n;
+    uint32_t *verts = e->packed.as<uint32_t>(total);
+    compact_paths_kernel<<<grid_for(e, (uint64_t)n * 32, 256), 256, 0, e->stream>>>(n, r.length, r.path_off, r.cap,
+                                                                                   r.path, off, verts);
+    KK_CUDA_CHECK(cudaGetLastError());
+    *d_off_out = off;
+    *d_verts_out = verts;
+    return total;
+}
+
+/* Runs all epochs; sink(epoch_begin, n, d_len, d_off, d_verts, total_vertices) per epoch. */
+template <typename Sink>
+uint64_t walk_epochs(kk_engine *e, const kk_walk_opts *o, Sink sink)
+{
+    validate_opts(e, o);
+    const uint32_t *d_start = upload_start(e, o);
+    uint32_t per = epoch_walkers(o);
+    uint64_t steps = 0;
+    uint32_t done = 0;
+    while (done < o->walker_num)
+    {
+        uint32_t num = o->walker_num - done < per ? o->walker_num - done : per;
+        WalkResult r;
+        run_epoch(e, o, d_start, o->walker_begin + done, num, true, r);
+        uint64_t *d_off;
+        uint32_t *d_verts;
+        uint64_t total = pack_paths(e, r, &d_off, &d_verts);
+        sink(done, num, r.length, d_off, d_verts, total);
+        steps += r.total_steps;
+        done += num;
+    }
+    return steps;
+}
+
+} // namespace
+} // namespace kk
+
+using namespace kk;
+
+extern "C" {
+
+const char *kk_status_string(kk_status s)
+{
+    switch (s)
+    {
+    case KK_OK:
+        return "ok";
+    case KK_ERR_INVALID_CONFIG:
+        return "invalid configuration";
+    case KK_ERR_OOM:
+        return "out of memory";
+    case KK_ERR_IO:
+        return "I/O error";
+    case KK_ERR_TRIAL_LIMIT:
+        return "rejection-trial limit exceeded";
+    case KK_ERR_TIMEOUT:
+        return "timeout";
+    case KK_ERR_CUDA:
+        return "CUDA error";
+    case KK_ERR_NO_GRAPH:
+        return "no graph loaded";
+    case KK_ERR_PATH_CAPACITY:
+        return "path capacity exceeded";
+    default:
+        return "unknown status";
+    }
+}
+
+kk_status kk_engine_create(kk_engine **out, int device)
+{
+    if (out == nullptr)
+        return KK_ERR_INVALID_CONFIG;
+    *out = nullptr;
+    kk_engine *e = new (std::nothrow) kk_engine();
+    if (e == nullptr)
+        return KK_ERR_OOM;
+    kk_status s = guard(e, [&] {
+        e->device = device;
+        KK_CUDA_CHECK(cudaSetDevice(device));
+        KK_CUDA_CHECK(cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, device));
+        KK_CUDA_CHECK(cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking));
+        e->stream = e->own_stream;
+        for (int i = 0; i < 3; i++)
+            KK_CUDA_CHECK(cudaEventCreate(&e->ev[i]));
+    });
+    if (s != KK_OK)
+    {
+        delete e;
+        return s;
+    }
+    *out = e;
+    return KK_OK;
+}
+
+void kk_engine_destroy(kk_engine *e)
+{
+    if (e == nullptr)
+        return;
+    cudaSetDevice(e->device);
+    if (e->stream)
+        cudaStreamSynchronize(e->stream);
+    e->free_graph();
+    kk::DevBuf *bufs[] = {&e->alias, &e->sum,   &e->ra,    &e->scratch, &e->vmask,  &e->path,      &e->length,
+                          &e->path_off, &e->caps, &e->start, &e->small, &e->cub_tmp, &e->packed, &e->packed_off};
+    for (kk::DevBuf *b : bufs)
+        b->release();
+    for (int i = 0; i < 3; i++)
+        if (e->ev[i])
+            cudaEventDestroy(e->ev[i]);
+    if (e->own_stream)
+        cudaStreamDestroy(e->own_stream);
+    delete e;
+}
+
+kk_status kk_engine_set_stream(kk_engine *e, void *stream)
+{
+    if (!e)
+        return KK_ERR_INVALID_CONFIG;
+    return guard(e, [&] {
+        KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+        e->stream = stream ? (cudaStream_t)stream : e->own_stream;
+    });
+}
+
+const char *kk_last_error(const kk_engine *e)
+{
+    return e ? e->err.c_str() : "engine is NULL";
+}
+
+kk_status kk_graph_load_binary(kk_engine *e, uint32_t v_num, const char *path, int edge_kind, int make_undirected)
+{
+    if (!e)
+        return KK_ERR_INVALID_CONFIG;
+    return guard(e, [&] {
+        if (path == nullptr)
+            fail(KK_ERR_INVALID_CONFIG, "path is NULL");
+        graph_load_binary(e, v_num, path, edge_kind, make_undirected);
+    });
+}
+
+kk_status kk_graph_load_arrays(kk_engine *e, uint32_t v_num, uint64_t e_num, const int64_t *off, const uint32_t *nbr,
+                               const float *w, const uint8_t *type)
+{
+    if (!e)
+        return KK_ERR_INVALID_CONFIG;
+    return guard(e, [&] { graph_load_arrays(e, v_num, e_num, off, nbr, w, type); });
+}
+
+kk_status kk_graph_generate_rmat(kk_engine *e, uint32_t scale, uint32_t edge_factor, double a, double b, double c,
+                                 uint64_t seed, int weights, int types)
+{
+    if (!e)
+        return KK_ERR_INVALID_CONFIG;
+    return guard(e, [&] { graph_generate_rmat(e, scale, edge_factor, a, b, c, seed, weights, types); });
+}
+
+kk_status kk_graph_info(const kk_engine *e, uint32_t *v_num, uint64_t *e_num, int *has_weights, int *has_types)
+{
+    if (!e)
+        return KK_ERR_INVALID_CONFIG;
+    if (!e->has_graph)
+        return KK_ERR_NO_GRAPH;
+    if (v_num)
+        *v_num = e->V;
+    if (e_num)
+        *e_num = e->E;
+    if (has_weights)
+        *has_weights = e->d_w != nullptr;
+    if (has_types)
+        *has_types = e->d_type != nullptr;
+    return KK_OK;
+}
+
+kk_status kk_graph_download(kk_engine *e, int64_t *off, uint32_t *nbr, float *w, uint8_t *type)
+{
+    if (!e)
+        return KK_ERR_INVALID_CONFIG;
+    return guard(e, [&] {
+        require_graph(e);
+        if (off)
+            KK_CUDA_CHECK(cudaMemcpy(off, e->d_off, ((size_t)e->V + 1) * 8, cudaMemcpyDeviceToHost));
+        if (nbr)
+            KK_CUDA_CHECK(cudaMemcpy(nbr, e->d_nbr, e->E * 4, cudaMemcpyDeviceToHost));
+        if (w && e->d_w)
+            KK_CUDA_CHECK(cudaMemcpy(w, e->d_w, e->E * 4, cudaMemcpyDeviceToHost));
+        if (type && e->d_type)
+            KK_CUDA_CHECK(cudaMemcpy(type, e->d_type, e->E, cudaMemcpyDeviceToHost));
+    });
+}
+
+kk_status kk_graph_sort_adjacency(kk_engine *e)
+{
+    if (!e)
+        return KK_ERR_INVALID_CONFIG;
+    return guard(e, [&] { graph_sort_adjacency(e); });
+}
+
+kk_status kk_alias_build(kk_engine *e, float *p, uint32_t *p_idx, uint32_t *q_idx, float *sum)
+{
+    if (!e)
+        return KK_ERR_INVALID_CONFIG;
+    return guard(e, [&] {
+        require_graph(e);
+        if (e->d_w == nullptr)
+            fail(KK_ERR_INVALID_CONFIG, "alias tables need edge weights");
+        apps::WeightStatic ws{e->d_w};
+        TransitionConfig<EmptyData, apps::FixedLengthExt<EmptyData>, apps::WeightStatic> tc;
+        tc.static_comp = ws;
+        float *d_sum = e->sum.as<float>(e->V);
+        KK_CUDA_CHECK(cudaMemsetAsync(d_sum, 0, (size_t)e->V * 4, e->stream));
+        build_alias(e, tc);
+        uint64_t E = e->E;
+        float *dp = nullptr;
+        uint32_t *dpi = nullptr, *dqi = nullptr;
+        KK_CUDA_CHECK(cudaMalloc(&dp, E * 4 + 4));
+        KK_CUDA_CHECK(cudaMalloc(&dpi, E * 4 + 4));
+        KK_CUDA_CHECK(cudaMalloc(&dqi, E * 4 + 4));
+        cast_alias_kernel<<<grid_for(e, E, 256), 256, 0, e->stream>>>((const AliasBucket *)e->alias.p, E, dp, dpi,
+                                                                      dqi);
+        KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+        if (p)
+            KK_CUDA_CHECK(cudaMemcpy(p, dp, E * 4, cudaMemcpyDeviceToHost));
+        if (p_idx)
+            KK_CUDA_CHECK(cudaMemcpy(p_idx, dpi, E * 4, cudaMemcpyDeviceToHost));
+        if (q_idx)
+            KK_CUDA_CHECK(cudaMemcpy(q_idx, dqi, E * 4, cudaMemcpyDeviceToHost));
+        if (sum)
+            KK_CUDA_CHECK(cudaMemcpy(sum, d_sum, (size_t)e->V * 4, cudaMemcpyDeviceToHost));
+        cudaFree(dp);
+        cudaFree(dpi);
+        cudaFree(dqi);
+    });
+}
+
+kk_status kk_walk(kk_engine *e, const kk_walk_opts *opts, kk_paths **out)
+{
+    if (!e || !out)
+        return KK_ERR_INVALID_CONFIG;
+    *out = nullptr;
+    kk_paths *p = (kk_paths *)calloc(1, sizeof(kk_paths));
+    if (!p)
+        return KK_ERR_OOM;
+    kk_status s = guard(e, [&] {
+        validate_opts(e, opts);
+        uint32_t n = opts->walker_num;
+        p->walker_num = n;
+        p->walker_begin = opts->walker_begin;
+        p->epoch_walkers = epoch_walkers(opts);
+        p->length = (uint32_t *)malloc((size_t)n * 4 + 4);
+        p->offset = (uint64_t *)malloc((size_t)n * 8 + 8);
+        if (!p->length || !p->offset)
+            fail(KK_ERR_OOM, "host allocation failed");
+        std::vector<uint32_t *> chunks;
+        std::vector<uint64_t> chunk_len;
+        uint64_t base = 0;
+        p->total_steps = walk_epochs(e, opts, [&](uint32_t done, uint32_t num, const uint32_t *d_len,
+                                                  const uint64_t *d_off, const uint32_t *d_verts, uint64_t total) {
+            KK_CUDA_CHECK(cudaMemcpyAsync(p->length + done, d_len, (size_t)num * 4, cudaMemcpyDeviceToHost, e->stream));
+            KK_CUDA_CHECK(cudaMemcpyAsync(p->offset + done, d_off, (size_t)num * 8, cudaMemcpyDeviceToHost, e->stream));
+            uint32_t *h = (uint32_t *)malloc(total * 4 + 4);
+            if (!h)
+                fail(KK_ERR_OOM, "host allocation failed");
+            chunks.push_back(h);
+            chunk_len.push_back(total);
+            KK_CUDA_CHECK(cudaMemcpyAsync(h, d_verts, total * 4, cudaMemcpyDeviceToHost, e->stream));
+            KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+            for (uint32_t i = 0; i < num; i++)
+                p->offset[done + i] += base;
+            base += total;
+        });
+        p->vertices = (uint32_t *)malloc(base * 4 + 4);
+        if (!p->vertices)
+            fail(KK_ERR_OOM, "host allocation failed");
+        uint64_t at = 0;
+        for (size_t c = 0; c < chunks.size(); c++)
+        {
+            memcpy(p->vertices + at, chunks[c], chunk_len[c] * 4);
+            at += chunk_len[c];
+            free(chunks[c]);
+        }
+    });
+    if (s != KK_OK)
+    {
+        kk_paths_free(p);
+        return s;
+    }
+    *out = p;
+    return KK_OK;
+}
+
+static kk_status walk_app(kk_engine *e, const kk_walk_opts *opts, kk_paths **out, int app)
+{
+    if (!opts)
+        return KK_ERR_INVALID_CONFIG;
+    kk_walk_opts o = *opts;
+    o.app = app;
+    return kk_walk(e, &o, out);
+}
+
+kk_status kk_walk_deepwalk(kk_engine *e, const kk_walk_opts *o, kk_paths **out)
+{
+    return walk_app(e, o, out, KK_APP_DEEPWALK);
+}
+kk_status kk_walk_ppr(kk_engine *e, const kk_walk_opts *o, kk_paths **out)
+{
+    return walk_app(e, o, out, KK_APP_PPR);
+}
+kk_status kk_walk_node2vec(kk_engine *e, const kk_walk_opts *o, kk_paths **out)
+{
+    return walk_app(e, o, out, KK_APP_NODE2VEC);
+}
+kk_status kk_walk_metapath(kk_engine *e, const kk_walk_opts *o, kk_paths **out)
+{
+    return walk_app(e, o, out, KK_APP_METAPATH);
+}
+
+kk_status kk_walk_into(kk_engine *e, const kk_walk_opts *opts, uint32_t *h_length, uint64_t *h_offset,
+                       uint32_t *h_vertices, uint64_t vertices_capacity, uint64_t *total_steps)
+{
+    if (!e || !h_length || !h_offset || !h_vertices)
+        return KK_ERR_INVALID_CONFIG;
+    return guard(e, [&] {
+        uint64_t base = 0;
+        uint64_t steps = walk_epochs(e, opts, [&](uint32_t done, uint32_t num, const uint32_t *d_len,
+                                                  const uint64_t *d_off, const uint32_t *d_verts, uint64_t total) {
+            if (base + total > vertices_capacity)
+                fail(KK_ERR_PATH_CAPACITY, "vertices buffer too small");
+            KK_CUDA_CHECK(cudaMemcpyAsync(h_length + done, d_len, (size_t)num * 4, cudaMemcpyDeviceToHost, e->stream));
+            KK_CUDA_CHECK(cudaMemcpyAsync(h_offset + done, d_off, (size_t)num * 8, cudaMemcpyDeviceToHost, e->stream));
+            KK_CUDA_CHECK(cudaMemcpyAsync(h_vertices + base, d_verts, total * 4, cudaMemcpyDeviceToHost, e->stream));
+            KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+            if (base != 0)
+                for (uint32_t i = 0; i < num; i++)
+                    h_offset[done + i] += base;
+            base += total;
+        });
+        if (total_steps)
+            *total_steps = steps;
+    });
+}
+
+kk_status kk_walk_device(kk_engine *e, const kk_walk_opts *opts, uint64_t *total_steps, const uint32_t **d_length,
+                         const uint64_t **d_offset, const uint32_t **d_vertices)
+{
+    if (!e)
+        return KK_ERR_INVALID_CONFIG;
+    return guard(e, [&] {
+        validate_opts(e, opts);
+        const uint32_t *d_start = upload_start(e, opts);
+        WalkResult r;
+        run_epoch(e, opts, d_start, opts->walker_begin, opts->walker_num, d_vertices != nullptr, r);
+        if (total_steps)
+            *total_steps = r.total_steps;
+        if (d_length)
+            *d_length = r.length;
+        if (d_vertices)
+        {
+            uint64_t *d_off;
+            uint32_t *d_verts;
+            pack_paths(e, r, &d_off, &d_verts);
+            KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+            if (d_offset)
+                *d_offset = d_off;
+            *d_vertices = d_verts;
+        }
+    });
+}
+
+kk_status kk_last_walk_timing(const kk_engine *e, float *alias_ms, float *walk_ms)
+{
+    if (!e)
+        return KK_ERR_INVALID_CONFIG;
+    if (alias_ms)
+        *alias_ms = e->alias_ms;
+    if (walk_ms)
+        *walk_ms = e->walk_ms;
+    return KK_OK;
+}
+
+void kk_paths_free(kk_paths *p)
+{
+    if (!p)
+        return;
+    free(p->length);
+    free(p->offset);
+    free(p->vertices);
+    free(p);
+}
+
+kk_status kk_paths_dump(const kk_paths *p, const char *path, const char *mode, int with_head, int seg_num)
+{
+    if (!p || !path || !mode || seg_num < 1)
+        return KK_ERR_INVALID_CONFIG;
+    FILE *f = fopen(path, mode);
+    if (!f)
+        return KK_ERR_IO;
+    uint32_t per = p->epoch_walkers ? p->epoch_walkers : p->walker_num;
+    for (uint32_t eb = 0; eb < p->walker_num; eb += per)
+    {
+        uint32_t en = p->walker_num - eb < per ? p->walker_num - eb : per;
+        for (int t = 0; t < seg_num; t++)
+        {
+            for (uint32_t i = (uint32_t)t; i < en; i += (uint32_t)seg_num)
+            {
+                uint32_t w = eb + i;
+                if (with_head)
+                    fprintf(f, "%u %u", p->walker_begin + w, p->length[w]);
+                const uint32_t *v = p->vertices + p->offset[w];
+                for (uint32_t k = 0; k < p->length[w]; k++)
+                    fprintf(f, " %u", v[k]);
+                fprintf(f, "\n");
+            }
+        }
+    }
+    fclose(f);
+    return KK_OK;
+}
+
+} /* extern "C" */

@@ -1,0 +1,261 @@
+/*
+ * Engine internals shared by the C-ABI translation units.
+ *
+ * kk_engine owns the CSR in HBM (int64 off[V+1], uint32 nbr[E], float w[E],
+ * uint8 type[E]) and grow-only work buffers (alias tables, path buffers), all
+ * on one CUDA stream.  Errors inside are C++ exceptions (kk::Error) that the
+ * C-ABI entry points turn into kk_status codes; none crosses the ABI.
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "knightking_gb300.h"
+#include "knightking_gb300/apps.cuh"
+
+namespace kk
+{
+
+struct Error
+{
+    kk_status status;
+    std::string msg;
+};
+
+[[noreturn]] inline void fail(kk_status s, const std::string &msg)
+{
+    throw Error{s, msg};
+}
+
+#define KK_CUDA_CHECK(call)                                                                                         \
+    do                                                                                                              \
+    {                                                                                                               \
+        cudaError_t _e = (call);                                                                                    \
+        if (_e != cudaSuccess)                                                                                      \
+            ::kk::fail(_e == cudaErrorMemoryAllocation ? KK_ERR_OOM : KK_ERR_CUDA,                                  \
+                       std::string(#call) + ": " + cudaGetErrorString(_e));                                         \
+    } while (0)
+
+/* Grow-only device buffer. */
+struct DevBuf
+{
+    void *p = nullptr;
+    size_t bytes = 0;
+    void *ensure(size_t n)
+    {
+        if (n > bytes)
+        {
+            if (p)
+                cudaFree(p);
+            p = nullptr;
+            bytes = 0;
+            KK_CUDA_CHECK(cudaMalloc(&p, n));
+            bytes = n;
+        }
+        return p;
+    }
+    template <typename T>
+    T *as(size_t count)
+    {
+        return (T *)ensure(count * sizeof(T) > 0 ? count * sizeof(T) : 16);
+    }
+    void release()
+    {
+        if (p)
+            cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+/* Where one walk call's results are (device). */
+struct WalkResult
+{
+    uint32_t walker_num = 0;
+    uint32_t *length = nullptr;      /* walker_num */
+    const uint64_t *path_off = nullptr; /* walker_num + 1, or nullptr with fixed cap */
+    uint32_t cap = 0;
+    uint32_t *path = nullptr;
+    uint64_t total_steps = 0;
+};
+
+struct RunSpec
+{
+    uint64_t seed = 1;
+    walker_id_t walker_begin = 0;
+    uint32_t walker_num = 0;
+    const uint32_t *d_start = nullptr;
+    uint32_t n_start = 0;
+    bool fixed_cap = true;
+    uint32_t cap = 1;        /* vertices per walker, fixed_cap */
+    float const_ext = 0.0f;  /* !fixed_cap: constant extension probability */
+    bool want_paths = true;
+};
+
+} // namespace kk
+
+struct kk_engine
+{
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;     /* where work is issued */
+    cudaStream_t own_stream = nullptr; /* created with the engine */
+    std::string err;
+
+    /* graph */
+    bool has_graph = false;
+    uint32_t V = 0;
+    uint64_t E = 0;
+    int64_t *d_off = nullptr;
+    uint32_t *d_nbr = nullptr;
+    float *d_w = nullptr;
+    uint8_t *d_type = nullptr;
+    int sorted = -1; /* -1 unknown, 0 no, 1 adjacency sorted by neighbour */
+
+    /* work buffers */
+    kk::DevBuf alias, sum, ra, scratch, vmask, path, length, path_off, caps, start, small, cub_tmp, packed, packed_off;
+
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    float alias_ms = 0.0f, walk_ms = 0.0f;
+    /* Rejection trials allowed per walker step before the walk fails with
+     * KK_ERR_TRIAL_LIMIT (bounds every device loop; a valid configuration with
+     * acceptance probability 1e-5 exceeds it with probability ~e^-167). */
+    uint32_t trial_limit = 1u << 24;
+
+    kk::GraphView view() const { return kk::GraphView{V, E, d_off, d_nbr, d_w, d_type}; }
+    void free_graph();
+};
+
+namespace kk
+{
+
+inline void require_graph(const kk_engine *e)
+{
+    if (!e->has_graph)
+        fail(KK_ERR_NO_GRAPH, "no graph loaded");
+}
+
+inline unsigned grid_for(const kk_engine *e, uint64_t n, unsigned block)
+{
+    uint64_t g = (n + block - 1) / block;
+    if (g == 0)
+        g = 1;
+    if (g > 0x7fffffffULL)
+        g = 0x7fffffffULL;
+    return (unsigned)g;
+}
+
+/* Exclusive scan of n+1 uint64 values in place-ish: out[i] = sum(in[0..i)). */
+void exclusive_scan_u64(kk_engine *e, const uint64_t *in, uint64_t *out, uint64_t n);
+
+/* Builds alias tables into e->alias/e->sum for a static functor. */
+template <typename TC>
+void build_alias(kk_engine *e, const TC &tc)
+{
+    GraphView g = e->view();
+    AliasBucket *alias = e->alias.as<AliasBucket>(e->E);
+    float *sum = e->sum.as<float>(e->V);
+    uint2 *scratch = e->scratch.as<uint2>(2 * e->E);
+    alias_build_kernel<TC><<<grid_for(e, g.V, 128), 128, 0, e->stream>>>(g, tc, alias, sum, scratch);
+    KK_CUDA_CHECK(cudaGetLastError());
+}
+
+/* One walk over walkers [rs.walker_begin, + rs.walker_num): alias tables,
+ * regular area, path capacity, the walk kernel.  Events: ev0 before the alias
+ * build, ev1 before the walk, ev2 after. */
+template <typename S, typename WC, typename TC>
+void run_walk(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, WalkResult &res)
+{
+    GraphView g = e->view();
+    uint32_t n = rs.walker_num;
+    int *d_status = (int *)e->small.ensure(64);
+    unsigned long long *d_steps = (unsigned long long *)((char *)d_status + 16);
+    KK_CUDA_CHECK(cudaMemsetAsync(d_status, 0, 64, e->stream));
+    KK_CUDA_CHECK(cudaEventRecord(e->ev[0], e->stream));
+    const AliasBucket *alias = nullptr;
+    const float *ra = nullptr;
+    if constexpr (TC::has_static)
+    {
+        build_alias(e, tc);
+        alias = (const AliasBucket *)e->alias.p;
+    }
+    if constexpr (TC::has_outlier)
+    {
+        float *rap = e->ra.as<float>(e->V);
+        regular_area_kernel<TC><<<grid_for(e, g.V, 256), 256, 0, e->stream>>>(g, tc, (const float *)e->sum.p, rap);
+        KK_CUDA_CHECK(cudaGetLastError());
+        ra = rap;
+    }
+    WalkLaunch L;
+    L.seed = rs.seed;
+    L.walker_begin = rs.walker_begin;
+    L.walker_num = n;
+    L.start = rs.d_start;
+    L.n_start = rs.n_start;
+    L.total_steps = d_steps;
+    L.status = d_status;
+    L.trial_limit = e->trial_limit;
+    L.length = e->length.as<uint32_t>(n);
+    uint64_t total_cap;
+    if (rs.fixed_cap)
+    {
+        L.path_off = nullptr;
+        L.cap = rs.cap;
+        total_cap = (uint64_t)n * rs.cap;
+    }
+    else
+    {
+        uint64_t *caps = e->caps.as<uint64_t>((uint64_t)n + 1);
+        uint64_t *off = e->path_off.as<uint64_t>((uint64_t)n + 1);
+        KK_CUDA_CHECK(cudaMemsetAsync(caps + n, 0, sizeof(uint64_t), e->stream));
+        constant_extension_bound_kernel<<<grid_for(e, n, 256), 256, 0, e->stream>>>(
+            rs.seed, rs.walker_begin, n, rs.const_ext, 1u << 24, caps, d_status);
+        KK_CUDA_CHECK(cudaGetLastError());
+        exclusive_scan_u64(e, caps, off, (uint64_t)n + 1);
+        KK_CUDA_CHECK(cudaMemcpyAsync(&total_cap, off + n, sizeof(uint64_t), cudaMemcpyDeviceToHost, e->stream));
+        KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+        L.path_off = off;
+        L.cap = 0;
+    }
+    L.path = rs.want_paths ? e->path.as<uint32_t>(total_cap) : nullptr;
+    KK_CUDA_CHECK(cudaEventRecord(e->ev[1], e->stream));
+    unsigned grid = grid_for(e, n, 256);
+    if constexpr (TC::order == 1)
+        walk_first_order_kernel<S, WC, TC><<<grid, 256, 0, e->stream>>>(g, wc, tc, alias, ra, L);
+    else
+        walk_second_order_kernel<S, WC, TC><<<grid, 256, 0, e->stream>>>(g, wc, tc, alias, ra, L);
+    KK_CUDA_CHECK(cudaGetLastError());
+    KK_CUDA_CHECK(cudaEventRecord(e->ev[2], e->stream));
+    int h_small[8];
+    KK_CUDA_CHECK(cudaMemcpyAsync(h_small, d_status, sizeof(h_small), cudaMemcpyDeviceToHost, e->stream));
+    KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+    KK_CUDA_CHECK(cudaEventElapsedTime(&e->alias_ms, e->ev[0], e->ev[1]));
+    KK_CUDA_CHECK(cudaEventElapsedTime(&e->walk_ms, e->ev[1], e->ev[2]));
+    if (h_small[0] == KK_STATUS_TRIAL_LIMIT)
+        fail(KK_ERR_TRIAL_LIMIT, "a walker exceeded the rejection-trial limit");
+    if (h_small[0] == KK_STATUS_PATH_CAPACITY)
+        fail(KK_ERR_PATH_CAPACITY, "a walk exceeded its path capacity");
+    unsigned long long steps;
+    memcpy(&steps, (char *)h_small + 16, sizeof(steps));
+    res.walker_num = n;
+    res.length = L.length;
+    res.path_off = L.path_off;
+    res.cap = L.cap;
+    res.path = L.path;
+    res.total_steps = steps;
+}
+
+/* The built-in apps (apps_*.cu). */
+void run_app_first_order(kk_engine *e, const kk_walk_opts &o, const RunSpec &rs, WalkResult &res);
+void run_app_node2vec(kk_engine *e, const kk_walk_opts &o, const RunSpec &rs, WalkResult &res);
+
+/* Graph helpers (graph.cu). */
+void graph_check_sorted(kk_engine *e);
+void graph_sort_adjacency(kk_engine *e);
+
+} // namespace kk

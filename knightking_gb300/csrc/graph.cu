@@ -1,0 +1,433 @@
+/*
+ * Graph ingestion into HBM.
+ *
+ * - Binary edge-list files in the reference's format (include/storage.hpp:35-55,
+ *   Edge<T> of include/type.hpp:43-85), optionally mirrored edge by edge as
+ *   --make-undirected does (include/graph.hpp:430-443), grouped by source with
+ *   file order kept (include/graph.hpp:309-330).
+ * - Host CSR arrays.
+ * - A seeded R-MAT generator that builds the graph on the device:
+ *     draw i, level l: word l%4 of Philox4x32-10(key=seed, counter=(i, 0, l/4, 3));
+ *     quadrant by integer thresholds floor(a*2^32), floor((a+b)*2^32),
+ *     floor((a+b+c)*2^32) -> a:(0,0) b:(0,1) c:(1,0) d:(1,1), level 0 = top bit;
+ *     self-loops dropped, (min,max) pairs deduplicated, mirrored, sorted by
+ *     (src, dst);  per pair (u<v): Philox(key=seed+1000, counter=(u, v, 0, 4))
+ *     word0 -> uniform [1,5) weight 1 + 4*(w0>>8)*2^-24, or (words 2,3) a
+ *     lognormal(0,1) weight by Box-Muller; word1 -> type floor(w1*types/2^32).
+ */
+#include <stdio.h>
+
+#include <cub/cub.cuh>
+#include <vector>
+
+#include "engine.cuh"
+
+namespace kk
+{
+
+void exclusive_scan_u64(kk_engine *e, const uint64_t *in, uint64_t *out, uint64_t n)
+{
+    size_t bytes = 0;
+    KK_CUDA_CHECK(cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, out, (int64_t)n, e->stream));
+    void *tmp = e->cub_tmp.ensure(bytes);
+    KK_CUDA_CHECK(cub::DeviceScan::ExclusiveSum(tmp, bytes, in, out, (int64_t)n, e->stream));
+}
+
+namespace
+{
+
+__global__ void check_sorted_kernel(const int64_t *off, const uint32_t *nbr, uint32_t V, int *unsorted)
+{
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+    {
+        for (int64_t e = off[v] + 1; e < off[v + 1]; e++)
+        {
+            if (nbr[e - 1] > nbr[e])
+            {
+                atomicExch(unsorted, 1);
+                break;
+            }
+        }
+    }
+}
+
+__global__ void iota_u32_kernel(uint32_t *x, uint64_t n)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        x[i] = (uint32_t)i;
+}
+
+template <typename T>
+__global__ void gather_kernel(const T *src, const uint32_t *idx, T *dst, uint64_t n)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        dst[i] = src[idx[i]];
+}
+
+/* ---- R-MAT -------------------------------------------------------------- */
+
+struct RmatThresholds
+{
+    uint64_t ta, tab, tabc;
+};
+
+__global__ void rmat_draw_kernel(uint64_t m, uint32_t scale, uint64_t seed, RmatThresholds t, uint64_t *keys)
+{
+    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x)
+    {
+        uint64_t src = 0, dst = 0;
+        for (uint32_t blk = 0; blk * 4 < scale; blk++)
+        {
+            uint4 wv = philox4x32_10(make_uint4((uint32_t)i, 0, blk, 3), k0, k1);
+            uint32_t words[4] = {wv.x, wv.y, wv.z, wv.w};
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+            {
+                if (blk * 4 + j >= scale)
+                    break;
+                uint64_t w = words[j];
+                uint64_t sbit = w >= t.tab;
+                uint64_t dbit = ((w >= t.ta) && (w < t.tab)) || (w >= t.tabc);
+                src = (src << 1) | sbit;
+                dst = (dst << 1) | dbit;
+            }
+        }
+        uint64_t lo = src < dst ? src : dst, hi = src < dst ? dst : src;
+        keys[i] = (src == dst) ? ~0ull : ((lo << 32) | hi);
+    }
+}
+
+__global__ void rmat_mirror_kernel(const uint64_t *pairs, uint64_t u, uint64_t *out)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < u; i += (uint64_t)gridDim.x * blockDim.x)
+    {
+        uint64_t k = pairs[i];
+        out[2 * i] = k;
+        out[2 * i + 1] = (k << 32) | (k >> 32);
+    }
+}
+
+__global__ void rmat_csr_kernel(const uint64_t *keys, uint64_t e_num, uint32_t *nbr, unsigned int *deg, uint64_t seed,
+                                float *w, int weights, uint8_t *type, uint32_t types)
+{
+    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < e_num; i += (uint64_t)gridDim.x * blockDim.x)
+    {
+        uint64_t k = keys[i];
+        uint32_t s = (uint32_t)(k >> 32), d = (uint32_t)k;
+        nbr[i] = d;
+        atomicAdd(deg + s, 1u);
+        if (w != nullptr || type != nullptr)
+        {
+            uint32_t lo = s < d ? s : d, hi = s < d ? d : s;
+            uint4 r = philox4x32_10(make_uint4(lo, hi, 0, 4), k0, k1);
+            if (w != nullptr)
+            {
+                if (weights == 1)
+                {
+                    w[i] = fadd(1.0f, fmul(map_gen_float(r.x, 1.0f), 4.0f));
+                }
+                else
+                {
+                    float u1 = ((float)((r.z >> 8) + 1)) * 5.9604644775390625e-8f;
+                    float u2 = ((float)(r.w >> 8)) * 5.9604644775390625e-8f;
+                    float z = sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
+                    w[i] = expf(z);
+                }
+            }
+            if (type != nullptr)
+                type[i] = (uint8_t)__umulhi(r.y, types);
+        }
+    }
+}
+
+__global__ void deg_to_u64_kernel(const unsigned int *deg, uint64_t *out, uint32_t V)
+{
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v <= V; v += gridDim.x * blockDim.x)
+        out[v] = v < V ? deg[v] : 0;
+}
+
+} // namespace
+
+void graph_check_sorted(kk_engine *e)
+{
+    int *flag = (int *)e->small.ensure(64);
+    KK_CUDA_CHECK(cudaMemsetAsync(flag, 0, sizeof(int), e->stream));
+    check_sorted_kernel<<<grid_for(e, e->V, 256), 256, 0, e->stream>>>(e->d_off, e->d_nbr, e->V, flag);
+    KK_CUDA_CHECK(cudaGetLastError());
+    int h = 0;
+    KK_CUDA_CHECK(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+    KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+    e->sorted = h ? 0 : 1;
+}
+
+/* Sorts every adjacency by neighbour, carrying weights and types (what
+ * node2vec() does with std::sort, src/apps/node2vec.hpp:122-125).  Stable, so
+ * with duplicate neighbours the file order of the duplicates is kept. */
+void graph_sort_adjacency(kk_engine *e)
+{
+    require_graph(e);
+    if (e->sorted < 0)
+        graph_check_sorted(e);
+    if (e->sorted == 1)
+        return;
+    uint64_t E = e->E;
+    uint32_t *nbr_out = nullptr, *idx_in = nullptr, *idx_out = nullptr;
+    KK_CUDA_CHECK(cudaMalloc(&nbr_out, E * 4 + 4));
+    KK_CUDA_CHECK(cudaMalloc(&idx_in, E * 4 + 4));
+    KK_CUDA_CHECK(cudaMalloc(&idx_out, E * 4 + 4));
+    iota_u32_kernel<<<grid_for(e, E, 256), 256, 0, e->stream>>>(idx_in, E);
+    size_t bytes = 0;
+    KK_CUDA_CHECK(cub::DeviceSegmentedSort::StableSortPairs(nullptr, bytes, e->d_nbr, nbr_out, idx_in, idx_out,
+                                                            (int64_t)E, (int64_t)e->V, e->d_off, e->d_off + 1,
+                                                            e->stream));
+    void *tmp = e->cub_tmp.ensure(bytes);
+    KK_CUDA_CHECK(cub::DeviceSegmentedSort::StableSortPairs(tmp, bytes, e->d_nbr, nbr_out, idx_in, idx_out, (int64_t)E,
+                                                            (int64_t)e->V, e->d_off, e->d_off + 1, e->stream));
+    if (e->d_w)
+    {
+        float *w2 = nullptr;
+        KK_CUDA_CHECK(cudaMalloc(&w2, E * 4 + 4));
+        gather_kernel<float><<<grid_for(e, E, 256), 256, 0, e->stream>>>(e->d_w, idx_out, w2, E);
+        KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+        cudaFree(e->d_w);
+        e->d_w = w2;
+    }
+    if (e->d_type)
+    {
+        uint8_t *t2 = nullptr;
+        KK_CUDA_CHECK(cudaMalloc(&t2, E + 4));
+        gather_kernel<uint8_t><<<grid_for(e, E, 256), 256, 0, e->stream>>>(e->d_type, idx_out, t2, E);
+        KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+        cudaFree(e->d_type);
+        e->d_type = t2;
+    }
+    KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+    cudaFree(e->d_nbr);
+    e->d_nbr = nbr_out;
+    cudaFree(idx_in);
+    cudaFree(idx_out);
+    e->sorted = 1;
+}
+
+void graph_upload(kk_engine *e, uint32_t V, uint64_t E, const int64_t *off, const uint32_t *nbr, const float *w,
+                  const uint8_t *type)
+{
+    e->free_graph();
+    KK_CUDA_CHECK(cudaMalloc(&e->d_off, (V + 1) * sizeof(int64_t)));
+    KK_CUDA_CHECK(cudaMalloc(&e->d_nbr, E * 4 + 4));
+    KK_CUDA_CHECK(cudaMemcpyAsync(e->d_off, off, (V + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, e->stream));
+    KK_CUDA_CHECK(cudaMemcpyAsync(e->d_nbr, nbr, E * 4, cudaMemcpyHostToDevice, e->stream));
+    if (w)
+    {
+        KK_CUDA_CHECK(cudaMalloc(&e->d_w, E * 4 + 4));
+        KK_CUDA_CHECK(cudaMemcpyAsync(e->d_w, w, E * 4, cudaMemcpyHostToDevice, e->stream));
+    }
+    if (type)
+    {
+        KK_CUDA_CHECK(cudaMalloc(&e->d_type, E + 4));
+        KK_CUDA_CHECK(cudaMemcpyAsync(e->d_type, type, E, cudaMemcpyHostToDevice, e->stream));
+    }
+    KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+    e->V = V;
+    e->E = E;
+    e->has_graph = true;
+    e->sorted = -1;
+}
+
+void graph_load_arrays(kk_engine *e, uint32_t V, uint64_t E, const int64_t *off, const uint32_t *nbr, const float *w,
+                       const uint8_t *type)
+{
+    if (V == 0 || off == nullptr || (E > 0 && nbr == nullptr))
+        fail(KK_ERR_INVALID_CONFIG, "graph needs V > 0, off and nbr");
+    if (off[0] != 0 || (uint64_t)off[V] != E)
+        fail(KK_ERR_INVALID_CONFIG, "off[0] must be 0 and off[V] must be E");
+    for (uint32_t v = 0; v < V; v++)
+        if (off[v + 1] < off[v])
+            fail(KK_ERR_INVALID_CONFIG, "offsets must be non-decreasing");
+    for (uint64_t i = 0; i < E; i++)
+        if (nbr[i] >= V)
+            fail(KK_ERR_INVALID_CONFIG, "neighbour id out of range");
+    if (type)
+        for (uint64_t i = 0; i < E; i++)
+            if (type[i] >= 8)
+                fail(KK_ERR_INVALID_CONFIG, "edge types must be < 8 (8-bit type masks)");
+    graph_upload(e, V, E, off, nbr, w, type);
+}
+
+/* include/storage.hpp:35-55 + include/graph.hpp:408-530 on one rank. */
+void graph_load_binary(kk_engine *e, uint32_t V, const char *path, int kind, int undirected)
+{
+    size_t rec;
+    switch (kind)
+    {
+    case KK_EDGE_UNWEIGHTED:
+        rec = 8;
+        break;
+    case KK_EDGE_F32:
+    case KK_EDGE_META:
+        rec = 12;
+        break;
+    case KK_EDGE_META_F32:
+        rec = 16;
+        break;
+    default:
+        fail(KK_ERR_INVALID_CONFIG, "unknown edge kind");
+    }
+    if (V == 0)
+        fail(KK_ERR_INVALID_CONFIG, "v_num must be > 0");
+    FILE *f = fopen(path, "rb");
+    if (!f)
+        fail(KK_ERR_IO, std::string("cannot open ") + path);
+    fseek(f, 0, SEEK_END);
+    size_t bytes = (size_t)ftell(f);
+    fseek(f, 0, SEEK_SET);
+    size_t n = bytes / rec;
+    std::vector<unsigned char> raw(n * rec + 1);
+    size_t got = n ? fread(raw.data(), rec, n, f) : 0;
+    fclose(f);
+    if (got != n)
+        fail(KK_ERR_IO, std::string("short read from ") + path);
+    bool has_w = kind == KK_EDGE_F32 || kind == KK_EDGE_META_F32;
+    bool has_t = kind == KK_EDGE_META || kind == KK_EDGE_META_F32;
+    uint64_t m = undirected ? 2 * (uint64_t)n : n;
+    std::vector<uint32_t> src(m), dst(m);
+    std::vector<float> w(has_w ? m : 0);
+    std::vector<uint8_t> t(has_t ? m : 0);
+    for (size_t i = 0; i < n; i++)
+    {
+        const unsigned char *r = raw.data() + i * rec;
+        uint32_t s, d;
+        memcpy(&s, r, 4);
+        memcpy(&d, r + 4, 4);
+        if (s >= V || d >= V)
+            fail(KK_ERR_INVALID_CONFIG, "edge endpoint >= v_num");
+        float wt = 0.0f;
+        int32_t ty = 0;
+        if (kind == KK_EDGE_F32 || kind == KK_EDGE_META_F32)
+            memcpy(&wt, r + 8, 4);
+        if (kind == KK_EDGE_META)
+            memcpy(&ty, r + 8, 4);
+        if (kind == KK_EDGE_META_F32)
+            memcpy(&ty, r + 12, 4);
+        if (has_t && (ty < 0 || ty >= 8))
+            fail(KK_ERR_INVALID_CONFIG, "edge types must be in [0, 8)");
+        size_t j = undirected ? 2 * i : i;
+        src[j] = s;
+        dst[j] = d;
+        if (has_w)
+            w[j] = wt;
+        if (has_t)
+            t[j] = (uint8_t)ty;
+        if (undirected)
+        {
+            src[j + 1] = d;
+            dst[j + 1] = s;
+            if (has_w)
+                w[j + 1] = wt;
+            if (has_t)
+                t[j + 1] = (uint8_t)ty;
+        }
+    }
+    /* stable counting sort by source: file order within a source */
+    std::vector<int64_t> off((size_t)V + 1, 0);
+    for (uint64_t i = 0; i < m; i++)
+        off[src[i] + 1]++;
+    for (uint32_t v = 0; v < V; v++)
+        off[v + 1] += off[v];
+    std::vector<int64_t> pos(off.begin(), off.end() - 1);
+    std::vector<uint32_t> nbr(m + 1);
+    std::vector<float> ws(has_w ? m + 1 : 0);
+    std::vector<uint8_t> ts(has_t ? m + 1 : 0);
+    for (uint64_t i = 0; i < m; i++)
+    {
+        int64_t p = pos[src[i]]++;
+        nbr[p] = dst[i];
+        if (has_w)
+            ws[p] = w[i];
+        if (has_t)
+            ts[p] = t[i];
+    }
+    graph_upload(e, V, m, off.data(), nbr.data(), has_w ? ws.data() : nullptr, has_t ? ts.data() : nullptr);
+}
+
+void graph_generate_rmat(kk_engine *e, uint32_t scale, uint32_t ef, double a, double b, double c, uint64_t seed,
+                         int weights, int types)
+{
+    if (scale < 1 || scale > 30 || ef < 1)
+        fail(KK_ERR_INVALID_CONFIG, "R-MAT needs 1 <= scale <= 30 and edge_factor >= 1");
+    if (!(a >= 0 && b >= 0 && c >= 0 && a + b + c <= 1.0))
+        fail(KK_ERR_INVALID_CONFIG, "R-MAT probabilities must be >= 0 with a+b+c <= 1");
+    if (types < 0 || types > 8 || weights < 0 || weights > 2)
+        fail(KK_ERR_INVALID_CONFIG, "R-MAT weights in {0,1,2}, types in [0, 8]");
+    e->free_graph();
+    uint32_t V = 1u << scale;
+    uint64_t m = (uint64_t)ef << scale;
+    RmatThresholds t;
+    t.ta = (uint64_t)floor(a * 4294967296.0);
+    t.tab = (uint64_t)floor((a + b) * 4294967296.0);
+    t.tabc = (uint64_t)floor((a + b + c) * 4294967296.0);
+    uint64_t *k1 = nullptr, *k2 = nullptr;
+    int64_t *d_count = nullptr;
+    KK_CUDA_CHECK(cudaMalloc(&k1, m * 8 + 8));
+    KK_CUDA_CHECK(cudaMalloc(&k2, m * 8 + 8));
+    KK_CUDA_CHECK(cudaMalloc(&d_count, 16));
+    rmat_draw_kernel<<<grid_for(e, m, 256), 256, 0, e->stream>>>(m, scale, seed, t, k1);
+    KK_CUDA_CHECK(cudaGetLastError());
+    size_t bytes = 0;
+    int end_bit = 64;
+    KK_CUDA_CHECK(cub::DeviceRadixSort::SortKeys(nullptr, bytes, k1, k2, m, 0, end_bit, e->stream));
+    KK_CUDA_CHECK(cub::DeviceRadixSort::SortKeys(e->cub_tmp.ensure(bytes), bytes, k1, k2, m, 0, end_bit, e->stream));
+    KK_CUDA_CHECK(cub::DeviceSelect::Unique(nullptr, bytes, k2, k1, d_count, (int64_t)m, e->stream));
+    KK_CUDA_CHECK(cub::DeviceSelect::Unique(e->cub_tmp.ensure(bytes), bytes, k2, k1, d_count, (int64_t)m, e->stream));
+    int64_t u = 0;
+    KK_CUDA_CHECK(cudaMemcpyAsync(&u, d_count, 8, cudaMemcpyDeviceToHost, e->stream));
+    KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+    uint64_t last = 0;
+    if (u > 0)
+    {
+        KK_CUDA_CHECK(cudaMemcpy(&last, k1 + u - 1, 8, cudaMemcpyDeviceToHost));
+        if (last == ~0ull)
+            u--; /* the self-loop sentinel sorts last */
+    }
+    uint64_t E = 2 * (uint64_t)u;
+    /* mirror into k2 (size >= E since E <= 2m and k2 holds m... grow if needed) */
+    uint64_t *mir = nullptr, *mir_sorted = nullptr;
+    KK_CUDA_CHECK(cudaMalloc(&mir, E * 8 + 8));
+    KK_CUDA_CHECK(cudaMalloc(&mir_sorted, E * 8 + 8));
+    rmat_mirror_kernel<<<grid_for(e, u, 256), 256, 0, e->stream>>>(k1, (uint64_t)u, mir);
+    KK_CUDA_CHECK(cudaGetLastError());
+    cudaFree(k1);
+    cudaFree(k2);
+    KK_CUDA_CHECK(cub::DeviceRadixSort::SortKeys(nullptr, bytes, mir, mir_sorted, E, 0, 64, e->stream));
+    KK_CUDA_CHECK(cub::DeviceRadixSort::SortKeys(e->cub_tmp.ensure(bytes), bytes, mir, mir_sorted, E, 0, 64, e->stream));
+    cudaFree(mir);
+    KK_CUDA_CHECK(cudaMalloc(&e->d_nbr, E * 4 + 4));
+    if (weights)
+        KK_CUDA_CHECK(cudaMalloc(&e->d_w, E * 4 + 4));
+    if (types)
+        KK_CUDA_CHECK(cudaMalloc(&e->d_type, E + 4));
+    unsigned int *deg = nullptr;
+    uint64_t *deg64 = nullptr;
+    KK_CUDA_CHECK(cudaMalloc(&deg, (size_t)V * 4 + 4));
+    KK_CUDA_CHECK(cudaMalloc(&deg64, ((size_t)V + 1) * 8));
+    KK_CUDA_CHECK(cudaMemsetAsync(deg, 0, (size_t)V * 4, e->stream));
+    rmat_csr_kernel<<<grid_for(e, E, 256), 256, 0, e->stream>>>(mir_sorted, E, e->d_nbr, deg, seed + 1000, e->d_w,
+                                                                weights, e->d_type, (uint32_t)types);
+    KK_CUDA_CHECK(cudaGetLastError());
+    deg_to_u64_kernel<<<grid_for(e, (uint64_t)V + 1, 256), 256, 0, e->stream>>>(deg, deg64, V);
+    KK_CUDA_CHECK(cudaMalloc(&e->d_off, ((size_t)V + 1) * 8));
+    exclusive_scan_u64(e, deg64, (uint64_t *)e->d_off, (uint64_t)V + 1);
+    KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+    cudaFree(mir_sorted);
+    cudaFree(deg);
+    cudaFree(deg64);
+    cudaFree(d_count);
+    e->V = V;
+    e->E = E;
+    e->has_graph = true;
+    e->sorted = 1;
+}
+
+} // namespace kk

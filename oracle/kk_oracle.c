@@ -760,3 +760,106 @@ int ko_walk(const ko_graph *g, const ko_walk_params *p, uint32_t cap, uint32_t *
     free(c.tag_end);
     return status;
 }
+
+/* ---- synthetic inputs: the project's seeded R-MAT (see graphs.py) ------- */
+
+void ko_rmat_draw(uint32_t scale, uint64_t m, uint64_t ta, uint64_t tab, uint64_t tabc, uint64_t seed, uint64_t *keys,
+                  int threads)
+{
+    if (threads <= 0)
+        threads = omp_get_max_threads();
+#pragma omp parallel for schedule(static) num_threads(threads)
+    for (int64_t i = 0; i < (int64_t)m; i++)
+    {
+        uint64_t src = 0, dst = 0;
+        for (uint32_t blk = 0; blk * 4 < scale; blk++)
+        {
+            uint32_t ctr[4] = {(uint32_t)i, 0, blk, 3}, w4[4];
+            kko_philox4x32_10(ctr, seed, w4);
+            for (uint32_t j = 0; j < 4 && blk * 4 + j < scale; j++)
+            {
+                uint64_t w = w4[j];
+                uint64_t sbit = w >= tab;
+                uint64_t dbit = ((w >= ta) && (w < tab)) || (w >= tabc);
+                src = (src << 1) | sbit;
+                dst = (dst << 1) | dbit;
+            }
+        }
+        uint64_t lo = src < dst ? src : dst, hi = src < dst ? dst : src;
+        keys[i] = (src == dst) ? ~0ull : ((lo << 32) | hi);
+    }
+}
+
+/* Per directed edge (s, d): data of the unordered pair (min, max).  weights:
+ * 1 uniform [1,5), 2 lognormal(0,1) (Box-Muller); types > 0: edge type. */
+void ko_pair_data(uint64_t n, const uint32_t *src, const uint32_t *dst, uint64_t seed, int weights, uint32_t types,
+                  float *w, uint8_t *t, int threads)
+{
+    if (threads <= 0)
+        threads = omp_get_max_threads();
+#pragma omp parallel for schedule(static) num_threads(threads)
+    for (int64_t i = 0; i < (int64_t)n; i++)
+    {
+        uint32_t s = src[i], d = dst[i];
+        uint32_t ctr[4] = {s < d ? s : d, s < d ? d : s, 0, 4}, r[4];
+        kko_philox4x32_10(ctr, seed, r);
+        if (w != NULL)
+        {
+            if (weights == 1)
+            {
+                w[i] = 1.0f + kko_map_gen_float(r[0], 1.0f) * 4.0f;
+            }
+            else
+            {
+                float u1 = (float)((r[2] >> 8) + 1) * (1.0f / 16777216.0f);
+                float u2 = (float)(r[3] >> 8) * (1.0f / 16777216.0f);
+                w[i] = expf(sqrtf(-2.0f * logf(u1)) * cosf(6.283185307179586f * u2));
+            }
+        }
+        if (t != NULL)
+            t[i] = (uint8_t)(((uint64_t)r[1] * types) >> 32);
+    }
+}
+
+/* Stable LSD radix sort of the low `bits` bits of n keys (11-bit digits),
+ * parallel histograms and scatter; the result ends in keys. */
+void ko_radix_sort_u64(uint64_t n, uint64_t *keys, uint64_t *tmp, int bits, int threads)
+{
+    if (threads <= 0)
+        threads = omp_get_max_threads();
+    const int D = 11, R = 1 << 11;
+    uint64_t *hist = (uint64_t *)calloc((size_t)threads * R, sizeof(uint64_t));
+    uint64_t *src = keys, *dst = tmp;
+    for (int shift = 0; shift < bits; shift += D)
+    {
+        memset(hist, 0, (size_t)threads * R * sizeof(uint64_t));
+#pragma omp parallel num_threads(threads)
+        {
+            int t = omp_get_thread_num();
+            uint64_t lo = n * t / threads, hi = n * (t + 1) / threads;
+            uint64_t *h = hist + (size_t)t * R;
+            for (uint64_t i = lo; i < hi; i++)
+                h[(src[i] >> shift) & (R - 1)]++;
+#pragma omp barrier
+#pragma omp single
+            {
+                uint64_t run = 0;
+                for (int d = 0; d < R; d++)
+                    for (int u = 0; u < threads; u++)
+                    {
+                        uint64_t c = hist[(size_t)u * R + d];
+                        hist[(size_t)u * R + d] = run;
+                        run += c;
+                    }
+            }
+            for (uint64_t i = lo; i < hi; i++)
+                dst[h[(src[i] >> shift) & (R - 1)]++] = src[i];
+        }
+        uint64_t *x = src;
+        src = dst;
+        dst = x;
+    }
+    if (src != keys)
+        memcpy(keys, src, n * sizeof(uint64_t));
+    free(hist);
+}

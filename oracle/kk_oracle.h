@@ -87,6 +87,14 @@ int ko_walk(const ko_graph *g, const ko_walk_params *prm, uint32_t cap, uint32_t
 /* Seconds spent in the alias build and in the walk by the last ko_walk call. */
 void ko_last_timing(double *alias_seconds, double *walk_seconds);
 
+/* Synthetic inputs (the project's seeded R-MAT, see graphs.py): raw draws as
+ * (min << 32 | max) keys, ~0 for self-loops; and per-edge pair data. */
+void ko_rmat_draw(uint32_t scale, uint64_t m, uint64_t ta, uint64_t tab, uint64_t tabc, uint64_t seed, uint64_t *keys,
+                  int threads);
+void ko_radix_sort_u64(uint64_t n, uint64_t *keys, uint64_t *tmp, int bits, int threads);
+void ko_pair_data(uint64_t n, const uint32_t *src, const uint32_t *dst, uint64_t seed, int weights, uint32_t types,
+                  float *w, uint8_t *t, int threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -190,6 +190,55 @@ def walk(csr, prm, cap, threads=0, with_paths=True):
     return lens, flat, steps.value
 
 
+def rmat_graph(scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=None, weights=0, types=0, threads=0):
+    """The project's seeded R-MAT graph on the CPU (same definition as
+    oracle/graphs.py and the product's generator): C draws, numpy dedupe.
+    weights: 0 none, 1 uniform [1,5), 2 lognormal(0,1); types: type count."""
+    seed = scale if seed is None else seed
+    L = lib()
+    m = edge_factor << scale
+    keys = np.empty(m, np.uint64)
+    L.ko_rmat_draw.restype = None
+    L.ko_rmat_draw.argtypes = [ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                               ctypes.c_uint64, ctypes.c_void_p, ctypes.c_int]
+    L.ko_rmat_draw(scale, m, int(np.floor(a * 4294967296.0)), int(np.floor((a + b) * 4294967296.0)),
+                   int(np.floor((a + b + c) * 4294967296.0)), seed, keys.ctypes.data, threads)
+    L.ko_radix_sort_u64.restype = None
+    L.ko_radix_sort_u64.argtypes = [ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+    tmp = np.empty(m, np.uint64)
+    L.ko_radix_sort_u64(m, keys.ctypes.data, tmp.ctypes.data, 64, threads)
+    keep = np.empty(m, bool)
+    keep[0] = True
+    np.not_equal(keys[1:], keys[:-1], out=keep[1:])
+    keys = keys[keep]
+    if len(keys) and keys[-1] == np.uint64(0xFFFFFFFFFFFFFFFF):
+        keys = keys[:-1]
+    u = (keys >> np.uint64(32)).astype(np.uint32)
+    v = (keys & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+    del keys
+    sh = np.uint64(scale)
+    mirrored = np.concatenate([(u.astype(np.uint64) << sh) | v, (v.astype(np.uint64) << sh) | u])
+    if len(tmp) < len(mirrored):
+        tmp = np.empty(len(mirrored), np.uint64)
+    L.ko_radix_sort_u64(len(mirrored), mirrored.ctypes.data, tmp.ctypes.data, 2 * scale, threads)
+    del tmp
+    src = (mirrored >> sh).astype(np.uint32)
+    dst = (mirrored & np.uint64((1 << scale) - 1)).astype(np.uint32)
+    del mirrored
+    V = 1 << scale
+    off = np.zeros(V + 1, np.int64)
+    np.cumsum(np.bincount(src, minlength=V), out=off[1:])
+    w = np.empty(len(dst), np.float32) if weights else None
+    t = np.empty(len(dst), np.uint8) if types else None
+    if weights or types:
+        L.ko_pair_data.restype = None
+        L.ko_pair_data.argtypes = [ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int,
+                                   ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        L.ko_pair_data(len(dst), src.ctypes.data, dst.ctypes.data, seed + 1000, weights, types, _ptr(w), _ptr(t),
+                       threads)
+    return {"V": V, "off": off, "nbr": dst, "w": w, "type": t}
+
+
 def last_timing():
     a = ctypes.c_double(0)
     w = ctypes.c_double(0)

@@ -1,0 +1,204 @@
+"""GPU parity: the CUDA walker-step path against the reference's own outputs.
+
+* every golden fixture (paths of the reference's engine with the Philox hook):
+  bit-identical paths per walker id; alias tables index for index, 0 ulp;
+* R-MAT scale 16 (the node2vec configuration and its siblings): the device
+  generator reproduces the graph (SHA-256) and the walks reproduce the
+  reference's path digest over all 65,536 walkers;
+* fresh seeds and graphs beyond the fixtures, against the CPU oracle (itself
+  pinned to the reference by tests/test_oracle_golden.py).
+All calls go through the C-ABI (knightking_gb300 -> libknightking_gb300.so).
+"""
+
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from cases import GOLDEN, Case, case_ids, walk_kwargs
+from oracle import graphs as G
+
+pytestmark = pytest.mark.gpu
+
+APP_CASES = [c for c in case_ids() if not c.startswith("case_alias") and not c.startswith("case_t200")]
+
+
+@pytest.fixture(scope="module")
+def kk():
+    import knightking_gb300
+    return knightking_gb300
+
+
+@pytest.fixture(scope="module")
+def engine(kk):
+    e = kk.WalkEngine(0)
+    yield e
+    e.close()
+
+
+def load_case(engine, case):
+    g = case.graph()
+    engine.load_arrays(g["V"], g["off"], g["nbr"], g.get("w"), g.get("type"))
+
+
+def gpu_walk(engine, case):
+    kw = walk_kwargs(case)
+    n = kw.pop("walker_num")
+    return engine.walk(case.cmd, n, **kw)
+
+
+@pytest.mark.parametrize("name", APP_CASES)
+def test_paths_match_reference(engine, name):
+    case = Case(name)
+    load_case(engine, case)
+    ps = gpu_walk(engine, case)
+    np.testing.assert_array_equal(ps.path_length, case.lens)
+    np.testing.assert_array_equal(ps.vertices, case.verts)
+    assert ps.total_steps == int(case.lens.sum()) - len(case.lens)
+
+
+@pytest.mark.parametrize("name", case_ids("case_alias"))
+def test_alias_tables_match_reference(engine, name):
+    case = Case(name)
+    load_case(engine, case)
+    p, pi, qi, s = engine.alias_tables()
+    d = case.d
+    np.testing.assert_array_equal(pi, d["alias_pidx"])
+    np.testing.assert_array_equal(qi, d["alias_qidx"])
+    np.testing.assert_array_equal(p.view(np.uint32), d["alias_p"].view(np.uint32))
+    np.testing.assert_array_equal(s.view(np.uint32), d["alias_sum"].view(np.uint32))
+
+
+def _csr_digest(g):
+    h = hashlib.sha256()
+    for k in ("off", "nbr", "w", "type"):
+        if g.get(k) is not None:
+            h.update(np.ascontiguousarray(g[k]).tobytes())
+    return h.hexdigest()
+
+
+@pytest.mark.parametrize("name", case_ids("rmat16_"))
+def test_rmat16_matches_reference_digest(engine, name):
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    gen = json.loads(str(d["rmat"]))
+    engine.generate_rmat(gen["scale"], gen["edge_factor"], gen["a"], gen["b"], gen["c"], seed=gen["seed"],
+                         weights=1 if gen.get("weights") else 0, types=5 if gen.get("types") else 0)
+    g = engine.download_graph()
+    assert _csr_digest(g) == str(d["graph_sha256"]), "device R-MAT differs from the fixture's graph"
+    params = json.loads(str(d["params"]))
+    cmd = str(d["cmd"])
+    kw = dict(seed=params["seed"], weighted=str(d["kind"]) != "none")
+    if "len" in params:
+        kw["walk_length"] = params["len"]
+    if "term" in params:
+        kw["terminate_prob"] = float(np.float32(params["term"]))
+    if cmd == "node2vec":
+        kw["p"], kw["q"] = params["p"], params["q"]
+    if cmd == "metapath":
+        kw["schemes"] = params["schemes"]
+    ps = engine.walk(cmd, params["walkers"], **kw)
+    assert ps.total_steps == int(d["total_steps"])
+    nh = len(d["head_lens"])
+    np.testing.assert_array_equal(ps.path_length[:nh], d["head_lens"])
+    np.testing.assert_array_equal(ps.vertices[:int(d["head_lens"].sum())], d["head_verts"])
+    assert G.paths_digest(ps.path_length, ps.vertices) == str(d["paths_sha256"])
+
+
+# ---- beyond the fixtures: against the pinned CPU oracle ----
+
+FRESH = [
+    ("deepwalk", dict(weight="unif"), dict(walk_length=40)),
+    ("deepwalk", dict(), dict(walk_length=40)),
+    ("ppr", dict(weight="int5"), dict(terminate_prob=0.02)),
+    ("ppr", dict(), dict(terminate_prob=0.2)),
+    ("node2vec", dict(weight="unif"), dict(walk_length=30, p=0.4, q=1.7)),
+    ("node2vec", dict(weight="unif"), dict(walk_length=30, p=3.0, q=0.3)),
+    ("node2vec", dict(), dict(walk_length=30, p=0.2, q=0.9)),
+    ("metapath", dict(weight="unif", types="uniform"), dict(walk_length=30, schemes=[[3, 6, 12], [17, 8]])),
+    ("metapath", dict(types="uniform"), dict(walk_length=30, schemes=[[1, 2, 4, 8, 16]])),
+]
+
+
+@pytest.mark.parametrize("i", range(len(FRESH)))
+@pytest.mark.parametrize("seed", [7, 1234567890123])
+def test_fresh_walks_match_oracle(engine, oracle_lib, i, seed):
+    app, gkw, wkw = FRESH[i]
+    g = G.random_undirected(500, 6000, seed=seed % 1000 + i, **gkw)
+    csr = G.csr_file_order(500, g["src"], g["dst"], w=g.get("w"), type=g.get("type"))
+    engine.load_arrays(500, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
+    weighted = "w" in csr
+    n = 1500
+    ps = engine.walk(app, n, seed=seed, weighted=weighted, walker_begin=77, **wkw)
+    ocsr = oracle_lib.CSR(500, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
+    if app == "node2vec":
+        ocsr = ocsr.sorted_copy()
+    prm = oracle_lib.make_params(app, seed=seed, walker_begin=77, walker_num=n, weighted=weighted, **wkw)
+    lens, verts, steps = oracle_lib.walk(ocsr, prm, cap=4096)
+    np.testing.assert_array_equal(ps.path_length, lens)
+    np.testing.assert_array_equal(ps.vertices, verts)
+    assert ps.total_steps == steps
+
+
+def test_ppr_start_list_matches_oracle(engine, oracle_lib):
+    g = G.random_undirected(300, 3000, seed=3, weight="int5")
+    csr = G.csr_file_order(300, g["src"], g["dst"], w=g["w"])
+    engine.load_arrays(300, csr["off"], csr["nbr"], csr["w"])
+    start = np.array([5, 17, 17, 250, 3], np.uint32)
+    ps = engine.walk("ppr", 1000, seed=9, terminate_prob=0.05, start=start)
+    prm = oracle_lib.make_params("ppr", seed=9, walker_num=1000, terminate_prob=0.05, weighted=True, start=start)
+    lens, verts, _ = oracle_lib.walk(oracle_lib.CSR(300, csr["off"], csr["nbr"], csr["w"]), prm, cap=4096)
+    np.testing.assert_array_equal(ps.path_length, lens)
+    np.testing.assert_array_equal(ps.vertices, verts)
+
+
+def test_epochs_give_the_same_paths_and_dump(kk, engine, tmp_path):
+    """WalkConfig rate (-r) splits walkers into epochs (include/walk.hpp:804-844):
+    paths per walker do not change, and the dump equals the reference's text."""
+    d = np.load(os.path.join(GOLDEN, "dump_deepwalk_head1.npz"))
+    params = json.loads(str(d["params"]))
+    V = int(d["V"])
+    csr = G.csr_file_order(V, d["src"], d["dst"], w=d["w"])
+    engine.load_arrays(V, csr["off"], csr["nbr"], csr["w"])
+    conf = kk.WalkConfig()
+    conf.set_walk_rate(params["rate"])
+    conf.set_output_file(str(tmp_path / "walks"), True)
+    engine.set_concurrency(params["threads"])
+    ps = kk.deepwalk(engine, params["walkers"], params["len"], conf, seed=params["seed"])
+    engine.set_concurrency(1)
+    np.testing.assert_array_equal(ps.path_length, d["lens"])
+    np.testing.assert_array_equal(ps.vertices, d["verts"])
+    assert (tmp_path / "walks.0").read_text() == str(d["text"])
+
+
+def test_binary_file_load_matches_file_order(kk, engine, tmp_path):
+    g = G.random_undirected(200, 2000, seed=11, weight="int5")
+    f = tmp_path / "g.bin"
+    G.write_edge_file(f, g, "f32")
+    engine.load_graph(200, f, kind="f32")
+    dg = engine.download_graph()
+    csr = G.csr_file_order(200, g["src"], g["dst"], w=g["w"])
+    np.testing.assert_array_equal(dg["off"], csr["off"])
+    np.testing.assert_array_equal(dg["nbr"], csr["nbr"])
+    np.testing.assert_array_equal(dg["w"], csr["w"])
+    # --make-undirected on a directed file: edges mirrored one by one (include/graph.hpp:430-443)
+    half = {"V": 200, "src": g["src"][0::2], "dst": g["dst"][0::2], "w": g["w"][0::2]}
+    G.write_edge_file(f, half, "f32")
+    engine.load_graph(200, f, load_as_undirected=True, kind="f32")
+    dg2 = engine.download_graph()
+    np.testing.assert_array_equal(dg2["nbr"], csr["nbr"])
+
+
+def test_invalid_configs_raise(kk, engine):
+    g = G.random_undirected(50, 200, seed=1)
+    csr = G.csr_file_order(50, g["src"], g["dst"])
+    engine.load_arrays(50, csr["off"], csr["nbr"])
+    with pytest.raises(kk.KKError):
+        engine.walk("node2vec", 10, p=0.0, q=1.0)
+    with pytest.raises(kk.KKError):
+        engine.walk("deepwalk", 10, weighted=True)
+    with pytest.raises(kk.KKError):
+        engine.walk("metapath", 10, schemes=[[1]])
+    with pytest.raises(kk.KKError):
+        engine.walk("ppr", 10, terminate_prob=0.0)

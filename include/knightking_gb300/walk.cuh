@@ -114,99 +114,316 @@ struct __align__(16) AliasBucket
 
 /* ---- alias-table build (init_alias_tables, include/walk.hpp:538-652) -------
  *
- * Per vertex, exactly the reference's order: prob[e] = static_comp in CSR
- * order with a sequential float sum; ave = sum / deg; edges below ave go to
- * the p queue, the rest to the q queue, both in edge order; then FIFO pairing:
- * pop p, pop q, bucket = (prob[p]/ave, p, q), prob[q] -= ave - prob[p], q goes
- * to the p or q tail by the same test; leftovers get p = 1 and no alias.
+ * Per vertex, the reference's order: prob[e] = static_comp in CSR order with a
+ * sequential float sum; ave = sum / deg; edges below ave go to the p queue,
+ * the rest to the q queue, both in edge order; then FIFO pairing: pop p, pop
+ * q, bucket = (prob[p]/ave, p, q), prob[q] -= ave - prob[p], q goes to the p
+ * or q tail by the same test; leftovers get p = 1 and no alias.
  *
- * Each queue entry carries (index, current prob): an index sits in at most one
+ * Queue entries carry (index, current prob): an index sits in at most one
  * queue at a time and its prob only changes when it is popped from q, so the
  * entry's value is always the reference's prob[index].  Both queues are linear
  * arrays of deg entries (the q tail never passes deg: q_tail = B + I - C <= deg
- * for B initial bigs, I pairings and C conversions, since I <= S + C).  Scratch:
- * 2*deg (uint32 index, float prob) entries per vertex at 2*off[v]. */
-template <typename TC>
-__device__ __forceinline__ void alias_build_vertex(const GraphView &g, const TC &tc, uint32_t v, AliasBucket *out,
-                                                   float *sum_out, uint2 *scratch)
+ * for B initial bigs, I pairings and C conversions, since I <= S + C).
+ *
+ * Batched exact pairing: while both queues hold at least b live entries, the
+ * next b iterations read only entries that already exist (p[ph..ph+b),
+ * q[qh..qh+b)) and write only past the tails, so they are independent.  They
+ * run as one parallel batch: iteration i of the batch is lane/thread i, and
+ * the conversions and survivors are appended to the p and q tails in
+ * iteration order by a stable ballot/prefix compaction.  The result is the
+ * sequential algorithm's, bucket for bucket and bit for bit; only the serial
+ * sum stays sequential.
+ *
+ * Two kernels: a warp per vertex for degrees below kAliasBigDegree (queues in
+ * shared memory up to kAliasWarpSmem entries, else in the 16 B/edge scratch at
+ * 2*off[v]), and a 1024-thread block per vertex for the hubs above it. */
+
+constexpr uint32_t kAliasWarpSmem = 256;
+constexpr uint32_t kAliasBigDegree = 4096;
+constexpr unsigned kFullMask = 0xffffffffu;
+
+__device__ __forceinline__ uint32_t lanemask_lt()
 {
-    int64_t e0 = g.off[v];
-    uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
-    if (deg == 0)
-    {
-        return;
-    }
-    float sum = 0.0f;
-    for (uint32_t e = 0; e < deg; e++)
-    {
-        sum = fadd(sum, tc.static_comp(v, AdjUnit{g.nbr[e0 + e], (edge_id_t)(e0 + e)}));
-    }
-    if (sum_out != nullptr)
-    {
-        sum_out[v] = sum;
-    }
-    float ave = fdiv(sum, u2f(deg));
-    uint2 *P = scratch + 2 * e0;
-    uint2 *Q = P + deg;
-    uint32_t pt = 0, qt = 0;
-    for (uint32_t e = 0; e < deg; e++)
-    {
-        float x = tc.static_comp(v, AdjUnit{g.nbr[e0 + e], (edge_id_t)(e0 + e)});
-        uint2 entry = make_uint2(e, __float_as_uint(x));
-        if (x < ave)
-            P[pt++] = entry;
-        else
-            Q[qt++] = entry;
-    }
-    uint32_t ph = 0, qh = 0;
-    AliasBucket *b = out + e0;
-    while (pt != ph)
-    {
-        uint2 pe = P[ph++];
-        float pv = __uint_as_float(pe.y);
-        AliasBucket nb;
-        nb.pad = 0;
-        nb.p_idx = pe.x;
-        if (qt != qh)
-        {
-            uint2 qe = Q[qh++];
-            float qv = __uint_as_float(qe.y);
-            nb.p = fdiv(pv, ave);
-            nb.q_idx = qe.x;
-            float diff = fsub(ave, pv);
-            qv = fsub(qv, diff);
-            uint2 ne = make_uint2(qe.x, __float_as_uint(qv));
-            if (qv < ave)
-                P[pt++] = ne;
-            else
-                Q[qt++] = ne;
-        }
-        else
-        {
-            nb.p = 1.0f;
-            nb.q_idx = kNone;
-        }
-        *b++ = nb;
-    }
-    while (qt != qh)
-    {
-        uint2 qe = Q[qh++];
-        AliasBucket nb;
-        nb.p = 1.0f;
-        nb.p_idx = qe.x;
-        nb.q_idx = kNone;
-        nb.pad = 0;
-        *b++ = nb;
-    }
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
 }
 
 template <typename TC>
-__global__ void __launch_bounds__(128) alias_build_kernel(GraphView g, TC tc, AliasBucket *out, float *sum_out,
-                                                          uint2 *scratch)
+__device__ __forceinline__ float static_at(const GraphView &g, const TC &tc, uint32_t v, int64_t e)
+{
+    return tc.static_comp(v, AdjUnit{g.nbr[e], (edge_id_t)e});
+}
+
+template <typename TC>
+__global__ void __launch_bounds__(256) alias_build_warp_kernel(GraphView g, TC tc, AliasBucket *out, float *sum_out,
+                                                               uint2 *scratch)
+{
+    __shared__ uint2 sq[8][2 * kAliasWarpSmem];
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint32_t lt = lanemask_lt();
+    const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t v = blockIdx.x * (blockDim.x >> 5) + wib; v < g.V; v += nwarps)
+    {
+        const int64_t e0 = g.off[v];
+        const uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
+        if (deg == 0 || deg >= kAliasBigDegree)
+            continue;
+        /* sequential sum in CSR order (:579-584); every lane carries it */
+        float sum = 0.0f;
+        float x0 = 0.0f;
+        for (uint32_t base = 0; base < deg; base += 32)
+        {
+            const uint32_t n = min(32u, deg - base);
+            float x = lane < n ? static_at(g, tc, v, e0 + base + lane) : 0.0f;
+            if (base == 0)
+                x0 = x;
+            for (uint32_t j = 0; j < n; j++)
+                sum = fadd(sum, __shfl_sync(kFullMask, x, j));
+        }
+        if (lane == 0 && sum_out != nullptr)
+            sum_out[v] = sum;
+        const float ave = fdiv(sum, u2f(deg)); /* :589 */
+        uint2 *P, *Q;
+        if (deg <= kAliasWarpSmem)
+        {
+            P = sq[wib];
+            Q = sq[wib] + kAliasWarpSmem;
+        }
+        else
+        {
+            P = scratch + 2 * e0;
+            Q = P + deg;
+        }
+        /* stable split into the p and q queues (:594-603) */
+        uint32_t pt = 0, qt = 0;
+        for (uint32_t base = 0; base < deg; base += 32)
+        {
+            const bool valid = base + lane < deg;
+            float x = base == 0 ? x0 : (valid ? static_at(g, tc, v, e0 + base + lane) : 0.0f);
+            const bool sm = valid && x < ave;
+            const bool bg = valid && !(x < ave);
+            const uint32_t mp = __ballot_sync(kFullMask, sm), mq = __ballot_sync(kFullMask, bg);
+            const uint2 ent = make_uint2(base + lane, __float_as_uint(x));
+            if (sm)
+                P[pt + __popc(mp & lt)] = ent;
+            if (bg)
+                Q[qt + __popc(mq & lt)] = ent;
+            pt += __popc(mp);
+            qt += __popc(mq);
+        }
+        __syncwarp();
+        /* FIFO pairing in exact batches (:605-630) */
+        uint32_t ph = 0, qh = 0;
+        AliasBucket *o = out + e0;
+        while (ph < pt)
+        {
+            const uint32_t lp = pt - ph, lq = qt - qh;
+            if (lq == 0)
+            {
+                for (uint32_t i = lane; i < lp; i += 32)
+                    o[i] = AliasBucket{1.0f, P[ph + i].x, kNone, 0};
+                o += lp;
+                ph = pt;
+                break;
+            }
+            const uint32_t b = min(min(lp, lq), 32u);
+            const bool act = lane < b;
+            bool conv = false;
+            uint2 ne = make_uint2(0, 0);
+            if (act)
+            {
+                const uint2 pe = P[ph + lane], qe = Q[qh + lane];
+                const float pv = __uint_as_float(pe.y), qv = __uint_as_float(qe.y);
+                o[lane] = AliasBucket{fdiv(pv, ave), pe.x, qe.x, 0};
+                const float r = fsub(qv, fsub(ave, pv));
+                conv = r < ave;
+                ne = make_uint2(qe.x, __float_as_uint(r));
+            }
+            const uint32_t mc = __ballot_sync(kFullMask, act && conv), ms = __ballot_sync(kFullMask, act && !conv);
+            if (act)
+            {
+                if (conv)
+                    P[pt + __popc(mc & lt)] = ne;
+                else
+                    Q[qt + __popc(ms & lt)] = ne;
+            }
+            __syncwarp();
+            ph += b;
+            qh += b;
+            o += b;
+            pt += __popc(mc);
+            qt += __popc(ms);
+        }
+        /* leftovers of q (:631-638) */
+        for (uint32_t i = lane; i < qt - qh; i += 32)
+            o[i] = AliasBucket{1.0f, Q[qh + i].x, kNone, 0};
+        __syncwarp();
+    }
+}
+
+/* Block-wide stable ranks of two predicates (a, b): exclusive ranks in thread
+ * order and the totals.  scratch: 2 x 33 words of shared memory. */
+__device__ __forceinline__ void block_rank2(bool a, bool b, uint32_t &ra, uint32_t &rb, uint32_t &ta, uint32_t &tb,
+                                            uint32_t *sa, uint32_t *sb)
+{
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const uint32_t lt = lanemask_lt();
+    const uint32_t ma = __ballot_sync(kFullMask, a), mb = __ballot_sync(kFullMask, b);
+    if (lane == 0)
+    {
+        sa[wid] = __popc(ma);
+        sb[wid] = __popc(mb);
+    }
+    __syncthreads();
+    if (wid == 0)
+    {
+        uint32_t xa = lane < nw ? sa[lane] : 0, xb = lane < nw ? sb[lane] : 0;
+        uint32_t ia = xa, ib = xb;
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            uint32_t ya = __shfl_up_sync(kFullMask, ia, o), yb = __shfl_up_sync(kFullMask, ib, o);
+            if (lane >= (uint32_t)o)
+            {
+                ia += ya;
+                ib += yb;
+            }
+        }
+        if (lane < nw)
+        {
+            sa[lane] = ia - xa;
+            sb[lane] = ib - xb;
+        }
+        if (lane == 31)
+        {
+            sa[32] = ia;
+            sb[32] = ib;
+        }
+    }
+    __syncthreads();
+    ra = sa[wid] + __popc(ma & lt);
+    rb = sb[wid] + __popc(mb & lt);
+    ta = sa[32];
+    tb = sb[32];
+}
+
+template <typename TC>
+__global__ void __launch_bounds__(1024) alias_build_block_kernel(GraphView g, TC tc, AliasBucket *out, float *sum_out,
+                                                                 uint2 *scratch, const uint32_t *verts,
+                                                                 uint32_t nverts)
+{
+    __shared__ float chunk[1024];
+    __shared__ uint32_t sa[33], sb[33];
+    __shared__ float s_ave;
+    const uint32_t tid = threadIdx.x;
+    const uint32_t nt = blockDim.x;
+    for (uint32_t k = blockIdx.x; k < nverts; k += gridDim.x)
+    {
+        const uint32_t v = verts[k];
+        const int64_t e0 = g.off[v];
+        const uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
+        /* sequential sum, staged through shared memory (:579-584) */
+        float sum = 0.0f;
+        for (uint32_t base = 0; base < deg; base += nt)
+        {
+            const uint32_t n = min(nt, deg - base);
+            if (tid < n)
+                chunk[tid] = static_at(g, tc, v, e0 + base + tid);
+            __syncthreads();
+            if (tid == 0)
+            {
+#pragma unroll 8
+                for (uint32_t j = 0; j < n; j++)
+                    sum = fadd(sum, chunk[j]);
+            }
+            __syncthreads();
+        }
+        if (tid == 0)
+        {
+            s_ave = fdiv(sum, u2f(deg));
+            if (sum_out != nullptr)
+                sum_out[v] = sum;
+        }
+        __syncthreads();
+        const float ave = s_ave;
+        uint2 *P = scratch + 2 * e0;
+        uint2 *Q = P + deg;
+        uint32_t pt = 0, qt = 0;
+        for (uint32_t base = 0; base < deg; base += nt)
+        {
+            const bool valid = base + tid < deg;
+            const float x = valid ? static_at(g, tc, v, e0 + base + tid) : 0.0f;
+            const bool sm = valid && x < ave, bg = valid && !(x < ave);
+            uint32_t rs, rq, ts, tq;
+            block_rank2(sm, bg, rs, rq, ts, tq, sa, sb);
+            const uint2 ent = make_uint2(base + tid, __float_as_uint(x));
+            if (sm)
+                P[pt + rs] = ent;
+            if (bg)
+                Q[qt + rq] = ent;
+            pt += ts;
+            qt += tq;
+            __syncthreads();
+        }
+        uint32_t ph = 0, qh = 0;
+        AliasBucket *o = out + e0;
+        while (ph < pt)
+        {
+            const uint32_t lp = pt - ph, lq = qt - qh;
+            if (lq == 0)
+            {
+                for (uint32_t i = tid; i < lp; i += nt)
+                    o[i] = AliasBucket{1.0f, P[ph + i].x, kNone, 0};
+                o += lp;
+                ph = pt;
+                break;
+            }
+            const uint32_t b = min(min(lp, lq), nt);
+            const bool act = tid < b;
+            bool conv = false;
+            uint2 ne = make_uint2(0, 0);
+            if (act)
+            {
+                const uint2 pe = P[ph + tid], qe = Q[qh + tid];
+                const float pv = __uint_as_float(pe.y), qv = __uint_as_float(qe.y);
+                o[tid] = AliasBucket{fdiv(pv, ave), pe.x, qe.x, 0};
+                const float r = fsub(qv, fsub(ave, pv));
+                conv = r < ave;
+                ne = make_uint2(qe.x, __float_as_uint(r));
+            }
+            uint32_t rc, rs, tcn, tsn;
+            block_rank2(act && conv, act && !conv, rc, rs, tcn, tsn, sa, sb);
+            if (act)
+            {
+                if (conv)
+                    P[pt + rc] = ne;
+                else
+                    Q[qt + rs] = ne;
+            }
+            __syncthreads();
+            ph += b;
+            qh += b;
+            o += b;
+            pt += tcn;
+            qt += tsn;
+        }
+        for (uint32_t i = tid; i < qt - qh; i += nt)
+            o[i] = AliasBucket{1.0f, Q[qh + i].x, kNone, 0};
+        __syncthreads();
+    }
+}
+
+/* Vertices whose degree reaches `threshold`, as (degree << 32 | vertex), in
+ * no particular order. */
+static __global__ void collect_big_vertices_kernel(GraphView g, uint32_t threshold, unsigned long long *list,
+                                                   uint32_t *count)
 {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += gridDim.x * blockDim.x)
     {
-        alias_build_vertex(g, tc, v, out, sum_out, scratch);
+        uint64_t d = (uint64_t)(g.off[v + 1] - g.off[v]);
+        if (d >= threshold)
+            list[atomicAdd(count, 1u)] = (d << 32) | v;
     }
 }
 

@@ -36,6 +36,8 @@ void kk_engine::free_graph()
     V = 0;
     E = 0;
     sorted = -1;
+    big_valid = false;
+    n_big = 0;
 }
 
 namespace kk
@@ -266,8 +268,11 @@ kk_status kk_engine_create(kk_engine **out, int device)
         KK_CUDA_CHECK(cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, device));
         KK_CUDA_CHECK(cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking));
         e->stream = e->own_stream;
+        KK_CUDA_CHECK(cudaStreamCreateWithFlags(&e->side, cudaStreamNonBlocking));
         for (int i = 0; i < 3; i++)
             KK_CUDA_CHECK(cudaEventCreate(&e->ev[i]));
+        KK_CUDA_CHECK(cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming));
+        KK_CUDA_CHECK(cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming));
     });
     if (s != KK_OK)
     {
@@ -293,6 +298,16 @@ void kk_engine_destroy(kk_engine *e)
     for (int i = 0; i < 3; i++)
         if (e->ev[i])
             cudaEventDestroy(e->ev[i]);
+    if (e->ev_fork)
+        cudaEventDestroy(e->ev_fork);
+    if (e->ev_join)
+        cudaEventDestroy(e->ev_join);
+    e->big_list.release();
+    if (e->side)
+    {
+        cudaStreamSynchronize(e->side);
+        cudaStreamDestroy(e->side);
+    }
     if (e->own_stream)
         cudaStreamDestroy(e->own_stream);
     delete e;

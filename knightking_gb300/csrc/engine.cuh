@@ -121,6 +121,11 @@ struct kk_engine
     kk::DevBuf alias, sum, ra, scratch, vmask, path, length, path_off, caps, start, small, cub_tmp, packed, packed_off;
 
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    cudaStream_t side = nullptr; /* hub alias builds run here, joined by events */
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    kk::DevBuf big_list;
+    uint32_t n_big = 0;
+    bool big_valid = false;
     float alias_ms = 0.0f, walk_ms = 0.0f;
     /* Rejection trials allowed per walker step before the walk fails with
      * KK_ERR_TRIAL_LIMIT (bounds every device loop; a valid configuration with
@@ -153,6 +158,10 @@ inline unsigned grid_for(const kk_engine *e, uint64_t n, unsigned block)
 /* Exclusive scan of n+1 uint64 values in place-ish: out[i] = sum(in[0..i)). */
 void exclusive_scan_u64(kk_engine *e, const uint64_t *in, uint64_t *out, uint64_t n);
 
+/* Device list of the vertices with degree >= kAliasBigDegree, largest first
+ * (cached per graph). */
+const uint32_t *hub_list(kk_engine *e);
+
 /* Builds alias tables into e->alias/e->sum for a static functor. */
 template <typename TC>
 void build_alias(kk_engine *e, const TC &tc)
@@ -161,8 +170,21 @@ void build_alias(kk_engine *e, const TC &tc)
     AliasBucket *alias = e->alias.as<AliasBucket>(e->E);
     float *sum = e->sum.as<float>(e->V);
     uint2 *scratch = e->scratch.as<uint2>(2 * e->E);
-    alias_build_kernel<TC><<<grid_for(e, g.V, 128), 128, 0, e->stream>>>(g, tc, alias, sum, scratch);
+    const uint32_t *big = hub_list(e);
+    if (e->n_big)
+    {
+        /* hubs first, on the side stream, so the largest start at once */
+        KK_CUDA_CHECK(cudaEventRecord(e->ev_fork, e->stream));
+        KK_CUDA_CHECK(cudaStreamWaitEvent(e->side, e->ev_fork, 0));
+        unsigned hub_grid = e->n_big < (uint32_t)e->sm_count ? e->n_big : (unsigned)e->sm_count;
+        alias_build_block_kernel<TC><<<hub_grid, 1024, 0, e->side>>>(g, tc, alias, sum, scratch, big, e->n_big);
+        KK_CUDA_CHECK(cudaGetLastError());
+        KK_CUDA_CHECK(cudaEventRecord(e->ev_join, e->side));
+    }
+    alias_build_warp_kernel<TC><<<(unsigned)e->sm_count * 6, 256, 0, e->stream>>>(g, tc, alias, sum, scratch);
     KK_CUDA_CHECK(cudaGetLastError());
+    if (e->n_big)
+        KK_CUDA_CHECK(cudaStreamWaitEvent(e->stream, e->ev_join, 0));
 }
 
 /* One walk over walkers [rs.walker_begin, + rs.walker_num): alias tables,

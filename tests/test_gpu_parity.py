@@ -202,3 +202,46 @@ def test_invalid_configs_raise(kk, engine):
         engine.walk("metapath", 10, schemes=[[1]])
     with pytest.raises(kk.KKError):
         engine.walk("ppr", 10, terminate_prob=0.0)
+
+
+def _compare_alias(engine, oracle_lib, V, off, nbr, w):
+    p, pi, qi, s = engine.alias_tables()
+    op, opi, oqi, osum = oracle_lib.alias_build(oracle_lib.CSR(V, off, nbr, w))
+    np.testing.assert_array_equal(pi, opi)
+    np.testing.assert_array_equal(qi, oqi)
+    np.testing.assert_array_equal(p.view(np.uint32), op.view(np.uint32))
+    np.testing.assert_array_equal(s.view(np.uint32), osum.view(np.uint32))
+
+
+@pytest.mark.parametrize("weights", [1, 2])
+def test_alias_tables_match_oracle_rmat16(engine, oracle_lib, weights):
+    engine.generate_rmat(16, 16, seed=3, weights=weights)
+    g = engine.download_graph()
+    _compare_alias(engine, oracle_lib, g["V"], g["off"], g["nbr"], g["w"])
+
+
+@pytest.mark.parametrize("dist", ["lognormal", "pareto", "uniform", "equal", "twovalue"])
+def test_alias_tables_match_oracle_hubs(engine, oracle_lib, dist):
+    """Hubs of degree 40000, 5000, 300 and 31 exercise the block kernel, the
+    warp kernel with queues in global scratch and in shared memory."""
+    rng = np.random.default_rng(17)
+    degs = [40000, 5000, 300, 31] + list(rng.integers(0, 40, size=2000))
+    V = 60000
+    degs = np.array(degs + [0] * (V - len(degs)), np.int64)
+    off = np.zeros(V + 1, np.int64)
+    np.cumsum(degs, out=off[1:])
+    E = int(off[-1])
+    nbr = rng.integers(0, V, size=E).astype(np.uint32)
+    if dist == "lognormal":
+        w = rng.lognormal(0.0, 1.0, size=E)
+    elif dist == "pareto":
+        w = rng.pareto(1.2, size=E) + 0.01
+    elif dist == "uniform":
+        w = 1.0 + 4.0 * rng.random(E)
+    elif dist == "equal":
+        w = np.full(E, 0.3)
+    else:
+        w = np.where(rng.random(E) < 0.9, 1.0, 50.0)
+    w = w.astype(np.float32)
+    engine.load_arrays(V, off, nbr, w)
+    _compare_alias(engine, oracle_lib, V, off, nbr, w)

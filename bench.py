@@ -253,6 +253,7 @@ def run_ours(args, wl, world, rank, local):
     walk_ms = []
     alias_ms = []
     with ClockSampler(local) as clocks:
+        time.sleep(0.5)  # nvidia-smi's first sample lands inside the timed region
         ev0.record(stream)
         for _ in range(args.steps):
             total_steps += step()
@@ -339,15 +340,20 @@ def run_ours(args, wl, world, rank, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="deepwalk-s22", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--scale", type=int, default=None, help="override the R-MAT scale (profiling on a small case)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    wl = WORKLOADS[args.workload]
+    wl = dict(WORKLOADS[args.workload])
+    if args.scale is not None:
+        wl["scale"] = args.scale
+        wl["desc"] += " (scale overridden to %d)" % args.scale
+        args.workload += "@s%d" % args.scale
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, wl, world, rank, local)

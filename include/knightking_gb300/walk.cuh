@@ -100,17 +100,27 @@ struct SecondOrderTransitionConfig
     OutSearch outlier_search;
 };
 
-/* One alias bucket (AliasBucket, include/walk.hpp:52-57), 16 B aligned so a
- * bucket is one vector load and never straddles a 32 B sector.  p_idx/q_idx
- * are indices local to the vertex's adjacency; q_idx == kNone is the
- * reference's q_ptr == nullptr. */
-struct __align__(16) AliasBucket
+/* One alias bucket (AliasBucket, include/walk.hpp:52-57).  p_idx/q_idx are
+ * indices local to the vertex's adjacency (q_idx == kNone is the reference's
+ * q_ptr == nullptr); p_nbr/q_nbr are those edges' neighbours, so a walker
+ * gets its candidate's neighbour from the bucket without a second dependent
+ * gather.  32 B aligned: one bucket is exactly one DRAM sector. */
+struct __align__(32) AliasBucket
 {
     float p;
     uint32_t p_idx;
     uint32_t q_idx;
-    uint32_t pad;
+    uint32_t pad0;
+    uint32_t p_nbr;
+    uint32_t q_nbr;
+    uint32_t pad1;
+    uint32_t pad2;
 };
+
+__device__ __forceinline__ AliasBucket make_bucket(float p, uint32_t pi, uint32_t qi, const uint32_t *nb)
+{
+    return AliasBucket{p, pi, qi, 0, nb[pi], qi == kNone ? kNone : nb[qi], 0, 0};
+}
 
 /* ---- alias-table build (init_alias_tables, include/walk.hpp:538-652) -------
  *
@@ -124,7 +134,9 @@ struct __align__(16) AliasBucket
  * queue at a time and its prob only changes when it is popped from q, so the
  * entry's value is always the reference's prob[index].  Both queues are linear
  * arrays of deg entries (the q tail never passes deg: q_tail = B + I - C <= deg
- * for B initial bigs, I pairings and C conversions, since I <= S + C).
+ * for B initial bigs, I pairings and C conversions, since I <= S + C).  Every
+ * p pop writes one bucket, so bucket k of a vertex is its k-th p pop and the
+ * whole pairing state is (ph, pt, qh, qt).
  *
  * Batched exact pairing: while both queues hold at least b live entries, the
  * next b iterations read only entries that already exist (p[ph..ph+b),
@@ -133,14 +145,19 @@ struct __align__(16) AliasBucket
  * the conversions and survivors are appended to the p and q tails in
  * iteration order by a stable ballot/prefix compaction.  The result is the
  * sequential algorithm's, bucket for bucket and bit for bit; only the serial
- * sum stays sequential.
+ * sum stays sequential (one FADD chain per vertex).
  *
- * Two kernels: a warp per vertex for degrees below kAliasBigDegree (queues in
- * shared memory up to kAliasWarpSmem entries, else in the 16 B/edge scratch at
- * 2*off[v]), and a 1024-thread block per vertex for the hubs above it. */
+ * Vertices run in three tiers over a degree-descending vertex order:
+ *   hubs   (deg > kAliasMidMax): a 1024-thread block per vertex, queues in
+ *          the 16 B/edge scratch at 2*off[v];
+ *   middle (kAliasSmallMax < deg <= kAliasMidMax): a 256-thread block per
+ *          vertex, queues and staged weights in shared memory;
+ *   small  (deg <= kAliasSmallMax): a warp per vertex, all in shared memory.
+ * Block kernels hand batches of 32 or fewer to one warp (no block barrier). */
 
-constexpr uint32_t kAliasWarpSmem = 256;
-constexpr uint32_t kAliasBigDegree = 4096;
+constexpr uint32_t kAliasSmallMax = 32;
+constexpr uint32_t kAliasMidMax = 4096;
+constexpr size_t kAliasMidSmem = (size_t)kAliasMidMax * (2 * sizeof(uint2) + sizeof(float));
 constexpr unsigned kFullMask = 0xffffffffu;
 
 __device__ __forceinline__ uint32_t lanemask_lt()
@@ -156,115 +173,58 @@ __device__ __forceinline__ float static_at(const GraphView &g, const TC &tc, uin
     return tc.static_comp(v, AdjUnit{g.nbr[e], (edge_id_t)e});
 }
 
-template <typename TC>
-__global__ void __launch_bounds__(256) alias_build_warp_kernel(GraphView g, TC tc, AliasBucket *out, float *sum_out,
-                                                               uint2 *scratch)
+/* One warp runs pairing batches of at most 32 iterations until the pairing
+ * ends or both queues again hold more than stop_above live entries. */
+__device__ __forceinline__ void warp_pairing(uint2 *P, uint2 *Q, uint32_t &ph, uint32_t &pt, uint32_t &qh,
+                                             uint32_t &qt, float ave, AliasBucket *ob, const uint32_t *nb,
+                                             uint32_t stop_above)
 {
-    __shared__ uint2 sq[8][2 * kAliasWarpSmem];
-    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const uint32_t lt = lanemask_lt();
-    const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
-    for (uint32_t v = blockIdx.x * (blockDim.x >> 5) + wib; v < g.V; v += nwarps)
+    const uint32_t lane = threadIdx.x & 31, lt = lanemask_lt();
+    while (ph < pt)
     {
-        const int64_t e0 = g.off[v];
-        const uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
-        if (deg == 0 || deg >= kAliasBigDegree)
-            continue;
-        /* sequential sum in CSR order (:579-584); every lane carries it */
-        float sum = 0.0f;
-        float x0 = 0.0f;
-        for (uint32_t base = 0; base < deg; base += 32)
+        const uint32_t lp = pt - ph, lq = qt - qh;
+        if (lq == 0)
         {
-            const uint32_t n = min(32u, deg - base);
-            float x = lane < n ? static_at(g, tc, v, e0 + base + lane) : 0.0f;
-            if (base == 0)
-                x0 = x;
-            for (uint32_t j = 0; j < n; j++)
-                sum = fadd(sum, __shfl_sync(kFullMask, x, j));
+            for (uint32_t i = lane; i < lp; i += 32)
+                ob[ph + i] = make_bucket(1.0f, P[ph + i].x, kNone, nb);
+            ph = pt;
+            break;
         }
-        if (lane == 0 && sum_out != nullptr)
-            sum_out[v] = sum;
-        const float ave = fdiv(sum, u2f(deg)); /* :589 */
-        uint2 *P, *Q;
-        if (deg <= kAliasWarpSmem)
+        uint32_t b = min(lp, lq);
+        if (b > stop_above)
+            break;
+        if (b > 32)
+            b = 32;
+        const bool act = lane < b;
+        bool conv = false;
+        uint2 ne = make_uint2(0, 0);
+        if (act)
         {
-            P = sq[wib];
-            Q = sq[wib] + kAliasWarpSmem;
+            const uint2 pe = P[ph + lane], qe = Q[qh + lane];
+            const float pv = __uint_as_float(pe.y), qv = __uint_as_float(qe.y);
+            ob[ph + lane] = make_bucket(fdiv(pv, ave), pe.x, qe.x, nb);
+            const float r = fsub(qv, fsub(ave, pv));
+            conv = r < ave;
+            ne = make_uint2(qe.x, __float_as_uint(r));
         }
-        else
+        const uint32_t mc = __ballot_sync(kFullMask, act && conv), ms = __ballot_sync(kFullMask, act && !conv);
+        if (act)
         {
-            P = scratch + 2 * e0;
-            Q = P + deg;
-        }
-        /* stable split into the p and q queues (:594-603) */
-        uint32_t pt = 0, qt = 0;
-        for (uint32_t base = 0; base < deg; base += 32)
-        {
-            const bool valid = base + lane < deg;
-            float x = base == 0 ? x0 : (valid ? static_at(g, tc, v, e0 + base + lane) : 0.0f);
-            const bool sm = valid && x < ave;
-            const bool bg = valid && !(x < ave);
-            const uint32_t mp = __ballot_sync(kFullMask, sm), mq = __ballot_sync(kFullMask, bg);
-            const uint2 ent = make_uint2(base + lane, __float_as_uint(x));
-            if (sm)
-                P[pt + __popc(mp & lt)] = ent;
-            if (bg)
-                Q[qt + __popc(mq & lt)] = ent;
-            pt += __popc(mp);
-            qt += __popc(mq);
+            if (conv)
+                P[pt + __popc(mc & lt)] = ne;
+            else
+                Q[qt + __popc(ms & lt)] = ne;
         }
         __syncwarp();
-        /* FIFO pairing in exact batches (:605-630) */
-        uint32_t ph = 0, qh = 0;
-        AliasBucket *o = out + e0;
-        while (ph < pt)
-        {
-            const uint32_t lp = pt - ph, lq = qt - qh;
-            if (lq == 0)
-            {
-                for (uint32_t i = lane; i < lp; i += 32)
-                    o[i] = AliasBucket{1.0f, P[ph + i].x, kNone, 0};
-                o += lp;
-                ph = pt;
-                break;
-            }
-            const uint32_t b = min(min(lp, lq), 32u);
-            const bool act = lane < b;
-            bool conv = false;
-            uint2 ne = make_uint2(0, 0);
-            if (act)
-            {
-                const uint2 pe = P[ph + lane], qe = Q[qh + lane];
-                const float pv = __uint_as_float(pe.y), qv = __uint_as_float(qe.y);
-                o[lane] = AliasBucket{fdiv(pv, ave), pe.x, qe.x, 0};
-                const float r = fsub(qv, fsub(ave, pv));
-                conv = r < ave;
-                ne = make_uint2(qe.x, __float_as_uint(r));
-            }
-            const uint32_t mc = __ballot_sync(kFullMask, act && conv), ms = __ballot_sync(kFullMask, act && !conv);
-            if (act)
-            {
-                if (conv)
-                    P[pt + __popc(mc & lt)] = ne;
-                else
-                    Q[qt + __popc(ms & lt)] = ne;
-            }
-            __syncwarp();
-            ph += b;
-            qh += b;
-            o += b;
-            pt += __popc(mc);
-            qt += __popc(ms);
-        }
-        /* leftovers of q (:631-638) */
-        for (uint32_t i = lane; i < qt - qh; i += 32)
-            o[i] = AliasBucket{1.0f, Q[qh + i].x, kNone, 0};
-        __syncwarp();
+        ph += b;
+        qh += b;
+        pt += __popc(mc);
+        qt += __popc(ms);
     }
 }
 
 /* Block-wide stable ranks of two predicates (a, b): exclusive ranks in thread
- * order and the totals.  scratch: 2 x 33 words of shared memory. */
+ * order and the totals.  sa, sb: 33 words of shared memory each. */
 __device__ __forceinline__ void block_rank2(bool a, bool b, uint32_t &ra, uint32_t &rb, uint32_t &ta, uint32_t &tb,
                                             uint32_t *sa, uint32_t *sb)
 {
@@ -308,22 +268,202 @@ __device__ __forceinline__ void block_rank2(bool a, bool b, uint32_t &ra, uint32
     tb = sb[32];
 }
 
-template <typename TC>
-__global__ void __launch_bounds__(1024) alias_build_block_kernel(GraphView g, TC tc, AliasBucket *out, float *sum_out,
-                                                                 uint2 *scratch, const uint32_t *verts,
-                                                                 uint32_t nverts)
+/* Pairing loop of a block: block-wide batches while both queues are long,
+ * warp 0 alone for short stretches; then the q leftovers (:631-638). */
+__device__ __forceinline__ void block_pairing(uint2 *P, uint2 *Q, uint32_t pt, uint32_t qt, float ave, AliasBucket *ob, const uint32_t *nb,
+                                              uint32_t *sa, uint32_t *sb, uint32_t *s_state)
 {
-    __shared__ float chunk[1024];
-    __shared__ uint32_t sa[33], sb[33];
-    __shared__ float s_ave;
-    const uint32_t tid = threadIdx.x;
-    const uint32_t nt = blockDim.x;
-    for (uint32_t k = blockIdx.x; k < nverts; k += gridDim.x)
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    uint32_t ph = 0, qh = 0;
+    while (ph < pt)
     {
-        const uint32_t v = verts[k];
+        const uint32_t lp = pt - ph, lq = qt - qh;
+        if (lq == 0)
+        {
+            for (uint32_t i = tid; i < lp; i += nt)
+                ob[ph + i] = make_bucket(1.0f, P[ph + i].x, kNone, nb);
+            ph = pt;
+            break;
+        }
+        const uint32_t b = min(min(lp, lq), nt);
+        if (b <= 64)
+        {
+            if (tid < 32)
+            {
+                warp_pairing(P, Q, ph, pt, qh, qt, ave, ob, nb, 128);
+                if (tid == 0)
+                {
+                    s_state[0] = ph;
+                    s_state[1] = pt;
+                    s_state[2] = qh;
+                    s_state[3] = qt;
+                }
+            }
+            __syncthreads();
+            ph = s_state[0];
+            pt = s_state[1];
+            qh = s_state[2];
+            qt = s_state[3];
+            __syncthreads();
+            continue;
+        }
+        const bool act = tid < b;
+        bool conv = false;
+        uint2 ne = make_uint2(0, 0);
+        if (act)
+        {
+            const uint2 pe = P[ph + tid], qe = Q[qh + tid];
+            const float pv = __uint_as_float(pe.y), qv = __uint_as_float(qe.y);
+            ob[ph + tid] = make_bucket(fdiv(pv, ave), pe.x, qe.x, nb);
+            const float r = fsub(qv, fsub(ave, pv));
+            conv = r < ave;
+            ne = make_uint2(qe.x, __float_as_uint(r));
+        }
+        uint32_t rc, rs, tcn, tsn;
+        block_rank2(act && conv, act && !conv, rc, rs, tcn, tsn, sa, sb);
+        if (act)
+        {
+            if (conv)
+                P[pt + rc] = ne;
+            else
+                Q[qt + rs] = ne;
+        }
+        __syncthreads();
+        ph += b;
+        qh += b;
+        pt += tcn;
+        qt += tsn;
+    }
+    for (uint32_t i = tid; i < qt - qh; i += nt)
+        ob[pt + i] = make_bucket(1.0f, Q[qh + i].x, kNone, nb);
+    __syncthreads();
+}
+
+/* Stable block-wide split of the staged values into the p and q queues. */
+template <typename Load>
+__device__ __forceinline__ void block_split(Load load, uint32_t deg, float ave, uint2 *P, uint2 *Q, uint32_t &pt,
+                                            uint32_t &qt, uint32_t *sa, uint32_t *sb)
+{
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    pt = 0;
+    qt = 0;
+    for (uint32_t base = 0; base < deg; base += nt)
+    {
+        const bool valid = base + tid < deg;
+        const float x = valid ? load(base + tid) : 0.0f;
+        const bool sm = valid && x < ave, bg = valid && !(x < ave);
+        uint32_t rs, rq, ts, tq;
+        block_rank2(sm, bg, rs, rq, ts, tq, sa, sb);
+        const uint2 ent = make_uint2(base + tid, __float_as_uint(x));
+        if (sm)
+            P[pt + rs] = ent;
+        if (bg)
+            Q[qt + rq] = ent;
+        pt += ts;
+        qt += tq;
+        __syncthreads();
+    }
+}
+
+/* Small tier: a warp per vertex of degree <= 32, everything on chip. */
+template <typename TC>
+__global__ void __launch_bounds__(256) alias_build_small_kernel(GraphView g, TC tc, AliasBucket *out, float *sum_out,
+                                                                const uint32_t *order, uint32_t lo, uint32_t hi)
+{
+    __shared__ uint2 sq[8][2 * kAliasSmallMax];
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint32_t lt = lanemask_lt();
+    const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t k = lo + blockIdx.x * (blockDim.x >> 5) + wib; k < hi; k += nwarps)
+    {
+        const uint32_t v = order[k];
         const int64_t e0 = g.off[v];
         const uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
-        /* sequential sum, staged through shared memory (:579-584) */
+        const float x = lane < deg ? static_at(g, tc, v, e0 + lane) : 0.0f;
+        /* sequential sum in CSR order (:579-584), carried by every lane */
+        float sum = 0.0f;
+#pragma unroll
+        for (uint32_t j = 0; j < kAliasSmallMax; j++)
+        {
+            const float y = __shfl_sync(kFullMask, x, j);
+            if (j < deg)
+                sum = fadd(sum, y);
+        }
+        if (lane == 0 && sum_out != nullptr)
+            sum_out[v] = sum;
+        const float ave = fdiv(sum, u2f(deg)); /* :589 */
+        uint2 *P = sq[wib], *Q = sq[wib] + kAliasSmallMax;
+        const bool sm = lane < deg && x < ave, bg = lane < deg && !(x < ave);
+        const uint32_t mp = __ballot_sync(kFullMask, sm), mq = __ballot_sync(kFullMask, bg);
+        const uint2 ent = make_uint2(lane, __float_as_uint(x));
+        if (sm)
+            P[__popc(mp & lt)] = ent;
+        if (bg)
+            Q[__popc(mq & lt)] = ent;
+        __syncwarp();
+        uint32_t ph = 0, pt = __popc(mp), qh = 0, qt = __popc(mq);
+        AliasBucket *ob = out + e0;
+        const uint32_t *nb = g.nbr + e0;
+        warp_pairing(P, Q, ph, pt, qh, qt, ave, ob, nb, 0xffffffffu);
+        for (uint32_t i = lane; i < qt - qh; i += 32)
+            ob[pt + i] = make_bucket(1.0f, Q[qh + i].x, kNone, nb);
+        __syncwarp();
+    }
+}
+
+/* Middle tier: a 256-thread block per vertex, queues and weights in shared memory. */
+template <typename TC>
+__global__ void __launch_bounds__(256) alias_build_mid_kernel(GraphView g, TC tc, AliasBucket *out, float *sum_out,
+                                                              const uint32_t *order, uint32_t lo, uint32_t hi)
+{
+    extern __shared__ uint2 dyn[];
+    uint2 *P = dyn;
+    uint2 *Q = dyn + kAliasMidMax;
+    float *stage = (float *)(dyn + 2 * kAliasMidMax);
+    __shared__ uint32_t sa[33], sb[33], s_state[4];
+    __shared__ float s_ave;
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    for (uint32_t k = lo + blockIdx.x; k < hi; k += gridDim.x)
+    {
+        const uint32_t v = order[k];
+        const int64_t e0 = g.off[v];
+        const uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
+        for (uint32_t i = tid; i < deg; i += nt)
+            stage[i] = static_at(g, tc, v, e0 + i);
+        __syncthreads();
+        if (tid == 0)
+        {
+            float sum = 0.0f;
+#pragma unroll 8
+            for (uint32_t j = 0; j < deg; j++)
+                sum = fadd(sum, stage[j]);
+            s_ave = fdiv(sum, u2f(deg));
+            if (sum_out != nullptr)
+                sum_out[v] = sum;
+        }
+        __syncthreads();
+        const float ave = s_ave;
+        uint32_t pt, qt;
+        block_split([&](uint32_t i) { return stage[i]; }, deg, ave, P, Q, pt, qt, sa, sb);
+        block_pairing(P, Q, pt, qt, ave, out + e0, g.nbr + e0, sa, sb, s_state);
+    }
+}
+
+/* Hub tier: a 1024-thread block per vertex, queues in global scratch. */
+template <typename TC>
+__global__ void __launch_bounds__(1024) alias_build_hub_kernel(GraphView g, TC tc, AliasBucket *out, float *sum_out,
+                                                               uint2 *scratch, const uint32_t *order, uint32_t lo,
+                                                               uint32_t hi)
+{
+    __shared__ float chunk[1024];
+    __shared__ uint32_t sa[33], sb[33], s_state[4];
+    __shared__ float s_ave;
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    for (uint32_t k = lo + blockIdx.x; k < hi; k += gridDim.x)
+    {
+        const uint32_t v = order[k];
+        const int64_t e0 = g.off[v];
+        const uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
         float sum = 0.0f;
         for (uint32_t base = 0; base < deg; base += nt)
         {
@@ -349,81 +489,35 @@ __global__ void __launch_bounds__(1024) alias_build_block_kernel(GraphView g, TC
         const float ave = s_ave;
         uint2 *P = scratch + 2 * e0;
         uint2 *Q = P + deg;
-        uint32_t pt = 0, qt = 0;
-        for (uint32_t base = 0; base < deg; base += nt)
-        {
-            const bool valid = base + tid < deg;
-            const float x = valid ? static_at(g, tc, v, e0 + base + tid) : 0.0f;
-            const bool sm = valid && x < ave, bg = valid && !(x < ave);
-            uint32_t rs, rq, ts, tq;
-            block_rank2(sm, bg, rs, rq, ts, tq, sa, sb);
-            const uint2 ent = make_uint2(base + tid, __float_as_uint(x));
-            if (sm)
-                P[pt + rs] = ent;
-            if (bg)
-                Q[qt + rq] = ent;
-            pt += ts;
-            qt += tq;
-            __syncthreads();
-        }
-        uint32_t ph = 0, qh = 0;
-        AliasBucket *o = out + e0;
-        while (ph < pt)
-        {
-            const uint32_t lp = pt - ph, lq = qt - qh;
-            if (lq == 0)
-            {
-                for (uint32_t i = tid; i < lp; i += nt)
-                    o[i] = AliasBucket{1.0f, P[ph + i].x, kNone, 0};
-                o += lp;
-                ph = pt;
-                break;
-            }
-            const uint32_t b = min(min(lp, lq), nt);
-            const bool act = tid < b;
-            bool conv = false;
-            uint2 ne = make_uint2(0, 0);
-            if (act)
-            {
-                const uint2 pe = P[ph + tid], qe = Q[qh + tid];
-                const float pv = __uint_as_float(pe.y), qv = __uint_as_float(qe.y);
-                o[tid] = AliasBucket{fdiv(pv, ave), pe.x, qe.x, 0};
-                const float r = fsub(qv, fsub(ave, pv));
-                conv = r < ave;
-                ne = make_uint2(qe.x, __float_as_uint(r));
-            }
-            uint32_t rc, rs, tcn, tsn;
-            block_rank2(act && conv, act && !conv, rc, rs, tcn, tsn, sa, sb);
-            if (act)
-            {
-                if (conv)
-                    P[pt + rc] = ne;
-                else
-                    Q[qt + rs] = ne;
-            }
-            __syncthreads();
-            ph += b;
-            qh += b;
-            o += b;
-            pt += tcn;
-            qt += tsn;
-        }
-        for (uint32_t i = tid; i < qt - qh; i += nt)
-            o[i] = AliasBucket{1.0f, Q[qh + i].x, kNone, 0};
-        __syncthreads();
+        uint32_t pt, qt;
+        block_split([&](uint32_t i) { return static_at(g, tc, v, e0 + i); }, deg, ave, P, Q, pt, qt, sa, sb);
+        block_pairing(P, Q, pt, qt, ave, out + e0, g.nbr + e0, sa, sb, s_state);
     }
 }
 
-/* Vertices whose degree reaches `threshold`, as (degree << 32 | vertex), in
- * no particular order. */
-static __global__ void collect_big_vertices_kernel(GraphView g, uint32_t threshold, unsigned long long *list,
-                                                   uint32_t *count)
+/* Degree-descending vertex order support: degrees and iota for a radix sort. */
+static __global__ void degree_keys_kernel(GraphView g, uint32_t *deg, uint32_t *ids)
 {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += gridDim.x * blockDim.x)
     {
-        uint64_t d = (uint64_t)(g.off[v + 1] - g.off[v]);
-        if (d >= threshold)
-            list[atomicAdd(count, 1u)] = (d << 32) | v;
+        deg[v] = (uint32_t)(g.off[v + 1] - g.off[v]);
+        ids[v] = v;
+    }
+}
+
+/* Tier boundaries in the sorted degrees: counts of degree > hub, > small, > 0. */
+static __global__ void tier_bounds_kernel(const uint32_t *sorted_deg, uint32_t n, uint32_t mid_max, uint32_t small_max,
+                                          uint32_t *bounds)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const uint32_t d = sorted_deg[i], dn = i + 1 < n ? sorted_deg[i + 1] : 0;
+        if (d > mid_max && dn <= mid_max)
+            bounds[0] = i + 1;
+        if (d > small_max && dn <= small_max)
+            bounds[1] = i + 1;
+        if (d > 0 && dn == 0)
+            bounds[2] = i + 1;
     }
 }
 
@@ -492,20 +586,25 @@ __device__ __forceinline__ vertex_id_t walker_start(const GraphView &g, const WC
 }
 
 /* Candidate pick: uniform (include/walk.hpp:1016-1018) or alias
- * (:1020-1028; the coin is drawn only when the bucket has an alias). */
+ * (:1020-1028; the coin is drawn only when the bucket has an alias).
+ * Returns (index local to the adjacency, neighbour): an alias bucket carries
+ * both, read as two 16 B halves of one 32 B sector. */
 template <typename TC>
-__device__ __forceinline__ uint32_t pick_candidate(const AliasBucket *alias, int64_t e0, uint32_t deg, Sampler &rng)
+__device__ __forceinline__ uint2 pick_candidate(const GraphView &g, const AliasBucket *alias, int64_t e0, uint32_t deg,
+                                                Sampler &rng)
 {
     if constexpr (TC::has_static)
     {
-        AliasBucket b = alias[e0 + rng.gen(deg)];
-        if (b.q_idx == kNone || rng.gen_float(1.0f) < b.p)
-            return b.p_idx;
-        return b.q_idx;
+        const uint4 *b4 = reinterpret_cast<const uint4 *>(alias + e0 + rng.gen(deg));
+        const uint4 lo = __ldg(b4), hi = __ldg(b4 + 1);
+        if (lo.z == kNone || rng.gen_float(1.0f) < __uint_as_float(lo.x))
+            return make_uint2(lo.y, hi.x);
+        return make_uint2(lo.z, hi.y);
     }
     else
     {
-        return rng.gen(deg);
+        const uint32_t c = rng.gen(deg);
+        return make_uint2(c, g.nbr[e0 + c]);
     }
 }
 
@@ -595,8 +694,9 @@ __global__ void __launch_bounds__(256) walk_first_order_kernel(GraphView g, WC w
                             }
                         }
                     }
-                    uint32_t cand = pick_candidate<TC>(alias, e0, deg, rng);
-                    vertex_id_t cn = g.nbr[e0 + cand];
+                    const uint2 pc = pick_candidate<TC>(g, alias, e0, deg, rng);
+                    const uint32_t cand = pc.x;
+                    const vertex_id_t cn = pc.y;
                     if constexpr (TC::has_dynamic)
                     {
                         float dart = rng.gen_float(tc.dcomp_upperbound(v, adj));
@@ -734,8 +834,8 @@ __global__ void __launch_bounds__(256) walk_second_order_kernel(GraphView g, WC 
                         }
                         if (!in_app)
                         {
-                            uint32_t cand = pick_candidate<TC>(alias, e0, deg, rng);
-                            cu = AdjUnit{g.nbr[e0 + cand], (edge_id_t)(e0 + cand)};
+                            const uint2 pc = pick_candidate<TC>(g, alias, e0, deg, rng);
+                            cu = AdjUnit{pc.y, (edge_id_t)(e0 + pc.x)};
                             randval = rng.gen_float(tc.dcomp_upperbound(v, adj));
                             if constexpr (TC::has_lowerbound)
                                 accepted = randval <= tc.dcomp_lowerbound(v, adj);

@@ -36,8 +36,8 @@ void kk_engine::free_graph()
     V = 0;
     E = 0;
     sorted = -1;
-    big_valid = false;
-    n_big = 0;
+    order_valid = false;
+    n_hub = n_mid = n_nz = 0;
 }
 
 namespace kk
@@ -302,7 +302,7 @@ void kk_engine_destroy(kk_engine *e)
         cudaEventDestroy(e->ev_fork);
     if (e->ev_join)
         cudaEventDestroy(e->ev_join);
-    e->big_list.release();
+    e->order.release();
     if (e->side)
     {
         cudaStreamSynchronize(e->side);

@@ -123,9 +123,11 @@ struct kk_engine
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     cudaStream_t side = nullptr; /* hub alias builds run here, joined by events */
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    kk::DevBuf big_list;
-    uint32_t n_big = 0;
-    bool big_valid = false;
+    /* vertices by degree, descending (cached per graph), and the alias tiers:
+     * [0, n_hub) hubs, [n_hub, n_mid) middle, [n_mid, n_nz) small, rest isolated */
+    kk::DevBuf order;
+    uint32_t n_hub = 0, n_mid = 0, n_nz = 0;
+    bool order_valid = false;
     float alias_ms = 0.0f, walk_ms = 0.0f;
     /* Rejection trials allowed per walker step before the walk fails with
      * KK_ERR_TRIAL_LIMIT (bounds every device loop; a valid configuration with
@@ -158,9 +160,8 @@ inline unsigned grid_for(const kk_engine *e, uint64_t n, unsigned block)
 /* Exclusive scan of n+1 uint64 values in place-ish: out[i] = sum(in[0..i)). */
 void exclusive_scan_u64(kk_engine *e, const uint64_t *in, uint64_t *out, uint64_t n);
 
-/* Device list of the vertices with degree >= kAliasBigDegree, largest first
- * (cached per graph). */
-const uint32_t *hub_list(kk_engine *e);
+/* Vertices sorted by degree, descending, with the alias tiers (cached per graph). */
+const uint32_t *vertex_order(kk_engine *e);
 
 /* Builds alias tables into e->alias/e->sum for a static functor. */
 template <typename TC>
@@ -169,21 +170,42 @@ void build_alias(kk_engine *e, const TC &tc)
     GraphView g = e->view();
     AliasBucket *alias = e->alias.as<AliasBucket>(e->E);
     float *sum = e->sum.as<float>(e->V);
-    uint2 *scratch = e->scratch.as<uint2>(2 * e->E);
-    const uint32_t *big = hub_list(e);
-    if (e->n_big)
+    const uint32_t *order = vertex_order(e);
+    const unsigned sms = (unsigned)e->sm_count;
+    if (e->n_hub)
     {
-        /* hubs first, on the side stream, so the largest start at once */
+        /* hubs first, largest first, on the side stream so they start at once */
+        uint2 *scratch = e->scratch.as<uint2>(2 * e->E);
         KK_CUDA_CHECK(cudaEventRecord(e->ev_fork, e->stream));
         KK_CUDA_CHECK(cudaStreamWaitEvent(e->side, e->ev_fork, 0));
-        unsigned hub_grid = e->n_big < (uint32_t)e->sm_count ? e->n_big : (unsigned)e->sm_count;
-        alias_build_block_kernel<TC><<<hub_grid, 1024, 0, e->side>>>(g, tc, alias, sum, scratch, big, e->n_big);
+        unsigned grid = e->n_hub < sms ? e->n_hub : sms;
+        alias_build_hub_kernel<TC><<<grid, 1024, 0, e->side>>>(g, tc, alias, sum, scratch, order, 0, e->n_hub);
         KK_CUDA_CHECK(cudaGetLastError());
         KK_CUDA_CHECK(cudaEventRecord(e->ev_join, e->side));
     }
-    alias_build_warp_kernel<TC><<<(unsigned)e->sm_count * 6, 256, 0, e->stream>>>(g, tc, alias, sum, scratch);
-    KK_CUDA_CHECK(cudaGetLastError());
-    if (e->n_big)
+    if (e->n_mid > e->n_hub)
+    {
+        static bool smem_set = false;
+        if (!smem_set)
+        {
+            KK_CUDA_CHECK(cudaFuncSetAttribute(alias_build_mid_kernel<TC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)kAliasMidSmem));
+            smem_set = true;
+        }
+        uint32_t n = e->n_mid - e->n_hub;
+        unsigned grid = n < 2 * sms ? n : 2 * sms;
+        alias_build_mid_kernel<TC><<<grid, 256, kAliasMidSmem, e->stream>>>(g, tc, alias, sum, order, e->n_hub,
+                                                                           e->n_mid);
+        KK_CUDA_CHECK(cudaGetLastError());
+    }
+    if (e->n_nz > e->n_mid)
+    {
+        uint32_t warps = e->n_nz - e->n_mid;
+        unsigned grid = (warps + 7) / 8 < 8 * sms ? (warps + 7) / 8 : 8 * sms;
+        alias_build_small_kernel<TC><<<grid, 256, 0, e->stream>>>(g, tc, alias, sum, order, e->n_mid, e->n_nz);
+        KK_CUDA_CHECK(cudaGetLastError());
+    }
+    if (e->n_hub)
         KK_CUDA_CHECK(cudaStreamWaitEvent(e->stream, e->ev_join, 0));
 }
 

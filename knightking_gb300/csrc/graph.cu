@@ -151,36 +151,39 @@ __global__ void deg_to_u64_kernel(const unsigned int *deg, uint64_t *out, uint32
 
 } // namespace
 
-const uint32_t *hub_list(kk_engine *e)
+const uint32_t *vertex_order(kk_engine *e)
 {
-    if (e->big_valid)
-        return (const uint32_t *)e->big_list.p;
-    unsigned long long *keys = nullptr;
-    uint32_t *d_count = nullptr;
-    KK_CUDA_CHECK(cudaMalloc(&keys, ((size_t)e->V + 1) * 8));
-    KK_CUDA_CHECK(cudaMalloc(&d_count, 16));
-    KK_CUDA_CHECK(cudaMemsetAsync(d_count, 0, 16, e->stream));
-    collect_big_vertices_kernel<<<grid_for(e, e->V, 256), 256, 0, e->stream>>>(e->view(), kAliasBigDegree, keys,
-                                                                              d_count);
+    if (e->order_valid)
+        return (const uint32_t *)e->order.p;
+    const uint32_t V = e->V;
+    uint32_t *deg = nullptr, *deg_sorted = nullptr, *ids = nullptr, *bounds = nullptr;
+    KK_CUDA_CHECK(cudaMalloc(&deg, (size_t)V * 4 + 4));
+    KK_CUDA_CHECK(cudaMalloc(&deg_sorted, (size_t)V * 4 + 4));
+    KK_CUDA_CHECK(cudaMalloc(&ids, (size_t)V * 4 + 4));
+    KK_CUDA_CHECK(cudaMalloc(&bounds, 16));
+    uint32_t *order = e->order.as<uint32_t>(V);
+    degree_keys_kernel<<<grid_for(e, V, 256), 256, 0, e->stream>>>(e->view(), deg, ids);
     KK_CUDA_CHECK(cudaGetLastError());
-    uint32_t n = 0;
-    KK_CUDA_CHECK(cudaMemcpyAsync(&n, d_count, 4, cudaMemcpyDeviceToHost, e->stream));
+    size_t bytes = 0;
+    KK_CUDA_CHECK(cub::DeviceRadixSort::SortPairsDescending(nullptr, bytes, deg, deg_sorted, ids, order, (int64_t)V, 0,
+                                                            32, e->stream));
+    KK_CUDA_CHECK(cub::DeviceRadixSort::SortPairsDescending(e->cub_tmp.ensure(bytes), bytes, deg, deg_sorted, ids,
+                                                            order, (int64_t)V, 0, 32, e->stream));
+    KK_CUDA_CHECK(cudaMemsetAsync(bounds, 0, 16, e->stream));
+    tier_bounds_kernel<<<grid_for(e, V, 256), 256, 0, e->stream>>>(deg_sorted, V, kAliasMidMax, kAliasSmallMax, bounds);
+    KK_CUDA_CHECK(cudaGetLastError());
+    uint32_t h[3];
+    KK_CUDA_CHECK(cudaMemcpyAsync(h, bounds, 12, cudaMemcpyDeviceToHost, e->stream));
     KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
-    std::vector<unsigned long long> h(n);
-    if (n)
-        KK_CUDA_CHECK(cudaMemcpy(h.data(), keys, (size_t)n * 8, cudaMemcpyDeviceToHost));
-    cudaFree(keys);
-    cudaFree(d_count);
-    std::sort(h.begin(), h.end(), [](unsigned long long a, unsigned long long b) { return a > b; });
-    std::vector<uint32_t> verts(n);
-    for (uint32_t i = 0; i < n; i++)
-        verts[i] = (uint32_t)h[i];
-    uint32_t *list = e->big_list.as<uint32_t>(n ? n : 1);
-    if (n)
-        KK_CUDA_CHECK(cudaMemcpy(list, verts.data(), (size_t)n * 4, cudaMemcpyHostToDevice));
-    e->n_big = n;
-    e->big_valid = true;
-    return list;
+    cudaFree(deg);
+    cudaFree(deg_sorted);
+    cudaFree(ids);
+    cudaFree(bounds);
+    e->n_hub = h[0];
+    e->n_mid = h[1];
+    e->n_nz = h[2];
+    e->order_valid = true;
+    return order;
 }
 
 void graph_check_sorted(kk_engine *e)

@@ -52,10 +52,11 @@ WORKLOADS = {
 }
 
 # Bytes touched per walker-step by the walk kernel, at 32 B sector granularity:
-# int64 offset pair 16 B spans 1.25 sectors on average (40 B); a 16 B-aligned
-# alias bucket is one sector (32 B); the chosen neighbour id one sector (32 B);
-# the 4 B path write is coalesced by L2 into full sectors (4 B).
-B_STEP = {"deepwalk": 40 + 32 + 32 + 4, "ppr": 40 + 32 + 4}
+# int64 offset pair 16 B spans 1.25 sectors on average (40 B); a 32 B alias
+# bucket (which carries the candidate's neighbour) is one sector (32 B); an
+# unweighted pick reads one neighbour id (one sector, 32 B); the 4 B path
+# write is merged by L2 into full sectors (4 B).
+B_STEP = {"deepwalk": 40 + 32 + 4, "ppr": 40 + 32 + 4}
 
 
 def load_peaks():

@@ -147,17 +147,17 @@ __device__ __forceinline__ AliasBucket make_bucket(float p, uint32_t pi, uint32_
  * sequential algorithm's, bucket for bucket and bit for bit; only the serial
  * sum stays sequential (one FADD chain per vertex).
  *
- * Vertices run in three tiers over a degree-descending vertex order:
- *   hubs   (deg > kAliasMidMax): a 1024-thread block per vertex, queues in
- *          the 16 B/edge scratch at 2*off[v];
- *   middle (kAliasSmallMax < deg <= kAliasMidMax): a 256-thread block per
- *          vertex, queues and staged weights in shared memory;
- *   small  (deg <= kAliasSmallMax): a warp per vertex, all in shared memory.
- * Block kernels hand batches of 32 or fewer to one warp (no block barrier). */
+ * Vertices run over a degree-descending vertex order:
+ *   hubs (deg >= kAliasHubMin): a 1024-thread block per vertex does sum,
+ *        split and pairing, queues in the 16 B/edge scratch at 2*off[v];
+ *        batches of 64 or fewer go to one warp (no block barrier);
+ *   the rest: one thread per vertex computes the serial sums (balanced warps),
+ *        then a warp per vertex splits and pairs, queues in shared memory up
+ *        to kAliasWarpQueue entries, else in the scratch. */
 
-constexpr uint32_t kAliasSmallMax = 32;
-constexpr uint32_t kAliasMidMax = 4096;
-constexpr size_t kAliasMidSmem = (size_t)kAliasMidMax * (2 * sizeof(uint2) + sizeof(float));
+constexpr uint32_t kAliasHubMin = 4097;   /* degree from which a vertex is a hub */
+constexpr uint32_t kAliasWarpQueue = 512; /* shared-memory queue entries per warp */
+constexpr size_t kAliasPairSmem = (size_t)8 * 2 * kAliasWarpQueue * sizeof(uint2); /* 8 warps per block */
 constexpr unsigned kFullMask = 0xffffffffu;
 
 __device__ __forceinline__ uint32_t lanemask_lt()
@@ -365,87 +365,84 @@ __device__ __forceinline__ void block_split(Load load, uint32_t deg, float ave, 
     }
 }
 
-/* Small tier: a warp per vertex of degree <= 32, everything on chip. */
+/* Serial sums (:579-584) and averages (:589) of the non-hub vertices: one
+ * thread per vertex over the degree-sorted order, so a warp's vertices have
+ * similar degrees.  Loads are issued four at a time; the additions stay in
+ * CSR order. */
 template <typename TC>
-__global__ void __launch_bounds__(256) alias_build_small_kernel(GraphView g, TC tc, AliasBucket *out, float *sum_out,
-                                                                const uint32_t *order, uint32_t lo, uint32_t hi)
+__global__ void __launch_bounds__(256) alias_sum_kernel(GraphView g, TC tc, float *sum_out, float *ave_out,
+                                                        const uint32_t *order, uint32_t lo, uint32_t hi)
 {
-    __shared__ uint2 sq[8][2 * kAliasSmallMax];
+    for (uint32_t k = lo + blockIdx.x * blockDim.x + threadIdx.x; k < hi; k += gridDim.x * blockDim.x)
+    {
+        const uint32_t v = order[k];
+        const int64_t e0 = g.off[v];
+        const uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
+        float sum = 0.0f;
+        uint32_t j = 0;
+        for (; j + 4 <= deg; j += 4)
+        {
+            const float a = static_at(g, tc, v, e0 + j), b = static_at(g, tc, v, e0 + j + 1);
+            const float c = static_at(g, tc, v, e0 + j + 2), d = static_at(g, tc, v, e0 + j + 3);
+            sum = fadd(fadd(fadd(fadd(sum, a), b), c), d);
+        }
+        for (; j < deg; j++)
+            sum = fadd(sum, static_at(g, tc, v, e0 + j));
+        if (sum_out != nullptr)
+            sum_out[v] = sum;
+        ave_out[v] = fdiv(sum, u2f(deg));
+    }
+}
+
+/* Split (:594-603) and batched FIFO pairing (:605-638) of the non-hub
+ * vertices: a warp per vertex, queues in shared memory up to kAliasWarpQueue
+ * entries each, else in the global scratch at 2*off[v]. */
+template <typename TC>
+__global__ void __launch_bounds__(256) alias_pair_kernel(GraphView g, TC tc, AliasBucket *out, const float *ave_in,
+                                                         uint2 *scratch, const uint32_t *order, uint32_t lo,
+                                                         uint32_t hi)
+{
+    extern __shared__ uint2 dyn[];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t lt = lanemask_lt();
     const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+    uint2 *sP = dyn + (size_t)wib * 2 * kAliasWarpQueue;
+    uint2 *sQ = sP + kAliasWarpQueue;
     for (uint32_t k = lo + blockIdx.x * (blockDim.x >> 5) + wib; k < hi; k += nwarps)
     {
         const uint32_t v = order[k];
         const int64_t e0 = g.off[v];
         const uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
-        const float x = lane < deg ? static_at(g, tc, v, e0 + lane) : 0.0f;
-        /* sequential sum in CSR order (:579-584), carried by every lane */
-        float sum = 0.0f;
-#pragma unroll
-        for (uint32_t j = 0; j < kAliasSmallMax; j++)
+        const float ave = ave_in[v];
+        uint2 *P = sP, *Q = sQ;
+        if (deg > kAliasWarpQueue)
         {
-            const float y = __shfl_sync(kFullMask, x, j);
-            if (j < deg)
-                sum = fadd(sum, y);
+            P = scratch + 2 * e0;
+            Q = P + deg;
         }
-        if (lane == 0 && sum_out != nullptr)
-            sum_out[v] = sum;
-        const float ave = fdiv(sum, u2f(deg)); /* :589 */
-        uint2 *P = sq[wib], *Q = sq[wib] + kAliasSmallMax;
-        const bool sm = lane < deg && x < ave, bg = lane < deg && !(x < ave);
-        const uint32_t mp = __ballot_sync(kFullMask, sm), mq = __ballot_sync(kFullMask, bg);
-        const uint2 ent = make_uint2(lane, __float_as_uint(x));
-        if (sm)
-            P[__popc(mp & lt)] = ent;
-        if (bg)
-            Q[__popc(mq & lt)] = ent;
+        uint32_t pt = 0, qt = 0;
+        for (uint32_t base = 0; base < deg; base += 32)
+        {
+            const bool valid = base + lane < deg;
+            const float x = valid ? static_at(g, tc, v, e0 + base + lane) : 0.0f;
+            const bool sm = valid && x < ave, bg = valid && !(x < ave);
+            const uint32_t mp = __ballot_sync(kFullMask, sm), mq = __ballot_sync(kFullMask, bg);
+            const uint2 ent = make_uint2(base + lane, __float_as_uint(x));
+            if (sm)
+                P[pt + __popc(mp & lt)] = ent;
+            if (bg)
+                Q[qt + __popc(mq & lt)] = ent;
+            pt += __popc(mp);
+            qt += __popc(mq);
+        }
         __syncwarp();
-        uint32_t ph = 0, pt = __popc(mp), qh = 0, qt = __popc(mq);
+        uint32_t ph = 0, qh = 0;
         AliasBucket *ob = out + e0;
         const uint32_t *nb = g.nbr + e0;
         warp_pairing(P, Q, ph, pt, qh, qt, ave, ob, nb, 0xffffffffu);
         for (uint32_t i = lane; i < qt - qh; i += 32)
             ob[pt + i] = make_bucket(1.0f, Q[qh + i].x, kNone, nb);
         __syncwarp();
-    }
-}
-
-/* Middle tier: a 256-thread block per vertex, queues and weights in shared memory. */
-template <typename TC>
-__global__ void __launch_bounds__(256) alias_build_mid_kernel(GraphView g, TC tc, AliasBucket *out, float *sum_out,
-                                                              const uint32_t *order, uint32_t lo, uint32_t hi)
-{
-    extern __shared__ uint2 dyn[];
-    uint2 *P = dyn;
-    uint2 *Q = dyn + kAliasMidMax;
-    float *stage = (float *)(dyn + 2 * kAliasMidMax);
-    __shared__ uint32_t sa[33], sb[33], s_state[4];
-    __shared__ float s_ave;
-    const uint32_t tid = threadIdx.x, nt = blockDim.x;
-    for (uint32_t k = lo + blockIdx.x; k < hi; k += gridDim.x)
-    {
-        const uint32_t v = order[k];
-        const int64_t e0 = g.off[v];
-        const uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
-        for (uint32_t i = tid; i < deg; i += nt)
-            stage[i] = static_at(g, tc, v, e0 + i);
-        __syncthreads();
-        if (tid == 0)
-        {
-            float sum = 0.0f;
-#pragma unroll 8
-            for (uint32_t j = 0; j < deg; j++)
-                sum = fadd(sum, stage[j]);
-            s_ave = fdiv(sum, u2f(deg));
-            if (sum_out != nullptr)
-                sum_out[v] = sum;
-        }
-        __syncthreads();
-        const float ave = s_ave;
-        uint32_t pt, qt;
-        block_split([&](uint32_t i) { return stage[i]; }, deg, ave, P, Q, pt, qt, sa, sb);
-        block_pairing(P, Q, pt, qt, ave, out + e0, g.nbr + e0, sa, sb, s_state);
     }
 }
 

@@ -291,7 +291,7 @@ void kk_engine_destroy(kk_engine *e)
     if (e->stream)
         cudaStreamSynchronize(e->stream);
     e->free_graph();
-    kk::DevBuf *bufs[] = {&e->alias, &e->sum,   &e->ra,    &e->scratch, &e->vmask,  &e->path,      &e->length,
+    kk::DevBuf *bufs[] = {&e->alias, &e->sum, &e->ave, &e->ra, &e->scratch, &e->vmask,  &e->path,      &e->length,
                           &e->path_off, &e->caps, &e->start, &e->small, &e->cub_tmp, &e->packed, &e->packed_off};
     for (kk::DevBuf *b : bufs)
         b->release();

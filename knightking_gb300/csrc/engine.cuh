@@ -118,7 +118,7 @@ struct kk_engine
     int sorted = -1; /* -1 unknown, 0 no, 1 adjacency sorted by neighbour */
 
     /* work buffers */
-    kk::DevBuf alias, sum, ra, scratch, vmask, path, length, path_off, caps, start, small, cub_tmp, packed, packed_off;
+    kk::DevBuf alias, sum, ave, ra, scratch, vmask, path, length, path_off, caps, start, small, cub_tmp, packed, packed_off;
 
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     cudaStream_t side = nullptr; /* hub alias builds run here, joined by events */
@@ -172,10 +172,10 @@ void build_alias(kk_engine *e, const TC &tc)
     float *sum = e->sum.as<float>(e->V);
     const uint32_t *order = vertex_order(e);
     const unsigned sms = (unsigned)e->sm_count;
+    uint2 *scratch = e->scratch.as<uint2>(2 * e->E);
     if (e->n_hub)
     {
         /* hubs first, largest first, on the side stream so they start at once */
-        uint2 *scratch = e->scratch.as<uint2>(2 * e->E);
         KK_CUDA_CHECK(cudaEventRecord(e->ev_fork, e->stream));
         KK_CUDA_CHECK(cudaStreamWaitEvent(e->side, e->ev_fork, 0));
         unsigned grid = e->n_hub < sms ? e->n_hub : sms;
@@ -183,26 +183,22 @@ void build_alias(kk_engine *e, const TC &tc)
         KK_CUDA_CHECK(cudaGetLastError());
         KK_CUDA_CHECK(cudaEventRecord(e->ev_join, e->side));
     }
-    if (e->n_mid > e->n_hub)
+    if (e->n_nz > e->n_hub)
     {
         static bool smem_set = false;
         if (!smem_set)
         {
-            KK_CUDA_CHECK(cudaFuncSetAttribute(alias_build_mid_kernel<TC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)kAliasMidSmem));
+            KK_CUDA_CHECK(cudaFuncSetAttribute(alias_pair_kernel<TC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)kAliasPairSmem));
             smem_set = true;
         }
-        uint32_t n = e->n_mid - e->n_hub;
-        unsigned grid = n < 2 * sms ? n : 2 * sms;
-        alias_build_mid_kernel<TC><<<grid, 256, kAliasMidSmem, e->stream>>>(g, tc, alias, sum, order, e->n_hub,
-                                                                           e->n_mid);
+        const uint32_t n = e->n_nz - e->n_hub;
+        float *ave = e->ave.as<float>(e->V);
+        alias_sum_kernel<TC><<<grid_for(e, n, 256), 256, 0, e->stream>>>(g, tc, sum, ave, order, e->n_hub, e->n_nz);
         KK_CUDA_CHECK(cudaGetLastError());
-    }
-    if (e->n_nz > e->n_mid)
-    {
-        uint32_t warps = e->n_nz - e->n_mid;
-        unsigned grid = (warps + 7) / 8 < 8 * sms ? (warps + 7) / 8 : 8 * sms;
-        alias_build_small_kernel<TC><<<grid, 256, 0, e->stream>>>(g, tc, alias, sum, order, e->n_mid, e->n_nz);
+        unsigned grid = (n + 7) / 8 < 3 * sms ? (n + 7) / 8 : 3 * sms;
+        alias_pair_kernel<TC><<<grid, 256, kAliasPairSmem, e->stream>>>(g, tc, alias, ave, scratch, order, e->n_hub,
+                                                                        e->n_nz);
         KK_CUDA_CHECK(cudaGetLastError());
     }
     if (e->n_hub)

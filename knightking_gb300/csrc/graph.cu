@@ -170,7 +170,7 @@ const uint32_t *vertex_order(kk_engine *e)
     KK_CUDA_CHECK(cub::DeviceRadixSort::SortPairsDescending(e->cub_tmp.ensure(bytes), bytes, deg, deg_sorted, ids,
                                                             order, (int64_t)V, 0, 32, e->stream));
     KK_CUDA_CHECK(cudaMemsetAsync(bounds, 0, 16, e->stream));
-    tier_bounds_kernel<<<grid_for(e, V, 256), 256, 0, e->stream>>>(deg_sorted, V, kAliasMidMax, kAliasSmallMax, bounds);
+    tier_bounds_kernel<<<grid_for(e, V, 256), 256, 0, e->stream>>>(deg_sorted, V, kAliasHubMin - 1, 0, bounds);
     KK_CUDA_CHECK(cudaGetLastError());
     uint32_t h[3];
     KK_CUDA_CHECK(cudaMemcpyAsync(h, bounds, 12, cudaMemcpyDeviceToHost, e->stream));

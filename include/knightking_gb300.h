@@ -137,6 +137,23 @@ kk_status kk_graph_sort_adjacency(kk_engine *e);
  * the sequential float sum of v's weights.  Outputs are host arrays. */
 kk_status kk_alias_build(kk_engine *e, float *p, uint32_t *p_idx, uint32_t *q_idx, float *sum);
 
+/* Alias tables built with no device allocation.  This entry point has no
+ * counterpart in the reference.  It is for callers that cannot call
+ * cudaMalloc (for example a serving process whose device memory belongs to
+ * its own pool, or a latency-critical path where allocation and the device
+ * synchronisation of cudaFree are not allowed).  The caller passes its own
+ * device arrays: off[v_num+1] and w[E] in, p/p_idx/q_idx[E] and sum[v_num]
+ * (sum may be NULL) out, in the layout of kk_alias_build, with the same
+ * values bit for bit.  Its queue scratch is a fixed 32 MiB device array inside
+ * the library that every GPU which loads the library keeps until the process
+ * exits; a vertex degree above 16384 is rejected with KK_ERR_INVALID_CONFIG.
+ * The first call on a device looks up that array's address (make it before
+ * any stream capture); the work is queued on `stream` (a cudaStream_t, NULL =
+ * default stream) after a short degree check that synchronises the stream.
+ * Calls share the scratch: calls that overlap on the GPU race. */
+kk_status kk_alias_build_noalloc(uint32_t v_num, const int64_t *d_off, const float *d_w, float *d_p,
+                                 uint32_t *d_p_idx, uint32_t *d_q_idx, float *d_sum, void *stream);
+
 /* ---- walks (WalkEngine::random_walk, include/walk.hpp:423-436) ---------- */
 
 /* Runs one walk job and returns its paths in host memory (free with

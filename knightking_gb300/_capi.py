@@ -85,6 +85,7 @@ _SIGS = {
     "kk_graph_download": (ctypes.c_int, [_P, _P, _P, _P, _P]),
     "kk_graph_sort_adjacency": (ctypes.c_int, [_P]),
     "kk_alias_build": (ctypes.c_int, [_P, _P, _P, _P, _P]),
+    "kk_alias_build_noalloc": (ctypes.c_int, [ctypes.c_uint32, _P, _P, _P, _P, _P, _P, _P]),
     "kk_walk": (ctypes.c_int, [_P, _P, _P]),
     "kk_walk_deepwalk": (ctypes.c_int, [_P, _P, _P]),
     "kk_walk_ppr": (ctypes.c_int, [_P, _P, _P]),

@@ -244,6 +244,16 @@ def run_ours(args, wl, world, rank, local):
         steps, _, _, _ = engine.walk_device(app, walkers, paths=False, seed=1, walker_begin=walker_begin, **kw)
         return steps
 
+    # warm-up; it also picks the walk schedule (one walker per thread vs the
+    # persistent walker pool) by the walk kernel's event time
+    schedule_ms = {}
+    for sched in (0, 1):
+        engine.set_option("walk_schedule", sched)
+        step()
+        step()
+        schedule_ms[sched] = engine.last_timing()[1]
+    best_schedule = min(schedule_ms, key=schedule_ms.get)
+    engine.set_option("walk_schedule", best_schedule)
     for _ in range(args.warmup):
         step()
     barrier(world)
@@ -310,7 +320,8 @@ def run_ours(args, wl, world, rank, local):
                 traffic = json.load(f)["dram_bytes_per_step"] * steps_per_launch
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_kind": peak_kind, "bytes_per_step": b_step,
-                "kernel": "walk_first_order_kernel" if app != "node2vec" else "walk_second_order_kernel",
+                "kernel": ("walk_pool_kernel" if best_schedule == 1 else "walk_static_kernel") +
+                          (" (second order)" if app == "node2vec" else " (first order)"),
                 "kernel_ms": mean_walk_ms, "alias_build_ms": statistics.mean(alias_ms)}
 
     cpu = None
@@ -326,7 +337,9 @@ def run_ours(args, wl, world, rank, local):
             "data": "synthetic (seeded R-MAT generated on the GPU)",
             "config": {"workload": args.workload, "desc": wl["desc"], "vertices": V, "edges": E,
                        "walkers_per_gpu": walkers, "walker_steps_per_step": steps_per_launch,
-                       "l2": "inputs larger than L2 (graph + alias tables > 129 MB)", "parallelism": "replicas"},
+                       "l2": "inputs larger than L2 (graph + alias tables > 129 MB)", "parallelism": "replicas",
+                       "walk_schedule": "pool" if best_schedule == 1 else "one walker per thread",
+                       "walk_ms_by_schedule": {"per_thread": schedule_ms[0], "pool": schedule_ms[1]}},
             "e2e": {"value": e2e_value, "unit": "walker-steps/s", "h2d_bytes_per_step": walkers * 4 + 256,
                     "d2h_bytes_per_step": d2h // e2e_runs},
             "gpu_launches": 2 * args.steps if wl["weights"] else args.steps,

@@ -613,123 +613,234 @@ __device__ __forceinline__ void flush_steps(unsigned long long *total, unsigned 
         atomicAdd(total, mine);
 }
 
-/* First-order walk (include/walk.hpp:946-1067): one thread per walker, the
- * walker's state in registers for its whole walk. */
+/* Starts walker i of the launch: id, value-initialised state, start vertex,
+ * init state, path slot with the start vertex (include/walk.hpp:440-497). */
+template <typename S, typename WC>
+__device__ __forceinline__ void walk_begin(const GraphView &g, const WC &wc, const WalkLaunch &L, uint32_t i,
+                                           Walker<S> &w, vertex_id_t &v, Sampler &rng, uint32_t *&out, uint32_t &cap,
+                                           uint32_t &len)
+{
+    w.id = L.walker_begin + i;
+    w.step = 0;
+    w.data = S{};
+    v = walker_start<S>(g, wc, L, w, rng);
+    const uint64_t pbase = L.path_off ? L.path_off[i] : (uint64_t)i * L.cap;
+    cap = L.path_off ? (uint32_t)(L.path_off[i + 1] - pbase) : L.cap;
+    out = L.path ? L.path + pbase : nullptr;
+    if (out)
+        out[0] = v;
+    len = 1;
+}
+
+/* One step of one walker; false when its walk ends.
+ *
+ * First order (include/walk.hpp:954-1063): degree 0 ends the walk; the
+ * extension test (its draw only when 0 < ext < 1); rejection trials: [outlier
+ * appendix: r = gen_float(area * num + regular_area) - regular_area, r > 0
+ * picks an outlier], candidate by uniform or alias pick, dart = gen_float(ub)
+ * accepted under the lower bound or the dynamic component.
+ *
+ * Second order (include/walk.hpp:1082-1381): the reference's three supersteps
+ * per trial (candidate + query, response, accept) run inline; each pass of the
+ * trial loop re-evaluates the extension (and its draw) as the reference does
+ * at the start of every superstep (:1167-1172); a lower-bound pre-accept takes
+ * the step at once (:1226-1257); an outlier search that returns no edge retries
+ * without a new extension test (:1176-1258).
+ *
+ * Then step++, walker_update_state, the path write (include/walk.hpp:1043-1052). */
 template <typename S, typename WC, typename TC>
-__global__ void __launch_bounds__(256) walk_first_order_kernel(GraphView g, WC wc, TC tc, const AliasBucket *alias,
-                                                               const float *ra, WalkLaunch L)
+__device__ __forceinline__ bool walk_step(const GraphView &g, const WC &wc, const TC &tc, const AliasBucket *alias,
+                                          const float *ra, const WalkLaunch &L, Walker<S> &w, vertex_id_t &v,
+                                          Sampler &rng, uint32_t *out, uint32_t cap, uint32_t &len)
+{
+    const int64_t e0 = g.off[v];
+    const uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
+    if (deg == 0)
+        return false;
+    rng.enter(w.id, w.step, 0);
+    const AdjList adj{(edge_id_t)e0, (edge_id_t)(e0 + deg)};
+    uint32_t ac = kNone;
+    vertex_id_t nv = 0;
+    uint32_t trials = 0;
+    if constexpr (TC::order == 1)
+    {
+        const real_t ext = tc.extension_comp(w, v);
+        if (ext == 0.0f || (ext < 1.0f && rng.gen_float(1.0f) > ext))
+            return false;
+        while (ac == kNone)
+        {
+            if (++trials > L.trial_limit)
+            {
+                atomicExch(L.status, KK_STATUS_TRIAL_LIMIT);
+                return false;
+            }
+            if constexpr (TC::has_outlier)
+            {
+                real_t ob = 0.0f;
+                vertex_id_t on = 0;
+                tc.outlier_upperbound(w, v, adj, ob, on);
+                if (ob > 0.0f && on > 0)
+                {
+                    const float rav = ra[v];
+                    const float r = fsub(rng.gen_float(fadd(fmul(ob, u2f(on)), rav)), rav);
+                    if (r > 0.0f)
+                    {
+                        uint32_t oi = (uint32_t)fdiv(r, ob);
+                        if (oi + 1 > on)
+                            oi = on - 1;
+                        AdjUnit cu;
+                        if (tc.outlier_search(w, v, adj, oi, cu))
+                        {
+                            float sc = 1.0f;
+                            if constexpr (TC::has_static)
+                                sc = tc.static_comp(v, cu);
+                            const float r2 = fadd(fdiv(fsub(r, fmul(u2f(oi), ob)), sc), tc.dcomp_upperbound(v, adj));
+                            if (r2 <= tc.dynamic_comp(w, v, cu))
+                            {
+                                ac = (uint32_t)(cu.index - (edge_id_t)e0);
+                                nv = cu.neighbour;
+                            }
+                        }
+                        continue;
+                    }
+                }
+            }
+            const uint2 pc = pick_candidate<TC>(g, alias, e0, deg, rng);
+            if constexpr (TC::has_dynamic)
+            {
+                const float dart = rng.gen_float(tc.dcomp_upperbound(v, adj));
+                bool acc = false;
+                if constexpr (TC::has_lowerbound)
+                    acc = dart <= tc.dcomp_lowerbound(v, adj);
+                if (!acc)
+                    acc = dart <= tc.dynamic_comp(w, v, AdjUnit{pc.y, (edge_id_t)(e0 + pc.x)});
+                if (acc)
+                {
+                    ac = pc.x;
+                    nv = pc.y;
+                }
+            }
+            else
+            {
+                ac = pc.x;
+                nv = pc.y;
+            }
+        }
+    }
+    else
+    {
+        typedef typename TC::query_type Q;
+        typedef typename TC::response_type R;
+        for (;;)
+        {
+            const real_t ext = tc.extension_comp(w, v);
+            if (ext == 0.0f || (ext < 1.0f && rng.gen_float(1.0f) > ext))
+                return false;
+            AdjUnit cu{0, 0};
+            float randval = 0.0f;
+            bool accepted = false;
+            for (;;)
+            {
+                if (++trials > L.trial_limit)
+                {
+                    atomicExch(L.status, KK_STATUS_TRIAL_LIMIT);
+                    return false;
+                }
+                bool in_app = false;
+                if constexpr (TC::has_outlier)
+                {
+                    real_t ob = 0.0f;
+                    vertex_id_t on = 0;
+                    tc.outlier_upperbound(w, v, adj, ob, on);
+                    if (ob > 0.0f && on > 0)
+                    {
+                        const float rav = ra[v];
+                        const float r = fsub(rng.gen_float(fadd(fmul(ob, u2f(on)), rav)), rav);
+                        if (r > 0.0f)
+                        {
+                            in_app = true;
+                            uint32_t oi = (uint32_t)fdiv(r, ob);
+                            if (oi + 1 > on)
+                                oi = on - 1;
+                            if (tc.outlier_search(w, v, adj, oi, cu))
+                            {
+                                float sc = 1.0f;
+                                if constexpr (TC::has_static)
+                                    sc = tc.static_comp(v, cu);
+                                randval = fadd(fdiv(fsub(r, fmul(u2f(oi), ob)), sc), tc.dcomp_upperbound(v, adj));
+                                break;
+                            }
+                        }
+                    }
+                }
+                if (!in_app)
+                {
+                    const uint2 pc = pick_candidate<TC>(g, alias, e0, deg, rng);
+                    cu = AdjUnit{pc.y, (edge_id_t)(e0 + pc.x)};
+                    randval = rng.gen_float(tc.dcomp_upperbound(v, adj));
+                    if constexpr (TC::has_lowerbound)
+                        accepted = randval <= tc.dcomp_lowerbound(v, adj);
+                    break;
+                }
+            }
+            if (!accepted)
+            {
+                R resp{};
+                Q query{};
+                vertex_id_t target = 0;
+                if (tc.post_query(w, v, cu, target, query))
+                {
+                    const AdjList tadj{(edge_id_t)g.off[target], (edge_id_t)g.off[target + 1]};
+                    tc.respond_query(target, query, tadj, resp);
+                }
+                accepted = randval <= tc.dynamic_comp(w, resp, v, cu);
+            }
+            if (accepted)
+            {
+                ac = (uint32_t)(cu.index - (edge_id_t)e0);
+                nv = cu.neighbour;
+                break;
+            }
+        }
+    }
+    w.step++;
+    if constexpr (is_hook<decltype(wc.walker_update_state)>())
+        wc.walker_update_state(w, v, AdjUnit{nv, (edge_id_t)(e0 + ac)});
+    if (out)
+    {
+        if (len >= cap)
+        {
+            atomicExch(L.status, KK_STATUS_PATH_CAPACITY);
+            return false;
+        }
+        out[len] = nv;
+    }
+    len++;
+    v = nv;
+    return true;
+}
+
+/* One thread per walker for its whole walk, walker state in registers. */
+template <typename S, typename WC, typename TC>
+__global__ void __launch_bounds__(256) walk_static_kernel(GraphView g, WC wc, TC tc, const AliasBucket *alias,
+                                                          const float *ra, WalkLaunch L)
 {
     unsigned long long my_steps = 0;
-    uint32_t n_iter = (L.walker_num + gridDim.x * blockDim.x - 1) / (gridDim.x * blockDim.x);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t n_iter = (L.walker_num + stride - 1) / stride;
     for (uint32_t it = 0; it < n_iter; it++)
     {
-        uint32_t i = (it * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
+        const uint32_t i = (it * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
         if (i < L.walker_num)
         {
             Sampler rng;
             rng.init(L.seed);
             Walker<S> w;
-            w.id = L.walker_begin + i;
-            w.step = 0;
-            w.data = S{};
-            vertex_id_t v = walker_start<S>(g, wc, L, w, rng);
-            uint64_t pbase = L.path_off ? L.path_off[i] : (uint64_t)i * L.cap;
-            uint32_t cap = L.path_off ? (uint32_t)(L.path_off[i + 1] - pbase) : L.cap;
-            uint32_t *out = L.path ? L.path + pbase : nullptr;
-            if (out)
-                out[0] = v;
-            uint32_t len = 1;
-            for (;;)
+            vertex_id_t v;
+            uint32_t *out, cap, len;
+            walk_begin<S>(g, wc, L, i, w, v, rng, out, cap, len);
+            while (walk_step<S>(g, wc, tc, alias, ra, L, w, v, rng, out, cap, len))
             {
-                int64_t e0 = g.off[v];
-                uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
-                if (deg == 0)
-                    break;
-                rng.enter(w.id, w.step, 0);
-                real_t ext = tc.extension_comp(w, v);
-                if (ext == 0.0f || (ext < 1.0f && rng.gen_float(1.0f) > ext))
-                    break;
-                AdjList adj{(edge_id_t)e0, (edge_id_t)(e0 + deg)};
-                uint32_t ac = kNone;
-                vertex_id_t nv = 0;
-                uint32_t trials = 0;
-                while (ac == kNone)
-                {
-                    if (++trials > L.trial_limit)
-                    {
-                        atomicExch(L.status, KK_STATUS_TRIAL_LIMIT);
-                        break;
-                    }
-                    if constexpr (TC::has_outlier)
-                    {
-                        real_t ob = 0.0f;
-                        vertex_id_t on = 0;
-                        tc.outlier_upperbound(w, v, adj, ob, on);
-                        if (ob > 0.0f && on > 0)
-                        {
-                            float rav = ra[v];
-                            float r = fsub(rng.gen_float(fadd(fmul(ob, u2f(on)), rav)), rav);
-                            if (r > 0.0f)
-                            {
-                                uint32_t oi = (uint32_t)fdiv(r, ob);
-                                if (oi + 1 > on)
-                                    oi = on - 1;
-                                AdjUnit cu;
-                                if (tc.outlier_search(w, v, adj, oi, cu))
-                                {
-                                    float sc = 1.0f;
-                                    if constexpr (TC::has_static)
-                                        sc = tc.static_comp(v, cu);
-                                    float r2 = fadd(fdiv(fsub(r, fmul(u2f(oi), ob)), sc), tc.dcomp_upperbound(v, adj));
-                                    if (r2 <= tc.dynamic_comp(w, v, cu))
-                                    {
-                                        ac = (uint32_t)(cu.index - (edge_id_t)e0);
-                                        nv = cu.neighbour;
-                                    }
-                                }
-                                continue;
-                            }
-                        }
-                    }
-                    const uint2 pc = pick_candidate<TC>(g, alias, e0, deg, rng);
-                    const uint32_t cand = pc.x;
-                    const vertex_id_t cn = pc.y;
-                    if constexpr (TC::has_dynamic)
-                    {
-                        float dart = rng.gen_float(tc.dcomp_upperbound(v, adj));
-                        bool acc = false;
-                        if constexpr (TC::has_lowerbound)
-                            acc = dart <= tc.dcomp_lowerbound(v, adj);
-                        if (!acc)
-                            acc = dart <= tc.dynamic_comp(w, v, AdjUnit{cn, (edge_id_t)(e0 + cand)});
-                        if (acc)
-                        {
-                            ac = cand;
-                            nv = cn;
-                        }
-                    }
-                    else
-                    {
-                        ac = cand;
-                        nv = cn;
-                    }
-                }
-                if (ac == kNone)
-                    break; /* trial limit */
-                w.step++;
-                if constexpr (is_hook<decltype(wc.walker_update_state)>())
-                    wc.walker_update_state(w, v, AdjUnit{nv, (edge_id_t)(e0 + ac)});
-                if (out)
-                {
-                    if (len >= cap)
-                    {
-                        atomicExch(L.status, KK_STATUS_PATH_CAPACITY);
-                        break;
-                    }
-                    out[len] = nv;
-                }
-                len++;
-                v = nv;
             }
             L.length[i] = len;
             my_steps += len - 1;
@@ -738,147 +849,43 @@ __global__ void __launch_bounds__(256) walk_first_order_kernel(GraphView g, WC w
     flush_steps(L.total_steps, my_steps);
 }
 
-/* Second-order walk (include/walk.hpp:1082-1381).  The reference's three
- * supersteps per trial (candidate + query, response, accept) run inline per
- * walker: each pass of the trial loop re-evaluates the extension (and its draw)
- * as the reference does at the start of every superstep (:1167-1172); a
- * lower-bound pre-accept takes the step at once (:1226-1257); an outlier
- * search that returns no edge retries without a new extension test
- * (:1176-1258). */
+/* Device-resident walker pool: persistent blocks, each owning a contiguous
+ * range of walker ids handed out by a shared-memory counter.  Every loop
+ * iteration advances each lane's walker by one step; a lane whose walk ends
+ * writes its length and takes the next walker at once, so lanes do not idle
+ * on finished walks until the block's range runs dry.  Results are those of
+ * walk_static_kernel: every walker's draws depend only on its id. */
 template <typename S, typename WC, typename TC>
-__global__ void __launch_bounds__(256) walk_second_order_kernel(GraphView g, WC wc, TC tc, const AliasBucket *alias,
-                                                                const float *ra, WalkLaunch L)
+__global__ void __launch_bounds__(256) walk_pool_kernel(GraphView g, WC wc, TC tc, const AliasBucket *alias,
+                                                        const float *ra, WalkLaunch L)
 {
-    typedef typename TC::query_type Q;
-    typedef typename TC::response_type R;
+    __shared__ uint32_t s_next;
+    const uint32_t per = (uint32_t)(((uint64_t)L.walker_num + gridDim.x - 1) / gridDim.x);
+    const uint32_t lo = (uint32_t)min((uint64_t)blockIdx.x * per, (uint64_t)L.walker_num);
+    const uint32_t hi = (uint32_t)min((uint64_t)lo + per, (uint64_t)L.walker_num);
+    if (threadIdx.x == 0)
+        s_next = lo;
+    __syncthreads();
     unsigned long long my_steps = 0;
-    uint32_t n_iter = (L.walker_num + gridDim.x * blockDim.x - 1) / (gridDim.x * blockDim.x);
-    for (uint32_t it = 0; it < n_iter; it++)
+    Sampler rng;
+    rng.init(L.seed);
+    Walker<S> w;
+    vertex_id_t v = 0;
+    uint32_t *out = nullptr, cap = 0, len = 0;
+    uint32_t i = atomicAdd(&s_next, 1u);
+    bool have = i < hi;
+    if (have)
+        walk_begin<S>(g, wc, L, i, w, v, rng, out, cap, len);
+    while (__any_sync(kFullMask, have))
     {
-        uint32_t i = (it * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
-        if (i < L.walker_num)
+        if (have && !walk_step<S>(g, wc, tc, alias, ra, L, w, v, rng, out, cap, len))
         {
-            Sampler rng;
-            rng.init(L.seed);
-            Walker<S> w;
-            w.id = L.walker_begin + i;
-            w.step = 0;
-            w.data = S{};
-            vertex_id_t v = walker_start<S>(g, wc, L, w, rng);
-            uint64_t pbase = L.path_off ? L.path_off[i] : (uint64_t)i * L.cap;
-            uint32_t cap = L.path_off ? (uint32_t)(L.path_off[i + 1] - pbase) : L.cap;
-            uint32_t *out = L.path ? L.path + pbase : nullptr;
-            if (out)
-                out[0] = v;
-            uint32_t len = 1;
-            for (;;)
-            {
-                int64_t e0 = g.off[v];
-                uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
-                if (deg == 0)
-                    break;
-                rng.enter(w.id, w.step, 0);
-                AdjList adj{(edge_id_t)e0, (edge_id_t)(e0 + deg)};
-                uint32_t ac = kNone;
-                vertex_id_t nv = 0;
-                bool stop = false;
-                uint32_t trials = 0;
-                for (;;)
-                {
-                    real_t ext = tc.extension_comp(w, v);
-                    if (ext == 0.0f || (ext < 1.0f && rng.gen_float(1.0f) > ext))
-                    {
-                        stop = true;
-                        break;
-                    }
-                    AdjUnit cu{0, 0};
-                    float randval = 0.0f;
-                    bool accepted = false;
-                    for (;;)
-                    {
-                        if (++trials > L.trial_limit)
-                        {
-                            atomicExch(L.status, KK_STATUS_TRIAL_LIMIT);
-                            stop = true;
-                            break;
-                        }
-                        bool in_app = false;
-                        if constexpr (TC::has_outlier)
-                        {
-                            real_t ob = 0.0f;
-                            vertex_id_t on = 0;
-                            tc.outlier_upperbound(w, v, adj, ob, on);
-                            if (ob > 0.0f && on > 0)
-                            {
-                                float rav = ra[v];
-                                float r = fsub(rng.gen_float(fadd(fmul(ob, u2f(on)), rav)), rav);
-                                if (r > 0.0f)
-                                {
-                                    in_app = true;
-                                    uint32_t oi = (uint32_t)fdiv(r, ob);
-                                    if (oi + 1 > on)
-                                        oi = on - 1;
-                                    if (tc.outlier_search(w, v, adj, oi, cu))
-                                    {
-                                        float sc = 1.0f;
-                                        if constexpr (TC::has_static)
-                                            sc = tc.static_comp(v, cu);
-                                        randval = fadd(fdiv(fsub(r, fmul(u2f(oi), ob)), sc), tc.dcomp_upperbound(v, adj));
-                                        break;
-                                    }
-                                }
-                            }
-                        }
-                        if (!in_app)
-                        {
-                            const uint2 pc = pick_candidate<TC>(g, alias, e0, deg, rng);
-                            cu = AdjUnit{pc.y, (edge_id_t)(e0 + pc.x)};
-                            randval = rng.gen_float(tc.dcomp_upperbound(v, adj));
-                            if constexpr (TC::has_lowerbound)
-                                accepted = randval <= tc.dcomp_lowerbound(v, adj);
-                            break;
-                        }
-                    }
-                    if (stop)
-                        break;
-                    if (!accepted)
-                    {
-                        R resp{};
-                        Q query{};
-                        vertex_id_t target = 0;
-                        if (tc.post_query(w, v, cu, target, query))
-                        {
-                            AdjList tadj{(edge_id_t)g.off[target], (edge_id_t)g.off[target + 1]};
-                            tc.respond_query(target, query, tadj, resp);
-                        }
-                        accepted = randval <= tc.dynamic_comp(w, resp, v, cu);
-                    }
-                    if (accepted)
-                    {
-                        ac = (uint32_t)(cu.index - (edge_id_t)e0);
-                        nv = cu.neighbour;
-                        break;
-                    }
-                }
-                if (stop)
-                    break;
-                w.step++;
-                if constexpr (is_hook<decltype(wc.walker_update_state)>())
-                    wc.walker_update_state(w, v, AdjUnit{nv, (edge_id_t)(e0 + ac)});
-                if (out)
-                {
-                    if (len >= cap)
-                    {
-                        atomicExch(L.status, KK_STATUS_PATH_CAPACITY);
-                        break;
-                    }
-                    out[len] = nv;
-                }
-                len++;
-                v = nv;
-            }
             L.length[i] = len;
             my_steps += len - 1;
+            i = atomicAdd(&s_next, 1u);
+            have = i < hi;
+            if (have)
+                walk_begin<S>(g, wc, L, i, w, v, rng, out, cap, len);
         }
     }
     flush_steps(L.total_steps, my_steps);

@@ -141,6 +141,10 @@ class WalkEngine:
         """Issue the engine's work on a CUDA stream given by address (0: own stream)."""
         self._check(self._lib.kk_engine_set_stream(self._h, ctypes.c_void_p(stream_ptr or None)))
 
+    def set_option(self, name, value):
+        """Tuning knob (see kk_engine_set_option): walk_schedule, walk_blocks_per_sm, trial_limit."""
+        self._check(self._lib.kk_engine_set_option(self._h, name.encode(), int(value)))
+
     def set_concurrency(self, worker_num):
         """The GPU needs no thread count; it sets the segment count used by dumps
         so the text matches the reference run with that many workers."""

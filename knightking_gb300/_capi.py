@@ -75,6 +75,7 @@ _SIGS = {
     "kk_engine_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]),
     "kk_engine_destroy": (None, [_P]),
     "kk_engine_set_stream": (ctypes.c_int, [_P, _P]),
+    "kk_engine_set_option": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_int64]),
     "kk_last_error": (ctypes.c_char_p, [_P]),
     "kk_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "kk_graph_load_binary": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]),

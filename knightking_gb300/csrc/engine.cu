@@ -132,6 +132,8 @@ void validate_opts(kk_engine *e, const kk_walk_opts *o)
         fail(KK_ERR_INVALID_CONFIG, "start list with n_start == 0");
     if ((uint64_t)o->walker_begin + o->walker_num > 0x100000000ULL)
         fail(KK_ERR_INVALID_CONFIG, "walker ids exceed 32 bits");
+    if (o->walker_num > 0x80000000u)
+        fail(KK_ERR_INVALID_CONFIG, "at most 2^31 walkers per call");
     if (o->walk_length >= 0xfffffff0u)
         fail(KK_ERR_INVALID_CONFIG, "walk_length too large");
 }
@@ -320,6 +322,23 @@ kk_status kk_engine_set_stream(kk_engine *e, void *stream)
     return guard(e, [&] {
         KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
         e->stream = stream ? (cudaStream_t)stream : e->own_stream;
+    });
+}
+
+kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value)
+{
+    if (!e || !name)
+        return KK_ERR_INVALID_CONFIG;
+    return guard(e, [&] {
+        std::string n(name);
+        if (n == "walk_schedule" && (value == 0 || value == 1))
+            e->walk_schedule = (int)value;
+        else if (n == "walk_blocks_per_sm" && value >= 0 && value <= 64)
+            e->walk_blocks_per_sm = (int)value;
+        else if (n == "trial_limit" && value >= 1 && value <= 0xffffffffLL)
+            e->trial_limit = (uint32_t)value;
+        else
+            fail(KK_ERR_INVALID_CONFIG, "unknown option or value out of range: " + n);
     });
 }
 

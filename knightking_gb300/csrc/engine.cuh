@@ -133,6 +133,10 @@ struct kk_engine
      * KK_ERR_TRIAL_LIMIT (bounds every device loop; a valid configuration with
      * acceptance probability 1e-5 exceeds it with probability ~e^-167). */
     uint32_t trial_limit = 1u << 24;
+    /* walk scheduling (kk_engine_set_option): 0 one walker per thread,
+     * 1 persistent walker pool; pool blocks per SM (0 = as many as fit) */
+    int walk_schedule = 1;
+    int walk_blocks_per_sm = 0;
 
     kk::GraphView view() const { return kk::GraphView{V, E, d_off, d_nbr, d_w, d_type}; }
     void free_graph();
@@ -264,11 +268,22 @@ void run_walk(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, WalkR
     }
     L.path = rs.want_paths ? e->path.as<uint32_t>(total_cap) : nullptr;
     KK_CUDA_CHECK(cudaEventRecord(e->ev[1], e->stream));
-    unsigned grid = grid_for(e, n, 256);
-    if constexpr (TC::order == 1)
-        walk_first_order_kernel<S, WC, TC><<<grid, 256, 0, e->stream>>>(g, wc, tc, alias, ra, L);
+    if (e->walk_schedule == 0)
+    {
+        walk_static_kernel<S, WC, TC><<<grid_for(e, n, 256), 256, 0, e->stream>>>(g, wc, tc, alias, ra, L);
+    }
     else
-        walk_second_order_kernel<S, WC, TC><<<grid, 256, 0, e->stream>>>(g, wc, tc, alias, ra, L);
+    {
+        /* persistent walker pool: blocks_per_sm resident blocks on every SM */
+        static int resident = 0;
+        if (resident == 0)
+            KK_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, walk_pool_kernel<S, WC, TC>, 256, 0));
+        int per_sm = e->walk_blocks_per_sm > 0 && e->walk_blocks_per_sm < resident ? e->walk_blocks_per_sm : resident;
+        uint64_t want = (uint64_t)e->sm_count * (per_sm > 0 ? per_sm : 1);
+        uint64_t need = ((uint64_t)n + 255) / 256;
+        unsigned grid = (unsigned)(want < need ? want : (need ? need : 1));
+        walk_pool_kernel<S, WC, TC><<<grid, 256, 0, e->stream>>>(g, wc, tc, alias, ra, L);
+    }
     KK_CUDA_CHECK(cudaGetLastError());
     KK_CUDA_CHECK(cudaEventRecord(e->ev[2], e->stream));
     int h_small[8];

@@ -122,15 +122,20 @@ FRESH = [
 
 
 @pytest.mark.parametrize("i", range(len(FRESH)))
-@pytest.mark.parametrize("seed", [7, 1234567890123])
-def test_fresh_walks_match_oracle(engine, oracle_lib, i, seed):
+@pytest.mark.parametrize("seed,schedule", [(7, 1), (1234567890123, 1), (99, 0)])
+def test_fresh_walks_match_oracle(engine, oracle_lib, i, seed, schedule):
+    """Both walk schedules (one walker per thread, persistent walker pool)."""
     app, gkw, wkw = FRESH[i]
     g = G.random_undirected(500, 6000, seed=seed % 1000 + i, **gkw)
     csr = G.csr_file_order(500, g["src"], g["dst"], w=g.get("w"), type=g.get("type"))
     engine.load_arrays(500, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
     weighted = "w" in csr
     n = 1500
-    ps = engine.walk(app, n, seed=seed, weighted=weighted, walker_begin=77, **wkw)
+    engine.set_option("walk_schedule", schedule)
+    try:
+        ps = engine.walk(app, n, seed=seed, weighted=weighted, walker_begin=77, **wkw)
+    finally:
+        engine.set_option("walk_schedule", 1)
     ocsr = oracle_lib.CSR(500, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
     if app == "node2vec":
         ocsr = ocsr.sorted_copy()

@@ -99,7 +99,7 @@ kk_status kk_engine_set_stream(kk_engine *e, void *stream);
 /* Tuning knobs (results never change, only speed).  No counterpart in the
  * reference, whose CPU scheduling constants are compile-time macros
  * (include/constants.hpp:27-46):
- *   "walk_schedule"      0 one walker per thread, 1 persistent walker pool (default)
+ *   "walk_schedule"      0 one walker per thread (default), 1 persistent walker pool
  *   "walk_blocks_per_sm" pool blocks per SM, 0 = as many as fit (default)
  *   "trial_limit"        rejection trials per step before KK_ERR_TRIAL_LIMIT (default 2^24) */
 kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value);

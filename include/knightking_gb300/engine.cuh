@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -133,9 +134,10 @@ struct kk_engine
      * KK_ERR_TRIAL_LIMIT (bounds every device loop; a valid configuration with
      * acceptance probability 1e-5 exceeds it with probability ~e^-167). */
     uint32_t trial_limit = 1u << 24;
-    /* walk scheduling (kk_engine_set_option): 0 one walker per thread,
-     * 1 persistent walker pool; pool blocks per SM (0 = as many as fit) */
-    int walk_schedule = 1;
+    /* walk scheduling (kk_engine_set_option): 0 one walker per thread
+     * (measured faster on every workload), 1 persistent walker pool; pool
+     * blocks per SM (0 = as many as fit) */
+    int walk_schedule = 0;
     int walk_blocks_per_sm = 0;
 
     kk::GraphView view() const { return kk::GraphView{V, E, d_off, d_nbr, d_w, d_type}; }
@@ -312,5 +314,25 @@ void run_app_node2vec(kk_engine *e, const kk_walk_opts &o, const RunSpec &rs, Wa
 /* Graph helpers (graph.cu). */
 void graph_check_sorted(kk_engine *e);
 void graph_sort_adjacency(kk_engine *e);
+
+/* Runs one epoch of a walk: fills the WalkResult for rs's walkers. */
+typedef std::function<void(const RunSpec &, WalkResult &)> EpochRunner;
+
+/* kk_walk's epoch loop, path packing and copy-out, with `custom` (non-null)
+ * running a user's hooks instead of a built-in app (engine.cu). */
+kk_status walk_to_host(kk_engine *e, const kk_walk_opts *opts, kk_paths **out, const EpochRunner *custom);
+
+/* random_walk() with user-defined hooks (include/walk.hpp:423-436): the
+ * reference's WalkEngine::random_walk(WalkerConfig*, TransitionConfig*,
+ * WalkConfig*) for a graph already in the engine.  opts supplies the walker
+ * range, seed, start list and epoch rate; opts->walk_length bounds every walk
+ * (path capacity walk_length + 1 vertices; a longer walk fails with
+ * KK_ERR_PATH_CAPACITY).  Returns the paths like kk_walk. */
+template <typename S, typename WC, typename TC>
+kk_status random_walk(kk_engine *e, const WC &wc, const TC &tc, const kk_walk_opts &opts, kk_paths **out)
+{
+    EpochRunner run = [&](const RunSpec &rs, WalkResult &res) { run_walk<S>(e, wc, tc, rs, res); };
+    return walk_to_host(e, &opts, out, &run);
+}
 
 } // namespace kk

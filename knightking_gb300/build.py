@@ -22,6 +22,7 @@ LIB = os.path.join(LIBDIR, "libknightking_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["engine.cu", "graph.cu", "apps_first.cu", "apps_node2vec.cu", "alias_noalloc.cu"]
+EXAMPLES = ["tagwalk.cu"]  # knightking_gb300/examples/, each built into lib/libkk_example_<name>.so
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
@@ -42,6 +43,7 @@ def _obj(src):
 
 def _deps():
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    deps += [os.path.join(PKG, "examples", f) for f in os.listdir(os.path.join(PKG, "examples"))]
     for d, _, files in os.walk(INCLUDE):
         deps += [os.path.join(d, f) for f in files]
     return deps
@@ -61,7 +63,8 @@ def build(force=False, verbose=False, extra_flags=()):
         return LIB
 
     def compile_one(src):
-        cmd = [nvcc()] + ARCH + NVCC_FLAGS + list(extra_flags) + ["-c", os.path.join(CSRC, src), "-o", _obj(src)]
+        path = os.path.join(CSRC, src) if not src.startswith("examples/") else os.path.join(PKG, src)
+        cmd = [nvcc()] + ARCH + NVCC_FLAGS + list(extra_flags) + ["-c", path, "-o", _obj(os.path.basename(src))]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -69,18 +72,25 @@ def build(force=False, verbose=False, extra_flags=()):
             raise RuntimeError("nvcc failed on %s:\n%s%s" % (src, r.stdout, r.stderr))
         return r.stderr
 
-    with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        logs = list(ex.map(compile_one, SOURCES))
+    with ThreadPoolExecutor(max_workers=len(SOURCES) + len(EXAMPLES)) as ex:
+        logs = list(ex.map(compile_one, SOURCES + ["examples/" + s for s in EXAMPLES]))
     if verbose:
         for lg in logs:
             if lg:
                 print(lg, file=sys.stderr)
-    tmp = LIB + ".tmp"
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + [_obj(s) for s in SOURCES]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
-    os.replace(tmp, LIB)
+
+    def link(out, objs, extra):
+        tmp = out + ".tmp"
+        r = subprocess.run([nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + extra, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed for %s:\n%s%s" % (out, r.stdout, r.stderr))
+        os.replace(tmp, out)
+
+    link(LIB, [_obj(s) for s in SOURCES], [])
+    # examples of the plugin API, linked against the engine library
+    for s in EXAMPLES:
+        name = os.path.join(LIBDIR, "libkk_example_%s.so" % os.path.splitext(s)[0])
+        link(name, [_obj(s)], ["-L" + LIBDIR, "-lknightking_gb300", "-Xlinker", "-rpath,$ORIGIN"])
     return LIB
 
 

@@ -3,7 +3,7 @@
  * (src/apps/ppr.hpp:30-64) and metapath (src/apps/metapath.hpp:70-128), each
  * unweighted (uniform pick) or weighted (alias tables of the edge weight).
  */
-#include "engine.cuh"
+#include "knightking_gb300/engine.cuh"
 
 namespace kk
 {

@@ -4,7 +4,7 @@
  */
 #include <type_traits>
 
-#include "engine.cuh"
+#include "knightking_gb300/engine.cuh"
 
 namespace kk
 {

@@ -16,7 +16,7 @@
 #include <string>
 #include <vector>
 
-#include "engine.cuh"
+#include "knightking_gb300/engine.cuh"
 
 void kk_engine::free_graph()
 {
@@ -117,12 +117,12 @@ kk_status guard(kk_engine *e, F f)
     }
 }
 
-void validate_opts(kk_engine *e, const kk_walk_opts *o)
+void validate_opts(kk_engine *e, const kk_walk_opts *o, bool builtin)
 {
     if (o == nullptr)
         fail(KK_ERR_INVALID_CONFIG, "opts is NULL");
     require_graph(e);
-    if (o->app < KK_APP_DEEPWALK || o->app > KK_APP_METAPATH)
+    if (builtin && (o->app < KK_APP_DEEPWALK || o->app > KK_APP_METAPATH))
         fail(KK_ERR_INVALID_CONFIG, "unknown app");
     if (o->weighted && e->d_w == nullptr)
         fail(KK_ERR_INVALID_CONFIG, "weighted walk on a graph without weights");
@@ -198,11 +198,12 @@ uint64_t pack_paths(kk_engine *e, const WalkResult &r, uint64_t **d_off_out, uin
     return total;
 }
 
-/* Runs all epochs; sink(epoch_begin, n, d_len, d_off, d_verts, total_vertices) per epoch. */
+/* Runs all epochs; sink(epoch_begin, n, d_len, d_off, d_verts, total_vertices)
+ * per epoch.  `custom` runs a user's hooks instead of a built-in app. */
 template <typename Sink>
-uint64_t walk_epochs(kk_engine *e, const kk_walk_opts *o, Sink sink)
+uint64_t walk_epochs(kk_engine *e, const kk_walk_opts *o, const EpochRunner *custom, Sink sink)
 {
-    validate_opts(e, o);
+    validate_opts(e, o, custom == nullptr);
     const uint32_t *d_start = upload_start(e, o);
     uint32_t per = epoch_walkers(o);
     uint64_t steps = 0;
@@ -211,7 +212,22 @@ uint64_t walk_epochs(kk_engine *e, const kk_walk_opts *o, Sink sink)
     {
         uint32_t num = o->walker_num - done < per ? o->walker_num - done : per;
         WalkResult r;
-        run_epoch(e, o, d_start, o->walker_begin + done, num, true, r);
+        if (custom == nullptr)
+        {
+            run_epoch(e, o, d_start, o->walker_begin + done, num, true, r);
+        }
+        else
+        {
+            RunSpec rs;
+            rs.seed = o->seed;
+            rs.walker_begin = o->walker_begin + done;
+            rs.walker_num = num;
+            rs.d_start = d_start;
+            rs.n_start = o->n_start;
+            rs.fixed_cap = true;
+            rs.cap = o->walk_length + 1;
+            (*custom)(rs, r);
+        }
         uint64_t *d_off;
         uint32_t *d_verts;
         uint64_t total = pack_paths(e, r, &d_off, &d_verts);
@@ -452,7 +468,11 @@ kk_status kk_alias_build(kk_engine *e, float *p, uint32_t *p_idx, uint32_t *q_id
     });
 }
 
-kk_status kk_walk(kk_engine *e, const kk_walk_opts *opts, kk_paths **out)
+} /* extern "C" */
+
+namespace kk
+{
+kk_status walk_to_host(kk_engine *e, const kk_walk_opts *opts, kk_paths **out, const EpochRunner *custom)
 {
     if (!e || !out)
         return KK_ERR_INVALID_CONFIG;
@@ -461,7 +481,7 @@ kk_status kk_walk(kk_engine *e, const kk_walk_opts *opts, kk_paths **out)
     if (!p)
         return KK_ERR_OOM;
     kk_status s = guard(e, [&] {
-        validate_opts(e, opts);
+        validate_opts(e, opts, custom == nullptr);
         uint32_t n = opts->walker_num;
         p->walker_num = n;
         p->walker_begin = opts->walker_begin;
@@ -473,8 +493,9 @@ kk_status kk_walk(kk_engine *e, const kk_walk_opts *opts, kk_paths **out)
         std::vector<uint32_t *> chunks;
         std::vector<uint64_t> chunk_len;
         uint64_t base = 0;
-        p->total_steps = walk_epochs(e, opts, [&](uint32_t done, uint32_t num, const uint32_t *d_len,
-                                                  const uint64_t *d_off, const uint32_t *d_verts, uint64_t total) {
+        p->total_steps = walk_epochs(e, opts, custom, [&](uint32_t done, uint32_t num, const uint32_t *d_len,
+                                                          const uint64_t *d_off, const uint32_t *d_verts,
+                                                          uint64_t total) {
             KK_CUDA_CHECK(cudaMemcpyAsync(p->length + done, d_len, (size_t)num * 4, cudaMemcpyDeviceToHost, e->stream));
             KK_CUDA_CHECK(cudaMemcpyAsync(p->offset + done, d_off, (size_t)num * 8, cudaMemcpyDeviceToHost, e->stream));
             uint32_t *h = (uint32_t *)malloc(total * 4 + 4);
@@ -506,6 +527,14 @@ kk_status kk_walk(kk_engine *e, const kk_walk_opts *opts, kk_paths **out)
     }
     *out = p;
     return KK_OK;
+}
+} // namespace kk
+
+extern "C" {
+
+kk_status kk_walk(kk_engine *e, const kk_walk_opts *opts, kk_paths **out)
+{
+    return kk::walk_to_host(e, opts, out, nullptr);
 }
 
 static kk_status walk_app(kk_engine *e, const kk_walk_opts *opts, kk_paths **out, int app)
@@ -541,7 +570,7 @@ kk_status kk_walk_into(kk_engine *e, const kk_walk_opts *opts, uint32_t *h_lengt
         return KK_ERR_INVALID_CONFIG;
     return guard(e, [&] {
         uint64_t base = 0;
-        uint64_t steps = walk_epochs(e, opts, [&](uint32_t done, uint32_t num, const uint32_t *d_len,
+        uint64_t steps = walk_epochs(e, opts, nullptr, [&](uint32_t done, uint32_t num, const uint32_t *d_len,
                                                   const uint64_t *d_off, const uint32_t *d_verts, uint64_t total) {
             if (base + total > vertices_capacity)
                 fail(KK_ERR_PATH_CAPACITY, "vertices buffer too small");
@@ -565,7 +594,7 @@ kk_status kk_walk_device(kk_engine *e, const kk_walk_opts *opts, uint64_t *total
     if (!e)
         return KK_ERR_INVALID_CONFIG;
     return guard(e, [&] {
-        validate_opts(e, opts);
+        validate_opts(e, opts, true);
         const uint32_t *d_start = upload_start(e, opts);
         WalkResult r;
         run_epoch(e, opts, d_start, opts->walker_begin, opts->walker_num, d_vertices != nullptr, r);

@@ -21,7 +21,7 @@
 #include <cub/cub.cuh>
 #include <vector>
 
-#include "engine.cuh"
+#include "knightking_gb300/engine.cuh"
 
 namespace kk
 {

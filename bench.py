@@ -49,7 +49,27 @@ WORKLOADS = {
                               "5 edge types, uniform[1,5) weights"),
     "node2vec-s24": dict(app="node2vec", scale=24, weights=1, types=0, walk_length=80, p=2.0, q=0.5,
                          desc="node2vec p=2 q=0.5 len 80, one walker per vertex, R-MAT scale 24 ef16 uniform[1,5)"),
+    "metapath-batch-s22": dict(app="metapath", scale=22, weights=1, types=5, batch=16,
+                               schemes=[[1, 2, 4, 8], [2, 8, 2, 16], [4, 1, 16, 4]], scheme_round_robin=True,
+                               desc="16 metapath jobs (walkers 2^10..2^22, lengths 5..200, 3 schemes of 4 one-hot "
+                                    "type masks round robin) in one batched launch vs one launch per job, R-MAT "
+                                    "scale 22 ef16, 5 edge types, uniform[1,5) weights"),
 }
+
+
+def batch_jobs(wl):
+    """The batched workload's jobs: walker counts 2^10..2^22, lengths 5..200 in a fixed shuffled order."""
+    n = wl["batch"]
+    jobs = []
+    for k in range(n):
+        walkers = 1 << (10 + round(12 * k / (n - 1)))
+        length = 5 + (195 * ((7 * k) % n)) // (n - 1)
+        job = dict(walker_num=walkers, seed=100 + k, walk_length=length, weighted=bool(wl["weights"]))
+        for key in ("schemes", "scheme_round_robin", "p", "q"):
+            if key in wl:
+                job[key] = wl[key]
+        jobs.append(job)
+    return jobs
 
 # Bytes touched per walker-step by the walk kernel, at 32 B sector granularity:
 # int64 offset pair 16 B spans 1.25 sectors on average (40 B); a 32 B alias
@@ -223,6 +243,95 @@ def run_reference(args, wl, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_batch_bench(args, wl, world, rank, local):
+    """Batched jobs in one launch vs one launch per job (the reference runs one
+    random_walk() call per job), same jobs, same graph, timed back to back."""
+    import torch
+
+    import knightking_gb300 as kk
+
+    torch.cuda.set_device(local)
+    engine = kk.WalkEngine(local)
+    engine.generate_rmat(wl["scale"], 16, seed=wl["scale"], weights=wl["weights"], types=wl["types"])
+    V, E, _, _ = engine.info()
+    jobs = batch_jobs(wl)
+    for j in jobs:
+        j["walker_begin"] = rank * (1 << 22)
+    app = wl["app"]
+    stream = torch.cuda.Stream()
+    engine.set_stream(stream.cuda_stream)
+
+    def batched():
+        return engine.batch_walk_device(app, jobs, paths=True)
+
+    def plain():
+        steps = 0
+        for j in jobs:
+            kw = dict(j)
+            steps += engine.walk_device(app, kw.pop("walker_num"), paths="unpacked", **kw)[0]
+        return steps
+
+    def timed(fn, k):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        steps = sum(fn() for _ in range(k))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return steps, e0.elapsed_time(e1)
+
+    for _ in range(args.warmup):
+        batched()
+        plain()
+    barrier(world)
+    with ClockSampler(local) as clocks:
+        time.sleep(0.5)
+        b_steps, b_ms = timed(batched, args.steps)
+        p_steps, p_ms = timed(plain, args.steps)
+    b_ms = allreduce(world, b_ms, "max")
+    p_ms = allreduce(world, p_ms, "max")
+    value = allreduce(world, float(b_steps), "sum") / (b_ms / 1e3)
+    plain_value = allreduce(world, float(p_steps), "sum") / (p_ms / 1e3)
+    # e2e: the batch through kk_batch_walk, every job's paths copied to host memory
+    t0 = time.perf_counter()
+    e_steps = 0
+    d2h = 0
+    e2e_runs = max(1, min(args.steps, 3))
+    for _ in range(e2e_runs):
+        res = engine.batch_walk(app, jobs)
+        e_steps += sum(r.total_steps for r in res)
+        d2h += sum(r.path_num * 12 + len(r.vertices) * 4 for r in res)
+    e2e_s = allreduce(world, time.perf_counter() - t0, "max")
+    e2e_value = allreduce(world, float(e_steps), "sum") / e2e_s
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        g = engine.download_graph()
+        cpu = cpu_sample(g, dict(wl, walk_length=max(j["walk_length"] for j in jobs)), V, os.cpu_count() or 1,
+                         seed=1)
+    if rank == 0:
+        line = {
+            "metric": "walker-steps/s", "value": value, "unit": "walker-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": b_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded R-MAT generated on the GPU)",
+            "config": {"workload": args.workload, "desc": wl["desc"], "vertices": V, "edges": E,
+                       "jobs": [[j["walker_num"], j["walk_length"]] for j in jobs],
+                       "walker_steps_per_step": b_steps / args.steps, "parallelism": "replicas",
+                       "l2": "inputs larger than L2"},
+            "plain": {"value": plain_value, "unit": "walker-steps/s", "ms_per_step": p_ms / args.steps,
+                      "what": "one kk_walk_device launch per job, alias tables rebuilt per job"},
+            "batched_over_plain": value / plain_value,
+            "e2e": {"value": e2e_value, "unit": "walker-steps/s", "h2d_bytes_per_step": 64 * len(jobs),
+                    "d2h_bytes_per_step": d2h // e2e_runs},
+            "gpu_launches": args.steps * (4 if wl["weights"] else 1),
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    engine.close()
+
+
 def run_ours(args, wl, world, rank, local):
     import numpy as np
     import torch
@@ -241,7 +350,8 @@ def run_ours(args, wl, world, rank, local):
     app = wl["app"]
 
     def step():
-        steps, _, _, _ = engine.walk_device(app, walkers, paths=False, seed=1, walker_begin=walker_begin, **kw)
+        # paths are written to HBM as the walk produces them (no compaction pass)
+        steps, _, _, _ = engine.walk_device(app, walkers, paths="unpacked", seed=1, walker_begin=walker_begin, **kw)
         return steps
 
     # warm-up; it also picks the walk schedule (one walker per thread vs the
@@ -371,6 +481,8 @@ def main():
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, wl, world, rank, local)
+    elif "batch" in wl:
+        run_batch_bench(args, wl, world, rank, local)
     else:
         run_ours(args, wl, world, rank, local)
     if world > 1:

@@ -182,9 +182,27 @@ kk_status kk_walk_into(kk_engine *e, const kk_walk_opts *opts, uint32_t *h_lengt
 
 /* Same walk with paths left in HBM (no host copy): for callers that consume
  * paths on the GPU.  The buffers stay valid until the next walk call on this
- * engine.  *d_length / *d_offset / *d_vertices are device pointers. */
+ * engine.  *d_length / *d_offset / *d_vertices are device pointers.  With
+ * d_offset NULL and d_vertices non-NULL the paths are returned as the walk
+ * wrote them, unpacked: walker i's slot starts at i * (walk_length + 1)
+ * (DeepWalk, node2vec, metapath) or at its PPR capacity offset.  With both
+ * NULL no path is stored. */
 kk_status kk_walk_device(kk_engine *e, const kk_walk_opts *opts, uint64_t *total_steps, const uint32_t **d_length,
                          const uint64_t **d_offset, const uint32_t **d_vertices);
+
+/* ---- batches: many jobs in one launch (no counterpart in the reference,
+ * which runs one random_walk() call at a time) ---------------------------- */
+
+/* Runs n_jobs (1..1024) DeepWalk, node2vec or metapath jobs of one app and
+ * weighting in one launch; each job has its own seed, walkers, length, (p, q)
+ * or schemes, and its paths equal those of the job run alone.  Jobs take no
+ * start list and no epochs.  out[j] receives job j's paths (kk_paths_free each). */
+kk_status kk_batch_walk(kk_engine *e, const kk_walk_opts *jobs, int n_jobs, kk_paths **out);
+
+/* Same with paths left in HBM in the batch layout (job after job, walker i of a
+ * job at i * (walk_length + 1)); valid until the next walk call. */
+kk_status kk_batch_walk_device(kk_engine *e, const kk_walk_opts *jobs, int n_jobs, uint64_t *total_steps,
+                               const uint32_t **d_length, const uint32_t **d_vertices);
 
 /* Milliseconds of the alias build and of the walk kernels of the last walk
  * call, from CUDA events on the engine's stream. */

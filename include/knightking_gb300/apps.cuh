@@ -4,6 +4,8 @@
  */
 #pragma once
 
+#include <type_traits>
+
 #include "walk.cuh"
 
 namespace kk
@@ -201,15 +203,18 @@ struct MetaSchemes
     uint32_t n;
 };
 
+/* The hooks read their job's schemes from device memory (a batch gives each
+ * job its own set). */
+
 /* extension: 0 at the length or when no out-edge has an allowed type (metapath.hpp:102-105) */
 struct MetapathExt
 {
     const uint8_t *vertex_mask;
     step_t walk_length;
-    MetaSchemes sc;
+    const MetaSchemes *sc;
     __device__ __forceinline__ real_t operator()(const Walker<MetapathState> &w, vertex_id_t v) const
     {
-        return (w.step >= walk_length || !(vertex_mask[v] & sc.mask[w.data.scheme_id][w.data.state])) ? 0.0f : 1.0f;
+        return (w.step >= walk_length || !(vertex_mask[v] & sc->mask[w.data.scheme_id][w.data.state])) ? 0.0f : 1.0f;
     }
 };
 
@@ -217,20 +222,21 @@ struct MetapathExt
 struct MetapathDyn
 {
     const uint8_t *type;
-    MetaSchemes sc;
+    const MetaSchemes *sc;
     __device__ __forceinline__ real_t operator()(const Walker<MetapathState> &w, vertex_id_t, const AdjUnit &e) const
     {
-        return ((sc.mask[w.data.scheme_id][w.data.state] >> type[e.index]) & 1u) ? 1.0f : 0.0f;
+        return ((sc->mask[w.data.scheme_id][w.data.state] >> type[e.index]) & 1u) ? 1.0f : 0.0f;
     }
 };
 
 /* init_state: scheme = gen(#schemes) (metapath.hpp:91-95) or round robin; state 0 */
 struct MetapathInitState
 {
-    uint32_t n;
+    const MetaSchemes *sc;
     int round_robin;
     __device__ __forceinline__ void operator()(Walker<MetapathState> &w, vertex_id_t, Sampler &rng) const
     {
+        const uint32_t n = sc->n;
         w.data.scheme_id = round_robin ? (int)(w.id % n) : (int)rng.gen(n);
         w.data.state = 0;
     }
@@ -239,10 +245,10 @@ struct MetapathInitState
 /* update: state = (state + 1) % len(scheme) (metapath.hpp:96-99) */
 struct MetapathUpdate
 {
-    MetaSchemes sc;
+    const MetaSchemes *sc;
     __device__ __forceinline__ void operator()(Walker<MetapathState> &w, vertex_id_t, const AdjUnit &) const
     {
-        w.data.state = (w.data.state + 1) % (int)sc.len[w.data.scheme_id];
+        w.data.state = (w.data.state + 1) % (int)sc->len[w.data.scheme_id];
     }
 };
 
@@ -257,6 +263,83 @@ static __global__ void metapath_vertex_mask_kernel(GraphView g, uint8_t *vmask)
         vmask[v] = m;
     }
 }
+
+/* ---- batch builders: one job's hooks from its BatchJob row ---------------- */
+
+template <bool Weighted>
+struct DeepWalkBatch
+{
+    typedef EmptyData S;
+    typedef WalkerConfig<EmptyData> WC;
+    typedef TransitionConfig<EmptyData, FixedLengthExt<EmptyData>,
+                             typename std::conditional<Weighted, WeightStatic, NoHook>::type>
+        TC;
+    const float *w;
+    __device__ __forceinline__ void make(const BatchJob &j, WC &wc, TC &tc) const
+    {
+        wc.walker_num = j.walker_num;
+        tc.extension_comp = FixedLengthExt<EmptyData>{j.walk_length};
+        if constexpr (Weighted)
+            tc.static_comp = WeightStatic{w};
+    }
+};
+
+/* Every node2vec job uses the outlier-capable hooks: a job whose overflow
+ * 1/p - max(1, 1/q) is not positive gets an outlier area <= 0, so the
+ * area > 0 test skips the appendix and draws nothing, exactly as the
+ * reference does without the outlier hooks (src/apps/node2vec.hpp:137-139). */
+template <bool Weighted>
+struct Node2vecBatch
+{
+    typedef Node2vecState S;
+    typedef WalkerConfig<Node2vecState, NoHook, NoHook, Node2vecUpdate> WC;
+    typedef SecondOrderTransitionConfig<Node2vecState, vertex_id_t, bool, FixedLengthExt<Node2vecState>,
+                                        typename std::conditional<Weighted, WeightStatic, NoHook>::type,
+                                        Node2vecPostQuery, Node2vecRespond, Node2vecDyn, ConstBound, ConstBound,
+                                        Node2vecOutlierUB<Weighted>, Node2vecOutlierSearch>
+        TC;
+    const uint32_t *nbr;
+    const float *w;
+    __device__ __forceinline__ void make(const BatchJob &j, WC &wc, TC &tc) const
+    {
+        wc.walker_num = j.walker_num;
+        tc.extension_comp = FixedLengthExt<Node2vecState>{j.walk_length};
+        if constexpr (Weighted)
+            tc.static_comp = WeightStatic{w};
+        tc.post_query = Node2vecPostQuery{};
+        tc.respond_query = Node2vecRespond{nbr};
+        tc.dynamic_comp = Node2vecDyn{j.c[0], j.c[3], j.c[4]};
+        tc.dcomp_upperbound = ConstBound{j.c[0]};
+        tc.dcomp_lowerbound = ConstBound{j.c[1]};
+        tc.outlier_upperbound = Node2vecOutlierUB<Weighted>{nbr, w, j.c[2]};
+        tc.outlier_search = Node2vecOutlierSearch{nbr};
+    }
+};
+
+template <bool Weighted>
+struct MetapathBatch
+{
+    typedef MetapathState S;
+    typedef WalkerConfig<MetapathState, NoHook, MetapathInitState, MetapathUpdate> WC;
+    typedef TransitionConfig<MetapathState, MetapathExt,
+                             typename std::conditional<Weighted, WeightStatic, NoHook>::type, MetapathDyn, ConstBound>
+        TC;
+    const uint8_t *vmask;
+    const uint8_t *type;
+    const float *w;
+    __device__ __forceinline__ void make(const BatchJob &j, WC &wc, TC &tc) const
+    {
+        const MetaSchemes *sc = (const MetaSchemes *)j.param;
+        wc.walker_num = j.walker_num;
+        wc.walker_init_state = MetapathInitState{sc, j.flag};
+        wc.walker_update_state = MetapathUpdate{sc};
+        tc.extension_comp = MetapathExt{vmask, j.walk_length, sc};
+        if constexpr (Weighted)
+            tc.static_comp = WeightStatic{w};
+        tc.dynamic_comp = MetapathDyn{type, sc};
+        tc.dcomp_upperbound = ConstBound{1.0f};
+    }
+};
 
 } // namespace apps
 } // namespace kk

@@ -11,6 +11,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string.h>
+
 #include <functional>
 #include <stdexcept>
 #include <string>
@@ -129,6 +131,9 @@ struct kk_engine
     kk::DevBuf order;
     uint32_t n_hub = 0, n_mid = 0, n_nz = 0;
     bool order_valid = false;
+    kk::DevBuf schemes;    /* metapath schemes of the running job(s) */
+    kk::DevBuf batch_jobs; /* job table of the running batch */
+    bool vmask_valid = false;
     float alias_ms = 0.0f, walk_ms = 0.0f;
     /* Rejection trials allowed per walker step before the walk fails with
      * KK_ERR_TRIAL_LIMIT (bounds every device loop; a valid configuration with
@@ -146,6 +151,42 @@ struct kk_engine
 
 namespace kk
 {
+
+/* Runs f, turning the exceptions inside the engine into a status and the
+ * engine's last-error message (no exception crosses the C-ABI). */
+template <typename F>
+kk_status guard(kk_engine *e, F f)
+{
+    try
+    {
+        if (e)
+            e->err.clear();
+        f();
+        return KK_OK;
+    }
+    catch (const Error &x)
+    {
+        if (e)
+            e->err = x.msg;
+        return x.status;
+    }
+    catch (const std::bad_alloc &)
+    {
+        if (e)
+            e->err = "host allocation failed";
+        return KK_ERR_OOM;
+    }
+    catch (const std::exception &x)
+    {
+        if (e)
+            e->err = x.what();
+        return KK_ERR_CUDA;
+    }
+}
+
+/* Packs a walk's paths on the device: per-walker offsets and vertices
+ * (engine.cu); returns the number of vertices. */
+uint64_t pack_walk_paths(kk_engine *e, const WalkResult &r, uint64_t **d_off, uint32_t **d_verts);
 
 inline void require_graph(const kk_engine *e)
 {
@@ -168,6 +209,28 @@ void exclusive_scan_u64(kk_engine *e, const uint64_t *in, uint64_t *out, uint64_
 
 /* Vertices sorted by degree, descending, with the alias tiers (cached per graph). */
 const uint32_t *vertex_order(kk_engine *e);
+
+/* Per-vertex OR of 1 << edge type (metapath.hpp:77-88), cached per graph. */
+const uint8_t *metapath_vertex_masks(kk_engine *e);
+
+/* Metapath schemes of one job as per-state type masks, checked. */
+inline apps::MetaSchemes make_schemes(const kk_walk_opts &o)
+{
+    if (o.n_schemes < 1 || o.n_schemes > KK_MAX_SCHEMES)
+        fail(KK_ERR_INVALID_CONFIG, "metapath needs 1..16 schemes");
+    apps::MetaSchemes sc;
+    memset(&sc, 0, sizeof(sc));
+    sc.n = (uint32_t)o.n_schemes;
+    for (int s = 0; s < o.n_schemes; s++)
+    {
+        if (o.scheme_len[s] < 1 || o.scheme_len[s] > KK_MAX_SCHEME_LEN)
+            fail(KK_ERR_INVALID_CONFIG, "metapath scheme length must be 1..16");
+        sc.len[s] = (uint8_t)o.scheme_len[s];
+        for (int j = 0; j < o.scheme_len[s]; j++)
+            sc.mask[s][j] = o.scheme_mask[s][j];
+    }
+    return sc;
+}
 
 /* Builds alias tables into e->alias/e->sum for a static functor. */
 template <typename TC>
@@ -244,6 +307,7 @@ void run_walk(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, WalkR
     L.start = rs.d_start;
     L.n_start = rs.n_start;
     L.total_steps = d_steps;
+    L.alias_sum = (const float *)e->sum.p;
     L.status = d_status;
     L.trial_limit = e->trial_limit;
     L.length = e->length.as<uint32_t>(n);

@@ -552,6 +552,7 @@ struct WalkLaunch
     const uint32_t *start;    /* optional start-vertex list, start[id % n_start] */
     uint32_t n_start;
     unsigned long long *total_steps;
+    const float *alias_sum; /* static-component sums, for regular_area when ra is not precomputed */
     int *status;
     uint32_t trial_limit;
 };
@@ -611,6 +612,19 @@ __device__ __forceinline__ void flush_steps(unsigned long long *total, unsigned 
         mine += __shfl_down_sync(0xffffffffu, mine, o);
     if ((threadIdx.x & 31) == 0 && mine != 0)
         atomicAdd(total, mine);
+}
+
+/* regular_area[v] (include/walk.hpp:750-781): precomputed, or computed per
+ * use with the same two roundings, sum * ub or deg * ub, when the upper
+ * bound differs per job of a batch. */
+template <typename TC>
+__device__ __forceinline__ float regular_area(const TC &tc, const float *ra, const WalkLaunch &L, vertex_id_t v,
+                                              const AdjList &adj)
+{
+    if (ra != nullptr)
+        return ra[v];
+    const float base = TC::has_static ? L.alias_sum[v] : u2f(adj.degree());
+    return fmul(base, tc.dcomp_upperbound(v, adj));
 }
 
 /* Starts walker i of the launch: id, value-initialised state, start vertex,
@@ -681,7 +695,7 @@ __device__ __forceinline__ bool walk_step(const GraphView &g, const WC &wc, cons
                 tc.outlier_upperbound(w, v, adj, ob, on);
                 if (ob > 0.0f && on > 0)
                 {
-                    const float rav = ra[v];
+                    const float rav = regular_area<TC>(tc, ra, L, v, adj);
                     const float r = fsub(rng.gen_float(fadd(fmul(ob, u2f(on)), rav)), rav);
                     if (r > 0.0f)
                     {
@@ -754,7 +768,7 @@ __device__ __forceinline__ bool walk_step(const GraphView &g, const WC &wc, cons
                     tc.outlier_upperbound(w, v, adj, ob, on);
                     if (ob > 0.0f && on > 0)
                     {
-                        const float rav = ra[v];
+                        const float rav = regular_area<TC>(tc, ra, L, v, adj);
                         const float r = fsub(rng.gen_float(fadd(fmul(ob, u2f(on)), rav)), rav);
                         if (r > 0.0f)
                         {
@@ -889,6 +903,94 @@ __global__ void __launch_bounds__(256) walk_pool_kernel(GraphView g, WC wc, TC t
         }
     }
     flush_steps(L.total_steps, my_steps);
+}
+
+/* ---- batched walks --------------------------------------------------------
+ * Many walk jobs of one app in one launch.  A job has its own seed, walker
+ * range, length and app constants; its walkers get exactly the draws and
+ * decisions of the job run alone, because every draw is keyed by the job's
+ * seed and the walker's id and the job's hooks are rebuilt per walker. */
+
+constexpr uint32_t kMaxBatchJobs = 1024;
+
+struct BatchJob
+{
+    uint64_t seed;
+    uint64_t path_base;    /* first vertex slot of the job's paths */
+    uint32_t walker_begin; /* first walker id */
+    uint32_t walker_num;
+    uint32_t first_task;   /* position of the job's first walker in the batch */
+    uint32_t cap;          /* path capacity per walker, vertices */
+    uint32_t walk_length;
+    int32_t flag;          /* metapath: round-robin scheme assignment */
+    float c[5];            /* node2vec: upperbound, lowerbound, overflow, 1/p, 1/q */
+    const void *param;     /* metapath: the job's schemes (device) */
+};
+
+/* One thread per walker over the concatenated walkers of all jobs; the job of
+ * a walker by binary search over the jobs' first positions (shared memory).
+ * App::make(job, wc, tc) builds the job's WalkerConfig / TransitionConfig. */
+template <typename S, typename App>
+__global__ void __launch_bounds__(256) walk_batch_kernel(GraphView g, App app, const BatchJob *jobs, uint32_t njobs,
+                                                         uint32_t total, const AliasBucket *alias,
+                                                         const float *alias_sum, uint32_t *path, uint32_t *length,
+                                                         unsigned long long *total_steps, int *status,
+                                                         uint32_t trial_limit)
+{
+    __shared__ uint32_t s_first[kMaxBatchJobs];
+    for (uint32_t j = threadIdx.x; j < njobs; j += blockDim.x)
+        s_first[j] = jobs[j].first_task;
+    __syncthreads();
+    unsigned long long my_steps = 0;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t n_iter = (total + stride - 1) / stride;
+    for (uint32_t it = 0; it < n_iter; it++)
+    {
+        const uint32_t t = (it * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
+        if (t < total)
+        {
+            uint32_t lo = 0, hi = njobs;
+            while (hi - lo > 1)
+            {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (s_first[mid] <= t)
+                    lo = mid;
+                else
+                    hi = mid;
+            }
+            const BatchJob job = jobs[lo];
+            typename App::WC wc;
+            typename App::TC tc;
+            app.make(job, wc, tc);
+            WalkLaunch L;
+            L.seed = job.seed;
+            L.walker_begin = job.walker_begin;
+            L.walker_num = job.walker_num;
+            L.path_off = nullptr;
+            L.cap = job.cap;
+            L.path = path ? path + job.path_base : nullptr;
+            L.length = length + job.first_task;
+            L.start = nullptr;
+            L.n_start = 0;
+            L.total_steps = total_steps;
+            L.alias_sum = alias_sum;
+            L.status = status;
+            L.trial_limit = trial_limit;
+            const uint32_t i = t - job.first_task;
+            Sampler rng;
+            rng.init(L.seed);
+            Walker<S> w;
+            vertex_id_t v;
+            uint32_t *out, cap, len;
+            walk_begin<S>(g, wc, L, i, w, v, rng, out, cap, len);
+            while (walk_step<S>(g, wc, tc, alias, nullptr, L, w, v, rng, out, cap, len))
+            {
+            }
+            L.length[i] = len;
+            my_steps += len - 1;
+        }
+    }
+    flush_steps(total_steps, my_steps);
 }
 
 /* Upper bound on each walker's path length when the extension is a constant

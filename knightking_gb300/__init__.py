@@ -232,15 +232,52 @@ class WalkEngine:
                 walk_conf.output_consumer_func(paths)
         return paths
 
+    def _job_array(self, app, jobs):
+        arr = (_capi.KKWalkOpts * len(jobs))()
+        keep = []
+        for i, job in enumerate(jobs):
+            job = dict(job)
+            o = self.make_opts(app, job.pop("walker_num"), **job)
+            keep.append(o)
+            ctypes.memmove(ctypes.byref(arr[i]), ctypes.byref(o), ctypes.sizeof(o))
+        return arr, keep
+
+    def batch_walk(self, app, jobs):
+        """Many jobs of one app in one launch (kk_batch_walk); jobs are dicts of
+        make_opts keywords with walker_num.  Returns one PathSet per job."""
+        arr, keep = self._job_array(app, jobs)
+        outs = (ctypes.POINTER(_capi.KKPaths) * len(jobs))()
+        self._check(self._lib.kk_batch_walk(self._h, arr, len(jobs), outs))
+        res = []
+        try:
+            for p in outs:
+                res.append(PathSet(*_capi.paths_to_numpy(p.contents)))
+        finally:
+            for p in outs:
+                if p:
+                    self._lib.kk_paths_free(p)
+        return res
+
+    def batch_walk_device(self, app, jobs, paths=True):
+        """kk_batch_walk_device: paths stay in HBM; returns the total walker-steps."""
+        arr, keep = self._job_array(app, jobs)
+        steps = ctypes.c_uint64()
+        dl = ctypes.c_void_p()
+        dv = ctypes.c_void_p()
+        self._check(self._lib.kk_batch_walk_device(self._h, arr, len(jobs), ctypes.byref(steps), ctypes.byref(dl),
+                                                   ctypes.byref(dv) if paths else None))
+        return steps.value
+
     def walk_device(self, app, walker_num, paths=True, **kw):
-        """Walk with results left in HBM; returns (total_steps, d_length, d_offset, d_vertices) pointers."""
+        """Walk with results left in HBM; returns (total_steps, d_length, d_offset, d_vertices) pointers.
+        paths: True packed, "unpacked" as the walk wrote them (no compaction pass), False not stored."""
         opts = self.make_opts(app, walker_num, **kw)
         steps = ctypes.c_uint64()
         dl = ctypes.c_void_p()
         do = ctypes.c_void_p()
         dv = ctypes.c_void_p()
         self._check(self._lib.kk_walk_device(self._h, ctypes.byref(opts), ctypes.byref(steps), ctypes.byref(dl),
-                                             ctypes.byref(do) if paths else None,
+                                             ctypes.byref(do) if paths is True else None,
                                              ctypes.byref(dv) if paths else None))
         return steps.value, dl.value, do.value, dv.value
 

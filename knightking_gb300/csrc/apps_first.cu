@@ -69,28 +69,15 @@ void run_metapath(kk_engine *e, const kk_walk_opts &o, RunSpec rs, WalkResult &r
 {
     if (e->d_type == nullptr)
         fail(KK_ERR_INVALID_CONFIG, "metapath needs edge types");
-    if (o.n_schemes < 1 || o.n_schemes > KK_MAX_SCHEMES)
-        fail(KK_ERR_INVALID_CONFIG, "metapath needs 1..16 schemes");
-    MetaSchemes sc;
-    memset(&sc, 0, sizeof(sc));
-    sc.n = (uint32_t)o.n_schemes;
-    for (int s = 0; s < o.n_schemes; s++)
-    {
-        if (o.scheme_len[s] < 1 || o.scheme_len[s] > KK_MAX_SCHEME_LEN)
-            fail(KK_ERR_INVALID_CONFIG, "metapath scheme length must be 1..16");
-        sc.len[s] = (uint8_t)o.scheme_len[s];
-        for (int j = 0; j < o.scheme_len[s]; j++)
-            sc.mask[s][j] = o.scheme_mask[s][j];
-    }
-    GraphView g = e->view();
-    uint8_t *vmask = e->vmask.as<uint8_t>(e->V);
-    metapath_vertex_mask_kernel<<<grid_for(e, e->V, 256), 256, 0, e->stream>>>(g, vmask);
-    KK_CUDA_CHECK(cudaGetLastError());
+    const MetaSchemes host_sc = make_schemes(o);
+    MetaSchemes *sc = e->schemes.as<MetaSchemes>(1);
+    KK_CUDA_CHECK(cudaMemcpyAsync(sc, &host_sc, sizeof(MetaSchemes), cudaMemcpyHostToDevice, e->stream));
+    const uint8_t *vmask = metapath_vertex_masks(e);
     rs.fixed_cap = true;
     rs.cap = o.walk_length + 1;
     WalkerConfig<MetapathState, NoHook, MetapathInitState, MetapathUpdate> wc;
     wc.walker_num = rs.walker_num;
-    wc.walker_init_state = MetapathInitState{sc.n, o.scheme_round_robin};
+    wc.walker_init_state = MetapathInitState{sc, o.scheme_round_robin};
     wc.walker_update_state = MetapathUpdate{sc};
     MetapathExt ext{vmask, o.walk_length, sc};
     MetapathDyn dyn{e->d_type, sc};

@@ -1,0 +1,263 @@
+/*
+ * Batched walks: many walk jobs of one app in one launch.
+ *
+ * Jobs of uneven walker counts, lengths, node2vec (p, q) and metapath schemes
+ * share one kernel (walk_batch_kernel): the alias tables of the graph are built
+ * once for the batch, and small jobs fill the GPU alongside large ones instead
+ * of each paying a launch with an idle tail.  Every job's paths equal those of
+ * the same job run alone through kk_walk.
+ */
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "knightking_gb300/engine.cuh"
+
+namespace kk
+{
+namespace
+{
+using namespace apps;
+
+struct BatchPlan
+{
+    std::vector<BatchJob> jobs;
+    std::vector<MetaSchemes> schemes;
+    uint32_t total = 0;
+    uint64_t total_cap = 0;
+    int app = 0;
+    bool weighted = false;
+};
+
+BatchPlan plan_batch(kk_engine *e, const kk_walk_opts *jobs, int n)
+{
+    require_graph(e);
+    if (jobs == nullptr || n < 1 || (uint32_t)n > kMaxBatchJobs)
+        fail(KK_ERR_INVALID_CONFIG, "a batch holds 1..1024 jobs");
+    BatchPlan plan;
+    plan.app = jobs[0].app;
+    plan.weighted = jobs[0].weighted != 0;
+    if (plan.app != KK_APP_DEEPWALK && plan.app != KK_APP_NODE2VEC && plan.app != KK_APP_METAPATH)
+        fail(KK_ERR_INVALID_CONFIG, "batches take DeepWalk, node2vec or metapath jobs");
+    if (plan.weighted && e->d_w == nullptr)
+        fail(KK_ERR_INVALID_CONFIG, "weighted batch on a graph without weights");
+    if (plan.app == KK_APP_METAPATH && e->d_type == nullptr)
+        fail(KK_ERR_INVALID_CONFIG, "metapath needs edge types");
+    uint64_t first = 0, base = 0;
+    for (int j = 0; j < n; j++)
+    {
+        const kk_walk_opts &o = jobs[j];
+        if (o.app != plan.app || (o.weighted != 0) != plan.weighted)
+            fail(KK_ERR_INVALID_CONFIG, "all jobs of a batch have the same app and weighting");
+        if (o.start != nullptr || (o.rate != 0.0 && o.rate != 1.0))
+            fail(KK_ERR_INVALID_CONFIG, "batch jobs take no start list and no epochs");
+        if ((uint64_t)o.walker_begin + o.walker_num > 0x100000000ULL || o.walk_length >= 0xfffffff0u)
+            fail(KK_ERR_INVALID_CONFIG, "walker ids or walk length out of range");
+        BatchJob b;
+        memset(&b, 0, sizeof(b));
+        b.seed = o.seed;
+        b.walker_begin = o.walker_begin;
+        b.walker_num = o.walker_num;
+        b.first_task = (uint32_t)first;
+        b.cap = o.walk_length + 1;
+        b.path_base = base;
+        b.walk_length = o.walk_length;
+        b.flag = o.scheme_round_robin;
+        if (plan.app == KK_APP_NODE2VEC)
+        {
+            if (!(o.p > 0.0f) || !(o.q > 0.0f))
+                fail(KK_ERR_INVALID_CONFIG, "node2vec needs p > 0 and q > 0");
+            const Node2vecConstants c = Node2vecConstants::make(o.p, o.q);
+            b.c[0] = c.upperbound;
+            b.c[1] = c.lowerbound;
+            b.c[2] = c.overflow;
+            b.c[3] = c.inv_p;
+            b.c[4] = c.inv_q;
+        }
+        if (plan.app == KK_APP_METAPATH)
+            plan.schemes.push_back(make_schemes(o));
+        first += o.walker_num;
+        base += (uint64_t)o.walker_num * b.cap;
+        if (first > 0x80000000ULL)
+            fail(KK_ERR_INVALID_CONFIG, "at most 2^31 walkers per batch");
+        plan.jobs.push_back(b);
+    }
+    plan.total = (uint32_t)first;
+    plan.total_cap = base;
+    return plan;
+}
+
+template <typename App>
+void launch_batch(kk_engine *e, const App &app, const BatchPlan &plan, const BatchJob *d_jobs, const AliasBucket *alias,
+                  uint32_t *length, uint32_t *path, unsigned long long *steps, int *status)
+{
+    walk_batch_kernel<typename App::S, App><<<grid_for(e, plan.total, 256), 256, 0, e->stream>>>(
+        e->view(), app, d_jobs, (uint32_t)plan.jobs.size(), plan.total, alias, (const float *)e->sum.p, path, length,
+        steps, status, e->trial_limit);
+    KK_CUDA_CHECK(cudaGetLastError());
+}
+
+/* Runs the batch; paths stay in HBM in the batch layout: job j's walker i at
+ * path[path_base_j + i * cap_j], its length at length[first_task_j + i]. */
+uint64_t run_batch(kk_engine *e, BatchPlan &plan, uint32_t **d_length, uint32_t **d_path, bool want_paths)
+{
+    if (plan.app == KK_APP_NODE2VEC)
+        graph_sort_adjacency(e);
+    const uint8_t *vmask = nullptr;
+    if (plan.app == KK_APP_METAPATH)
+    {
+        MetaSchemes *d_sc = e->schemes.as<MetaSchemes>(plan.schemes.size());
+        KK_CUDA_CHECK(cudaMemcpyAsync(d_sc, plan.schemes.data(), plan.schemes.size() * sizeof(MetaSchemes),
+                                      cudaMemcpyHostToDevice, e->stream));
+        for (size_t j = 0; j < plan.jobs.size(); j++)
+            plan.jobs[j].param = d_sc + j;
+        vmask = metapath_vertex_masks(e);
+    }
+    BatchJob *d_jobs = e->batch_jobs.as<BatchJob>(plan.jobs.size());
+    KK_CUDA_CHECK(cudaMemcpyAsync(d_jobs, plan.jobs.data(), plan.jobs.size() * sizeof(BatchJob),
+                                  cudaMemcpyHostToDevice, e->stream));
+    int *d_status = (int *)e->small.ensure(64);
+    unsigned long long *d_steps = (unsigned long long *)((char *)d_status + 16);
+    KK_CUDA_CHECK(cudaMemsetAsync(d_status, 0, 64, e->stream));
+    KK_CUDA_CHECK(cudaEventRecord(e->ev[0], e->stream));
+    const AliasBucket *alias = nullptr;
+    if (plan.weighted)
+    {
+        TransitionConfig<EmptyData, FixedLengthExt<EmptyData>, WeightStatic> stc;
+        stc.static_comp = WeightStatic{e->d_w};
+        build_alias(e, stc);
+        alias = (const AliasBucket *)e->alias.p;
+    }
+    uint32_t *length = e->length.as<uint32_t>(plan.total);
+    uint32_t *path = want_paths ? e->path.as<uint32_t>(plan.total_cap) : nullptr;
+    KK_CUDA_CHECK(cudaEventRecord(e->ev[1], e->stream));
+    const GraphView g = e->view();
+    if (plan.app == KK_APP_DEEPWALK)
+    {
+        if (plan.weighted)
+            launch_batch(e, DeepWalkBatch<true>{e->d_w}, plan, d_jobs, alias, length, path, d_steps, d_status);
+        else
+            launch_batch(e, DeepWalkBatch<false>{nullptr}, plan, d_jobs, alias, length, path, d_steps, d_status);
+    }
+    else if (plan.app == KK_APP_NODE2VEC)
+    {
+        if (plan.weighted)
+            launch_batch(e, Node2vecBatch<true>{g.nbr, e->d_w}, plan, d_jobs, alias, length, path, d_steps, d_status);
+        else
+            launch_batch(e, Node2vecBatch<false>{g.nbr, nullptr}, plan, d_jobs, alias, length, path, d_steps,
+                         d_status);
+    }
+    else
+    {
+        if (plan.weighted)
+            launch_batch(e, MetapathBatch<true>{vmask, e->d_type, e->d_w}, plan, d_jobs, alias, length, path,
+                         d_steps, d_status);
+        else
+            launch_batch(e, MetapathBatch<false>{vmask, e->d_type, nullptr}, plan, d_jobs, alias, length, path,
+                         d_steps, d_status);
+    }
+    KK_CUDA_CHECK(cudaEventRecord(e->ev[2], e->stream));
+    int h_small[8];
+    KK_CUDA_CHECK(cudaMemcpyAsync(h_small, d_status, sizeof(h_small), cudaMemcpyDeviceToHost, e->stream));
+    KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+    KK_CUDA_CHECK(cudaEventElapsedTime(&e->alias_ms, e->ev[0], e->ev[1]));
+    KK_CUDA_CHECK(cudaEventElapsedTime(&e->walk_ms, e->ev[1], e->ev[2]));
+    if (h_small[0] == KK_STATUS_TRIAL_LIMIT)
+        fail(KK_ERR_TRIAL_LIMIT, "a walker exceeded the rejection-trial limit");
+    if (h_small[0] == KK_STATUS_PATH_CAPACITY)
+        fail(KK_ERR_PATH_CAPACITY, "a walk exceeded its path capacity");
+    unsigned long long steps;
+    memcpy(&steps, (char *)h_small + 16, sizeof(steps));
+    *d_length = length;
+    *d_path = path;
+    return steps;
+}
+
+} // namespace
+} // namespace kk
+
+using namespace kk;
+
+extern "C" {
+
+kk_status kk_batch_walk_device(kk_engine *e, const kk_walk_opts *jobs, int n_jobs, uint64_t *total_steps,
+                               const uint32_t **d_length, const uint32_t **d_vertices)
+{
+    if (!e)
+        return KK_ERR_INVALID_CONFIG;
+    return guard(e, [&] {
+        BatchPlan plan = plan_batch(e, jobs, n_jobs);
+        uint32_t *len = nullptr, *path = nullptr;
+        uint64_t steps = run_batch(e, plan, &len, &path, d_vertices != nullptr);
+        if (total_steps)
+            *total_steps = steps;
+        if (d_length)
+            *d_length = len;
+        if (d_vertices)
+            *d_vertices = path;
+    });
+}
+
+kk_status kk_batch_walk(kk_engine *e, const kk_walk_opts *jobs, int n_jobs, kk_paths **out)
+{
+    if (!e || !out)
+        return KK_ERR_INVALID_CONFIG;
+    for (int j = 0; j < n_jobs; j++)
+        out[j] = nullptr;
+    kk_status s = guard(e, [&] {
+        BatchPlan plan = plan_batch(e, jobs, n_jobs);
+        uint32_t *len = nullptr, *path = nullptr;
+        run_batch(e, plan, &len, &path, true);
+        std::vector<uint32_t> h_len(plan.total + 1);
+        KK_CUDA_CHECK(cudaMemcpy(h_len.data(), len, (size_t)plan.total * 4, cudaMemcpyDeviceToHost));
+        for (int j = 0; j < n_jobs; j++)
+        {
+            const BatchJob &b = plan.jobs[j];
+            kk_paths *p = (kk_paths *)calloc(1, sizeof(kk_paths));
+            if (!p)
+                fail(KK_ERR_OOM, "host allocation failed");
+            out[j] = p;
+            p->walker_num = b.walker_num;
+            p->walker_begin = b.walker_begin;
+            p->epoch_walkers = b.walker_num;
+            uint64_t total = 0;
+            for (uint32_t i = 0; i < b.walker_num; i++)
+                total += h_len[b.first_task + i];
+            p->total_steps = total - b.walker_num;
+            p->length = (uint32_t *)malloc((size_t)b.walker_num * 4 + 4);
+            p->offset = (uint64_t *)malloc((size_t)b.walker_num * 8 + 8);
+            p->vertices = (uint32_t *)malloc(total * 4 + 4);
+            if (!p->length || !p->offset || !p->vertices)
+                fail(KK_ERR_OOM, "host allocation failed");
+            memcpy(p->length, h_len.data() + b.first_task, (size_t)b.walker_num * 4);
+            if (b.walker_num == 0)
+                continue;
+            WalkResult r;
+            r.walker_num = b.walker_num;
+            r.length = len + b.first_task;
+            r.path_off = nullptr;
+            r.cap = b.cap;
+            r.path = path + b.path_base;
+            r.total_steps = p->total_steps;
+            uint64_t *d_off;
+            uint32_t *d_verts;
+            pack_walk_paths(e, r, &d_off, &d_verts);
+            KK_CUDA_CHECK(cudaMemcpyAsync(p->offset, d_off, (size_t)b.walker_num * 8, cudaMemcpyDeviceToHost,
+                                          e->stream));
+            KK_CUDA_CHECK(cudaMemcpyAsync(p->vertices, d_verts, total * 4, cudaMemcpyDeviceToHost, e->stream));
+            KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+        }
+    });
+    if (s != KK_OK)
+    {
+        for (int j = 0; j < n_jobs; j++)
+        {
+            kk_paths_free(out[j]);
+            out[j] = nullptr;
+        }
+    }
+    return s;
+}
+
+} /* extern "C" */

@@ -38,6 +38,7 @@ void kk_engine::free_graph()
     sorted = -1;
     order_valid = false;
     n_hub = n_mid = n_nz = 0;
+    vmask_valid = false;
 }
 
 namespace kk
@@ -84,36 +85,6 @@ __global__ void cast_alias_kernel(const AliasBucket *b, uint64_t n, float *p, ui
         p[i] = x.p;
         pi[i] = x.p_idx;
         qi[i] = x.q_idx;
-    }
-}
-
-template <typename F>
-kk_status guard(kk_engine *e, F f)
-{
-    try
-    {
-        if (e)
-            e->err.clear();
-        f();
-        return KK_OK;
-    }
-    catch (const Error &x)
-    {
-        if (e)
-            e->err = x.msg;
-        return x.status;
-    }
-    catch (const std::bad_alloc &)
-    {
-        if (e)
-            e->err = "host allocation failed";
-        return KK_ERR_OOM;
-    }
-    catch (const std::exception &x)
-    {
-        if (e)
-            e->err = x.what();
-        return KK_ERR_CUDA;
     }
 }
 
@@ -239,6 +210,12 @@ uint64_t walk_epochs(kk_engine *e, const kk_walk_opts *o, const EpochRunner *cus
 }
 
 } // namespace
+
+uint64_t pack_walk_paths(kk_engine *e, const WalkResult &r, uint64_t **d_off, uint32_t **d_verts)
+{
+    return pack_paths(e, r, d_off, d_verts);
+}
+
 } // namespace kk
 
 using namespace kk;
@@ -310,7 +287,8 @@ void kk_engine_destroy(kk_engine *e)
         cudaStreamSynchronize(e->stream);
     e->free_graph();
     kk::DevBuf *bufs[] = {&e->alias, &e->sum, &e->ave, &e->ra, &e->scratch, &e->vmask,  &e->path,      &e->length,
-                          &e->path_off, &e->caps, &e->start, &e->small, &e->cub_tmp, &e->packed, &e->packed_off};
+                          &e->path_off, &e->caps, &e->start, &e->small, &e->cub_tmp, &e->packed, &e->packed_off,
+                          &e->schemes, &e->batch_jobs};
     for (kk::DevBuf *b : bufs)
         b->release();
     for (int i = 0; i < 3; i++)
@@ -602,15 +580,18 @@ kk_status kk_walk_device(kk_engine *e, const kk_walk_opts *opts, uint64_t *total
             *total_steps = r.total_steps;
         if (d_length)
             *d_length = r.length;
-        if (d_vertices)
+        if (d_vertices && d_offset)
         {
             uint64_t *d_off;
             uint32_t *d_verts;
             pack_paths(e, r, &d_off, &d_verts);
             KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
-            if (d_offset)
-                *d_offset = d_off;
+            *d_offset = d_off;
             *d_vertices = d_verts;
+        }
+        else if (d_vertices)
+        {
+            *d_vertices = r.path; /* unpacked: walker i's slot as the walk wrote it */
         }
     });
 }

@@ -186,6 +186,18 @@ const uint32_t *vertex_order(kk_engine *e)
     return order;
 }
 
+const uint8_t *metapath_vertex_masks(kk_engine *e)
+{
+    uint8_t *vmask = e->vmask.as<uint8_t>(e->V);
+    if (!e->vmask_valid)
+    {
+        apps::metapath_vertex_mask_kernel<<<grid_for(e, e->V, 256), 256, 0, e->stream>>>(e->view(), vmask);
+        KK_CUDA_CHECK(cudaGetLastError());
+        e->vmask_valid = true;
+    }
+    return vmask;
+}
+
 void graph_check_sorted(kk_engine *e)
 {
     int *flag = (int *)e->small.ensure(64);

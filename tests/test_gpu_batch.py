@@ -1,0 +1,79 @@
+"""Batched walks (kk_batch_walk): every job of a batch has exactly the paths it
+has when run alone through kk_walk, which the other tests pin to the reference.
+
+Jobs in one batch differ in seed, walker range, walk length, node2vec (p, q)
+(in and out of the outlier regime) and metapath schemes."""
+
+import numpy as np
+import pytest
+
+from oracle import graphs as G
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def engine():
+    import knightking_gb300 as kk
+    e = kk.WalkEngine(0)
+    yield e
+    e.close()
+
+
+def _load(engine, seed, weighted, types=False):
+    g = G.random_undirected(400, 5000, seed=seed, weight="unif" if weighted else None,
+                            types="uniform" if types else None)
+    csr = G.csr_file_order(400, g["src"], g["dst"], w=g.get("w"), type=g.get("type"))
+    engine.load_arrays(400, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
+
+
+def _check(engine, app, jobs):
+    batch = engine.batch_walk(app, jobs)
+    assert len(batch) == len(jobs)
+    for job, got in zip(jobs, batch):
+        kw = dict(job)
+        n = kw.pop("walker_num")
+        alone = engine.walk(app, n, **kw)
+        np.testing.assert_array_equal(got.path_length, alone.path_length)
+        np.testing.assert_array_equal(got.vertices, alone.vertices)
+        assert got.walker_begin == alone.walker_begin
+        assert got.total_steps == alone.total_steps
+
+
+@pytest.mark.parametrize("weighted", [True, False])
+def test_node2vec_batch_equals_single_jobs(engine, weighted):
+    _load(engine, 3, weighted)
+    jobs = [dict(walker_num=300, seed=1, walk_length=20, p=2.0, q=0.5, weighted=weighted),
+            dict(walker_num=7, seed=2, walk_length=50, p=0.25, q=4.0, weighted=weighted, walker_begin=1000),
+            dict(walker_num=0, seed=3, walk_length=10, p=1.0, q=1.0, weighted=weighted),
+            dict(walker_num=513, seed=4, walk_length=5, p=0.5, q=2.0, weighted=weighted),
+            dict(walker_num=64, seed=5, walk_length=33, p=3.0, q=0.3, weighted=weighted, walker_begin=77)]
+    _check(engine, "node2vec", jobs)
+
+
+@pytest.mark.parametrize("weighted", [True, False])
+def test_metapath_batch_equals_single_jobs(engine, weighted):
+    _load(engine, 4, weighted, types=True)
+    jobs = [dict(walker_num=400, seed=7, walk_length=30, weighted=weighted, schemes=[[1, 2, 4, 8], [2, 8, 2, 16]]),
+            dict(walker_num=129, seed=8, walk_length=12, weighted=weighted, schemes=[[3, 12]],
+                 scheme_round_robin=True),
+            dict(walker_num=1000, seed=9, walk_length=60, weighted=weighted,
+                 schemes=[[31], [1, 2], [4, 16, 8]], scheme_round_robin=True)]
+    _check(engine, "metapath", jobs)
+
+
+@pytest.mark.parametrize("weighted", [True, False])
+def test_deepwalk_batch_equals_single_jobs(engine, weighted):
+    _load(engine, 5, weighted)
+    jobs = [dict(walker_num=n, seed=s, walk_length=l, weighted=weighted, walker_begin=b)
+            for n, s, l, b in ((1, 1, 80, 0), (1024, 2, 5, 10), (333, 3, 200, 5000), (2048, 4, 17, 0))]
+    _check(engine, "deepwalk", jobs)
+
+
+def test_batch_rejects_mixed_apps_and_ppr(engine):
+    import knightking_gb300 as kk
+    _load(engine, 6, True)
+    with pytest.raises(kk.KKError):
+        engine.batch_walk("deepwalk", [dict(walker_num=3, weighted=True), dict(walker_num=3, weighted=False)])
+    with pytest.raises(kk.KKError):
+        engine.batch_walk("ppr", [dict(walker_num=3, terminate_prob=0.1)])

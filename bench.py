@@ -71,12 +71,18 @@ def batch_jobs(wl):
         jobs.append(job)
     return jobs
 
-# Bytes touched per walker-step by the walk kernel, at 32 B sector granularity:
-# int64 offset pair 16 B spans 1.25 sectors on average (40 B); a 32 B alias
-# bucket (which carries the candidate's neighbour) is one sector (32 B); an
-# unweighted pick reads one neighbour id (one sector, 32 B); the 4 B path
-# write is merged by L2 into full sectors (4 B).
-B_STEP = {"deepwalk": 40 + 32 + 4, "ppr": 40 + 32 + 4}
+# Algorithmic bytes per walker-step (the roofline numerator): bytes touched at
+# 32 B sector granularity by the reference's access pattern.  An int64 offset
+# pair (16 B) spans 1.25 sectors on average (40 B); a 12 B alias bucket spans
+# 1.25 sectors (40 B); the candidate's neighbour id is one sector (32 B); the
+# 4 B path write is merged by L2 into full sectors (4 B).
+#   alias DeepWalk: 40 + 40 + 32 + 4 = 116;  unweighted PPR: 40 + 32 + 4 = 76.
+B_STEP = {"deepwalk": 40 + 40 + 32 + 4, "ppr": 40 + 32 + 4}
+# Bytes this engine's layout touches per step: alias DeepWalk reads one 32 B
+# cursor bucket (candidate, neighbour and the neighbour's adjacency position)
+# plus the path write; unweighted PPR reads the offset pair, the neighbour id
+# and writes the path.
+DESIGN_B_STEP = {"deepwalk": 32 + 4, "ppr": 40 + 32 + 4}
 
 
 def load_peaks():
@@ -354,16 +360,29 @@ def run_ours(args, wl, world, rank, local):
         steps, _, _, _ = engine.walk_device(app, walkers, paths="unpacked", seed=1, walker_begin=walker_begin, **kw)
         return steps
 
-    # warm-up; it also picks the walk schedule (one walker per thread vs the
-    # persistent walker pool) by the walk kernel's event time
-    schedule_ms = {}
-    for sched in (0, 1):
+    # warm-up; it also tunes the engine by the event time of alias build +
+    # walk: the alias-table layout (cursor vs index buckets), the context's L2
+    # fetch-granularity hint, then the walk schedule (one walker per thread vs
+    # the persistent walker pool)
+    def measure(sched, layout, l2):
         engine.set_option("walk_schedule", sched)
+        engine.set_option("alias_layout", layout)
+        engine.set_option("l2_fetch_bytes", l2)
         step()
         step()
-        schedule_ms[sched] = engine.last_timing()[1]
-    best_schedule = min(schedule_ms, key=schedule_ms.get)
+        return sum(engine.last_timing()[:2])
+
+    schedule_ms = {}
+    layouts = (0, 1) if wl["weights"] else (0,)
+    for layout in layouts:
+        for l2 in (0, 32, 64):
+            schedule_ms[(0, layout, l2)] = measure(0, layout, l2)
+    _, best_layout, best_l2 = min(schedule_ms, key=schedule_ms.get)
+    schedule_ms[(1, best_layout, best_l2)] = measure(1, best_layout, best_l2)
+    best_schedule, best_layout, best_l2 = min(schedule_ms, key=schedule_ms.get)
     engine.set_option("walk_schedule", best_schedule)
+    engine.set_option("alias_layout", best_layout)
+    engine.set_option("l2_fetch_bytes", best_l2)
     for _ in range(args.warmup):
         step()
     barrier(world)
@@ -430,6 +449,7 @@ def run_ours(args, wl, world, rank, local):
                 traffic = json.load(f)["dram_bytes_per_step"] * steps_per_launch
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_kind": peak_kind, "bytes_per_step": b_step,
+                "design_bytes_per_step": DESIGN_B_STEP.get(app),
                 "kernel": ("walk_pool_kernel" if best_schedule == 1 else "walk_static_kernel") +
                           (" (second order)" if app == "node2vec" else " (first order)"),
                 "kernel_ms": mean_walk_ms, "alias_build_ms": statistics.mean(alias_ms)}
@@ -449,7 +469,12 @@ def run_ours(args, wl, world, rank, local):
                        "walkers_per_gpu": walkers, "walker_steps_per_step": steps_per_launch,
                        "l2": "inputs larger than L2 (graph + alias tables > 129 MB)", "parallelism": "replicas",
                        "walk_schedule": "pool" if best_schedule == 1 else "one walker per thread",
-                       "walk_ms_by_schedule": {"per_thread": schedule_ms[0], "pool": schedule_ms[1]}},
+                       "alias_layout": "cursor buckets" if best_layout == 0 else "index buckets",
+                       "l2_fetch_bytes": best_l2 or "default",
+                       "step_ms_by_choice": {("per_thread" if k[0] == 0 else "pool") + "/" +
+                                             ("cursor" if k[1] == 0 else "index") + "/l2fetch=" +
+                                             (str(k[2]) if k[2] else "default"): v
+                                             for k, v in schedule_ms.items()}},
             "e2e": {"value": e2e_value, "unit": "walker-steps/s", "h2d_bytes_per_step": walkers * 4 + 256,
                     "d2h_bytes_per_step": d2h // e2e_runs},
             "gpu_launches": 2 * args.steps if wl["weights"] else args.steps,

@@ -204,6 +204,59 @@ kk_status kk_batch_walk(kk_engine *e, const kk_walk_opts *jobs, int n_jobs, kk_p
 kk_status kk_batch_walk_device(kk_engine *e, const kk_walk_opts *jobs, int n_jobs, uint64_t *total_steps,
                                const uint32_t **d_length, const uint32_t **d_vertices);
 
+/* ---- serving: continuous batching of walk requests (no counterpart in the
+ * reference) ---------------------------------------------------------------
+ * A server owns the engine while it runs (no other engine call until
+ * kk_serve_stop).  It keeps the graph, the sorted adjacency and the alias
+ * tables resident and runs `slots` batches at once, each on its own stream:
+ * a slot that finishes takes the requests that arrived meanwhile (first come
+ * first served, as many as fit its job count and memory), so new requests are
+ * admitted while earlier ones are still on the GPU and their kernels overlap.
+ * Every request's paths equal those of the same request run alone through
+ * kk_walk.  Submit and poll are thread-safe. */
+typedef struct kk_server kk_server;
+
+typedef struct
+{
+    int app;                /* KK_APP_DEEPWALK, KK_APP_NODE2VEC or KK_APP_METAPATH */
+    int weighted;
+    int slots;              /* batches in flight, 1..8 (0: 2) */
+    uint32_t max_jobs;      /* requests per batch, 1..1024 (0: 256) */
+    uint64_t slot_bytes;    /* admission: device bytes of walker paths and state per slot
+                               (walkers * ((walk_length + 1) * 4 + 4) per request; 0: 1 GiB) */
+} kk_serve_opts;
+
+typedef struct
+{
+    kk_status status;       /* the request's outcome */
+    kk_paths *paths;        /* its paths (caller frees with kk_paths_free); offsets have
+                               walk_length + 1 slots per walker */
+    double queue_ms;        /* submit to launch */
+    double latency_ms;      /* submit to paths on the host */
+    uint32_t batch_jobs;    /* requests in the batch it ran in */
+} kk_serve_result;
+
+typedef struct
+{
+    uint64_t completed, failed, batches;
+    uint64_t walker_steps;
+    double p50_ms, p99_ms, mean_ms; /* latency of the completed requests */
+    double mean_batch_jobs;
+} kk_serve_stats;
+
+kk_status kk_serve_start(kk_engine *e, const kk_serve_opts *opts, kk_server **out);
+/* Queues one request (a kk_walk_opts of the server's app and weighting, no
+ * start list, no epochs); ticket identifies it.  KK_ERR_INVALID_CONFIG for a
+ * request the server cannot run, larger than a slot included. */
+kk_status kk_serve_submit(kk_server *s, const kk_walk_opts *req, uint64_t *ticket);
+/* Waits up to timeout_ms (-1: no limit) for the request; KK_ERR_TIMEOUT if it
+ * is not done yet.  A result is handed out once. */
+kk_status kk_serve_poll(kk_server *s, uint64_t ticket, int timeout_ms, kk_serve_result *out);
+kk_status kk_serve_stats_get(kk_server *s, kk_serve_stats *out);
+/* Finishes the queued requests, stops the slots and frees the server (results
+ * not yet polled are freed). */
+kk_status kk_serve_stop(kk_server *s);
+
 /* Milliseconds of the alias build and of the walk kernels of the last walk
  * call, from CUDA events on the engine's stream. */
 kk_status kk_last_walk_timing(const kk_engine *e, float *alias_ms, float *walk_ms);

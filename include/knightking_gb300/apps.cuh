@@ -62,7 +62,7 @@ __device__ __forceinline__ uint32_t lower_bound_adj(const uint32_t *nbr, edge_id
     while (lo < hi)
     {
         uint32_t mid = lo + ((hi - lo) >> 1);
-        if (nbr[b + mid] < x)
+        if (gather(nbr + b + mid) < x)
             lo = mid + 1;
         else
             hi = mid;
@@ -73,6 +73,7 @@ __device__ __forceinline__ uint32_t lower_bound_adj(const uint32_t *nbr, edge_id
 /* update: previous_vertex = current (node2vec.hpp:129-136) */
 struct Node2vecUpdate
 {
+    static constexpr bool reads_edge_index = false;
     __device__ __forceinline__ void operator()(Walker<Node2vecState> &w, vertex_id_t cur, const AdjUnit &) const
     {
         w.data.previous_vertex = cur;
@@ -82,6 +83,7 @@ struct Node2vecUpdate
 /* post_query: from step 1 on, ask the previous vertex about the candidate (node2vec.hpp:150-158) */
 struct Node2vecPostQuery
 {
+    static constexpr bool reads_edge_index = false;
     __device__ __forceinline__ bool operator()(const Walker<Node2vecState> &w, vertex_id_t, const AdjUnit &cand,
                                                vertex_id_t &target, vertex_id_t &query) const
     {
@@ -102,7 +104,7 @@ struct Node2vecRespond
     {
         uint32_t deg = adj.degree();
         uint32_t i = lower_bound_adj(nbr, adj.begin, deg, query);
-        resp = i < deg && nbr[adj.begin + i] == query;
+        resp = i < deg && gather(nbr + adj.begin + i) == query;
     }
 };
 
@@ -111,6 +113,7 @@ struct Node2vecRespond
  * float parameters). */
 struct Node2vecDyn
 {
+    static constexpr bool reads_edge_index = false;
     real_t upperbound, inv_p, inv_q;
     __device__ __forceinline__ real_t operator()(const Walker<Node2vecState> &w, const bool &resp, vertex_id_t,
                                                  const AdjUnit &e) const
@@ -142,7 +145,7 @@ struct Node2vecOutlierUB
         {
             uint32_t deg = adj.degree();
             uint32_t i = lower_bound_adj(nbr, adj.begin, deg, wk.data.previous_vertex);
-            area = i < deg ? fmul(w[adj.begin + i], overflow) : 0.0f;
+            area = i < deg ? fmul(gather(w + adj.begin + i), overflow) : 0.0f;
         }
         else
         {
@@ -163,7 +166,7 @@ struct Node2vecOutlierSearch
         uint32_t i = lower_bound_adj(nbr, adj.begin, deg, wk.data.previous_vertex);
         if (i >= deg)
             return false;
-        out = AdjUnit{nbr[adj.begin + i], adj.begin + i};
+        out = AdjUnit{gather(nbr + adj.begin + i), adj.begin + i};
         return true;
     }
 };
@@ -214,7 +217,8 @@ struct MetapathExt
     const MetaSchemes *sc;
     __device__ __forceinline__ real_t operator()(const Walker<MetapathState> &w, vertex_id_t v) const
     {
-        return (w.step >= walk_length || !(vertex_mask[v] & sc->mask[w.data.scheme_id][w.data.state])) ? 0.0f : 1.0f;
+        return (w.step >= walk_length || !(gather(vertex_mask + v) & sc->mask[w.data.scheme_id][w.data.state])) ? 0.0f
+                                                                                                            : 1.0f;
     }
 };
 
@@ -225,7 +229,7 @@ struct MetapathDyn
     const MetaSchemes *sc;
     __device__ __forceinline__ real_t operator()(const Walker<MetapathState> &w, vertex_id_t, const AdjUnit &e) const
     {
-        return ((sc->mask[w.data.scheme_id][w.data.state] >> type[e.index]) & 1u) ? 1.0f : 0.0f;
+        return ((sc->mask[w.data.scheme_id][w.data.state] >> gather(type + e.index)) & 1u) ? 1.0f : 0.0f;
     }
 };
 

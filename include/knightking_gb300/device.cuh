@@ -162,4 +162,18 @@ __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b)
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ float u2f(uint32_t a) { return __uint2float_rn(a); }
 
+/* Random gathers of the walk (read-only data path). */
+__device__ __forceinline__ uint32_t gather(const uint32_t *p) { return __ldg(p); }
+__device__ __forceinline__ float gather(const float *p) { return __ldg(p); }
+__device__ __forceinline__ uint8_t gather(const uint8_t *p) { return __ldg(p); }
+__device__ __forceinline__ uint4 gather(const uint4 *p) { return __ldg(p); }
+__device__ __forceinline__ int64_t gather(const int64_t *p)
+{
+    return (int64_t)__ldg(reinterpret_cast<const long long *>(p));
+}
+__device__ __forceinline__ uint64_t gather(const uint64_t *p)
+{
+    return (uint64_t)__ldg(reinterpret_cast<const unsigned long long *>(p));
+}
+
 } // namespace kk

@@ -87,6 +87,27 @@ struct WalkResult
     uint64_t total_steps = 0;
 };
 
+/* Stream, events and buffers one batch runs on: the engine's own (for the
+ * synchronous batch calls) or a serving slot's, so that batches on different
+ * slots run concurrently. */
+struct BatchSlot
+{
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    DevBuf jobs, small, length, path, schemes;
+    float alias_ms = 0.0f, walk_ms = 0.0f;
+    void release()
+    {
+        DevBuf *b[] = {&jobs, &small, &length, &path, &schemes};
+        for (DevBuf *x : b)
+            x->release();
+        for (int i = 0; i < 3; i++)
+            if (ev[i])
+                cudaEventDestroy(ev[i]);
+        ev[0] = ev[1] = ev[2] = nullptr;
+    }
+};
+
 struct RunSpec
 {
     uint64_t seed = 1;
@@ -127,12 +148,15 @@ struct kk_engine
     cudaStream_t side = nullptr; /* hub alias builds run here, joined by events */
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     /* vertices by degree, descending (cached per graph), and the alias tiers:
-     * [0, n_hub) hubs, [n_hub, n_mid) middle, [n_mid, n_nz) small, rest isolated */
+     * [0, n_hub) hubs, [n_hub, n_warp) warp tier, [n_warp, n_t32) degree
+     * 33..128, [n_t32, n_nz) degree 1..32, rest isolated */
     kk::DevBuf order;
-    uint32_t n_hub = 0, n_mid = 0, n_nz = 0;
+    uint32_t n_hub = 0, n_warp = 0, n_t32 = 0, n_nz = 0;
     bool order_valid = false;
-    kk::DevBuf schemes;    /* metapath schemes of the running job(s) */
-    kk::DevBuf batch_jobs; /* job table of the running batch */
+    kk::DevBuf vcur; /* vertex cursors (begin | degree << 40), cached per graph */
+    bool vcur_valid = false;
+    kk::DevBuf schemes;    /* metapath schemes of the running job */
+    kk::BatchSlot bslot;   /* where the synchronous batch calls run */
     bool vmask_valid = false;
     float alias_ms = 0.0f, walk_ms = 0.0f;
     /* Rejection trials allowed per walker step before the walk fails with
@@ -144,6 +168,20 @@ struct kk_engine
      * blocks per SM (0 = as many as fit) */
     int walk_schedule = 0;
     int walk_blocks_per_sm = 0;
+    /* alias-table layout: 0 cursor buckets where the hooks allow them, 1 index
+     * buckets always */
+    int alias_layout = 0;
+    /* alias_cache (option): keep the edge-weight alias tables of the built-in
+     * apps across calls instead of rebuilding them per call as the reference
+     * does (same tables either way).  alias_cached: layout the tables in
+     * e->alias hold (0 cursor, 1 index), -1 none. */
+    int alias_cache = 0;
+    int alias_cached = -1;
+    /* l2_fetch_bytes (option): the context's cudaLimitMaxL2FetchGranularity
+     * hint while the engine lives (0: left as found); the value found is put
+     * back when the option returns to 0 and when the engine is destroyed. */
+    int l2_fetch = 0;
+    size_t l2_fetch_saved = 0;
 
     kk::GraphView view() const { return kk::GraphView{V, E, d_off, d_nbr, d_w, d_type}; }
     void free_graph();
@@ -210,8 +248,37 @@ void exclusive_scan_u64(kk_engine *e, const uint64_t *in, uint64_t *out, uint64_
 /* Vertices sorted by degree, descending, with the alias tiers (cached per graph). */
 const uint32_t *vertex_order(kk_engine *e);
 
+/* Vertex cursors, cached per graph. */
+const uint64_t *vertex_cursors(kk_engine *e);
+
 /* Per-vertex OR of 1 << edge type (metapath.hpp:77-88), cached per graph. */
 const uint8_t *metapath_vertex_masks(kk_engine *e);
+
+/* A batch of walk jobs (batch.cu): the job table, the metapath schemes and
+ * the batch's walker and path-slot totals. */
+struct BatchPlan
+{
+    std::vector<BatchJob> jobs;
+    std::vector<apps::MetaSchemes> schemes;
+    uint32_t total = 0;
+    uint64_t total_cap = 0;
+    int app = 0;
+    bool weighted = false;
+};
+
+/* Checks the jobs and lays out the batch (fails on mixed apps or weighting). */
+BatchPlan plan_batch(kk_engine *e, const kk_walk_opts *jobs, int n);
+
+/* Everything a batch of the plan's app reads besides the graph, on the
+ * engine's stream: the sorted adjacency (node2vec), the vertex type masks
+ * (metapath), the alias tables in the layout the walk uses (weighted). */
+void batch_prepare(kk_engine *e, const BatchPlan &plan);
+
+/* Runs the batch on a slot, paths in HBM in the batch layout: job j's walker i
+ * at path[path_base_j + i * cap_j], its length at length[first_task_j + i].
+ * prepared: batch_prepare already ran for this app (the slot then only reads
+ * the shared tables).  Returns the walker-steps; fails on a walk error. */
+uint64_t run_batch(kk_engine *e, BatchPlan &plan, BatchSlot &slot, bool want_paths, bool prepared);
 
 /* Metapath schemes of one job as per-state type masks, checked. */
 inline apps::MetaSchemes make_schemes(const kk_walk_opts &o)
@@ -232,14 +299,24 @@ inline apps::MetaSchemes make_schemes(const kk_walk_opts &o)
     return sc;
 }
 
-/* Builds alias tables into e->alias/e->sum for a static functor. */
-template <typename TC>
+/* Builds alias tables in the Bucket layout into e->alias/e->sum for a
+ * static functor. */
+template <typename TC, typename Bucket = IndexBucket>
 void build_alias(kk_engine *e, const TC &tc)
 {
+    constexpr bool weight_tables = std::is_same<typename TC::static_type, apps::WeightStatic>::value;
+    const int layout = Bucket::cursor ? 0 : 1;
+    if constexpr (weight_tables)
+    {
+        if (e->alias_cache && e->alias_cached == layout && tc.static_comp.w == e->d_w)
+            return;
+    }
+    e->alias_cached = -1;
     GraphView g = e->view();
-    AliasBucket *alias = e->alias.as<AliasBucket>(e->E);
+    Bucket *alias = e->alias.as<Bucket>(e->E);
     float *sum = e->sum.as<float>(e->V);
     const uint32_t *order = vertex_order(e);
+    const uint64_t *vcur = Bucket::cursor ? vertex_cursors(e) : nullptr;
     const unsigned sms = (unsigned)e->sm_count;
     uint2 *scratch = e->scratch.as<uint2>(2 * e->E);
     if (e->n_hub)
@@ -248,37 +325,57 @@ void build_alias(kk_engine *e, const TC &tc)
         KK_CUDA_CHECK(cudaEventRecord(e->ev_fork, e->stream));
         KK_CUDA_CHECK(cudaStreamWaitEvent(e->side, e->ev_fork, 0));
         unsigned grid = e->n_hub < sms ? e->n_hub : sms;
-        alias_build_hub_kernel<TC><<<grid, 1024, 0, e->side>>>(g, tc, alias, sum, scratch, order, 0, e->n_hub);
+        alias_build_hub_kernel<TC, Bucket>
+            <<<grid, 1024, 0, e->side>>>(g, tc, alias, vcur, sum, scratch, order, 0, e->n_hub);
         KK_CUDA_CHECK(cudaGetLastError());
         KK_CUDA_CHECK(cudaEventRecord(e->ev_join, e->side));
     }
-    if (e->n_nz > e->n_hub)
+    if (e->n_warp > e->n_hub)
     {
         static bool smem_set = false;
         if (!smem_set)
         {
-            KK_CUDA_CHECK(cudaFuncSetAttribute(alias_pair_kernel<TC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)kAliasPairSmem));
+            KK_CUDA_CHECK(cudaFuncSetAttribute(alias_pair_kernel<TC, Bucket>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kAliasPairSmem));
             smem_set = true;
         }
-        const uint32_t n = e->n_nz - e->n_hub;
+        const uint32_t n = e->n_warp - e->n_hub;
         float *ave = e->ave.as<float>(e->V);
-        alias_sum_kernel<TC><<<grid_for(e, n, 256), 256, 0, e->stream>>>(g, tc, sum, ave, order, e->n_hub, e->n_nz);
+        alias_sum_kernel<TC><<<grid_for(e, n, 256), 256, 0, e->stream>>>(g, tc, sum, ave, order, e->n_hub, e->n_warp);
         KK_CUDA_CHECK(cudaGetLastError());
         unsigned grid = (n + 7) / 8 < 3 * sms ? (n + 7) / 8 : 3 * sms;
-        alias_pair_kernel<TC><<<grid, 256, kAliasPairSmem, e->stream>>>(g, tc, alias, ave, scratch, order, e->n_hub,
-                                                                        e->n_nz);
+        alias_pair_kernel<TC, Bucket><<<grid, 256, kAliasPairSmem, e->stream>>>(g, tc, alias, vcur, ave, scratch,
+                                                                                order, e->n_hub, e->n_warp);
+        KK_CUDA_CHECK(cudaGetLastError());
+    }
+    if (e->n_t32 > e->n_warp)
+    {
+        const uint32_t n = e->n_t32 - e->n_warp;
+        alias_thread_kernel<TC, Bucket, kAliasThreadMax, 64>
+            <<<(n + 63) / 64, 64, 0, e->stream>>>(g, tc, alias, vcur, sum, order, e->n_warp, e->n_t32);
+        KK_CUDA_CHECK(cudaGetLastError());
+    }
+    if (e->n_nz > e->n_t32)
+    {
+        const uint32_t n = e->n_nz - e->n_t32;
+        alias_thread_kernel<TC, Bucket, kAliasThreadSmall, 256>
+            <<<(n + 255) / 256, 256, 0, e->stream>>>(g, tc, alias, vcur, sum, order, e->n_t32, e->n_nz);
         KK_CUDA_CHECK(cudaGetLastError());
     }
     if (e->n_hub)
         KK_CUDA_CHECK(cudaStreamWaitEvent(e->stream, e->ev_join, 0));
+    if constexpr (weight_tables)
+    {
+        if (tc.static_comp.w == e->d_w)
+            e->alias_cached = layout;
+    }
 }
 
 /* One walk over walkers [rs.walker_begin, + rs.walker_num): alias tables,
  * regular area, path capacity, the walk kernel.  Events: ev0 before the alias
  * build, ev1 before the walk, ev2 after. */
-template <typename S, typename WC, typename TC>
-void run_walk(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, WalkResult &res)
+template <typename S, typename WC, typename TC, typename Bucket>
+void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, WalkResult &res)
 {
     GraphView g = e->view();
     uint32_t n = rs.walker_num;
@@ -286,12 +383,12 @@ void run_walk(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, WalkR
     unsigned long long *d_steps = (unsigned long long *)((char *)d_status + 16);
     KK_CUDA_CHECK(cudaMemsetAsync(d_status, 0, 64, e->stream));
     KK_CUDA_CHECK(cudaEventRecord(e->ev[0], e->stream));
-    const AliasBucket *alias = nullptr;
+    const Bucket *alias = nullptr;
     const float *ra = nullptr;
     if constexpr (TC::has_static)
     {
-        build_alias(e, tc);
-        alias = (const AliasBucket *)e->alias.p;
+        build_alias<TC, Bucket>(e, tc);
+        alias = (const Bucket *)e->alias.p;
     }
     if constexpr (TC::has_outlier)
     {
@@ -336,19 +433,19 @@ void run_walk(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, WalkR
     KK_CUDA_CHECK(cudaEventRecord(e->ev[1], e->stream));
     if (e->walk_schedule == 0)
     {
-        walk_static_kernel<S, WC, TC><<<grid_for(e, n, 256), 256, 0, e->stream>>>(g, wc, tc, alias, ra, L);
+        walk_static_kernel<S, WC, TC, Bucket><<<grid_for(e, n, 256), 256, 0, e->stream>>>(g, wc, tc, alias, ra, L);
     }
     else
     {
         /* persistent walker pool: blocks_per_sm resident blocks on every SM */
         static int resident = 0;
         if (resident == 0)
-            KK_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, walk_pool_kernel<S, WC, TC>, 256, 0));
+            KK_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, walk_pool_kernel<S, WC, TC, Bucket>, 256, 0));
         int per_sm = e->walk_blocks_per_sm > 0 && e->walk_blocks_per_sm < resident ? e->walk_blocks_per_sm : resident;
         uint64_t want = (uint64_t)e->sm_count * (per_sm > 0 ? per_sm : 1);
         uint64_t need = ((uint64_t)n + 255) / 256;
         unsigned grid = (unsigned)(want < need ? want : (need ? need : 1));
-        walk_pool_kernel<S, WC, TC><<<grid, 256, 0, e->stream>>>(g, wc, tc, alias, ra, L);
+        walk_pool_kernel<S, WC, TC, Bucket><<<grid, 256, 0, e->stream>>>(g, wc, tc, alias, ra, L);
     }
     KK_CUDA_CHECK(cudaGetLastError());
     KK_CUDA_CHECK(cudaEventRecord(e->ev[2], e->stream));
@@ -369,6 +466,22 @@ void run_walk(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, WalkR
     res.cap = L.cap;
     res.path = L.path;
     res.total_steps = steps;
+}
+
+/* Runs a walk with the alias-table layout the engine's alias_layout option
+ * picks: cursor buckets where the hooks allow them (auto), or index buckets. */
+template <typename S, typename WC, typename TC>
+void run_walk(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, WalkResult &res)
+{
+    if constexpr (use_cursor_buckets<WC, TC>())
+    {
+        if (e->alias_layout == 0)
+        {
+            run_walk_with<S, WC, TC, CursorBucket>(e, wc, tc, rs, res);
+            return;
+        }
+    }
+    run_walk_with<S, WC, TC, IndexBucket>(e, wc, tc, rs, res);
 }
 
 /* The built-in apps (apps_*.cu). */

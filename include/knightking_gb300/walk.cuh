@@ -52,6 +52,9 @@ struct TransitionConfig
     typedef S state_type;
     typedef EmptyData query_type;
     typedef EmptyData response_type;
+    typedef Static static_type;
+    typedef Dyn dyn_type;
+    typedef NoHook post_query_type;
     static constexpr bool has_static = is_hook<Static>();
     static constexpr bool has_dynamic = is_hook<Dyn>();
     static constexpr bool has_lowerbound = is_hook<LB>();
@@ -80,6 +83,9 @@ struct SecondOrderTransitionConfig
     typedef S state_type;
     typedef Q query_type;
     typedef R response_type;
+    typedef Static static_type;
+    typedef Dyn dyn_type;
+    typedef PostQuery post_query_type;
     static constexpr bool has_static = is_hook<Static>();
     static constexpr bool has_dynamic = true;
     static constexpr bool has_lowerbound = is_hook<LB>();
@@ -100,12 +106,60 @@ struct SecondOrderTransitionConfig
     OutSearch outlier_search;
 };
 
-/* One alias bucket (AliasBucket, include/walk.hpp:52-57).  p_idx/q_idx are
- * indices local to the vertex's adjacency (q_idx == kNone is the reference's
- * q_ptr == nullptr); p_nbr/q_nbr are those edges' neighbours, so a walker
- * gets its candidate's neighbour from the bucket without a second dependent
- * gather.  32 B aligned: one bucket is exactly one DRAM sector. */
-struct __align__(32) AliasBucket
+/* ---- vertex cursors --------------------------------------------------------
+ * A vertex's adjacency position packed in 64 bits: begin offset in the low 40
+ * bits, degree in the high 24 (kCursorDegMax means "this or more": the degree
+ * is then read from the offsets).  Cursor alias buckets carry the cursors of
+ * their two candidates, so a walker that moves to a candidate already holds
+ * the next vertex's adjacency position. */
+constexpr uint32_t kCursorDegMax = 0xFFFFFFu;
+constexpr uint64_t kCursorBeginMask = (1ull << 40) - 1;
+constexpr uint64_t kCursorMaxEdges = 1ull << 40;
+
+__host__ __device__ __forceinline__ uint64_t make_cursor(int64_t begin, uint32_t deg)
+{
+    return (uint64_t)begin | ((uint64_t)(deg < kCursorDegMax ? deg : kCursorDegMax) << 40);
+}
+
+/* Adjacency position of the vertex a walker stands on. */
+struct Pos
+{
+    int64_t e0;
+    uint32_t deg;
+};
+
+__device__ __forceinline__ Pos pos_from_offsets(const GraphView &g, vertex_id_t v)
+{
+    const int64_t e0 = gather(g.off + v);
+    return Pos{e0, (uint32_t)(gather(g.off + v + 1) - e0)};
+}
+
+__device__ __forceinline__ Pos pos_from_cursor(const GraphView &g, vertex_id_t v, uint64_t c)
+{
+    Pos p{(int64_t)(c & kCursorBeginMask), (uint32_t)(c >> 40)};
+    if (p.deg == kCursorDegMax)
+        p.deg = (uint32_t)(gather(g.off + v + 1) - p.e0);
+    return p;
+}
+
+/* cursors of all vertices */
+static __global__ void vertex_cursor_kernel(GraphView g, uint64_t *cur)
+{
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += gridDim.x * blockDim.x)
+        cur[v] = make_cursor(g.off[v], (uint32_t)(g.off[v + 1] - g.off[v]));
+}
+
+/* One alias bucket (AliasBucket, include/walk.hpp:52-57), in one of two 32 B
+ * layouts (one DRAM sector each):
+ *
+ * IndexBucket: p, p_idx, q_idx (indices local to the vertex's adjacency;
+ *   q_idx == kNone is the reference's q_ptr == nullptr) and the two edges'
+ *   neighbours, so a walker gets its candidate's neighbour without a second
+ *   dependent gather.  Used when a hook reads the taken edge's index.
+ * CursorBucket: p, the two neighbours (q_nbr == kNone: no alias) and their
+ *   vertex cursors; used when no hook reads the edge index, so one 32 B read
+ *   per step gives the next vertex and its adjacency position. */
+struct __align__(32) IndexBucket
 {
     float p;
     uint32_t p_idx;
@@ -115,11 +169,60 @@ struct __align__(32) AliasBucket
     uint32_t q_nbr;
     uint32_t pad1;
     uint32_t pad2;
+
+    static constexpr bool cursor = false;
+    __device__ __forceinline__ static IndexBucket make(float p, uint32_t pi, uint32_t qi, const uint32_t *nb,
+                                                       const uint64_t *)
+    {
+        return IndexBucket{p, pi, qi, 0, nb[pi], qi == kNone ? kNone : nb[qi], 0, 0};
+    }
 };
 
-__device__ __forceinline__ AliasBucket make_bucket(float p, uint32_t pi, uint32_t qi, const uint32_t *nb)
+struct __align__(32) CursorBucket
 {
-    return AliasBucket{p, pi, qi, 0, nb[pi], qi == kNone ? kNone : nb[qi], 0, 0};
+    float p;
+    uint32_t p_nbr;
+    uint32_t q_nbr;
+    uint32_t pad0;
+    uint64_t p_cur;
+    uint64_t q_cur;
+
+    static constexpr bool cursor = true;
+    __device__ __forceinline__ static CursorBucket make(float p, uint32_t pi, uint32_t qi, const uint32_t *nb,
+                                                        const uint64_t *vcur)
+    {
+        const uint32_t pn = nb[pi];
+        if (qi == kNone)
+            return CursorBucket{p, pn, kNone, 0, gather(vcur + pn), 0};
+        const uint32_t qn = nb[qi];
+        return CursorBucket{p, pn, qn, 0, gather(vcur + pn), gather(vcur + qn)};
+    }
+};
+static_assert(sizeof(IndexBucket) == 32 && sizeof(CursorBucket) == 32, "one sector per bucket");
+typedef IndexBucket AliasBucket;
+
+/* Whether a hook reads the index of the edge it is given: hooks declare
+ * `static constexpr bool reads_edge_index = false` to allow cursor buckets;
+ * hooks that do not say are assumed to read it. */
+template <typename F, typename = void>
+struct hook_reads_index
+{
+    static constexpr bool value = is_hook<F>();
+};
+template <typename F>
+struct hook_reads_index<F, std::void_t<decltype(F::reads_edge_index)>>
+{
+    static constexpr bool value = F::reads_edge_index;
+};
+
+/* The walk of (WC, TC) may use cursor buckets: it samples by alias tables and
+ * none of the hooks that see the picked edge reads its index. */
+template <typename WC, typename TC>
+constexpr bool use_cursor_buckets()
+{
+    return TC::has_static && !hook_reads_index<typename TC::dyn_type>::value &&
+           !hook_reads_index<typename TC::post_query_type>::value &&
+           !hook_reads_index<decltype(WC::walker_update_state)>::value;
 }
 
 /* ---- alias-table build (init_alias_tables, include/walk.hpp:538-652) -------
@@ -151,11 +254,16 @@ __device__ __forceinline__ AliasBucket make_bucket(float p, uint32_t pi, uint32_
  *   hubs (deg >= kAliasHubMin): a 1024-thread block per vertex does sum,
  *        split and pairing, queues in the 16 B/edge scratch at 2*off[v];
  *        batches of 64 or fewer go to one warp (no block barrier);
- *   the rest: one thread per vertex computes the serial sums (balanced warps),
- *        then a warp per vertex splits and pairs, queues in shared memory up
- *        to kAliasWarpQueue entries, else in the scratch. */
+ *   warp tier (kAliasThreadMax < deg < kAliasHubMin): one thread per vertex
+ *        computes the serial sums (balanced warps), then a warp per vertex
+ *        splits and pairs, queues in shared memory up to kAliasWarpQueue
+ *        entries, else in the scratch;
+ *   thread tiers (deg <= kAliasThreadMax): one thread per vertex runs the
+ *        serial algorithm on rings in shared memory (alias_thread_kernel). */
 
 constexpr uint32_t kAliasHubMin = 4097;   /* degree from which a vertex is a hub */
+constexpr uint32_t kAliasThreadMax = 128; /* largest degree of the thread tiers */
+constexpr uint32_t kAliasThreadSmall = 32; /* largest degree of the narrow thread tier */
 constexpr uint32_t kAliasWarpQueue = 512; /* shared-memory queue entries per warp */
 constexpr size_t kAliasPairSmem = (size_t)8 * 2 * kAliasWarpQueue * sizeof(uint2); /* 8 warps per block */
 constexpr unsigned kFullMask = 0xffffffffu;
@@ -175,9 +283,10 @@ __device__ __forceinline__ float static_at(const GraphView &g, const TC &tc, uin
 
 /* One warp runs pairing batches of at most 32 iterations until the pairing
  * ends or both queues again hold more than stop_above live entries. */
+template <typename Bucket>
 __device__ __forceinline__ void warp_pairing(uint2 *P, uint2 *Q, uint32_t &ph, uint32_t &pt, uint32_t &qh,
-                                             uint32_t &qt, float ave, AliasBucket *ob, const uint32_t *nb,
-                                             uint32_t stop_above)
+                                             uint32_t &qt, float ave, Bucket *ob, const uint32_t *nb,
+                                             const uint64_t *vcur, uint32_t stop_above)
 {
     const uint32_t lane = threadIdx.x & 31, lt = lanemask_lt();
     while (ph < pt)
@@ -186,7 +295,7 @@ __device__ __forceinline__ void warp_pairing(uint2 *P, uint2 *Q, uint32_t &ph, u
         if (lq == 0)
         {
             for (uint32_t i = lane; i < lp; i += 32)
-                ob[ph + i] = make_bucket(1.0f, P[ph + i].x, kNone, nb);
+                ob[ph + i] = Bucket::make(1.0f, P[ph + i].x, kNone, nb, vcur);
             ph = pt;
             break;
         }
@@ -202,7 +311,7 @@ __device__ __forceinline__ void warp_pairing(uint2 *P, uint2 *Q, uint32_t &ph, u
         {
             const uint2 pe = P[ph + lane], qe = Q[qh + lane];
             const float pv = __uint_as_float(pe.y), qv = __uint_as_float(qe.y);
-            ob[ph + lane] = make_bucket(fdiv(pv, ave), pe.x, qe.x, nb);
+            ob[ph + lane] = Bucket::make(fdiv(pv, ave), pe.x, qe.x, nb, vcur);
             const float r = fsub(qv, fsub(ave, pv));
             conv = r < ave;
             ne = make_uint2(qe.x, __float_as_uint(r));
@@ -270,8 +379,10 @@ __device__ __forceinline__ void block_rank2(bool a, bool b, uint32_t &ra, uint32
 
 /* Pairing loop of a block: block-wide batches while both queues are long,
  * warp 0 alone for short stretches; then the q leftovers (:631-638). */
-__device__ __forceinline__ void block_pairing(uint2 *P, uint2 *Q, uint32_t pt, uint32_t qt, float ave, AliasBucket *ob, const uint32_t *nb,
-                                              uint32_t *sa, uint32_t *sb, uint32_t *s_state)
+template <typename Bucket>
+__device__ __forceinline__ void block_pairing(uint2 *P, uint2 *Q, uint32_t pt, uint32_t qt, float ave, Bucket *ob,
+                                              const uint32_t *nb, const uint64_t *vcur, uint32_t *sa, uint32_t *sb,
+                                              uint32_t *s_state)
 {
     const uint32_t tid = threadIdx.x, nt = blockDim.x;
     uint32_t ph = 0, qh = 0;
@@ -281,7 +392,7 @@ __device__ __forceinline__ void block_pairing(uint2 *P, uint2 *Q, uint32_t pt, u
         if (lq == 0)
         {
             for (uint32_t i = tid; i < lp; i += nt)
-                ob[ph + i] = make_bucket(1.0f, P[ph + i].x, kNone, nb);
+                ob[ph + i] = Bucket::make(1.0f, P[ph + i].x, kNone, nb, vcur);
             ph = pt;
             break;
         }
@@ -290,7 +401,7 @@ __device__ __forceinline__ void block_pairing(uint2 *P, uint2 *Q, uint32_t pt, u
         {
             if (tid < 32)
             {
-                warp_pairing(P, Q, ph, pt, qh, qt, ave, ob, nb, 128);
+                warp_pairing(P, Q, ph, pt, qh, qt, ave, ob, nb, vcur, 128);
                 if (tid == 0)
                 {
                     s_state[0] = ph;
@@ -314,7 +425,7 @@ __device__ __forceinline__ void block_pairing(uint2 *P, uint2 *Q, uint32_t pt, u
         {
             const uint2 pe = P[ph + tid], qe = Q[qh + tid];
             const float pv = __uint_as_float(pe.y), qv = __uint_as_float(qe.y);
-            ob[ph + tid] = make_bucket(fdiv(pv, ave), pe.x, qe.x, nb);
+            ob[ph + tid] = Bucket::make(fdiv(pv, ave), pe.x, qe.x, nb, vcur);
             const float r = fsub(qv, fsub(ave, pv));
             conv = r < ave;
             ne = make_uint2(qe.x, __float_as_uint(r));
@@ -335,7 +446,7 @@ __device__ __forceinline__ void block_pairing(uint2 *P, uint2 *Q, uint32_t pt, u
         qt += tsn;
     }
     for (uint32_t i = tid; i < qt - qh; i += nt)
-        ob[pt + i] = make_bucket(1.0f, Q[qh + i].x, kNone, nb);
+        ob[pt + i] = Bucket::make(1.0f, Q[qh + i].x, kNone, nb, vcur);
     __syncthreads();
 }
 
@@ -397,10 +508,10 @@ __global__ void __launch_bounds__(256) alias_sum_kernel(GraphView g, TC tc, floa
 /* Split (:594-603) and batched FIFO pairing (:605-638) of the non-hub
  * vertices: a warp per vertex, queues in shared memory up to kAliasWarpQueue
  * entries each, else in the global scratch at 2*off[v]. */
-template <typename TC>
-__global__ void __launch_bounds__(256) alias_pair_kernel(GraphView g, TC tc, AliasBucket *out, const float *ave_in,
-                                                         uint2 *scratch, const uint32_t *order, uint32_t lo,
-                                                         uint32_t hi)
+template <typename TC, typename Bucket>
+__global__ void __launch_bounds__(256) alias_pair_kernel(GraphView g, TC tc, Bucket *out, const uint64_t *vcur,
+                                                         const float *ave_in, uint2 *scratch, const uint32_t *order,
+                                                         uint32_t lo, uint32_t hi)
 {
     extern __shared__ uint2 dyn[];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -437,20 +548,20 @@ __global__ void __launch_bounds__(256) alias_pair_kernel(GraphView g, TC tc, Ali
         }
         __syncwarp();
         uint32_t ph = 0, qh = 0;
-        AliasBucket *ob = out + e0;
+        Bucket *ob = out + e0;
         const uint32_t *nb = g.nbr + e0;
-        warp_pairing(P, Q, ph, pt, qh, qt, ave, ob, nb, 0xffffffffu);
+        warp_pairing(P, Q, ph, pt, qh, qt, ave, ob, nb, vcur, 0xffffffffu);
         for (uint32_t i = lane; i < qt - qh; i += 32)
-            ob[pt + i] = make_bucket(1.0f, Q[qh + i].x, kNone, nb);
+            ob[pt + i] = Bucket::make(1.0f, Q[qh + i].x, kNone, nb, vcur);
         __syncwarp();
     }
 }
 
 /* Hub tier: a 1024-thread block per vertex, queues in global scratch. */
-template <typename TC>
-__global__ void __launch_bounds__(1024) alias_build_hub_kernel(GraphView g, TC tc, AliasBucket *out, float *sum_out,
-                                                               uint2 *scratch, const uint32_t *order, uint32_t lo,
-                                                               uint32_t hi)
+template <typename TC, typename Bucket>
+__global__ void __launch_bounds__(1024) alias_build_hub_kernel(GraphView g, TC tc, Bucket *out, const uint64_t *vcur,
+                                                               float *sum_out, uint2 *scratch, const uint32_t *order,
+                                                               uint32_t lo, uint32_t hi)
 {
     __shared__ float chunk[1024];
     __shared__ uint32_t sa[33], sb[33], s_state[4];
@@ -488,7 +599,103 @@ __global__ void __launch_bounds__(1024) alias_build_hub_kernel(GraphView g, TC t
         uint2 *Q = P + deg;
         uint32_t pt, qt;
         block_split([&](uint32_t i) { return static_at(g, tc, v, e0 + i); }, deg, ave, P, Q, pt, qt, sa, sb);
-        block_pairing(P, Q, pt, qt, ave, out + e0, g.nbr + e0, sa, sb, s_state);
+        block_pairing(P, Q, pt, qt, ave, out + e0, g.nbr + e0, vcur, sa, sb, s_state);
+    }
+}
+
+/* Thread tiers: one thread per vertex of degree <= D runs the sequential
+ * algorithm itself (sum, split, pairing, leftovers).  Every pairing pops one
+ * entry from each queue and pushes at most one back, so neither queue ever
+ * holds more entries than it started with: the p queue is a ring over the
+ * first S0 slots of a deg-slot array and the q queue a ring over the last B0
+ * slots, counted from the end (S0 + B0 = deg).  prob[] and the ring live in
+ * shared memory with slot j of thread t at word j*NT + t (ring bytes packed
+ * four to a word), so every lane stays in its own bank whatever its slot. */
+template <typename TC, typename Bucket, uint32_t D, uint32_t NT>
+__global__ void __launch_bounds__(NT) alias_thread_kernel(GraphView g, TC tc, Bucket *out, const uint64_t *vcur,
+                                                          float *sum_out, const uint32_t *order, uint32_t lo,
+                                                          uint32_t hi)
+{
+    static_assert(D <= 256 && D % 4 == 0 && NT % 32 == 0, "ring slots are bytes, four per word");
+    static_assert((size_t)D * NT * 5 <= 48 * 1024, "static shared memory");
+    __shared__ float s_prob[D * NT];
+    __shared__ uint32_t s_ring[(D / 4) * NT];
+    const uint32_t t = threadIdx.x;
+    float *prob = s_prob + t;
+    uint8_t *ring = reinterpret_cast<uint8_t *>(s_ring + t);
+    auto slot = [](uint32_t j) { return (j >> 2) * (NT * 4) + (j & 3); };
+    for (uint32_t k = lo + blockIdx.x * NT + t; k < hi; k += gridDim.x * NT)
+    {
+        const uint32_t v = order[k];
+        const int64_t e0 = g.off[v];
+        const uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
+        float sum = 0.0f;
+        uint32_t j = 0;
+        for (; j + 4 <= deg; j += 4)
+        {
+            const float a = static_at(g, tc, v, e0 + j), b = static_at(g, tc, v, e0 + j + 1);
+            const float c = static_at(g, tc, v, e0 + j + 2), d = static_at(g, tc, v, e0 + j + 3);
+            prob[j * NT] = a;
+            prob[(j + 1) * NT] = b;
+            prob[(j + 2) * NT] = c;
+            prob[(j + 3) * NT] = d;
+            sum = fadd(fadd(fadd(fadd(sum, a), b), c), d);
+        }
+        for (; j < deg; j++)
+        {
+            const float a = static_at(g, tc, v, e0 + j);
+            prob[j * NT] = a;
+            sum = fadd(sum, a);
+        }
+        if (sum_out != nullptr)
+            sum_out[v] = sum;
+        const float ave = fdiv(sum, u2f(deg));
+        /* split in edge order: p ring from the front, q ring from the back */
+        uint32_t S0 = 0, B0 = 0;
+        for (j = 0; j < deg; j++)
+        {
+            if (prob[j * NT] < ave)
+                ring[slot(S0++)] = (uint8_t)j;
+            else
+                ring[slot(deg - 1 - B0++)] = (uint8_t)j;
+        }
+        /* pairing; pt/qt are the push slots (ph + lp) mod S0 and (qh + lq) mod B0 */
+        uint32_t ph = 0, pt = 0, lp = S0, qh = 0, qt = 0, lq = B0, nb_out = 0;
+        Bucket *ob = out + e0;
+        const uint32_t *nb = g.nbr + e0;
+        while (lp != 0 && lq != 0)
+        {
+            const uint32_t pi = ring[slot(ph)], qi = ring[slot(deg - 1 - qh)];
+            ph = ph + 1 == S0 ? 0 : ph + 1;
+            qh = qh + 1 == B0 ? 0 : qh + 1;
+            const float pv = prob[pi * NT], qv = prob[qi * NT];
+            ob[nb_out++] = Bucket::make(fdiv(pv, ave), pi, qi, nb, vcur);
+            const float r = fsub(qv, fsub(ave, pv));
+            prob[qi * NT] = r;
+            if (r < ave)
+            {
+                ring[slot(pt)] = (uint8_t)qi;
+                pt = pt + 1 == S0 ? 0 : pt + 1;
+                lq--;
+            }
+            else
+            {
+                ring[slot(deg - 1 - qt)] = (uint8_t)qi;
+                qt = qt + 1 == B0 ? 0 : qt + 1;
+                lp--;
+            }
+        }
+        /* leftovers (:623-638): the rest of whichever queue is non-empty */
+        for (; lp != 0; lp--)
+        {
+            ob[nb_out++] = Bucket::make(1.0f, ring[slot(ph)], kNone, nb, vcur);
+            ph = ph + 1 == S0 ? 0 : ph + 1;
+        }
+        for (; lq != 0; lq--)
+        {
+            ob[nb_out++] = Bucket::make(1.0f, ring[slot(deg - 1 - qh)], kNone, nb, vcur);
+            qh = qh + 1 == B0 ? 0 : qh + 1;
+        }
     }
 }
 
@@ -502,19 +709,22 @@ static __global__ void degree_keys_kernel(GraphView g, uint32_t *deg, uint32_t *
     }
 }
 
-/* Tier boundaries in the sorted degrees: counts of degree > hub, > small, > 0. */
-static __global__ void tier_bounds_kernel(const uint32_t *sorted_deg, uint32_t n, uint32_t mid_max, uint32_t small_max,
-                                          uint32_t *bounds)
+/* Tier boundaries in the descending degrees: bounds[i] = number of vertices
+ * of degree > thr[i] (bounds zeroed by the caller). */
+struct TierThresholds
+{
+    uint32_t thr[4];
+};
+
+static __global__ void tier_bounds_kernel(const uint32_t *sorted_deg, uint32_t n, TierThresholds t, uint32_t *bounds)
 {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     {
         const uint32_t d = sorted_deg[i], dn = i + 1 < n ? sorted_deg[i + 1] : 0;
-        if (d > mid_max && dn <= mid_max)
-            bounds[0] = i + 1;
-        if (d > small_max && dn <= small_max)
-            bounds[1] = i + 1;
-        if (d > 0 && dn == 0)
-            bounds[2] = i + 1;
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (d > t.thr[k] && dn <= t.thr[k])
+                bounds[k] = i + 1;
     }
 }
 
@@ -583,26 +793,46 @@ __device__ __forceinline__ vertex_id_t walker_start(const GraphView &g, const WC
     return v;
 }
 
+/* A picked candidate: index local to the adjacency (kNone when the bucket
+ * does not carry it), neighbour, and the neighbour's cursor when the bucket
+ * carries one (has_cur). */
+struct Cand
+{
+    uint32_t idx;
+    vertex_id_t nbr;
+    uint64_t cur;
+    bool has_cur;
+};
+
 /* Candidate pick: uniform (include/walk.hpp:1016-1018) or alias
- * (:1020-1028; the coin is drawn only when the bucket has an alias).
- * Returns (index local to the adjacency, neighbour): an alias bucket carries
- * both, read as two 16 B halves of one 32 B sector. */
-template <typename TC>
-__device__ __forceinline__ uint2 pick_candidate(const GraphView &g, const AliasBucket *alias, int64_t e0, uint32_t deg,
-                                                Sampler &rng)
+ * (:1020-1028; the coin is drawn only when the bucket has an alias).  A
+ * bucket is read as the two 16 B halves of its 32 B sector. */
+template <typename TC, typename Bucket>
+__device__ __forceinline__ Cand pick_candidate(const GraphView &g, const Bucket *alias, const Pos &pos, Sampler &rng)
 {
     if constexpr (TC::has_static)
     {
-        const uint4 *b4 = reinterpret_cast<const uint4 *>(alias + e0 + rng.gen(deg));
-        const uint4 lo = __ldg(b4), hi = __ldg(b4 + 1);
-        if (lo.z == kNone || rng.gen_float(1.0f) < __uint_as_float(lo.x))
-            return make_uint2(lo.y, hi.x);
-        return make_uint2(lo.z, hi.y);
+        const uint4 *b4 = reinterpret_cast<const uint4 *>(alias + pos.e0 + rng.gen(pos.deg));
+        const uint4 lo = gather(b4), hi = gather(b4 + 1);
+        if constexpr (Bucket::cursor)
+        {
+            /* lo = {p, p_nbr, q_nbr, -}, hi = {p_cur, q_cur} */
+            if (lo.z == kNone || rng.gen_float(1.0f) < __uint_as_float(lo.x))
+                return Cand{kNone, lo.y, ((uint64_t)hi.y << 32) | hi.x, true};
+            return Cand{kNone, lo.z, ((uint64_t)hi.w << 32) | hi.z, true};
+        }
+        else
+        {
+            /* lo = {p, p_idx, q_idx, -}, hi = {p_nbr, q_nbr, -, -} */
+            if (lo.z == kNone || rng.gen_float(1.0f) < __uint_as_float(lo.x))
+                return Cand{lo.y, hi.x, 0, false};
+            return Cand{lo.z, hi.y, 0, false};
+        }
     }
     else
     {
-        const uint32_t c = rng.gen(deg);
-        return make_uint2(c, g.nbr[e0 + c]);
+        const uint32_t c = rng.gen(pos.deg);
+        return Cand{c, gather(g.nbr + pos.e0 + c), 0, false};
     }
 }
 
@@ -622,28 +852,47 @@ __device__ __forceinline__ float regular_area(const TC &tc, const float *ra, con
                                               const AdjList &adj)
 {
     if (ra != nullptr)
-        return ra[v];
-    const float base = TC::has_static ? L.alias_sum[v] : u2f(adj.degree());
+        return gather(ra + v);
+    const float base = TC::has_static ? gather(L.alias_sum + v) : u2f(adj.degree());
     return fmul(base, tc.dcomp_upperbound(v, adj));
 }
+
+/* One walker's loop state: the walker, the vertex it stands on and that
+ * vertex's adjacency position (pos.e0 < 0: not read yet), the vertex it came
+ * from with its position (second-order queries to it need no offset read),
+ * and its path slot. */
+template <typename S>
+struct WalkerRun
+{
+    Walker<S> w;
+    vertex_id_t v;
+    Pos pos;
+    vertex_id_t pv;
+    Pos ppos;
+    uint32_t *out;
+    uint32_t cap;
+    uint32_t len;
+};
 
 /* Starts walker i of the launch: id, value-initialised state, start vertex,
  * init state, path slot with the start vertex (include/walk.hpp:440-497). */
 template <typename S, typename WC>
 __device__ __forceinline__ void walk_begin(const GraphView &g, const WC &wc, const WalkLaunch &L, uint32_t i,
-                                           Walker<S> &w, vertex_id_t &v, Sampler &rng, uint32_t *&out, uint32_t &cap,
-                                           uint32_t &len)
+                                           WalkerRun<S> &r, Sampler &rng)
 {
-    w.id = L.walker_begin + i;
-    w.step = 0;
-    w.data = S{};
-    v = walker_start<S>(g, wc, L, w, rng);
+    r.w.id = L.walker_begin + i;
+    r.w.step = 0;
+    r.w.data = S{};
+    r.v = walker_start<S>(g, wc, L, r.w, rng);
+    r.pos = Pos{-1, 0};
+    r.pv = kNone;
+    r.ppos = Pos{-1, 0};
     const uint64_t pbase = L.path_off ? L.path_off[i] : (uint64_t)i * L.cap;
-    cap = L.path_off ? (uint32_t)(L.path_off[i + 1] - pbase) : L.cap;
-    out = L.path ? L.path + pbase : nullptr;
-    if (out)
-        out[0] = v;
-    len = 1;
+    r.cap = L.path_off ? (uint32_t)(L.path_off[i + 1] - pbase) : L.cap;
+    r.out = L.path ? L.path + pbase : nullptr;
+    if (r.out)
+        r.out[0] = r.v;
+    r.len = 1;
 }
 
 /* One step of one walker; false when its walk ends.
@@ -661,27 +910,33 @@ __device__ __forceinline__ void walk_begin(const GraphView &g, const WC &wc, con
  * the step at once (:1226-1257); an outlier search that returns no edge retries
  * without a new extension test (:1176-1258).
  *
- * Then step++, walker_update_state, the path write (include/walk.hpp:1043-1052). */
-template <typename S, typename WC, typename TC>
-__device__ __forceinline__ bool walk_step(const GraphView &g, const WC &wc, const TC &tc, const AliasBucket *alias,
-                                          const float *ra, const WalkLaunch &L, Walker<S> &w, vertex_id_t &v,
-                                          Sampler &rng, uint32_t *out, uint32_t cap, uint32_t &len)
+ * Then step++, walker_update_state, the path write (include/walk.hpp:1043-1052).
+ * The new vertex's adjacency position comes from the taken bucket's cursor
+ * when it has one, else it is read from the offsets at the next step. */
+template <typename S, typename WC, typename TC, typename Bucket>
+__device__ __forceinline__ bool walk_step(const GraphView &g, const WC &wc, const TC &tc, const Bucket *alias,
+                                          const float *ra, const WalkLaunch &L, WalkerRun<S> &run, Sampler &rng)
 {
-    const int64_t e0 = g.off[v];
-    const uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
+    Walker<S> &w = run.w;
+    const vertex_id_t v = run.v;
+    if (run.pos.e0 < 0)
+        run.pos = pos_from_offsets(g, v);
+    const Pos pos = run.pos;
+    const int64_t e0 = pos.e0;
+    const uint32_t deg = pos.deg;
     if (deg == 0)
         return false;
     rng.enter(w.id, w.step, 0);
     const AdjList adj{(edge_id_t)e0, (edge_id_t)(e0 + deg)};
-    uint32_t ac = kNone;
-    vertex_id_t nv = 0;
+    Cand ac{kNone, 0, 0, false};
+    bool taken = false;
     uint32_t trials = 0;
     if constexpr (TC::order == 1)
     {
         const real_t ext = tc.extension_comp(w, v);
         if (ext == 0.0f || (ext < 1.0f && rng.gen_float(1.0f) > ext))
             return false;
-        while (ac == kNone)
+        while (!taken)
         {
             if (++trials > L.trial_limit)
             {
@@ -711,15 +966,15 @@ __device__ __forceinline__ bool walk_step(const GraphView &g, const WC &wc, cons
                             const float r2 = fadd(fdiv(fsub(r, fmul(u2f(oi), ob)), sc), tc.dcomp_upperbound(v, adj));
                             if (r2 <= tc.dynamic_comp(w, v, cu))
                             {
-                                ac = (uint32_t)(cu.index - (edge_id_t)e0);
-                                nv = cu.neighbour;
+                                ac = Cand{(uint32_t)(cu.index - (edge_id_t)e0), cu.neighbour, 0, false};
+                                taken = true;
                             }
                         }
                         continue;
                     }
                 }
             }
-            const uint2 pc = pick_candidate<TC>(g, alias, e0, deg, rng);
+            const Cand pc = pick_candidate<TC>(g, alias, pos, rng);
             if constexpr (TC::has_dynamic)
             {
                 const float dart = rng.gen_float(tc.dcomp_upperbound(v, adj));
@@ -727,17 +982,17 @@ __device__ __forceinline__ bool walk_step(const GraphView &g, const WC &wc, cons
                 if constexpr (TC::has_lowerbound)
                     acc = dart <= tc.dcomp_lowerbound(v, adj);
                 if (!acc)
-                    acc = dart <= tc.dynamic_comp(w, v, AdjUnit{pc.y, (edge_id_t)(e0 + pc.x)});
+                    acc = dart <= tc.dynamic_comp(w, v, AdjUnit{pc.nbr, (edge_id_t)(e0 + pc.idx)});
                 if (acc)
                 {
-                    ac = pc.x;
-                    nv = pc.y;
+                    ac = pc;
+                    taken = true;
                 }
             }
             else
             {
-                ac = pc.x;
-                nv = pc.y;
+                ac = pc;
+                taken = true;
             }
         }
     }
@@ -750,7 +1005,7 @@ __device__ __forceinline__ bool walk_step(const GraphView &g, const WC &wc, cons
             const real_t ext = tc.extension_comp(w, v);
             if (ext == 0.0f || (ext < 1.0f && rng.gen_float(1.0f) > ext))
                 return false;
-            AdjUnit cu{0, 0};
+            Cand cd{kNone, 0, 0, false};
             float randval = 0.0f;
             bool accepted = false;
             for (;;)
@@ -776,12 +1031,14 @@ __device__ __forceinline__ bool walk_step(const GraphView &g, const WC &wc, cons
                             uint32_t oi = (uint32_t)fdiv(r, ob);
                             if (oi + 1 > on)
                                 oi = on - 1;
+                            AdjUnit cu;
                             if (tc.outlier_search(w, v, adj, oi, cu))
                             {
                                 float sc = 1.0f;
                                 if constexpr (TC::has_static)
                                     sc = tc.static_comp(v, cu);
                                 randval = fadd(fdiv(fsub(r, fmul(u2f(oi), ob)), sc), tc.dcomp_upperbound(v, adj));
+                                cd = Cand{(uint32_t)(cu.index - (edge_id_t)e0), cu.neighbour, 0, false};
                                 break;
                             }
                         }
@@ -789,14 +1046,14 @@ __device__ __forceinline__ bool walk_step(const GraphView &g, const WC &wc, cons
                 }
                 if (!in_app)
                 {
-                    const uint2 pc = pick_candidate<TC>(g, alias, e0, deg, rng);
-                    cu = AdjUnit{pc.y, (edge_id_t)(e0 + pc.x)};
+                    cd = pick_candidate<TC>(g, alias, pos, rng);
                     randval = rng.gen_float(tc.dcomp_upperbound(v, adj));
                     if constexpr (TC::has_lowerbound)
                         accepted = randval <= tc.dcomp_lowerbound(v, adj);
                     break;
                 }
             }
+            const AdjUnit cu{cd.nbr, (edge_id_t)(e0 + cd.idx)};
             if (!accepted)
             {
                 R resp{};
@@ -804,39 +1061,45 @@ __device__ __forceinline__ bool walk_step(const GraphView &g, const WC &wc, cons
                 vertex_id_t target = 0;
                 if (tc.post_query(w, v, cu, target, query))
                 {
-                    const AdjList tadj{(edge_id_t)g.off[target], (edge_id_t)g.off[target + 1]};
+                    const Pos tp = (target == run.pv && run.ppos.e0 >= 0) ? run.ppos : pos_from_offsets(g, target);
+                    const AdjList tadj{(edge_id_t)tp.e0, (edge_id_t)(tp.e0 + tp.deg)};
                     tc.respond_query(target, query, tadj, resp);
                 }
                 accepted = randval <= tc.dynamic_comp(w, resp, v, cu);
             }
             if (accepted)
             {
-                ac = (uint32_t)(cu.index - (edge_id_t)e0);
-                nv = cu.neighbour;
+                ac = cd;
                 break;
             }
         }
     }
     w.step++;
     if constexpr (is_hook<decltype(wc.walker_update_state)>())
-        wc.walker_update_state(w, v, AdjUnit{nv, (edge_id_t)(e0 + ac)});
-    if (out)
+        wc.walker_update_state(w, v, AdjUnit{ac.nbr, (edge_id_t)(e0 + ac.idx)});
+    if (run.out)
     {
-        if (len >= cap)
+        if (run.len >= run.cap)
         {
             atomicExch(L.status, KK_STATUS_PATH_CAPACITY);
             return false;
         }
-        out[len] = nv;
+        run.out[run.len] = ac.nbr;
     }
-    len++;
-    v = nv;
+    run.len++;
+    run.pv = v;
+    run.ppos = pos;
+    run.v = ac.nbr;
+    if (ac.has_cur)
+        run.pos = pos_from_cursor(g, ac.nbr, ac.cur);
+    else
+        run.pos = Pos{-1, 0};
     return true;
 }
 
 /* One thread per walker for its whole walk, walker state in registers. */
-template <typename S, typename WC, typename TC>
-__global__ void __launch_bounds__(256) walk_static_kernel(GraphView g, WC wc, TC tc, const AliasBucket *alias,
+template <typename S, typename WC, typename TC, typename Bucket>
+__global__ void __launch_bounds__(256) walk_static_kernel(GraphView g, WC wc, TC tc, const Bucket *alias,
                                                           const float *ra, WalkLaunch L)
 {
     unsigned long long my_steps = 0;
@@ -849,15 +1112,13 @@ __global__ void __launch_bounds__(256) walk_static_kernel(GraphView g, WC wc, TC
         {
             Sampler rng;
             rng.init(L.seed);
-            Walker<S> w;
-            vertex_id_t v;
-            uint32_t *out, cap, len;
-            walk_begin<S>(g, wc, L, i, w, v, rng, out, cap, len);
-            while (walk_step<S>(g, wc, tc, alias, ra, L, w, v, rng, out, cap, len))
+            WalkerRun<S> run;
+            walk_begin<S>(g, wc, L, i, run, rng);
+            while (walk_step<S>(g, wc, tc, alias, ra, L, run, rng))
             {
             }
-            L.length[i] = len;
-            my_steps += len - 1;
+            L.length[i] = run.len;
+            my_steps += run.len - 1;
         }
     }
     flush_steps(L.total_steps, my_steps);
@@ -869,8 +1130,8 @@ __global__ void __launch_bounds__(256) walk_static_kernel(GraphView g, WC wc, TC
  * writes its length and takes the next walker at once, so lanes do not idle
  * on finished walks until the block's range runs dry.  Results are those of
  * walk_static_kernel: every walker's draws depend only on its id. */
-template <typename S, typename WC, typename TC>
-__global__ void __launch_bounds__(256) walk_pool_kernel(GraphView g, WC wc, TC tc, const AliasBucket *alias,
+template <typename S, typename WC, typename TC, typename Bucket>
+__global__ void __launch_bounds__(256) walk_pool_kernel(GraphView g, WC wc, TC tc, const Bucket *alias,
                                                         const float *ra, WalkLaunch L)
 {
     __shared__ uint32_t s_next;
@@ -883,23 +1144,21 @@ __global__ void __launch_bounds__(256) walk_pool_kernel(GraphView g, WC wc, TC t
     unsigned long long my_steps = 0;
     Sampler rng;
     rng.init(L.seed);
-    Walker<S> w;
-    vertex_id_t v = 0;
-    uint32_t *out = nullptr, cap = 0, len = 0;
+    WalkerRun<S> run;
     uint32_t i = atomicAdd(&s_next, 1u);
     bool have = i < hi;
     if (have)
-        walk_begin<S>(g, wc, L, i, w, v, rng, out, cap, len);
+        walk_begin<S>(g, wc, L, i, run, rng);
     while (__any_sync(kFullMask, have))
     {
-        if (have && !walk_step<S>(g, wc, tc, alias, ra, L, w, v, rng, out, cap, len))
+        if (have && !walk_step<S>(g, wc, tc, alias, ra, L, run, rng))
         {
-            L.length[i] = len;
-            my_steps += len - 1;
+            L.length[i] = run.len;
+            my_steps += run.len - 1;
             i = atomicAdd(&s_next, 1u);
             have = i < hi;
             if (have)
-                walk_begin<S>(g, wc, L, i, w, v, rng, out, cap, len);
+                walk_begin<S>(g, wc, L, i, run, rng);
         }
     }
     flush_steps(L.total_steps, my_steps);
@@ -930,9 +1189,9 @@ struct BatchJob
 /* One thread per walker over the concatenated walkers of all jobs; the job of
  * a walker by binary search over the jobs' first positions (shared memory).
  * App::make(job, wc, tc) builds the job's WalkerConfig / TransitionConfig. */
-template <typename S, typename App>
+template <typename S, typename App, typename Bucket>
 __global__ void __launch_bounds__(256) walk_batch_kernel(GraphView g, App app, const BatchJob *jobs, uint32_t njobs,
-                                                         uint32_t total, const AliasBucket *alias,
+                                                         uint32_t total, const Bucket *alias,
                                                          const float *alias_sum, uint32_t *path, uint32_t *length,
                                                          unsigned long long *total_steps, int *status,
                                                          uint32_t trial_limit)
@@ -979,15 +1238,13 @@ __global__ void __launch_bounds__(256) walk_batch_kernel(GraphView g, App app, c
             const uint32_t i = t - job.first_task;
             Sampler rng;
             rng.init(L.seed);
-            Walker<S> w;
-            vertex_id_t v;
-            uint32_t *out, cap, len;
-            walk_begin<S>(g, wc, L, i, w, v, rng, out, cap, len);
-            while (walk_step<S>(g, wc, tc, alias, nullptr, L, w, v, rng, out, cap, len))
+            WalkerRun<S> run;
+            walk_begin<S>(g, wc, L, i, run, rng);
+            while (walk_step<S>(g, wc, tc, alias, nullptr, L, run, rng))
             {
             }
-            L.length[i] = len;
-            my_steps += len - 1;
+            L.length[i] = run.len;
+            my_steps += run.len - 1;
         }
     }
     flush_steps(total_steps, my_steps);

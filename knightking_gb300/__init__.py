@@ -291,6 +291,10 @@ class WalkEngine:
                                            ctypes.c_uint64(cap), ctypes.byref(steps)))
         return steps.value
 
+    def serve(self, app, weighted=None, slots=2, max_jobs=256, slot_bytes=1 << 30):
+        """Starts a Server (continuous batching) that owns this engine until stopped."""
+        return Server(self, app, weighted, slots, max_jobs, slot_bytes)
+
     def last_timing(self):
         a = ctypes.c_float()
         w = ctypes.c_float()
@@ -352,3 +356,78 @@ def read_metapath_schemes(path):
 
 def _here():
     return os.path.dirname(os.path.abspath(__file__))
+
+
+class ServeResult:
+    """One served request: its PathSet, status, queueing and total latency."""
+
+    def __init__(self, paths, status, queue_ms, latency_ms, batch_jobs):
+        self.paths = paths
+        self.status = status
+        self.queue_ms = queue_ms
+        self.latency_ms = latency_ms
+        self.batch_jobs = batch_jobs
+
+
+class Server:
+    """Continuous batching of walk requests (kk_serve_*).  submit() and poll()
+    may be called from several threads; the engine is the server's until stop()."""
+
+    def __init__(self, engine, app, weighted=None, slots=2, max_jobs=256, slot_bytes=1 << 30):
+        self._engine = engine
+        self._lib = engine._lib
+        self.app = app
+        if weighted is None:
+            weighted = engine.info()[2]
+        self.weighted = bool(weighted)
+        o = _capi.KKServeOpts()
+        o.app = _capi.APPS[app]
+        o.weighted = int(self.weighted)
+        o.slots = int(slots)
+        o.max_jobs = int(max_jobs)
+        o.slot_bytes = int(slot_bytes)
+        h = ctypes.c_void_p()
+        engine._check(self._lib.kk_serve_start(engine._h, ctypes.byref(o), ctypes.byref(h)))
+        self._h = h
+
+    def submit(self, walker_num, **kw):
+        """Queues a request (make_opts keywords); returns its ticket."""
+        kw.setdefault("weighted", self.weighted)
+        opts = self._engine.make_opts(self.app, walker_num, **kw)
+        t = ctypes.c_uint64()
+        st = self._lib.kk_serve_submit(self._h, ctypes.byref(opts), ctypes.byref(t))
+        if st != _capi.KK_OK:
+            raise KKError(st, "request refused")
+        return t.value
+
+    def poll(self, ticket, timeout_ms=-1):
+        """The request's ServeResult, or None if it is not done within timeout_ms."""
+        r = _capi.KKServeResult()
+        st = self._lib.kk_serve_poll(self._h, ctypes.c_uint64(ticket), int(timeout_ms), ctypes.byref(r))
+        if st == _capi.KK_ERR_TIMEOUT:
+            return None
+        if st != _capi.KK_OK:
+            raise KKError(st, "unknown ticket")
+        paths = None
+        if r.paths:
+            try:
+                paths = PathSet(*_capi.paths_to_numpy(r.paths.contents))
+            finally:
+                self._lib.kk_paths_free(r.paths)
+        return ServeResult(paths, r.status, r.queue_ms, r.latency_ms, r.batch_jobs)
+
+    def stats(self):
+        s = _capi.KKServeStats()
+        self._lib.kk_serve_stats_get(self._h, ctypes.byref(s))
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def stop(self):
+        if self._h:
+            self._lib.kk_serve_stop(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.stop()

@@ -68,6 +68,39 @@ class KKPaths(ctypes.Structure):
     ]
 
 
+class KKServeOpts(ctypes.Structure):
+    _fields_ = [
+        ("app", ctypes.c_int),
+        ("weighted", ctypes.c_int),
+        ("slots", ctypes.c_int),
+        ("max_jobs", ctypes.c_uint32),
+        ("slot_bytes", ctypes.c_uint64),
+    ]
+
+
+class KKServeResult(ctypes.Structure):
+    _fields_ = [
+        ("status", ctypes.c_int),
+        ("paths", ctypes.POINTER(KKPaths)),
+        ("queue_ms", ctypes.c_double),
+        ("latency_ms", ctypes.c_double),
+        ("batch_jobs", ctypes.c_uint32),
+    ]
+
+
+class KKServeStats(ctypes.Structure):
+    _fields_ = [
+        ("completed", ctypes.c_uint64),
+        ("failed", ctypes.c_uint64),
+        ("batches", ctypes.c_uint64),
+        ("walker_steps", ctypes.c_uint64),
+        ("p50_ms", ctypes.c_double),
+        ("p99_ms", ctypes.c_double),
+        ("mean_ms", ctypes.c_double),
+        ("mean_batch_jobs", ctypes.c_double),
+    ]
+
+
 _lib = None
 
 _P = ctypes.c_void_p
@@ -97,6 +130,11 @@ _SIGS = {
     "kk_batch_walk_device": (ctypes.c_int, [_P, _P, ctypes.c_int, _P, _P, _P]),
     "kk_walk_device": (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
     "kk_last_walk_timing": (ctypes.c_int, [_P, _P, _P]),
+    "kk_serve_start": (ctypes.c_int, [_P, _P, _P]),
+    "kk_serve_submit": (ctypes.c_int, [_P, _P, _P]),
+    "kk_serve_poll": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.c_int, _P]),
+    "kk_serve_stats_get": (ctypes.c_int, [_P, _P]),
+    "kk_serve_stop": (ctypes.c_int, [_P]),
     "kk_paths_free": (None, [_P]),
     "kk_paths_dump": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]),
 }
@@ -173,9 +211,21 @@ def make_opts(app, walker_num, seed, walker_begin, walk_length, terminate_prob, 
 
 
 def paths_to_numpy(p):
+    """A kk_paths as numpy arrays, packed: walker i's vertices at the prefix
+    sum of the lengths (paths with gaps between walkers are compacted)."""
     n = p.walker_num
     length = np.ctypeslib.as_array(p.length, shape=(n,)).copy() if n else np.zeros(0, np.uint32)
     offset = np.ctypeslib.as_array(p.offset, shape=(n,)).copy() if n else np.zeros(0, np.uint64)
     total = int(p.total_steps) + n
-    verts = np.ctypeslib.as_array(p.vertices, shape=(total,)).copy() if total else np.zeros(0, np.uint32)
+    packed = np.zeros(n, np.uint64)
+    if n:
+        np.cumsum(length[:-1], out=packed[1:])
+    if n == 0 or np.array_equal(offset, packed):
+        verts = np.ctypeslib.as_array(p.vertices, shape=(total,)).copy() if total else np.zeros(0, np.uint32)
+    else:
+        extent = int((offset + length.astype(np.uint64)).max())
+        raw = np.ctypeslib.as_array(p.vertices, shape=(max(extent, 1),))
+        idx = np.repeat(offset.astype(np.int64) - packed.astype(np.int64), length) + np.arange(total, dtype=np.int64)
+        verts = raw[idx].copy()
+        offset = packed
     return p.walker_begin, p.epoch_walkers, length, offset, verts, p.total_steps

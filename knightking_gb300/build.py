@@ -21,7 +21,7 @@ LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libknightking_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-SOURCES = ["engine.cu", "graph.cu", "apps_first.cu", "apps_node2vec.cu", "alias_noalloc.cu", "batch.cu"]
+SOURCES = ["engine.cu", "graph.cu", "apps_first.cu", "apps_node2vec.cu", "alias_noalloc.cu", "batch.cu", "serve.cu"]
 EXAMPLES = ["tagwalk.cu"]  # knightking_gb300/examples/, each built into lib/libkk_example_<name>.so
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [

@@ -16,19 +16,7 @@
 
 namespace kk
 {
-namespace
-{
 using namespace apps;
-
-struct BatchPlan
-{
-    std::vector<BatchJob> jobs;
-    std::vector<MetaSchemes> schemes;
-    uint32_t total = 0;
-    uint64_t total_cap = 0;
-    int app = 0;
-    bool weighted = false;
-};
 
 BatchPlan plan_batch(kk_engine *e, const kk_walk_opts *jobs, int n)
 {
@@ -88,94 +76,171 @@ BatchPlan plan_batch(kk_engine *e, const kk_walk_opts *jobs, int n)
     return plan;
 }
 
-template <typename App>
-void launch_batch(kk_engine *e, const App &app, const BatchPlan &plan, const BatchJob *d_jobs, const AliasBucket *alias,
-                  uint32_t *length, uint32_t *path, unsigned long long *steps, int *status)
+namespace
 {
-    walk_batch_kernel<typename App::S, App><<<grid_for(e, plan.total, 256), 256, 0, e->stream>>>(
-        e->view(), app, d_jobs, (uint32_t)plan.jobs.size(), plan.total, alias, (const float *)e->sum.p, path, length,
+
+/* Launches the batch on the slot, reading alias tables in the Bucket layout
+ * (built on the engine's stream first unless prepared). */
+template <typename App, typename Bucket>
+void launch_batch_with(kk_engine *e, const App &app, const BatchPlan &plan, BatchSlot &slot, const BatchJob *d_jobs,
+                       uint32_t *length, uint32_t **path, unsigned long long *steps, int *status, bool want_paths,
+                       bool prepared)
+{
+    typedef typename App::TC TC;
+    const Bucket *alias = nullptr;
+    if constexpr (TC::has_static)
+    {
+        if (!prepared)
+        {
+            TransitionConfig<EmptyData, FixedLengthExt<EmptyData>, WeightStatic> stc;
+            stc.static_comp = WeightStatic{e->d_w};
+            build_alias<decltype(stc), Bucket>(e, stc);
+        }
+        alias = (const Bucket *)e->alias.p;
+    }
+    *path = want_paths ? slot.path.as<uint32_t>(plan.total_cap) : nullptr;
+    KK_CUDA_CHECK(cudaEventRecord(slot.ev[1], slot.stream));
+    walk_batch_kernel<typename App::S, App, Bucket><<<grid_for(e, plan.total, 256), 256, 0, slot.stream>>>(
+        e->view(), app, d_jobs, (uint32_t)plan.jobs.size(), plan.total, alias, (const float *)e->sum.p, *path, length,
         steps, status, e->trial_limit);
     KK_CUDA_CHECK(cudaGetLastError());
 }
 
-/* Runs the batch; paths stay in HBM in the batch layout: job j's walker i at
- * path[path_base_j + i * cap_j], its length at length[first_task_j + i]. */
-uint64_t run_batch(kk_engine *e, BatchPlan &plan, uint32_t **d_length, uint32_t **d_path, bool want_paths)
+/* The alias layout the engine's alias_layout option picks for the app:
+ * cursor buckets where the app's hooks allow them, else index buckets. */
+template <typename App>
+bool app_uses_cursor(const kk_engine *e)
+{
+    return use_cursor_buckets<typename App::WC, typename App::TC>() && e->alias_layout == 0;
+}
+
+template <typename App>
+void launch_batch(kk_engine *e, const App &app, const BatchPlan &plan, BatchSlot &slot, const BatchJob *d_jobs,
+                  uint32_t *length, uint32_t **path, unsigned long long *steps, int *status, bool want_paths,
+                  bool prepared)
+{
+    if constexpr (use_cursor_buckets<typename App::WC, typename App::TC>())
+    {
+        if (app_uses_cursor<App>(e))
+        {
+            launch_batch_with<App, CursorBucket>(e, app, plan, slot, d_jobs, length, path, steps, status,
+                                                 want_paths, prepared);
+            return;
+        }
+    }
+    launch_batch_with<App, IndexBucket>(e, app, plan, slot, d_jobs, length, path, steps, status, want_paths,
+                                        prepared);
+}
+
+/* Builds the weight alias tables in the layout App's walk reads. */
+template <typename App>
+void prepare_tables(kk_engine *e)
+{
+    TransitionConfig<EmptyData, FixedLengthExt<EmptyData>, WeightStatic> stc;
+    stc.static_comp = WeightStatic{e->d_w};
+    if (app_uses_cursor<App>(e))
+        build_alias<decltype(stc), CursorBucket>(e, stc);
+    else
+        build_alias<decltype(stc), IndexBucket>(e, stc);
+}
+
+} // namespace
+
+void batch_prepare(kk_engine *e, const BatchPlan &plan)
 {
     if (plan.app == KK_APP_NODE2VEC)
         graph_sort_adjacency(e);
-    const uint8_t *vmask = nullptr;
     if (plan.app == KK_APP_METAPATH)
-    {
-        MetaSchemes *d_sc = e->schemes.as<MetaSchemes>(plan.schemes.size());
-        KK_CUDA_CHECK(cudaMemcpyAsync(d_sc, plan.schemes.data(), plan.schemes.size() * sizeof(MetaSchemes),
-                                      cudaMemcpyHostToDevice, e->stream));
-        for (size_t j = 0; j < plan.jobs.size(); j++)
-            plan.jobs[j].param = d_sc + j;
-        vmask = metapath_vertex_masks(e);
-    }
-    BatchJob *d_jobs = e->batch_jobs.as<BatchJob>(plan.jobs.size());
-    KK_CUDA_CHECK(cudaMemcpyAsync(d_jobs, plan.jobs.data(), plan.jobs.size() * sizeof(BatchJob),
-                                  cudaMemcpyHostToDevice, e->stream));
-    int *d_status = (int *)e->small.ensure(64);
-    unsigned long long *d_steps = (unsigned long long *)((char *)d_status + 16);
-    KK_CUDA_CHECK(cudaMemsetAsync(d_status, 0, 64, e->stream));
-    KK_CUDA_CHECK(cudaEventRecord(e->ev[0], e->stream));
-    const AliasBucket *alias = nullptr;
+        metapath_vertex_masks(e);
     if (plan.weighted)
     {
-        TransitionConfig<EmptyData, FixedLengthExt<EmptyData>, WeightStatic> stc;
-        stc.static_comp = WeightStatic{e->d_w};
-        build_alias(e, stc);
-        alias = (const AliasBucket *)e->alias.p;
+        if (plan.app == KK_APP_DEEPWALK)
+            prepare_tables<DeepWalkBatch<true>>(e);
+        else if (plan.app == KK_APP_NODE2VEC)
+            prepare_tables<Node2vecBatch<true>>(e);
+        else
+            prepare_tables<MetapathBatch<true>>(e);
     }
-    uint32_t *length = e->length.as<uint32_t>(plan.total);
-    uint32_t *path = want_paths ? e->path.as<uint32_t>(plan.total_cap) : nullptr;
-    KK_CUDA_CHECK(cudaEventRecord(e->ev[1], e->stream));
+}
+
+uint64_t run_batch(kk_engine *e, BatchPlan &plan, BatchSlot &slot, bool want_paths, bool prepared)
+{
+    for (int i = 0; i < 3; i++)
+        if (slot.ev[i] == nullptr)
+            KK_CUDA_CHECK(cudaEventCreate(&slot.ev[i]));
+    const uint8_t *vmask = nullptr;
+    if (!prepared && plan.app == KK_APP_NODE2VEC)
+        graph_sort_adjacency(e);
+    if (plan.app == KK_APP_METAPATH)
+    {
+        MetaSchemes *d_sc = slot.schemes.as<MetaSchemes>(plan.schemes.size());
+        KK_CUDA_CHECK(cudaMemcpyAsync(d_sc, plan.schemes.data(), plan.schemes.size() * sizeof(MetaSchemes),
+                                      cudaMemcpyHostToDevice, slot.stream));
+        for (size_t j = 0; j < plan.jobs.size(); j++)
+            plan.jobs[j].param = d_sc + j;
+        vmask = prepared ? (const uint8_t *)e->vmask.p : metapath_vertex_masks(e);
+    }
+    BatchJob *d_jobs = slot.jobs.as<BatchJob>(plan.jobs.size());
+    KK_CUDA_CHECK(cudaMemcpyAsync(d_jobs, plan.jobs.data(), plan.jobs.size() * sizeof(BatchJob),
+                                  cudaMemcpyHostToDevice, slot.stream));
+    int *d_status = (int *)slot.small.ensure(64);
+    unsigned long long *d_steps = (unsigned long long *)((char *)d_status + 16);
+    KK_CUDA_CHECK(cudaMemsetAsync(d_status, 0, 64, slot.stream));
+    KK_CUDA_CHECK(cudaEventRecord(slot.ev[0], slot.stream));
+    if (!prepared && slot.stream != e->stream)
+    {
+        /* tables are built on the engine's stream */
+        KK_CUDA_CHECK(cudaEventRecord(e->ev_fork, slot.stream));
+        KK_CUDA_CHECK(cudaStreamWaitEvent(e->stream, e->ev_fork, 0));
+    }
+    uint32_t *length = slot.length.as<uint32_t>(plan.total);
+    uint32_t *path = nullptr;
     const GraphView g = e->view();
+    const bool p = prepared;
     if (plan.app == KK_APP_DEEPWALK)
     {
         if (plan.weighted)
-            launch_batch(e, DeepWalkBatch<true>{e->d_w}, plan, d_jobs, alias, length, path, d_steps, d_status);
+            launch_batch(e, DeepWalkBatch<true>{e->d_w}, plan, slot, d_jobs, length, &path, d_steps, d_status,
+                         want_paths, p);
         else
-            launch_batch(e, DeepWalkBatch<false>{nullptr}, plan, d_jobs, alias, length, path, d_steps, d_status);
+            launch_batch(e, DeepWalkBatch<false>{nullptr}, plan, slot, d_jobs, length, &path, d_steps, d_status,
+                         want_paths, p);
     }
     else if (plan.app == KK_APP_NODE2VEC)
     {
         if (plan.weighted)
-            launch_batch(e, Node2vecBatch<true>{g.nbr, e->d_w}, plan, d_jobs, alias, length, path, d_steps, d_status);
+            launch_batch(e, Node2vecBatch<true>{g.nbr, e->d_w}, plan, slot, d_jobs, length, &path, d_steps,
+                         d_status, want_paths, p);
         else
-            launch_batch(e, Node2vecBatch<false>{g.nbr, nullptr}, plan, d_jobs, alias, length, path, d_steps,
-                         d_status);
+            launch_batch(e, Node2vecBatch<false>{g.nbr, nullptr}, plan, slot, d_jobs, length, &path, d_steps,
+                         d_status, want_paths, p);
     }
     else
     {
         if (plan.weighted)
-            launch_batch(e, MetapathBatch<true>{vmask, e->d_type, e->d_w}, plan, d_jobs, alias, length, path,
-                         d_steps, d_status);
+            launch_batch(e, MetapathBatch<true>{vmask, e->d_type, e->d_w}, plan, slot, d_jobs, length, &path,
+                         d_steps, d_status, want_paths, p);
         else
-            launch_batch(e, MetapathBatch<false>{vmask, e->d_type, nullptr}, plan, d_jobs, alias, length, path,
-                         d_steps, d_status);
+            launch_batch(e, MetapathBatch<false>{vmask, e->d_type, nullptr}, plan, slot, d_jobs, length, &path,
+                         d_steps, d_status, want_paths, p);
     }
-    KK_CUDA_CHECK(cudaEventRecord(e->ev[2], e->stream));
+    KK_CUDA_CHECK(cudaEventRecord(slot.ev[2], slot.stream));
     int h_small[8];
-    KK_CUDA_CHECK(cudaMemcpyAsync(h_small, d_status, sizeof(h_small), cudaMemcpyDeviceToHost, e->stream));
-    KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
-    KK_CUDA_CHECK(cudaEventElapsedTime(&e->alias_ms, e->ev[0], e->ev[1]));
-    KK_CUDA_CHECK(cudaEventElapsedTime(&e->walk_ms, e->ev[1], e->ev[2]));
+    KK_CUDA_CHECK(cudaMemcpyAsync(h_small, d_status, sizeof(h_small), cudaMemcpyDeviceToHost, slot.stream));
+    KK_CUDA_CHECK(cudaStreamSynchronize(slot.stream));
+    KK_CUDA_CHECK(cudaEventElapsedTime(&slot.alias_ms, slot.ev[0], slot.ev[1]));
+    KK_CUDA_CHECK(cudaEventElapsedTime(&slot.walk_ms, slot.ev[1], slot.ev[2]));
     if (h_small[0] == KK_STATUS_TRIAL_LIMIT)
         fail(KK_ERR_TRIAL_LIMIT, "a walker exceeded the rejection-trial limit");
     if (h_small[0] == KK_STATUS_PATH_CAPACITY)
         fail(KK_ERR_PATH_CAPACITY, "a walk exceeded its path capacity");
     unsigned long long steps;
     memcpy(&steps, (char *)h_small + 16, sizeof(steps));
-    *d_length = length;
-    *d_path = path;
     return steps;
 }
 
-} // namespace
 } // namespace kk
+
 
 using namespace kk;
 
@@ -188,14 +253,18 @@ kk_status kk_batch_walk_device(kk_engine *e, const kk_walk_opts *jobs, int n_job
         return KK_ERR_INVALID_CONFIG;
     return guard(e, [&] {
         BatchPlan plan = plan_batch(e, jobs, n_jobs);
-        uint32_t *len = nullptr, *path = nullptr;
-        uint64_t steps = run_batch(e, plan, &len, &path, d_vertices != nullptr);
+        BatchSlot &slot = e->bslot;
+        slot.stream = e->stream;
+        const bool want = d_vertices != nullptr;
+        uint64_t steps = run_batch(e, plan, slot, want, false);
+        e->alias_ms = slot.alias_ms;
+        e->walk_ms = slot.walk_ms;
         if (total_steps)
             *total_steps = steps;
         if (d_length)
-            *d_length = len;
+            *d_length = (const uint32_t *)slot.length.p;
         if (d_vertices)
-            *d_vertices = path;
+            *d_vertices = (const uint32_t *)slot.path.p;
     });
 }
 
@@ -207,8 +276,12 @@ kk_status kk_batch_walk(kk_engine *e, const kk_walk_opts *jobs, int n_jobs, kk_p
         out[j] = nullptr;
     kk_status s = guard(e, [&] {
         BatchPlan plan = plan_batch(e, jobs, n_jobs);
-        uint32_t *len = nullptr, *path = nullptr;
-        run_batch(e, plan, &len, &path, true);
+        BatchSlot &slot = e->bslot;
+        slot.stream = e->stream;
+        run_batch(e, plan, slot, true, false);
+        e->alias_ms = slot.alias_ms;
+        e->walk_ms = slot.walk_ms;
+        const uint32_t *len = (const uint32_t *)slot.length.p, *path = (const uint32_t *)slot.path.p;
         std::vector<uint32_t> h_len(plan.total + 1);
         KK_CUDA_CHECK(cudaMemcpy(h_len.data(), len, (size_t)plan.total * 4, cudaMemcpyDeviceToHost));
         for (int j = 0; j < n_jobs; j++)
@@ -235,10 +308,10 @@ kk_status kk_batch_walk(kk_engine *e, const kk_walk_opts *jobs, int n_jobs, kk_p
                 continue;
             WalkResult r;
             r.walker_num = b.walker_num;
-            r.length = len + b.first_task;
+            r.length = const_cast<uint32_t *>(len) + b.first_task;
             r.path_off = nullptr;
             r.cap = b.cap;
-            r.path = path + b.path_base;
+            r.path = const_cast<uint32_t *>(path) + b.path_base;
             r.total_steps = p->total_steps;
             uint64_t *d_off;
             uint32_t *d_verts;

@@ -37,7 +37,9 @@ void kk_engine::free_graph()
     E = 0;
     sorted = -1;
     order_valid = false;
-    n_hub = n_mid = n_nz = 0;
+    vcur_valid = false;
+    alias_cached = -1;
+    n_hub = n_warp = n_t32 = n_nz = 0;
     vmask_valid = false;
 }
 
@@ -107,6 +109,17 @@ void validate_opts(kk_engine *e, const kk_walk_opts *o, bool builtin)
         fail(KK_ERR_INVALID_CONFIG, "at most 2^31 walkers per call");
     if (o->walk_length >= 0xfffffff0u)
         fail(KK_ERR_INVALID_CONFIG, "walk_length too large");
+}
+
+/* The context's L2 fetch-granularity hint: v bytes, or the value found (0). */
+void set_l2_fetch(kk_engine *e, int v)
+{
+    if (v == e->l2_fetch)
+        return;
+    if (e->l2_fetch == 0)
+        KK_CUDA_CHECK(cudaDeviceGetLimit(&e->l2_fetch_saved, cudaLimitMaxL2FetchGranularity));
+    KK_CUDA_CHECK(cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, v == 0 ? e->l2_fetch_saved : (size_t)v));
+    e->l2_fetch = v;
 }
 
 /* Walkers per epoch: walker_num * rate, at least 1 (include/walk.hpp:706-709). */
@@ -283,12 +296,14 @@ void kk_engine_destroy(kk_engine *e)
     if (e == nullptr)
         return;
     cudaSetDevice(e->device);
+    if (e->l2_fetch != 0)
+        cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, e->l2_fetch_saved);
     if (e->stream)
         cudaStreamSynchronize(e->stream);
     e->free_graph();
     kk::DevBuf *bufs[] = {&e->alias, &e->sum, &e->ave, &e->ra, &e->scratch, &e->vmask,  &e->path,      &e->length,
                           &e->path_off, &e->caps, &e->start, &e->small, &e->cub_tmp, &e->packed, &e->packed_off,
-                          &e->schemes, &e->batch_jobs};
+                          &e->schemes};
     for (kk::DevBuf *b : bufs)
         b->release();
     for (int i = 0; i < 3; i++)
@@ -299,6 +314,8 @@ void kk_engine_destroy(kk_engine *e)
     if (e->ev_join)
         cudaEventDestroy(e->ev_join);
     e->order.release();
+    e->vcur.release();
+    e->bslot.release();
     if (e->side)
     {
         cudaStreamSynchronize(e->side);
@@ -331,6 +348,12 @@ kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value)
             e->walk_blocks_per_sm = (int)value;
         else if (n == "trial_limit" && value >= 1 && value <= 0xffffffffLL)
             e->trial_limit = (uint32_t)value;
+        else if (n == "alias_layout" && (value == 0 || value == 1))
+            e->alias_layout = (int)value;
+        else if (n == "alias_cache" && (value == 0 || value == 1))
+            e->alias_cache = (int)value;
+        else if (n == "l2_fetch_bytes" && (value == 0 || value == 32 || value == 64 || value == 128))
+            set_l2_fetch(e, (int)value);
         else
             fail(KK_ERR_INVALID_CONFIG, "unknown option or value out of range: " + n);
     });

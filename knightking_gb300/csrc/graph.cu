@@ -170,20 +170,36 @@ const uint32_t *vertex_order(kk_engine *e)
     KK_CUDA_CHECK(cub::DeviceRadixSort::SortPairsDescending(e->cub_tmp.ensure(bytes), bytes, deg, deg_sorted, ids,
                                                             order, (int64_t)V, 0, 32, e->stream));
     KK_CUDA_CHECK(cudaMemsetAsync(bounds, 0, 16, e->stream));
-    tier_bounds_kernel<<<grid_for(e, V, 256), 256, 0, e->stream>>>(deg_sorted, V, kAliasHubMin - 1, 0, bounds);
+    const TierThresholds thr{{kAliasHubMin - 1, kAliasThreadMax, kAliasThreadSmall, 0}};
+    tier_bounds_kernel<<<grid_for(e, V, 256), 256, 0, e->stream>>>(deg_sorted, V, thr, bounds);
     KK_CUDA_CHECK(cudaGetLastError());
-    uint32_t h[3];
-    KK_CUDA_CHECK(cudaMemcpyAsync(h, bounds, 12, cudaMemcpyDeviceToHost, e->stream));
+    uint32_t h[4];
+    KK_CUDA_CHECK(cudaMemcpyAsync(h, bounds, 16, cudaMemcpyDeviceToHost, e->stream));
     KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
     cudaFree(deg);
     cudaFree(deg_sorted);
     cudaFree(ids);
     cudaFree(bounds);
     e->n_hub = h[0];
-    e->n_mid = h[1];
-    e->n_nz = h[2];
+    e->n_warp = h[1];
+    e->n_t32 = h[2];
+    e->n_nz = h[3];
     e->order_valid = true;
     return order;
+}
+
+const uint64_t *vertex_cursors(kk_engine *e)
+{
+    uint64_t *cur = e->vcur.as<uint64_t>(e->V);
+    if (!e->vcur_valid)
+    {
+        if (e->E >= kCursorMaxEdges)
+            fail(KK_ERR_INVALID_CONFIG, "vertex cursors hold edge offsets below 2^40");
+        vertex_cursor_kernel<<<grid_for(e, e->V, 256), 256, 0, e->stream>>>(e->view(), cur);
+        KK_CUDA_CHECK(cudaGetLastError());
+        e->vcur_valid = true;
+    }
+    return cur;
 }
 
 const uint8_t *metapath_vertex_masks(kk_engine *e)
@@ -220,6 +236,7 @@ void graph_sort_adjacency(kk_engine *e)
         graph_check_sorted(e);
     if (e->sorted == 1)
         return;
+    e->alias_cached = -1; /* the tables follow the adjacency order */
     uint64_t E = e->E;
     uint32_t *nbr_out = nullptr, *idx_in = nullptr, *idx_out = nullptr;
     KK_CUDA_CHECK(cudaMalloc(&nbr_out, E * 4 + 4));

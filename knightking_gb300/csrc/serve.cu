@@ -1,0 +1,383 @@
+/*
+ * Serving: continuous batching of walk requests on resident tables.
+ *
+ * The server prepares once what every request of its app reads (sorted
+ * adjacency, vertex type masks, alias tables kept with the engine's
+ * alias_cache) and runs `slots` host threads, each driving one BatchSlot (its
+ * own CUDA stream and buffers).  A free slot takes the requests queued so far,
+ * first come first served, up to max_jobs and slot_bytes of walker paths and
+ * state, and runs them as one walk_batch_kernel launch; so requests that
+ * arrive while other batches are on the GPU start as soon as a slot frees up,
+ * and the slots' kernels overlap on the device.  Each request's walkers are
+ * keyed by its own seed and walker ids, so its paths are those of the request
+ * run alone.
+ */
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "knightking_gb300/engine.cuh"
+
+using namespace kk;
+
+namespace
+{
+typedef std::chrono::steady_clock Clock;
+
+struct Request
+{
+    uint64_t ticket;
+    kk_walk_opts opts;
+    uint64_t bytes;
+    Clock::time_point t_submit;
+};
+
+double ms_between(Clock::time_point a, Clock::time_point b)
+{
+    return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+/* Device bytes of a request in a slot: each walker's path slots and length. */
+uint64_t request_bytes(const kk_walk_opts &o)
+{
+    return (uint64_t)o.walker_num * (((uint64_t)o.walk_length + 1) * 4 + 4);
+}
+
+/* One job's paths from a finished batch, to the host, in the batch layout
+ * (walker i's vertices at offset i * (walk_length + 1)). */
+kk_paths *job_paths(const BatchJob &b, const uint32_t *h_len_all, const uint32_t *d_path, cudaStream_t st)
+{
+    kk_paths *p = (kk_paths *)calloc(1, sizeof(kk_paths));
+    if (!p)
+        fail(KK_ERR_OOM, "host allocation failed");
+    const uint32_t n = b.walker_num;
+    p->walker_num = n;
+    p->walker_begin = b.walker_begin;
+    p->epoch_walkers = n;
+    p->length = (uint32_t *)malloc((size_t)n * 4 + 4);
+    p->offset = (uint64_t *)malloc((size_t)n * 8 + 8);
+    p->vertices = (uint32_t *)malloc((size_t)n * b.cap * 4 + 4);
+    if (!p->length || !p->offset || !p->vertices)
+    {
+        kk_paths_free(p);
+        fail(KK_ERR_OOM, "host allocation failed");
+    }
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < n; i++)
+    {
+        p->length[i] = h_len_all[b.first_task + i];
+        p->offset[i] = (uint64_t)i * b.cap;
+        total += p->length[i];
+    }
+    p->total_steps = total - n;
+    if (n != 0)
+    {
+        cudaError_t err = cudaMemcpyAsync(p->vertices, d_path + b.path_base, (size_t)n * b.cap * 4,
+                                          cudaMemcpyDeviceToHost, st);
+        if (err != cudaSuccess)
+        {
+            kk_paths_free(p);
+            fail(KK_ERR_CUDA, std::string("path copy: ") + cudaGetErrorString(err));
+        }
+    }
+    return p;
+}
+
+} // namespace
+
+struct kk_server
+{
+    kk_engine *e = nullptr;
+    kk_serve_opts o;
+    std::mutex m;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Request> queue;
+    std::unordered_map<uint64_t, kk_serve_result> done;
+    uint64_t next_ticket = 1;
+    bool stopping = false;
+    int prev_alias_cache = 0;
+    std::vector<BatchSlot> slots;
+    std::vector<std::thread> threads;
+    /* statistics of completed requests */
+    std::vector<double> latencies;
+    uint64_t completed = 0, failed = 0, batches = 0, steps = 0, batch_jobs_sum = 0;
+};
+
+namespace
+{
+
+/* One slot's loop: take a batch of queued requests, run it, hand out results. */
+void slot_loop(kk_server *s, int k)
+{
+    cudaSetDevice(s->e->device);
+    BatchSlot &slot = s->slots[k];
+    for (;;)
+    {
+        std::vector<Request> batch;
+        {
+            std::unique_lock<std::mutex> lk(s->m);
+            s->cv_work.wait(lk, [&] { return s->stopping || !s->queue.empty(); });
+            if (s->queue.empty())
+                return; /* stopping, queue drained */
+            uint64_t bytes = 0;
+            while (!s->queue.empty() && batch.size() < s->o.max_jobs)
+            {
+                const Request &r = s->queue.front();
+                if (!batch.empty() && bytes + r.bytes > s->o.slot_bytes)
+                    break;
+                bytes += r.bytes;
+                batch.push_back(r);
+                s->queue.pop_front();
+            }
+        }
+        const Clock::time_point t_launch = Clock::now();
+        const size_t n = batch.size();
+        std::vector<kk_walk_opts> jobs(n);
+        for (size_t j = 0; j < n; j++)
+            jobs[j] = batch[j].opts;
+        std::vector<kk_paths *> paths(n, nullptr);
+        kk_status st = KK_OK;
+        uint64_t steps = 0;
+        try
+        {
+            BatchPlan plan = plan_batch(s->e, jobs.data(), (int)n);
+            steps = run_batch(s->e, plan, slot, true, true);
+            std::vector<uint32_t> h_len(plan.total + 1);
+            KK_CUDA_CHECK(cudaMemcpyAsync(h_len.data(), slot.length.p, (size_t)plan.total * 4,
+                                          cudaMemcpyDeviceToHost, slot.stream));
+            KK_CUDA_CHECK(cudaStreamSynchronize(slot.stream));
+            for (size_t j = 0; j < n; j++)
+                paths[j] = job_paths(plan.jobs[j], h_len.data(), (const uint32_t *)slot.path.p, slot.stream);
+            KK_CUDA_CHECK(cudaStreamSynchronize(slot.stream));
+        }
+        catch (const Error &x)
+        {
+            st = x.status;
+        }
+        catch (const std::bad_alloc &)
+        {
+            st = KK_ERR_OOM;
+        }
+        catch (...)
+        {
+            st = KK_ERR_CUDA;
+        }
+        if (st != KK_OK)
+            for (size_t j = 0; j < n; j++)
+            {
+                kk_paths_free(paths[j]);
+                paths[j] = nullptr;
+            }
+        const Clock::time_point t_done = Clock::now();
+        {
+            std::lock_guard<std::mutex> lk(s->m);
+            for (size_t j = 0; j < n; j++)
+            {
+                kk_serve_result r;
+                r.status = st;
+                r.paths = paths[j];
+                r.queue_ms = ms_between(batch[j].t_submit, t_launch);
+                r.latency_ms = ms_between(batch[j].t_submit, t_done);
+                r.batch_jobs = (uint32_t)n;
+                s->done[batch[j].ticket] = r;
+                if (st == KK_OK)
+                {
+                    s->completed++;
+                    s->latencies.push_back(r.latency_ms);
+                }
+                else
+                {
+                    s->failed++;
+                }
+            }
+            s->batches++;
+            s->batch_jobs_sum += n;
+            s->steps += steps;
+        }
+        s->cv_done.notify_all();
+    }
+}
+
+} // namespace
+
+extern "C" {
+
+kk_status kk_serve_start(kk_engine *e, const kk_serve_opts *opts, kk_server **out)
+{
+    if (!e || !opts || !out)
+        return KK_ERR_INVALID_CONFIG;
+    *out = nullptr;
+    kk_server *s = new (std::nothrow) kk_server();
+    if (!s)
+        return KK_ERR_OOM;
+    kk_status st = guard(e, [&] {
+        require_graph(e);
+        kk_serve_opts o = *opts;
+        if (o.app != KK_APP_DEEPWALK && o.app != KK_APP_NODE2VEC && o.app != KK_APP_METAPATH)
+            fail(KK_ERR_INVALID_CONFIG, "the server runs DeepWalk, node2vec or metapath requests");
+        if (o.weighted && e->d_w == nullptr)
+            fail(KK_ERR_INVALID_CONFIG, "weighted server on a graph without weights");
+        if (o.app == KK_APP_METAPATH && e->d_type == nullptr)
+            fail(KK_ERR_INVALID_CONFIG, "metapath needs edge types");
+        if (o.slots == 0)
+            o.slots = 2;
+        if (o.max_jobs == 0)
+            o.max_jobs = 256;
+        if (o.slot_bytes == 0)
+            o.slot_bytes = 1ull << 30;
+        if (o.slots < 1 || o.slots > 8 || o.max_jobs > kMaxBatchJobs)
+            fail(KK_ERR_INVALID_CONFIG, "slots 1..8, max_jobs 1..1024");
+        s->e = e;
+        s->o = o;
+        /* resident tables, built once on the engine's stream */
+        s->prev_alias_cache = e->alias_cache;
+        e->alias_cache = 1;
+        BatchPlan plan;
+        plan.app = o.app;
+        plan.weighted = o.weighted != 0;
+        batch_prepare(e, plan);
+        KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+        s->slots.resize(o.slots);
+        for (BatchSlot &sl : s->slots)
+            KK_CUDA_CHECK(cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking));
+        for (int k = 0; k < o.slots; k++)
+            s->threads.emplace_back(slot_loop, s, k);
+    });
+    if (st != KK_OK)
+    {
+        if (s->e)
+            e->alias_cache = s->prev_alias_cache;
+        for (BatchSlot &sl : s->slots)
+        {
+            if (sl.stream)
+                cudaStreamDestroy(sl.stream);
+            sl.release();
+        }
+        delete s;
+        return st;
+    }
+    *out = s;
+    return KK_OK;
+}
+
+kk_status kk_serve_submit(kk_server *s, const kk_walk_opts *req, uint64_t *ticket)
+{
+    if (!s || !req || !ticket)
+        return KK_ERR_INVALID_CONFIG;
+    if (req->app != s->o.app || (req->weighted != 0) != (s->o.weighted != 0))
+        return KK_ERR_INVALID_CONFIG;
+    if (req->start != nullptr || (req->rate != 0.0 && req->rate != 1.0))
+        return KK_ERR_INVALID_CONFIG;
+    if ((uint64_t)req->walker_begin + req->walker_num > 0x100000000ULL || req->walker_num > 0x80000000u ||
+        req->walk_length >= 0xfffffff0u)
+        return KK_ERR_INVALID_CONFIG;
+    if (req->app == KK_APP_NODE2VEC && !(req->p > 0.0f && req->q > 0.0f))
+        return KK_ERR_INVALID_CONFIG;
+    if (req->app == KK_APP_METAPATH)
+    {
+        if (req->n_schemes < 1 || req->n_schemes > KK_MAX_SCHEMES)
+            return KK_ERR_INVALID_CONFIG;
+        for (int i = 0; i < req->n_schemes; i++)
+            if (req->scheme_len[i] < 1 || req->scheme_len[i] > KK_MAX_SCHEME_LEN)
+                return KK_ERR_INVALID_CONFIG;
+    }
+    Request r;
+    r.opts = *req;
+    r.bytes = request_bytes(*req);
+    if (r.bytes > s->o.slot_bytes)
+        return KK_ERR_INVALID_CONFIG;
+    r.t_submit = Clock::now();
+    {
+        std::lock_guard<std::mutex> lk(s->m);
+        if (s->stopping)
+            return KK_ERR_INVALID_CONFIG;
+        r.ticket = s->next_ticket++;
+        s->queue.push_back(r);
+    }
+    *ticket = r.ticket;
+    s->cv_work.notify_one();
+    return KK_OK;
+}
+
+kk_status kk_serve_poll(kk_server *s, uint64_t ticket, int timeout_ms, kk_serve_result *out)
+{
+    if (!s || !out || ticket == 0)
+        return KK_ERR_INVALID_CONFIG;
+    std::unique_lock<std::mutex> lk(s->m);
+    if (ticket >= s->next_ticket)
+        return KK_ERR_INVALID_CONFIG;
+    auto ready = [&] { return s->done.count(ticket) != 0; };
+    if (timeout_ms < 0)
+        s->cv_done.wait(lk, ready);
+    else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready))
+        return KK_ERR_TIMEOUT;
+    *out = s->done[ticket];
+    s->done.erase(ticket);
+    return KK_OK;
+}
+
+kk_status kk_serve_stats_get(kk_server *s, kk_serve_stats *out)
+{
+    if (!s || !out)
+        return KK_ERR_INVALID_CONFIG;
+    std::lock_guard<std::mutex> lk(s->m);
+    memset(out, 0, sizeof(*out));
+    out->completed = s->completed;
+    out->failed = s->failed;
+    out->batches = s->batches;
+    out->walker_steps = s->steps;
+    out->mean_batch_jobs = s->batches ? (double)s->batch_jobs_sum / (double)s->batches : 0.0;
+    if (!s->latencies.empty())
+    {
+        std::vector<double> l = s->latencies;
+        std::sort(l.begin(), l.end());
+        auto pct = [&](double q) {
+            size_t i = (size_t)(q * (double)(l.size() - 1) + 0.5);
+            return l[i < l.size() ? i : l.size() - 1];
+        };
+        out->p50_ms = pct(0.50);
+        out->p99_ms = pct(0.99);
+        double sum = 0.0;
+        for (double x : l)
+            sum += x;
+        out->mean_ms = sum / (double)l.size();
+    }
+    return KK_OK;
+}
+
+kk_status kk_serve_stop(kk_server *s)
+{
+    if (!s)
+        return KK_ERR_INVALID_CONFIG;
+    {
+        std::lock_guard<std::mutex> lk(s->m);
+        s->stopping = true;
+    }
+    s->cv_work.notify_all();
+    for (std::thread &t : s->threads)
+        t.join();
+    for (BatchSlot &sl : s->slots)
+    {
+        if (sl.stream)
+        {
+            cudaStreamSynchronize(sl.stream);
+            cudaStreamDestroy(sl.stream);
+        }
+        sl.release();
+    }
+    for (auto &kv : s->done)
+        kk_paths_free(kv.second.paths);
+    s->e->alias_cache = s->prev_alias_cache;
+    delete s;
+    return KK_OK;
+}
+
+} /* extern "C" */

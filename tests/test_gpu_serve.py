@@ -1,0 +1,93 @@
+"""Serving (kk_serve_*): continuous batching of requests from several client
+threads on two slots.  Every request's paths equal those of the same request
+run alone through kk_walk (bit-identical), whatever else shared its batch and
+whichever slot ran it; the server reports its latency statistics."""
+
+import threading
+
+import numpy as np
+import pytest
+
+from oracle import graphs as G
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def engine():
+    import knightking_gb300 as kk
+    e = kk.WalkEngine(0)
+    yield e
+    e.close()
+
+
+def _load(engine, seed, types=False):
+    g = G.random_undirected(600, 8000, seed=seed, weight="unif", types="uniform" if types else None)
+    csr = G.csr_file_order(600, g["src"], g["dst"], w=g.get("w"), type=g.get("type"))
+    engine.load_arrays(600, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
+
+
+def _requests(app, n, seed):
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(n):
+        r = dict(walker_num=int(np.clip(rng.lognormal(np.log(64), 1.0), 1, 2000)), seed=int(rng.integers(1, 2**40)),
+                 walk_length=int(rng.integers(5, 120)), walker_begin=int(rng.integers(0, 1 << 20)))
+        if app == "node2vec":
+            r["p"] = float(np.exp(rng.uniform(np.log(0.25), np.log(4))))
+            r["q"] = float(np.exp(rng.uniform(np.log(0.25), np.log(4))))
+        if app == "metapath":
+            r["schemes"] = [[1 << int(t) for t in rng.integers(0, 5, int(rng.integers(1, 5)))] for _ in range(3)]
+        reqs.append(r)
+    return reqs
+
+
+def _serve_all(engine, app, reqs, clients=4, **server_kw):
+    results = [None] * len(reqs)
+    srv = engine.serve(app, **server_kw)
+    try:
+        def client(k):
+            tickets = [(i, srv.submit(**reqs[i])) for i in range(k, len(reqs), clients)]
+            for i, t in tickets:
+                results[i] = srv.poll(t)
+        th = [threading.Thread(target=client, args=(k,)) for k in range(clients)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        stats = srv.stats()
+    finally:
+        srv.stop()
+    return results, stats
+
+
+@pytest.mark.parametrize("app", ["node2vec", "deepwalk", "metapath"])
+def test_served_requests_equal_alone(engine, app):
+    _load(engine, 11, types=app == "metapath")
+    reqs = _requests(app, 60, seed=5)
+    results, stats = _serve_all(engine, app, reqs, slots=2, max_jobs=16, slot_bytes=8 << 20)
+    assert stats["completed"] == len(reqs) and stats["failed"] == 0
+    assert stats["batches"] >= 2
+    assert stats["p99_ms"] >= stats["p50_ms"] > 0
+    for r, res in zip(reqs, results):
+        assert res.status == 0
+        kw = dict(r)
+        alone = engine.walk(app, kw.pop("walker_num"), **kw)
+        np.testing.assert_array_equal(res.paths.path_length, alone.path_length)
+        np.testing.assert_array_equal(res.paths.vertices, alone.vertices)
+        assert res.paths.total_steps == alone.total_steps
+        assert res.latency_ms >= res.queue_ms >= 0
+
+
+def test_server_refuses_bad_requests(engine):
+    import knightking_gb300 as kk
+    _load(engine, 12)
+    with engine.serve("node2vec", slots=1, max_jobs=4, slot_bytes=1 << 20) as srv:
+        with pytest.raises(kk.KKError):
+            srv.submit(100000, walk_length=80, p=1.0, q=1.0)      # larger than a slot
+        with pytest.raises(kk.KKError):
+            srv.submit(10, walk_length=80, p=0.0, q=1.0)           # p must be > 0
+        t = srv.submit(10, walk_length=10, p=1.0, q=2.0)
+        assert srv.poll(t).status == 0
+        with pytest.raises(kk.KKError):
+            srv.poll(t)                                             # handed out once

@@ -360,29 +360,12 @@ def run_ours(args, wl, world, rank, local):
         steps, _, _, _ = engine.walk_device(app, walkers, paths="unpacked", seed=1, walker_begin=walker_begin, **kw)
         return steps
 
-    # warm-up; it also tunes the engine by the event time of alias build +
-    # walk: the alias-table layout (cursor vs index buckets), the context's L2
-    # fetch-granularity hint, then the walk schedule (one walker per thread vs
-    # the persistent walker pool)
-    def measure(sched, layout, l2):
-        engine.set_option("walk_schedule", sched)
-        engine.set_option("alias_layout", layout)
-        engine.set_option("l2_fetch_bytes", l2)
-        step()
-        step()
-        return sum(engine.last_timing()[:2])
-
-    schedule_ms = {}
-    layouts = (0, 1) if wl["weights"] else (0,)
-    for layout in layouts:
-        for l2 in (0, 32, 64):
-            schedule_ms[(0, layout, l2)] = measure(0, layout, l2)
-    _, best_layout, best_l2 = min(schedule_ms, key=schedule_ms.get)
-    schedule_ms[(1, best_layout, best_l2)] = measure(1, best_layout, best_l2)
-    best_schedule, best_layout, best_l2 = min(schedule_ms, key=schedule_ms.get)
-    engine.set_option("walk_schedule", best_schedule)
-    engine.set_option("alias_layout", best_layout)
-    engine.set_option("l2_fetch_bytes", best_l2)
+    # warm-up; it also runs the engine's autotuner (knightking_gb300.tuning):
+    # alias-table layout, node2vec adjacency test, walk block size, L2 fetch
+    # hint and walk schedule, each picked by the event time of alias build + walk
+    from knightking_gb300 import tuning
+    best, tune_table = tuning.autotune(engine, step, tuning.space_for(app, bool(wl["weights"])))
+    best_schedule = best.get("walk_schedule", 0)
     for _ in range(args.warmup):
         step()
     barrier(world)
@@ -469,12 +452,8 @@ def run_ours(args, wl, world, rank, local):
                        "walkers_per_gpu": walkers, "walker_steps_per_step": steps_per_launch,
                        "l2": "inputs larger than L2 (graph + alias tables > 129 MB)", "parallelism": "replicas",
                        "walk_schedule": "pool" if best_schedule == 1 else "one walker per thread",
-                       "alias_layout": "cursor buckets" if best_layout == 0 else "index buckets",
-                       "l2_fetch_bytes": best_l2 or "default",
-                       "step_ms_by_choice": {("per_thread" if k[0] == 0 else "pool") + "/" +
-                                             ("cursor" if k[1] == 0 else "index") + "/l2fetch=" +
-                                             (str(k[2]) if k[2] else "default"): v
-                                             for k, v in schedule_ms.items()}},
+                       "tuned": best,
+                       "tuning_ms": [[cfg, ms] for cfg, ms in tune_table]},
             "e2e": {"value": e2e_value, "unit": "walker-steps/s", "h2d_bytes_per_step": walkers * 4 + 256,
                     "d2h_bytes_per_step": d2h // e2e_runs},
             "gpu_launches": 2 * args.steps if wl["weights"] else args.steps,

@@ -101,7 +101,16 @@ kk_status kk_engine_set_stream(kk_engine *e, void *stream);
  * (include/constants.hpp:27-46):
  *   "walk_schedule"      0 one walker per thread (default), 1 persistent walker pool
  *   "walk_blocks_per_sm" pool blocks per SM, 0 = as many as fit (default)
- *   "trial_limit"        rejection trials per step before KK_ERR_TRIAL_LIMIT (default 2^24) */
+ *   "walk_block"         threads per block of the walk kernels, 32..256 step 32 (default 256)
+ *   "trial_limit"        rejection trials per step before KK_ERR_TRIAL_LIMIT (default 2^24)
+ *   "alias_layout"       0 cursor buckets where no hook reads the taken edge's index
+ *                        (a step reads one 32 B bucket), 1 index buckets always
+ *   "alias_cache"        1 keeps the built-in apps' edge-weight alias tables across calls
+ *                        (the reference rebuilds them per call; the tables are the same)
+ *   "node2vec_adjacency" 0 edge-set lookup (built once per graph), 1 binary search of the
+ *                        sorted adjacency, as node2vec.hpp:159-166
+ *   "l2_fetch_bytes"     the context's cudaLimitMaxL2FetchGranularity while the engine
+ *                        lives: 32, 64, 128, or 0 for the value found (restored on destroy) */
 kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value);
 /* Message of the last failed call on this engine ("" if none). */
 const char *kk_last_error(const kk_engine *e);

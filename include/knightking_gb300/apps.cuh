@@ -95,13 +95,22 @@ struct Node2vecPostQuery
     }
 };
 
-/* respond_query: std::binary_search of the candidate in N(previous) (node2vec.hpp:159-166) */
+/* respond_query: whether the candidate is in N(previous), the result of
+ * node2vec.hpp:159-166's std::binary_search over the sorted adjacency; looked
+ * up in the edge set when the engine has one (same answer, one sector). */
 struct Node2vecRespond
 {
     const uint32_t *nbr;
-    __device__ __forceinline__ void operator()(vertex_id_t, const vertex_id_t &query, const AdjList &adj,
+    EdgeSetView set;
+    __device__ __forceinline__ bool needs_adjacency() const { return set.slots == nullptr; }
+    __device__ __forceinline__ void operator()(vertex_id_t target, const vertex_id_t &query, const AdjList &adj,
                                                bool &resp) const
     {
+        if (set.slots != nullptr)
+        {
+            resp = edge_set_contains(set, target, query);
+            return;
+        }
         uint32_t deg = adj.degree();
         uint32_t i = lower_bound_adj(nbr, adj.begin, deg, query);
         resp = i < deg && gather(nbr + adj.begin + i) == query;
@@ -304,6 +313,7 @@ struct Node2vecBatch
         TC;
     const uint32_t *nbr;
     const float *w;
+    EdgeSetView set;
     __device__ __forceinline__ void make(const BatchJob &j, WC &wc, TC &tc) const
     {
         wc.walker_num = j.walker_num;
@@ -311,7 +321,7 @@ struct Node2vecBatch
         if constexpr (Weighted)
             tc.static_comp = WeightStatic{w};
         tc.post_query = Node2vecPostQuery{};
-        tc.respond_query = Node2vecRespond{nbr};
+        tc.respond_query = Node2vecRespond{nbr, set};
         tc.dynamic_comp = Node2vecDyn{j.c[0], j.c[3], j.c[4]};
         tc.dcomp_upperbound = ConstBound{j.c[0]};
         tc.dcomp_lowerbound = ConstBound{j.c[1]};

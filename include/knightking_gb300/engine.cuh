@@ -155,6 +155,12 @@ struct kk_engine
     bool order_valid = false;
     kk::DevBuf vcur; /* vertex cursors (begin | degree << 40), cached per graph */
     bool vcur_valid = false;
+    /* node2vec adjacency test: 0 edge set (built once per graph), 1 binary
+     * search of the sorted adjacency (option node2vec_adjacency) */
+    int n2v_adjacency = 0;
+    kk::DevBuf edge_set;
+    uint64_t edge_set_mask = 0;
+    bool edge_set_valid = false;
     kk::DevBuf schemes;    /* metapath schemes of the running job */
     kk::BatchSlot bslot;   /* where the synchronous batch calls run */
     bool vmask_valid = false;
@@ -168,6 +174,9 @@ struct kk_engine
      * blocks per SM (0 = as many as fit) */
     int walk_schedule = 0;
     int walk_blocks_per_sm = 0;
+    /* threads per block of the one-walker-per-thread and batch walk kernels
+     * (option walk_block: 32..256, a multiple of 32) */
+    int walk_block = 256;
     /* alias-table layout: 0 cursor buckets where the hooks allow them, 1 index
      * buckets always */
     int alias_layout = 0;
@@ -250,6 +259,11 @@ const uint32_t *vertex_order(kk_engine *e);
 
 /* Vertex cursors, cached per graph. */
 const uint64_t *vertex_cursors(kk_engine *e);
+
+/* The edge set the node2vec adjacency test reads (cached per graph), or an
+ * empty view when the engine's node2vec_adjacency option asks for binary
+ * search. */
+EdgeSetView node2vec_edge_set(kk_engine *e);
 
 /* Per-vertex OR of 1 << edge type (metapath.hpp:77-88), cached per graph. */
 const uint8_t *metapath_vertex_masks(kk_engine *e);
@@ -433,7 +447,8 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
     KK_CUDA_CHECK(cudaEventRecord(e->ev[1], e->stream));
     if (e->walk_schedule == 0)
     {
-        walk_static_kernel<S, WC, TC, Bucket><<<grid_for(e, n, 256), 256, 0, e->stream>>>(g, wc, tc, alias, ra, L);
+        const unsigned bs = (unsigned)e->walk_block;
+        walk_static_kernel<S, WC, TC, Bucket><<<grid_for(e, n, bs), bs, 0, e->stream>>>(g, wc, tc, alias, ra, L);
     }
     else
     {

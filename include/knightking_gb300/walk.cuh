@@ -106,6 +106,95 @@ struct SecondOrderTransitionConfig
     OutSearch outlier_search;
 };
 
+/* ---- edge set ---------------------------------------------------------------
+ * Exact membership of directed edges (u, v): open addressing over 32 B
+ * buckets of four 64-bit keys u << 32 | v, linear probing bucket by bucket,
+ * a power-of-two bucket count with load at most 1/2.  Keys only ever go from
+ * empty to filled and an insert moves past a bucket only when all four slots
+ * hold other keys, so a lookup that meets an empty slot may stop.  A lookup
+ * reads one 32 B sector in the common case, where a binary search of a sorted
+ * adjacency reads about log2(degree) dependent sectors. */
+constexpr uint64_t kEdgeSetEmpty = ~0ull;
+
+struct EdgeSetView
+{
+    const uint64_t *slots; /* 4 * (bucket_mask + 1) keys; nullptr: no set */
+    uint64_t bucket_mask;
+};
+
+/* splitmix64 finalizer (Steele, Lea, Flood, OOPSLA 2014) */
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t x)
+{
+    x ^= x >> 30;
+    x *= 0xbf58476d1ce4e5b9ull;
+    x ^= x >> 27;
+    x *= 0x94d049bb133111ebull;
+    x ^= x >> 31;
+    return x;
+}
+
+__device__ __forceinline__ bool edge_set_contains(const EdgeSetView &s, vertex_id_t u, vertex_id_t v)
+{
+    const uint64_t key = ((uint64_t)u << 32) | v;
+    uint64_t b = mix64(key) & s.bucket_mask;
+    for (uint64_t probe = 0; probe <= s.bucket_mask; probe++)
+    {
+        const uint4 *p = reinterpret_cast<const uint4 *>(s.slots + b * 4);
+        const uint4 x = __ldg(p), y = __ldg(p + 1);
+        const uint64_t k0 = ((uint64_t)x.y << 32) | x.x, k1 = ((uint64_t)x.w << 32) | x.z;
+        const uint64_t k2 = ((uint64_t)y.y << 32) | y.x, k3 = ((uint64_t)y.w << 32) | y.z;
+        if (k0 == key || k1 == key || k2 == key || k3 == key)
+            return true;
+        if (k0 == kEdgeSetEmpty || k1 == kEdgeSetEmpty || k2 == kEdgeSetEmpty || k3 == kEdgeSetEmpty)
+            return false;
+        b = (b + 1) & s.bucket_mask;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void edge_set_insert(uint64_t *slots, uint64_t bucket_mask, vertex_id_t u, vertex_id_t v)
+{
+    const uint64_t key = ((uint64_t)u << 32) | v;
+    uint64_t b = mix64(key) & bucket_mask;
+    for (uint64_t probe = 0; probe <= bucket_mask; probe++)
+    {
+        for (int j = 0; j < 4; j++)
+        {
+            const unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long *>(slots + b * 4 + j),
+                                                     (unsigned long long)kEdgeSetEmpty, (unsigned long long)key);
+            if (old == kEdgeSetEmpty || old == key)
+                return;
+        }
+        b = (b + 1) & bucket_mask;
+    }
+}
+
+/* Inserts the out-edges of the vertices order[lo, hi): a block per vertex
+ * (hubs) or a warp per vertex. */
+static __global__ void edge_set_block_kernel(GraphView g, uint64_t *slots, uint64_t mask, const uint32_t *order,
+                                             uint32_t lo, uint32_t hi)
+{
+    for (uint32_t k = lo + blockIdx.x; k < hi; k += gridDim.x)
+    {
+        const uint32_t v = order[k];
+        for (int64_t e = g.off[v] + threadIdx.x; e < g.off[v + 1]; e += blockDim.x)
+            edge_set_insert(slots, mask, v, g.nbr[e]);
+    }
+}
+
+static __global__ void edge_set_warp_kernel(GraphView g, uint64_t *slots, uint64_t mask, const uint32_t *order,
+                                            uint32_t lo, uint32_t hi)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t k = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); k < hi; k += nwarps)
+    {
+        const uint32_t v = order[k];
+        for (int64_t e = g.off[v] + lane; e < g.off[v + 1]; e += 32)
+            edge_set_insert(slots, mask, v, g.nbr[e]);
+    }
+}
+
 /* ---- vertex cursors --------------------------------------------------------
  * A vertex's adjacency position packed in 64 bits: begin offset in the low 40
  * bits, degree in the high 24 (kCursorDegMax means "this or more": the degree
@@ -793,6 +882,25 @@ __device__ __forceinline__ vertex_id_t walker_start(const GraphView &g, const WC
     return v;
 }
 
+/* Whether a respond_query hook reads the target's adjacency: hooks may say
+ * so per call with `bool needs_adjacency() const`; others always get it. */
+template <typename F, typename = void>
+struct has_needs_adjacency : std::false_type
+{
+};
+template <typename F>
+struct has_needs_adjacency<F, std::void_t<decltype(std::declval<const F &>().needs_adjacency())>> : std::true_type
+{
+};
+template <typename F>
+__device__ __forceinline__ bool respond_needs_adjacency(const F &f)
+{
+    if constexpr (has_needs_adjacency<F>::value)
+        return f.needs_adjacency();
+    else
+        return true;
+}
+
 /* A picked candidate: index local to the adjacency (kNone when the bucket
  * does not carry it), neighbour, and the neighbour's cursor when the bucket
  * carries one (has_cur). */
@@ -1061,8 +1169,13 @@ __device__ __forceinline__ bool walk_step(const GraphView &g, const WC &wc, cons
                 vertex_id_t target = 0;
                 if (tc.post_query(w, v, cu, target, query))
                 {
-                    const Pos tp = (target == run.pv && run.ppos.e0 >= 0) ? run.ppos : pos_from_offsets(g, target);
-                    const AdjList tadj{(edge_id_t)tp.e0, (edge_id_t)(tp.e0 + tp.deg)};
+                    AdjList tadj{0, 0};
+                    if (respond_needs_adjacency(tc.respond_query))
+                    {
+                        const Pos tp =
+                            (target == run.pv && run.ppos.e0 >= 0) ? run.ppos : pos_from_offsets(g, target);
+                        tadj = AdjList{(edge_id_t)tp.e0, (edge_id_t)(tp.e0 + tp.deg)};
+                    }
                     tc.respond_query(target, query, tadj, resp);
                 }
                 accepted = randval <= tc.dynamic_comp(w, resp, v, cu);

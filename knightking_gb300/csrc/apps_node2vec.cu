@@ -14,7 +14,8 @@ namespace
 {
 
 template <bool Weighted, bool Outlier>
-void run_n2v(kk_engine *e, const kk_walk_opts &o, const Node2vecConstants &c, const RunSpec &rs, WalkResult &res)
+void run_n2v(kk_engine *e, const kk_walk_opts &o, const Node2vecConstants &c, const RunSpec &rs, WalkResult &res,
+             EdgeSetView set)
 {
     typedef typename std::conditional<Weighted, WeightStatic, NoHook>::type StaticT;
     typedef typename std::conditional<Outlier, Node2vecOutlierUB<Weighted>, NoHook>::type OutUBT;
@@ -27,7 +28,7 @@ void run_n2v(kk_engine *e, const kk_walk_opts &o, const Node2vecConstants &c, co
     if constexpr (Weighted)
         tc.static_comp = WeightStatic{e->d_w};
     tc.post_query = Node2vecPostQuery{};
-    tc.respond_query = Node2vecRespond{e->d_nbr};
+    tc.respond_query = Node2vecRespond{e->d_nbr, set};
     tc.dynamic_comp = Node2vecDyn{c.upperbound, c.inv_p, c.inv_q};
     tc.dcomp_upperbound = ConstBound{c.upperbound};
     tc.dcomp_lowerbound = ConstBound{c.lowerbound};
@@ -54,19 +55,20 @@ void run_app_node2vec(kk_engine *e, const kk_walk_opts &o, const RunSpec &rs0, W
     rs.fixed_cap = true;
     rs.cap = o.walk_length + 1;
     Node2vecConstants c = Node2vecConstants::make(o.p, o.q);
+    const EdgeSetView set = node2vec_edge_set(e);
     if (o.weighted)
     {
         if (c.outlier)
-            run_n2v<true, true>(e, o, c, rs, res);
+            run_n2v<true, true>(e, o, c, rs, res, set);
         else
-            run_n2v<true, false>(e, o, c, rs, res);
+            run_n2v<true, false>(e, o, c, rs, res, set);
     }
     else
     {
         if (c.outlier)
-            run_n2v<false, true>(e, o, c, rs, res);
+            run_n2v<false, true>(e, o, c, rs, res, set);
         else
-            run_n2v<false, false>(e, o, c, rs, res);
+            run_n2v<false, false>(e, o, c, rs, res, set);
     }
 }
 

@@ -100,7 +100,8 @@ void launch_batch_with(kk_engine *e, const App &app, const BatchPlan &plan, Batc
     }
     *path = want_paths ? slot.path.as<uint32_t>(plan.total_cap) : nullptr;
     KK_CUDA_CHECK(cudaEventRecord(slot.ev[1], slot.stream));
-    walk_batch_kernel<typename App::S, App, Bucket><<<grid_for(e, plan.total, 256), 256, 0, slot.stream>>>(
+    const unsigned bs = (unsigned)e->walk_block;
+    walk_batch_kernel<typename App::S, App, Bucket><<<grid_for(e, plan.total, bs), bs, 0, slot.stream>>>(
         e->view(), app, d_jobs, (uint32_t)plan.jobs.size(), plan.total, alias, (const float *)e->sum.p, *path, length,
         steps, status, e->trial_limit);
     KK_CUDA_CHECK(cudaGetLastError());
@@ -149,7 +150,10 @@ void prepare_tables(kk_engine *e)
 void batch_prepare(kk_engine *e, const BatchPlan &plan)
 {
     if (plan.app == KK_APP_NODE2VEC)
+    {
         graph_sort_adjacency(e);
+        node2vec_edge_set(e);
+    }
     if (plan.app == KK_APP_METAPATH)
         metapath_vertex_masks(e);
     if (plan.weighted)
@@ -208,11 +212,15 @@ uint64_t run_batch(kk_engine *e, BatchPlan &plan, BatchSlot &slot, bool want_pat
     }
     else if (plan.app == KK_APP_NODE2VEC)
     {
+        const EdgeSetView set = p ? e->n2v_adjacency == 0 ? EdgeSetView{(const uint64_t *)e->edge_set.p,
+                                                                         e->edge_set_mask}
+                                                           : EdgeSetView{nullptr, 0}
+                                  : node2vec_edge_set(e);
         if (plan.weighted)
-            launch_batch(e, Node2vecBatch<true>{g.nbr, e->d_w}, plan, slot, d_jobs, length, &path, d_steps,
+            launch_batch(e, Node2vecBatch<true>{g.nbr, e->d_w, set}, plan, slot, d_jobs, length, &path, d_steps,
                          d_status, want_paths, p);
         else
-            launch_batch(e, Node2vecBatch<false>{g.nbr, nullptr}, plan, slot, d_jobs, length, &path, d_steps,
+            launch_batch(e, Node2vecBatch<false>{g.nbr, nullptr, set}, plan, slot, d_jobs, length, &path, d_steps,
                          d_status, want_paths, p);
     }
     else

@@ -38,6 +38,7 @@ void kk_engine::free_graph()
     sorted = -1;
     order_valid = false;
     vcur_valid = false;
+    edge_set_valid = false;
     alias_cached = -1;
     n_hub = n_warp = n_t32 = n_nz = 0;
     vmask_valid = false;
@@ -315,6 +316,7 @@ void kk_engine_destroy(kk_engine *e)
         cudaEventDestroy(e->ev_join);
     e->order.release();
     e->vcur.release();
+    e->edge_set.release();
     e->bslot.release();
     if (e->side)
     {
@@ -354,6 +356,10 @@ kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value)
             e->alias_cache = (int)value;
         else if (n == "l2_fetch_bytes" && (value == 0 || value == 32 || value == 64 || value == 128))
             set_l2_fetch(e, (int)value);
+        else if (n == "node2vec_adjacency" && (value == 0 || value == 1))
+            e->n2v_adjacency = (int)value;
+        else if (n == "walk_block" && value >= 32 && value <= 256 && value % 32 == 0)
+            e->walk_block = (int)value;
         else
             fail(KK_ERR_INVALID_CONFIG, "unknown option or value out of range: " + n);
     });

@@ -202,6 +202,37 @@ const uint64_t *vertex_cursors(kk_engine *e)
     return cur;
 }
 
+EdgeSetView node2vec_edge_set(kk_engine *e)
+{
+    if (e->n2v_adjacency != 0)
+        return EdgeSetView{nullptr, 0};
+    if (!e->edge_set_valid)
+    {
+        uint64_t nb = 1;
+        while (nb * 4 < 2 * e->E)
+            nb <<= 1;
+        uint64_t *slots = e->edge_set.as<uint64_t>(nb * 4);
+        KK_CUDA_CHECK(cudaMemsetAsync(slots, 0xff, nb * 4 * sizeof(uint64_t), e->stream));
+        const uint32_t *order = vertex_order(e);
+        const GraphView g = e->view();
+        if (e->n_hub)
+        {
+            const unsigned grid = e->n_hub < 4u * e->sm_count ? e->n_hub : 4u * e->sm_count;
+            edge_set_block_kernel<<<grid, 1024, 0, e->stream>>>(g, slots, nb - 1, order, 0, e->n_hub);
+            KK_CUDA_CHECK(cudaGetLastError());
+        }
+        if (e->n_nz > e->n_hub)
+        {
+            edge_set_warp_kernel<<<grid_for(e, (uint64_t)(e->n_nz - e->n_hub) * 32, 256), 256, 0, e->stream>>>(
+                g, slots, nb - 1, order, e->n_hub, e->n_nz);
+            KK_CUDA_CHECK(cudaGetLastError());
+        }
+        e->edge_set_mask = nb - 1;
+        e->edge_set_valid = true;
+    }
+    return EdgeSetView{(const uint64_t *)e->edge_set.p, e->edge_set_mask};
+}
+
 const uint8_t *metapath_vertex_masks(kk_engine *e)
 {
     uint8_t *vmask = e->vmask.as<uint8_t>(e->V);

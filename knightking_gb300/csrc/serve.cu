@@ -22,6 +22,7 @@
 #include <mutex>
 #include <thread>
 #include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "knightking_gb300/engine.cuh"
@@ -101,6 +102,7 @@ struct kk_server
     std::condition_variable cv_work, cv_done;
     std::deque<Request> queue;
     std::unordered_map<uint64_t, kk_serve_result> done;
+    std::unordered_set<uint64_t> pending; /* submitted, result not yet handed out */
     uint64_t next_ticket = 1;
     bool stopping = false;
     int prev_alias_cache = 0;
@@ -301,6 +303,7 @@ kk_status kk_serve_submit(kk_server *s, const kk_walk_opts *req, uint64_t *ticke
             return KK_ERR_INVALID_CONFIG;
         r.ticket = s->next_ticket++;
         s->queue.push_back(r);
+        s->pending.insert(r.ticket);
     }
     *ticket = r.ticket;
     s->cv_work.notify_one();
@@ -312,8 +315,8 @@ kk_status kk_serve_poll(kk_server *s, uint64_t ticket, int timeout_ms, kk_serve_
     if (!s || !out || ticket == 0)
         return KK_ERR_INVALID_CONFIG;
     std::unique_lock<std::mutex> lk(s->m);
-    if (ticket >= s->next_ticket)
-        return KK_ERR_INVALID_CONFIG;
+    if (s->pending.count(ticket) == 0)
+        return KK_ERR_INVALID_CONFIG; /* never submitted, or already handed out */
     auto ready = [&] { return s->done.count(ticket) != 0; };
     if (timeout_ms < 0)
         s->cv_done.wait(lk, ready);
@@ -321,6 +324,7 @@ kk_status kk_serve_poll(kk_server *s, uint64_t ticket, int timeout_ms, kk_serve_
         return KK_ERR_TIMEOUT;
     *out = s->done[ticket];
     s->done.erase(ticket);
+    s->pending.erase(ticket);
     return KK_OK;
 }
 

@@ -1,0 +1,56 @@
+"""Autotuner of the engine's speed options.
+
+The options (kk_engine_set_option) never change a path, only how fast it is
+produced: alias-table layout, node2vec adjacency test, walk block size, the
+context's L2 fetch-granularity hint and the walk schedule.  The tuner runs a
+caller-supplied step (one walk call on the real workload) under candidate
+settings and keeps, option by option, the value with the shortest alias-build
+plus walk time as the engine's CUDA events measure it (greedy coordinate
+descent: each option in turn, the others held at their best so far).
+"""
+
+DEFAULT_SPACE = (
+    ("alias_layout", (0, 1)),
+    ("node2vec_adjacency", (0, 1)),
+    ("walk_block", (256, 128, 64)),
+    ("l2_fetch_bytes", (0, 64)),
+    ("walk_schedule", (0, 1)),
+)
+
+
+def space_for(app, weighted):
+    """The options that matter for a built-in app: the alias layout only with
+    alias tables, the adjacency test only for node2vec."""
+    out = []
+    for name, vals in DEFAULT_SPACE:
+        if name == "alias_layout" and not weighted:
+            continue
+        if name == "node2vec_adjacency" and app != "node2vec":
+            continue
+        out.append((name, vals))
+    return tuple(out)
+
+
+def autotune(engine, step, space=DEFAULT_SPACE, repeats=2):
+    """Tunes `engine` on `step()` (one walk call).  Returns (best, table):
+    best maps option -> value (already set on the engine), table lists
+    (settings, ms) for every setting timed."""
+    best = {name: vals[0] for name, vals in space}
+    for name, v in best.items():
+        engine.set_option(name, v)
+    table = []
+    for name, vals in space:
+        if len(vals) < 2:
+            continue
+        timed = {}
+        for v in vals:
+            engine.set_option(name, v)
+            ms = []
+            for _ in range(repeats):
+                step()
+                ms.append(sum(engine.last_timing()[:2]))
+            timed[v] = min(ms)
+            table.append((dict(best, **{name: v}), timed[v]))
+        best[name] = min(timed, key=timed.get)
+        engine.set_option(name, best[name])
+    return best, table

@@ -10,7 +10,7 @@ import pytest
 
 from oracle import graphs as G
 
-pytestmark = pytest.mark.gpu
+pytestmark = [pytest.mark.gpu, pytest.mark.timeout(300)]
 
 
 @pytest.fixture(scope="module")

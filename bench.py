@@ -49,6 +49,11 @@ WORKLOADS = {
                               "5 edge types, uniform[1,5) weights"),
     "node2vec-s24": dict(app="node2vec", scale=24, weights=1, types=0, walk_length=80, p=2.0, q=0.5,
                          desc="node2vec p=2 q=0.5 len 80, one walker per vertex, R-MAT scale 24 ef16 uniform[1,5)"),
+    "node2vec-serve-s24": dict(app="node2vec", scale=24, weights=1, types=0, serve=3000,
+                               desc="served node2vec request stream on a resident R-MAT scale 24 ef16 uniform[1,5) "
+                                    "graph: per request p, q log-uniform [0.25, 4], length uniform [5, 200], "
+                                    "walkers lognormal (median 4096, sigma 1) clipped to [1, 2^20], each request "
+                                    "its own seed and walker-id range"),
     "metapath-batch-s22": dict(app="metapath", scale=22, weights=1, types=5, batch=16,
                                schemes=[[1, 2, 4, 8], [2, 8, 2, 16], [4, 1, 16, 4]], scheme_round_robin=True,
                                desc="16 metapath jobs (walkers 2^10..2^22, lengths 5..200, 3 schemes of 4 one-hot "
@@ -249,6 +254,188 @@ def run_reference(args, wl, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def serve_requests(wl, V, seed=5):
+    """The served workload's request stream (seeded)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(wl["serve"]):
+        walkers = int(np.clip(round(rng.lognormal(np.log(4096), 1.0)), 1, 1 << 20))
+        reqs.append(dict(walker_num=walkers, seed=1000 + i, walk_length=int(rng.integers(5, 201)),
+                         p=float(np.exp(rng.uniform(np.log(0.25), np.log(4.0)))),
+                         q=float(np.exp(rng.uniform(np.log(0.25), np.log(4.0)))),
+                         walker_begin=int(rng.integers(0, V)), weighted=bool(wl["weights"])))
+    return reqs
+
+
+def run_serve_bench(args, wl, world, rank, local):
+    """Served request stream (continuous batching on two slots) against plain
+    per-request launches and device-side batches of the same requests.
+
+    value = saturated serving throughput: every request submitted at once,
+    walker-steps over first submit -> last paths on the host.  Latency: an
+    open-loop Poisson stream at 70% of that throughput, p50/p99 of submit ->
+    paths on the host.  plain: one kk_walk_device per request (alias tables
+    kept, or rebuilt per call as the reference's random_walk does)."""
+    import numpy as np
+    import torch
+
+    import knightking_gb300 as kk
+
+    torch.cuda.set_device(local)
+    engine = kk.WalkEngine(local)
+    engine.generate_rmat(wl["scale"], 16, seed=wl["scale"], weights=wl["weights"], types=wl["types"])
+    V, E, _, _ = engine.info()
+    app = wl["app"]
+    reqs = serve_requests(wl, V)
+    total_req_steps_cap = sum(r["walker_num"] * r["walk_length"] for r in reqs)
+    stream = torch.cuda.Stream()
+    engine.set_stream(stream.cuda_stream)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        steps = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return steps, e0.elapsed_time(e1)
+
+    def plain(rs):
+        steps = 0
+        for r in rs:
+            kw = dict(r)
+            steps += engine.walk_device(app, kw.pop("walker_num"), paths="unpacked", **kw)[0]
+        return steps
+
+    def batched(rs):
+        steps = 0
+        for k in range(0, len(rs), 1024):
+            steps += engine.batch_walk_device(app, rs[k:k + 1024], paths=True)
+        return steps
+
+    # tables resident (sorted adjacency, edge set, alias tables), then tune the
+    # batch kernel on the whole stream
+    engine.set_option("alias_cache", 1)
+    from knightking_gb300 import tuning
+    space = tuple((n, v) for n, v in tuning.space_for(app, bool(wl["weights"])) if n != "walk_schedule")
+    best, tune_table = tuning.autotune(engine, lambda: batched(reqs), space, repeats=1)
+    for _ in range(args.warmup):
+        batched(reqs[:64])
+        plain(reqs[:8])
+    barrier(world)
+    n_plain = min(len(reqs), 300)
+    with ClockSampler(local) as clocks:
+        time.sleep(0.5)
+        b_steps, b_ms = timed(lambda: batched(reqs))
+        p_steps, p_ms = timed(lambda: plain(reqs[:n_plain]))
+        engine.set_option("alias_cache", 0)
+        r_steps, r_ms = timed(lambda: plain(reqs[:12]))
+        engine.set_option("alias_cache", 1)
+        # saturated serving
+        srv = engine.serve(app, slots=2, max_jobs=256, slot_bytes=2 << 30)
+        t0 = time.perf_counter()
+        tickets = [srv.submit(**r) for r in reqs]
+        s_steps = 0
+        for t in tickets:
+            res = srv.poll(t, keep_paths=False)
+            assert res.status == 0
+            s_steps += res.total_steps
+        s_s = time.perf_counter() - t0
+        sat = srv.stats()
+        srv.stop()
+    served_value = s_steps / s_s
+    # latency under an open-loop Poisson stream at 70% of the saturated rate
+    rate = 0.7 * served_value / (s_steps / len(reqs))
+    rng = np.random.default_rng(11)
+    gaps = rng.exponential(1.0 / rate, len(reqs))
+    srv = engine.serve(app, slots=2, max_jobs=256, slot_bytes=2 << 30)
+    results = [None] * len(reqs)
+
+    def poller(ts):
+        for i, t in ts:
+            results[i] = srv.poll(t, keep_paths=False)
+
+    import threading
+    t_start = time.perf_counter()
+    due = t_start
+    pending = []
+    pollers = []
+    for i, r in enumerate(reqs):
+        due += gaps[i]
+        d = due - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+        pending.append((i, srv.submit(**r)))
+        if len(pending) == 64:
+            th = threading.Thread(target=poller, args=(pending,))
+            th.start()
+            pollers.append(th)
+            pending = []
+    if pending:
+        th = threading.Thread(target=poller, args=(pending,))
+        th.start()
+        pollers.append(th)
+    for th in pollers:
+        th.join()
+    open_s = time.perf_counter() - t_start
+    lat = srv.stats()
+    srv.stop()
+    open_steps = sum(r.total_steps for r in results)
+
+    # access counts of the stream (binary-search probe counts), for the byte model
+    engine.set_option("walk_stats", 1)
+    engine.set_option("node2vec_adjacency", 1)
+    c_steps = batched(reqs[:1024])
+    trials, queries, probes = engine.last_stats()
+    engine.set_option("walk_stats", 0)
+    engine.set_option("node2vec_adjacency", best.get("node2vec_adjacency", 0))
+    T, Q, P = trials / c_steps, queries / c_steps, probes / c_steps
+    b_step = 40 + T * (40 + 32) + P * 32 + 4
+    design_b = 40 + T * 32 + Q * 32 + 4
+    peak, peak_kind = load_peaks()
+    batched_value = b_steps / (b_ms / 1e3)
+    plain_value = p_steps / (p_ms / 1e3)
+    rebuild_value = r_steps / (r_ms / 1e3)
+    achieved = batched_value * b_step / 1e9
+    if rank == 0:
+        line = {
+            "metric": "walker-steps/s", "value": served_value, "unit": "walker-steps/s", "n_gpus": world,
+            "steps": 1, "warmup": args.warmup, "ms_per_step": s_s * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded R-MAT generated on the GPU, seeded request stream)",
+            "config": {"workload": args.workload, "desc": wl["desc"], "vertices": V, "edges": E,
+                       "requests": len(reqs), "walker_step_capacity": total_req_steps_cap,
+                       "parallelism": "replicas", "l2": "inputs larger than L2", "slots": 2, "max_jobs": 256,
+                       "tuned": best, "tuning_ms": [[c, ms] for c, ms in tune_table]},
+            "served": {"value": served_value, "what": "all requests submitted at once; submit -> paths on host",
+                       "batches": sat["batches"], "mean_batch_jobs": sat["mean_batch_jobs"]},
+            "latency": {"offered_rate_req_s": rate, "p50_ms": lat["p50_ms"], "p99_ms": lat["p99_ms"],
+                        "mean_ms": lat["mean_ms"], "throughput": open_steps / open_s,
+                        "what": "open-loop Poisson arrivals at 70% of the saturated rate"},
+            "batched": {"value": batched_value, "unit": "walker-steps/s", "ms": b_ms,
+                        "what": "kk_batch_walk_device, 1024 requests per launch, paths in HBM"},
+            "plain": {"value": plain_value, "unit": "walker-steps/s", "requests": n_plain,
+                      "what": "one kk_walk_device launch per request, alias tables kept"},
+            "plain_rebuild": {"value": rebuild_value, "unit": "walker-steps/s", "requests": 12,
+                              "what": "one launch per request, alias tables rebuilt per call (reference)"},
+            "served_over_plain": served_value / plain_value,
+            "batched_over_plain": batched_value / plain_value,
+            "e2e": {"value": served_value, "unit": "walker-steps/s",
+                    "h2d_bytes_per_step": len(reqs) * 120, "d2h_bytes_per_step": 4 * (s_steps + sum(
+                        r["walker_num"] for r in reqs))},
+            "gpu_launches": sat["batches"],
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                         "bytes_per_step": b_step, "design_bytes_per_step": design_b,
+                         "access_counts": {"trials_per_step": T, "queries_per_step": Q, "probes_per_step": P},
+                         "kernel": "walk_batch_kernel (second order), from the batched throughput"},
+            "cpu_baseline": None, "clocks": clocks.summary(),
+        }
+        print(json.dumps(line))
+
+
 def run_batch_bench(args, wl, world, rank, local):
     """Batched jobs in one launch vs one launch per job (the reference runs one
     random_walk() call per job), same jobs, same graph, timed back to back."""
@@ -421,6 +608,33 @@ def run_ours(args, wl, world, rank, local):
     peak, peak_kind = load_peaks()
     steps_per_launch = total_steps / args.steps
     b_step = B_STEP.get(app)
+    design_b = DESIGN_B_STEP.get(app)
+    counts = None
+    if app in ("node2vec", "metapath"):
+        # one counted walk after the timed region (same paths): trials per step
+        # and the probes a binary search of the query targets' adjacency takes
+        # give the byte model of a rejection-sampled step
+        engine.set_option("walk_stats", 1)
+        adj = best.get("node2vec_adjacency", 0)
+        if app == "node2vec":
+            engine.set_option("node2vec_adjacency", 1)
+        st_steps = step()
+        trials, queries, probes = engine.last_stats()
+        engine.set_option("walk_stats", 0)
+        if app == "node2vec":
+            engine.set_option("node2vec_adjacency", adj)
+        T, Q, P = trials / st_steps, queries / st_steps, probes / st_steps
+        counts = {"trials_per_step": T, "queries_per_step": Q, "probes_per_step": P}
+        if app == "node2vec":
+            # offsets 40 + T x (bucket 40 + neighbour 32) + probes x 32 + path 4
+            b_step = 40 + T * (40 + 32) + P * 32 + 4
+            # this engine: offsets 40 + T x one 32 B bucket + one edge-set sector per query + path 4
+            design_b = 40 + T * 32 + Q * 32 + 4
+        else:
+            # vertex mask 32 + offsets 40 + T x (bucket 40 + type 32) + neighbour 32 + path 4
+            b_step = 32 + 40 + T * (40 + 32) + 32 + 4
+            # this engine: mask 32 + offsets 40 + T x (bucket 32 + type 32) + path 4
+            design_b = 32 + 40 + T * (32 + 32) + 4
     mean_walk_ms = statistics.mean(walk_ms)
     roof = None
     if b_step is not None:
@@ -432,7 +646,7 @@ def run_ours(args, wl, world, rank, local):
                 traffic = json.load(f)["dram_bytes_per_step"] * steps_per_launch
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_kind": peak_kind, "bytes_per_step": b_step,
-                "design_bytes_per_step": DESIGN_B_STEP.get(app),
+                "design_bytes_per_step": design_b, "access_counts": counts,
                 "kernel": ("walk_pool_kernel" if best_schedule == 1 else "walk_static_kernel") +
                           (" (second order)" if app == "node2vec" else " (first order)"),
                 "kernel_ms": mean_walk_ms, "alias_build_ms": statistics.mean(alias_ms)}
@@ -487,6 +701,8 @@ def main():
         run_reference(args, wl, world, rank, local)
     elif "batch" in wl:
         run_batch_bench(args, wl, world, rank, local)
+    elif "serve" in wl:
+        run_serve_bench(args, wl, world, rank, local)
     else:
         run_ours(args, wl, world, rank, local)
     if world > 1:

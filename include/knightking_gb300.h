@@ -110,7 +110,8 @@ kk_status kk_engine_set_stream(kk_engine *e, void *stream);
  *   "node2vec_adjacency" 0 edge-set lookup (built once per graph), 1 binary search of the
  *                        sorted adjacency, as node2vec.hpp:159-166
  *   "l2_fetch_bytes"     the context's cudaLimitMaxL2FetchGranularity while the engine
- *                        lives: 32, 64, 128, or 0 for the value found (restored on destroy) */
+ *                        lives: 32, 64, 128, or 0 for the value found (restored on destroy)
+ *   "walk_stats"         1 counts trials, queries and probes (kk_last_walk_stats) */
 kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value);
 /* Message of the last failed call on this engine ("" if none). */
 const char *kk_last_error(const kk_engine *e);
@@ -265,6 +266,12 @@ kk_status kk_serve_stats_get(kk_server *s, kk_serve_stats *out);
 /* Finishes the queued requests, stops the slots and frees the server (results
  * not yet polled are freed). */
 kk_status kk_serve_stop(kk_server *s);
+
+/* Access counts of the last walk call's last epoch when the walk_stats option
+ * is on (zeros otherwise): rejection trials, second-order queries, and the
+ * probes a binary search of each query target's sorted adjacency takes
+ * (ceil(log2(degree + 1)); counted only with node2vec_adjacency = 1). */
+kk_status kk_last_walk_stats(const kk_engine *e, uint64_t *trials, uint64_t *queries, uint64_t *probes);
 
 /* Milliseconds of the alias build and of the walk kernels of the last walk
  * call, from CUDA events on the engine's stream. */

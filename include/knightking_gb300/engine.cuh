@@ -177,6 +177,10 @@ struct kk_engine
     /* threads per block of the one-walker-per-thread and batch walk kernels
      * (option walk_block: 32..256, a multiple of 32) */
     int walk_block = 256;
+    /* walk_stats (option): count trials, queries and binary-search probes of
+     * the walks (kk_last_walk_stats) */
+    int walk_stats = 0;
+    uint64_t last_stats[3] = {0, 0, 0};
     /* alias-table layout: 0 cursor buckets where the hooks allow them, 1 index
      * buckets always */
     int alias_layout = 0;
@@ -421,6 +425,7 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
     L.alias_sum = (const float *)e->sum.p;
     L.status = d_status;
     L.trial_limit = e->trial_limit;
+    L.stats = e->walk_stats ? (unsigned long long *)((char *)d_status + 24) : nullptr;
     L.length = e->length.as<uint32_t>(n);
     uint64_t total_cap;
     if (rs.fixed_cap)
@@ -464,9 +469,10 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
     }
     KK_CUDA_CHECK(cudaGetLastError());
     KK_CUDA_CHECK(cudaEventRecord(e->ev[2], e->stream));
-    int h_small[8];
+    int h_small[16];
     KK_CUDA_CHECK(cudaMemcpyAsync(h_small, d_status, sizeof(h_small), cudaMemcpyDeviceToHost, e->stream));
     KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+    memcpy(e->last_stats, (char *)h_small + 24, sizeof(e->last_stats));
     KK_CUDA_CHECK(cudaEventElapsedTime(&e->alias_ms, e->ev[0], e->ev[1]));
     KK_CUDA_CHECK(cudaEventElapsedTime(&e->walk_ms, e->ev[1], e->ev[2]));
     if (h_small[0] == KK_STATUS_TRIAL_LIMIT)

@@ -854,6 +854,7 @@ struct WalkLaunch
     const float *alias_sum; /* static-component sums, for regular_area when ra is not precomputed */
     int *status;
     uint32_t trial_limit;
+    unsigned long long *stats; /* trials, queries, probes of the launch, or nullptr */
 };
 
 template <typename S, typename WC>
@@ -952,6 +953,7 @@ __device__ __forceinline__ void flush_steps(unsigned long long *total, unsigned 
         atomicAdd(total, mine);
 }
 
+
 /* regular_area[v] (include/walk.hpp:750-781): precomputed, or computed per
  * use with the same two roundings, sum * ub or deg * ub, when the upper
  * bound differs per job of a batch. */
@@ -980,6 +982,31 @@ struct WalkerRun
     uint32_t *out;
     uint32_t cap;
     uint32_t len;
+    /* access counts of the walk (reported when the launch asks for them):
+     * rejection trials, second-order queries, and the probes a binary search
+     * of the target's sorted adjacency takes for those queries */
+    uint32_t trials, queries, probes;
+};
+
+/* Per-thread access counts of finished walks, flushed once per thread. */
+struct WalkCounts
+{
+    unsigned long long trials = 0, queries = 0, probes = 0;
+    template <typename S>
+    __device__ __forceinline__ void add(const WalkerRun<S> &r)
+    {
+        trials += r.trials;
+        queries += r.queries;
+        probes += r.probes;
+    }
+    __device__ __forceinline__ void flush(unsigned long long *stats)
+    {
+        if (stats == nullptr)
+            return;
+        flush_steps(stats, trials);
+        flush_steps(stats + 1, queries);
+        flush_steps(stats + 2, probes);
+    }
 };
 
 /* Starts walker i of the launch: id, value-initialised state, start vertex,
@@ -1001,6 +1028,7 @@ __device__ __forceinline__ void walk_begin(const GraphView &g, const WC &wc, con
     if (r.out)
         r.out[0] = r.v;
     r.len = 1;
+    r.trials = r.queries = r.probes = 0;
 }
 
 /* One step of one walker; false when its walk ends.
@@ -1112,7 +1140,10 @@ __device__ __forceinline__ bool walk_step(const GraphView &g, const WC &wc, cons
         {
             const real_t ext = tc.extension_comp(w, v);
             if (ext == 0.0f || (ext < 1.0f && rng.gen_float(1.0f) > ext))
+            {
+                run.trials += trials;
                 return false;
+            }
             Cand cd{kNone, 0, 0, false};
             float randval = 0.0f;
             bool accepted = false;
@@ -1170,11 +1201,13 @@ __device__ __forceinline__ bool walk_step(const GraphView &g, const WC &wc, cons
                 if (tc.post_query(w, v, cu, target, query))
                 {
                     AdjList tadj{0, 0};
+                    run.queries++;
                     if (respond_needs_adjacency(tc.respond_query))
                     {
                         const Pos tp =
                             (target == run.pv && run.ppos.e0 >= 0) ? run.ppos : pos_from_offsets(g, target);
                         tadj = AdjList{(edge_id_t)tp.e0, (edge_id_t)(tp.e0 + tp.deg)};
+                        run.probes += 32 - __clz(tp.deg);
                     }
                     tc.respond_query(target, query, tadj, resp);
                 }
@@ -1187,6 +1220,7 @@ __device__ __forceinline__ bool walk_step(const GraphView &g, const WC &wc, cons
             }
         }
     }
+    run.trials += trials;
     w.step++;
     if constexpr (is_hook<decltype(wc.walker_update_state)>())
         wc.walker_update_state(w, v, AdjUnit{ac.nbr, (edge_id_t)(e0 + ac.idx)});
@@ -1216,6 +1250,7 @@ __global__ void __launch_bounds__(256) walk_static_kernel(GraphView g, WC wc, TC
                                                           const float *ra, WalkLaunch L)
 {
     unsigned long long my_steps = 0;
+    WalkCounts counts;
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t n_iter = (L.walker_num + stride - 1) / stride;
     for (uint32_t it = 0; it < n_iter; it++)
@@ -1232,9 +1267,11 @@ __global__ void __launch_bounds__(256) walk_static_kernel(GraphView g, WC wc, TC
             }
             L.length[i] = run.len;
             my_steps += run.len - 1;
+            counts.add(run);
         }
     }
     flush_steps(L.total_steps, my_steps);
+    counts.flush(L.stats);
 }
 
 /* Device-resident walker pool: persistent blocks, each owning a contiguous
@@ -1255,6 +1292,7 @@ __global__ void __launch_bounds__(256) walk_pool_kernel(GraphView g, WC wc, TC t
         s_next = lo;
     __syncthreads();
     unsigned long long my_steps = 0;
+    WalkCounts counts;
     Sampler rng;
     rng.init(L.seed);
     WalkerRun<S> run;
@@ -1268,6 +1306,7 @@ __global__ void __launch_bounds__(256) walk_pool_kernel(GraphView g, WC wc, TC t
         {
             L.length[i] = run.len;
             my_steps += run.len - 1;
+            counts.add(run);
             i = atomicAdd(&s_next, 1u);
             have = i < hi;
             if (have)
@@ -1275,6 +1314,7 @@ __global__ void __launch_bounds__(256) walk_pool_kernel(GraphView g, WC wc, TC t
         }
     }
     flush_steps(L.total_steps, my_steps);
+    counts.flush(L.stats);
 }
 
 /* ---- batched walks --------------------------------------------------------
@@ -1307,13 +1347,14 @@ __global__ void __launch_bounds__(256) walk_batch_kernel(GraphView g, App app, c
                                                          uint32_t total, const Bucket *alias,
                                                          const float *alias_sum, uint32_t *path, uint32_t *length,
                                                          unsigned long long *total_steps, int *status,
-                                                         uint32_t trial_limit)
+                                                         uint32_t trial_limit, unsigned long long *stats)
 {
     __shared__ uint32_t s_first[kMaxBatchJobs];
     for (uint32_t j = threadIdx.x; j < njobs; j += blockDim.x)
         s_first[j] = jobs[j].first_task;
     __syncthreads();
     unsigned long long my_steps = 0;
+    WalkCounts counts;
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t n_iter = (total + stride - 1) / stride;
     for (uint32_t it = 0; it < n_iter; it++)
@@ -1348,6 +1389,7 @@ __global__ void __launch_bounds__(256) walk_batch_kernel(GraphView g, App app, c
             L.alias_sum = alias_sum;
             L.status = status;
             L.trial_limit = trial_limit;
+            L.stats = nullptr;
             const uint32_t i = t - job.first_task;
             Sampler rng;
             rng.init(L.seed);
@@ -1358,9 +1400,11 @@ __global__ void __launch_bounds__(256) walk_batch_kernel(GraphView g, App app, c
             }
             L.length[i] = run.len;
             my_steps += run.len - 1;
+            counts.add(run);
         }
     }
     flush_steps(total_steps, my_steps);
+    counts.flush(stats);
 }
 
 /* Upper bound on each walker's path length when the extension is a constant

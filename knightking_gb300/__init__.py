@@ -295,6 +295,12 @@ class WalkEngine:
         """Starts a Server (continuous batching) that owns this engine until stopped."""
         return Server(self, app, weighted, slots, max_jobs, slot_bytes)
 
+    def last_stats(self):
+        """(trials, queries, probes) of the last walk (walk_stats option)."""
+        t, q, p = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(self._lib.kk_last_walk_stats(self._h, ctypes.byref(t), ctypes.byref(q), ctypes.byref(p)))
+        return t.value, q.value, p.value
+
     def last_timing(self):
         a = ctypes.c_float()
         w = ctypes.c_float()
@@ -400,8 +406,10 @@ class Server:
             raise KKError(st, "request refused")
         return t.value
 
-    def poll(self, ticket, timeout_ms=-1):
-        """The request's ServeResult, or None if it is not done within timeout_ms."""
+    def poll(self, ticket, timeout_ms=-1, keep_paths=True):
+        """The request's ServeResult, or None if it is not done within
+        timeout_ms.  keep_paths=False frees the paths unread (result.paths is
+        then None and result.total_steps still counts them)."""
         r = _capi.KKServeResult()
         st = self._lib.kk_serve_poll(self._h, ctypes.c_uint64(ticket), int(timeout_ms), ctypes.byref(r))
         if st == _capi.KK_ERR_TIMEOUT:
@@ -409,12 +417,17 @@ class Server:
         if st != _capi.KK_OK:
             raise KKError(st, "unknown ticket")
         paths = None
+        total_steps = 0
         if r.paths:
             try:
-                paths = PathSet(*_capi.paths_to_numpy(r.paths.contents))
+                total_steps = r.paths.contents.total_steps
+                if keep_paths:
+                    paths = PathSet(*_capi.paths_to_numpy(r.paths.contents))
             finally:
                 self._lib.kk_paths_free(r.paths)
-        return ServeResult(paths, r.status, r.queue_ms, r.latency_ms, r.batch_jobs)
+        res = ServeResult(paths, r.status, r.queue_ms, r.latency_ms, r.batch_jobs)
+        res.total_steps = int(total_steps)
+        return res
 
     def stats(self):
         s = _capi.KKServeStats()

@@ -103,7 +103,7 @@ void launch_batch_with(kk_engine *e, const App &app, const BatchPlan &plan, Batc
     const unsigned bs = (unsigned)e->walk_block;
     walk_batch_kernel<typename App::S, App, Bucket><<<grid_for(e, plan.total, bs), bs, 0, slot.stream>>>(
         e->view(), app, d_jobs, (uint32_t)plan.jobs.size(), plan.total, alias, (const float *)e->sum.p, *path, length,
-        steps, status, e->trial_limit);
+        steps, status, e->trial_limit, e->walk_stats ? steps + 1 : nullptr);
     KK_CUDA_CHECK(cudaGetLastError());
 }
 
@@ -233,9 +233,11 @@ uint64_t run_batch(kk_engine *e, BatchPlan &plan, BatchSlot &slot, bool want_pat
                          d_steps, d_status, want_paths, p);
     }
     KK_CUDA_CHECK(cudaEventRecord(slot.ev[2], slot.stream));
-    int h_small[8];
+    int h_small[16];
     KK_CUDA_CHECK(cudaMemcpyAsync(h_small, d_status, sizeof(h_small), cudaMemcpyDeviceToHost, slot.stream));
     KK_CUDA_CHECK(cudaStreamSynchronize(slot.stream));
+    if (&slot == &e->bslot)
+        memcpy(e->last_stats, (char *)h_small + 24, sizeof(e->last_stats));
     KK_CUDA_CHECK(cudaEventElapsedTime(&slot.alias_ms, slot.ev[0], slot.ev[1]));
     KK_CUDA_CHECK(cudaEventElapsedTime(&slot.walk_ms, slot.ev[1], slot.ev[2]));
     if (h_small[0] == KK_STATUS_TRIAL_LIMIT)

@@ -360,6 +360,8 @@ kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value)
             e->n2v_adjacency = (int)value;
         else if (n == "walk_block" && value >= 32 && value <= 256 && value % 32 == 0)
             e->walk_block = (int)value;
+        else if (n == "walk_stats" && (value == 0 || value == 1))
+            e->walk_stats = (int)value;
         else
             fail(KK_ERR_INVALID_CONFIG, "unknown option or value out of range: " + n);
     });
@@ -623,6 +625,19 @@ kk_status kk_walk_device(kk_engine *e, const kk_walk_opts *opts, uint64_t *total
             *d_vertices = r.path; /* unpacked: walker i's slot as the walk wrote it */
         }
     });
+}
+
+kk_status kk_last_walk_stats(const kk_engine *e, uint64_t *trials, uint64_t *queries, uint64_t *probes)
+{
+    if (!e)
+        return KK_ERR_INVALID_CONFIG;
+    if (trials)
+        *trials = e->last_stats[0];
+    if (queries)
+        *queries = e->last_stats[1];
+    if (probes)
+        *probes = e->last_stats[2];
+    return KK_OK;
 }
 
 kk_status kk_last_walk_timing(const kk_engine *e, float *alias_ms, float *walk_ms)

@@ -150,8 +150,16 @@ struct Node2vecOutlierUB
     __device__ __forceinline__ void operator()(const Walker<Node2vecState> &wk, vertex_id_t, const AdjList &adj,
                                                real_t &area, vertex_id_t &num) const
     {
+        num = 1;
         if constexpr (Weighted)
         {
+            /* a non-positive overflow gives a non-positive area whatever the
+             * return edge's weight: the appendix is skipped without the search */
+            if (!(overflow > 0.0f))
+            {
+                area = overflow;
+                return;
+            }
             uint32_t deg = adj.degree();
             uint32_t i = lower_bound_adj(nbr, adj.begin, deg, wk.data.previous_vertex);
             area = i < deg ? fmul(gather(w + adj.begin + i), overflow) : 0.0f;
@@ -160,7 +168,6 @@ struct Node2vecOutlierUB
         {
             area = overflow;
         }
-        num = 1;
     }
 };
 

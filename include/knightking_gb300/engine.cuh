@@ -317,6 +317,26 @@ inline apps::MetaSchemes make_schemes(const kk_walk_opts &o)
     return sc;
 }
 
+/* One thread tier: blocks of NT vertices, a few resident per SM. */
+template <typename TC, typename Bucket, uint32_t D, uint32_t NT>
+void launch_alias_thread(kk_engine *e, const TC &tc, Bucket *alias, const uint64_t *vcur, float *sum,
+                         const uint32_t *order, uint32_t lo, uint32_t hi)
+{
+    constexpr size_t smem = alias_thread_smem<D, NT>();
+    static bool attr_set = false;
+    if (!attr_set)
+    {
+        KK_CUDA_CHECK(cudaFuncSetAttribute(alias_thread_kernel<TC, Bucket, D, NT>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr_set = true;
+    }
+    const uint32_t blocks = (hi - lo + NT - 1) / NT;
+    const uint32_t cap = 4u * (uint32_t)e->sm_count;
+    alias_thread_kernel<TC, Bucket, D, NT>
+        <<<blocks < cap ? blocks : cap, NT, smem, e->stream>>>(e->view(), tc, alias, vcur, sum, order, lo, hi);
+    KK_CUDA_CHECK(cudaGetLastError());
+}
+
 /* Builds alias tables in the Bucket layout into e->alias/e->sum for a
  * static functor. */
 template <typename TC, typename Bucket = IndexBucket>
@@ -358,28 +378,15 @@ void build_alias(kk_engine *e, const TC &tc)
             smem_set = true;
         }
         const uint32_t n = e->n_warp - e->n_hub;
-        float *ave = e->ave.as<float>(e->V);
-        alias_sum_kernel<TC><<<grid_for(e, n, 256), 256, 0, e->stream>>>(g, tc, sum, ave, order, e->n_hub, e->n_warp);
-        KK_CUDA_CHECK(cudaGetLastError());
-        unsigned grid = (n + 7) / 8 < 3 * sms ? (n + 7) / 8 : 3 * sms;
-        alias_pair_kernel<TC, Bucket><<<grid, 256, kAliasPairSmem, e->stream>>>(g, tc, alias, vcur, ave, scratch,
+        unsigned grid = (n + 7) / 8 < 4 * sms ? (n + 7) / 8 : 4 * sms;
+        alias_pair_kernel<TC, Bucket><<<grid, 256, kAliasPairSmem, e->stream>>>(g, tc, alias, vcur, sum, scratch,
                                                                                 order, e->n_hub, e->n_warp);
         KK_CUDA_CHECK(cudaGetLastError());
     }
     if (e->n_t32 > e->n_warp)
-    {
-        const uint32_t n = e->n_t32 - e->n_warp;
-        alias_thread_kernel<TC, Bucket, kAliasThreadMax, 64>
-            <<<(n + 63) / 64, 64, 0, e->stream>>>(g, tc, alias, vcur, sum, order, e->n_warp, e->n_t32);
-        KK_CUDA_CHECK(cudaGetLastError());
-    }
+        launch_alias_thread<TC, Bucket, kAliasThreadMax, 64>(e, tc, alias, vcur, sum, order, e->n_warp, e->n_t32);
     if (e->n_nz > e->n_t32)
-    {
-        const uint32_t n = e->n_nz - e->n_t32;
-        alias_thread_kernel<TC, Bucket, kAliasThreadSmall, 256>
-            <<<(n + 255) / 256, 256, 0, e->stream>>>(g, tc, alias, vcur, sum, order, e->n_t32, e->n_nz);
-        KK_CUDA_CHECK(cudaGetLastError());
-    }
+        launch_alias_thread<TC, Bucket, kAliasThreadSmall, 256>(e, tc, alias, vcur, sum, order, e->n_t32, e->n_nz);
     if (e->n_hub)
         KK_CUDA_CHECK(cudaStreamWaitEvent(e->stream, e->ev_join, 0));
     if constexpr (weight_tables)

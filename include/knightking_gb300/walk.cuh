@@ -12,6 +12,7 @@
  *   dcomp_upperbound   real_t (vertex_id_t, const AdjList&)   (pure: called per use)
  *   dcomp_lowerbound   real_t (vertex_id_t, const AdjList&)   (pure: called per use)
  *   outlier_upperbound void   (const Walker<S>&, vertex_id_t, const AdjList&, real_t& area, vertex_id_t& num)
+ *                             (pure: called once per step)
  *   outlier_search     bool   (const Walker<S>&, vertex_id_t, const AdjList&, vertex_id_t idx, AdjUnit& out)
  *                             (false = the reference's nullptr)
  *   post_query         bool   (const Walker<S>&, vertex_id_t cur, const AdjUnit& cand, vertex_id_t& target, Q&)
@@ -260,10 +261,16 @@ struct __align__(32) IndexBucket
     uint32_t pad2;
 
     static constexpr bool cursor = false;
-    __device__ __forceinline__ static IndexBucket make(float p, uint32_t pi, uint32_t qi, const uint32_t *nb,
-                                                       const uint64_t *)
+    /* pn, qn: the neighbours of edges pi, qi (qn unused when qi == kNone) */
+    __device__ __forceinline__ static IndexBucket make_n(float p, uint32_t pi, uint32_t qi, uint32_t pn, uint32_t qn,
+                                                         const uint64_t *)
     {
-        return IndexBucket{p, pi, qi, 0, nb[pi], qi == kNone ? kNone : nb[qi], 0, 0};
+        return IndexBucket{p, pi, qi, 0, pn, qi == kNone ? kNone : qn, 0, 0};
+    }
+    __device__ __forceinline__ static IndexBucket make(float p, uint32_t pi, uint32_t qi, const uint32_t *nb,
+                                                       const uint64_t *vcur)
+    {
+        return make_n(p, pi, qi, nb[pi], qi == kNone ? kNone : nb[qi], vcur);
     }
 };
 
@@ -277,14 +284,17 @@ struct __align__(32) CursorBucket
     uint64_t q_cur;
 
     static constexpr bool cursor = true;
+    __device__ __forceinline__ static CursorBucket make_n(float p, uint32_t, uint32_t qi, uint32_t pn, uint32_t qn,
+                                                          const uint64_t *vcur)
+    {
+        if (qi == kNone)
+            return CursorBucket{p, pn, kNone, 0, gather(vcur + pn), 0};
+        return CursorBucket{p, pn, qn, 0, gather(vcur + pn), gather(vcur + qn)};
+    }
     __device__ __forceinline__ static CursorBucket make(float p, uint32_t pi, uint32_t qi, const uint32_t *nb,
                                                         const uint64_t *vcur)
     {
-        const uint32_t pn = nb[pi];
-        if (qi == kNone)
-            return CursorBucket{p, pn, kNone, 0, gather(vcur + pn), 0};
-        const uint32_t qn = nb[qi];
-        return CursorBucket{p, pn, qn, 0, gather(vcur + pn), gather(vcur + qn)};
+        return make_n(p, pi, qi, nb[pi], qi == kNone ? kNone : nb[qi], vcur);
     }
 };
 static_assert(sizeof(IndexBucket) == 32 && sizeof(CursorBucket) == 32, "one sector per bucket");
@@ -343,18 +353,18 @@ constexpr bool use_cursor_buckets()
  *   hubs (deg >= kAliasHubMin): a 1024-thread block per vertex does sum,
  *        split and pairing, queues in the 16 B/edge scratch at 2*off[v];
  *        batches of 64 or fewer go to one warp (no block barrier);
- *   warp tier (kAliasThreadMax < deg < kAliasHubMin): one thread per vertex
- *        computes the serial sums (balanced warps), then a warp per vertex
- *        splits and pairs, queues in shared memory up to kAliasWarpQueue
- *        entries, else in the scratch;
+ *   warp tier (kAliasThreadMax < deg < kAliasHubMin): a warp per vertex
+ *        sums (lane 0, from coalesced chunks in shared memory), splits and
+ *        pairs, queues and neighbours in shared memory up to kAliasWarpQueue
+ *        entries, else queues in the scratch;
  *   thread tiers (deg <= kAliasThreadMax): one thread per vertex runs the
  *        serial algorithm on rings in shared memory (alias_thread_kernel). */
 
-constexpr uint32_t kAliasHubMin = 4097;   /* degree from which a vertex is a hub */
+constexpr uint32_t kAliasHubMin = 16385;  /* degree from which a vertex is a hub */
 constexpr uint32_t kAliasThreadMax = 128; /* largest degree of the thread tiers */
 constexpr uint32_t kAliasThreadSmall = 32; /* largest degree of the narrow thread tier */
 constexpr uint32_t kAliasWarpQueue = 512; /* shared-memory queue entries per warp */
-constexpr size_t kAliasPairSmem = (size_t)8 * 2 * kAliasWarpQueue * sizeof(uint2); /* 8 warps per block */
+constexpr size_t kAliasPairSmem = (size_t)8 * kAliasWarpQueue * (sizeof(uint2) + sizeof(uint32_t)); /* 8 warps */
 constexpr unsigned kFullMask = 0xffffffffu;
 
 __device__ __forceinline__ uint32_t lanemask_lt()
@@ -594,34 +604,161 @@ __global__ void __launch_bounds__(256) alias_sum_kernel(GraphView g, TC tc, floa
     }
 }
 
-/* Split (:594-603) and batched FIFO pairing (:605-638) of the non-hub
- * vertices: a warp per vertex, queues in shared memory up to kAliasWarpQueue
- * entries each, else in the global scratch at 2*off[v]. */
+/* Split (:594-603) and batched FIFO pairing (:605-638) of the warp tier: a
+ * warp per vertex.  The queues are the rings of the thread tiers (p from the
+ * front of a deg-entry array, q from the back; neither outgrows its start) with
+ * (index, prob) entries; up to kAliasWarpQueue entries they and the row's
+ * neighbours sit in shared memory, so a batch's bucket writes wait on no
+ * global load; larger rows use the global scratch at 2*off[v].  A batch of b
+ * pairings reads entries [h, h+b) of both rings and writes only behind their
+ * tails, and all its reads precede its writes (the ballots depend on them). */
+template <typename Bucket, typename Nb>
+__device__ __forceinline__ void warp_pairing_ring(uint2 *R, uint32_t deg, uint32_t S0, uint32_t B0, float ave,
+                                                  Bucket *ob, Nb nb, const uint64_t *vcur)
+{
+    const uint32_t lane = threadIdx.x & 31, lt = lanemask_lt();
+    uint32_t ph = 0, pt = 0, lp = S0, qh = 0, qt = 0, lq = B0, npop = 0;
+    auto pp = [&](uint32_t s) { return s >= S0 ? s - S0 : s; };           /* s < 2*S0 */
+    auto pq = [&](uint32_t s) { return deg - 1 - (s >= B0 ? s - B0 : s); }; /* s < 2*B0 */
+    while (lp != 0 && lq != 0)
+    {
+        const uint32_t b = min(min(lp, lq), 32u);
+        const bool act = lane < b;
+        bool conv = false;
+        uint2 ne = make_uint2(0, 0);
+        if (act)
+        {
+            const uint2 pe = R[pp(ph + lane)], qe = R[pq(qh + lane)];
+            const float pv = __uint_as_float(pe.y), qv = __uint_as_float(qe.y);
+            ob[npop + lane] = Bucket::make_n(fdiv(pv, ave), pe.x, qe.x, nb(pe.x), nb(qe.x), vcur);
+            const float r = fsub(qv, fsub(ave, pv));
+            conv = r < ave;
+            ne = make_uint2(qe.x, __float_as_uint(r));
+        }
+        const uint32_t mc = __ballot_sync(kFullMask, act && conv), ms = __ballot_sync(kFullMask, act && !conv);
+        if (act)
+        {
+            if (conv)
+                R[pp(pt + __popc(mc & lt))] = ne;
+            else
+                R[pq(qt + __popc(ms & lt))] = ne;
+        }
+        __syncwarp();
+        const uint32_t nc = __popc(mc), ns = __popc(ms);
+        ph = pp(ph + b);
+        qh = B0 ? (qh + b >= B0 ? qh + b - B0 : qh + b) : 0;
+        pt = pp(pt + nc);
+        qt = qt + ns >= B0 ? qt + ns - B0 : qt + ns;
+        lp = lp - b + nc;
+        lq = lq - b + ns;
+        npop += b;
+    }
+    /* leftovers (:623-638): the rest of whichever ring is non-empty */
+    for (uint32_t i = lane; i < lp; i += 32)
+    {
+        const uint32_t x = R[pp(ph + i)].x;
+        ob[npop + i] = Bucket::make_n(1.0f, x, kNone, nb(x), 0, vcur);
+    }
+    for (uint32_t i = lane; i < lq; i += 32)
+    {
+        const uint32_t x = R[pq(qh + i)].x;
+        ob[npop + lp + i] = Bucket::make_n(1.0f, x, kNone, nb(x), 0, vcur);
+    }
+    __syncwarp();
+}
+
+/* Sequential sum (:579-584) of a row by a warp: chunks of the row are loaded
+ * coalesced into the warp's shared buffer F (kAliasWarpQueue floats) and lane 0
+ * adds them in edge order; the sum is broadcast.  Staged rows (deg <=
+ * kAliasWarpQueue) also keep their values in x[] (element 32c + lane). */
+template <typename TC>
+__device__ __forceinline__ float warp_row_sum(const GraphView &g, const TC &tc, vertex_id_t v, int64_t e0,
+                                              uint32_t deg, float *F, float (&x)[kAliasWarpQueue / 32])
+{
+    const uint32_t lane = threadIdx.x & 31;
+    float sum = 0.0f;
+    for (uint32_t base = 0; base < deg; base += kAliasWarpQueue)
+    {
+        const uint32_t n = min(deg - base, kAliasWarpQueue);
+#pragma unroll
+        for (uint32_t c = 0; c < kAliasWarpQueue / 32; c++)
+        {
+            const uint32_t i = c * 32 + lane;
+            if (i < n)
+            {
+                const float val = static_at(g, tc, v, e0 + base + i);
+                x[c] = val;
+                F[i] = val;
+            }
+        }
+        __syncwarp();
+        if (lane == 0)
+        {
+            uint32_t i = 0;
+            for (; i + 8 <= n; i += 8)
+                sum = fadd(fadd(fadd(fadd(fadd(fadd(fadd(fadd(sum, F[i]), F[i + 1]), F[i + 2]), F[i + 3]), F[i + 4]),
+                                     F[i + 5]),
+                                F[i + 6]),
+                           F[i + 7]);
+            for (; i < n; i++)
+                sum = fadd(sum, F[i]);
+        }
+        __syncwarp();
+    }
+    return __shfl_sync(kFullMask, sum, 0);
+}
+
 template <typename TC, typename Bucket>
 __global__ void __launch_bounds__(256) alias_pair_kernel(GraphView g, TC tc, Bucket *out, const uint64_t *vcur,
-                                                         const float *ave_in, uint2 *scratch, const uint32_t *order,
+                                                         float *sum_out, uint2 *scratch, const uint32_t *order,
                                                          uint32_t lo, uint32_t hi)
 {
     extern __shared__ uint2 dyn[];
-    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwib = blockDim.x >> 5;
     const uint32_t lt = lanemask_lt();
-    const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
-    uint2 *sP = dyn + (size_t)wib * 2 * kAliasWarpQueue;
-    uint2 *sQ = sP + kAliasWarpQueue;
-    for (uint32_t k = lo + blockIdx.x * (blockDim.x >> 5) + wib; k < hi; k += nwarps)
+    const uint32_t nwarps = gridDim.x * nwib;
+    uint2 *sR = dyn + (size_t)wib * kAliasWarpQueue;
+    uint32_t *sNb = reinterpret_cast<uint32_t *>(dyn + (size_t)nwib * kAliasWarpQueue) + (size_t)wib * kAliasWarpQueue;
+    for (uint32_t k = lo + blockIdx.x * nwib + wib; k < hi; k += nwarps)
     {
         const uint32_t v = order[k];
         const int64_t e0 = g.off[v];
         const uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
-        const float ave = ave_in[v];
-        uint2 *P = sP, *Q = sQ;
-        if (deg > kAliasWarpQueue)
+        const bool staged = deg <= kAliasWarpQueue;
+        /* the sum, with the ring's shared memory as the chunk buffer */
+        float x[kAliasWarpQueue / 32];
+        const float sum = warp_row_sum(g, tc, v, e0, deg, reinterpret_cast<float *>(sR), x);
+        if (lane == 0 && sum_out != nullptr)
+            sum_out[v] = sum;
+        const float ave = fdiv(sum, u2f(deg));
+        __syncwarp();
+        uint2 *R = staged ? sR : scratch + 2 * e0;
+        uint32_t S0 = 0, B0 = 0;
+        if (staged)
         {
-            P = scratch + 2 * e0;
-            Q = P + deg;
+            /* split from the values kept in registers; neighbours to shared memory */
+#pragma unroll
+            for (uint32_t c = 0; c < kAliasWarpQueue / 32; c++)
+            {
+                const uint32_t base = c * 32;
+                if (base >= deg)
+                    break;
+                const bool valid = base + lane < deg;
+                if (valid)
+                    sNb[base + lane] = g.nbr[e0 + base + lane];
+                const float xv = x[c];
+                const bool sm = valid && xv < ave, bg = valid && !(xv < ave);
+                const uint32_t mp = __ballot_sync(kFullMask, sm), mq = __ballot_sync(kFullMask, bg);
+                const uint2 ent = make_uint2(base + lane, __float_as_uint(xv));
+                if (sm)
+                    R[S0 + __popc(mp & lt)] = ent;
+                if (bg)
+                    R[deg - 1 - (B0 + __popc(mq & lt))] = ent;
+                S0 += __popc(mp);
+                B0 += __popc(mq);
+            }
         }
-        uint32_t pt = 0, qt = 0;
-        for (uint32_t base = 0; base < deg; base += 32)
+        for (uint32_t base = 0; !staged && base < deg; base += 32)
         {
             const bool valid = base + lane < deg;
             const float x = valid ? static_at(g, tc, v, e0 + base + lane) : 0.0f;
@@ -629,20 +766,21 @@ __global__ void __launch_bounds__(256) alias_pair_kernel(GraphView g, TC tc, Buc
             const uint32_t mp = __ballot_sync(kFullMask, sm), mq = __ballot_sync(kFullMask, bg);
             const uint2 ent = make_uint2(base + lane, __float_as_uint(x));
             if (sm)
-                P[pt + __popc(mp & lt)] = ent;
+                R[S0 + __popc(mp & lt)] = ent;
             if (bg)
-                Q[qt + __popc(mq & lt)] = ent;
-            pt += __popc(mp);
-            qt += __popc(mq);
+                R[deg - 1 - (B0 + __popc(mq & lt))] = ent;
+            S0 += __popc(mp);
+            B0 += __popc(mq);
         }
         __syncwarp();
-        uint32_t ph = 0, qh = 0;
         Bucket *ob = out + e0;
-        const uint32_t *nb = g.nbr + e0;
-        warp_pairing(P, Q, ph, pt, qh, qt, ave, ob, nb, vcur, 0xffffffffu);
-        for (uint32_t i = lane; i < qt - qh; i += 32)
-            ob[pt + i] = Bucket::make(1.0f, Q[qh + i].x, kNone, nb, vcur);
-        __syncwarp();
+        if (staged)
+            warp_pairing_ring(R, deg, S0, B0, ave, ob, [&](uint32_t i) { return sNb[i]; }, vcur);
+        else
+        {
+            const uint32_t *nb = g.nbr + e0;
+            warp_pairing_ring(R, deg, S0, B0, ave, ob, [&](uint32_t i) { return nb[i]; }, vcur);
+        }
     }
 }
 
@@ -693,49 +831,84 @@ __global__ void __launch_bounds__(1024) alias_build_hub_kernel(GraphView g, TC t
 }
 
 /* Thread tiers: one thread per vertex of degree <= D runs the sequential
- * algorithm itself (sum, split, pairing, leftovers).  Every pairing pops one
- * entry from each queue and pushes at most one back, so neither queue ever
- * holds more entries than it started with: the p queue is a ring over the
- * first S0 slots of a deg-slot array and the q queue a ring over the last B0
- * slots, counted from the end (S0 + B0 = deg).  prob[] and the ring live in
- * shared memory with slot j of thread t at word j*NT + t (ring bytes packed
- * four to a word), so every lane stays in its own bank whatever its slot. */
+ * algorithm itself (sum, split, pairing, leftovers) on its row staged in
+ * shared memory.
+ *
+ * Staging: the block's NT vertices (consecutive in the degree order, so of
+ * similar degree) are loaded row by row by whole warps, coalesced: weights
+ * (through static_comp) and neighbours.  Element i of thread j's row sits at
+ * word i*NT + (j ^ (i & 31)): the warp writing 32 consecutive elements of one
+ * row hits 32 banks, and each thread then reads its own row from shared
+ * memory only.
+ *
+ * Queues: every pairing pops one entry from each queue and pushes at most one
+ * back, so neither queue ever holds more entries than it started with: the p
+ * queue is a ring over the first S0 slots of a deg-slot byte array and the q
+ * queue a ring over the last B0 slots, counted from the end (S0 + B0 = deg).
+ * Ring bytes of thread j are packed four to a word at (s/4)*NT + j. */
+template <uint32_t D, uint32_t NT>
+constexpr size_t alias_thread_smem()
+{
+    return (size_t)D * NT * 9 + (size_t)NT * 16;
+}
+
 template <typename TC, typename Bucket, uint32_t D, uint32_t NT>
 __global__ void __launch_bounds__(NT) alias_thread_kernel(GraphView g, TC tc, Bucket *out, const uint64_t *vcur,
                                                           float *sum_out, const uint32_t *order, uint32_t lo,
                                                           uint32_t hi)
 {
     static_assert(D <= 256 && D % 4 == 0 && NT % 32 == 0, "ring slots are bytes, four per word");
-    static_assert((size_t)D * NT * 5 <= 48 * 1024, "static shared memory");
-    __shared__ float s_prob[D * NT];
-    __shared__ uint32_t s_ring[(D / 4) * NT];
-    const uint32_t t = threadIdx.x;
-    float *prob = s_prob + t;
-    uint8_t *ring = reinterpret_cast<uint8_t *>(s_ring + t);
-    auto slot = [](uint32_t j) { return (j >> 2) * (NT * 4) + (j & 3); };
-    for (uint32_t k = lo + blockIdx.x * NT + t; k < hi; k += gridDim.x * NT)
+    extern __shared__ uint32_t smem[];
+    float *s_prob = reinterpret_cast<float *>(smem);
+    uint32_t *s_nb = smem + (size_t)D * NT;
+    int64_t *s_e0 = reinterpret_cast<int64_t *>(smem + (size_t)D * NT * 9 / 4);
+    uint32_t *s_deg = reinterpret_cast<uint32_t *>(s_e0 + NT);
+    uint32_t *s_v = s_deg + NT;
+    const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    uint8_t *ring = reinterpret_cast<uint8_t *>(smem + (size_t)2 * D * NT + t);
+    auto slot = [](uint32_t s) { return (s >> 2) * (NT * 4) + (s & 3); };
+    auto at = [](uint32_t i, uint32_t j) { return i * NT + (j ^ (i & 31)); };
+    for (uint32_t base = lo + blockIdx.x * NT; base < hi; base += gridDim.x * NT)
     {
-        const uint32_t v = order[k];
-        const int64_t e0 = g.off[v];
-        const uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
+        /* each thread fetches its own vertex's adjacency range, all in parallel */
+        uint32_t v = 0, deg = 0;
+        int64_t e0 = 0;
+        if (base + t < hi)
+        {
+            v = order[base + t];
+            e0 = g.off[v];
+            deg = (uint32_t)(g.off[v + 1] - e0);
+        }
+        __syncthreads(); /* the previous tile is done with the shared rows */
+        s_e0[t] = e0;
+        s_deg[t] = deg;
+        s_v[t] = v;
+        __syncthreads();
+        /* then whole warps copy the rows, several rows' loads in flight */
+#pragma unroll 4
+        for (uint32_t j = warp; j < NT; j += NT / 32)
+        {
+            const int64_t r0 = s_e0[j];
+            const uint32_t rd = s_deg[j], rv = s_v[j];
+            for (uint32_t i = lane; i < rd; i += 32)
+            {
+                s_prob[at(i, j)] = static_at(g, tc, rv, r0 + i);
+                s_nb[at(i, j)] = g.nbr[r0 + i];
+            }
+        }
+        __syncthreads();
+        if (base + t >= hi)
+            continue;
         float sum = 0.0f;
         uint32_t j = 0;
         for (; j + 4 <= deg; j += 4)
         {
-            const float a = static_at(g, tc, v, e0 + j), b = static_at(g, tc, v, e0 + j + 1);
-            const float c = static_at(g, tc, v, e0 + j + 2), d = static_at(g, tc, v, e0 + j + 3);
-            prob[j * NT] = a;
-            prob[(j + 1) * NT] = b;
-            prob[(j + 2) * NT] = c;
-            prob[(j + 3) * NT] = d;
+            const float a = s_prob[at(j, t)], b = s_prob[at(j + 1, t)];
+            const float c = s_prob[at(j + 2, t)], d = s_prob[at(j + 3, t)];
             sum = fadd(fadd(fadd(fadd(sum, a), b), c), d);
         }
         for (; j < deg; j++)
-        {
-            const float a = static_at(g, tc, v, e0 + j);
-            prob[j * NT] = a;
-            sum = fadd(sum, a);
-        }
+            sum = fadd(sum, s_prob[at(j, t)]);
         if (sum_out != nullptr)
             sum_out[v] = sum;
         const float ave = fdiv(sum, u2f(deg));
@@ -743,7 +916,7 @@ __global__ void __launch_bounds__(NT) alias_thread_kernel(GraphView g, TC tc, Bu
         uint32_t S0 = 0, B0 = 0;
         for (j = 0; j < deg; j++)
         {
-            if (prob[j * NT] < ave)
+            if (s_prob[at(j, t)] < ave)
                 ring[slot(S0++)] = (uint8_t)j;
             else
                 ring[slot(deg - 1 - B0++)] = (uint8_t)j;
@@ -751,16 +924,15 @@ __global__ void __launch_bounds__(NT) alias_thread_kernel(GraphView g, TC tc, Bu
         /* pairing; pt/qt are the push slots (ph + lp) mod S0 and (qh + lq) mod B0 */
         uint32_t ph = 0, pt = 0, lp = S0, qh = 0, qt = 0, lq = B0, nb_out = 0;
         Bucket *ob = out + e0;
-        const uint32_t *nb = g.nbr + e0;
         while (lp != 0 && lq != 0)
         {
             const uint32_t pi = ring[slot(ph)], qi = ring[slot(deg - 1 - qh)];
             ph = ph + 1 == S0 ? 0 : ph + 1;
             qh = qh + 1 == B0 ? 0 : qh + 1;
-            const float pv = prob[pi * NT], qv = prob[qi * NT];
-            ob[nb_out++] = Bucket::make(fdiv(pv, ave), pi, qi, nb, vcur);
+            const float pv = s_prob[at(pi, t)], qv = s_prob[at(qi, t)];
+            ob[nb_out++] = Bucket::make_n(fdiv(pv, ave), pi, qi, s_nb[at(pi, t)], s_nb[at(qi, t)], vcur);
             const float r = fsub(qv, fsub(ave, pv));
-            prob[qi * NT] = r;
+            s_prob[at(qi, t)] = r;
             if (r < ave)
             {
                 ring[slot(pt)] = (uint8_t)qi;
@@ -777,12 +949,14 @@ __global__ void __launch_bounds__(NT) alias_thread_kernel(GraphView g, TC tc, Bu
         /* leftovers (:623-638): the rest of whichever queue is non-empty */
         for (; lp != 0; lp--)
         {
-            ob[nb_out++] = Bucket::make(1.0f, ring[slot(ph)], kNone, nb, vcur);
+            const uint32_t pi = ring[slot(ph)];
+            ob[nb_out++] = Bucket::make_n(1.0f, pi, kNone, s_nb[at(pi, t)], 0, vcur);
             ph = ph + 1 == S0 ? 0 : ph + 1;
         }
         for (; lq != 0; lq--)
         {
-            ob[nb_out++] = Bucket::make(1.0f, ring[slot(deg - 1 - qh)], kNone, nb, vcur);
+            const uint32_t qi = ring[slot(deg - 1 - qh)];
+            ob[nb_out++] = Bucket::make_n(1.0f, qi, kNone, s_nb[at(qi, t)], 0, vcur);
             qh = qh + 1 == B0 ? 0 : qh + 1;
         }
     }
@@ -1067,6 +1241,12 @@ __device__ __forceinline__ bool walk_step(const GraphView &g, const WC &wc, cons
     Cand ac{kNone, 0, 0, false};
     bool taken = false;
     uint32_t trials = 0;
+    /* the outlier bound of this step: the hook is a pure function of (walker,
+     * vertex, adjacency), all fixed within a step, so one call serves every
+     * trial (the reference calls it per trial with the same arguments) */
+    real_t ob_c = 0.0f;
+    vertex_id_t on_c = 0;
+    bool ob_known = false;
     if constexpr (TC::order == 1)
     {
         const real_t ext = tc.extension_comp(w, v);
@@ -1081,9 +1261,13 @@ __device__ __forceinline__ bool walk_step(const GraphView &g, const WC &wc, cons
             }
             if constexpr (TC::has_outlier)
             {
-                real_t ob = 0.0f;
-                vertex_id_t on = 0;
-                tc.outlier_upperbound(w, v, adj, ob, on);
+                if (!ob_known)
+                {
+                    tc.outlier_upperbound(w, v, adj, ob_c, on_c);
+                    ob_known = true;
+                }
+                const real_t ob = ob_c;
+                const vertex_id_t on = on_c;
                 if (ob > 0.0f && on > 0)
                 {
                     const float rav = regular_area<TC>(tc, ra, L, v, adj);
@@ -1157,9 +1341,13 @@ __device__ __forceinline__ bool walk_step(const GraphView &g, const WC &wc, cons
                 bool in_app = false;
                 if constexpr (TC::has_outlier)
                 {
-                    real_t ob = 0.0f;
-                    vertex_id_t on = 0;
-                    tc.outlier_upperbound(w, v, adj, ob, on);
+                    if (!ob_known)
+                    {
+                        tc.outlier_upperbound(w, v, adj, ob_c, on_c);
+                        ob_known = true;
+                    }
+                    const real_t ob = ob_c;
+                    const vertex_id_t on = on_c;
                     if (ob > 0.0f && on > 0)
                     {
                         const float rav = regular_area<TC>(tc, ra, L, v, adj);

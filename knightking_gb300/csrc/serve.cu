@@ -52,9 +52,10 @@ uint64_t request_bytes(const kk_walk_opts &o)
     return (uint64_t)o.walker_num * (((uint64_t)o.walk_length + 1) * 4 + 4);
 }
 
-/* One job's paths from a finished batch, to the host, in the batch layout
- * (walker i's vertices at offset i * (walk_length + 1)). */
-kk_paths *job_paths(const BatchJob &b, const uint32_t *h_len_all, const uint32_t *d_path, cudaStream_t st)
+/* One job's paths from a finished batch whose path buffer was copied to the
+ * pinned staging h_path, in the batch layout (walker i's vertices at offset
+ * i * (walk_length + 1)). */
+kk_paths *job_paths(const BatchJob &b, const uint32_t *h_len_all, const uint32_t *h_path)
 {
     kk_paths *p = (kk_paths *)calloc(1, sizeof(kk_paths));
     if (!p)
@@ -80,15 +81,7 @@ kk_paths *job_paths(const BatchJob &b, const uint32_t *h_len_all, const uint32_t
     }
     p->total_steps = total - n;
     if (n != 0)
-    {
-        cudaError_t err = cudaMemcpyAsync(p->vertices, d_path + b.path_base, (size_t)n * b.cap * 4,
-                                          cudaMemcpyDeviceToHost, st);
-        if (err != cudaSuccess)
-        {
-            kk_paths_free(p);
-            fail(KK_ERR_CUDA, std::string("path copy: ") + cudaGetErrorString(err));
-        }
-    }
+        memcpy(p->vertices, h_path + b.path_base, (size_t)n * b.cap * 4);
     return p;
 }
 
@@ -107,6 +100,7 @@ struct kk_server
     bool stopping = false;
     int prev_alias_cache = 0;
     std::vector<BatchSlot> slots;
+    std::vector<uint32_t *> staging; /* pinned host copy of each slot's path buffer */
     std::vector<std::thread> threads;
     /* statistics of completed requests */
     std::vector<double> latencies;
@@ -155,10 +149,11 @@ void slot_loop(kk_server *s, int k)
             std::vector<uint32_t> h_len(plan.total + 1);
             KK_CUDA_CHECK(cudaMemcpyAsync(h_len.data(), slot.length.p, (size_t)plan.total * 4,
                                           cudaMemcpyDeviceToHost, slot.stream));
+            KK_CUDA_CHECK(cudaMemcpyAsync(s->staging[k], slot.path.p, plan.total_cap * 4, cudaMemcpyDeviceToHost,
+                                          slot.stream));
             KK_CUDA_CHECK(cudaStreamSynchronize(slot.stream));
             for (size_t j = 0; j < n; j++)
-                paths[j] = job_paths(plan.jobs[j], h_len.data(), (const uint32_t *)slot.path.p, slot.stream);
-            KK_CUDA_CHECK(cudaStreamSynchronize(slot.stream));
+                paths[j] = job_paths(plan.jobs[j], h_len.data(), s->staging[k]);
         }
         catch (const Error &x)
         {
@@ -248,8 +243,12 @@ kk_status kk_serve_start(kk_engine *e, const kk_serve_opts *opts, kk_server **ou
         batch_prepare(e, plan);
         KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
         s->slots.resize(o.slots);
-        for (BatchSlot &sl : s->slots)
-            KK_CUDA_CHECK(cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking));
+        s->staging.assign(o.slots, nullptr);
+        for (int k = 0; k < o.slots; k++)
+        {
+            KK_CUDA_CHECK(cudaStreamCreateWithFlags(&s->slots[k].stream, cudaStreamNonBlocking));
+            KK_CUDA_CHECK(cudaHostAlloc((void **)&s->staging[k], o.slot_bytes, cudaHostAllocDefault));
+        }
         for (int k = 0; k < o.slots; k++)
             s->threads.emplace_back(slot_loop, s, k);
     });
@@ -263,6 +262,9 @@ kk_status kk_serve_start(kk_engine *e, const kk_serve_opts *opts, kk_server **ou
                 cudaStreamDestroy(sl.stream);
             sl.release();
         }
+        for (uint32_t *h : s->staging)
+            if (h)
+                cudaFreeHost(h);
         delete s;
         return st;
     }
@@ -377,6 +379,9 @@ kk_status kk_serve_stop(kk_server *s)
         }
         sl.release();
     }
+    for (uint32_t *h : s->staging)
+        if (h)
+            cudaFreeHost(h);
     for (auto &kv : s->done)
         kk_paths_free(kv.second.paths);
     s->e->alias_cache = s->prev_alias_cache;

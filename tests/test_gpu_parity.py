@@ -233,10 +233,11 @@ def test_alias_tables_match_oracle_rmat16(engine, oracle_lib, weights):
 
 @pytest.mark.parametrize("dist", ["lognormal", "pareto", "uniform", "equal", "twovalue"])
 def test_alias_tables_match_oracle_hubs(engine, oracle_lib, dist):
-    """Hubs of degree 40000, 5000, 300 and 31 exercise the block kernel, the
-    warp kernel with queues in global scratch and in shared memory."""
+    """Degrees 40000 (block kernel), 12000 / 5000 / 600 (warp kernel, rings in
+    the global scratch), 300 / 129 (warp kernel, rings in shared memory), 100
+    and 31 plus many small ones (thread tiers)."""
     rng = np.random.default_rng(17)
-    degs = [40000, 5000, 300, 31] + list(rng.integers(0, 40, size=2000))
+    degs = [40000, 12000, 5000, 600, 300, 129, 100, 31] + list(rng.integers(0, 40, size=2000))
     V = 60000
     degs = np.array(degs + [0] * (V - len(degs)), np.int64)
     off = np.zeros(V + 1, np.int64)

@@ -410,7 +410,9 @@ def run_serve_bench(args, wl, world, rank, local):
                        "parallelism": "replicas", "l2": "inputs larger than L2", "slots": 2, "max_jobs": 256,
                        "tuned": best, "tuning_ms": [[c, ms] for c, ms in tune_table]},
             "served": {"value": served_value, "what": "all requests submitted at once; submit -> paths on host",
-                       "batches": sat["batches"], "mean_batch_jobs": sat["mean_batch_jobs"]},
+                       "batches": sat["batches"], "mean_batch_jobs": sat["mean_batch_jobs"],
+                       "slot_time_ms": {"walk": sat["walk_ms"], "copy_to_pinned": sat["copy_ms"],
+                                        "per_request_copies": sat["host_ms"]}},
             "latency": {"offered_rate_req_s": rate, "p50_ms": lat["p50_ms"], "p99_ms": lat["p99_ms"],
                         "mean_ms": lat["mean_ms"], "throughput": open_steps / open_s,
                         "what": "open-loop Poisson arrivals at 70% of the saturated rate"},

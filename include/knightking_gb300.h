@@ -111,7 +111,8 @@ kk_status kk_engine_set_stream(kk_engine *e, void *stream);
  *                        sorted adjacency, as node2vec.hpp:159-166
  *   "l2_fetch_bytes"     the context's cudaLimitMaxL2FetchGranularity while the engine
  *                        lives: 32, 64, 128, or 0 for the value found (restored on destroy)
- *   "walk_stats"         1 counts trials, queries and probes (kk_last_walk_stats) */
+ *   "walk_stats"         1 counts trials, queries and probes (kk_last_walk_stats)
+ *   "alias_mid_tier"     alias build of degrees 33..128: 0 one thread per vertex, 1 a warp per vertex */
 kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value);
 /* Message of the last failed call on this engine ("" if none). */
 const char *kk_last_error(const kk_engine *e);
@@ -252,6 +253,8 @@ typedef struct
     uint64_t walker_steps;
     double p50_ms, p99_ms, mean_ms; /* latency of the completed requests */
     double mean_batch_jobs;
+    double walk_ms, copy_ms, host_ms; /* summed over batches: the batch on the GPU (launch to
+                                         status), its paths to pinned memory, the per-request copies */
 } kk_serve_stats;
 
 kk_status kk_serve_start(kk_engine *e, const kk_serve_opts *opts, kk_server **out);

@@ -102,13 +102,13 @@ struct Node2vecRespond
 {
     const uint32_t *nbr;
     EdgeSetView set;
-    __device__ __forceinline__ bool needs_adjacency() const { return set.slots == nullptr; }
+    __device__ __forceinline__ bool needs_adjacency() const { return set.keys == nullptr; }
     __device__ __forceinline__ void operator()(vertex_id_t target, const vertex_id_t &query, const AdjList &adj,
                                                bool &resp) const
     {
-        if (set.slots != nullptr)
+        if (set.keys != nullptr)
         {
-            resp = edge_set_contains(set, target, query);
+            resp = edge_set_slot(set, target, query) != ~0ull;
             return;
         }
         uint32_t deg = adj.degree();
@@ -141,13 +141,28 @@ struct Node2vecDyn
  * overflow * w(return edge) (weighted), one outlier.  Where the previous
  * vertex is not a neighbour (directed graphs) the reference reads past the
  * adjacency; here the area is empty. */
+/* The position std::lower_bound(N(v), x) of node2vec.hpp:71-78 / :91-97: from
+ * the edge set when x is a neighbour (its smallest index), else by search. */
+__device__ __forceinline__ uint32_t n2v_lower_bound(const uint32_t *nbr, const EdgeSetView &set, vertex_id_t v,
+                                                    const AdjList &adj, vertex_id_t x)
+{
+    if (set.keys != nullptr)
+    {
+        const uint64_t slot = edge_set_slot(set, v, x);
+        if (slot != ~0ull)
+            return __ldg(set.pos + slot);
+    }
+    return lower_bound_adj(nbr, adj.begin, adj.degree(), x);
+}
+
 template <bool Weighted>
 struct Node2vecOutlierUB
 {
     const uint32_t *nbr;
     const float *w;
     real_t overflow;
-    __device__ __forceinline__ void operator()(const Walker<Node2vecState> &wk, vertex_id_t, const AdjList &adj,
+    EdgeSetView set;
+    __device__ __forceinline__ void operator()(const Walker<Node2vecState> &wk, vertex_id_t v, const AdjList &adj,
                                                real_t &area, vertex_id_t &num) const
     {
         num = 1;
@@ -161,7 +176,7 @@ struct Node2vecOutlierUB
                 return;
             }
             uint32_t deg = adj.degree();
-            uint32_t i = lower_bound_adj(nbr, adj.begin, deg, wk.data.previous_vertex);
+            uint32_t i = n2v_lower_bound(nbr, set, v, adj, wk.data.previous_vertex);
             area = i < deg ? fmul(gather(w + adj.begin + i), overflow) : 0.0f;
         }
         else
@@ -175,11 +190,12 @@ struct Node2vecOutlierUB
 struct Node2vecOutlierSearch
 {
     const uint32_t *nbr;
-    __device__ __forceinline__ bool operator()(const Walker<Node2vecState> &wk, vertex_id_t, const AdjList &adj,
+    EdgeSetView set;
+    __device__ __forceinline__ bool operator()(const Walker<Node2vecState> &wk, vertex_id_t v, const AdjList &adj,
                                                vertex_id_t, AdjUnit &out) const
     {
         uint32_t deg = adj.degree();
-        uint32_t i = lower_bound_adj(nbr, adj.begin, deg, wk.data.previous_vertex);
+        uint32_t i = n2v_lower_bound(nbr, set, v, adj, wk.data.previous_vertex);
         if (i >= deg)
             return false;
         out = AdjUnit{gather(nbr + adj.begin + i), adj.begin + i};
@@ -332,8 +348,8 @@ struct Node2vecBatch
         tc.dynamic_comp = Node2vecDyn{j.c[0], j.c[3], j.c[4]};
         tc.dcomp_upperbound = ConstBound{j.c[0]};
         tc.dcomp_lowerbound = ConstBound{j.c[1]};
-        tc.outlier_upperbound = Node2vecOutlierUB<Weighted>{nbr, w, j.c[2]};
-        tc.outlier_search = Node2vecOutlierSearch{nbr};
+        tc.outlier_upperbound = Node2vecOutlierUB<Weighted>{nbr, w, j.c[2], set};
+        tc.outlier_search = Node2vecOutlierSearch{nbr, set};
     }
 };
 

@@ -148,18 +148,19 @@ struct kk_engine
     cudaStream_t side = nullptr; /* hub alias builds run here, joined by events */
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     /* vertices by degree, descending (cached per graph), and the alias tiers:
-     * [0, n_hub) hubs, [n_hub, n_warp) warp tier, [n_warp, n_t32) degree
-     * 33..128, [n_t32, n_nz) degree 1..32, rest isolated */
+     * [0, n_hub) hubs, [n_hub, n_warp) warp tier (rings in the scratch up to
+     * n_staged, in shared memory after), [n_warp, n_t32) degree 33..128,
+     * [n_t32, n_nz) degree 1..32, rest isolated */
     kk::DevBuf order;
-    uint32_t n_hub = 0, n_warp = 0, n_t32 = 0, n_nz = 0;
+    uint32_t n_hub = 0, n_staged = 0, n_warp = 0, n_t32 = 0, n_nz = 0;
     bool order_valid = false;
     kk::DevBuf vcur; /* vertex cursors (begin | degree << 40), cached per graph */
     bool vcur_valid = false;
     /* node2vec adjacency test: 0 edge set (built once per graph), 1 binary
      * search of the sorted adjacency (option node2vec_adjacency) */
     int n2v_adjacency = 0;
-    kk::DevBuf edge_set;
-    uint64_t edge_set_mask = 0;
+    kk::DevBuf edge_set, edge_pos;
+    uint64_t edge_set_nb = 0;
     bool edge_set_valid = false;
     kk::DevBuf schemes;    /* metapath schemes of the running job */
     kk::BatchSlot bslot;   /* where the synchronous batch calls run */
@@ -190,6 +191,9 @@ struct kk_engine
      * e->alias hold (0 cursor, 1 index), -1 none. */
     int alias_cache = 0;
     int alias_cached = -1;
+    /* alias_mid_tier (option): degrees 33..128 by the thread tier (0) or by
+     * the warp kernel with staged rows (1) */
+    int alias_mid_tier = 0;
     /* l2_fetch_bytes (option): the context's cudaLimitMaxL2FetchGranularity
      * hint while the engine lives (0: left as found); the value found is put
      * back when the option returns to 0 and when the engine is destroyed. */
@@ -377,13 +381,22 @@ void build_alias(kk_engine *e, const TC &tc)
                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kAliasPairSmem));
             smem_set = true;
         }
-        const uint32_t n = e->n_warp - e->n_hub;
-        unsigned grid = (n + 7) / 8 < 4 * sms ? (n + 7) / 8 : 4 * sms;
-        alias_pair_kernel<TC, Bucket><<<grid, 256, kAliasPairSmem, e->stream>>>(g, tc, alias, vcur, sum, scratch,
-                                                                                order, e->n_hub, e->n_warp);
+        /* two launches: rows with rings in the scratch, then rows staged in
+         * shared memory (separate kernels in a launch list) */
+        const uint32_t bounds[3] = {e->n_hub, e->n_staged, e->alias_mid_tier ? e->n_t32 : e->n_warp};
+        for (int r = 0; r < 2; r++)
+        {
+            const uint32_t n = bounds[r + 1] - bounds[r];
+            if (n == 0)
+                continue;
+            unsigned grid = (n + 7) / 8 < 4 * sms ? (n + 7) / 8 : 4 * sms;
+            alias_pair_kernel<TC, Bucket><<<grid, 256, kAliasPairSmem, e->stream>>>(
+                g, tc, alias, vcur, sum, scratch, order, bounds[r], bounds[r + 1]);
+            KK_CUDA_CHECK(cudaGetLastError());
+        }
         KK_CUDA_CHECK(cudaGetLastError());
     }
-    if (e->n_t32 > e->n_warp)
+    if (e->n_t32 > e->n_warp && !e->alias_mid_tier)
         launch_alias_thread<TC, Bucket, kAliasThreadMax, 64>(e, tc, alias, vcur, sum, order, e->n_warp, e->n_t32);
     if (e->n_nz > e->n_t32)
         launch_alias_thread<TC, Bucket, kAliasThreadSmall, 256>(e, tc, alias, vcur, sum, order, e->n_t32, e->n_nz);

@@ -108,19 +108,24 @@ struct SecondOrderTransitionConfig
 };
 
 /* ---- edge set ---------------------------------------------------------------
- * Exact membership of directed edges (u, v): open addressing over 32 B
- * buckets of four 64-bit keys u << 32 | v, linear probing bucket by bucket,
- * a power-of-two bucket count with load at most 1/2.  Keys only ever go from
- * empty to filled and an insert moves past a bucket only when all four slots
- * hold other keys, so a lookup that meets an empty slot may stop.  A lookup
- * reads one 32 B sector in the common case, where a binary search of a sorted
- * adjacency reads about log2(degree) dependent sectors. */
+ * Exact lookup of directed edges (u, v): open addressing over 32 B buckets of
+ * four 64-bit keys u << 32 | v (one sector), linear probing bucket by bucket
+ * from bucket mulhi(mix(key), nbuckets), 4 * nbuckets >= 4E so the load is at
+ * most 1/4 and a lookup rarely leaves its first bucket.
+ * Beside each key slot a 32-bit position: the smallest index of (u, v) within
+ * u's adjacency, which for a sorted adjacency is std::lower_bound's position
+ * of v in N(u).  Keys only go from empty to filled and an insert moves past a
+ * bucket only when all four of its slots hold other keys, so a lookup that
+ * meets an empty slot may stop.  A membership test reads one 32 B sector in
+ * the common case, where a binary search of a sorted adjacency reads about
+ * log2(degree) dependent sectors. */
 constexpr uint64_t kEdgeSetEmpty = ~0ull;
 
 struct EdgeSetView
 {
-    const uint64_t *slots; /* 4 * (bucket_mask + 1) keys; nullptr: no set */
-    uint64_t bucket_mask;
+    const uint64_t *keys; /* 4 per bucket; nullptr: no set */
+    const uint32_t *pos;  /* position within the source's adjacency, per key slot */
+    uint64_t nbuckets;
 };
 
 /* splitmix64 finalizer (Steele, Lea, Flood, OOPSLA 2014) */
@@ -134,65 +139,80 @@ __host__ __device__ __forceinline__ uint64_t mix64(uint64_t x)
     return x;
 }
 
-__device__ __forceinline__ bool edge_set_contains(const EdgeSetView &s, vertex_id_t u, vertex_id_t v)
+/* The slot of edge (u, v), or ~0 when (u, v) is not an edge. */
+__device__ __forceinline__ uint64_t edge_set_slot(const EdgeSetView &s, vertex_id_t u, vertex_id_t v)
 {
     const uint64_t key = ((uint64_t)u << 32) | v;
-    uint64_t b = mix64(key) & s.bucket_mask;
-    for (uint64_t probe = 0; probe <= s.bucket_mask; probe++)
+    uint64_t b = __umul64hi(mix64(key), s.nbuckets);
+    for (uint64_t probe = 0; probe < s.nbuckets; probe++)
     {
-        const uint4 *p = reinterpret_cast<const uint4 *>(s.slots + b * 4);
-        const uint4 x = __ldg(p), y = __ldg(p + 1);
-        const uint64_t k0 = ((uint64_t)x.y << 32) | x.x, k1 = ((uint64_t)x.w << 32) | x.z;
-        const uint64_t k2 = ((uint64_t)y.y << 32) | y.x, k3 = ((uint64_t)y.w << 32) | y.z;
-        if (k0 == key || k1 == key || k2 == key || k3 == key)
-            return true;
-        if (k0 == kEdgeSetEmpty || k1 == kEdgeSetEmpty || k2 == kEdgeSetEmpty || k3 == kEdgeSetEmpty)
-            return false;
-        b = (b + 1) & s.bucket_mask;
+        const uint4 *p = reinterpret_cast<const uint4 *>(s.keys + b * 4);
+        uint4 q[2];
+#pragma unroll
+        for (int j = 0; j < 2; j++)
+            q[j] = __ldg(p + j);
+#pragma unroll
+        for (int j = 0; j < 2; j++)
+        {
+            const uint64_t k0 = ((uint64_t)q[j].y << 32) | q[j].x, k1 = ((uint64_t)q[j].w << 32) | q[j].z;
+            if (k0 == key)
+                return b * 4 + 2 * j;
+            if (k1 == key)
+                return b * 4 + 2 * j + 1;
+            if (k0 == kEdgeSetEmpty || k1 == kEdgeSetEmpty)
+                return ~0ull;
+        }
+        b = b + 1 == s.nbuckets ? 0 : b + 1;
     }
-    return false;
+    return ~0ull;
 }
 
-__device__ __forceinline__ void edge_set_insert(uint64_t *slots, uint64_t bucket_mask, vertex_id_t u, vertex_id_t v)
+__device__ __forceinline__ void edge_set_insert(uint64_t *keys, uint32_t *pos, uint64_t nbuckets, vertex_id_t u,
+                                                vertex_id_t v, uint32_t local)
 {
     const uint64_t key = ((uint64_t)u << 32) | v;
-    uint64_t b = mix64(key) & bucket_mask;
-    for (uint64_t probe = 0; probe <= bucket_mask; probe++)
+    uint64_t b = __umul64hi(mix64(key), nbuckets);
+    for (uint64_t probe = 0; probe < nbuckets; probe++)
     {
         for (int j = 0; j < 4; j++)
         {
-            const unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long *>(slots + b * 4 + j),
-                                                     (unsigned long long)kEdgeSetEmpty, (unsigned long long)key);
+            unsigned long long *k = reinterpret_cast<unsigned long long *>(keys + b * 4 + j);
+            const unsigned long long old = atomicCAS(k, (unsigned long long)kEdgeSetEmpty, (unsigned long long)key);
             if (old == kEdgeSetEmpty || old == key)
+            {
+                atomicMin(pos + b * 4 + j, local);
                 return;
+            }
         }
-        b = (b + 1) & bucket_mask;
+        b = b + 1 == nbuckets ? 0 : b + 1;
     }
 }
 
 /* Inserts the out-edges of the vertices order[lo, hi): a block per vertex
  * (hubs) or a warp per vertex. */
-static __global__ void edge_set_block_kernel(GraphView g, uint64_t *slots, uint64_t mask, const uint32_t *order,
-                                             uint32_t lo, uint32_t hi)
+static __global__ void edge_set_block_kernel(GraphView g, uint64_t *keys, uint32_t *pos, uint64_t nbuckets,
+                                             const uint32_t *order, uint32_t lo, uint32_t hi)
 {
     for (uint32_t k = lo + blockIdx.x; k < hi; k += gridDim.x)
     {
         const uint32_t v = order[k];
-        for (int64_t e = g.off[v] + threadIdx.x; e < g.off[v + 1]; e += blockDim.x)
-            edge_set_insert(slots, mask, v, g.nbr[e]);
+        const int64_t e0 = g.off[v];
+        for (int64_t e = e0 + threadIdx.x; e < g.off[v + 1]; e += blockDim.x)
+            edge_set_insert(keys, pos, nbuckets, v, g.nbr[e], (uint32_t)(e - e0));
     }
 }
 
-static __global__ void edge_set_warp_kernel(GraphView g, uint64_t *slots, uint64_t mask, const uint32_t *order,
-                                            uint32_t lo, uint32_t hi)
+static __global__ void edge_set_warp_kernel(GraphView g, uint64_t *keys, uint32_t *pos, uint64_t nbuckets,
+                                            const uint32_t *order, uint32_t lo, uint32_t hi)
 {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t k = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); k < hi; k += nwarps)
     {
         const uint32_t v = order[k];
-        for (int64_t e = g.off[v] + lane; e < g.off[v + 1]; e += 32)
-            edge_set_insert(slots, mask, v, g.nbr[e]);
+        const int64_t e0 = g.off[v];
+        for (int64_t e = e0 + lane; e < g.off[v + 1]; e += 32)
+            edge_set_insert(keys, pos, nbuckets, v, g.nbr[e], (uint32_t)(e - e0));
     }
 }
 
@@ -976,7 +996,7 @@ static __global__ void degree_keys_kernel(GraphView g, uint32_t *deg, uint32_t *
  * of degree > thr[i] (bounds zeroed by the caller). */
 struct TierThresholds
 {
-    uint32_t thr[4];
+    uint32_t thr[5];
 };
 
 static __global__ void tier_bounds_kernel(const uint32_t *sorted_deg, uint32_t n, TierThresholds t, uint32_t *bounds)
@@ -985,7 +1005,7 @@ static __global__ void tier_bounds_kernel(const uint32_t *sorted_deg, uint32_t n
     {
         const uint32_t d = sorted_deg[i], dn = i + 1 < n ? sorted_deg[i + 1] : 0;
 #pragma unroll
-        for (int k = 0; k < 4; k++)
+        for (int k = 0; k < 5; k++)
             if (d > t.thr[k] && dn <= t.thr[k])
                 bounds[k] = i + 1;
     }
@@ -1156,6 +1176,12 @@ struct WalkerRun
     uint32_t *out;
     uint32_t cap;
     uint32_t len;
+    /* the current step: started (stream entered), extension still to test,
+     * its trials so far, and its outlier bound once computed */
+    bool in_step, need_ext, ob_known;
+    uint32_t step_trials;
+    real_t ob_c;
+    vertex_id_t on_c;
     /* access counts of the walk (reported when the launch asks for them):
      * rejection trials, second-order queries, and the probes a binary search
      * of the target's sorted adjacency takes for those queries */
@@ -1202,98 +1228,166 @@ __device__ __forceinline__ void walk_begin(const GraphView &g, const WC &wc, con
     if (r.out)
         r.out[0] = r.v;
     r.len = 1;
+    r.in_step = r.need_ext = r.ob_known = false;
+    r.step_trials = 0;
+    r.ob_c = 0.0f;
+    r.on_c = 0;
     r.trials = r.queries = r.probes = 0;
 }
 
-/* One step of one walker; false when its walk ends.
+/* One rejection trial of one walker; false when its walk ends.  The kernels
+ * loop over trials, not steps: a lane whose trial is accepted starts its next
+ * step on the next iteration instead of waiting for the warp's slowest
+ * walker to finish its trials (the reference's second order likewise runs one
+ * trial per walker per superstep).  The draws are those of the per-step loop:
+ * the stream is entered once per step and its counter runs across the step's
+ * trials.
  *
- * First order (include/walk.hpp:954-1063): degree 0 ends the walk; the
- * extension test (its draw only when 0 < ext < 1); rejection trials: [outlier
- * appendix: r = gen_float(area * num + regular_area) - regular_area, r > 0
- * picks an outlier], candidate by uniform or alias pick, dart = gen_float(ub)
- * accepted under the lower bound or the dynamic component.
+ * First order (include/walk.hpp:954-1063): at a step's first trial, degree 0
+ * ends the walk, then the extension test (its draw only when 0 < ext < 1).  A
+ * trial: [outlier appendix: r = gen_float(area * num + regular_area) -
+ * regular_area, r > 0 picks an outlier], candidate by uniform or alias pick,
+ * dart = gen_float(ub) accepted under the lower bound or the dynamic
+ * component.
  *
- * Second order (include/walk.hpp:1082-1381): the reference's three supersteps
- * per trial (candidate + query, response, accept) run inline; each pass of the
- * trial loop re-evaluates the extension (and its draw) as the reference does
- * at the start of every superstep (:1167-1172); a lower-bound pre-accept takes
- * the step at once (:1226-1257); an outlier search that returns no edge retries
+ * Second order (include/walk.hpp:1082-1381): a trial is the reference's three
+ * supersteps (candidate + query, response, accept), inline.  It starts by
+ * re-evaluating the extension (and its draw) as the reference does at the
+ * start of every superstep (:1167-1172); a lower-bound pre-accept takes the
+ * step at once (:1226-1257); an outlier search that returns no edge retries
  * without a new extension test (:1176-1258).
  *
- * Then step++, walker_update_state, the path write (include/walk.hpp:1043-1052).
- * The new vertex's adjacency position comes from the taken bucket's cursor
- * when it has one, else it is read from the offsets at the next step. */
+ * An accepted trial: step++, walker_update_state, the path write
+ * (include/walk.hpp:1043-1052).  The new vertex's adjacency position comes
+ * from the taken bucket's cursor when it has one, else it is read from the
+ * offsets when its step starts. */
 template <typename S, typename WC, typename TC, typename Bucket>
-__device__ __forceinline__ bool walk_step(const GraphView &g, const WC &wc, const TC &tc, const Bucket *alias,
-                                          const float *ra, const WalkLaunch &L, WalkerRun<S> &run, Sampler &rng)
+__device__ __forceinline__ bool walk_trial(const GraphView &g, const WC &wc, const TC &tc, const Bucket *alias,
+                                           const float *ra, const WalkLaunch &L, WalkerRun<S> &run, Sampler &rng)
 {
     Walker<S> &w = run.w;
     const vertex_id_t v = run.v;
-    if (run.pos.e0 < 0)
-        run.pos = pos_from_offsets(g, v);
-    const Pos pos = run.pos;
-    const int64_t e0 = pos.e0;
-    const uint32_t deg = pos.deg;
-    if (deg == 0)
-        return false;
-    rng.enter(w.id, w.step, 0);
-    const AdjList adj{(edge_id_t)e0, (edge_id_t)(e0 + deg)};
-    Cand ac{kNone, 0, 0, false};
-    bool taken = false;
-    uint32_t trials = 0;
-    /* the outlier bound of this step: the hook is a pure function of (walker,
-     * vertex, adjacency), all fixed within a step, so one call serves every
-     * trial (the reference calls it per trial with the same arguments) */
-    real_t ob_c = 0.0f;
-    vertex_id_t on_c = 0;
-    bool ob_known = false;
-    if constexpr (TC::order == 1)
+    if constexpr (TC::order == 1 && !TC::has_dynamic)
     {
+        /* every trial is accepted (no dynamic component, hence no outlier):
+         * a step is one trial, without the trial state */
+        if (run.pos.e0 < 0)
+            run.pos = pos_from_offsets(g, v);
+        const Pos pos = run.pos;
+        if (pos.deg == 0)
+            return false;
+        rng.enter(w.id, w.step, 0);
         const real_t ext = tc.extension_comp(w, v);
         if (ext == 0.0f || (ext < 1.0f && rng.gen_float(1.0f) > ext))
             return false;
-        while (!taken)
+        run.trials++;
+        const Cand ac = pick_candidate<TC>(g, alias, pos, rng);
+        w.step++;
+        if constexpr (is_hook<decltype(wc.walker_update_state)>())
+            wc.walker_update_state(w, v, AdjUnit{ac.nbr, (edge_id_t)(pos.e0 + ac.idx)});
+        if (run.out)
         {
-            if (++trials > L.trial_limit)
+            if (run.len >= run.cap)
             {
-                atomicExch(L.status, KK_STATUS_TRIAL_LIMIT);
+                atomicExch(L.status, KK_STATUS_PATH_CAPACITY);
                 return false;
             }
-            if constexpr (TC::has_outlier)
+            run.out[run.len] = ac.nbr;
+        }
+        run.len++;
+        run.pv = v;
+        run.ppos = pos;
+        run.v = ac.nbr;
+        run.pos = ac.has_cur ? pos_from_cursor(g, ac.nbr, ac.cur) : Pos{-1, 0};
+        return true;
+    }
+    if (!run.in_step)
+    {
+        if (run.pos.e0 < 0)
+            run.pos = pos_from_offsets(g, v);
+        if (run.pos.deg == 0)
+            return false;
+        rng.enter(w.id, w.step, 0);
+        run.in_step = true;
+        run.need_ext = true;
+        run.step_trials = 0;
+        run.ob_known = false;
+    }
+    const Pos pos = run.pos;
+    const int64_t e0 = pos.e0;
+    const AdjList adj{(edge_id_t)e0, (edge_id_t)(e0 + pos.deg)};
+    Cand ac{kNone, 0, 0, false};
+    bool taken = false;
+    if (run.need_ext)
+    {
+        /* first order: once per step; second order: at every superstep */
+        const real_t ext = tc.extension_comp(w, v);
+        if (ext == 0.0f || (ext < 1.0f && rng.gen_float(1.0f) > ext))
+        {
+            run.trials += run.step_trials;
+            return false;
+        }
+        run.need_ext = false;
+    }
+    if (++run.step_trials > L.trial_limit)
+    {
+        atomicExch(L.status, KK_STATUS_TRIAL_LIMIT);
+        run.trials += run.step_trials;
+        return false;
+    }
+    /* outlier appendix; the bound is a pure function of (walker, vertex,
+     * adjacency), all fixed within a step, so one call serves every trial */
+    bool in_app = false, found = false;
+    Cand cd{kNone, 0, 0, false};
+    float randval = 0.0f;
+    if constexpr (TC::has_outlier)
+    {
+        if (!run.ob_known)
+        {
+            tc.outlier_upperbound(w, v, adj, run.ob_c, run.on_c);
+            run.ob_known = true;
+        }
+        const real_t ob = run.ob_c;
+        const vertex_id_t on = run.on_c;
+        if (ob > 0.0f && on > 0)
+        {
+            const float rav = regular_area<TC>(tc, ra, L, v, adj);
+            const float r = fsub(rng.gen_float(fadd(fmul(ob, u2f(on)), rav)), rav);
+            if (r > 0.0f)
             {
-                if (!ob_known)
+                in_app = true;
+                uint32_t oi = (uint32_t)fdiv(r, ob);
+                if (oi + 1 > on)
+                    oi = on - 1;
+                AdjUnit cu;
+                if (tc.outlier_search(w, v, adj, oi, cu))
                 {
-                    tc.outlier_upperbound(w, v, adj, ob_c, on_c);
-                    ob_known = true;
-                }
-                const real_t ob = ob_c;
-                const vertex_id_t on = on_c;
-                if (ob > 0.0f && on > 0)
-                {
-                    const float rav = regular_area<TC>(tc, ra, L, v, adj);
-                    const float r = fsub(rng.gen_float(fadd(fmul(ob, u2f(on)), rav)), rav);
-                    if (r > 0.0f)
-                    {
-                        uint32_t oi = (uint32_t)fdiv(r, ob);
-                        if (oi + 1 > on)
-                            oi = on - 1;
-                        AdjUnit cu;
-                        if (tc.outlier_search(w, v, adj, oi, cu))
-                        {
-                            float sc = 1.0f;
-                            if constexpr (TC::has_static)
-                                sc = tc.static_comp(v, cu);
-                            const float r2 = fadd(fdiv(fsub(r, fmul(u2f(oi), ob)), sc), tc.dcomp_upperbound(v, adj));
-                            if (r2 <= tc.dynamic_comp(w, v, cu))
-                            {
-                                ac = Cand{(uint32_t)(cu.index - (edge_id_t)e0), cu.neighbour, 0, false};
-                                taken = true;
-                            }
-                        }
-                        continue;
-                    }
+                    found = true;
+                    float sc = 1.0f;
+                    if constexpr (TC::has_static)
+                        sc = tc.static_comp(v, cu);
+                    randval = fadd(fdiv(fsub(r, fmul(u2f(oi), ob)), sc), tc.dcomp_upperbound(v, adj));
+                    cd = Cand{(uint32_t)(cu.index - (edge_id_t)e0), cu.neighbour, 0, false};
                 }
             }
+        }
+    }
+    if constexpr (TC::order == 1)
+    {
+        bool outlier_trial = false;
+        if constexpr (TC::has_outlier)
+        {
+            /* an outlier trial: accepted against the dynamic component, and
+             * in any case the next trial follows (no extension test) */
+            outlier_trial = in_app;
+            if (in_app && found && randval <= tc.dynamic_comp(w, v, AdjUnit{cd.nbr, (edge_id_t)(e0 + cd.idx)}))
+            {
+                ac = cd;
+                taken = true;
+            }
+        }
+        if (!outlier_trial)
+        {
             const Cand pc = pick_candidate<TC>(g, alias, pos, rng);
             if constexpr (TC::has_dynamic)
             {
@@ -1320,95 +1414,48 @@ __device__ __forceinline__ bool walk_step(const GraphView &g, const WC &wc, cons
     {
         typedef typename TC::query_type Q;
         typedef typename TC::response_type R;
-        for (;;)
+        if (in_app && !found)
+            return true; /* the reference's retry within the superstep: no extension test */
+        bool accepted = false;
+        if (!in_app)
         {
-            const real_t ext = tc.extension_comp(w, v);
-            if (ext == 0.0f || (ext < 1.0f && rng.gen_float(1.0f) > ext))
-            {
-                run.trials += trials;
-                return false;
-            }
-            Cand cd{kNone, 0, 0, false};
-            float randval = 0.0f;
-            bool accepted = false;
-            for (;;)
-            {
-                if (++trials > L.trial_limit)
-                {
-                    atomicExch(L.status, KK_STATUS_TRIAL_LIMIT);
-                    return false;
-                }
-                bool in_app = false;
-                if constexpr (TC::has_outlier)
-                {
-                    if (!ob_known)
-                    {
-                        tc.outlier_upperbound(w, v, adj, ob_c, on_c);
-                        ob_known = true;
-                    }
-                    const real_t ob = ob_c;
-                    const vertex_id_t on = on_c;
-                    if (ob > 0.0f && on > 0)
-                    {
-                        const float rav = regular_area<TC>(tc, ra, L, v, adj);
-                        const float r = fsub(rng.gen_float(fadd(fmul(ob, u2f(on)), rav)), rav);
-                        if (r > 0.0f)
-                        {
-                            in_app = true;
-                            uint32_t oi = (uint32_t)fdiv(r, ob);
-                            if (oi + 1 > on)
-                                oi = on - 1;
-                            AdjUnit cu;
-                            if (tc.outlier_search(w, v, adj, oi, cu))
-                            {
-                                float sc = 1.0f;
-                                if constexpr (TC::has_static)
-                                    sc = tc.static_comp(v, cu);
-                                randval = fadd(fdiv(fsub(r, fmul(u2f(oi), ob)), sc), tc.dcomp_upperbound(v, adj));
-                                cd = Cand{(uint32_t)(cu.index - (edge_id_t)e0), cu.neighbour, 0, false};
-                                break;
-                            }
-                        }
-                    }
-                }
-                if (!in_app)
-                {
-                    cd = pick_candidate<TC>(g, alias, pos, rng);
-                    randval = rng.gen_float(tc.dcomp_upperbound(v, adj));
-                    if constexpr (TC::has_lowerbound)
-                        accepted = randval <= tc.dcomp_lowerbound(v, adj);
-                    break;
-                }
-            }
-            const AdjUnit cu{cd.nbr, (edge_id_t)(e0 + cd.idx)};
-            if (!accepted)
-            {
-                R resp{};
-                Q query{};
-                vertex_id_t target = 0;
-                if (tc.post_query(w, v, cu, target, query))
-                {
-                    AdjList tadj{0, 0};
-                    run.queries++;
-                    if (respond_needs_adjacency(tc.respond_query))
-                    {
-                        const Pos tp =
-                            (target == run.pv && run.ppos.e0 >= 0) ? run.ppos : pos_from_offsets(g, target);
-                        tadj = AdjList{(edge_id_t)tp.e0, (edge_id_t)(tp.e0 + tp.deg)};
-                        run.probes += 32 - __clz(tp.deg);
-                    }
-                    tc.respond_query(target, query, tadj, resp);
-                }
-                accepted = randval <= tc.dynamic_comp(w, resp, v, cu);
-            }
-            if (accepted)
-            {
-                ac = cd;
-                break;
-            }
+            cd = pick_candidate<TC>(g, alias, pos, rng);
+            randval = rng.gen_float(tc.dcomp_upperbound(v, adj));
+            if constexpr (TC::has_lowerbound)
+                accepted = randval <= tc.dcomp_lowerbound(v, adj);
         }
+        const AdjUnit cu{cd.nbr, (edge_id_t)(e0 + cd.idx)};
+        if (!accepted)
+        {
+            R resp{};
+            Q query{};
+            vertex_id_t target = 0;
+            if (tc.post_query(w, v, cu, target, query))
+            {
+                AdjList tadj{0, 0};
+                run.queries++;
+                if (respond_needs_adjacency(tc.respond_query))
+                {
+                    const Pos tp = (target == run.pv && run.ppos.e0 >= 0) ? run.ppos : pos_from_offsets(g, target);
+                    tadj = AdjList{(edge_id_t)tp.e0, (edge_id_t)(tp.e0 + tp.deg)};
+                    run.probes += 32 - __clz(tp.deg);
+                }
+                tc.respond_query(target, query, tadj, resp);
+            }
+            accepted = randval <= tc.dynamic_comp(w, resp, v, cu);
+        }
+        if (!accepted)
+        {
+            run.need_ext = true; /* the next superstep re-tests the extension */
+            return true;
+        }
+        ac = cd;
+        taken = true;
     }
-    run.trials += trials;
+    if (!taken)
+        return true;
+    run.trials += run.step_trials;
+    run.in_step = false;
     w.step++;
     if constexpr (is_hook<decltype(wc.walker_update_state)>())
         wc.walker_update_state(w, v, AdjUnit{ac.nbr, (edge_id_t)(e0 + ac.idx)});
@@ -1434,7 +1481,7 @@ __device__ __forceinline__ bool walk_step(const GraphView &g, const WC &wc, cons
 
 /* One thread per walker for its whole walk, walker state in registers. */
 template <typename S, typename WC, typename TC, typename Bucket>
-__global__ void __launch_bounds__(256) walk_static_kernel(GraphView g, WC wc, TC tc, const Bucket *alias,
+__global__ void __launch_bounds__(256, 4) walk_static_kernel(GraphView g, WC wc, TC tc, const Bucket *alias,
                                                           const float *ra, WalkLaunch L)
 {
     unsigned long long my_steps = 0;
@@ -1450,7 +1497,7 @@ __global__ void __launch_bounds__(256) walk_static_kernel(GraphView g, WC wc, TC
             rng.init(L.seed);
             WalkerRun<S> run;
             walk_begin<S>(g, wc, L, i, run, rng);
-            while (walk_step<S>(g, wc, tc, alias, ra, L, run, rng))
+            while (walk_trial<S>(g, wc, tc, alias, ra, L, run, rng))
             {
             }
             L.length[i] = run.len;
@@ -1490,7 +1537,7 @@ __global__ void __launch_bounds__(256) walk_pool_kernel(GraphView g, WC wc, TC t
         walk_begin<S>(g, wc, L, i, run, rng);
     while (__any_sync(kFullMask, have))
     {
-        if (have && !walk_step<S>(g, wc, tc, alias, ra, L, run, rng))
+        if (have && !walk_trial<S>(g, wc, tc, alias, ra, L, run, rng))
         {
             L.length[i] = run.len;
             my_steps += run.len - 1;
@@ -1531,7 +1578,7 @@ struct BatchJob
  * a walker by binary search over the jobs' first positions (shared memory).
  * App::make(job, wc, tc) builds the job's WalkerConfig / TransitionConfig. */
 template <typename S, typename App, typename Bucket>
-__global__ void __launch_bounds__(256) walk_batch_kernel(GraphView g, App app, const BatchJob *jobs, uint32_t njobs,
+__global__ void __launch_bounds__(256, 4) walk_batch_kernel(GraphView g, App app, const BatchJob *jobs, uint32_t njobs,
                                                          uint32_t total, const Bucket *alias,
                                                          const float *alias_sum, uint32_t *path, uint32_t *length,
                                                          unsigned long long *total_steps, int *status,
@@ -1583,7 +1630,7 @@ __global__ void __launch_bounds__(256) walk_batch_kernel(GraphView g, App app, c
             rng.init(L.seed);
             WalkerRun<S> run;
             walk_begin<S>(g, wc, L, i, run, rng);
-            while (walk_step<S>(g, wc, tc, alias, nullptr, L, run, rng))
+            while (walk_trial<S>(g, wc, tc, alias, nullptr, L, run, rng))
             {
             }
             L.length[i] = run.len;

@@ -98,6 +98,9 @@ class KKServeStats(ctypes.Structure):
         ("p99_ms", ctypes.c_double),
         ("mean_ms", ctypes.c_double),
         ("mean_batch_jobs", ctypes.c_double),
+        ("walk_ms", ctypes.c_double),
+        ("copy_ms", ctypes.c_double),
+        ("host_ms", ctypes.c_double),
     ]
 
 

@@ -34,8 +34,8 @@ void run_n2v(kk_engine *e, const kk_walk_opts &o, const Node2vecConstants &c, co
     tc.dcomp_lowerbound = ConstBound{c.lowerbound};
     if constexpr (Outlier)
     {
-        tc.outlier_upperbound = Node2vecOutlierUB<Weighted>{e->d_nbr, e->d_w, c.overflow};
-        tc.outlier_search = Node2vecOutlierSearch{e->d_nbr};
+        tc.outlier_upperbound = Node2vecOutlierUB<Weighted>{e->d_nbr, e->d_w, c.overflow, set};
+        tc.outlier_search = Node2vecOutlierSearch{e->d_nbr, set};
     }
     WalkerConfig<Node2vecState, NoHook, NoHook, Node2vecUpdate> wc;
     wc.walker_num = rs.walker_num;

@@ -213,8 +213,9 @@ uint64_t run_batch(kk_engine *e, BatchPlan &plan, BatchSlot &slot, bool want_pat
     else if (plan.app == KK_APP_NODE2VEC)
     {
         const EdgeSetView set = p ? e->n2v_adjacency == 0 ? EdgeSetView{(const uint64_t *)e->edge_set.p,
-                                                                         e->edge_set_mask}
-                                                           : EdgeSetView{nullptr, 0}
+                                                                         (const uint32_t *)e->edge_pos.p,
+                                                                         e->edge_set_nb}
+                                                           : EdgeSetView{nullptr, nullptr, 0}
                                   : node2vec_edge_set(e);
         if (plan.weighted)
             launch_batch(e, Node2vecBatch<true>{g.nbr, e->d_w, set}, plan, slot, d_jobs, length, &path, d_steps,

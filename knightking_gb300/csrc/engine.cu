@@ -40,7 +40,7 @@ void kk_engine::free_graph()
     vcur_valid = false;
     edge_set_valid = false;
     alias_cached = -1;
-    n_hub = n_warp = n_t32 = n_nz = 0;
+    n_hub = n_staged = n_warp = n_t32 = n_nz = 0;
     vmask_valid = false;
 }
 
@@ -317,6 +317,7 @@ void kk_engine_destroy(kk_engine *e)
     e->order.release();
     e->vcur.release();
     e->edge_set.release();
+    e->edge_pos.release();
     e->bslot.release();
     if (e->side)
     {
@@ -362,6 +363,8 @@ kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value)
             e->walk_block = (int)value;
         else if (n == "walk_stats" && (value == 0 || value == 1))
             e->walk_stats = (int)value;
+        else if (n == "alias_mid_tier" && (value == 0 || value == 1))
+            e->alias_mid_tier = (int)value;
         else
             fail(KK_ERR_INVALID_CONFIG, "unknown option or value out of range: " + n);
     });

@@ -160,7 +160,7 @@ const uint32_t *vertex_order(kk_engine *e)
     KK_CUDA_CHECK(cudaMalloc(&deg, (size_t)V * 4 + 4));
     KK_CUDA_CHECK(cudaMalloc(&deg_sorted, (size_t)V * 4 + 4));
     KK_CUDA_CHECK(cudaMalloc(&ids, (size_t)V * 4 + 4));
-    KK_CUDA_CHECK(cudaMalloc(&bounds, 16));
+    KK_CUDA_CHECK(cudaMalloc(&bounds, 32));
     uint32_t *order = e->order.as<uint32_t>(V);
     degree_keys_kernel<<<grid_for(e, V, 256), 256, 0, e->stream>>>(e->view(), deg, ids);
     KK_CUDA_CHECK(cudaGetLastError());
@@ -169,21 +169,22 @@ const uint32_t *vertex_order(kk_engine *e)
                                                             32, e->stream));
     KK_CUDA_CHECK(cub::DeviceRadixSort::SortPairsDescending(e->cub_tmp.ensure(bytes), bytes, deg, deg_sorted, ids,
                                                             order, (int64_t)V, 0, 32, e->stream));
-    KK_CUDA_CHECK(cudaMemsetAsync(bounds, 0, 16, e->stream));
-    const TierThresholds thr{{kAliasHubMin - 1, kAliasThreadMax, kAliasThreadSmall, 0}};
+    KK_CUDA_CHECK(cudaMemsetAsync(bounds, 0, 32, e->stream));
+    const TierThresholds thr{{kAliasHubMin - 1, kAliasWarpQueue, kAliasThreadMax, kAliasThreadSmall, 0}};
     tier_bounds_kernel<<<grid_for(e, V, 256), 256, 0, e->stream>>>(deg_sorted, V, thr, bounds);
     KK_CUDA_CHECK(cudaGetLastError());
-    uint32_t h[4];
-    KK_CUDA_CHECK(cudaMemcpyAsync(h, bounds, 16, cudaMemcpyDeviceToHost, e->stream));
+    uint32_t h[5];
+    KK_CUDA_CHECK(cudaMemcpyAsync(h, bounds, 20, cudaMemcpyDeviceToHost, e->stream));
     KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
     cudaFree(deg);
     cudaFree(deg_sorted);
     cudaFree(ids);
     cudaFree(bounds);
     e->n_hub = h[0];
-    e->n_warp = h[1];
-    e->n_t32 = h[2];
-    e->n_nz = h[3];
+    e->n_staged = h[1];
+    e->n_warp = h[2];
+    e->n_t32 = h[3];
+    e->n_nz = h[4];
     e->order_valid = true;
     return order;
 }
@@ -205,32 +206,32 @@ const uint64_t *vertex_cursors(kk_engine *e)
 EdgeSetView node2vec_edge_set(kk_engine *e)
 {
     if (e->n2v_adjacency != 0)
-        return EdgeSetView{nullptr, 0};
+        return EdgeSetView{nullptr, nullptr, 0};
     if (!e->edge_set_valid)
     {
-        uint64_t nb = 1;
-        while (nb * 4 < 2 * e->E)
-            nb <<= 1;
-        uint64_t *slots = e->edge_set.as<uint64_t>(nb * 4);
-        KK_CUDA_CHECK(cudaMemsetAsync(slots, 0xff, nb * 4 * sizeof(uint64_t), e->stream));
+        const uint64_t nb = e->E > 0 ? e->E : 1; /* four slots per bucket: load <= 1/4 */
+        uint64_t *keys = e->edge_set.as<uint64_t>(nb * 4);
+        uint32_t *pos = e->edge_pos.as<uint32_t>(nb * 4);
+        KK_CUDA_CHECK(cudaMemsetAsync(keys, 0xff, nb * 4 * sizeof(uint64_t), e->stream));
+        KK_CUDA_CHECK(cudaMemsetAsync(pos, 0xff, nb * 4 * sizeof(uint32_t), e->stream));
         const uint32_t *order = vertex_order(e);
         const GraphView g = e->view();
         if (e->n_hub)
         {
             const unsigned grid = e->n_hub < 4u * e->sm_count ? e->n_hub : 4u * e->sm_count;
-            edge_set_block_kernel<<<grid, 1024, 0, e->stream>>>(g, slots, nb - 1, order, 0, e->n_hub);
+            edge_set_block_kernel<<<grid, 1024, 0, e->stream>>>(g, keys, pos, nb, order, 0, e->n_hub);
             KK_CUDA_CHECK(cudaGetLastError());
         }
         if (e->n_nz > e->n_hub)
         {
             edge_set_warp_kernel<<<grid_for(e, (uint64_t)(e->n_nz - e->n_hub) * 32, 256), 256, 0, e->stream>>>(
-                g, slots, nb - 1, order, e->n_hub, e->n_nz);
+                g, keys, pos, nb, order, e->n_hub, e->n_nz);
             KK_CUDA_CHECK(cudaGetLastError());
         }
-        e->edge_set_mask = nb - 1;
+        e->edge_set_nb = nb;
         e->edge_set_valid = true;
     }
-    return EdgeSetView{(const uint64_t *)e->edge_set.p, e->edge_set_mask};
+    return EdgeSetView{(const uint64_t *)e->edge_set.p, (const uint32_t *)e->edge_pos.p, e->edge_set_nb};
 }
 
 const uint8_t *metapath_vertex_masks(kk_engine *e)
@@ -267,7 +268,8 @@ void graph_sort_adjacency(kk_engine *e)
         graph_check_sorted(e);
     if (e->sorted == 1)
         return;
-    e->alias_cached = -1; /* the tables follow the adjacency order */
+    e->alias_cached = -1;      /* the tables follow the adjacency order */
+    e->edge_set_valid = false; /* and so do the edge set's indices */
     uint64_t E = e->E;
     uint32_t *nbr_out = nullptr, *idx_in = nullptr, *idx_out = nullptr;
     KK_CUDA_CHECK(cudaMalloc(&nbr_out, E * 4 + 4));

@@ -105,6 +105,7 @@ struct kk_server
     /* statistics of completed requests */
     std::vector<double> latencies;
     uint64_t completed = 0, failed = 0, batches = 0, steps = 0, batch_jobs_sum = 0;
+    double walk_ms = 0.0, copy_ms = 0.0, host_ms = 0.0;
 };
 
 namespace
@@ -142,16 +143,19 @@ void slot_loop(kk_server *s, int k)
         std::vector<kk_paths *> paths(n, nullptr);
         kk_status st = KK_OK;
         uint64_t steps = 0;
+        Clock::time_point t_walked = t_launch, t_copied = t_launch;
         try
         {
             BatchPlan plan = plan_batch(s->e, jobs.data(), (int)n);
             steps = run_batch(s->e, plan, slot, true, true);
+            t_walked = Clock::now();
             std::vector<uint32_t> h_len(plan.total + 1);
             KK_CUDA_CHECK(cudaMemcpyAsync(h_len.data(), slot.length.p, (size_t)plan.total * 4,
                                           cudaMemcpyDeviceToHost, slot.stream));
             KK_CUDA_CHECK(cudaMemcpyAsync(s->staging[k], slot.path.p, plan.total_cap * 4, cudaMemcpyDeviceToHost,
                                           slot.stream));
             KK_CUDA_CHECK(cudaStreamSynchronize(slot.stream));
+            t_copied = Clock::now();
             for (size_t j = 0; j < n; j++)
                 paths[j] = job_paths(plan.jobs[j], h_len.data(), s->staging[k]);
         }
@@ -198,6 +202,9 @@ void slot_loop(kk_server *s, int k)
             s->batches++;
             s->batch_jobs_sum += n;
             s->steps += steps;
+            s->walk_ms += ms_between(t_launch, t_walked);
+            s->copy_ms += ms_between(t_walked, t_copied);
+            s->host_ms += ms_between(t_copied, t_done);
         }
         s->cv_done.notify_all();
     }
@@ -341,6 +348,9 @@ kk_status kk_serve_stats_get(kk_server *s, kk_serve_stats *out)
     out->batches = s->batches;
     out->walker_steps = s->steps;
     out->mean_batch_jobs = s->batches ? (double)s->batch_jobs_sum / (double)s->batches : 0.0;
+    out->walk_ms = s->walk_ms;
+    out->copy_ms = s->copy_ms;
+    out->host_ms = s->host_ms;
     if (!s->latencies.empty())
     {
         std::vector<double> l = s->latencies;

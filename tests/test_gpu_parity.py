@@ -231,8 +231,9 @@ def test_alias_tables_match_oracle_rmat16(engine, oracle_lib, weights):
     _compare_alias(engine, oracle_lib, g["V"], g["off"], g["nbr"], g["w"])
 
 
+@pytest.mark.parametrize("mid_tier", [0, 1])
 @pytest.mark.parametrize("dist", ["lognormal", "pareto", "uniform", "equal", "twovalue"])
-def test_alias_tables_match_oracle_hubs(engine, oracle_lib, dist):
+def test_alias_tables_match_oracle_hubs(engine, oracle_lib, dist, mid_tier):
     """Degrees 40000 (block kernel), 12000 / 5000 / 600 (warp kernel, rings in
     the global scratch), 300 / 129 (warp kernel, rings in shared memory), 100
     and 31 plus many small ones (thread tiers)."""
@@ -256,4 +257,8 @@ def test_alias_tables_match_oracle_hubs(engine, oracle_lib, dist):
         w = np.where(rng.random(E) < 0.9, 1.0, 50.0)
     w = w.astype(np.float32)
     engine.load_arrays(V, off, nbr, w)
-    _compare_alias(engine, oracle_lib, V, off, nbr, w)
+    engine.set_option("alias_mid_tier", mid_tier)
+    try:
+        _compare_alias(engine, oracle_lib, V, off, nbr, w)
+    finally:
+        engine.set_option("alias_mid_tier", 0)

@@ -86,6 +86,7 @@ typedef struct
     uint32_t *length;
     uint64_t *offset;
     uint32_t *vertices;
+    void *owner; /* library-internal: who holds the three arrays (NULL: malloc) */
 } kk_paths;
 
 /* ---- engine ------------------------------------------------------------- */
@@ -126,6 +127,21 @@ const char *kk_status_string(kk_status s);
  * and builds the CSR in HBM with file order kept per source
  * (include/graph.hpp:309-330). */
 kk_status kk_graph_load_binary(kk_engine *e, uint32_t v_num, const char *path, int edge_kind, int make_undirected);
+
+/* Reads a text edge list (read_edge_txt, include/storage.hpp:107-115): one
+ * "src dst" (weighted = 0) or "src dst weight" (weighted = 1) per line, '#' or
+ * '%' lines are comments, any other malformed line fails with KK_ERR_IO; then
+ * as kk_graph_load_binary. */
+kk_status kk_graph_load_text(kk_engine *e, uint32_t v_num, const char *path, int weighted, int make_undirected);
+
+/* gconverter (src/tools/gconverter.cpp:69-100): a text edge list to the
+ * binary Edge<T> file; *edges (nullable) gets the edge count.  Host only. */
+kk_status kk_text_to_binary(const char *text_path, const char *binary_path, int weighted, uint64_t *edges);
+
+/* read_metapath_schemes (src/apps/metascheme.hpp:69-98): a scheme file
+ * ("schemes types", then per scheme its length and length x types 0/1 flags)
+ * into opts' n_schemes / scheme_len / scheme_mask.  Host only. */
+kk_status kk_read_metapath_schemes(const char *path, kk_walk_opts *opts);
 
 /* Uploads a host CSR: off[V+1] int64, nbr[E], w[E] (nullable), type[E] (nullable). */
 kk_status kk_graph_load_arrays(kk_engine *e, uint32_t v_num, uint64_t e_num, const int64_t *off,
@@ -266,6 +282,8 @@ kk_status kk_serve_submit(kk_server *s, const kk_walk_opts *req, uint64_t *ticke
  * is not done yet.  A result is handed out once. */
 kk_status kk_serve_poll(kk_server *s, uint64_t ticket, int timeout_ms, kk_serve_result *out);
 kk_status kk_serve_stats_get(kk_server *s, kk_serve_stats *out);
+/* Starts the statistics afresh (e.g. after a warm-up). */
+kk_status kk_serve_stats_reset(kk_server *s);
 /* Finishes the queued requests, stops the slots and frees the server (results
  * not yet polled are freed). */
 kk_status kk_serve_stop(kk_server *s);

@@ -14,6 +14,7 @@
 #include <string.h>
 
 #include <functional>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -106,6 +107,87 @@ struct BatchSlot
                 cudaEventDestroy(ev[i]);
         ev[0] = ev[1] = ev[2] = nullptr;
     }
+};
+
+/* Pinned host blocks recycled by size class (powers of two from 64 KiB).
+ * Reference-counted: the owner holds one reference and every block handed out
+ * holds one, so blocks may be returned after the owner is gone. */
+struct HostPool
+{
+    std::mutex m;
+    std::vector<std::pair<size_t, void *>> free_blocks; /* (class bytes, block) */
+    size_t cached = 0, limit = 0;
+    int refs = 1;
+
+    static size_t class_of(size_t bytes)
+    {
+        size_t c = 64 * 1024;
+        while (c < bytes)
+            c <<= 1;
+        return c;
+    }
+    /* A block of at least `bytes`; its class in *cls. */
+    void *get(size_t bytes, size_t *cls)
+    {
+        const size_t c = class_of(bytes);
+        *cls = c;
+        {
+            std::lock_guard<std::mutex> lk(m);
+            refs++;
+            for (size_t i = 0; i < free_blocks.size(); i++)
+                if (free_blocks[i].first == c)
+                {
+                    void *p = free_blocks[i].second;
+                    free_blocks[i] = free_blocks.back();
+                    free_blocks.pop_back();
+                    cached -= c;
+                    return p;
+                }
+        }
+        void *p = nullptr;
+        if (cudaHostAlloc(&p, c, cudaHostAllocDefault) != cudaSuccess)
+        {
+            cudaGetLastError();
+            put(nullptr, 0);
+            return nullptr;
+        }
+        return p;
+    }
+    /* Returns a block (nullptr: only the reference) and drops its reference. */
+    void put(void *p, size_t cls)
+    {
+        bool last;
+        {
+            std::lock_guard<std::mutex> lk(m);
+            if (p != nullptr)
+            {
+                if (cached + cls <= limit)
+                {
+                    free_blocks.push_back({cls, p});
+                    cached += cls;
+                    p = nullptr;
+                }
+            }
+            last = --refs == 0;
+        }
+        if (p != nullptr)
+            cudaFreeHost(p);
+        if (last)
+        {
+            for (auto &b : free_blocks)
+                cudaFreeHost(b.second);
+            delete this;
+        }
+    }
+    void release() { put(nullptr, 0); }
+};
+
+/* Owner record of a kk_paths whose arrays live in one pooled block. */
+struct PooledPaths
+{
+    HostPool *pool;
+    void *block;
+    size_t cls;
 };
 
 struct RunSpec

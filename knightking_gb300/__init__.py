@@ -152,6 +152,13 @@ class WalkEngine:
 
     # ---- graph (GraphEngine::load_graph, include/graph.hpp:408-530) ----
     def load_graph(self, v_num, graph_path, load_as_undirected=False, kind="f32"):
+        """load_graph (include/graph.hpp:408-530): kind is a binary Edge<T> kind
+        ("unweighted", "f32", "meta", "meta_f32") or a text edge list ("text",
+        "text_f32")."""
+        if kind in ("text", "text_f32"):
+            self._check(self._lib.kk_graph_load_text(self._h, int(v_num), str(graph_path).encode(),
+                                                     int(kind == "text_f32"), int(bool(load_as_undirected))))
+            return
         self._check(self._lib.kk_graph_load_binary(self._h, int(v_num), str(graph_path).encode(),
                                                    EDGE_KINDS[kind], int(bool(load_as_undirected))))
 
@@ -347,6 +354,24 @@ def metapath(graph, schemes, walker_num, walk_length, walk_conf=None, seed=1, **
     return graph.walk("metapath", walker_num, walk_conf, walk_length=walk_length, schemes=masks, seed=seed, **kw)
 
 
+def text_to_binary(text_path, binary_path, weighted=False):
+    """gconverter (src/tools/gconverter.cpp:69-100): text edge list -> binary
+    Edge<T> file; returns the edge count."""
+    n = ctypes.c_uint64()
+    st = lib().kk_text_to_binary(str(text_path).encode(), str(binary_path).encode(), int(bool(weighted)),
+                                 ctypes.byref(n))
+    _capi.check(st, None)
+    return n.value
+
+
+def read_metapath_scheme_masks(path):
+    """The scheme file as per-state edge-type masks (kk_read_metapath_schemes):
+    a list of schemes, each a list of masks (bit t = type t allowed)."""
+    o = _capi.KKWalkOpts()
+    _capi.check(lib().kk_read_metapath_schemes(str(path).encode(), ctypes.byref(o)), None)
+    return [[int(o.scheme_mask[s][j]) for j in range(o.scheme_len[s])] for s in range(o.n_schemes)]
+
+
 def read_metapath_schemes(path):
     """read_metapath_schemes (src/apps/metascheme.hpp:69-98)."""
     with open(path) as f:
@@ -433,6 +458,9 @@ class Server:
         s = _capi.KKServeStats()
         self._lib.kk_serve_stats_get(self._h, ctypes.byref(s))
         return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def reset_stats(self):
+        self._lib.kk_serve_stats_reset(self._h)
 
     def stop(self):
         if self._h:

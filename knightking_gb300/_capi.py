@@ -65,6 +65,7 @@ class KKPaths(ctypes.Structure):
         ("length", ctypes.POINTER(ctypes.c_uint32)),
         ("offset", ctypes.POINTER(ctypes.c_uint64)),
         ("vertices", ctypes.POINTER(ctypes.c_uint32)),
+        ("owner", ctypes.c_void_p),
     ]
 
 
@@ -116,6 +117,9 @@ _SIGS = {
     "kk_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "kk_graph_load_binary": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]),
     "kk_graph_load_arrays": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_uint64, _P, _P, _P, _P]),
+    "kk_graph_load_text": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]),
+    "kk_text_to_binary": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, _P]),
+    "kk_read_metapath_schemes": (ctypes.c_int, [ctypes.c_char_p, _P]),
     "kk_graph_generate_rmat": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, ctypes.c_double,
                                               ctypes.c_double, ctypes.c_uint64, ctypes.c_int, ctypes.c_int]),
     "kk_graph_info": (ctypes.c_int, [_P, _P, _P, _P, _P]),
@@ -138,6 +142,7 @@ _SIGS = {
     "kk_serve_submit": (ctypes.c_int, [_P, _P, _P]),
     "kk_serve_poll": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.c_int, _P]),
     "kk_serve_stats_get": (ctypes.c_int, [_P, _P]),
+    "kk_serve_stats_reset": (ctypes.c_int, [_P]),
     "kk_serve_stop": (ctypes.c_int, [_P]),
     "kk_paths_free": (None, [_P]),
     "kk_paths_dump": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]),

@@ -51,6 +51,9 @@ void graph_upload(kk_engine *e, uint32_t V, uint64_t E, const int64_t *off, cons
 void graph_load_arrays(kk_engine *e, uint32_t V, uint64_t E, const int64_t *off, const uint32_t *nbr, const float *w,
                        const uint8_t *type);
 void graph_load_binary(kk_engine *e, uint32_t V, const char *path, int kind, int undirected);
+void graph_load_text(kk_engine *e, uint32_t V, const char *path, int weighted, int undirected);
+void parse_text_edges(const char *path, bool weighted, uint32_t V, std::vector<uint32_t> &src,
+                      std::vector<uint32_t> &dst, std::vector<float> &w);
 void graph_generate_rmat(kk_engine *e, uint32_t scale, uint32_t ef, double a, double b, double c, uint64_t seed,
                          int weights, int types);
 
@@ -386,6 +389,85 @@ kk_status kk_graph_load_binary(kk_engine *e, uint32_t v_num, const char *path, i
     });
 }
 
+kk_status kk_graph_load_text(kk_engine *e, uint32_t v_num, const char *path, int weighted, int make_undirected)
+{
+    if (!e)
+        return KK_ERR_INVALID_CONFIG;
+    return guard(e, [&] {
+        if (path == nullptr)
+            fail(KK_ERR_INVALID_CONFIG, "path is NULL");
+        graph_load_text(e, v_num, path, weighted, make_undirected);
+    });
+}
+
+kk_status kk_text_to_binary(const char *text_path, const char *binary_path, int weighted, uint64_t *edges)
+{
+    if (!text_path || !binary_path)
+        return KK_ERR_INVALID_CONFIG;
+    return guard(nullptr, [&] {
+        std::vector<uint32_t> src, dst;
+        std::vector<float> w;
+        parse_text_edges(text_path, weighted != 0, 0xffffffffu, src, dst, w);
+        FILE *f = fopen(binary_path, "wb");
+        if (!f)
+            fail(KK_ERR_IO, std::string("cannot create ") + binary_path);
+        const size_t rec = weighted ? 12 : 8;
+        std::vector<unsigned char> out(src.size() * rec);
+        for (size_t i = 0; i < src.size(); i++)
+        {
+            memcpy(out.data() + i * rec, &src[i], 4);
+            memcpy(out.data() + i * rec + 4, &dst[i], 4);
+            if (weighted)
+                memcpy(out.data() + i * rec + 8, &w[i], 4);
+        }
+        const size_t put = out.empty() ? 0 : fwrite(out.data(), 1, out.size(), f);
+        const bool ok = put == out.size() && fclose(f) == 0;
+        if (!ok)
+            fail(KK_ERR_IO, std::string("write failed: ") + binary_path);
+        if (edges)
+            *edges = src.size();
+    });
+}
+
+kk_status kk_read_metapath_schemes(const char *path, kk_walk_opts *opts)
+{
+    if (!path || !opts)
+        return KK_ERR_INVALID_CONFIG;
+    return guard(nullptr, [&] {
+        FILE *f = fopen(path, "r");
+        if (!f)
+            fail(KK_ERR_IO, std::string("cannot open ") + path);
+        int n = 0, states = 0;
+        bool ok = fscanf(f, "%d %d", &n, &states) == 2 && n >= 1 && n <= KK_MAX_SCHEMES && states >= 1 && states <= 8;
+        int len[KK_MAX_SCHEMES] = {0};
+        uint8_t mask[KK_MAX_SCHEMES][KK_MAX_SCHEME_LEN];
+        memset(mask, 0, sizeof(mask));
+        for (int s = 0; ok && s < n; s++)
+        {
+            ok = fscanf(f, "%d", &len[s]) == 1 && len[s] >= 1 && len[s] <= KK_MAX_SCHEME_LEN;
+            for (int l = 0; ok && l < len[s]; l++)
+                for (int t = 0; ok && t < states; t++)
+                {
+                    int x = 0;
+                    ok = fscanf(f, "%d", &x) == 1;
+                    if (ok && x != 0)
+                        mask[s][l] |= (uint8_t)(1u << t);
+                }
+        }
+        fclose(f);
+        if (!ok)
+            fail(KK_ERR_IO, std::string("malformed metapath scheme file (1..16 schemes of length 1..16 over 1..8 "
+                                        "types): ") + path);
+        opts->n_schemes = n;
+        for (int s = 0; s < KK_MAX_SCHEMES; s++)
+        {
+            opts->scheme_len[s] = s < n ? len[s] : 0;
+            for (int l = 0; l < KK_MAX_SCHEME_LEN; l++)
+                opts->scheme_mask[s][l] = s < n ? mask[s][l] : 0;
+        }
+    });
+}
+
 kk_status kk_graph_load_arrays(kk_engine *e, uint32_t v_num, uint64_t e_num, const int64_t *off, const uint32_t *nbr,
                                const float *w, const uint8_t *type)
 {
@@ -658,9 +740,18 @@ void kk_paths_free(kk_paths *p)
 {
     if (!p)
         return;
-    free(p->length);
-    free(p->offset);
-    free(p->vertices);
+    if (p->owner != nullptr)
+    {
+        kk::PooledPaths *o = (kk::PooledPaths *)p->owner;
+        o->pool->put(o->block, o->cls);
+        delete o;
+    }
+    else
+    {
+        free(p->length);
+        free(p->offset);
+        free(p->vertices);
+    }
     free(p);
 }
 

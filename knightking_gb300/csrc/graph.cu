@@ -17,8 +17,13 @@
  */
 #include <stdio.h>
 
+#include <stdlib.h>
+#include <string.h>
+
 #include <algorithm>
 #include <cub/cub.cuh>
+#include <string>
+#include <thread>
 #include <vector>
 
 #include "knightking_gb300/engine.cuh"
@@ -355,6 +360,231 @@ void graph_load_arrays(kk_engine *e, uint32_t V, uint64_t E, const int64_t *off,
 }
 
 /* include/storage.hpp:35-55 + include/graph.hpp:408-530 on one rank. */
+namespace
+{
+
+__global__ void count_sources_kernel(const uint32_t *src, uint64_t m, unsigned long long *cnt)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x)
+        atomicAdd(cnt + src[i], 1ull);
+}
+
+template <typename T>
+__global__ void permute_kernel(const T *in, const uint32_t *perm, T *out, uint64_t m)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = in[perm[i]];
+}
+
+} // namespace
+
+/* CSR in HBM from an edge list in file order (include/graph.hpp:309-330):
+ * a stable radix sort of the edge positions by source keeps file order within
+ * each source; offsets are the exclusive scan of the source counts. */
+void csr_from_edges(kk_engine *e, uint32_t V, uint64_t m, const uint32_t *h_src, const uint32_t *h_dst,
+                    const float *h_w, const uint8_t *h_t)
+{
+    if (m >= 0xffffffffull)
+        fail(KK_ERR_INVALID_CONFIG, "edge lists are limited to 2^32 - 1 edges");
+    e->free_graph();
+    struct Temps
+    {
+        DevBuf src, src2, idx, perm, cnt, in;
+        ~Temps()
+        {
+            DevBuf *b[] = {&src, &src2, &idx, &perm, &cnt, &in};
+            for (DevBuf *x : b)
+                x->release();
+        }
+    } tmp;
+    uint32_t *d_src = tmp.src.as<uint32_t>(m), *d_src2 = tmp.src2.as<uint32_t>(m);
+    uint32_t *d_idx = tmp.idx.as<uint32_t>(m), *d_perm = tmp.perm.as<uint32_t>(m);
+    KK_CUDA_CHECK(cudaMemcpyAsync(d_src, h_src, m * 4, cudaMemcpyHostToDevice, e->stream));
+    iota_u32_kernel<<<grid_for(e, m, 256), 256, 0, e->stream>>>(d_idx, m);
+    KK_CUDA_CHECK(cudaGetLastError());
+    int bits = 1;
+    while (bits < 32 && ((uint64_t)1 << bits) < V)
+        bits++;
+    size_t bytes = 0;
+    KK_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(nullptr, bytes, d_src, d_src2, d_idx, d_perm, (int64_t)m, 0, bits,
+                                                  e->stream));
+    KK_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(e->cub_tmp.ensure(bytes), bytes, d_src, d_src2, d_idx, d_perm,
+                                                  (int64_t)m, 0, bits, e->stream));
+    /* offsets */
+    unsigned long long *cnt = tmp.cnt.as<unsigned long long>((uint64_t)V + 1);
+    KK_CUDA_CHECK(cudaMemsetAsync(cnt, 0, ((uint64_t)V + 1) * 8, e->stream));
+    count_sources_kernel<<<grid_for(e, m, 256), 256, 0, e->stream>>>(d_src, m, cnt);
+    KK_CUDA_CHECK(cudaGetLastError());
+    KK_CUDA_CHECK(cudaMalloc(&e->d_off, ((uint64_t)V + 1) * sizeof(int64_t)));
+    exclusive_scan_u64(e, (const uint64_t *)cnt, (uint64_t *)e->d_off, (uint64_t)V + 1);
+    /* neighbours, weights, types in sorted order */
+    KK_CUDA_CHECK(cudaMalloc(&e->d_nbr, m * 4 + 4));
+    uint32_t *d_in = tmp.in.as<uint32_t>(m);
+    KK_CUDA_CHECK(cudaMemcpyAsync(d_in, h_dst, m * 4, cudaMemcpyHostToDevice, e->stream));
+    permute_kernel<uint32_t><<<grid_for(e, m, 256), 256, 0, e->stream>>>(d_in, d_perm, e->d_nbr, m);
+    KK_CUDA_CHECK(cudaGetLastError());
+    if (h_w)
+    {
+        KK_CUDA_CHECK(cudaMalloc(&e->d_w, m * 4 + 4));
+        KK_CUDA_CHECK(cudaMemcpyAsync(d_in, h_w, m * 4, cudaMemcpyHostToDevice, e->stream));
+        permute_kernel<float><<<grid_for(e, m, 256), 256, 0, e->stream>>>((const float *)d_in, d_perm, e->d_w, m);
+        KK_CUDA_CHECK(cudaGetLastError());
+    }
+    if (h_t)
+    {
+        KK_CUDA_CHECK(cudaMalloc(&e->d_type, m + 4));
+        KK_CUDA_CHECK(cudaMemcpyAsync(d_in, h_t, m, cudaMemcpyHostToDevice, e->stream));
+        permute_kernel<uint8_t><<<grid_for(e, m, 256), 256, 0, e->stream>>>((const uint8_t *)d_in, d_perm, e->d_type,
+                                                                            m);
+        KK_CUDA_CHECK(cudaGetLastError());
+    }
+    KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+    e->V = V;
+    e->E = m;
+    e->has_graph = true;
+    e->sorted = -1;
+}
+
+/* Text edge lists (read_edge_txt, include/storage.hpp:107-115): "src dst" or
+ * "src dst weight" per line, parsed in parallel over newline-aligned chunks of
+ * the file and kept in file order.  Lines that start with '#' or '%' are
+ * comments; any other malformed line is an error (the reference's fscanf loop
+ * stops or spins there). */
+void parse_text_edges(const char *path, bool weighted, uint32_t V, std::vector<uint32_t> &src,
+                      std::vector<uint32_t> &dst, std::vector<float> &w)
+{
+    FILE *f = fopen(path, "rb");
+    if (!f)
+        fail(KK_ERR_IO, std::string("cannot open ") + path);
+    fseek(f, 0, SEEK_END);
+    const size_t bytes = (size_t)ftell(f);
+    fseek(f, 0, SEEK_SET);
+    std::vector<char> buf(bytes + 1);
+    const size_t got = bytes ? fread(buf.data(), 1, bytes, f) : 0;
+    fclose(f);
+    if (got != bytes)
+        fail(KK_ERR_IO, std::string("short read from ") + path);
+    buf[bytes] = '\0';
+    unsigned nt = std::thread::hardware_concurrency();
+    if (nt == 0)
+        nt = 1;
+    if (nt > 64)
+        nt = 64;
+    if (bytes < (1u << 20))
+        nt = 1;
+    std::vector<size_t> cut(nt + 1, bytes);
+    cut[0] = 0;
+    for (unsigned t = 1; t < nt; t++)
+    {
+        size_t c = bytes / nt * t;
+        while (c < bytes && buf[c - 1] != '\n')
+            c++;
+        cut[t] = c < cut[t - 1] ? cut[t - 1] : c;
+    }
+    struct Part
+    {
+        std::vector<uint32_t> s, d;
+        std::vector<float> w;
+        std::string err;
+    };
+    std::vector<Part> parts(nt);
+    auto work = [&](unsigned t) {
+        Part &pt = parts[t];
+        const char *p = buf.data() + cut[t], *end = buf.data() + cut[t + 1];
+        while (p < end)
+        {
+            const char *eol = (const char *)memchr(p, '\n', (size_t)(end - p));
+            if (!eol)
+                eol = end;
+            const char *q = p;
+            while (q < eol && (*q == ' ' || *q == '\t' || *q == '\r'))
+                q++;
+            if (q < eol && *q != '#' && *q != '%')
+            {
+                char *x;
+                const unsigned long a = strtoul(q, &x, 10);
+                const bool ok_a = x != q;
+                q = x;
+                const unsigned long b = strtoul(q, &x, 10);
+                const bool ok_b = x != q;
+                q = x;
+                float wt = 0.0f;
+                bool ok_w = true;
+                if (weighted)
+                {
+                    wt = strtof(q, &x);
+                    ok_w = x != q;
+                    q = x;
+                }
+                while (q < eol && (*q == ' ' || *q == '\t' || *q == '\r'))
+                    q++;
+                if (!ok_a || !ok_b || !ok_w || q != eol || a >= V || b >= V)
+                {
+                    pt.err = std::string(p, (size_t)(eol - p));
+                    return;
+                }
+                pt.s.push_back((uint32_t)a);
+                pt.d.push_back((uint32_t)b);
+                if (weighted)
+                    pt.w.push_back(wt);
+            }
+            p = eol + 1;
+        }
+    };
+    std::vector<std::thread> th;
+    for (unsigned t = 1; t < nt; t++)
+        th.emplace_back(work, t);
+    work(0);
+    for (auto &x : th)
+        x.join();
+    size_t total = 0;
+    for (auto &pt : parts)
+    {
+        if (!pt.err.empty())
+            fail(KK_ERR_IO, "malformed edge line (or vertex id >= v_num): " + pt.err.substr(0, 80));
+        total += pt.s.size();
+    }
+    src.reserve(total);
+    dst.reserve(total);
+    w.reserve(weighted ? total : 0);
+    for (auto &pt : parts)
+    {
+        src.insert(src.end(), pt.s.begin(), pt.s.end());
+        dst.insert(dst.end(), pt.d.begin(), pt.d.end());
+        if (weighted)
+            w.insert(w.end(), pt.w.begin(), pt.w.end());
+    }
+}
+
+void graph_load_text(kk_engine *e, uint32_t V, const char *path, int weighted, int undirected)
+{
+    if (V == 0)
+        fail(KK_ERR_INVALID_CONFIG, "v_num must be > 0");
+    std::vector<uint32_t> src, dst;
+    std::vector<float> w;
+    parse_text_edges(path, weighted != 0, V, src, dst, w);
+    if (undirected)
+    {
+        /* --make-undirected (include/graph.hpp:430-443): every edge followed by its mirror */
+        const size_t n = src.size();
+        std::vector<uint32_t> s2(2 * n), d2(2 * n);
+        std::vector<float> w2(weighted ? 2 * n : 0);
+        for (size_t i = 0; i < n; i++)
+        {
+            s2[2 * i] = src[i];
+            d2[2 * i] = dst[i];
+            s2[2 * i + 1] = dst[i];
+            d2[2 * i + 1] = src[i];
+            if (weighted)
+                w2[2 * i] = w2[2 * i + 1] = w[i];
+        }
+        src.swap(s2);
+        dst.swap(d2);
+        w.swap(w2);
+    }
+    csr_from_edges(e, V, src.size(), src.data(), dst.data(), weighted ? w.data() : nullptr, nullptr);
+}
+
 void graph_load_binary(kk_engine *e, uint32_t V, const char *path, int kind, int undirected)
 {
     size_t rec;
@@ -428,26 +658,8 @@ void graph_load_binary(kk_engine *e, uint32_t V, const char *path, int kind, int
                 t[j + 1] = (uint8_t)ty;
         }
     }
-    /* stable counting sort by source: file order within a source */
-    std::vector<int64_t> off((size_t)V + 1, 0);
-    for (uint64_t i = 0; i < m; i++)
-        off[src[i] + 1]++;
-    for (uint32_t v = 0; v < V; v++)
-        off[v + 1] += off[v];
-    std::vector<int64_t> pos(off.begin(), off.end() - 1);
-    std::vector<uint32_t> nbr(m + 1);
-    std::vector<float> ws(has_w ? m + 1 : 0);
-    std::vector<uint8_t> ts(has_t ? m + 1 : 0);
-    for (uint64_t i = 0; i < m; i++)
-    {
-        int64_t p = pos[src[i]]++;
-        nbr[p] = dst[i];
-        if (has_w)
-            ws[p] = w[i];
-        if (has_t)
-            ts[p] = t[i];
-    }
-    graph_upload(e, V, m, off.data(), nbr.data(), has_w ? ws.data() : nullptr, has_t ? ts.data() : nullptr);
+    /* file order within a source, sorted on the device */
+    csr_from_edges(e, V, m, src.data(), dst.data(), has_w ? w.data() : nullptr, has_t ? t.data() : nullptr);
 }
 
 void graph_generate_rmat(kk_engine *e, uint32_t scale, uint32_t ef, double a, double b, double c, uint64_t seed,

@@ -52,26 +52,36 @@ uint64_t request_bytes(const kk_walk_opts &o)
     return (uint64_t)o.walker_num * (((uint64_t)o.walk_length + 1) * 4 + 4);
 }
 
-/* One job's paths from a finished batch whose path buffer was copied to the
- * pinned staging h_path, in the batch layout (walker i's vertices at offset
- * i * (walk_length + 1)). */
-kk_paths *job_paths(const BatchJob &b, const uint32_t *h_len_all, const uint32_t *h_path)
+/* One job's paths from a finished batch, in a pooled pinned block: lengths,
+ * offsets (walker i at i * (walk_length + 1)) and the vertices, copied
+ * straight from the slot's path buffer (asynchronously on the slot's stream). */
+kk_paths *job_paths(HostPool *pool, const BatchJob &b, const uint32_t *h_len_all, const uint32_t *d_path,
+                    cudaStream_t st)
 {
-    kk_paths *p = (kk_paths *)calloc(1, sizeof(kk_paths));
-    if (!p)
-        fail(KK_ERR_OOM, "host allocation failed");
     const uint32_t n = b.walker_num;
+    const size_t len_bytes = ((size_t)n * 4 + 15) & ~(size_t)15;
+    const size_t off_bytes = ((size_t)n * 8 + 15) & ~(size_t)15;
+    const size_t vert_bytes = (size_t)n * b.cap * 4;
+    kk_paths *p = (kk_paths *)calloc(1, sizeof(kk_paths));
+    PooledPaths *o = new (std::nothrow) PooledPaths();
+    size_t cls = 0;
+    char *blk = (p && o) ? (char *)pool->get(len_bytes + off_bytes + vert_bytes + 16, &cls) : nullptr;
+    if (!blk)
+    {
+        free(p);
+        delete o;
+        fail(KK_ERR_OOM, "host allocation failed");
+    }
+    o->pool = pool;
+    o->block = blk;
+    o->cls = cls;
+    p->owner = o;
     p->walker_num = n;
     p->walker_begin = b.walker_begin;
     p->epoch_walkers = n;
-    p->length = (uint32_t *)malloc((size_t)n * 4 + 4);
-    p->offset = (uint64_t *)malloc((size_t)n * 8 + 8);
-    p->vertices = (uint32_t *)malloc((size_t)n * b.cap * 4 + 4);
-    if (!p->length || !p->offset || !p->vertices)
-    {
-        kk_paths_free(p);
-        fail(KK_ERR_OOM, "host allocation failed");
-    }
+    p->length = (uint32_t *)blk;
+    p->offset = (uint64_t *)(blk + len_bytes);
+    p->vertices = (uint32_t *)(blk + len_bytes + off_bytes);
     uint64_t total = 0;
     for (uint32_t i = 0; i < n; i++)
     {
@@ -81,7 +91,15 @@ kk_paths *job_paths(const BatchJob &b, const uint32_t *h_len_all, const uint32_t
     }
     p->total_steps = total - n;
     if (n != 0)
-        memcpy(p->vertices, h_path + b.path_base, (size_t)n * b.cap * 4);
+    {
+        const cudaError_t err = cudaMemcpyAsync(p->vertices, d_path + b.path_base, vert_bytes,
+                                                cudaMemcpyDeviceToHost, st);
+        if (err != cudaSuccess)
+        {
+            kk_paths_free(p);
+            fail(KK_ERR_CUDA, std::string("path copy: ") + cudaGetErrorString(err));
+        }
+    }
     return p;
 }
 
@@ -100,7 +118,7 @@ struct kk_server
     bool stopping = false;
     int prev_alias_cache = 0;
     std::vector<BatchSlot> slots;
-    std::vector<uint32_t *> staging; /* pinned host copy of each slot's path buffer */
+    HostPool *pool = nullptr; /* pinned blocks of the results handed out */
     std::vector<std::thread> threads;
     /* statistics of completed requests */
     std::vector<double> latencies;
@@ -152,12 +170,12 @@ void slot_loop(kk_server *s, int k)
             std::vector<uint32_t> h_len(plan.total + 1);
             KK_CUDA_CHECK(cudaMemcpyAsync(h_len.data(), slot.length.p, (size_t)plan.total * 4,
                                           cudaMemcpyDeviceToHost, slot.stream));
-            KK_CUDA_CHECK(cudaMemcpyAsync(s->staging[k], slot.path.p, plan.total_cap * 4, cudaMemcpyDeviceToHost,
-                                          slot.stream));
+            KK_CUDA_CHECK(cudaStreamSynchronize(slot.stream));
+            for (size_t j = 0; j < n; j++)
+                paths[j] = job_paths(s->pool, plan.jobs[j], h_len.data(), (const uint32_t *)slot.path.p,
+                                     slot.stream);
             KK_CUDA_CHECK(cudaStreamSynchronize(slot.stream));
             t_copied = Clock::now();
-            for (size_t j = 0; j < n; j++)
-                paths[j] = job_paths(plan.jobs[j], h_len.data(), s->staging[k]);
         }
         catch (const Error &x)
         {
@@ -250,12 +268,10 @@ kk_status kk_serve_start(kk_engine *e, const kk_serve_opts *opts, kk_server **ou
         batch_prepare(e, plan);
         KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
         s->slots.resize(o.slots);
-        s->staging.assign(o.slots, nullptr);
         for (int k = 0; k < o.slots; k++)
-        {
             KK_CUDA_CHECK(cudaStreamCreateWithFlags(&s->slots[k].stream, cudaStreamNonBlocking));
-            KK_CUDA_CHECK(cudaHostAlloc((void **)&s->staging[k], o.slot_bytes, cudaHostAllocDefault));
-        }
+        s->pool = new HostPool();
+        s->pool->limit = (size_t)o.slots * 2 * o.slot_bytes;
         for (int k = 0; k < o.slots; k++)
             s->threads.emplace_back(slot_loop, s, k);
     });
@@ -269,9 +285,8 @@ kk_status kk_serve_start(kk_engine *e, const kk_serve_opts *opts, kk_server **ou
                 cudaStreamDestroy(sl.stream);
             sl.release();
         }
-        for (uint32_t *h : s->staging)
-            if (h)
-                cudaFreeHost(h);
+        if (s->pool)
+            s->pool->release();
         delete s;
         return st;
     }
@@ -369,6 +384,17 @@ kk_status kk_serve_stats_get(kk_server *s, kk_serve_stats *out)
     return KK_OK;
 }
 
+kk_status kk_serve_stats_reset(kk_server *s)
+{
+    if (!s)
+        return KK_ERR_INVALID_CONFIG;
+    std::lock_guard<std::mutex> lk(s->m);
+    s->latencies.clear();
+    s->completed = s->failed = s->batches = s->steps = s->batch_jobs_sum = 0;
+    s->walk_ms = s->copy_ms = s->host_ms = 0.0;
+    return KK_OK;
+}
+
 kk_status kk_serve_stop(kk_server *s)
 {
     if (!s)
@@ -389,11 +415,9 @@ kk_status kk_serve_stop(kk_server *s)
         }
         sl.release();
     }
-    for (uint32_t *h : s->staging)
-        if (h)
-            cudaFreeHost(h);
     for (auto &kv : s->done)
         kk_paths_free(kv.second.paths);
+    s->pool->release();
     s->e->alias_cache = s->prev_alias_cache;
     delete s;
     return KK_OK;

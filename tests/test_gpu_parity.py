@@ -201,6 +201,31 @@ def test_binary_file_load_matches_file_order(kk, engine, tmp_path):
     np.testing.assert_array_equal(dg2["nbr"], csr["nbr"])
 
 
+@pytest.mark.parametrize("undirected", [False, True])
+def test_text_file_load_matches_file_order(kk, engine, tmp_path, undirected):
+    """Text edge lists (read_edge_txt, include/storage.hpp:107-115) build the
+    same CSR as the binary file, in file order, mirrored edge by edge for
+    --make-undirected; metapath types come from binary files only."""
+    g = G.random_undirected(300, 3000, seed=13, weight="unif")
+    src, dst, w = (g["src"][0::2], g["dst"][0::2], g["w"][0::2]) if undirected else (g["src"], g["dst"], g["w"])
+    f = tmp_path / "g.txt"
+    with open(f, "w") as out:
+        out.write("% a comment\n")
+        for i in range(len(src)):
+            out.write("%d %d %.9g\n" % (src[i], dst[i], w[i]))
+    engine.load_graph(300, f, load_as_undirected=undirected, kind="text_f32")
+    dg = engine.download_graph()
+    csr = G.csr_file_order(300, g["src"], g["dst"], w=g["w"])
+    np.testing.assert_array_equal(dg["off"], csr["off"])
+    np.testing.assert_array_equal(dg["nbr"], csr["nbr"])
+    np.testing.assert_array_equal(dg["w"], csr["w"])
+    # and it walks like the arrays it equals
+    a = engine.walk("deepwalk", 500, seed=5, walk_length=20)
+    engine.load_arrays(300, csr["off"], csr["nbr"], csr["w"])
+    b = engine.walk("deepwalk", 500, seed=5, walk_length=20)
+    np.testing.assert_array_equal(a.vertices, b.vertices)
+
+
 def test_invalid_configs_raise(kk, engine):
     g = G.random_undirected(50, 200, seed=1)
     csr = G.csr_file_order(50, g["src"], g["dst"])

@@ -190,39 +190,48 @@ def walk_kwargs(wl):
     return kw
 
 
-def cpu_sample(g, wl, walkers, threads, seed, target_steps=2_000_000, chunks=16):
-    """Times the oracle (CPU restatement) on a bounded sample of the workload.
+def cpu_sample(g, wl, walkers, threads, seed, target_s=10.0, chunks=16):
+    """Times the oracle (CPU restatement) on a bounded sample of the workload,
+    about target_s seconds of walking on `threads` host threads.
 
     Alias tables (weighted) are built once for the whole graph and their time
     is charged per walker (t_alias * sample/walkers); the walk runs `chunks`
-    contiguous walker-id ranges spread over the id space.
+    contiguous walker-id ranges spread over the id space, sized from a short
+    calibration walk.
     """
     from oracle import pyoracle
     csr = pyoracle.CSR(g["V"], g["off"], g["nbr"], g.get("w"), g.get("type"))
     weighted = g.get("w") is not None
-    per_walker = max(1, wl.get("walk_length", 80))
-    sample = max(chunks * 64, min(walkers, target_steps // per_walker))
-    chunk = max(1, sample // chunks)
     kw = walk_kwargs(wl)
     t_alias = 0.0
     if weighted:
         t0 = time.perf_counter()
         pyoracle.alias_build(csr, threads=threads)
         t_alias = time.perf_counter() - t0
-    steps = 0
-    t_walk = 0.0
-    n_done = 0
-    for c in range(chunks):
-        begin = (walkers // chunks) * c
-        prm = pyoracle.make_params(wl["app"], seed=seed, walker_begin=begin, walker_num=chunk, weighted=weighted, **kw)
-        _, _, st = pyoracle.walk(csr, prm, cap=1, threads=threads, with_paths=False)
-        _, tw = pyoracle.last_timing()
-        steps += st
-        t_walk += tw
-        n_done += chunk
+
+    def run(n_per_chunk):
+        steps, t_walk, n_done = 0, 0.0, 0
+        for c in range(chunks):
+            begin = (walkers // chunks) * c
+            prm = pyoracle.make_params(wl["app"], seed=seed, walker_begin=begin, walker_num=n_per_chunk,
+                                       weighted=weighted, **kw)
+            _, _, st = pyoracle.walk(csr, prm, cap=1, threads=threads, with_paths=False)
+            steps += st
+            t_walk += pyoracle.last_timing()[1]
+            n_done += n_per_chunk
+        return steps, t_walk, n_done
+
+    chunk = max(1, min(walkers // chunks, 256))
+    steps, t_walk, n_done = run(chunk)
+    for _ in range(2):  # grow the sample toward target_s (per-call costs make small runs misleading)
+        if t_walk >= 0.5 * target_s or chunk >= walkers // chunks:
+            break
+        chunk = max(1, min(walkers // chunks, int(chunk * target_s / max(t_walk, 1e-6))))
+        steps, t_walk, n_done = run(chunk)
     t_total = t_walk + t_alias * (n_done / walkers)
     return {
         "value": steps / t_total, "unit": "walker-steps/s", "cores": threads, "kind": "port",
+        "seconds": t_total,
         "sample": "%d walkers in %d id ranges spread over %d (%d steps, %.2f s walking); alias build over the "
                   "full graph %.2f s charged pro rata" % (n_done, chunks, walkers, steps, t_walk, t_alias),
     }
@@ -238,14 +247,17 @@ def run_reference(args, wl, world, rank, local):
     walkers = g["V"] if wl["app"] != "node2vec" or wl["scale"] != 16 else 65536
     threads = os.cpu_count() or 1
     vals = []
+    # each step: a bounded sample of ~2 s of walking, so the whole run stays
+    # within a few minutes
     for _ in range(args.warmup):
-        cpu_sample(g, wl, walkers, threads, seed=1, target_steps=500_000, chunks=4)
+        cpu_sample(g, wl, walkers, threads, seed=1, target_s=0.5, chunks=4)
     for _ in range(args.steps):
-        vals.append(cpu_sample(g, wl, walkers, threads, seed=1))
+        vals.append(cpu_sample(g, wl, walkers, threads, seed=1, target_s=2.0))
     value = statistics.median(v["value"] for v in vals)
     line = {
         "impl": "reference", "metric": "walker-steps/s", "value": value, "unit": "walker-steps/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * statistics.median(v["seconds"] for v in vals), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded R-MAT)",
         "config": {"workload": args.workload, "desc": wl["desc"], "walkers": walkers},
         "cpu_baseline": dict(vals[-1], value=value),

@@ -331,8 +331,8 @@ def run_serve_bench(args, wl, world, rank, local):
     # batch kernel on the whole stream
     engine.set_option("alias_cache", 1)
     from knightking_gb300 import tuning
-    space = tuple((n, v) for n, v in tuning.space_for(app, bool(wl["weights"])) if n != "walk_schedule")
-    best, tune_table = tuning.autotune(engine, lambda: batched(reqs), space, repeats=1)
+    best, tune_table = tuning.autotune(engine, lambda: batched(reqs), tuning.space_for(app, bool(wl["weights"])),
+                                      repeats=1)
     for _ in range(args.warmup):
         batched(reqs[:64])
         plain(reqs[:8])

@@ -1577,6 +1577,50 @@ struct BatchJob
 /* One thread per walker over the concatenated walkers of all jobs; the job of
  * a walker by binary search over the jobs' first positions (shared memory).
  * App::make(job, wc, tc) builds the job's WalkerConfig / TransitionConfig. */
+/* Walker t of a batch: its job (binary search over the jobs' first positions
+ * in shared memory), the job's hooks and launch record, the walker started. */
+template <typename S, typename App>
+__device__ __forceinline__ uint32_t batch_walker_begin(const GraphView &g, const App &app, const BatchJob *jobs,
+                                                       const uint32_t *s_first, uint32_t njobs, uint32_t t,
+                                                       const float *alias_sum, uint32_t *path, uint32_t *length,
+                                                       unsigned long long *total_steps, int *status,
+                                                       uint32_t trial_limit, typename App::WC &wc,
+                                                       typename App::TC &tc, WalkLaunch &L, WalkerRun<S> &run,
+                                                       Sampler &rng)
+{
+    uint32_t lo = 0, hi = njobs;
+    while (hi - lo > 1)
+    {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (s_first[mid] <= t)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    const BatchJob job = jobs[lo];
+    app.make(job, wc, tc);
+    L.seed = job.seed;
+    L.walker_begin = job.walker_begin;
+    L.walker_num = job.walker_num;
+    L.path_off = nullptr;
+    L.cap = job.cap;
+    L.path = path ? path + job.path_base : nullptr;
+    L.length = length + job.first_task;
+    L.start = nullptr;
+    L.n_start = 0;
+    L.total_steps = total_steps;
+    L.alias_sum = alias_sum;
+    L.status = status;
+    L.trial_limit = trial_limit;
+    L.stats = nullptr;
+    const uint32_t i = t - job.first_task;
+    rng.init(L.seed);
+    walk_begin<S>(g, wc, L, i, run, rng);
+    return i;
+}
+
+/* One thread per walker over the concatenated walkers of all jobs.
+ * App::make(job, wc, tc) builds the job's WalkerConfig / TransitionConfig. */
 template <typename S, typename App, typename Bucket>
 __global__ void __launch_bounds__(256, 4) walk_batch_kernel(GraphView g, App app, const BatchJob *jobs, uint32_t njobs,
                                                          uint32_t total, const Bucket *alias,
@@ -1597,45 +1641,72 @@ __global__ void __launch_bounds__(256, 4) walk_batch_kernel(GraphView g, App app
         const uint32_t t = (it * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
         if (t < total)
         {
-            uint32_t lo = 0, hi = njobs;
-            while (hi - lo > 1)
-            {
-                const uint32_t mid = (lo + hi) >> 1;
-                if (s_first[mid] <= t)
-                    lo = mid;
-                else
-                    hi = mid;
-            }
-            const BatchJob job = jobs[lo];
             typename App::WC wc;
             typename App::TC tc;
-            app.make(job, wc, tc);
             WalkLaunch L;
-            L.seed = job.seed;
-            L.walker_begin = job.walker_begin;
-            L.walker_num = job.walker_num;
-            L.path_off = nullptr;
-            L.cap = job.cap;
-            L.path = path ? path + job.path_base : nullptr;
-            L.length = length + job.first_task;
-            L.start = nullptr;
-            L.n_start = 0;
-            L.total_steps = total_steps;
-            L.alias_sum = alias_sum;
-            L.status = status;
-            L.trial_limit = trial_limit;
-            L.stats = nullptr;
-            const uint32_t i = t - job.first_task;
-            Sampler rng;
-            rng.init(L.seed);
             WalkerRun<S> run;
-            walk_begin<S>(g, wc, L, i, run, rng);
+            Sampler rng;
+            const uint32_t i = batch_walker_begin<S>(g, app, jobs, s_first, njobs, t, alias_sum, path, length,
+                                                     total_steps, status, trial_limit, wc, tc, L, run, rng);
             while (walk_trial<S>(g, wc, tc, alias, nullptr, L, run, rng))
             {
             }
             L.length[i] = run.len;
             my_steps += run.len - 1;
             counts.add(run);
+        }
+    }
+    flush_steps(total_steps, my_steps);
+    counts.flush(stats);
+}
+
+/* Walker pool over a batch: persistent blocks, each owning a contiguous range
+ * of the concatenated walkers handed out by a shared-memory counter; a lane
+ * whose walk ends takes the next walker (of whatever job) at once, so walks
+ * with more rejection trials do not hold idle lanes.  Paths are those of
+ * walk_batch_kernel: every walker's draws depend only on its job and id. */
+template <typename S, typename App, typename Bucket>
+__global__ void __launch_bounds__(256, 4) walk_batch_pool_kernel(GraphView g, App app, const BatchJob *jobs,
+                                                              uint32_t njobs, uint32_t total, const Bucket *alias,
+                                                              const float *alias_sum, uint32_t *path,
+                                                              uint32_t *length, unsigned long long *total_steps,
+                                                              int *status, uint32_t trial_limit,
+                                                              unsigned long long *stats)
+{
+    __shared__ uint32_t s_first[kMaxBatchJobs];
+    __shared__ uint32_t s_next;
+    for (uint32_t j = threadIdx.x; j < njobs; j += blockDim.x)
+        s_first[j] = jobs[j].first_task;
+    const uint32_t per = (uint32_t)(((uint64_t)total + gridDim.x - 1) / gridDim.x);
+    const uint32_t lo = (uint32_t)min((uint64_t)blockIdx.x * per, (uint64_t)total);
+    const uint32_t hi = (uint32_t)min((uint64_t)lo + per, (uint64_t)total);
+    if (threadIdx.x == 0)
+        s_next = lo;
+    __syncthreads();
+    unsigned long long my_steps = 0;
+    WalkCounts counts;
+    typename App::WC wc;
+    typename App::TC tc;
+    WalkLaunch L;
+    WalkerRun<S> run;
+    Sampler rng;
+    uint32_t t = atomicAdd(&s_next, 1u), i = 0;
+    bool have = t < hi;
+    if (have)
+        i = batch_walker_begin<S>(g, app, jobs, s_first, njobs, t, alias_sum, path, length, total_steps, status,
+                                  trial_limit, wc, tc, L, run, rng);
+    while (__any_sync(kFullMask, have))
+    {
+        if (have && !walk_trial<S>(g, wc, tc, alias, nullptr, L, run, rng))
+        {
+            L.length[i] = run.len;
+            my_steps += run.len - 1;
+            counts.add(run);
+            t = atomicAdd(&s_next, 1u);
+            have = t < hi;
+            if (have)
+                i = batch_walker_begin<S>(g, app, jobs, s_first, njobs, t, alias_sum, path, length, total_steps,
+                                          status, trial_limit, wc, tc, L, run, rng);
         }
     }
     flush_steps(total_steps, my_steps);

@@ -101,9 +101,28 @@ void launch_batch_with(kk_engine *e, const App &app, const BatchPlan &plan, Batc
     *path = want_paths ? slot.path.as<uint32_t>(plan.total_cap) : nullptr;
     KK_CUDA_CHECK(cudaEventRecord(slot.ev[1], slot.stream));
     const unsigned bs = (unsigned)e->walk_block;
-    walk_batch_kernel<typename App::S, App, Bucket><<<grid_for(e, plan.total, bs), bs, 0, slot.stream>>>(
-        e->view(), app, d_jobs, (uint32_t)plan.jobs.size(), plan.total, alias, (const float *)e->sum.p, *path, length,
-        steps, status, e->trial_limit, e->walk_stats ? steps + 1 : nullptr);
+    const uint32_t nj = (uint32_t)plan.jobs.size();
+    unsigned long long *st = e->walk_stats ? steps + 1 : nullptr;
+    if (e->walk_schedule == 0)
+    {
+        walk_batch_kernel<typename App::S, App, Bucket><<<grid_for(e, plan.total, bs), bs, 0, slot.stream>>>(
+            e->view(), app, d_jobs, nj, plan.total, alias, (const float *)e->sum.p, *path, length, steps, status,
+            e->trial_limit, st);
+    }
+    else
+    {
+        /* persistent walker pool: as many resident blocks as fit, on every SM */
+        static int resident = 0;
+        if (resident == 0)
+            KK_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &resident, walk_batch_pool_kernel<typename App::S, App, Bucket>, (int)bs, 0));
+        const uint64_t want = (uint64_t)e->sm_count * (resident > 0 ? resident : 1);
+        const uint64_t need = ((uint64_t)plan.total + bs - 1) / bs;
+        const unsigned grid = (unsigned)(want < need ? want : (need ? need : 1));
+        walk_batch_pool_kernel<typename App::S, App, Bucket><<<grid, bs, 0, slot.stream>>>(
+            e->view(), app, d_jobs, nj, plan.total, alias, (const float *)e->sum.p, *path, length, steps, status,
+            e->trial_limit, st);
+    }
     KK_CUDA_CHECK(cudaGetLastError());
 }
 

@@ -28,7 +28,16 @@ def _load(engine, seed, weighted, types=False):
 
 
 def _check(engine, app, jobs):
+    """Both batch schedules: one walker per thread and the persistent pool."""
     batch = engine.batch_walk(app, jobs)
+    engine.set_option("walk_schedule", 1)
+    try:
+        pooled = engine.batch_walk(app, jobs)
+    finally:
+        engine.set_option("walk_schedule", 0)
+    for a, b in zip(batch, pooled):
+        np.testing.assert_array_equal(a.path_length, b.path_length)
+        np.testing.assert_array_equal(a.vertices, b.vertices)
     assert len(batch) == len(jobs)
     for job, got in zip(jobs, batch):
         kw = dict(job)

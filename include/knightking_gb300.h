@@ -113,7 +113,8 @@ kk_status kk_engine_set_stream(kk_engine *e, void *stream);
  *   "l2_fetch_bytes"     the context's cudaLimitMaxL2FetchGranularity while the engine
  *                        lives: 32, 64, 128, or 0 for the value found (restored on destroy)
  *   "walk_stats"         1 counts trials, queries and probes (kk_last_walk_stats)
- *   "alias_mid_tier"     alias build of degrees 33..128: 0 one thread per vertex, 1 a warp per vertex */
+ *   "alias_mid_tier"     alias build of degrees 33..128: 0 one thread per vertex, 1 a warp per vertex
+ *   "walk_multi"         walkers per thread (1, 2, 4) of first-order walks without a dynamic component */
 kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value);
 /* Message of the last failed call on this engine ("" if none). */
 const char *kk_last_error(const kk_engine *e);
@@ -251,6 +252,8 @@ typedef struct
     uint32_t max_jobs;      /* requests per batch, 1..1024 (0: 256) */
     uint64_t slot_bytes;    /* admission: device bytes of walker paths and state per slot
                                (walkers * ((walk_length + 1) * 4 + 4) per request; 0: 1 GiB) */
+    int launch_mode;        /* 0: each slot replays one captured CUDA graph per batch (job table
+                               upload, status reset, walk kernel, status read-back); 1: stream launches */
 } kk_serve_opts;
 
 typedef struct

@@ -261,7 +261,8 @@ struct MetapathDyn
     const MetaSchemes *sc;
     __device__ __forceinline__ real_t operator()(const Walker<MetapathState> &w, vertex_id_t, const AdjUnit &e) const
     {
-        return ((sc->mask[w.data.scheme_id][w.data.state] >> gather(type + e.index)) & 1u) ? 1.0f : 0.0f;
+        const uint32_t t = (e.type_tag & 0x100u) ? (e.type_tag & 0xffu) : gather(type + e.index);
+        return ((sc->mask[w.data.scheme_id][w.data.state] >> t) & 1u) ? 1.0f : 0.0f;
     }
 };
 

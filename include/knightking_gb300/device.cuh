@@ -41,6 +41,9 @@ struct AdjUnit
 {
     vertex_id_t neighbour;
     edge_id_t index;
+    /* the edge's type when the engine already holds it (bit 8 set, type in
+     * bits 0-7; an alias bucket carries its candidates' types), else 0 */
+    uint32_t type_tag = 0;
 };
 
 /* A vertex's adjacency (AdjList, include/graph.hpp:63-73) as an index range. */

@@ -97,6 +97,15 @@ struct BatchSlot
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     DevBuf jobs, small, length, path, schemes;
     float alias_ms = 0.0f, walk_ms = 0.0f;
+    /* CUDA-graph mode (serving): buffers sized once for a full slot, the job
+     * table and counts staged in pinned memory, the kernel reading the counts
+     * from device memory, so one captured graph (uploads, status reset,
+     * kernel, status read-back) is replayed for every batch */
+    bool graph_mode = false;
+    uint32_t max_walkers = 0;
+    uint64_t max_cap = 0;
+    cudaGraphExec_t exec = nullptr;
+    char *h_stage = nullptr; /* pinned: jobs | schemes | header | status */
     void release()
     {
         DevBuf *b[] = {&jobs, &small, &length, &path, &schemes};
@@ -106,6 +115,12 @@ struct BatchSlot
             if (ev[i])
                 cudaEventDestroy(ev[i]);
         ev[0] = ev[1] = ev[2] = nullptr;
+        if (exec)
+            cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        if (h_stage)
+            cudaFreeHost(h_stage);
+        h_stage = nullptr;
     }
 };
 
@@ -260,6 +275,9 @@ struct kk_engine
     /* threads per block of the one-walker-per-thread and batch walk kernels
      * (option walk_block: 32..256, a multiple of 32) */
     int walk_block = 256;
+    /* walkers per thread of the always-accepting first-order walks (option
+     * walk_multi: 1, 2 or 4) */
+    int walk_multi = 1;
     /* walk_stats (option): count trials, queries and binary-search probes of
      * the walks (kk_last_walk_stats) */
     int walk_stats = 0;
@@ -383,6 +401,11 @@ void batch_prepare(kk_engine *e, const BatchPlan &plan);
  * prepared: batch_prepare already ran for this app (the slot then only reads
  * the shared tables).  Returns the walker-steps; fails on a walk error. */
 uint64_t run_batch(kk_engine *e, BatchPlan &plan, BatchSlot &slot, bool want_paths, bool prepared);
+
+/* Puts a slot in CUDA-graph mode for batches of up to max_walkers walkers and
+ * max_cap path vertices (batch_prepare must have run: the graph reads the
+ * shared tables). */
+void batch_slot_graph_mode(kk_engine *e, BatchSlot &slot, uint32_t max_walkers, uint64_t max_cap);
 
 /* Metapath schemes of one job as per-state type masks, checked. */
 inline apps::MetaSchemes make_schemes(const kk_walk_opts &o)
@@ -541,7 +564,7 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
         uint64_t *caps = e->caps.as<uint64_t>((uint64_t)n + 1);
         uint64_t *off = e->path_off.as<uint64_t>((uint64_t)n + 1);
         KK_CUDA_CHECK(cudaMemsetAsync(caps + n, 0, sizeof(uint64_t), e->stream));
-        constant_extension_bound_kernel<<<grid_for(e, n, 256), 256, 0, e->stream>>>(
+        constant_extension_bound_kernel<<<grid_for(e, (uint64_t)n * 32, 256), 256, 0, e->stream>>>(
             rs.seed, rs.walker_begin, n, rs.const_ext, 1u << 24, caps, d_status);
         KK_CUDA_CHECK(cudaGetLastError());
         exclusive_scan_u64(e, caps, off, (uint64_t)n + 1);
@@ -552,6 +575,22 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
     }
     L.path = rs.want_paths ? e->path.as<uint32_t>(total_cap) : nullptr;
     KK_CUDA_CHECK(cudaEventRecord(e->ev[1], e->stream));
+    if constexpr (TC::order == 1 && !TC::has_dynamic)
+    {
+        if (e->walk_schedule == 0 && e->walk_multi > 1)
+        {
+            /* W walkers per thread, gathers of all W in flight together */
+            const unsigned bs = (unsigned)e->walk_block;
+            const uint64_t threads = ((uint64_t)n + e->walk_multi - 1) / e->walk_multi;
+            if (e->walk_multi == 2)
+                walk_multi_kernel<S, WC, TC, Bucket, 2><<<grid_for(e, threads, bs), bs, 0, e->stream>>>(g, wc, tc,
+                                                                                                       alias, L);
+            else
+                walk_multi_kernel<S, WC, TC, Bucket, 4><<<grid_for(e, threads, bs), bs, 0, e->stream>>>(g, wc, tc,
+                                                                                                       alias, L);
+            goto launched;
+        }
+    }
     if (e->walk_schedule == 0)
     {
         const unsigned bs = (unsigned)e->walk_block;
@@ -569,6 +608,7 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
         unsigned grid = (unsigned)(want < need ? want : (need ? need : 1));
         walk_pool_kernel<S, WC, TC, Bucket><<<grid, 256, 0, e->stream>>>(g, wc, tc, alias, ra, L);
     }
+launched:
     KK_CUDA_CHECK(cudaGetLastError());
     KK_CUDA_CHECK(cudaEventRecord(e->ev[2], e->stream));
     int h_small[16];

@@ -281,16 +281,25 @@ struct __align__(32) IndexBucket
     uint32_t pad2;
 
     static constexpr bool cursor = false;
-    /* pn, qn: the neighbours of edges pi, qi (qn unused when qi == kNone) */
+    /* pn, qn: the neighbours of edges pi, qi (qn unused when qi == kNone);
+     * ty: the row's edge types, stored as type | 0x100 in pad1 / pad2 so a
+     * pick also knows its candidate's type (nullptr: no types) */
     __device__ __forceinline__ static IndexBucket make_n(float p, uint32_t pi, uint32_t qi, uint32_t pn, uint32_t qn,
-                                                         const uint64_t *)
+                                                         const uint64_t *, const uint8_t *ty)
     {
-        return IndexBucket{p, pi, qi, 0, pn, qi == kNone ? kNone : qn, 0, 0};
+        uint32_t pt = 0, qt = 0;
+        if (ty != nullptr)
+        {
+            pt = 0x100u | ty[pi];
+            if (qi != kNone)
+                qt = 0x100u | ty[qi];
+        }
+        return IndexBucket{p, pi, qi, 0, pn, qi == kNone ? kNone : qn, pt, qt};
     }
     __device__ __forceinline__ static IndexBucket make(float p, uint32_t pi, uint32_t qi, const uint32_t *nb,
-                                                       const uint64_t *vcur)
+                                                       const uint64_t *vcur, const uint8_t *ty)
     {
-        return make_n(p, pi, qi, nb[pi], qi == kNone ? kNone : nb[qi], vcur);
+        return make_n(p, pi, qi, nb[pi], qi == kNone ? kNone : nb[qi], vcur, ty);
     }
 };
 
@@ -305,16 +314,16 @@ struct __align__(32) CursorBucket
 
     static constexpr bool cursor = true;
     __device__ __forceinline__ static CursorBucket make_n(float p, uint32_t, uint32_t qi, uint32_t pn, uint32_t qn,
-                                                          const uint64_t *vcur)
+                                                          const uint64_t *vcur, const uint8_t *)
     {
         if (qi == kNone)
             return CursorBucket{p, pn, kNone, 0, gather(vcur + pn), 0};
         return CursorBucket{p, pn, qn, 0, gather(vcur + pn), gather(vcur + qn)};
     }
     __device__ __forceinline__ static CursorBucket make(float p, uint32_t pi, uint32_t qi, const uint32_t *nb,
-                                                        const uint64_t *vcur)
+                                                        const uint64_t *vcur, const uint8_t *ty)
     {
-        return make_n(p, pi, qi, nb[pi], qi == kNone ? kNone : nb[qi], vcur);
+        return make_n(p, pi, qi, nb[pi], qi == kNone ? kNone : nb[qi], vcur, ty);
     }
 };
 static_assert(sizeof(IndexBucket) == 32 && sizeof(CursorBucket) == 32, "one sector per bucket");
@@ -405,7 +414,7 @@ __device__ __forceinline__ float static_at(const GraphView &g, const TC &tc, uin
 template <typename Bucket>
 __device__ __forceinline__ void warp_pairing(uint2 *P, uint2 *Q, uint32_t &ph, uint32_t &pt, uint32_t &qh,
                                              uint32_t &qt, float ave, Bucket *ob, const uint32_t *nb,
-                                             const uint64_t *vcur, uint32_t stop_above)
+                                             const uint64_t *vcur, const uint8_t *ty, uint32_t stop_above)
 {
     const uint32_t lane = threadIdx.x & 31, lt = lanemask_lt();
     while (ph < pt)
@@ -414,7 +423,7 @@ __device__ __forceinline__ void warp_pairing(uint2 *P, uint2 *Q, uint32_t &ph, u
         if (lq == 0)
         {
             for (uint32_t i = lane; i < lp; i += 32)
-                ob[ph + i] = Bucket::make(1.0f, P[ph + i].x, kNone, nb, vcur);
+                ob[ph + i] = Bucket::make(1.0f, P[ph + i].x, kNone, nb, vcur, ty);
             ph = pt;
             break;
         }
@@ -430,7 +439,7 @@ __device__ __forceinline__ void warp_pairing(uint2 *P, uint2 *Q, uint32_t &ph, u
         {
             const uint2 pe = P[ph + lane], qe = Q[qh + lane];
             const float pv = __uint_as_float(pe.y), qv = __uint_as_float(qe.y);
-            ob[ph + lane] = Bucket::make(fdiv(pv, ave), pe.x, qe.x, nb, vcur);
+            ob[ph + lane] = Bucket::make(fdiv(pv, ave), pe.x, qe.x, nb, vcur, ty);
             const float r = fsub(qv, fsub(ave, pv));
             conv = r < ave;
             ne = make_uint2(qe.x, __float_as_uint(r));
@@ -500,8 +509,8 @@ __device__ __forceinline__ void block_rank2(bool a, bool b, uint32_t &ra, uint32
  * warp 0 alone for short stretches; then the q leftovers (:631-638). */
 template <typename Bucket>
 __device__ __forceinline__ void block_pairing(uint2 *P, uint2 *Q, uint32_t pt, uint32_t qt, float ave, Bucket *ob,
-                                              const uint32_t *nb, const uint64_t *vcur, uint32_t *sa, uint32_t *sb,
-                                              uint32_t *s_state)
+                                              const uint32_t *nb, const uint64_t *vcur, const uint8_t *ty,
+                                              uint32_t *sa, uint32_t *sb, uint32_t *s_state)
 {
     const uint32_t tid = threadIdx.x, nt = blockDim.x;
     uint32_t ph = 0, qh = 0;
@@ -511,7 +520,7 @@ __device__ __forceinline__ void block_pairing(uint2 *P, uint2 *Q, uint32_t pt, u
         if (lq == 0)
         {
             for (uint32_t i = tid; i < lp; i += nt)
-                ob[ph + i] = Bucket::make(1.0f, P[ph + i].x, kNone, nb, vcur);
+                ob[ph + i] = Bucket::make(1.0f, P[ph + i].x, kNone, nb, vcur, ty);
             ph = pt;
             break;
         }
@@ -520,7 +529,7 @@ __device__ __forceinline__ void block_pairing(uint2 *P, uint2 *Q, uint32_t pt, u
         {
             if (tid < 32)
             {
-                warp_pairing(P, Q, ph, pt, qh, qt, ave, ob, nb, vcur, 128);
+                warp_pairing(P, Q, ph, pt, qh, qt, ave, ob, nb, vcur, ty, 128);
                 if (tid == 0)
                 {
                     s_state[0] = ph;
@@ -544,7 +553,7 @@ __device__ __forceinline__ void block_pairing(uint2 *P, uint2 *Q, uint32_t pt, u
         {
             const uint2 pe = P[ph + tid], qe = Q[qh + tid];
             const float pv = __uint_as_float(pe.y), qv = __uint_as_float(qe.y);
-            ob[ph + tid] = Bucket::make(fdiv(pv, ave), pe.x, qe.x, nb, vcur);
+            ob[ph + tid] = Bucket::make(fdiv(pv, ave), pe.x, qe.x, nb, vcur, ty);
             const float r = fsub(qv, fsub(ave, pv));
             conv = r < ave;
             ne = make_uint2(qe.x, __float_as_uint(r));
@@ -565,7 +574,7 @@ __device__ __forceinline__ void block_pairing(uint2 *P, uint2 *Q, uint32_t pt, u
         qt += tsn;
     }
     for (uint32_t i = tid; i < qt - qh; i += nt)
-        ob[pt + i] = Bucket::make(1.0f, Q[qh + i].x, kNone, nb, vcur);
+        ob[pt + i] = Bucket::make(1.0f, Q[qh + i].x, kNone, nb, vcur, ty);
     __syncthreads();
 }
 
@@ -634,7 +643,7 @@ __global__ void __launch_bounds__(256) alias_sum_kernel(GraphView g, TC tc, floa
  * tails, and all its reads precede its writes (the ballots depend on them). */
 template <typename Bucket, typename Nb>
 __device__ __forceinline__ void warp_pairing_ring(uint2 *R, uint32_t deg, uint32_t S0, uint32_t B0, float ave,
-                                                  Bucket *ob, Nb nb, const uint64_t *vcur)
+                                                  Bucket *ob, Nb nb, const uint64_t *vcur, const uint8_t *ty)
 {
     const uint32_t lane = threadIdx.x & 31, lt = lanemask_lt();
     uint32_t ph = 0, pt = 0, lp = S0, qh = 0, qt = 0, lq = B0, npop = 0;
@@ -650,7 +659,7 @@ __device__ __forceinline__ void warp_pairing_ring(uint2 *R, uint32_t deg, uint32
         {
             const uint2 pe = R[pp(ph + lane)], qe = R[pq(qh + lane)];
             const float pv = __uint_as_float(pe.y), qv = __uint_as_float(qe.y);
-            ob[npop + lane] = Bucket::make_n(fdiv(pv, ave), pe.x, qe.x, nb(pe.x), nb(qe.x), vcur);
+            ob[npop + lane] = Bucket::make_n(fdiv(pv, ave), pe.x, qe.x, nb(pe.x), nb(qe.x), vcur, ty);
             const float r = fsub(qv, fsub(ave, pv));
             conv = r < ave;
             ne = make_uint2(qe.x, __float_as_uint(r));
@@ -677,12 +686,12 @@ __device__ __forceinline__ void warp_pairing_ring(uint2 *R, uint32_t deg, uint32
     for (uint32_t i = lane; i < lp; i += 32)
     {
         const uint32_t x = R[pp(ph + i)].x;
-        ob[npop + i] = Bucket::make_n(1.0f, x, kNone, nb(x), 0, vcur);
+        ob[npop + i] = Bucket::make_n(1.0f, x, kNone, nb(x), 0, vcur, ty);
     }
     for (uint32_t i = lane; i < lq; i += 32)
     {
         const uint32_t x = R[pq(qh + i)].x;
-        ob[npop + lp + i] = Bucket::make_n(1.0f, x, kNone, nb(x), 0, vcur);
+        ob[npop + lp + i] = Bucket::make_n(1.0f, x, kNone, nb(x), 0, vcur, ty);
     }
     __syncwarp();
 }
@@ -794,12 +803,13 @@ __global__ void __launch_bounds__(256) alias_pair_kernel(GraphView g, TC tc, Buc
         }
         __syncwarp();
         Bucket *ob = out + e0;
+        const uint8_t *ty = g.type != nullptr ? g.type + e0 : nullptr;
         if (staged)
-            warp_pairing_ring(R, deg, S0, B0, ave, ob, [&](uint32_t i) { return sNb[i]; }, vcur);
+            warp_pairing_ring(R, deg, S0, B0, ave, ob, [&](uint32_t i) { return sNb[i]; }, vcur, ty);
         else
         {
             const uint32_t *nb = g.nbr + e0;
-            warp_pairing_ring(R, deg, S0, B0, ave, ob, [&](uint32_t i) { return nb[i]; }, vcur);
+            warp_pairing_ring(R, deg, S0, B0, ave, ob, [&](uint32_t i) { return nb[i]; }, vcur, ty);
         }
     }
 }
@@ -846,7 +856,8 @@ __global__ void __launch_bounds__(1024) alias_build_hub_kernel(GraphView g, TC t
         uint2 *Q = P + deg;
         uint32_t pt, qt;
         block_split([&](uint32_t i) { return static_at(g, tc, v, e0 + i); }, deg, ave, P, Q, pt, qt, sa, sb);
-        block_pairing(P, Q, pt, qt, ave, out + e0, g.nbr + e0, vcur, sa, sb, s_state);
+        block_pairing(P, Q, pt, qt, ave, out + e0, g.nbr + e0, vcur, g.type != nullptr ? g.type + e0 : nullptr, sa,
+                      sb, s_state);
     }
 }
 
@@ -944,13 +955,14 @@ __global__ void __launch_bounds__(NT) alias_thread_kernel(GraphView g, TC tc, Bu
         /* pairing; pt/qt are the push slots (ph + lp) mod S0 and (qh + lq) mod B0 */
         uint32_t ph = 0, pt = 0, lp = S0, qh = 0, qt = 0, lq = B0, nb_out = 0;
         Bucket *ob = out + e0;
+        const uint8_t *ty = g.type != nullptr ? g.type + e0 : nullptr;
         while (lp != 0 && lq != 0)
         {
             const uint32_t pi = ring[slot(ph)], qi = ring[slot(deg - 1 - qh)];
             ph = ph + 1 == S0 ? 0 : ph + 1;
             qh = qh + 1 == B0 ? 0 : qh + 1;
             const float pv = s_prob[at(pi, t)], qv = s_prob[at(qi, t)];
-            ob[nb_out++] = Bucket::make_n(fdiv(pv, ave), pi, qi, s_nb[at(pi, t)], s_nb[at(qi, t)], vcur);
+            ob[nb_out++] = Bucket::make_n(fdiv(pv, ave), pi, qi, s_nb[at(pi, t)], s_nb[at(qi, t)], vcur, ty);
             const float r = fsub(qv, fsub(ave, pv));
             s_prob[at(qi, t)] = r;
             if (r < ave)
@@ -970,13 +982,13 @@ __global__ void __launch_bounds__(NT) alias_thread_kernel(GraphView g, TC tc, Bu
         for (; lp != 0; lp--)
         {
             const uint32_t pi = ring[slot(ph)];
-            ob[nb_out++] = Bucket::make_n(1.0f, pi, kNone, s_nb[at(pi, t)], 0, vcur);
+            ob[nb_out++] = Bucket::make_n(1.0f, pi, kNone, s_nb[at(pi, t)], 0, vcur, ty);
             ph = ph + 1 == S0 ? 0 : ph + 1;
         }
         for (; lq != 0; lq--)
         {
             const uint32_t qi = ring[slot(deg - 1 - qh)];
-            ob[nb_out++] = Bucket::make_n(1.0f, qi, kNone, s_nb[at(qi, t)], 0, vcur);
+            ob[nb_out++] = Bucket::make_n(1.0f, qi, kNone, s_nb[at(qi, t)], 0, vcur, ty);
             qh = qh + 1 == B0 ? 0 : qh + 1;
         }
     }
@@ -1105,6 +1117,7 @@ struct Cand
     vertex_id_t nbr;
     uint64_t cur;
     bool has_cur;
+    uint32_t tag; /* AdjUnit::type_tag of the candidate edge */
 };
 
 /* Candidate pick: uniform (include/walk.hpp:1016-1018) or alias
@@ -1121,21 +1134,21 @@ __device__ __forceinline__ Cand pick_candidate(const GraphView &g, const Bucket 
         {
             /* lo = {p, p_nbr, q_nbr, -}, hi = {p_cur, q_cur} */
             if (lo.z == kNone || rng.gen_float(1.0f) < __uint_as_float(lo.x))
-                return Cand{kNone, lo.y, ((uint64_t)hi.y << 32) | hi.x, true};
-            return Cand{kNone, lo.z, ((uint64_t)hi.w << 32) | hi.z, true};
+                return Cand{kNone, lo.y, ((uint64_t)hi.y << 32) | hi.x, true, 0};
+            return Cand{kNone, lo.z, ((uint64_t)hi.w << 32) | hi.z, true, 0};
         }
         else
         {
-            /* lo = {p, p_idx, q_idx, -}, hi = {p_nbr, q_nbr, -, -} */
+            /* lo = {p, p_idx, q_idx, -}, hi = {p_nbr, q_nbr, p_type tag, q_type tag} */
             if (lo.z == kNone || rng.gen_float(1.0f) < __uint_as_float(lo.x))
-                return Cand{lo.y, hi.x, 0, false};
-            return Cand{lo.z, hi.y, 0, false};
+                return Cand{lo.y, hi.x, 0, false, hi.z};
+            return Cand{lo.z, hi.y, 0, false, hi.w};
         }
     }
     else
     {
         const uint32_t c = rng.gen(pos.deg);
-        return Cand{c, gather(g.nbr + pos.e0 + c), 0, false};
+        return Cand{c, gather(g.nbr + pos.e0 + c), 0, false, 0};
     }
 }
 
@@ -1396,7 +1409,7 @@ __device__ __forceinline__ bool walk_trial(const GraphView &g, const WC &wc, con
                 if constexpr (TC::has_lowerbound)
                     acc = dart <= tc.dcomp_lowerbound(v, adj);
                 if (!acc)
-                    acc = dart <= tc.dynamic_comp(w, v, AdjUnit{pc.nbr, (edge_id_t)(e0 + pc.idx)});
+                    acc = dart <= tc.dynamic_comp(w, v, AdjUnit{pc.nbr, (edge_id_t)(e0 + pc.idx), pc.tag});
                 if (acc)
                 {
                     ac = pc;
@@ -1424,7 +1437,7 @@ __device__ __forceinline__ bool walk_trial(const GraphView &g, const WC &wc, con
             if constexpr (TC::has_lowerbound)
                 accepted = randval <= tc.dcomp_lowerbound(v, adj);
         }
-        const AdjUnit cu{cd.nbr, (edge_id_t)(e0 + cd.idx)};
+        const AdjUnit cu{cd.nbr, (edge_id_t)(e0 + cd.idx), cd.tag};
         if (!accepted)
         {
             R resp{};
@@ -1503,6 +1516,175 @@ __global__ void __launch_bounds__(256, 4) walk_static_kernel(GraphView g, WC wc,
             L.length[i] = run.len;
             my_steps += run.len - 1;
             counts.add(run);
+        }
+    }
+    flush_steps(L.total_steps, my_steps);
+    counts.flush(L.stats);
+}
+
+/* Several walkers per thread for walks whose every trial is accepted (first
+ * order without a dynamic component: DeepWalk, PPR).  A step is two dependent
+ * gathers (the adjacency position, when the bucket did not carry it, then the
+ * bucket); the thread runs its W walkers in lockstep phases so that the
+ * gathers of all W are in flight together instead of one at a time.  Each
+ * walker keeps its own stream and state, so the paths are those of
+ * walk_static_kernel.  Thread t walks t, t + T, t + 2T, ... (T threads),
+ * taking the next as soon as one of its walks ends. */
+template <typename S, typename WC, typename TC, typename Bucket, int W>
+__global__ void __launch_bounds__(256, 4) walk_multi_kernel(GraphView g, WC wc, TC tc, const Bucket *alias,
+                                                            WalkLaunch L)
+{
+    static_assert(TC::order == 1 && !TC::has_dynamic, "every trial accepted");
+    const uint32_t T = gridDim.x * blockDim.x;
+    const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long my_steps = 0;
+    WalkCounts counts;
+    WalkerRun<S> run[W];
+    Sampler rng[W];
+    uint32_t idx[W];
+    bool act[W];
+    uint32_t next = t0;
+#pragma unroll
+    for (int k = 0; k < W; k++)
+    {
+        act[k] = next < L.walker_num;
+        idx[k] = next;
+        if (act[k])
+        {
+            rng[k].init(L.seed);
+            walk_begin<S>(g, wc, L, next, run[k], rng[k]);
+        }
+        next += T;
+    }
+    for (;;)
+    {
+        bool any = false;
+#pragma unroll
+        for (int k = 0; k < W; k++)
+            any |= act[k];
+        if (!any)
+            break;
+        /* phase 1: adjacency positions not carried by a bucket */
+        int64_t o0[W], o1[W];
+#pragma unroll
+        for (int k = 0; k < W; k++)
+            if (act[k] && run[k].pos.e0 < 0)
+            {
+                o0[k] = gather(g.off + run[k].v);
+                o1[k] = gather(g.off + run[k].v + 1);
+            }
+#pragma unroll
+        for (int k = 0; k < W; k++)
+            if (act[k] && run[k].pos.e0 < 0)
+                run[k].pos = Pos{o0[k], (uint32_t)(o1[k] - o0[k])};
+        /* phase 2: end tests, draws and the bucket (or neighbour) gathers */
+        bool live[W];
+        uint4 lo[W], hi[W];
+        uint32_t c[W];
+#pragma unroll
+        for (int k = 0; k < W; k++)
+        {
+            live[k] = false;
+            if (!act[k])
+                continue;
+            const Pos pos = run[k].pos;
+            Walker<S> &w = run[k].w;
+            bool ends = pos.deg == 0;
+            if (!ends)
+            {
+                rng[k].enter(w.id, w.step, 0);
+                const real_t ext = tc.extension_comp(w, run[k].v);
+                ends = ext == 0.0f || (ext < 1.0f && rng[k].gen_float(1.0f) > ext);
+            }
+            if (ends)
+            {
+                L.length[idx[k]] = run[k].len;
+                my_steps += run[k].len - 1;
+                counts.add(run[k]);
+                act[k] = next < L.walker_num;
+                idx[k] = next;
+                if (act[k])
+                {
+                    rng[k].init(L.seed);
+                    walk_begin<S>(g, wc, L, next, run[k], rng[k]);
+                }
+                next += T;
+                continue;
+            }
+            live[k] = true;
+            c[k] = rng[k].gen(pos.deg);
+            if constexpr (TC::has_static)
+            {
+                const uint4 *b4 = reinterpret_cast<const uint4 *>(alias + pos.e0 + c[k]);
+                lo[k] = gather(b4);
+                hi[k] = gather(b4 + 1);
+            }
+            else
+            {
+                lo[k].y = gather(g.nbr + pos.e0 + c[k]);
+            }
+        }
+        /* phase 3: the coin, the step, the path write */
+#pragma unroll
+        for (int k = 0; k < W; k++)
+        {
+            if (!live[k])
+                continue;
+            Cand ac;
+            if constexpr (TC::has_static)
+            {
+                if constexpr (Bucket::cursor)
+                {
+                    if (lo[k].z == kNone || rng[k].gen_float(1.0f) < __uint_as_float(lo[k].x))
+                        ac = Cand{kNone, lo[k].y, ((uint64_t)hi[k].y << 32) | hi[k].x, true, 0};
+                    else
+                        ac = Cand{kNone, lo[k].z, ((uint64_t)hi[k].w << 32) | hi[k].z, true, 0};
+                }
+                else
+                {
+                    if (lo[k].z == kNone || rng[k].gen_float(1.0f) < __uint_as_float(lo[k].x))
+                        ac = Cand{lo[k].y, hi[k].x, 0, false, hi[k].z};
+                    else
+                        ac = Cand{lo[k].z, hi[k].y, 0, false, hi[k].w};
+                }
+            }
+            else
+            {
+                ac = Cand{c[k], lo[k].y, 0, false, 0};
+            }
+            WalkerRun<S> &r = run[k];
+            const Pos pos = r.pos;
+            const vertex_id_t v = r.v;
+            r.trials++;
+            r.w.step++;
+            if constexpr (is_hook<decltype(wc.walker_update_state)>())
+                wc.walker_update_state(r.w, v, AdjUnit{ac.nbr, (edge_id_t)(pos.e0 + ac.idx), ac.tag});
+            bool over = false;
+            if (r.out)
+            {
+                if (r.len >= r.cap)
+                {
+                    atomicExch(L.status, KK_STATUS_PATH_CAPACITY);
+                    over = true;
+                }
+                else
+                {
+                    r.out[r.len] = ac.nbr;
+                }
+            }
+            if (over)
+            {
+                L.length[idx[k]] = r.len;
+                my_steps += r.len - 1;
+                counts.add(r);
+                act[k] = false;
+                continue;
+            }
+            r.len++;
+            r.pv = v;
+            r.ppos = pos;
+            r.v = ac.nbr;
+            r.pos = ac.has_cur ? pos_from_cursor(g, ac.nbr, ac.cur) : Pos{-1, 0};
         }
     }
     flush_steps(L.total_steps, my_steps);
@@ -1626,9 +1808,16 @@ __global__ void __launch_bounds__(256, 4) walk_batch_kernel(GraphView g, App app
                                                          uint32_t total, const Bucket *alias,
                                                          const float *alias_sum, uint32_t *path, uint32_t *length,
                                                          unsigned long long *total_steps, int *status,
-                                                         uint32_t trial_limit, unsigned long long *stats)
+                                                         uint32_t trial_limit, unsigned long long *stats,
+                                                         const uint32_t *hdr)
 {
     __shared__ uint32_t s_first[kMaxBatchJobs];
+    if (hdr != nullptr)
+    {
+        /* counts from device memory: one captured launch serves every batch */
+        njobs = hdr[0];
+        total = hdr[1];
+    }
     for (uint32_t j = threadIdx.x; j < njobs; j += blockDim.x)
         s_first[j] = jobs[j].first_task;
     __syncthreads();
@@ -1671,10 +1860,15 @@ __global__ void __launch_bounds__(256, 4) walk_batch_pool_kernel(GraphView g, Ap
                                                               const float *alias_sum, uint32_t *path,
                                                               uint32_t *length, unsigned long long *total_steps,
                                                               int *status, uint32_t trial_limit,
-                                                              unsigned long long *stats)
+                                                              unsigned long long *stats, const uint32_t *hdr)
 {
     __shared__ uint32_t s_first[kMaxBatchJobs];
     __shared__ uint32_t s_next;
+    if (hdr != nullptr)
+    {
+        njobs = hdr[0];
+        total = hdr[1];
+    }
     for (uint32_t j = threadIdx.x; j < njobs; j += blockDim.x)
         s_first[j] = jobs[j].first_task;
     const uint32_t per = (uint32_t)(((uint64_t)total + gridDim.x - 1) / gridDim.x);
@@ -1716,24 +1910,42 @@ __global__ void __launch_bounds__(256, 4) walk_batch_pool_kernel(GraphView g, Ap
 /* Upper bound on each walker's path length when the extension is a constant
  * probability ext in (0,1) (PPR, src/apps/ppr.hpp:55-58): the walk cannot pass
  * the first step whose first draw (the extension draw, draw 0) says stop.
- * cap[i] = that step + 1 vertices; fails when no stop comes within max_steps. */
-static __global__ void constant_extension_bound_kernel(uint64_t seed, walker_id_t walker_begin, uint32_t walker_num, float ext,
-                                                uint32_t max_steps, uint64_t *cap_out, int *status)
+ * cap[i] = that step + 1 vertices; fails when no stop comes within max_steps.
+ * A warp per walker tests 32 consecutive steps at a time and takes the first
+ * stop by ballot, so geometric lengths leave no lane waiting on the longest
+ * walk of its warp. */
+static __global__ void constant_extension_bound_kernel(uint64_t seed, walker_id_t walker_begin, uint32_t walker_num,
+                                                       float ext, uint32_t max_steps, uint64_t *cap_out, int *status)
 {
-    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < walker_num; i += gridDim.x * blockDim.x)
+    const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < walker_num; i += nwarps)
     {
-        walker_id_t id = walker_begin + i;
-        uint32_t s = 0;
-        for (; s < max_steps; s++)
+        const walker_id_t id = walker_begin + (uint32_t)i;
+        uint32_t stop = max_steps;
+        for (uint32_t base = 0; base < max_steps; base += 32)
         {
-            uint4 b = philox4x32_10(make_uint4(id, s, 0, 0), k0, k1);
-            if (map_gen_float(b.x, 1.0f) > ext)
+            const uint32_t s = base + lane;
+            bool says_stop = false;
+            if (s < max_steps)
+            {
+                const uint4 b = philox4x32_10(make_uint4(id, s, 0, 0), k0, k1);
+                says_stop = map_gen_float(b.x, 1.0f) > ext;
+            }
+            const uint32_t m = __ballot_sync(kFullMask, says_stop);
+            if (m != 0)
+            {
+                stop = base + __ffs(m) - 1;
                 break;
+            }
         }
-        if (s == max_steps)
-            atomicExch(status, KK_STATUS_PATH_CAPACITY);
-        cap_out[i] = (uint64_t)s + 1;
+        if (lane == 0)
+        {
+            if (stop == max_steps)
+                atomicExch(status, KK_STATUS_PATH_CAPACITY);
+            cap_out[i] = (uint64_t)stop + 1;
+        }
     }
 }
 

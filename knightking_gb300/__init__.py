@@ -298,9 +298,10 @@ class WalkEngine:
                                            ctypes.c_uint64(cap), ctypes.byref(steps)))
         return steps.value
 
-    def serve(self, app, weighted=None, slots=2, max_jobs=256, slot_bytes=1 << 30):
-        """Starts a Server (continuous batching) that owns this engine until stopped."""
-        return Server(self, app, weighted, slots, max_jobs, slot_bytes)
+    def serve(self, app, weighted=None, slots=2, max_jobs=256, slot_bytes=1 << 30, graphs=True):
+        """Starts a Server (continuous batching) that owns this engine until
+        stopped; graphs: each slot replays a captured CUDA graph per batch."""
+        return Server(self, app, weighted, slots, max_jobs, slot_bytes, graphs)
 
     def last_stats(self):
         """(trials, queries, probes) of the last walk (walk_stats option)."""
@@ -404,7 +405,7 @@ class Server:
     """Continuous batching of walk requests (kk_serve_*).  submit() and poll()
     may be called from several threads; the engine is the server's until stop()."""
 
-    def __init__(self, engine, app, weighted=None, slots=2, max_jobs=256, slot_bytes=1 << 30):
+    def __init__(self, engine, app, weighted=None, slots=2, max_jobs=256, slot_bytes=1 << 30, graphs=True):
         self._engine = engine
         self._lib = engine._lib
         self.app = app
@@ -417,6 +418,7 @@ class Server:
         o.slots = int(slots)
         o.max_jobs = int(max_jobs)
         o.slot_bytes = int(slot_bytes)
+        o.launch_mode = 0 if graphs else 1
         h = ctypes.c_void_p()
         engine._check(self._lib.kk_serve_start(engine._h, ctypes.byref(o), ctypes.byref(h)))
         self._h = h

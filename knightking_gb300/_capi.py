@@ -76,6 +76,7 @@ class KKServeOpts(ctypes.Structure):
         ("slots", ctypes.c_int),
         ("max_jobs", ctypes.c_uint32),
         ("slot_bytes", ctypes.c_uint64),
+        ("launch_mode", ctypes.c_int),
     ]
 
 

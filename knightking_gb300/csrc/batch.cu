@@ -84,7 +84,7 @@ namespace
 template <typename App, typename Bucket>
 void launch_batch_with(kk_engine *e, const App &app, const BatchPlan &plan, BatchSlot &slot, const BatchJob *d_jobs,
                        uint32_t *length, uint32_t **path, unsigned long long *steps, int *status, bool want_paths,
-                       bool prepared)
+                       bool prepared, const uint32_t *hdr)
 {
     typedef typename App::TC TC;
     const Bucket *alias = nullptr;
@@ -98,16 +98,24 @@ void launch_batch_with(kk_engine *e, const App &app, const BatchPlan &plan, Batc
         }
         alias = (const Bucket *)e->alias.p;
     }
-    *path = want_paths ? slot.path.as<uint32_t>(plan.total_cap) : nullptr;
-    KK_CUDA_CHECK(cudaEventRecord(slot.ev[1], slot.stream));
+    /* a captured launch (hdr != nullptr) serves every batch of the slot: the
+     * buffers are the slot's full-size ones and the counts come from hdr */
+    const uint64_t cap = hdr ? slot.max_cap : plan.total_cap;
+    const uint32_t walkers = hdr ? slot.max_walkers : plan.total;
+    *path = want_paths ? slot.path.as<uint32_t>(cap) : nullptr;
+    if (!hdr)
+        KK_CUDA_CHECK(cudaEventRecord(slot.ev[1], slot.stream));
     const unsigned bs = (unsigned)e->walk_block;
     const uint32_t nj = (uint32_t)plan.jobs.size();
     unsigned long long *st = e->walk_stats ? steps + 1 : nullptr;
     if (e->walk_schedule == 0)
     {
-        walk_batch_kernel<typename App::S, App, Bucket><<<grid_for(e, plan.total, bs), bs, 0, slot.stream>>>(
+        unsigned grid = grid_for(e, walkers, bs);
+        if (hdr && grid > 64u * (unsigned)e->sm_count)
+            grid = 64u * (unsigned)e->sm_count; /* grid-stride over whatever the header holds */
+        walk_batch_kernel<typename App::S, App, Bucket><<<grid, bs, 0, slot.stream>>>(
             e->view(), app, d_jobs, nj, plan.total, alias, (const float *)e->sum.p, *path, length, steps, status,
-            e->trial_limit, st);
+            e->trial_limit, st, hdr);
     }
     else
     {
@@ -117,11 +125,11 @@ void launch_batch_with(kk_engine *e, const App &app, const BatchPlan &plan, Batc
             KK_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                 &resident, walk_batch_pool_kernel<typename App::S, App, Bucket>, (int)bs, 0));
         const uint64_t want = (uint64_t)e->sm_count * (resident > 0 ? resident : 1);
-        const uint64_t need = ((uint64_t)plan.total + bs - 1) / bs;
+        const uint64_t need = ((uint64_t)walkers + bs - 1) / bs;
         const unsigned grid = (unsigned)(want < need ? want : (need ? need : 1));
         walk_batch_pool_kernel<typename App::S, App, Bucket><<<grid, bs, 0, slot.stream>>>(
             e->view(), app, d_jobs, nj, plan.total, alias, (const float *)e->sum.p, *path, length, steps, status,
-            e->trial_limit, st);
+            e->trial_limit, st, hdr);
     }
     KK_CUDA_CHECK(cudaGetLastError());
 }
@@ -137,19 +145,62 @@ bool app_uses_cursor(const kk_engine *e)
 template <typename App>
 void launch_batch(kk_engine *e, const App &app, const BatchPlan &plan, BatchSlot &slot, const BatchJob *d_jobs,
                   uint32_t *length, uint32_t **path, unsigned long long *steps, int *status, bool want_paths,
-                  bool prepared)
+                  bool prepared, const uint32_t *hdr = nullptr)
 {
     if constexpr (use_cursor_buckets<typename App::WC, typename App::TC>())
     {
         if (app_uses_cursor<App>(e))
         {
             launch_batch_with<App, CursorBucket>(e, app, plan, slot, d_jobs, length, path, steps, status,
-                                                 want_paths, prepared);
+                                                 want_paths, prepared, hdr);
             return;
         }
     }
     launch_batch_with<App, IndexBucket>(e, app, plan, slot, d_jobs, length, path, steps, status, want_paths,
-                                        prepared);
+                                        prepared, hdr);
+}
+
+/* The app's launch (the dispatch of run_batch), for a prepared engine. */
+void launch_app_batch(kk_engine *e, const BatchPlan &plan, BatchSlot &slot, const BatchJob *d_jobs, uint32_t *length,
+                      uint32_t **path, unsigned long long *d_steps, int *d_status, bool want_paths, bool p,
+                      const uint32_t *hdr)
+{
+    const GraphView g = e->view();
+    const uint8_t *vmask = (const uint8_t *)e->vmask.p;
+    if (plan.app == KK_APP_DEEPWALK)
+    {
+        if (plan.weighted)
+            launch_batch(e, DeepWalkBatch<true>{e->d_w}, plan, slot, d_jobs, length, path, d_steps, d_status,
+                         want_paths, p, hdr);
+        else
+            launch_batch(e, DeepWalkBatch<false>{nullptr}, plan, slot, d_jobs, length, path, d_steps, d_status,
+                         want_paths, p, hdr);
+    }
+    else if (plan.app == KK_APP_NODE2VEC)
+    {
+        const EdgeSetView set = p ? e->n2v_adjacency == 0 ? EdgeSetView{(const uint64_t *)e->edge_set.p,
+                                                                         (const uint32_t *)e->edge_pos.p,
+                                                                         e->edge_set_nb}
+                                                           : EdgeSetView{nullptr, nullptr, 0}
+                                  : node2vec_edge_set(e);
+        if (plan.weighted)
+            launch_batch(e, Node2vecBatch<true>{g.nbr, e->d_w, set}, plan, slot, d_jobs, length, path, d_steps,
+                         d_status, want_paths, p, hdr);
+        else
+            launch_batch(e, Node2vecBatch<false>{g.nbr, nullptr, set}, plan, slot, d_jobs, length, path, d_steps,
+                         d_status, want_paths, p, hdr);
+    }
+    else
+    {
+        if (!p)
+            vmask = metapath_vertex_masks(e);
+        if (plan.weighted)
+            launch_batch(e, MetapathBatch<true>{vmask, e->d_type, e->d_w}, plan, slot, d_jobs, length, path,
+                         d_steps, d_status, want_paths, p, hdr);
+        else
+            launch_batch(e, MetapathBatch<false>{vmask, e->d_type, nullptr}, plan, slot, d_jobs, length, path,
+                         d_steps, d_status, want_paths, p, hdr);
+    }
 }
 
 /* Builds the weight alias tables in the layout App's walk reads. */
@@ -186,12 +237,117 @@ void batch_prepare(kk_engine *e, const BatchPlan &plan)
     }
 }
 
-uint64_t run_batch(kk_engine *e, BatchPlan &plan, BatchSlot &slot, bool want_paths, bool prepared)
+/* Staging layout of a graph-mode slot (pinned): the job table, the metapath
+ * schemes, the counts header, the status words. */
+struct GraphStage
+{
+    BatchJob *jobs;
+    MetaSchemes *schemes;
+    uint32_t *hdr;
+    int *status;
+};
+
+static GraphStage graph_stage(const BatchSlot &slot)
+{
+    GraphStage g;
+    g.jobs = (BatchJob *)slot.h_stage;
+    g.schemes = (MetaSchemes *)(g.jobs + kMaxBatchJobs);
+    g.hdr = (uint32_t *)(g.schemes + kMaxBatchJobs);
+    g.status = (int *)(g.hdr + 4);
+    return g;
+}
+
+void batch_slot_graph_mode(kk_engine *e, BatchSlot &slot, uint32_t max_walkers, uint64_t max_cap)
 {
     for (int i = 0; i < 3; i++)
         if (slot.ev[i] == nullptr)
             KK_CUDA_CHECK(cudaEventCreate(&slot.ev[i]));
-    const uint8_t *vmask = nullptr;
+    slot.max_walkers = max_walkers;
+    slot.max_cap = max_cap;
+    slot.jobs.as<BatchJob>(kMaxBatchJobs);
+    slot.schemes.as<MetaSchemes>(kMaxBatchJobs);
+    slot.small.ensure(128);
+    slot.length.as<uint32_t>(max_walkers);
+    slot.path.as<uint32_t>(max_cap);
+    const size_t stage = kMaxBatchJobs * (sizeof(BatchJob) + sizeof(MetaSchemes)) + 16 + 64;
+    KK_CUDA_CHECK(cudaHostAlloc((void **)&slot.h_stage, stage, cudaHostAllocDefault));
+    memset(slot.h_stage, 0, stage);
+    slot.graph_mode = true;
+    (void)e;
+}
+
+/* One graph-mode batch: stage the job table and counts, replay (capturing it
+ * on first use) the slot's graph, read the status back. */
+static uint64_t run_batch_graph(kk_engine *e, BatchPlan &plan, BatchSlot &slot)
+{
+    if (plan.total > slot.max_walkers || plan.total_cap > slot.max_cap)
+        fail(KK_ERR_INVALID_CONFIG, "batch larger than the slot");
+    const GraphStage h = graph_stage(slot);
+    BatchJob *d_jobs = (BatchJob *)slot.jobs.p;
+    MetaSchemes *d_sc = (MetaSchemes *)slot.schemes.p;
+    int *d_status = (int *)slot.small.p;
+    unsigned long long *d_steps = (unsigned long long *)((char *)d_status + 16);
+    const uint32_t *d_hdr = (const uint32_t *)((char *)d_status + 64);
+    const uint32_t nj = (uint32_t)plan.jobs.size();
+    for (uint32_t j = 0; j < nj; j++)
+        plan.jobs[j].param = d_sc + j;
+    memcpy(h.jobs, plan.jobs.data(), nj * sizeof(BatchJob));
+    if (!plan.schemes.empty())
+        memcpy(h.schemes, plan.schemes.data(), plan.schemes.size() * sizeof(MetaSchemes));
+    h.hdr[0] = nj;
+    h.hdr[1] = plan.total;
+    if (slot.exec == nullptr)
+    {
+        cudaGraph_t graph = nullptr;
+        KK_CUDA_CHECK(cudaStreamBeginCapture(slot.stream, cudaStreamCaptureModeThreadLocal));
+        try
+        {
+            KK_CUDA_CHECK(cudaMemcpyAsync(d_jobs, h.jobs, kMaxBatchJobs * sizeof(BatchJob), cudaMemcpyHostToDevice,
+                                          slot.stream));
+            if (plan.app == KK_APP_METAPATH)
+                KK_CUDA_CHECK(cudaMemcpyAsync(d_sc, h.schemes, kMaxBatchJobs * sizeof(MetaSchemes),
+                                              cudaMemcpyHostToDevice, slot.stream));
+            KK_CUDA_CHECK(cudaMemcpyAsync((void *)d_hdr, h.hdr, 16, cudaMemcpyHostToDevice, slot.stream));
+            KK_CUDA_CHECK(cudaMemsetAsync(d_status, 0, 64, slot.stream));
+            uint32_t *path = nullptr;
+            launch_app_batch(e, plan, slot, d_jobs, (uint32_t *)slot.length.p, &path, d_steps, d_status, true, true,
+                             d_hdr);
+            KK_CUDA_CHECK(cudaMemcpyAsync(h.status, d_status, 64, cudaMemcpyDeviceToHost, slot.stream));
+        }
+        catch (...)
+        {
+            cudaStreamEndCapture(slot.stream, &graph);
+            if (graph)
+                cudaGraphDestroy(graph);
+            throw;
+        }
+        KK_CUDA_CHECK(cudaStreamEndCapture(slot.stream, &graph));
+        const cudaError_t ie = cudaGraphInstantiate(&slot.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        KK_CUDA_CHECK(ie);
+    }
+    KK_CUDA_CHECK(cudaEventRecord(slot.ev[1], slot.stream));
+    KK_CUDA_CHECK(cudaGraphLaunch(slot.exec, slot.stream));
+    KK_CUDA_CHECK(cudaEventRecord(slot.ev[2], slot.stream));
+    KK_CUDA_CHECK(cudaStreamSynchronize(slot.stream));
+    slot.alias_ms = 0.0f;
+    KK_CUDA_CHECK(cudaEventElapsedTime(&slot.walk_ms, slot.ev[1], slot.ev[2]));
+    if (h.status[0] == KK_STATUS_TRIAL_LIMIT)
+        fail(KK_ERR_TRIAL_LIMIT, "a walker exceeded the rejection-trial limit");
+    if (h.status[0] == KK_STATUS_PATH_CAPACITY)
+        fail(KK_ERR_PATH_CAPACITY, "a walk exceeded its path capacity");
+    unsigned long long steps;
+    memcpy(&steps, (char *)h.status + 16, sizeof(steps));
+    return steps;
+}
+
+uint64_t run_batch(kk_engine *e, BatchPlan &plan, BatchSlot &slot, bool want_paths, bool prepared)
+{
+    if (slot.graph_mode)
+        return run_batch_graph(e, plan, slot);
+    for (int i = 0; i < 3; i++)
+        if (slot.ev[i] == nullptr)
+            KK_CUDA_CHECK(cudaEventCreate(&slot.ev[i]));
     if (!prepared && plan.app == KK_APP_NODE2VEC)
         graph_sort_adjacency(e);
     if (plan.app == KK_APP_METAPATH)
@@ -201,7 +357,6 @@ uint64_t run_batch(kk_engine *e, BatchPlan &plan, BatchSlot &slot, bool want_pat
                                       cudaMemcpyHostToDevice, slot.stream));
         for (size_t j = 0; j < plan.jobs.size(); j++)
             plan.jobs[j].param = d_sc + j;
-        vmask = prepared ? (const uint8_t *)e->vmask.p : metapath_vertex_masks(e);
     }
     BatchJob *d_jobs = slot.jobs.as<BatchJob>(plan.jobs.size());
     KK_CUDA_CHECK(cudaMemcpyAsync(d_jobs, plan.jobs.data(), plan.jobs.size() * sizeof(BatchJob),
@@ -218,40 +373,7 @@ uint64_t run_batch(kk_engine *e, BatchPlan &plan, BatchSlot &slot, bool want_pat
     }
     uint32_t *length = slot.length.as<uint32_t>(plan.total);
     uint32_t *path = nullptr;
-    const GraphView g = e->view();
-    const bool p = prepared;
-    if (plan.app == KK_APP_DEEPWALK)
-    {
-        if (plan.weighted)
-            launch_batch(e, DeepWalkBatch<true>{e->d_w}, plan, slot, d_jobs, length, &path, d_steps, d_status,
-                         want_paths, p);
-        else
-            launch_batch(e, DeepWalkBatch<false>{nullptr}, plan, slot, d_jobs, length, &path, d_steps, d_status,
-                         want_paths, p);
-    }
-    else if (plan.app == KK_APP_NODE2VEC)
-    {
-        const EdgeSetView set = p ? e->n2v_adjacency == 0 ? EdgeSetView{(const uint64_t *)e->edge_set.p,
-                                                                         (const uint32_t *)e->edge_pos.p,
-                                                                         e->edge_set_nb}
-                                                           : EdgeSetView{nullptr, nullptr, 0}
-                                  : node2vec_edge_set(e);
-        if (plan.weighted)
-            launch_batch(e, Node2vecBatch<true>{g.nbr, e->d_w, set}, plan, slot, d_jobs, length, &path, d_steps,
-                         d_status, want_paths, p);
-        else
-            launch_batch(e, Node2vecBatch<false>{g.nbr, nullptr, set}, plan, slot, d_jobs, length, &path, d_steps,
-                         d_status, want_paths, p);
-    }
-    else
-    {
-        if (plan.weighted)
-            launch_batch(e, MetapathBatch<true>{vmask, e->d_type, e->d_w}, plan, slot, d_jobs, length, &path,
-                         d_steps, d_status, want_paths, p);
-        else
-            launch_batch(e, MetapathBatch<false>{vmask, e->d_type, nullptr}, plan, slot, d_jobs, length, &path,
-                         d_steps, d_status, want_paths, p);
-    }
+    launch_app_batch(e, plan, slot, d_jobs, length, &path, d_steps, d_status, want_paths, prepared, nullptr);
     KK_CUDA_CHECK(cudaEventRecord(slot.ev[2], slot.stream));
     int h_small[16];
     KK_CUDA_CHECK(cudaMemcpyAsync(h_small, d_status, sizeof(h_small), cudaMemcpyDeviceToHost, slot.stream));

@@ -368,6 +368,8 @@ kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value)
             e->walk_stats = (int)value;
         else if (n == "alias_mid_tier" && (value == 0 || value == 1))
             e->alias_mid_tier = (int)value;
+        else if (n == "walk_multi" && (value == 1 || value == 2 || value == 4))
+            e->walk_multi = (int)value;
         else
             fail(KK_ERR_INVALID_CONFIG, "unknown option or value out of range: " + n);
     });

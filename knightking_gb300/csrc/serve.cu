@@ -255,8 +255,8 @@ kk_status kk_serve_start(kk_engine *e, const kk_serve_opts *opts, kk_server **ou
             o.max_jobs = 256;
         if (o.slot_bytes == 0)
             o.slot_bytes = 1ull << 30;
-        if (o.slots < 1 || o.slots > 8 || o.max_jobs > kMaxBatchJobs)
-            fail(KK_ERR_INVALID_CONFIG, "slots 1..8, max_jobs 1..1024");
+        if (o.slots < 1 || o.slots > 8 || o.max_jobs > kMaxBatchJobs || o.launch_mode < 0 || o.launch_mode > 1)
+            fail(KK_ERR_INVALID_CONFIG, "slots 1..8, max_jobs 1..1024, launch_mode 0 or 1");
         s->e = e;
         s->o = o;
         /* resident tables, built once on the engine's stream */
@@ -269,7 +269,12 @@ kk_status kk_serve_start(kk_engine *e, const kk_serve_opts *opts, kk_server **ou
         KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
         s->slots.resize(o.slots);
         for (int k = 0; k < o.slots; k++)
+        {
             KK_CUDA_CHECK(cudaStreamCreateWithFlags(&s->slots[k].stream, cudaStreamNonBlocking));
+            if (o.launch_mode == 0)
+                batch_slot_graph_mode(e, s->slots[k], (uint32_t)std::min<uint64_t>(o.slot_bytes / 8, 0x80000000ull),
+                                      o.slot_bytes / 4);
+        }
         s->pool = new HostPool();
         s->pool->limit = (size_t)o.slots * 2 * o.slot_bytes;
         for (int k = 0; k < o.slots; k++)

@@ -14,6 +14,7 @@ DEFAULT_SPACE = (
     ("alias_mid_tier", (0, 1)),
     ("node2vec_adjacency", (0, 1)),
     ("walk_block", (256, 128, 64)),
+    ("walk_multi", (1, 2, 4)),
     ("l2_fetch_bytes", (0, 64)),
     ("walk_schedule", (0, 1)),
 )
@@ -27,6 +28,8 @@ def space_for(app, weighted):
         if name in ("alias_layout", "alias_mid_tier") and not weighted:
             continue
         if name == "node2vec_adjacency" and app != "node2vec":
+            continue
+        if name == "walk_multi" and app not in ("deepwalk", "ppr"):
             continue
         out.append((name, vals))
     return tuple(out)

@@ -152,6 +152,32 @@ def test_fresh_walks_match_oracle(engine, oracle_lib, i, seed, schedule, layout)
     assert ps.total_steps == steps
 
 
+@pytest.mark.parametrize("multi", [2, 4])
+@pytest.mark.parametrize("i", [0, 1, 2, 3])
+def test_multi_walker_kernel_matches_oracle(engine, oracle_lib, i, multi):
+    """Several walkers per thread (DeepWalk and PPR), both alias layouts."""
+    app, gkw, wkw = FRESH[i]
+    g = G.random_undirected(500, 6000, seed=40 + i, **gkw)
+    csr = G.csr_file_order(500, g["src"], g["dst"], w=g.get("w"), type=g.get("type"))
+    engine.load_arrays(500, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
+    weighted = "w" in csr
+    n = 1500
+    ocsr = oracle_lib.CSR(500, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
+    prm = oracle_lib.make_params(app, seed=31, walker_begin=9, walker_num=n, weighted=weighted, **wkw)
+    lens, verts, steps = oracle_lib.walk(ocsr, prm, cap=4096)
+    engine.set_option("walk_multi", multi)
+    try:
+        for layout in (0, 1):
+            engine.set_option("alias_layout", layout)
+            ps = engine.walk(app, n, seed=31, weighted=weighted, walker_begin=9, **wkw)
+            np.testing.assert_array_equal(ps.path_length, lens)
+            np.testing.assert_array_equal(ps.vertices, verts)
+            assert ps.total_steps == steps
+    finally:
+        engine.set_option("walk_multi", 1)
+        engine.set_option("alias_layout", 0)
+
+
 def test_ppr_start_list_matches_oracle(engine, oracle_lib):
     g = G.random_undirected(300, 3000, seed=3, weight="int5")
     csr = G.csr_file_order(300, g["src"], g["dst"], w=g["w"])

@@ -61,11 +61,13 @@ def _serve_all(engine, app, reqs, clients=4, **server_kw):
     return results, stats
 
 
+@pytest.mark.parametrize("graphs", [True, False])
 @pytest.mark.parametrize("app", ["node2vec", "deepwalk", "metapath"])
-def test_served_requests_equal_alone(engine, app):
+def test_served_requests_equal_alone(engine, app, graphs):
+    """Slots replaying captured CUDA graphs, and slots launching on their streams."""
     _load(engine, 11, types=app == "metapath")
     reqs = _requests(app, 60, seed=5)
-    results, stats = _serve_all(engine, app, reqs, slots=2, max_jobs=16, slot_bytes=8 << 20)
+    results, stats = _serve_all(engine, app, reqs, slots=2, max_jobs=16, slot_bytes=8 << 20, graphs=graphs)
     assert stats["completed"] == len(reqs) and stats["failed"] == 0
     assert stats["batches"] >= 2
     assert stats["p99_ms"] >= stats["p50_ms"] > 0

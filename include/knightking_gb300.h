@@ -113,7 +113,6 @@ kk_status kk_engine_set_stream(kk_engine *e, void *stream);
  *   "l2_fetch_bytes"     the context's cudaLimitMaxL2FetchGranularity while the engine
  *                        lives: 32, 64, 128, or 0 for the value found (restored on destroy)
  *   "walk_stats"         1 counts trials, queries and probes (kk_last_walk_stats)
- *   "alias_mid_tier"     alias build of degrees 33..128: 0 one thread per vertex, 1 a warp per vertex
  *   "walk_multi"         walkers per thread (1, 2, 4) of first-order walks without a dynamic component */
 kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value);
 /* Message of the last failed call on this engine ("" if none). */

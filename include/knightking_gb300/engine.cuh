@@ -244,12 +244,14 @@ struct kk_engine
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     cudaStream_t side = nullptr; /* hub alias builds run here, joined by events */
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    /* vertices by degree, descending (cached per graph), and the alias tiers:
-     * [0, n_hub) hubs, [n_hub, n_warp) warp tier (rings in the scratch up to
-     * n_staged, in shared memory after), [n_warp, n_t32) degree 33..128,
-     * [n_t32, n_nz) degree 1..32, rest isolated */
+    /* vertices by degree, descending (cached per graph), and the alias-build
+     * classes: tier[k] = number of vertices of degree > kAliasClassMax[k]
+     * (k < 8) and tier[8] = number of degree > 0, so [0, n_hub) are the hubs,
+     * [tier[c - 1], tier[c]) class c, [n_nz, V) isolated */
     kk::DevBuf order;
-    uint32_t n_hub = 0, n_staged = 0, n_warp = 0, n_t32 = 0, n_nz = 0;
+    uint32_t tier[kk::kTierBounds] = {};
+    uint32_t n_hub = 0, n_nz = 0;
+    kk::DevBuf alias_next; /* the classes' work counters */
     bool order_valid = false;
     kk::DevBuf vcur; /* vertex cursors (begin | degree << 40), cached per graph */
     bool vcur_valid = false;
@@ -291,9 +293,6 @@ struct kk_engine
      * e->alias hold (0 cursor, 1 index), -1 none. */
     int alias_cache = 0;
     int alias_cached = -1;
-    /* alias_mid_tier (option): degrees 33..128 by the thread tier (0) or by
-     * the warp kernel with staged rows (1) */
-    int alias_mid_tier = 0;
     /* l2_fetch_bytes (option): the context's cudaLimitMaxL2FetchGranularity
      * hint while the engine lives (0: left as found); the value found is put
      * back when the option returns to 0 and when the engine is destroyed. */
@@ -427,27 +426,32 @@ inline apps::MetaSchemes make_schemes(const kk_walk_opts &o)
 }
 
 /* One thread tier: blocks of NT vertices, a few resident per SM. */
-template <typename TC, typename Bucket, uint32_t D, uint32_t NT>
-void launch_alias_thread(kk_engine *e, const TC &tc, Bucket *alias, const uint64_t *vcur, float *sum,
-                         const uint32_t *order, uint32_t lo, uint32_t hi)
+/* Launches one alias class [lo, hi) with kernel `kern` of nt threads and
+ * smem bytes of dynamic shared memory per block, as many blocks as fit on
+ * every SM (at most one per `per_block` vertices). */
+template <typename K>
+void launch_alias_class(kk_engine *e, K kern, unsigned nt, size_t smem, uint32_t per_block, uint32_t lo, uint32_t hi,
+                        int &resident, const std::function<void(unsigned)> &launch)
 {
-    constexpr size_t smem = alias_thread_smem<D, NT>();
-    static bool attr_set = false;
-    if (!attr_set)
+    if (hi <= lo)
+        return;
+    if (resident == 0)
     {
-        KK_CUDA_CHECK(cudaFuncSetAttribute(alias_thread_kernel<TC, Bucket, D, NT>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr_set = true;
+        /* the opt-in limit counts dynamic bytes only; static shared memory comes on top */
+        KK_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        KK_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, (int)nt, smem));
+        if (resident < 1)
+            resident = 1;
     }
-    const uint32_t blocks = (hi - lo + NT - 1) / NT;
-    const uint32_t cap = 4u * (uint32_t)e->sm_count;
-    alias_thread_kernel<TC, Bucket, D, NT>
-        <<<blocks < cap ? blocks : cap, NT, smem, e->stream>>>(e->view(), tc, alias, vcur, sum, order, lo, hi);
+    const uint64_t want = (uint64_t)resident * (uint64_t)e->sm_count;
+    const uint64_t need = ((uint64_t)(hi - lo) + per_block - 1) / per_block;
+    launch((unsigned)(need < want ? need : want));
     KK_CUDA_CHECK(cudaGetLastError());
 }
 
 /* Builds alias tables in the Bucket layout into e->alias/e->sum for a
- * static functor. */
+ * static functor: hubs on the side stream, the other classes in turn on the
+ * main stream, every class largest vertex first from its own counter. */
 template <typename TC, typename Bucket = IndexBucket>
 void build_alias(kk_engine *e, const TC &tc)
 {
@@ -464,47 +468,53 @@ void build_alias(kk_engine *e, const TC &tc)
     float *sum = e->sum.as<float>(e->V);
     const uint32_t *order = vertex_order(e);
     const uint64_t *vcur = Bucket::cursor ? vertex_cursors(e) : nullptr;
-    const unsigned sms = (unsigned)e->sm_count;
     uint2 *scratch = e->scratch.as<uint2>(2 * e->E);
+    uint32_t *next = e->alias_next.as<uint32_t>(16);
+    KK_CUDA_CHECK(cudaMemsetAsync(next, 0, 16 * sizeof(uint32_t), e->stream));
+    const uint32_t *t = e->tier;
+    cudaStream_t st = e->stream;
     if (e->n_hub)
     {
         /* hubs first, largest first, on the side stream so they start at once */
         KK_CUDA_CHECK(cudaEventRecord(e->ev_fork, e->stream));
         KK_CUDA_CHECK(cudaStreamWaitEvent(e->side, e->ev_fork, 0));
-        unsigned grid = e->n_hub < sms ? e->n_hub : sms;
-        alias_build_hub_kernel<TC, Bucket>
-            <<<grid, 1024, 0, e->side>>>(g, tc, alias, vcur, sum, scratch, order, 0, e->n_hub);
+        const unsigned grid = e->n_hub < (uint32_t)e->sm_count ? e->n_hub : (unsigned)e->sm_count;
+        alias_build_hub_kernel<TC, Bucket><<<grid, 1024, 0, e->side>>>(g, tc, alias, vcur, sum, scratch, order, 0,
+                                                                       e->n_hub, next);
         KK_CUDA_CHECK(cudaGetLastError());
         KK_CUDA_CHECK(cudaEventRecord(e->ev_join, e->side));
     }
-    if (e->n_warp > e->n_hub)
+    /* 4097..16384: the hub kernel in 256-thread blocks */
     {
-        static bool smem_set = false;
-        if (!smem_set)
-        {
-            KK_CUDA_CHECK(cudaFuncSetAttribute(alias_pair_kernel<TC, Bucket>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kAliasPairSmem));
-            smem_set = true;
-        }
-        /* two launches: rows with rings in the scratch, then rows staged in
-         * shared memory (separate kernels in a launch list) */
-        const uint32_t bounds[3] = {e->n_hub, e->n_staged, e->alias_mid_tier ? e->n_t32 : e->n_warp};
-        for (int r = 0; r < 2; r++)
-        {
-            const uint32_t n = bounds[r + 1] - bounds[r];
-            if (n == 0)
-                continue;
-            unsigned grid = (n + 7) / 8 < 4 * sms ? (n + 7) / 8 : 4 * sms;
-            alias_pair_kernel<TC, Bucket><<<grid, 256, kAliasPairSmem, e->stream>>>(
-                g, tc, alias, vcur, sum, scratch, order, bounds[r], bounds[r + 1]);
-            KK_CUDA_CHECK(cudaGetLastError());
-        }
-        KK_CUDA_CHECK(cudaGetLastError());
+        static int res = 0;
+        launch_alias_class(e, alias_build_hub_kernel<TC, Bucket>, 256, 0, 1, t[0], t[1], res, [&](unsigned grid) {
+            alias_build_hub_kernel<TC, Bucket><<<grid, 256, 0, st>>>(g, tc, alias, vcur, sum, scratch, order, t[0],
+                                                                     t[1], next + 1);
+        });
     }
-    if (e->n_t32 > e->n_warp && !e->alias_mid_tier)
-        launch_alias_thread<TC, Bucket, kAliasThreadMax, 64>(e, tc, alias, vcur, sum, order, e->n_warp, e->n_t32);
-    if (e->n_nz > e->n_t32)
-        launch_alias_thread<TC, Bucket, kAliasThreadSmall, 256>(e, tc, alias, vcur, sum, order, e->n_t32, e->n_nz);
+    /* 2049..4096: a block per vertex, the row in shared memory */
+    {
+        static int res = 0;
+        constexpr size_t smem = alias_block_row_smem<4096>();
+        launch_alias_class(e, alias_block_row_kernel<TC, Bucket, 256, 4096>, 256, smem, 1, t[1], t[2], res,
+                           [&](unsigned grid) {
+                               alias_block_row_kernel<TC, Bucket, 256, 4096>
+                                   <<<grid, 256, smem, st>>>(g, tc, alias, vcur, sum, order, t[1], t[2], next + 2);
+                           });
+    }
+    /* 1..2048: lane groups, 32/G vertices per warp */
+    auto group = [&](auto kern, uint32_t G, size_t smem, int c, int &res) {
+        launch_alias_class(e, kern, 32, smem, 32 / G, t[c - 1], t[c], res, [&](unsigned grid) {
+            kern<<<grid, 32, smem, st>>>(g, tc, alias, vcur, sum, order, t[c - 1], t[c], next + c);
+        });
+    };
+    static int r3 = 0, r4 = 0, r5 = 0, r6 = 0, r7 = 0, r8 = 0;
+    group(alias_group_kernel<TC, Bucket, 32, 2048>, 32, alias_group_smem_per_warp<32, 2048>(), 3, r3);
+    group(alias_group_kernel<TC, Bucket, 32, 1024>, 32, alias_group_smem_per_warp<32, 1024>(), 4, r4);
+    group(alias_group_kernel<TC, Bucket, 16, 512>, 16, alias_group_smem_per_warp<16, 512>(), 5, r5);
+    group(alias_group_kernel<TC, Bucket, 8, 128>, 8, alias_group_smem_per_warp<8, 128>(), 6, r6);
+    group(alias_group_kernel<TC, Bucket, 4, 32>, 4, alias_group_smem_per_warp<4, 32>(), 7, r7);
+    group(alias_group_kernel<TC, Bucket, 2, 16>, 2, alias_group_smem_per_warp<2, 16>(), 8, r8);
     if (e->n_hub)
         KK_CUDA_CHECK(cudaStreamWaitEvent(e->stream, e->ev_join, 0));
     if constexpr (weight_tables)

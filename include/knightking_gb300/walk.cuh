@@ -378,22 +378,27 @@ constexpr bool use_cursor_buckets()
  * sequential algorithm's, bucket for bucket and bit for bit; only the serial
  * sum stays sequential (one FADD chain per vertex).
  *
- * Vertices run over a degree-descending vertex order:
- *   hubs (deg >= kAliasHubMin): a 1024-thread block per vertex does sum,
- *        split and pairing, queues in the 16 B/edge scratch at 2*off[v];
- *        batches of 64 or fewer go to one warp (no block barrier);
- *   warp tier (kAliasThreadMax < deg < kAliasHubMin): a warp per vertex
- *        sums (lane 0, from coalesced chunks in shared memory), splits and
- *        pairs, queues and neighbours in shared memory up to kAliasWarpQueue
- *        entries, else queues in the scratch;
- *   thread tiers (deg <= kAliasThreadMax): one thread per vertex runs the
- *        serial algorithm on rings in shared memory (alias_thread_kernel). */
+ * Vertices run over a degree-descending vertex order, in degree classes
+ * (kAliasClassMax), each taken largest first from an atomic counter:
+ *   hubs (deg > 16384): a 1024-thread block per vertex does sum, split and
+ *        pairing, queues in the 16 B/edge scratch at 2*off[v]; batches of 64
+ *        or fewer go to one warp (no block barrier); on a side stream;
+ *   4097..16384: the same kernel with 256-thread blocks, several per SM;
+ *   2049..4096: a block per vertex, the row and its queues in shared memory
+ *        (alias_block_row_kernel);
+ *   1..2048: groups of G lanes per vertex, 32/G vertices per warp, rows and
+ *        queues in shared memory (alias_group_kernel): G = 32 above 512,
+ *        16 above 128, 8 above 32, 4 above 16, else 2.
+ * A group's batches are at most G wide; the average batch of a FIFO pairing
+ * over lognormal weights is about deg/30 wide, so narrow groups on small rows
+ * keep the lanes busy, and the groups of a warp run converged (every loop to
+ * the warp's maximum), sharing each instruction. */
 
-constexpr uint32_t kAliasHubMin = 16385;  /* degree from which a vertex is a hub */
-constexpr uint32_t kAliasThreadMax = 128; /* largest degree of the thread tiers */
-constexpr uint32_t kAliasThreadSmall = 32; /* largest degree of the narrow thread tier */
-constexpr uint32_t kAliasWarpQueue = 512; /* shared-memory queue entries per warp */
-constexpr size_t kAliasPairSmem = (size_t)8 * kAliasWarpQueue * (sizeof(uint2) + sizeof(uint32_t)); /* 8 warps */
+constexpr uint32_t kAliasHubMin = 16385; /* degree from which a vertex is a hub */
+/* largest degree of each class after the hubs; class c holds the vertices of
+ * degree in (kAliasClassMax[c], kAliasClassMax[c - 1]] */
+constexpr uint32_t kAliasClasses = 8;
+constexpr uint32_t kAliasClassMax[kAliasClasses] = {16384, 4096, 2048, 1024, 512, 128, 32, 16};
 constexpr unsigned kFullMask = 0xffffffffu;
 
 __device__ __forceinline__ uint32_t lanemask_lt()
@@ -604,213 +609,381 @@ __device__ __forceinline__ void block_split(Load load, uint32_t deg, float ave, 
     }
 }
 
-/* Serial sums (:579-584) and averages (:589) of the non-hub vertices: one
- * thread per vertex over the degree-sorted order, so a warp's vertices have
- * similar degrees.  Loads are issued four at a time; the additions stay in
- * CSR order. */
-template <typename TC>
-__global__ void __launch_bounds__(256) alias_sum_kernel(GraphView g, TC tc, float *sum_out, float *ave_out,
-                                                        const uint32_t *order, uint32_t lo, uint32_t hi)
+/* Group tiers: a group of G lanes per vertex of degree <= DMAX, 32/G vertices
+ * per warp side by side, each row staged in shared memory at 10 B/edge:
+ *   F[i]  its probability (static_comp), then its residual (prob[] of :582,
+ *         updated in place as :613 does);
+ *   N[i]  its neighbour;
+ *   Q[s]  the two queues as 16-bit edge indices: the p queue a ring over the
+ *         first S0 slots, the q queue a ring over the last B0 slots counted
+ *         from the end (neither queue outgrows its start).
+ * A pairing batch is min(lp, lq, G) iterations on the group's lanes, so a
+ * vertex whose batches are short shares its warp with other vertices instead
+ * of idling 32 - b lanes.  Vertices are taken from *next in degree-descending
+ * order, 32/G consecutive ones per warp (vertices of similar degree side by
+ * side). */
+template <uint32_t G, uint32_t DMAX>
+constexpr size_t alias_group_smem_per_warp()
 {
-    for (uint32_t k = lo + blockIdx.x * blockDim.x + threadIdx.x; k < hi; k += gridDim.x * blockDim.x)
-    {
-        const uint32_t v = order[k];
-        const int64_t e0 = g.off[v];
-        const uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
-        float sum = 0.0f;
-        uint32_t j = 0;
-        for (; j + 4 <= deg; j += 4)
-        {
-            const float a = static_at(g, tc, v, e0 + j), b = static_at(g, tc, v, e0 + j + 1);
-            const float c = static_at(g, tc, v, e0 + j + 2), d = static_at(g, tc, v, e0 + j + 3);
-            sum = fadd(fadd(fadd(fadd(sum, a), b), c), d);
-        }
-        for (; j < deg; j++)
-            sum = fadd(sum, static_at(g, tc, v, e0 + j));
-        if (sum_out != nullptr)
-            sum_out[v] = sum;
-        ave_out[v] = fdiv(sum, u2f(deg));
-    }
+    return (size_t)(32 / G) * DMAX * 10;
 }
 
-/* Split (:594-603) and batched FIFO pairing (:605-638) of the warp tier: a
- * warp per vertex.  The queues are the rings of the thread tiers (p from the
- * front of a deg-entry array, q from the back; neither outgrows its start) with
- * (index, prob) entries; up to kAliasWarpQueue entries they and the row's
- * neighbours sit in shared memory, so a batch's bucket writes wait on no
- * global load; larger rows use the global scratch at 2*off[v].  A batch of b
- * pairings reads entries [h, h+b) of both rings and writes only behind their
- * tails, and all its reads precede its writes (the ballots depend on them). */
-template <typename Bucket, typename Nb>
-__device__ __forceinline__ void warp_pairing_ring(uint2 *R, uint32_t deg, uint32_t S0, uint32_t B0, float ave,
-                                                  Bucket *ob, Nb nb, const uint64_t *vcur, const uint8_t *ty)
+template <typename TC, typename Bucket, uint32_t G, uint32_t DMAX>
+__global__ void __launch_bounds__(32) alias_group_kernel(GraphView g, TC tc, Bucket *out, const uint64_t *vcur,
+                                                         float *sum_out, const uint32_t *order, uint32_t lo,
+                                                         uint32_t hi, uint32_t *next)
 {
-    const uint32_t lane = threadIdx.x & 31, lt = lanemask_lt();
-    uint32_t ph = 0, pt = 0, lp = S0, qh = 0, qt = 0, lq = B0, npop = 0;
-    auto pp = [&](uint32_t s) { return s >= S0 ? s - S0 : s; };           /* s < 2*S0 */
-    auto pq = [&](uint32_t s) { return deg - 1 - (s >= B0 ? s - B0 : s); }; /* s < 2*B0 */
-    while (lp != 0 && lq != 0)
+    static_assert(G == 2 || G == 4 || G == 8 || G == 16 || G == 32, "group of 2, 4, 8, 16 or 32 lanes");
+    static_assert(DMAX % 4 == 0 && DMAX <= 65535, "16-bit queue entries");
+    constexpr uint32_t RPW = 32 / G;
+    constexpr uint32_t gbits = G == 32 ? kFullMask : (1u << G) - 1u;
+    extern __shared__ uint32_t smem[];
+    const uint32_t lane = threadIdx.x & 31, grp = lane / G, gl = lane % G, gsh = grp * G;
+    const uint32_t glt = (1u << gl) - 1u;
+    float *F = reinterpret_cast<float *>(smem) + (size_t)grp * DMAX;
+    uint32_t *N = smem + (size_t)RPW * DMAX + (size_t)grp * DMAX;
+    uint16_t *Qs = reinterpret_cast<uint16_t *>(smem + (size_t)2 * RPW * DMAX) + (size_t)grp * DMAX;
+    /* every loop below runs to the warp's maximum with per-group predicates,
+     * so the groups stay converged and share each instruction */
+    for (;;)
     {
-        const uint32_t b = min(min(lp, lq), 32u);
-        const bool act = lane < b;
-        bool conv = false;
-        uint2 ne = make_uint2(0, 0);
-        if (act)
-        {
-            const uint2 pe = R[pp(ph + lane)], qe = R[pq(qh + lane)];
-            const float pv = __uint_as_float(pe.y), qv = __uint_as_float(qe.y);
-            ob[npop + lane] = Bucket::make_n(fdiv(pv, ave), pe.x, qe.x, nb(pe.x), nb(qe.x), vcur, ty);
-            const float r = fsub(qv, fsub(ave, pv));
-            conv = r < ave;
-            ne = make_uint2(qe.x, __float_as_uint(r));
-        }
-        const uint32_t mc = __ballot_sync(kFullMask, act && conv), ms = __ballot_sync(kFullMask, act && !conv);
-        if (act)
-        {
-            if (conv)
-                R[pp(pt + __popc(mc & lt))] = ne;
-            else
-                R[pq(qt + __popc(ms & lt))] = ne;
-        }
-        __syncwarp();
-        const uint32_t nc = __popc(mc), ns = __popc(ms);
-        ph = pp(ph + b);
-        qh = B0 ? (qh + b >= B0 ? qh + b - B0 : qh + b) : 0;
-        pt = pp(pt + nc);
-        qt = qt + ns >= B0 ? qt + ns - B0 : qt + ns;
-        lp = lp - b + nc;
-        lq = lq - b + ns;
-        npop += b;
-    }
-    /* leftovers (:623-638): the rest of whichever ring is non-empty */
-    for (uint32_t i = lane; i < lp; i += 32)
-    {
-        const uint32_t x = R[pp(ph + i)].x;
-        ob[npop + i] = Bucket::make_n(1.0f, x, kNone, nb(x), 0, vcur, ty);
-    }
-    for (uint32_t i = lane; i < lq; i += 32)
-    {
-        const uint32_t x = R[pq(qh + i)].x;
-        ob[npop + lp + i] = Bucket::make_n(1.0f, x, kNone, nb(x), 0, vcur, ty);
-    }
-    __syncwarp();
-}
-
-/* Sequential sum (:579-584) of a row by a warp: chunks of the row are loaded
- * coalesced into the warp's shared buffer F (kAliasWarpQueue floats) and lane 0
- * adds them in edge order; the sum is broadcast.  Staged rows (deg <=
- * kAliasWarpQueue) also keep their values in x[] (element 32c + lane). */
-template <typename TC>
-__device__ __forceinline__ float warp_row_sum(const GraphView &g, const TC &tc, vertex_id_t v, int64_t e0,
-                                              uint32_t deg, float *F, float (&x)[kAliasWarpQueue / 32])
-{
-    const uint32_t lane = threadIdx.x & 31;
-    float sum = 0.0f;
-    for (uint32_t base = 0; base < deg; base += kAliasWarpQueue)
-    {
-        const uint32_t n = min(deg - base, kAliasWarpQueue);
-#pragma unroll
-        for (uint32_t c = 0; c < kAliasWarpQueue / 32; c++)
-        {
-            const uint32_t i = c * 32 + lane;
-            if (i < n)
-            {
-                const float val = static_at(g, tc, v, e0 + base + i);
-                x[c] = val;
-                F[i] = val;
-            }
-        }
-        __syncwarp();
+        uint32_t t = 0;
         if (lane == 0)
+            t = atomicAdd(next, RPW);
+        t = __shfl_sync(kFullMask, t, 0);
+        if (t >= hi - lo)
+            break;
+        const uint32_t k = lo + t + grp;
+        uint32_t v = 0, deg = 0;
+        int64_t e0 = 0;
+        if (k < hi)
         {
-            uint32_t i = 0;
-            for (; i + 8 <= n; i += 8)
-                sum = fadd(fadd(fadd(fadd(fadd(fadd(fadd(fadd(sum, F[i]), F[i + 1]), F[i + 2]), F[i + 3]), F[i + 4]),
-                                     F[i + 5]),
-                                F[i + 6]),
-                           F[i + 7]);
-            for (; i < n; i++)
-                sum = fadd(sum, F[i]);
+            v = order[k];
+            e0 = g.off[v];
+            deg = (uint32_t)(g.off[v + 1] - e0);
         }
-        __syncwarp();
-    }
-    return __shfl_sync(kFullMask, sum, 0);
-}
-
-template <typename TC, typename Bucket>
-__global__ void __launch_bounds__(256) alias_pair_kernel(GraphView g, TC tc, Bucket *out, const uint64_t *vcur,
-                                                         float *sum_out, uint2 *scratch, const uint32_t *order,
-                                                         uint32_t lo, uint32_t hi)
-{
-    extern __shared__ uint2 dyn[];
-    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwib = blockDim.x >> 5;
-    const uint32_t lt = lanemask_lt();
-    const uint32_t nwarps = gridDim.x * nwib;
-    uint2 *sR = dyn + (size_t)wib * kAliasWarpQueue;
-    uint32_t *sNb = reinterpret_cast<uint32_t *>(dyn + (size_t)nwib * kAliasWarpQueue) + (size_t)wib * kAliasWarpQueue;
-    for (uint32_t k = lo + blockIdx.x * nwib + wib; k < hi; k += nwarps)
-    {
-        const uint32_t v = order[k];
-        const int64_t e0 = g.off[v];
-        const uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
-        const bool staged = deg <= kAliasWarpQueue;
-        /* the sum, with the ring's shared memory as the chunk buffer */
-        float x[kAliasWarpQueue / 32];
-        const float sum = warp_row_sum(g, tc, v, e0, deg, reinterpret_cast<float *>(sR), x);
-        if (lane == 0 && sum_out != nullptr)
-            sum_out[v] = sum;
-        const float ave = fdiv(sum, u2f(deg));
-        __syncwarp();
-        uint2 *R = staged ? sR : scratch + 2 * e0;
-        uint32_t S0 = 0, B0 = 0;
-        if (staged)
-        {
-            /* split from the values kept in registers; neighbours to shared memory */
-#pragma unroll
-            for (uint32_t c = 0; c < kAliasWarpQueue / 32; c++)
+        const uint32_t wdeg = __reduce_max_sync(kFullMask, deg);
+        /* stage the rows: probabilities and neighbours, G consecutive edges per load */
+#pragma unroll 4
+        for (uint32_t i = gl; i < wdeg; i += G)
+            if (i < deg)
             {
-                const uint32_t base = c * 32;
-                if (base >= deg)
-                    break;
-                const bool valid = base + lane < deg;
-                if (valid)
-                    sNb[base + lane] = g.nbr[e0 + base + lane];
-                const float xv = x[c];
-                const bool sm = valid && xv < ave, bg = valid && !(xv < ave);
-                const uint32_t mp = __ballot_sync(kFullMask, sm), mq = __ballot_sync(kFullMask, bg);
-                const uint2 ent = make_uint2(base + lane, __float_as_uint(xv));
-                if (sm)
-                    R[S0 + __popc(mp & lt)] = ent;
-                if (bg)
-                    R[deg - 1 - (B0 + __popc(mq & lt))] = ent;
-                S0 += __popc(mp);
-                B0 += __popc(mq);
+                F[i] = static_at(g, tc, v, e0 + i);
+                N[i] = g.nbr[e0 + i];
+            }
+        __syncwarp();
+        /* the sum in edge order (:579-584), one lane per group */
+        float sum = 0.0f;
+        if constexpr (RPW == 1)
+        {
+            if (lane == 0)
+            {
+                uint32_t i = 0;
+                for (; i + 8 <= deg; i += 8)
+                    sum = fadd(fadd(fadd(fadd(fadd(fadd(fadd(fadd(sum, F[i]), F[i + 1]), F[i + 2]), F[i + 3]),
+                                                   F[i + 4]),
+                                              F[i + 5]),
+                                         F[i + 6]),
+                                    F[i + 7]);
+                for (; i < deg; i++)
+                    sum = fadd(sum, F[i]);
+                if (deg != 0 && sum_out != nullptr)
+                    sum_out[v] = sum;
             }
         }
-        for (uint32_t base = 0; !staged && base < deg; base += 32)
+        else if (gl == 0)
         {
-            const bool valid = base + lane < deg;
-            const float x = valid ? static_at(g, tc, v, e0 + base + lane) : 0.0f;
+            /* a group past its row's end adds +0.0f, which leaves a sum of
+             * non-negative terms unchanged, so the FADD chain has no select */
+            uint32_t i = 0;
+            for (; i + 4 <= wdeg; i += 4)
+            {
+                const float a0 = i < deg ? F[i] : 0.0f, a1 = i + 1 < deg ? F[i + 1] : 0.0f;
+                const float a2 = i + 2 < deg ? F[i + 2] : 0.0f, a3 = i + 3 < deg ? F[i + 3] : 0.0f;
+                sum = fadd(fadd(fadd(fadd(sum, a0), a1), a2), a3);
+            }
+            for (; i < wdeg; i++)
+                sum = fadd(sum, i < deg ? F[i] : 0.0f);
+            if (deg != 0 && sum_out != nullptr)
+                sum_out[v] = sum;
+        }
+        sum = __shfl_sync(kFullMask, sum, gsh);
+        const float ave = fdiv(sum, u2f(deg));
+        /* split in edge order (:593-602): p queue from the front, q queue from the back */
+        uint32_t S0 = 0, B0 = 0;
+        for (uint32_t base = 0; base < wdeg; base += G)
+        {
+            const uint32_t i = base + gl;
+            const bool valid = i < deg;
+            const float x = valid ? F[i] : 0.0f;
             const bool sm = valid && x < ave, bg = valid && !(x < ave);
-            const uint32_t mp = __ballot_sync(kFullMask, sm), mq = __ballot_sync(kFullMask, bg);
-            const uint2 ent = make_uint2(base + lane, __float_as_uint(x));
+            const uint32_t mp = (__ballot_sync(kFullMask, sm) >> gsh) & gbits;
+            const uint32_t mq = (__ballot_sync(kFullMask, bg) >> gsh) & gbits;
             if (sm)
-                R[S0 + __popc(mp & lt)] = ent;
+                Qs[S0 + __popc(mp & glt)] = (uint16_t)i;
             if (bg)
-                R[deg - 1 - (B0 + __popc(mq & lt))] = ent;
+                Qs[deg - 1 - (B0 + __popc(mq & glt))] = (uint16_t)i;
             S0 += __popc(mp);
             B0 += __popc(mq);
         }
         __syncwarp();
+        /* pairing (:603-630) in batches of at most G iterations; a batch of
+         * b = 0 leaves a finished group's state unchanged */
         Bucket *ob = out + e0;
         const uint8_t *ty = g.type != nullptr ? g.type + e0 : nullptr;
-        if (staged)
-            warp_pairing_ring(R, deg, S0, B0, ave, ob, [&](uint32_t i) { return sNb[i]; }, vcur, ty);
-        else
+        uint32_t ph = 0, pt = 0, lp = S0, qh = 0, qt = 0, lq = B0, npop = 0;
+        for (;;)
         {
-            const uint32_t *nb = g.nbr + e0;
-            warp_pairing_ring(R, deg, S0, B0, ave, ob, [&](uint32_t i) { return nb[i]; }, vcur, ty);
+            const bool live = lp != 0 && lq != 0;
+            if (!__any_sync(kFullMask, live))
+                break;
+            const uint32_t b = live ? min(min(lp, lq), G) : 0;
+            const bool act = gl < b;
+            bool conv = false;
+            uint32_t qi = 0;
+            if (act)
+            {
+                const uint32_t ps = ph + gl, qs = qh + gl;
+                const uint32_t pi = Qs[ps >= S0 ? ps - S0 : ps];
+                qi = Qs[deg - 1 - (qs >= B0 ? qs - B0 : qs)];
+                const float pv = F[pi], qv = F[qi];
+                ob[npop + gl] = Bucket::make_n(fdiv(pv, ave), pi, qi, N[pi], N[qi], vcur, ty);
+                const float r = fsub(qv, fsub(ave, pv));
+                F[qi] = r;
+                conv = r < ave;
+            }
+            const uint32_t mc = (__ballot_sync(kFullMask, act && conv) >> gsh) & gbits;
+            const uint32_t ms = (__ballot_sync(kFullMask, act && !conv) >> gsh) & gbits;
+            if (act)
+            {
+                if (conv)
+                {
+                    const uint32_t s = pt + __popc(mc & glt);
+                    Qs[s >= S0 ? s - S0 : s] = (uint16_t)qi;
+                }
+                else
+                {
+                    const uint32_t s = qt + __popc(ms & glt);
+                    Qs[deg - 1 - (s >= B0 ? s - B0 : s)] = (uint16_t)qi;
+                }
+            }
+            __syncwarp();
+            const uint32_t nc = __popc(mc), ns = __popc(ms);
+            ph = ph + b >= S0 ? ph + b - S0 : ph + b;
+            qh = qh + b >= B0 ? qh + b - B0 : qh + b;
+            pt = pt + nc >= S0 ? pt + nc - S0 : pt + nc;
+            qt = qt + ns >= B0 ? qt + ns - B0 : qt + ns;
+            lp = lp - b + nc;
+            lq = lq - b + ns;
+            npop += b;
         }
+        /* leftovers (:623-638): the rest of whichever queue is non-empty */
+        const uint32_t wleft = __reduce_max_sync(kFullMask, lp + lq);
+        for (uint32_t i = gl; i < wleft; i += G)
+        {
+            if (i < lp)
+            {
+                const uint32_t s = ph + i >= S0 ? ph + i - S0 : ph + i;
+                const uint32_t x = Qs[s];
+                ob[npop + i] = Bucket::make_n(1.0f, x, kNone, N[x], 0, vcur, ty);
+            }
+            else if (i < lp + lq)
+            {
+                const uint32_t j = i - lp;
+                const uint32_t s = qh + j >= B0 ? qh + j - B0 : qh + j;
+                const uint32_t x = Qs[deg - 1 - s];
+                ob[npop + i] = Bucket::make_n(1.0f, x, kNone, N[x], 0, vcur, ty);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+/* Block-row tier: one NT-thread block per vertex of degree <= DMAX, the row
+ * staged in shared memory (12 B/edge): F[i] its probability then residual,
+ * N[i] its neighbour, and the p and q queues as linear arrays of 16-bit edge
+ * indices (each holds at most deg entries over the whole pairing).  Pairing
+ * batches span the block (b = min(lp, lq, NT) iterations, one per thread,
+ * conversions and survivors appended by block-wide stable ranks) while both
+ * queues are long, and warp 0 alone runs them in batches of 32 while one is
+ * short.  Vertices come from *next, largest first. */
+template <uint32_t DMAX>
+constexpr size_t alias_block_row_smem()
+{
+    return (size_t)DMAX * 12;
+}
+
+template <typename TC, typename Bucket, uint32_t NT, uint32_t DMAX>
+__global__ void __launch_bounds__(NT) alias_block_row_kernel(GraphView g, TC tc, Bucket *out, const uint64_t *vcur,
+                                                             float *sum_out, const uint32_t *order, uint32_t lo,
+                                                             uint32_t hi, uint32_t *next)
+{
+    static_assert(NT % 32 == 0 && NT <= 1024 && DMAX % 8 == 0 && DMAX <= 65535, "block-row tier shape");
+    extern __shared__ uint32_t smem[];
+    __shared__ uint32_t sa[33], sb[33], s_row[4];
+    __shared__ float s_ave;
+    float *F = reinterpret_cast<float *>(smem);
+    uint32_t *N = smem + DMAX;
+    uint16_t *P = reinterpret_cast<uint16_t *>(smem + 2 * DMAX);
+    uint16_t *Q = P + DMAX;
+    const uint32_t tid = threadIdx.x, lane = tid & 31;
+    for (;;)
+    {
+        if (tid == 0)
+            s_row[0] = atomicAdd(next, 1u);
+        __syncthreads();
+        const uint32_t t = s_row[0];
+        if (t >= hi - lo)
+            break;
+        const uint32_t v = order[lo + t];
+        const int64_t e0 = g.off[v];
+        const uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
+#pragma unroll 4
+        for (uint32_t i = tid; i < deg; i += NT)
+        {
+            F[i] = static_at(g, tc, v, e0 + i);
+            N[i] = g.nbr[e0 + i];
+        }
+        __syncthreads();
+        /* the sum in edge order (:579-584) by thread 0 */
+        if (tid == 0)
+        {
+            float sum = 0.0f;
+            uint32_t i = 0;
+            for (; i + 8 <= deg; i += 8)
+                sum = fadd(fadd(fadd(fadd(fadd(fadd(fadd(fadd(sum, F[i]), F[i + 1]), F[i + 2]), F[i + 3]), F[i + 4]),
+                                     F[i + 5]),
+                                F[i + 6]),
+                           F[i + 7]);
+            for (; i < deg; i++)
+                sum = fadd(sum, F[i]);
+            if (sum_out != nullptr)
+                sum_out[v] = sum;
+            s_ave = fdiv(sum, u2f(deg));
+        }
+        __syncthreads();
+        const float ave = s_ave;
+        /* stable split in edge order (:593-602) */
+        uint32_t pt = 0, qt = 0;
+        for (uint32_t base = 0; base < deg; base += NT)
+        {
+            const uint32_t i = base + tid;
+            const bool valid = i < deg;
+            const float x = valid ? F[i] : 0.0f;
+            const bool sm = valid && x < ave, bg = valid && !(x < ave);
+            uint32_t rs, rq, ts, tq;
+            block_rank2(sm, bg, rs, rq, ts, tq, sa, sb);
+            if (sm)
+                P[pt + rs] = (uint16_t)i;
+            if (bg)
+                Q[qt + rq] = (uint16_t)i;
+            pt += ts;
+            qt += tq;
+            __syncthreads();
+        }
+        /* pairing (:603-630); bucket k is the k-th p pop */
+        Bucket *ob = out + e0;
+        const uint8_t *ty = g.type != nullptr ? g.type + e0 : nullptr;
+        uint32_t ph = 0, qh = 0;
+        while (ph < pt && qh < qt)
+        {
+            const uint32_t b = min(min(pt - ph, qt - qh), NT);
+            if (b <= 64)
+            {
+                /* warp 0 alone until the pairing ends or both queues are long again */
+                if (tid < 32)
+                {
+                    uint32_t wph = ph, wpt = pt, wqh = qh, wqt = qt;
+                    const uint32_t lt = (1u << lane) - 1u;
+                    while (wph < wpt && wqh < wqt)
+                    {
+                        const uint32_t wb = min(min(wpt - wph, wqt - wqh), 32u);
+                        if (wb == 32u && min(wpt - wph, wqt - wqh) > 128u)
+                            break;
+                        const bool act = lane < wb;
+                        bool conv = false;
+                        uint32_t qi = 0;
+                        if (act)
+                        {
+                            const uint32_t pi = P[wph + lane];
+                            qi = Q[wqh + lane];
+                            const float pv = F[pi], qv = F[qi];
+                            ob[wph + lane] = Bucket::make_n(fdiv(pv, ave), pi, qi, N[pi], N[qi], vcur, ty);
+                            const float r = fsub(qv, fsub(ave, pv));
+                            F[qi] = r;
+                            conv = r < ave;
+                        }
+                        const uint32_t mc = __ballot_sync(kFullMask, act && conv);
+                        const uint32_t ms = __ballot_sync(kFullMask, act && !conv);
+                        if (act)
+                        {
+                            if (conv)
+                                P[wpt + __popc(mc & lt)] = (uint16_t)qi;
+                            else
+                                Q[wqt + __popc(ms & lt)] = (uint16_t)qi;
+                        }
+                        __syncwarp();
+                        wph += wb;
+                        wqh += wb;
+                        wpt += __popc(mc);
+                        wqt += __popc(ms);
+                    }
+                    if (tid == 0)
+                    {
+                        s_row[0] = wph;
+                        s_row[1] = wpt;
+                        s_row[2] = wqh;
+                        s_row[3] = wqt;
+                    }
+                }
+                __syncthreads();
+                ph = s_row[0];
+                pt = s_row[1];
+                qh = s_row[2];
+                qt = s_row[3];
+                __syncthreads();
+                continue;
+            }
+            const bool act = tid < b;
+            bool conv = false;
+            uint32_t qi = 0;
+            if (act)
+            {
+                const uint32_t pi = P[ph + tid];
+                qi = Q[qh + tid];
+                const float pv = F[pi], qv = F[qi];
+                ob[ph + tid] = Bucket::make_n(fdiv(pv, ave), pi, qi, N[pi], N[qi], vcur, ty);
+                const float r = fsub(qv, fsub(ave, pv));
+                F[qi] = r;
+                conv = r < ave;
+            }
+            uint32_t rc, rs, tcn, tsn;
+            block_rank2(act && conv, act && !conv, rc, rs, tcn, tsn, sa, sb);
+            if (act)
+            {
+                if (conv)
+                    P[pt + rc] = (uint16_t)qi;
+                else
+                    Q[qt + rs] = (uint16_t)qi;
+            }
+            __syncthreads();
+            ph += b;
+            qh += b;
+            pt += tcn;
+            qt += tsn;
+        }
+        /* leftovers (:623-638): p entries with no q left, then q entries */
+        for (uint32_t i = tid; i < pt - ph; i += NT)
+        {
+            const uint32_t x = P[ph + i];
+            ob[ph + i] = Bucket::make_n(1.0f, x, kNone, N[x], 0, vcur, ty);
+        }
+        for (uint32_t i = tid; i < qt - qh; i += NT)
+        {
+            const uint32_t x = Q[qh + i];
+            ob[pt + i] = Bucket::make_n(1.0f, x, kNone, N[x], 0, vcur, ty);
+        }
+        __syncthreads();
     }
 }
 
@@ -818,30 +991,55 @@ __global__ void __launch_bounds__(256) alias_pair_kernel(GraphView g, TC tc, Buc
 template <typename TC, typename Bucket>
 __global__ void __launch_bounds__(1024) alias_build_hub_kernel(GraphView g, TC tc, Bucket *out, const uint64_t *vcur,
                                                                float *sum_out, uint2 *scratch, const uint32_t *order,
-                                                               uint32_t lo, uint32_t hi)
+                                                               uint32_t lo, uint32_t hi, uint32_t *next)
 {
-    __shared__ float chunk[1024];
+    __shared__ float chunk[2][1024];
     __shared__ uint32_t sa[33], sb[33], s_state[4];
     __shared__ float s_ave;
+    __shared__ uint32_t s_k;
     const uint32_t tid = threadIdx.x, nt = blockDim.x;
-    for (uint32_t k = lo + blockIdx.x; k < hi; k += gridDim.x)
+    for (;;)
     {
+        /* vertices from *next, largest first */
+        if (tid == 0)
+            s_k = lo + atomicAdd(next, 1u);
+        __syncthreads();
+        const uint32_t k = s_k;
+        __syncthreads();
+        if (k >= hi)
+            break;
         const uint32_t v = order[k];
         const int64_t e0 = g.off[v];
         const uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
+        /* the sum in edge order (:579-584) by thread 0, double-buffered: the
+         * block loads chunk c + 1 while thread 0 adds chunk c */
         float sum = 0.0f;
-        for (uint32_t base = 0; base < deg; base += nt)
+        if (tid < deg)
+            chunk[0][tid] = static_at(g, tc, v, e0 + tid);
+        __syncthreads();
+        for (uint32_t base = 0, c = 0; base < deg; base += nt, c ^= 1u)
         {
-            const uint32_t n = min(nt, deg - base);
-            if (tid < n)
-                chunk[tid] = static_at(g, tc, v, e0 + base + tid);
-            __syncthreads();
+            const uint32_t nx = base + nt + tid;
+            const bool more = nx < deg;
+            float x = 0.0f;
+            if (more)
+                x = static_at(g, tc, v, e0 + nx);
             if (tid == 0)
             {
-#pragma unroll 8
-                for (uint32_t j = 0; j < n; j++)
-                    sum = fadd(sum, chunk[j]);
+                const uint32_t n = min(nt, deg - base);
+                const float *cc = chunk[c];
+                uint32_t j = 0;
+                for (; j + 8 <= n; j += 8)
+                    sum = fadd(fadd(fadd(fadd(fadd(fadd(fadd(fadd(sum, cc[j]), cc[j + 1]), cc[j + 2]), cc[j + 3]),
+                                                   cc[j + 4]),
+                                              cc[j + 5]),
+                                         cc[j + 6]),
+                                    cc[j + 7]);
+                for (; j < n; j++)
+                    sum = fadd(sum, cc[j]);
             }
+            if (more)
+                chunk[c ^ 1u][tid] = x;
             __syncthreads();
         }
         if (tid == 0)
@@ -861,139 +1059,6 @@ __global__ void __launch_bounds__(1024) alias_build_hub_kernel(GraphView g, TC t
     }
 }
 
-/* Thread tiers: one thread per vertex of degree <= D runs the sequential
- * algorithm itself (sum, split, pairing, leftovers) on its row staged in
- * shared memory.
- *
- * Staging: the block's NT vertices (consecutive in the degree order, so of
- * similar degree) are loaded row by row by whole warps, coalesced: weights
- * (through static_comp) and neighbours.  Element i of thread j's row sits at
- * word i*NT + (j ^ (i & 31)): the warp writing 32 consecutive elements of one
- * row hits 32 banks, and each thread then reads its own row from shared
- * memory only.
- *
- * Queues: every pairing pops one entry from each queue and pushes at most one
- * back, so neither queue ever holds more entries than it started with: the p
- * queue is a ring over the first S0 slots of a deg-slot byte array and the q
- * queue a ring over the last B0 slots, counted from the end (S0 + B0 = deg).
- * Ring bytes of thread j are packed four to a word at (s/4)*NT + j. */
-template <uint32_t D, uint32_t NT>
-constexpr size_t alias_thread_smem()
-{
-    return (size_t)D * NT * 9 + (size_t)NT * 16;
-}
-
-template <typename TC, typename Bucket, uint32_t D, uint32_t NT>
-__global__ void __launch_bounds__(NT) alias_thread_kernel(GraphView g, TC tc, Bucket *out, const uint64_t *vcur,
-                                                          float *sum_out, const uint32_t *order, uint32_t lo,
-                                                          uint32_t hi)
-{
-    static_assert(D <= 256 && D % 4 == 0 && NT % 32 == 0, "ring slots are bytes, four per word");
-    extern __shared__ uint32_t smem[];
-    float *s_prob = reinterpret_cast<float *>(smem);
-    uint32_t *s_nb = smem + (size_t)D * NT;
-    int64_t *s_e0 = reinterpret_cast<int64_t *>(smem + (size_t)D * NT * 9 / 4);
-    uint32_t *s_deg = reinterpret_cast<uint32_t *>(s_e0 + NT);
-    uint32_t *s_v = s_deg + NT;
-    const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    uint8_t *ring = reinterpret_cast<uint8_t *>(smem + (size_t)2 * D * NT + t);
-    auto slot = [](uint32_t s) { return (s >> 2) * (NT * 4) + (s & 3); };
-    auto at = [](uint32_t i, uint32_t j) { return i * NT + (j ^ (i & 31)); };
-    for (uint32_t base = lo + blockIdx.x * NT; base < hi; base += gridDim.x * NT)
-    {
-        /* each thread fetches its own vertex's adjacency range, all in parallel */
-        uint32_t v = 0, deg = 0;
-        int64_t e0 = 0;
-        if (base + t < hi)
-        {
-            v = order[base + t];
-            e0 = g.off[v];
-            deg = (uint32_t)(g.off[v + 1] - e0);
-        }
-        __syncthreads(); /* the previous tile is done with the shared rows */
-        s_e0[t] = e0;
-        s_deg[t] = deg;
-        s_v[t] = v;
-        __syncthreads();
-        /* then whole warps copy the rows, several rows' loads in flight */
-#pragma unroll 4
-        for (uint32_t j = warp; j < NT; j += NT / 32)
-        {
-            const int64_t r0 = s_e0[j];
-            const uint32_t rd = s_deg[j], rv = s_v[j];
-            for (uint32_t i = lane; i < rd; i += 32)
-            {
-                s_prob[at(i, j)] = static_at(g, tc, rv, r0 + i);
-                s_nb[at(i, j)] = g.nbr[r0 + i];
-            }
-        }
-        __syncthreads();
-        if (base + t >= hi)
-            continue;
-        float sum = 0.0f;
-        uint32_t j = 0;
-        for (; j + 4 <= deg; j += 4)
-        {
-            const float a = s_prob[at(j, t)], b = s_prob[at(j + 1, t)];
-            const float c = s_prob[at(j + 2, t)], d = s_prob[at(j + 3, t)];
-            sum = fadd(fadd(fadd(fadd(sum, a), b), c), d);
-        }
-        for (; j < deg; j++)
-            sum = fadd(sum, s_prob[at(j, t)]);
-        if (sum_out != nullptr)
-            sum_out[v] = sum;
-        const float ave = fdiv(sum, u2f(deg));
-        /* split in edge order: p ring from the front, q ring from the back */
-        uint32_t S0 = 0, B0 = 0;
-        for (j = 0; j < deg; j++)
-        {
-            if (s_prob[at(j, t)] < ave)
-                ring[slot(S0++)] = (uint8_t)j;
-            else
-                ring[slot(deg - 1 - B0++)] = (uint8_t)j;
-        }
-        /* pairing; pt/qt are the push slots (ph + lp) mod S0 and (qh + lq) mod B0 */
-        uint32_t ph = 0, pt = 0, lp = S0, qh = 0, qt = 0, lq = B0, nb_out = 0;
-        Bucket *ob = out + e0;
-        const uint8_t *ty = g.type != nullptr ? g.type + e0 : nullptr;
-        while (lp != 0 && lq != 0)
-        {
-            const uint32_t pi = ring[slot(ph)], qi = ring[slot(deg - 1 - qh)];
-            ph = ph + 1 == S0 ? 0 : ph + 1;
-            qh = qh + 1 == B0 ? 0 : qh + 1;
-            const float pv = s_prob[at(pi, t)], qv = s_prob[at(qi, t)];
-            ob[nb_out++] = Bucket::make_n(fdiv(pv, ave), pi, qi, s_nb[at(pi, t)], s_nb[at(qi, t)], vcur, ty);
-            const float r = fsub(qv, fsub(ave, pv));
-            s_prob[at(qi, t)] = r;
-            if (r < ave)
-            {
-                ring[slot(pt)] = (uint8_t)qi;
-                pt = pt + 1 == S0 ? 0 : pt + 1;
-                lq--;
-            }
-            else
-            {
-                ring[slot(deg - 1 - qt)] = (uint8_t)qi;
-                qt = qt + 1 == B0 ? 0 : qt + 1;
-                lp--;
-            }
-        }
-        /* leftovers (:623-638): the rest of whichever queue is non-empty */
-        for (; lp != 0; lp--)
-        {
-            const uint32_t pi = ring[slot(ph)];
-            ob[nb_out++] = Bucket::make_n(1.0f, pi, kNone, s_nb[at(pi, t)], 0, vcur, ty);
-            ph = ph + 1 == S0 ? 0 : ph + 1;
-        }
-        for (; lq != 0; lq--)
-        {
-            const uint32_t qi = ring[slot(deg - 1 - qh)];
-            ob[nb_out++] = Bucket::make_n(1.0f, qi, kNone, s_nb[at(qi, t)], 0, vcur, ty);
-            qh = qh + 1 == B0 ? 0 : qh + 1;
-        }
-    }
-}
-
 /* Degree-descending vertex order support: degrees and iota for a radix sort. */
 static __global__ void degree_keys_kernel(GraphView g, uint32_t *deg, uint32_t *ids)
 {
@@ -1006,9 +1071,10 @@ static __global__ void degree_keys_kernel(GraphView g, uint32_t *deg, uint32_t *
 
 /* Tier boundaries in the descending degrees: bounds[i] = number of vertices
  * of degree > thr[i] (bounds zeroed by the caller). */
+constexpr int kTierBounds = kAliasClasses + 1; /* the class maxima, then 0 */
 struct TierThresholds
 {
-    uint32_t thr[5];
+    uint32_t thr[kTierBounds];
 };
 
 static __global__ void tier_bounds_kernel(const uint32_t *sorted_deg, uint32_t n, TierThresholds t, uint32_t *bounds)
@@ -1017,7 +1083,7 @@ static __global__ void tier_bounds_kernel(const uint32_t *sorted_deg, uint32_t n
     {
         const uint32_t d = sorted_deg[i], dn = i + 1 < n ? sorted_deg[i + 1] : 0;
 #pragma unroll
-        for (int k = 0; k < 5; k++)
+        for (int k = 0; k < kTierBounds; k++)
             if (d > t.thr[k] && dn <= t.thr[k])
                 bounds[k] = i + 1;
     }

@@ -40,7 +40,8 @@ void kk_engine::free_graph()
     vcur_valid = false;
     edge_set_valid = false;
     alias_cached = -1;
-    n_hub = n_staged = n_warp = n_t32 = n_nz = 0;
+    n_hub = n_nz = 0;
+    memset(tier, 0, sizeof(tier));
     vmask_valid = false;
 }
 
@@ -366,8 +367,6 @@ kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value)
             e->walk_block = (int)value;
         else if (n == "walk_stats" && (value == 0 || value == 1))
             e->walk_stats = (int)value;
-        else if (n == "alias_mid_tier" && (value == 0 || value == 1))
-            e->alias_mid_tier = (int)value;
         else if (n == "walk_multi" && (value == 1 || value == 2 || value == 4))
             e->walk_multi = (int)value;
         else

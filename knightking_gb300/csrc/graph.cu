@@ -165,7 +165,7 @@ const uint32_t *vertex_order(kk_engine *e)
     KK_CUDA_CHECK(cudaMalloc(&deg, (size_t)V * 4 + 4));
     KK_CUDA_CHECK(cudaMalloc(&deg_sorted, (size_t)V * 4 + 4));
     KK_CUDA_CHECK(cudaMalloc(&ids, (size_t)V * 4 + 4));
-    KK_CUDA_CHECK(cudaMalloc(&bounds, 32));
+    KK_CUDA_CHECK(cudaMalloc(&bounds, kTierBounds * sizeof(uint32_t)));
     uint32_t *order = e->order.as<uint32_t>(V);
     degree_keys_kernel<<<grid_for(e, V, 256), 256, 0, e->stream>>>(e->view(), deg, ids);
     KK_CUDA_CHECK(cudaGetLastError());
@@ -174,22 +174,21 @@ const uint32_t *vertex_order(kk_engine *e)
                                                             32, e->stream));
     KK_CUDA_CHECK(cub::DeviceRadixSort::SortPairsDescending(e->cub_tmp.ensure(bytes), bytes, deg, deg_sorted, ids,
                                                             order, (int64_t)V, 0, 32, e->stream));
-    KK_CUDA_CHECK(cudaMemsetAsync(bounds, 0, 32, e->stream));
-    const TierThresholds thr{{kAliasHubMin - 1, kAliasWarpQueue, kAliasThreadMax, kAliasThreadSmall, 0}};
+    KK_CUDA_CHECK(cudaMemsetAsync(bounds, 0, kTierBounds * sizeof(uint32_t), e->stream));
+    TierThresholds thr;
+    for (uint32_t k = 0; k < kAliasClasses; k++)
+        thr.thr[k] = kAliasClassMax[k];
+    thr.thr[kAliasClasses] = 0;
     tier_bounds_kernel<<<grid_for(e, V, 256), 256, 0, e->stream>>>(deg_sorted, V, thr, bounds);
     KK_CUDA_CHECK(cudaGetLastError());
-    uint32_t h[5];
-    KK_CUDA_CHECK(cudaMemcpyAsync(h, bounds, 20, cudaMemcpyDeviceToHost, e->stream));
+    KK_CUDA_CHECK(cudaMemcpyAsync(e->tier, bounds, kTierBounds * sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream));
     KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
     cudaFree(deg);
     cudaFree(deg_sorted);
     cudaFree(ids);
     cudaFree(bounds);
-    e->n_hub = h[0];
-    e->n_staged = h[1];
-    e->n_warp = h[2];
-    e->n_t32 = h[3];
-    e->n_nz = h[4];
+    e->n_hub = e->tier[0];
+    e->n_nz = e->tier[kAliasClasses];
     e->order_valid = true;
     return order;
 }

@@ -11,7 +11,6 @@ descent: each option in turn, the others held at their best so far).
 
 DEFAULT_SPACE = (
     ("alias_layout", (0, 1)),
-    ("alias_mid_tier", (0, 1)),
     ("node2vec_adjacency", (0, 1)),
     ("walk_block", (256, 128, 64)),
     ("walk_multi", (1, 2, 4)),
@@ -25,7 +24,7 @@ def space_for(app, weighted):
     alias tables, the adjacency test only for node2vec."""
     out = []
     for name, vals in DEFAULT_SPACE:
-        if name in ("alias_layout", "alias_mid_tier") and not weighted:
+        if name == "alias_layout" and not weighted:
             continue
         if name == "node2vec_adjacency" and app != "node2vec":
             continue

@@ -282,14 +282,17 @@ def test_alias_tables_match_oracle_rmat16(engine, oracle_lib, weights):
     _compare_alias(engine, oracle_lib, g["V"], g["off"], g["nbr"], g["w"])
 
 
-@pytest.mark.parametrize("mid_tier", [0, 1])
 @pytest.mark.parametrize("dist", ["lognormal", "pareto", "uniform", "equal", "twovalue"])
-def test_alias_tables_match_oracle_hubs(engine, oracle_lib, dist, mid_tier):
-    """Degrees 40000 (block kernel), 12000 / 5000 / 600 (warp kernel, rings in
-    the global scratch), 300 / 129 (warp kernel, rings in shared memory), 100
-    and 31 plus many small ones (thread tiers)."""
+def test_alias_tables_match_oracle_hubs(engine, oracle_lib, dist):
+    """Every build class and both sides of every class boundary: hubs (40000,
+    20000, 16385), 4097..16384 (block per vertex, queues in the scratch),
+    2049..4096 (block per vertex, shared memory), 1..2048 (lane groups of 32,
+    16, 8, 4 and 2), with rows of unequal degree side by side in a warp."""
     rng = np.random.default_rng(17)
-    degs = [40000, 12000, 5000, 600, 300, 129, 100, 31] + list(rng.integers(0, 40, size=2000))
+    degs = [40000, 20000, 16385, 16384, 12000, 5000, 4097, 4096, 3000, 2049, 2048, 1500, 1025, 1024, 600, 513, 512,
+            300, 129, 128, 100, 33, 32, 31, 17, 16, 7, 1]
+    degs += list(rng.integers(0, 40, size=2000)) + list(rng.integers(100, 600, size=60))
+    degs += list(rng.integers(900, 1100, size=20)) + list(rng.integers(2000, 4200, size=6))
     V = 60000
     degs = np.array(degs + [0] * (V - len(degs)), np.int64)
     off = np.zeros(V + 1, np.int64)
@@ -308,8 +311,4 @@ def test_alias_tables_match_oracle_hubs(engine, oracle_lib, dist, mid_tier):
         w = np.where(rng.random(E) < 0.9, 1.0, 50.0)
     w = w.astype(np.float32)
     engine.load_arrays(V, off, nbr, w)
-    engine.set_option("alias_mid_tier", mid_tier)
-    try:
-        _compare_alias(engine, oracle_lib, V, off, nbr, w)
-    finally:
-        engine.set_option("alias_mid_tier", 0)
+    _compare_alias(engine, oracle_lib, V, off, nbr, w)

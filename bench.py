@@ -237,6 +237,15 @@ def cpu_sample(g, wl, walkers, threads, seed, target_s=10.0, chunks=16):
     }
 
 
+def walk_kernel_name(app, best):
+    """The walk kernel the engine launches under the tuned options."""
+    if best.get("walk_schedule", 0) == 1:
+        return "walk_pool_kernel"
+    if best.get("walk_multi", 1) > 1 and app in ("deepwalk", "ppr"):
+        return "walk_multi_kernel<%d>" % best["walk_multi"]
+    return "walk_static_kernel"
+
+
 def run_reference(args, wl, world, rank, local):
     """The reference's CPU path (its C restatement, pinned to the reference) on all host cores."""
     if rank != 0:
@@ -497,7 +506,9 @@ def run_batch_bench(args, wl, world, rank, local):
     barrier(world)
     with ClockSampler(local) as clocks:
         time.sleep(0.5)
+        l0 = engine.launch_count()
         b_steps, b_ms = timed(batched, args.steps)
+        b_launches = engine.launch_count() - l0
         p_steps, p_ms = timed(plain, args.steps)
     b_ms = allreduce(world, b_ms, "max")
     p_ms = allreduce(world, p_ms, "max")
@@ -534,7 +545,7 @@ def run_batch_bench(args, wl, world, rank, local):
             "batched_over_plain": value / plain_value,
             "e2e": {"value": e2e_value, "unit": "walker-steps/s", "h2d_bytes_per_step": 64 * len(jobs),
                     "d2h_bytes_per_step": d2h // e2e_runs},
-            "gpu_launches": args.steps * (4 if wl["weights"] else 1),
+            "gpu_launches": b_launches,
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
         }
@@ -582,6 +593,7 @@ def run_ours(args, wl, world, rank, local):
     with ClockSampler(local) as clocks:
         time.sleep(0.5)  # nvidia-smi's first sample lands inside the timed region
         ev0.record(stream)
+        l0 = engine.launch_count()
         for _ in range(args.steps):
             total_steps += step()
             a, w = engine.last_timing()
@@ -589,6 +601,7 @@ def run_ours(args, wl, world, rank, local):
             walk_ms.append(w)
         ev1.record(stream)
         torch.cuda.synchronize()
+        launches = engine.launch_count() - l0
     elapsed_ms = ev0.elapsed_time(ev1)
     barrier(world)
     elapsed_ms = allreduce(world, elapsed_ms, "max")
@@ -664,8 +677,7 @@ def run_ours(args, wl, world, rank, local):
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_kind": peak_kind, "bytes_per_step": b_step,
                 "design_bytes_per_step": design_b, "access_counts": counts,
-                "kernel": ("walk_pool_kernel" if best_schedule == 1 else "walk_static_kernel") +
-                          (" (second order)" if app == "node2vec" else " (first order)"),
+                "kernel": walk_kernel_name(app, best) + (" (second order)" if app == "node2vec" else " (first order)"),
                 "kernel_ms": mean_walk_ms, "alias_build_ms": statistics.mean(alias_ms)}
 
     cpu = None
@@ -687,7 +699,7 @@ def run_ours(args, wl, world, rank, local):
                        "tuning_ms": [[cfg, ms] for cfg, ms in tune_table]},
             "e2e": {"value": e2e_value, "unit": "walker-steps/s", "h2d_bytes_per_step": walkers * 4 + 256,
                     "d2h_bytes_per_step": d2h // e2e_runs},
-            "gpu_launches": 2 * args.steps if wl["weights"] else args.steps,
+            "gpu_launches": launches,
             "roofline": roof,
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),

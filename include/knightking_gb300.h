@@ -113,7 +113,8 @@ kk_status kk_engine_set_stream(kk_engine *e, void *stream);
  *   "l2_fetch_bytes"     the context's cudaLimitMaxL2FetchGranularity while the engine
  *                        lives: 32, 64, 128, or 0 for the value found (restored on destroy)
  *   "walk_stats"         1 counts trials, queries and probes (kk_last_walk_stats)
- *   "walk_multi"         walkers per thread (1, 2, 4) of first-order walks without a dynamic component */
+ *   "walk_multi"         walkers per thread (1, 2, 4) of first-order walks without a dynamic component
+ *   "alias_hub_grid"     blocks of the hub alias kernel (0: one per SM) */
 kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value);
 /* Message of the last failed call on this engine ("" if none). */
 const char *kk_last_error(const kk_engine *e);
@@ -299,6 +300,11 @@ kk_status kk_last_walk_stats(const kk_engine *e, uint64_t *trials, uint64_t *que
 /* Milliseconds of the alias build and of the walk kernels of the last walk
  * call, from CUDA events on the engine's stream. */
 kk_status kk_last_walk_timing(const kk_engine *e, float *alias_ms, float *walk_ms);
+
+/* Kernels this library has launched on the engine's streams since the engine
+ * was created (alias builds, walks, batches, graph loading; the replays of a
+ * serving slot's captured CUDA graph are not counted). */
+kk_status kk_engine_launch_count(const kk_engine *e, uint64_t *count);
 
 void kk_paths_free(kk_paths *p);
 

@@ -13,6 +13,7 @@
 
 #include <string.h>
 
+#include <atomic>
 #include <functional>
 #include <mutex>
 #include <stdexcept>
@@ -248,10 +249,13 @@ struct kk_engine
      * classes: tier[k] = number of vertices of degree > kAliasClassMax[k]
      * (k < 8) and tier[8] = number of degree > 0, so [0, n_hub) are the hubs,
      * [tier[c - 1], tier[c]) class c, [n_nz, V) isolated */
-    kk::DevBuf order;
+    kk::DevBuf order, rows; /* rows: RowDesc of each position of the order */
     uint32_t tier[kk::kTierBounds] = {};
     uint32_t n_hub = 0, n_nz = 0;
     kk::DevBuf alias_next; /* the classes' work counters */
+    /* kernels this library has launched on the engine's streams (CUDA-graph
+     * replays not counted; kk_engine_launch_count) */
+    std::atomic<uint64_t> launches{0};
     bool order_valid = false;
     kk::DevBuf vcur; /* vertex cursors (begin | degree << 40), cached per graph */
     bool vcur_valid = false;
@@ -293,6 +297,9 @@ struct kk_engine
      * e->alias hold (0 cursor, 1 index), -1 none. */
     int alias_cache = 0;
     int alias_cached = -1;
+    /* alias_hub_grid (option): blocks of the hub alias kernel (0: one per SM);
+     * fewer leave more of the SMs to the classes on the main stream */
+    int alias_hub_grid = 0;
     /* l2_fetch_bytes (option): the context's cudaLimitMaxL2FetchGranularity
      * hint while the engine lives (0: left as found); the value found is put
      * back when the option returns to 0 and when the engine is destroyed. */
@@ -305,6 +312,9 @@ struct kk_engine
 
 namespace kk
 {
+
+/* One more kernel launched on the engine's streams (any host thread). */
+inline void count_launch(kk_engine *e) { e->launches.fetch_add(1, std::memory_order_relaxed); }
 
 /* Runs f, turning the exceptions inside the engine into a status and the
  * engine's last-error message (no exception crosses the C-ABI). */
@@ -431,7 +441,7 @@ inline apps::MetaSchemes make_schemes(const kk_walk_opts &o)
  * every SM (at most one per `per_block` vertices). */
 template <typename K>
 void launch_alias_class(kk_engine *e, K kern, unsigned nt, size_t smem, uint32_t per_block, uint32_t lo, uint32_t hi,
-                        int &resident, const std::function<void(unsigned)> &launch)
+                        int &resident, const std::function<void(unsigned)> &launch, int cap_per_sm = 0)
 {
     if (hi <= lo)
         return;
@@ -443,7 +453,8 @@ void launch_alias_class(kk_engine *e, K kern, unsigned nt, size_t smem, uint32_t
         if (resident < 1)
             resident = 1;
     }
-    const uint64_t want = (uint64_t)resident * (uint64_t)e->sm_count;
+    const int per_sm = cap_per_sm > 0 && cap_per_sm < resident ? cap_per_sm : resident;
+    const uint64_t want = (uint64_t)per_sm * (uint64_t)e->sm_count;
     const uint64_t need = ((uint64_t)(hi - lo) + per_block - 1) / per_block;
     launch((unsigned)(need < want ? need : want));
     KK_CUDA_CHECK(cudaGetLastError());
@@ -467,6 +478,7 @@ void build_alias(kk_engine *e, const TC &tc)
     Bucket *alias = e->alias.as<Bucket>(e->E);
     float *sum = e->sum.as<float>(e->V);
     const uint32_t *order = vertex_order(e);
+    const RowDesc *rows = (const RowDesc *)e->rows.p;
     const uint64_t *vcur = Bucket::cursor ? vertex_cursors(e) : nullptr;
     uint2 *scratch = e->scratch.as<uint2>(2 * e->E);
     uint32_t *next = e->alias_next.as<uint32_t>(16);
@@ -478,9 +490,11 @@ void build_alias(kk_engine *e, const TC &tc)
         /* hubs first, largest first, on the side stream so they start at once */
         KK_CUDA_CHECK(cudaEventRecord(e->ev_fork, e->stream));
         KK_CUDA_CHECK(cudaStreamWaitEvent(e->side, e->ev_fork, 0));
-        const unsigned grid = e->n_hub < (uint32_t)e->sm_count ? e->n_hub : (unsigned)e->sm_count;
+        const uint32_t cap = e->alias_hub_grid > 0 ? (uint32_t)e->alias_hub_grid : (uint32_t)e->sm_count;
+        const unsigned grid = e->n_hub < cap ? e->n_hub : cap;
         alias_build_hub_kernel<TC, Bucket><<<grid, 1024, 0, e->side>>>(g, tc, alias, vcur, sum, scratch, order, 0,
                                                                        e->n_hub, next);
+        count_launch(e);
         KK_CUDA_CHECK(cudaGetLastError());
         KK_CUDA_CHECK(cudaEventRecord(e->ev_join, e->side));
     }
@@ -490,6 +504,7 @@ void build_alias(kk_engine *e, const TC &tc)
         launch_alias_class(e, alias_build_hub_kernel<TC, Bucket>, 256, 0, 1, t[0], t[1], res, [&](unsigned grid) {
             alias_build_hub_kernel<TC, Bucket><<<grid, 256, 0, st>>>(g, tc, alias, vcur, sum, scratch, order, t[0],
                                                                      t[1], next + 1);
+            count_launch(e);
         });
     }
     /* 2049..4096: a block per vertex, the row in shared memory */
@@ -500,12 +515,14 @@ void build_alias(kk_engine *e, const TC &tc)
                            [&](unsigned grid) {
                                alias_block_row_kernel<TC, Bucket, 256, 4096>
                                    <<<grid, 256, smem, st>>>(g, tc, alias, vcur, sum, order, t[1], t[2], next + 2);
+                               count_launch(e);
                            });
     }
     /* 1..2048: lane groups, 32/G vertices per warp */
     auto group = [&](auto kern, uint32_t G, size_t smem, int c, int &res) {
         launch_alias_class(e, kern, 32, smem, 32 / G, t[c - 1], t[c], res, [&](unsigned grid) {
-            kern<<<grid, 32, smem, st>>>(g, tc, alias, vcur, sum, order, t[c - 1], t[c], next + c);
+            kern<<<grid, 32, smem, st>>>(g, tc, alias, vcur, sum, rows, t[c - 1], t[c], next + c);
+            count_launch(e);
         });
     };
     static int r3 = 0, r4 = 0, r5 = 0, r6 = 0, r7 = 0, r8 = 0;
@@ -547,6 +564,7 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
     {
         float *rap = e->ra.as<float>(e->V);
         regular_area_kernel<TC><<<grid_for(e, g.V, 256), 256, 0, e->stream>>>(g, tc, (const float *)e->sum.p, rap);
+        count_launch(e);
         KK_CUDA_CHECK(cudaGetLastError());
         ra = rap;
     }
@@ -576,6 +594,7 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
         KK_CUDA_CHECK(cudaMemsetAsync(caps + n, 0, sizeof(uint64_t), e->stream));
         constant_extension_bound_kernel<<<grid_for(e, (uint64_t)n * 32, 256), 256, 0, e->stream>>>(
             rs.seed, rs.walker_begin, n, rs.const_ext, 1u << 24, caps, d_status);
+        count_launch(e);
         KK_CUDA_CHECK(cudaGetLastError());
         exclusive_scan_u64(e, caps, off, (uint64_t)n + 1);
         KK_CUDA_CHECK(cudaMemcpyAsync(&total_cap, off + n, sizeof(uint64_t), cudaMemcpyDeviceToHost, e->stream));
@@ -598,6 +617,7 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
             else
                 walk_multi_kernel<S, WC, TC, Bucket, 4><<<grid_for(e, threads, bs), bs, 0, e->stream>>>(g, wc, tc,
                                                                                                        alias, L);
+            count_launch(e);
             goto launched;
         }
     }
@@ -605,6 +625,7 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
     {
         const unsigned bs = (unsigned)e->walk_block;
         walk_static_kernel<S, WC, TC, Bucket><<<grid_for(e, n, bs), bs, 0, e->stream>>>(g, wc, tc, alias, ra, L);
+        count_launch(e);
     }
     else
     {
@@ -617,6 +638,7 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
         uint64_t need = ((uint64_t)n + 255) / 256;
         unsigned grid = (unsigned)(want < need ? want : (need ? need : 1));
         walk_pool_kernel<S, WC, TC, Bucket><<<grid, 256, 0, e->stream>>>(g, wc, tc, alias, ra, L);
+        count_launch(e);
     }
 launched:
     KK_CUDA_CHECK(cudaGetLastError());

@@ -401,6 +401,16 @@ constexpr uint32_t kAliasClasses = 8;
 constexpr uint32_t kAliasClassMax[kAliasClasses] = {16384, 4096, 2048, 1024, 512, 128, 32, 16};
 constexpr unsigned kFullMask = 0xffffffffu;
 
+/* A vertex of the degree-descending order with its adjacency range, so an
+ * alias kernel reaches a row with one 16-byte load instead of order[] then
+ * off[] (two dependent round trips). */
+struct __align__(16) RowDesc
+{
+    int64_t e0;
+    uint32_t v;
+    uint32_t deg;
+};
+
 __device__ __forceinline__ uint32_t lanemask_lt()
 {
     uint32_t m;
@@ -630,10 +640,10 @@ constexpr size_t alias_group_smem_per_warp()
 
 template <typename TC, typename Bucket, uint32_t G, uint32_t DMAX>
 __global__ void __launch_bounds__(32) alias_group_kernel(GraphView g, TC tc, Bucket *out, const uint64_t *vcur,
-                                                         float *sum_out, const uint32_t *order, uint32_t lo,
+                                                         float *sum_out, const RowDesc *rows, uint32_t lo,
                                                          uint32_t hi, uint32_t *next)
 {
-    static_assert(G == 2 || G == 4 || G == 8 || G == 16 || G == 32, "group of 2, 4, 8, 16 or 32 lanes");
+    static_assert(G == 1 || G == 2 || G == 4 || G == 8 || G == 16 || G == 32, "group of 1 to 32 lanes");
     static_assert(DMAX % 4 == 0 && DMAX <= 65535, "16-bit queue entries");
     constexpr uint32_t RPW = 32 / G;
     constexpr uint32_t gbits = G == 32 ? kFullMask : (1u << G) - 1u;
@@ -644,24 +654,24 @@ __global__ void __launch_bounds__(32) alias_group_kernel(GraphView g, TC tc, Buc
     uint32_t *N = smem + (size_t)RPW * DMAX + (size_t)grp * DMAX;
     uint16_t *Qs = reinterpret_cast<uint16_t *>(smem + (size_t)2 * RPW * DMAX) + (size_t)grp * DMAX;
     /* every loop below runs to the warp's maximum with per-group predicates,
-     * so the groups stay converged and share each instruction */
-    for (;;)
+     * so the groups stay converged and share each instruction.  The next
+     * vertices' counter value and row descriptors are fetched while the
+     * current ones are processed. */
+    const uint32_t n = hi - lo;
+    uint32_t t = 0;
+    if (lane == 0)
+        t = atomicAdd(next, RPW);
+    t = __shfl_sync(kFullMask, t, 0);
+    RowDesc d{0, 0, 0};
+    if (t + grp < n)
+        d = rows[lo + t + grp];
+    while (t < n)
     {
-        uint32_t t = 0;
+        uint32_t tn = 0;
         if (lane == 0)
-            t = atomicAdd(next, RPW);
-        t = __shfl_sync(kFullMask, t, 0);
-        if (t >= hi - lo)
-            break;
-        const uint32_t k = lo + t + grp;
-        uint32_t v = 0, deg = 0;
-        int64_t e0 = 0;
-        if (k < hi)
-        {
-            v = order[k];
-            e0 = g.off[v];
-            deg = (uint32_t)(g.off[v + 1] - e0);
-        }
+            tn = atomicAdd(next, RPW);
+        const uint32_t v = d.v, deg = d.deg;
+        const int64_t e0 = d.e0;
         const uint32_t wdeg = __reduce_max_sync(kFullMask, deg);
         /* stage the rows: probabilities and neighbours, G consecutive edges per load */
 #pragma unroll 4
@@ -672,6 +682,10 @@ __global__ void __launch_bounds__(32) alias_group_kernel(GraphView g, TC tc, Buc
                 N[i] = g.nbr[e0 + i];
             }
         __syncwarp();
+        tn = __shfl_sync(kFullMask, tn, 0);
+        RowDesc dn{0, 0, 0};
+        if (tn + grp < n)
+            dn = rows[lo + tn + grp];
         /* the sum in edge order (:579-584), one lane per group */
         float sum = 0.0f;
         if constexpr (RPW == 1)
@@ -796,6 +810,8 @@ __global__ void __launch_bounds__(32) alias_group_kernel(GraphView g, TC tc, Buc
             }
         }
         __syncwarp();
+        t = tn;
+        d = dn;
     }
 }
 
@@ -1056,6 +1072,17 @@ __global__ void __launch_bounds__(1024) alias_build_hub_kernel(GraphView g, TC t
         block_split([&](uint32_t i) { return static_at(g, tc, v, e0 + i); }, deg, ave, P, Q, pt, qt, sa, sb);
         block_pairing(P, Q, pt, qt, ave, out + e0, g.nbr + e0, vcur, g.type != nullptr ? g.type + e0 : nullptr, sa,
                       sb, s_state);
+    }
+}
+
+/* Row descriptors of the vertex order. */
+static __global__ void row_desc_kernel(GraphView g, const uint32_t *order, RowDesc *rows)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < g.V; i += gridDim.x * blockDim.x)
+    {
+        const uint32_t v = order[i];
+        const int64_t e0 = g.off[v];
+        rows[i] = RowDesc{e0, v, (uint32_t)(g.off[v + 1] - e0)};
     }
 }
 

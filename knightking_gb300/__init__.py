@@ -315,6 +315,13 @@ class WalkEngine:
         self._check(self._lib.kk_last_walk_timing(self._h, ctypes.byref(a), ctypes.byref(w)))
         return a.value, w.value
 
+    def launch_count(self):
+        """Kernels the library has launched on this engine's streams so far
+        (captured CUDA-graph replays of a serving slot not counted)."""
+        c = ctypes.c_uint64()
+        self._check(self._lib.kk_engine_launch_count(self._h, ctypes.byref(c)))
+        return c.value
+
 
 # ---- the apps' entry points (src/apps/*.hpp) ----
 

@@ -116,6 +116,7 @@ void launch_batch_with(kk_engine *e, const App &app, const BatchPlan &plan, Batc
         walk_batch_kernel<typename App::S, App, Bucket><<<grid, bs, 0, slot.stream>>>(
             e->view(), app, d_jobs, nj, plan.total, alias, (const float *)e->sum.p, *path, length, steps, status,
             e->trial_limit, st, hdr);
+        count_launch(e);
     }
     else
     {
@@ -130,6 +131,7 @@ void launch_batch_with(kk_engine *e, const App &app, const BatchPlan &plan, Batc
         walk_batch_pool_kernel<typename App::S, App, Bucket><<<grid, bs, 0, slot.stream>>>(
             e->view(), app, d_jobs, nj, plan.total, alias, (const float *)e->sum.p, *path, length, steps, status,
             e->trial_limit, st, hdr);
+        count_launch(e);
     }
     KK_CUDA_CHECK(cudaGetLastError());
 }

@@ -176,11 +176,13 @@ uint64_t pack_paths(kk_engine *e, const WalkResult &r, uint64_t **d_off_out, uin
     uint64_t *lens64 = e->caps.as<uint64_t>((uint64_t)n + 1);
     uint64_t *off = e->packed_off.as<uint64_t>((uint64_t)n + 1);
     length_to_u64_kernel<<<grid_for(e, (uint64_t)n + 1, 256), 256, 0, e->stream>>>(r.length, lens64, n);
+    count_launch(e);
     exclusive_scan_u64(e, lens64, off, (uint64_t)n + 1);
     uint64_t total = r.total_steps + n;
     uint32_t *verts = e->packed.as<uint32_t>(total);
     compact_paths_kernel<<<grid_for(e, (uint64_t)n * 32, 256), 256, 0, e->stream>>>(n, r.length, r.path_off, r.cap,
                                                                                    r.path, off, verts);
+    count_launch(e);
     KK_CUDA_CHECK(cudaGetLastError());
     *d_off_out = off;
     *d_verts_out = verts;
@@ -319,6 +321,8 @@ void kk_engine_destroy(kk_engine *e)
     if (e->ev_join)
         cudaEventDestroy(e->ev_join);
     e->order.release();
+    e->rows.release();
+    e->alias_next.release();
     e->vcur.release();
     e->edge_set.release();
     e->edge_pos.release();
@@ -367,6 +371,8 @@ kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value)
             e->walk_block = (int)value;
         else if (n == "walk_stats" && (value == 0 || value == 1))
             e->walk_stats = (int)value;
+        else if (n == "alias_hub_grid" && value >= 0 && value <= 4096)
+            e->alias_hub_grid = (int)value;
         else if (n == "walk_multi" && (value == 1 || value == 2 || value == 4))
             e->walk_multi = (int)value;
         else
@@ -548,6 +554,7 @@ kk_status kk_alias_build(kk_engine *e, float *p, uint32_t *p_idx, uint32_t *q_id
         KK_CUDA_CHECK(cudaMalloc(&dqi, E * 4 + 4));
         cast_alias_kernel<<<grid_for(e, E, 256), 256, 0, e->stream>>>((const AliasBucket *)e->alias.p, E, dp, dpi,
                                                                       dqi);
+        count_launch(e);
         KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
         if (p)
             KK_CUDA_CHECK(cudaMemcpy(p, dp, E * 4, cudaMemcpyDeviceToHost));
@@ -723,6 +730,14 @@ kk_status kk_last_walk_stats(const kk_engine *e, uint64_t *trials, uint64_t *que
         *queries = e->last_stats[1];
     if (probes)
         *probes = e->last_stats[2];
+    return KK_OK;
+}
+
+kk_status kk_engine_launch_count(const kk_engine *e, uint64_t *count)
+{
+    if (!e || !count)
+        return KK_ERR_INVALID_CONFIG;
+    *count = e->launches.load(std::memory_order_relaxed);
     return KK_OK;
 }
 

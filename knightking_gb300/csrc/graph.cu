@@ -168,6 +168,7 @@ const uint32_t *vertex_order(kk_engine *e)
     KK_CUDA_CHECK(cudaMalloc(&bounds, kTierBounds * sizeof(uint32_t)));
     uint32_t *order = e->order.as<uint32_t>(V);
     degree_keys_kernel<<<grid_for(e, V, 256), 256, 0, e->stream>>>(e->view(), deg, ids);
+    count_launch(e);
     KK_CUDA_CHECK(cudaGetLastError());
     size_t bytes = 0;
     KK_CUDA_CHECK(cub::DeviceRadixSort::SortPairsDescending(nullptr, bytes, deg, deg_sorted, ids, order, (int64_t)V, 0,
@@ -180,6 +181,7 @@ const uint32_t *vertex_order(kk_engine *e)
         thr.thr[k] = kAliasClassMax[k];
     thr.thr[kAliasClasses] = 0;
     tier_bounds_kernel<<<grid_for(e, V, 256), 256, 0, e->stream>>>(deg_sorted, V, thr, bounds);
+    count_launch(e);
     KK_CUDA_CHECK(cudaGetLastError());
     KK_CUDA_CHECK(cudaMemcpyAsync(e->tier, bounds, kTierBounds * sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream));
     KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
@@ -189,6 +191,10 @@ const uint32_t *vertex_order(kk_engine *e)
     cudaFree(bounds);
     e->n_hub = e->tier[0];
     e->n_nz = e->tier[kAliasClasses];
+    RowDesc *rows = e->rows.as<RowDesc>(V > 0 ? V : 1);
+    row_desc_kernel<<<grid_for(e, V, 256), 256, 0, e->stream>>>(e->view(), order, rows);
+    count_launch(e);
+    KK_CUDA_CHECK(cudaGetLastError());
     e->order_valid = true;
     return order;
 }
@@ -201,6 +207,7 @@ const uint64_t *vertex_cursors(kk_engine *e)
         if (e->E >= kCursorMaxEdges)
             fail(KK_ERR_INVALID_CONFIG, "vertex cursors hold edge offsets below 2^40");
         vertex_cursor_kernel<<<grid_for(e, e->V, 256), 256, 0, e->stream>>>(e->view(), cur);
+        count_launch(e);
         KK_CUDA_CHECK(cudaGetLastError());
         e->vcur_valid = true;
     }
@@ -224,12 +231,14 @@ EdgeSetView node2vec_edge_set(kk_engine *e)
         {
             const unsigned grid = e->n_hub < 4u * e->sm_count ? e->n_hub : 4u * e->sm_count;
             edge_set_block_kernel<<<grid, 1024, 0, e->stream>>>(g, keys, pos, nb, order, 0, e->n_hub);
+            count_launch(e);
             KK_CUDA_CHECK(cudaGetLastError());
         }
         if (e->n_nz > e->n_hub)
         {
             edge_set_warp_kernel<<<grid_for(e, (uint64_t)(e->n_nz - e->n_hub) * 32, 256), 256, 0, e->stream>>>(
                 g, keys, pos, nb, order, e->n_hub, e->n_nz);
+            count_launch(e);
             KK_CUDA_CHECK(cudaGetLastError());
         }
         e->edge_set_nb = nb;
@@ -244,6 +253,7 @@ const uint8_t *metapath_vertex_masks(kk_engine *e)
     if (!e->vmask_valid)
     {
         apps::metapath_vertex_mask_kernel<<<grid_for(e, e->V, 256), 256, 0, e->stream>>>(e->view(), vmask);
+        count_launch(e);
         KK_CUDA_CHECK(cudaGetLastError());
         e->vmask_valid = true;
     }
@@ -255,6 +265,7 @@ void graph_check_sorted(kk_engine *e)
     int *flag = (int *)e->small.ensure(64);
     KK_CUDA_CHECK(cudaMemsetAsync(flag, 0, sizeof(int), e->stream));
     check_sorted_kernel<<<grid_for(e, e->V, 256), 256, 0, e->stream>>>(e->d_off, e->d_nbr, e->V, flag);
+    count_launch(e);
     KK_CUDA_CHECK(cudaGetLastError());
     int h = 0;
     KK_CUDA_CHECK(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
@@ -280,6 +291,7 @@ void graph_sort_adjacency(kk_engine *e)
     KK_CUDA_CHECK(cudaMalloc(&idx_in, E * 4 + 4));
     KK_CUDA_CHECK(cudaMalloc(&idx_out, E * 4 + 4));
     iota_u32_kernel<<<grid_for(e, E, 256), 256, 0, e->stream>>>(idx_in, E);
+    count_launch(e);
     size_t bytes = 0;
     KK_CUDA_CHECK(cub::DeviceSegmentedSort::StableSortPairs(nullptr, bytes, e->d_nbr, nbr_out, idx_in, idx_out,
                                                             (int64_t)E, (int64_t)e->V, e->d_off, e->d_off + 1,
@@ -292,6 +304,7 @@ void graph_sort_adjacency(kk_engine *e)
         float *w2 = nullptr;
         KK_CUDA_CHECK(cudaMalloc(&w2, E * 4 + 4));
         gather_kernel<float><<<grid_for(e, E, 256), 256, 0, e->stream>>>(e->d_w, idx_out, w2, E);
+        count_launch(e);
         KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
         cudaFree(e->d_w);
         e->d_w = w2;
@@ -301,6 +314,7 @@ void graph_sort_adjacency(kk_engine *e)
         uint8_t *t2 = nullptr;
         KK_CUDA_CHECK(cudaMalloc(&t2, E + 4));
         gather_kernel<uint8_t><<<grid_for(e, E, 256), 256, 0, e->stream>>>(e->d_type, idx_out, t2, E);
+        count_launch(e);
         KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
         cudaFree(e->d_type);
         e->d_type = t2;
@@ -400,6 +414,7 @@ void csr_from_edges(kk_engine *e, uint32_t V, uint64_t m, const uint32_t *h_src,
     uint32_t *d_idx = tmp.idx.as<uint32_t>(m), *d_perm = tmp.perm.as<uint32_t>(m);
     KK_CUDA_CHECK(cudaMemcpyAsync(d_src, h_src, m * 4, cudaMemcpyHostToDevice, e->stream));
     iota_u32_kernel<<<grid_for(e, m, 256), 256, 0, e->stream>>>(d_idx, m);
+    count_launch(e);
     KK_CUDA_CHECK(cudaGetLastError());
     int bits = 1;
     while (bits < 32 && ((uint64_t)1 << bits) < V)
@@ -413,6 +428,7 @@ void csr_from_edges(kk_engine *e, uint32_t V, uint64_t m, const uint32_t *h_src,
     unsigned long long *cnt = tmp.cnt.as<unsigned long long>((uint64_t)V + 1);
     KK_CUDA_CHECK(cudaMemsetAsync(cnt, 0, ((uint64_t)V + 1) * 8, e->stream));
     count_sources_kernel<<<grid_for(e, m, 256), 256, 0, e->stream>>>(d_src, m, cnt);
+    count_launch(e);
     KK_CUDA_CHECK(cudaGetLastError());
     KK_CUDA_CHECK(cudaMalloc(&e->d_off, ((uint64_t)V + 1) * sizeof(int64_t)));
     exclusive_scan_u64(e, (const uint64_t *)cnt, (uint64_t *)e->d_off, (uint64_t)V + 1);
@@ -421,12 +437,14 @@ void csr_from_edges(kk_engine *e, uint32_t V, uint64_t m, const uint32_t *h_src,
     uint32_t *d_in = tmp.in.as<uint32_t>(m);
     KK_CUDA_CHECK(cudaMemcpyAsync(d_in, h_dst, m * 4, cudaMemcpyHostToDevice, e->stream));
     permute_kernel<uint32_t><<<grid_for(e, m, 256), 256, 0, e->stream>>>(d_in, d_perm, e->d_nbr, m);
+    count_launch(e);
     KK_CUDA_CHECK(cudaGetLastError());
     if (h_w)
     {
         KK_CUDA_CHECK(cudaMalloc(&e->d_w, m * 4 + 4));
         KK_CUDA_CHECK(cudaMemcpyAsync(d_in, h_w, m * 4, cudaMemcpyHostToDevice, e->stream));
         permute_kernel<float><<<grid_for(e, m, 256), 256, 0, e->stream>>>((const float *)d_in, d_perm, e->d_w, m);
+        count_launch(e);
         KK_CUDA_CHECK(cudaGetLastError());
     }
     if (h_t)
@@ -435,6 +453,7 @@ void csr_from_edges(kk_engine *e, uint32_t V, uint64_t m, const uint32_t *h_src,
         KK_CUDA_CHECK(cudaMemcpyAsync(d_in, h_t, m, cudaMemcpyHostToDevice, e->stream));
         permute_kernel<uint8_t><<<grid_for(e, m, 256), 256, 0, e->stream>>>((const uint8_t *)d_in, d_perm, e->d_type,
                                                                             m);
+        count_launch(e);
         KK_CUDA_CHECK(cudaGetLastError());
     }
     KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
@@ -683,6 +702,7 @@ void graph_generate_rmat(kk_engine *e, uint32_t scale, uint32_t ef, double a, do
     KK_CUDA_CHECK(cudaMalloc(&k2, m * 8 + 8));
     KK_CUDA_CHECK(cudaMalloc(&d_count, 16));
     rmat_draw_kernel<<<grid_for(e, m, 256), 256, 0, e->stream>>>(m, scale, seed, t, k1);
+    count_launch(e);
     KK_CUDA_CHECK(cudaGetLastError());
     size_t bytes = 0;
     int end_bit = 64;
@@ -706,6 +726,7 @@ void graph_generate_rmat(kk_engine *e, uint32_t scale, uint32_t ef, double a, do
     KK_CUDA_CHECK(cudaMalloc(&mir, E * 8 + 8));
     KK_CUDA_CHECK(cudaMalloc(&mir_sorted, E * 8 + 8));
     rmat_mirror_kernel<<<grid_for(e, u, 256), 256, 0, e->stream>>>(k1, (uint64_t)u, mir);
+    count_launch(e);
     KK_CUDA_CHECK(cudaGetLastError());
     cudaFree(k1);
     cudaFree(k2);
@@ -724,8 +745,10 @@ void graph_generate_rmat(kk_engine *e, uint32_t scale, uint32_t ef, double a, do
     KK_CUDA_CHECK(cudaMemsetAsync(deg, 0, (size_t)V * 4, e->stream));
     rmat_csr_kernel<<<grid_for(e, E, 256), 256, 0, e->stream>>>(mir_sorted, E, e->d_nbr, deg, seed + 1000, e->d_w,
                                                                 weights, e->d_type, (uint32_t)types);
+    count_launch(e);
     KK_CUDA_CHECK(cudaGetLastError());
     deg_to_u64_kernel<<<grid_for(e, (uint64_t)V + 1, 256), 256, 0, e->stream>>>(deg, deg64, V);
+    count_launch(e);
     KK_CUDA_CHECK(cudaMalloc(&e->d_off, ((size_t)V + 1) * 8));
     exclusive_scan_u64(e, deg64, (uint64_t *)e->d_off, (uint64_t)V + 1);
     KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));

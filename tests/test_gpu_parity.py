@@ -282,8 +282,9 @@ def test_alias_tables_match_oracle_rmat16(engine, oracle_lib, weights):
     _compare_alias(engine, oracle_lib, g["V"], g["off"], g["nbr"], g["w"])
 
 
+@pytest.mark.parametrize("hub_grid", [0, 2])
 @pytest.mark.parametrize("dist", ["lognormal", "pareto", "uniform", "equal", "twovalue"])
-def test_alias_tables_match_oracle_hubs(engine, oracle_lib, dist):
+def test_alias_tables_match_oracle_hubs(engine, oracle_lib, dist, hub_grid):
     """Every build class and both sides of every class boundary: hubs (40000,
     20000, 16385), 4097..16384 (block per vertex, queues in the scratch),
     2049..4096 (block per vertex, shared memory), 1..2048 (lane groups of 32,
@@ -311,4 +312,8 @@ def test_alias_tables_match_oracle_hubs(engine, oracle_lib, dist):
         w = np.where(rng.random(E) < 0.9, 1.0, 50.0)
     w = w.astype(np.float32)
     engine.load_arrays(V, off, nbr, w)
-    _compare_alias(engine, oracle_lib, V, off, nbr, w)
+    engine.set_option("alias_hub_grid", hub_grid)
+    try:
+        _compare_alias(engine, oracle_lib, V, off, nbr, w)
+    finally:
+        engine.set_option("alias_hub_grid", 0)

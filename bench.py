@@ -423,6 +423,7 @@ def run_serve_bench(args, wl, world, rank, local):
     plain_value = p_steps / (p_ms / 1e3)
     rebuild_value = r_steps / (r_ms / 1e3)
     achieved = batched_value * b_step / 1e9
+    ceiling = engine.gather_ceiling(4 << 30)
     if rank == 0:
         line = {
             "metric": "walker-steps/s", "value": served_value, "unit": "walker-steps/s", "n_gpus": world,
@@ -456,7 +457,12 @@ def run_serve_bench(args, wl, world, rank, local):
                          "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
                          "bytes_per_step": b_step, "design_bytes_per_step": design_b,
                          "access_counts": {"trials_per_step": T, "queries_per_step": Q, "probes_per_step": P},
-                         "kernel": "walk_batch_kernel (second order), from the batched throughput"},
+                         "kernel": "walk_batch_kernel (second order), from the batched throughput",
+                         "gather": {"ceiling_reads_per_s": ceiling, "reads_per_step": T + Q,
+                                    "achieved_reads_per_s": batched_value * (T + Q),
+                                    "frac": batched_value * (T + Q) / ceiling,
+                                    "what": "alias buckets + edge-set sectors per step (batched throughput) vs "
+                                            "kk_gather_ceiling (4 GiB, this GPU, this run)"}},
             "cpu_baseline": None, "clocks": clocks.summary(),
         }
         print(json.dumps(line))
@@ -679,6 +685,30 @@ def run_ours(args, wl, world, rank, local):
                 "design_bytes_per_step": design_b, "access_counts": counts,
                 "kernel": walk_kernel_name(app, best) + (" (second order)" if app == "node2vec" else " (first order)"),
                 "kernel_ms": mean_walk_ms, "alias_build_ms": statistics.mean(alias_ms)}
+
+    # ---- the random-gather ceiling: dependent random 32 B reads per second
+    # over 4 GiB, measured on this GPU now; each step of these walks makes
+    # reads_per_step such reads into structures far larger than L2 ----
+    ceiling = engine.gather_ceiling(4 << 30)
+    if app == "deepwalk":
+        rps = 1.0  # one alias bucket (index or cursor layout); offsets of S22 sit in L2
+    elif app == "ppr":
+        rps = 1.0 if best.get("cursor_adjacency", 0) else 2.0  # cursor adjacency entry, or offsets + neighbour
+    elif counts is not None and app == "node2vec":
+        rps = counts["trials_per_step"] + counts["queries_per_step"]  # buckets + edge-set sectors
+    elif counts is not None:
+        rps = counts["trials_per_step"]  # buckets (edge types ride in them)
+    else:
+        rps = None
+    steps_per_s_kernel = steps_per_launch / (mean_walk_ms / 1e3)
+    gather = None
+    if rps is not None:
+        gather = {"ceiling_reads_per_s": ceiling, "reads_per_step": rps,
+                  "achieved_reads_per_s": steps_per_s_kernel * rps,
+                  "frac": steps_per_s_kernel * rps / ceiling, "kernel": roof["kernel"] if roof else None,
+                  "what": "walk kernel's dependent random reads vs kk_gather_ceiling (4 GiB, this GPU, this run)"}
+    if roof is not None:
+        roof["gather"] = gather
 
     cpu = None
     if rank == 0 and not args.no_cpu:

@@ -114,7 +114,9 @@ kk_status kk_engine_set_stream(kk_engine *e, void *stream);
  *                        lives: 32, 64, 128, or 0 for the value found (restored on destroy)
  *   "walk_stats"         1 counts trials, queries and probes (kk_last_walk_stats)
  *   "walk_multi"         walkers per thread (1, 2, 4) of first-order walks without a dynamic component
- *   "alias_hub_grid"     blocks of the hub alias kernel (0: one per SM) */
+ *   "alias_hub_grid"     blocks of the hub alias kernel (0: one per SM)
+ *   "cursor_adjacency"   1 uniform picks read a per-graph adjacency copy holding each neighbour's
+ *                        position (16 B/edge, built on first use): one dependent read per step */
 kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value);
 /* Message of the last failed call on this engine ("" if none). */
 const char *kk_last_error(const kk_engine *e);
@@ -300,6 +302,13 @@ kk_status kk_last_walk_stats(const kk_engine *e, uint64_t *trials, uint64_t *que
 /* Milliseconds of the alias build and of the walk kernels of the last walk
  * call, from CUDA events on the engine's stream. */
 kk_status kk_last_walk_timing(const kk_engine *e, float *alias_ms, float *walk_ms);
+
+/* The GPU's rate of dependent random 32-byte reads over a buffer of `bytes`
+ * (>= 64 MiB; above the L2 size it measures HBM): every thread follows
+ * chains of reads whose next address depends on the value read, as a walk
+ * step does.  The random-gather ceiling the walk kernels are compared with;
+ * allocates and frees `bytes` of device memory. */
+kk_status kk_gather_ceiling(kk_engine *e, uint64_t bytes, double *reads_per_s);
 
 /* Kernels this library has launched on the engine's streams since the engine
  * was created (alias builds, walks, batches, graph loading; the replays of a

@@ -33,6 +33,10 @@ struct GraphView
     const uint32_t *nbr;
     const float *w;
     const uint8_t *type;
+    /* cursor adjacency (optional): per edge {neighbour, 0, the neighbour's
+     * vertex cursor}, so a uniform pick yields the next vertex and where its
+     * adjacency lies in one 16 B read */
+    const uint4 *adjc = nullptr;
 };
 
 /* An edge as the hooks see it (AdjUnit, include/graph.hpp:49-61): its

@@ -259,6 +259,13 @@ struct kk_engine
     bool order_valid = false;
     kk::DevBuf vcur; /* vertex cursors (begin | degree << 40), cached per graph */
     bool vcur_valid = false;
+    /* cursor_adjacency (option): uniform picks read a per-graph copy of the
+     * adjacency holding each neighbour's cursor (16 B/edge), one dependent
+     * random read per step instead of the offsets then the neighbour */
+    int cursor_adjacency = 0;
+    kk::DevBuf adjc;
+    bool adjc_valid = false;
+    float adjc_ms = 0.0f; /* time of its last build */
     /* node2vec adjacency test: 0 edge set (built once per graph), 1 binary
      * search of the sorted adjacency (option node2vec_adjacency) */
     int n2v_adjacency = 0;
@@ -376,6 +383,8 @@ const uint32_t *vertex_order(kk_engine *e);
 
 /* Vertex cursors, cached per graph. */
 const uint64_t *vertex_cursors(kk_engine *e);
+/* The cursor adjacency of the loaded graph (built once per graph). */
+const uint4 *cursor_adjacency_of(kk_engine *e);
 
 /* The edge set the node2vec adjacency test reads (cached per graph), or an
  * empty view when the engine's node2vec_adjacency option asks for binary
@@ -548,6 +557,11 @@ template <typename S, typename WC, typename TC, typename Bucket>
 void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, WalkResult &res)
 {
     GraphView g = e->view();
+    if constexpr (!TC::has_static)
+    {
+        if (e->cursor_adjacency)
+            g.adjc = cursor_adjacency_of(e);
+    }
     uint32_t n = rs.walker_num;
     int *d_status = (int *)e->small.ensure(64);
     unsigned long long *d_steps = (unsigned long long *)((char *)d_status + 16);

@@ -259,6 +259,17 @@ static __global__ void vertex_cursor_kernel(GraphView g, uint64_t *cur)
         cur[v] = make_cursor(g.off[v], (uint32_t)(g.off[v + 1] - g.off[v]));
 }
 
+/* cursor adjacency: every edge's neighbour with that neighbour's cursor */
+static __global__ void adj_cursor_kernel(GraphView g, const uint64_t *cur, uint4 *adjc)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < g.E; e += (uint64_t)gridDim.x * blockDim.x)
+    {
+        const uint32_t n = g.nbr[e];
+        const uint64_t c = __ldg(cur + n);
+        adjc[e] = make_uint4(n, 0u, (uint32_t)c, (uint32_t)(c >> 32));
+    }
+}
+
 /* One alias bucket (AliasBucket, include/walk.hpp:52-57), in one of two 32 B
  * layouts (one DRAM sector each):
  *
@@ -1241,6 +1252,11 @@ __device__ __forceinline__ Cand pick_candidate(const GraphView &g, const Bucket 
     else
     {
         const uint32_t c = rng.gen(pos.deg);
+        if (g.adjc != nullptr)
+        {
+            const uint4 a = gather(g.adjc + pos.e0 + c);
+            return Cand{c, a.x, ((uint64_t)a.w << 32) | a.z, true, 0};
+        }
         return Cand{c, gather(g.nbr + pos.e0 + c), 0, false, 0};
     }
 }

@@ -315,6 +315,13 @@ class WalkEngine:
         self._check(self._lib.kk_last_walk_timing(self._h, ctypes.byref(a), ctypes.byref(w)))
         return a.value, w.value
 
+    def gather_ceiling(self, nbytes=4 << 30):
+        """Dependent random 32 B reads per second over an nbytes buffer (the
+        random-gather ceiling of this GPU)."""
+        r = ctypes.c_double()
+        self._check(self._lib.kk_gather_ceiling(self._h, ctypes.c_uint64(nbytes), ctypes.byref(r)))
+        return r.value
+
     def launch_count(self):
         """Kernels the library has launched on this engine's streams so far
         (captured CUDA-graph replays of a serving slot not counted)."""

@@ -105,6 +105,12 @@ void launch_batch_with(kk_engine *e, const App &app, const BatchPlan &plan, Batc
     *path = want_paths ? slot.path.as<uint32_t>(cap) : nullptr;
     if (!hdr)
         KK_CUDA_CHECK(cudaEventRecord(slot.ev[1], slot.stream));
+    GraphView gv = e->view();
+    if constexpr (!TC::has_static)
+    {
+        if (e->cursor_adjacency)
+            gv.adjc = !prepared ? cursor_adjacency_of(e) : e->adjc_valid ? (const uint4 *)e->adjc.p : nullptr;
+    }
     const unsigned bs = (unsigned)e->walk_block;
     const uint32_t nj = (uint32_t)plan.jobs.size();
     unsigned long long *st = e->walk_stats ? steps + 1 : nullptr;
@@ -114,7 +120,7 @@ void launch_batch_with(kk_engine *e, const App &app, const BatchPlan &plan, Batc
         if (hdr && grid > 64u * (unsigned)e->sm_count)
             grid = 64u * (unsigned)e->sm_count; /* grid-stride over whatever the header holds */
         walk_batch_kernel<typename App::S, App, Bucket><<<grid, bs, 0, slot.stream>>>(
-            e->view(), app, d_jobs, nj, plan.total, alias, (const float *)e->sum.p, *path, length, steps, status,
+            gv, app, d_jobs, nj, plan.total, alias, (const float *)e->sum.p, *path, length, steps, status,
             e->trial_limit, st, hdr);
         count_launch(e);
     }
@@ -129,7 +135,7 @@ void launch_batch_with(kk_engine *e, const App &app, const BatchPlan &plan, Batc
         const uint64_t need = ((uint64_t)walkers + bs - 1) / bs;
         const unsigned grid = (unsigned)(want < need ? want : (need ? need : 1));
         walk_batch_pool_kernel<typename App::S, App, Bucket><<<grid, bs, 0, slot.stream>>>(
-            e->view(), app, d_jobs, nj, plan.total, alias, (const float *)e->sum.p, *path, length, steps, status,
+            gv, app, d_jobs, nj, plan.total, alias, (const float *)e->sum.p, *path, length, steps, status,
             e->trial_limit, st, hdr);
         count_launch(e);
     }
@@ -228,6 +234,8 @@ void batch_prepare(kk_engine *e, const BatchPlan &plan)
     }
     if (plan.app == KK_APP_METAPATH)
         metapath_vertex_masks(e);
+    if (!plan.weighted && e->cursor_adjacency)
+        cursor_adjacency_of(e);
     if (plan.weighted)
     {
         if (plan.app == KK_APP_DEEPWALK)

@@ -39,6 +39,7 @@ void kk_engine::free_graph()
     order_valid = false;
     vcur_valid = false;
     edge_set_valid = false;
+    adjc_valid = false;
     alias_cached = -1;
     n_hub = n_nz = 0;
     memset(tier, 0, sizeof(tier));
@@ -82,6 +83,34 @@ __global__ void length_to_u64_kernel(const uint32_t *len, uint64_t *out, uint32_
 {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += gridDim.x * blockDim.x)
         out[i] = i < n ? len[i] : 0;
+}
+
+/* Gather-ceiling probe: every thread follows two dependent chains of random
+ * 32 B-aligned reads over n sectors (the access a walk step makes: the next
+ * address depends on the value read). */
+__device__ __forceinline__ uint64_t probe_mix(uint64_t x)
+{
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdULL;
+    x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ULL;
+    x ^= x >> 33;
+    return x;
+}
+
+__global__ void gather_probe_kernel(const uint4 *buf, uint64_t n, int iters, uint32_t *out)
+{
+    const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    uint64_t a = probe_mix(2 * tid) % n, b = probe_mix(2 * tid + 1) % n;
+    uint32_t acc = 0;
+    for (int it = 0; it < iters; it++)
+    {
+        const uint4 x = __ldg(buf + 2 * a), y = __ldg(buf + 2 * b);
+        acc ^= x.x ^ y.x;
+        a = probe_mix(a ^ x.x ^ (uint64_t)it) % n;
+        b = probe_mix(b ^ y.x ^ (uint64_t)it) % n;
+    }
+    out[tid] = acc;
 }
 
 __global__ void cast_alias_kernel(const AliasBucket *b, uint64_t n, float *p, uint32_t *pi, uint32_t *qi)
@@ -322,6 +351,7 @@ void kk_engine_destroy(kk_engine *e)
         cudaEventDestroy(e->ev_join);
     e->order.release();
     e->rows.release();
+    e->adjc.release();
     e->alias_next.release();
     e->vcur.release();
     e->edge_set.release();
@@ -371,6 +401,8 @@ kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value)
             e->walk_block = (int)value;
         else if (n == "walk_stats" && (value == 0 || value == 1))
             e->walk_stats = (int)value;
+        else if (n == "cursor_adjacency" && (value == 0 || value == 1))
+            e->cursor_adjacency = (int)value;
         else if (n == "alias_hub_grid" && value >= 0 && value <= 4096)
             e->alias_hub_grid = (int)value;
         else if (n == "walk_multi" && (value == 1 || value == 2 || value == 4))
@@ -731,6 +763,40 @@ kk_status kk_last_walk_stats(const kk_engine *e, uint64_t *trials, uint64_t *que
     if (probes)
         *probes = e->last_stats[2];
     return KK_OK;
+}
+
+kk_status kk_gather_ceiling(kk_engine *e, uint64_t bytes, double *reads_per_s)
+{
+    if (!e || !reads_per_s || bytes < (64ull << 20))
+        return KK_ERR_INVALID_CONFIG;
+    return kk::guard(e, [&] {
+        KK_CUDA_CHECK(cudaSetDevice(e->device));
+        const uint64_t n = bytes / 32;
+        const unsigned threads = 256, blocks = 4u * (unsigned)e->sm_count;
+        const int iters = 64;
+        uint4 *buf = nullptr;
+        uint32_t *out = nullptr;
+        KK_CUDA_CHECK(cudaMalloc(&buf, n * 32));
+        KK_CUDA_CHECK(cudaMalloc(&out, (size_t)blocks * threads * 4));
+        KK_CUDA_CHECK(cudaMemsetAsync(buf, 0x5a, n * 32, e->stream));
+        float best = 1e30f;
+        for (int r = 0; r < 4; r++)
+        {
+            KK_CUDA_CHECK(cudaEventRecord(e->ev[0], e->stream));
+            gather_probe_kernel<<<blocks, threads, 0, e->stream>>>(buf, n, iters, out);
+            count_launch(e);
+            KK_CUDA_CHECK(cudaGetLastError());
+            KK_CUDA_CHECK(cudaEventRecord(e->ev[1], e->stream));
+            KK_CUDA_CHECK(cudaEventSynchronize(e->ev[1]));
+            float ms = 0.0f;
+            KK_CUDA_CHECK(cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]));
+            if (r > 0 && ms < best)
+                best = ms;
+        }
+        cudaFree(buf);
+        cudaFree(out);
+        *reads_per_s = 2.0 * iters * (double)blocks * threads / (best / 1e3);
+    });
 }
 
 kk_status kk_engine_launch_count(const kk_engine *e, uint64_t *count)

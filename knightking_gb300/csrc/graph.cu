@@ -214,6 +214,24 @@ const uint64_t *vertex_cursors(kk_engine *e)
     return cur;
 }
 
+const uint4 *cursor_adjacency_of(kk_engine *e)
+{
+    if (!e->adjc_valid)
+    {
+        const uint64_t *cur = vertex_cursors(e);
+        uint4 *a = e->adjc.as<uint4>(e->E > 0 ? e->E : 1);
+        KK_CUDA_CHECK(cudaEventRecord(e->ev[0], e->stream));
+        adj_cursor_kernel<<<grid_for(e, e->E, 256), 256, 0, e->stream>>>(e->view(), cur, a);
+        count_launch(e);
+        KK_CUDA_CHECK(cudaGetLastError());
+        KK_CUDA_CHECK(cudaEventRecord(e->ev[1], e->stream));
+        KK_CUDA_CHECK(cudaEventSynchronize(e->ev[1]));
+        KK_CUDA_CHECK(cudaEventElapsedTime(&e->adjc_ms, e->ev[0], e->ev[1]));
+        e->adjc_valid = true;
+    }
+    return (const uint4 *)e->adjc.p;
+}
+
 EdgeSetView node2vec_edge_set(kk_engine *e)
 {
     if (e->n2v_adjacency != 0)
@@ -285,6 +303,7 @@ void graph_sort_adjacency(kk_engine *e)
         return;
     e->alias_cached = -1;      /* the tables follow the adjacency order */
     e->edge_set_valid = false; /* and so do the edge set's indices */
+    e->adjc_valid = false;     /* and the cursor adjacency */
     uint64_t E = e->E;
     uint32_t *nbr_out = nullptr, *idx_in = nullptr, *idx_out = nullptr;
     KK_CUDA_CHECK(cudaMalloc(&nbr_out, E * 4 + 4));

@@ -1,8 +1,9 @@
 """Autotuner of the engine's speed options.
 
 The options (kk_engine_set_option) never change a path, only how fast it is
-produced: alias-table layout, node2vec adjacency test, walk block size, the
-context's L2 fetch-granularity hint and the walk schedule.  The tuner runs a
+produced: alias-table layout, node2vec adjacency test, walk block size,
+walkers per thread, the context's L2 fetch-granularity hint, the walk schedule
+and the cursor adjacency of uniform walks.  The tuner runs a
 caller-supplied step (one walk call on the real workload) under candidate
 settings and keeps, option by option, the value with the shortest alias-build
 plus walk time as the engine's CUDA events measure it (greedy coordinate
@@ -16,6 +17,7 @@ DEFAULT_SPACE = (
     ("walk_multi", (1, 2, 4)),
     ("l2_fetch_bytes", (0, 64)),
     ("walk_schedule", (0, 1)),
+    ("cursor_adjacency", (0, 1)),
 )
 
 
@@ -29,6 +31,8 @@ def space_for(app, weighted):
         if name == "node2vec_adjacency" and app != "node2vec":
             continue
         if name == "walk_multi" and app not in ("deepwalk", "ppr"):
+            continue
+        if name == "cursor_adjacency" and weighted:
             continue
         out.append((name, vals))
     return tuple(out)

@@ -28,16 +28,24 @@ def _load(engine, seed, weighted, types=False):
 
 
 def _check(engine, app, jobs):
-    """Both batch schedules: one walker per thread and the persistent pool."""
+    """Both batch schedules (one walker per thread, the persistent pool) and
+    uniform picks with and without the cursor adjacency."""
     batch = engine.batch_walk(app, jobs)
     engine.set_option("walk_schedule", 1)
     try:
         pooled = engine.batch_walk(app, jobs)
     finally:
         engine.set_option("walk_schedule", 0)
-    for a, b in zip(batch, pooled):
+    engine.set_option("cursor_adjacency", 1)
+    try:
+        cursored = engine.batch_walk(app, jobs)
+    finally:
+        engine.set_option("cursor_adjacency", 0)
+    for a, b, c in zip(batch, pooled, cursored):
         np.testing.assert_array_equal(a.path_length, b.path_length)
         np.testing.assert_array_equal(a.vertices, b.vertices)
+        np.testing.assert_array_equal(a.path_length, c.path_length)
+        np.testing.assert_array_equal(a.vertices, c.vertices)
     assert len(batch) == len(jobs)
     for job, got in zip(jobs, batch):
         kw = dict(job)

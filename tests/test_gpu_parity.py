@@ -125,8 +125,9 @@ FRESH = [
 @pytest.mark.parametrize("seed,schedule,layout", [(7, 0, 0), (1234567890123, 1, 1), (99, 1, 0), (5, 0, 1)])
 def test_fresh_walks_match_oracle(engine, oracle_lib, i, seed, schedule, layout):
     """Both walk schedules (one walker per thread, persistent walker pool),
-    both alias-table layouts (cursor buckets where allowed, index buckets) and
-    both node2vec adjacency tests (edge set, binary search)."""
+    both alias-table layouts (cursor buckets where allowed, index buckets),
+    both node2vec adjacency tests (edge set, binary search) and uniform picks
+    with and without the cursor adjacency."""
     app, gkw, wkw = FRESH[i]
     g = G.random_undirected(500, 6000, seed=seed % 1000 + i, **gkw)
     csr = G.csr_file_order(500, g["src"], g["dst"], w=g.get("w"), type=g.get("type"))
@@ -136,12 +137,14 @@ def test_fresh_walks_match_oracle(engine, oracle_lib, i, seed, schedule, layout)
     engine.set_option("walk_schedule", schedule)
     engine.set_option("alias_layout", layout)
     engine.set_option("node2vec_adjacency", layout)
+    engine.set_option("cursor_adjacency", 1 - layout)
     try:
         ps = engine.walk(app, n, seed=seed, weighted=weighted, walker_begin=77, **wkw)
     finally:
         engine.set_option("walk_schedule", 0)
         engine.set_option("alias_layout", 0)
         engine.set_option("node2vec_adjacency", 0)
+        engine.set_option("cursor_adjacency", 0)
     ocsr = oracle_lib.CSR(500, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
     if app == "node2vec":
         ocsr = ocsr.sorted_copy()
@@ -169,6 +172,7 @@ def test_multi_walker_kernel_matches_oracle(engine, oracle_lib, i, multi):
     try:
         for layout in (0, 1):
             engine.set_option("alias_layout", layout)
+            engine.set_option("cursor_adjacency", layout)
             ps = engine.walk(app, n, seed=31, weighted=weighted, walker_begin=9, **wkw)
             np.testing.assert_array_equal(ps.path_length, lens)
             np.testing.assert_array_equal(ps.vertices, verts)
@@ -176,6 +180,7 @@ def test_multi_walker_kernel_matches_oracle(engine, oracle_lib, i, multi):
     finally:
         engine.set_option("walk_multi", 1)
         engine.set_option("alias_layout", 0)
+        engine.set_option("cursor_adjacency", 0)
 
 
 def test_ppr_start_list_matches_oracle(engine, oracle_lib):

@@ -679,7 +679,10 @@ def run_ours(args, wl, world, rank, local):
         tf = os.path.join(ROOT, "profiles", "traffic_%s.json" % args.workload)
         if os.path.exists(tf):
             with open(tf) as f:
-                traffic = json.load(f)["dram_bytes_per_step"] * steps_per_launch
+                per_kernel = json.load(f)["dram_bytes_per_step"]
+            # ncu's DRAM bytes per step of the kernel this run launched
+            b = per_kernel.get(walk_kernel_name(app, best)) if isinstance(per_kernel, dict) else per_kernel
+            traffic = b * steps_per_launch if b is not None else None
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_kind": peak_kind, "bytes_per_step": b_step,
                 "design_bytes_per_step": design_b, "access_counts": counts,

@@ -615,7 +615,10 @@ def run_ours(args, wl, world, rank, local):
     value = all_steps / (elapsed_ms / 1e3)
 
     # ---- e2e: public C-ABI call with host buffers and copies in the timed region ----
-    start = np.arange(walkers, dtype=np.uint32) % np.uint32(V)
+    # the start list lives in pinned host memory, as the step's inputs should
+    start_pin = torch.empty(walkers, dtype=torch.int32, pin_memory=True)
+    start = start_pin.numpy().view(np.uint32)
+    start[:] = np.arange(walkers, dtype=np.uint32) % np.uint32(V)
     cap_per = (wl.get("walk_length", 0) + 1) if "walk_length" in wl else 0
     if cap_per == 0:
         cap_vertices = int(total_steps // args.steps) + walkers + 1024

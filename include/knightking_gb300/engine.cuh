@@ -55,8 +55,12 @@ struct DevBuf
     {
         if (n > bytes)
         {
+            /* work in flight on any stream may still read the old buffer */
             if (p)
+            {
+                cudaDeviceSynchronize();
                 cudaFree(p);
+            }
             p = nullptr;
             bytes = 0;
             KK_CUDA_CHECK(cudaMalloc(&p, n));
@@ -253,6 +257,17 @@ struct kk_engine
     uint32_t tier[kk::kTierBounds] = {};
     uint32_t n_hub = 0, n_nz = 0;
     kk::DevBuf alias_next; /* the classes' work counters */
+    /* kk_walk_into in walker chunks (option into_chunks): chunk c + 1 walks
+     * into the other output set (walk_set) while chunk c is packed and copied
+     * to the caller's buffers on copy_stream */
+    int walk_set = 0;
+    int into_chunks = 4;
+    kk::DevBuf path_b, length_b, path_off_b, caps_b;
+    kk::DevBuf into_lens[2], into_off[2], into_offb[2], into_verts[2], into_cub[2];
+    cudaStream_t copy_stream = nullptr;
+    void *h_status = nullptr;      /* mapped pinned words for the walks' status and capacity reads */
+    void *d_status_host = nullptr; /* the device address of h_status */
+    cudaEvent_t ev_walked[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
     /* kernels this library has launched on the engine's streams (CUDA-graph
      * replays not counted; kk_engine_launch_count) */
     std::atomic<uint64_t> launches{0};
@@ -323,6 +338,10 @@ namespace kk
 /* One more kernel launched on the engine's streams (any host thread). */
 inline void count_launch(kk_engine *e) { e->launches.fetch_add(1, std::memory_order_relaxed); }
 
+/* n 32-bit words from src to the engine's mapped host words at word `at`,
+ * written by a kernel on the engine's stream (no copy engine involved). */
+void words_to_host(kk_engine *e, const uint32_t *src, int at, int n);
+
 /* Runs f, turning the exceptions inside the engine into a status and the
  * engine's last-error message (no exception crosses the C-ABI). */
 template <typename F>
@@ -377,6 +396,9 @@ inline unsigned grid_for(const kk_engine *e, uint64_t n, unsigned block)
 
 /* Exclusive scan of n+1 uint64 values in place-ish: out[i] = sum(in[0..i)). */
 void exclusive_scan_u64(kk_engine *e, const uint64_t *in, uint64_t *out, uint64_t n);
+/* The same on stream st with temporary storage tmp. */
+void exclusive_scan_u64(kk_engine *e, const uint64_t *in, uint64_t *out, uint64_t n, cudaStream_t st,
+                        kk::DevBuf &tmp);
 
 /* Vertices sorted by degree, descending, with the alias tiers (cached per graph). */
 const uint32_t *vertex_order(kk_engine *e);
@@ -593,7 +615,11 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
     L.status = d_status;
     L.trial_limit = e->trial_limit;
     L.stats = e->walk_stats ? (unsigned long long *)((char *)d_status + 24) : nullptr;
-    L.length = e->length.as<uint32_t>(n);
+    /* the walk's output set (two sets let a chunked kk_walk_into walk one
+     * chunk while the previous one is packed and copied out) */
+    kk::DevBuf &b_length = e->walk_set ? e->length_b : e->length, &b_caps = e->walk_set ? e->caps_b : e->caps;
+    kk::DevBuf &b_off = e->walk_set ? e->path_off_b : e->path_off, &b_path = e->walk_set ? e->path_b : e->path;
+    L.length = b_length.as<uint32_t>(n);
     uint64_t total_cap;
     if (rs.fixed_cap)
     {
@@ -603,20 +629,21 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
     }
     else
     {
-        uint64_t *caps = e->caps.as<uint64_t>((uint64_t)n + 1);
-        uint64_t *off = e->path_off.as<uint64_t>((uint64_t)n + 1);
+        uint64_t *caps = b_caps.as<uint64_t>((uint64_t)n + 1);
+        uint64_t *off = b_off.as<uint64_t>((uint64_t)n + 1);
         KK_CUDA_CHECK(cudaMemsetAsync(caps + n, 0, sizeof(uint64_t), e->stream));
         constant_extension_bound_kernel<<<grid_for(e, (uint64_t)n * 32, 256), 256, 0, e->stream>>>(
             rs.seed, rs.walker_begin, n, rs.const_ext, 1u << 24, caps, d_status);
         count_launch(e);
         KK_CUDA_CHECK(cudaGetLastError());
         exclusive_scan_u64(e, caps, off, (uint64_t)n + 1);
-        KK_CUDA_CHECK(cudaMemcpyAsync(&total_cap, off + n, sizeof(uint64_t), cudaMemcpyDeviceToHost, e->stream));
+        words_to_host(e, (const uint32_t *)(off + n), 32, 2); /* host words 32, 33 of the 64 */
         KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+        total_cap = ((volatile uint64_t *)e->h_status)[16];
         L.path_off = off;
         L.cap = 0;
     }
-    L.path = rs.want_paths ? e->path.as<uint32_t>(total_cap) : nullptr;
+    L.path = rs.want_paths ? b_path.as<uint32_t>(total_cap) : nullptr;
     KK_CUDA_CHECK(cudaEventRecord(e->ev[1], e->stream));
     if constexpr (TC::order == 1 && !TC::has_dynamic)
     {
@@ -657,9 +684,10 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
 launched:
     KK_CUDA_CHECK(cudaGetLastError());
     KK_CUDA_CHECK(cudaEventRecord(e->ev[2], e->stream));
-    int h_small[16];
-    KK_CUDA_CHECK(cudaMemcpyAsync(h_small, d_status, sizeof(h_small), cudaMemcpyDeviceToHost, e->stream));
+    words_to_host(e, (const uint32_t *)d_status, 0, 16);
     KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+    int h_small[16];
+    memcpy(h_small, e->h_status, sizeof(h_small));
     memcpy(e->last_stats, (char *)h_small + 24, sizeof(e->last_stats));
     KK_CUDA_CHECK(cudaEventElapsedTime(&e->alias_ms, e->ev[0], e->ev[1]));
     KK_CUDA_CHECK(cudaEventElapsedTime(&e->walk_ms, e->ev[1], e->ev[2]));
@@ -667,6 +695,8 @@ launched:
         fail(KK_ERR_TRIAL_LIMIT, "a walker exceeded the rejection-trial limit");
     if (h_small[0] == KK_STATUS_PATH_CAPACITY)
         fail(KK_ERR_PATH_CAPACITY, "a walk exceeded its path capacity");
+    if (h_small[0] == KK_STATUS_BAD_START)
+        fail(KK_ERR_INVALID_CONFIG, "start vertex >= v_num");
     unsigned long long steps;
     memcpy(&steps, (char *)h_small + 16, sizeof(steps));
     res.walker_num = n;

@@ -1148,6 +1148,7 @@ __global__ void regular_area_kernel(GraphView g, TC tc, const float *sum, float 
 #define KK_STATUS_OK 0
 #define KK_STATUS_TRIAL_LIMIT 4
 #define KK_STATUS_PATH_CAPACITY 8
+#define KK_STATUS_BAD_START 16
 
 struct WalkLaunch
 {
@@ -1184,6 +1185,13 @@ __device__ __forceinline__ vertex_id_t walker_start(const GraphView &g, const WC
     else
     {
         v = w.id % g.V;
+    }
+    if (v >= g.V)
+    {
+        /* a start vertex outside the graph fails the call (the host reads
+         * the status); the walker stands on vertex 0 meanwhile */
+        atomicExch(L.status, KK_STATUS_BAD_START);
+        v = 0;
     }
     if constexpr (is_hook<decltype(wc.walker_init_state)>())
     {

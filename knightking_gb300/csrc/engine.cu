@@ -85,6 +85,20 @@ __global__ void length_to_u64_kernel(const uint32_t *len, uint64_t *out, uint32_
         out[i] = i < n ? len[i] : 0;
 }
 
+__global__ void words_to_host_kernel(const uint32_t *src, volatile uint32_t *dst, int n)
+{
+    if (threadIdx.x < (unsigned)n)
+        dst[threadIdx.x] = src[threadIdx.x];
+}
+
+/* Host-side path offsets of a chunk: its packed offsets plus the chunk's base
+ * in the caller's vertex buffer, or i * cap + base when no packing was needed. */
+__global__ void offsets_plus_base_kernel(const uint64_t *off, uint32_t cap, uint64_t base, uint32_t n, uint64_t *out)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = (off ? off[i] : (uint64_t)i * cap) + base;
+}
+
 /* Gather-ceiling probe: every thread follows two dependent chains of random
  * 32 B-aligned reads over n sectors (the access a walk step makes: the next
  * address depends on the value read). */
@@ -174,9 +188,7 @@ const uint32_t *upload_start(kk_engine *e, const kk_walk_opts *o)
 {
     if (o->start == nullptr)
         return nullptr;
-    for (uint32_t i = 0; i < o->n_start; i++)
-        if (o->start[i] >= e->V)
-            fail(KK_ERR_INVALID_CONFIG, "start vertex >= v_num");
+    /* the walk kernels check the vertices (KK_STATUS_BAD_START) */
     uint32_t *d = e->start.as<uint32_t>(o->n_start);
     KK_CUDA_CHECK(cudaMemcpyAsync(d, o->start, (size_t)o->n_start * 4, cudaMemcpyHostToDevice, e->stream));
     return d;
@@ -216,6 +228,126 @@ uint64_t pack_paths(kk_engine *e, const WalkResult &r, uint64_t **d_off_out, uin
     *d_off_out = off;
     *d_verts_out = verts;
     return total;
+}
+
+/* Packs a walk's paths on stream st into output set s for the host copy:
+ * *verts the packed vertices, *offb the per-walker offsets plus base.  A
+ * fixed-capacity walk whose walkers all used their whole capacity is already
+ * packed and is copied from where the walk wrote it. */
+uint64_t pack_paths_on(kk_engine *e, const WalkResult &r, cudaStream_t st, int s, uint64_t base,
+                       const uint64_t **offb, const uint32_t **verts)
+{
+    const uint32_t n = r.walker_num;
+    const uint64_t total = r.total_steps + n;
+    uint64_t *ob = e->into_offb[s].as<uint64_t>((uint64_t)n + 1);
+    if (r.path_off == nullptr && total == (uint64_t)n * r.cap)
+    {
+        offsets_plus_base_kernel<<<grid_for(e, n, 256), 256, 0, st>>>(nullptr, r.cap, base, n, ob);
+        count_launch(e);
+        KK_CUDA_CHECK(cudaGetLastError());
+        *offb = ob;
+        *verts = r.path;
+        return total;
+    }
+    uint64_t *lens64 = e->into_lens[s].as<uint64_t>((uint64_t)n + 1);
+    uint64_t *off = e->into_off[s].as<uint64_t>((uint64_t)n + 1);
+    length_to_u64_kernel<<<grid_for(e, (uint64_t)n + 1, 256), 256, 0, st>>>(r.length, lens64, n);
+    count_launch(e);
+    exclusive_scan_u64(e, lens64, off, (uint64_t)n + 1, st, e->into_cub[s]);
+    uint32_t *vv = e->into_verts[s].as<uint32_t>(total);
+    compact_paths_kernel<<<grid_for(e, (uint64_t)n * 32, 256), 256, 0, st>>>(n, r.length, r.path_off, r.cap, r.path,
+                                                                            off, vv);
+    count_launch(e);
+    offsets_plus_base_kernel<<<grid_for(e, n, 256), 256, 0, st>>>(off, 0, base, n, ob);
+    count_launch(e);
+    KK_CUDA_CHECK(cudaGetLastError());
+    *offb = ob;
+    *verts = vv;
+    return total;
+}
+
+/* kk_walk_into for the built-in apps: the walkers of each epoch in chunks
+ * (the into_chunks option; chunks of at least kIntoMinChunk walkers).  Chunk
+ * c + 1 walks into the other output set while chunk c's lengths, packed
+ * offsets and vertices go to the caller's buffers on the copy stream.  The
+ * alias tables are built once per call, by the first chunk (the same tables
+ * every chunk would build), unless the alias_cache option keeps them across
+ * calls anyway. */
+constexpr uint32_t kIntoMinChunk = 1u << 18;
+
+uint64_t walk_into_chunked(kk_engine *e, const kk_walk_opts *o, uint32_t *h_length, uint64_t *h_offset,
+                           uint32_t *h_vertices, uint64_t capacity)
+{
+    validate_opts(e, o, true);
+    const uint32_t *d_start = upload_start(e, o);
+    if (e->copy_stream == nullptr)
+    {
+        /* the highest priority: a chunk's packing kernels start as soon as its
+         * walk ends, not after the next chunk's walk blocks are all issued */
+        int lo = 0, hi = 0;
+        KK_CUDA_CHECK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        KK_CUDA_CHECK(cudaStreamCreateWithPriority(&e->copy_stream, cudaStreamNonBlocking, hi));
+        for (int i = 0; i < 2; i++)
+        {
+            KK_CUDA_CHECK(cudaEventCreateWithFlags(&e->ev_walked[i], cudaEventDisableTiming));
+            KK_CUDA_CHECK(cudaEventCreateWithFlags(&e->ev_copied[i], cudaEventDisableTiming));
+        }
+    }
+    const int user_cache = e->alias_cache;
+    struct Restore
+    {
+        kk_engine *e;
+        int cache;
+        ~Restore()
+        {
+            e->alias_cache = cache;
+            e->walk_set = 0;
+            cudaStreamSynchronize(e->copy_stream);
+        }
+    } restore{e, user_cache};
+    if (!user_cache)
+        e->alias_cached = -1; /* this call builds its own tables */
+    const uint32_t per = epoch_walkers(o);
+    uint64_t base = 0, steps = 0;
+    uint32_t done = 0, chunk = 0;
+    while (done < o->walker_num)
+    {
+        const uint32_t epoch_n = o->walker_num - done < per ? o->walker_num - done : per;
+        uint32_t nch = e->into_chunks > 1 ? (uint32_t)e->into_chunks : 1u;
+        if (nch > epoch_n / kIntoMinChunk)
+            nch = epoch_n / kIntoMinChunk > 1 ? epoch_n / kIntoMinChunk : 1u;
+        for (uint32_t k = 0; k < nch; k++, chunk++)
+        {
+            const uint32_t cb = done + (uint32_t)((uint64_t)epoch_n * k / nch);
+            const uint32_t ce = done + (uint32_t)((uint64_t)epoch_n * (k + 1) / nch);
+            const uint32_t num = ce - cb;
+            const int s = (int)(chunk & 1u);
+            /* the set's previous chunk must be out before this walk overwrites it */
+            KK_CUDA_CHECK(cudaStreamWaitEvent(e->stream, e->ev_copied[s], 0));
+            e->walk_set = s;
+            WalkResult r;
+            run_epoch(e, o, d_start, o->walker_begin + cb, num, true, r);
+            e->alias_cache = 1;
+            steps += r.total_steps;
+            const uint64_t total = r.total_steps + num;
+            if (base + total > capacity)
+                fail(KK_ERR_PATH_CAPACITY, "vertices buffer too small");
+            KK_CUDA_CHECK(cudaEventRecord(e->ev_walked[s], e->stream));
+            cudaStream_t cs = e->copy_stream;
+            KK_CUDA_CHECK(cudaStreamWaitEvent(cs, e->ev_walked[s], 0));
+            const uint64_t *offb;
+            const uint32_t *verts;
+            pack_paths_on(e, r, cs, s, base, &offb, &verts);
+            KK_CUDA_CHECK(cudaMemcpyAsync(h_length + cb, r.length, (size_t)num * 4, cudaMemcpyDeviceToHost, cs));
+            KK_CUDA_CHECK(cudaMemcpyAsync(h_offset + cb, offb, (size_t)num * 8, cudaMemcpyDeviceToHost, cs));
+            KK_CUDA_CHECK(cudaMemcpyAsync(h_vertices + base, verts, total * 4, cudaMemcpyDeviceToHost, cs));
+            KK_CUDA_CHECK(cudaEventRecord(e->ev_copied[s], cs));
+            base += total;
+        }
+        done += epoch_n;
+    }
+    KK_CUDA_CHECK(cudaStreamSynchronize(e->copy_stream));
+    return steps;
 }
 
 /* Runs all epochs; sink(epoch_begin, n, d_len, d_off, d_verts, total_vertices)
@@ -259,6 +391,13 @@ uint64_t walk_epochs(kk_engine *e, const kk_walk_opts *o, const EpochRunner *cus
 }
 
 } // namespace
+
+void words_to_host(kk_engine *e, const uint32_t *src, int at, int n)
+{
+    words_to_host_kernel<<<1, 32, 0, e->stream>>>(src, (volatile uint32_t *)e->d_status_host + at, n);
+    count_launch(e);
+    KK_CUDA_CHECK(cudaGetLastError());
+}
 
 uint64_t pack_walk_paths(kk_engine *e, const WalkResult &r, uint64_t **d_off, uint32_t **d_verts)
 {
@@ -317,9 +456,16 @@ kk_status kk_engine_create(kk_engine **out, int device)
             KK_CUDA_CHECK(cudaEventCreate(&e->ev[i]));
         KK_CUDA_CHECK(cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming));
         KK_CUDA_CHECK(cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming));
+        /* mapped pinned words the walks' status and capacity reads land in:
+         * a kernel writes them (kk::words_to_host), so the host read waits on
+         * the engine's stream only, never on copies queued on other streams */
+        KK_CUDA_CHECK(cudaHostAlloc(&e->h_status, 256, cudaHostAllocMapped));
+        KK_CUDA_CHECK(cudaHostGetDevicePointer(&e->d_status_host, e->h_status, 0));
     });
     if (s != KK_OK)
     {
+        if (e->h_status)
+            cudaFreeHost(e->h_status);
         delete e;
         return s;
     }
@@ -352,6 +498,29 @@ void kk_engine_destroy(kk_engine *e)
     e->order.release();
     e->rows.release();
     e->adjc.release();
+    if (e->h_status)
+        cudaFreeHost(e->h_status);
+    if (e->copy_stream)
+    {
+        cudaStreamSynchronize(e->copy_stream);
+        cudaStreamDestroy(e->copy_stream);
+        for (int i = 0; i < 2; i++)
+        {
+            cudaEventDestroy(e->ev_walked[i]);
+            cudaEventDestroy(e->ev_copied[i]);
+        }
+    }
+    kk::DevBuf *into_bufs[] = {&e->path_b, &e->length_b, &e->path_off_b, &e->caps_b};
+    for (kk::DevBuf *b : into_bufs)
+        b->release();
+    for (int i = 0; i < 2; i++)
+    {
+        e->into_lens[i].release();
+        e->into_off[i].release();
+        e->into_offb[i].release();
+        e->into_verts[i].release();
+        e->into_cub[i].release();
+    }
     e->alias_next.release();
     e->vcur.release();
     e->edge_set.release();
@@ -401,6 +570,8 @@ kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value)
             e->walk_block = (int)value;
         else if (n == "walk_stats" && (value == 0 || value == 1))
             e->walk_stats = (int)value;
+        else if (n == "into_chunks" && value >= 1 && value <= 64)
+            e->into_chunks = (int)value;
         else if (n == "cursor_adjacency" && (value == 0 || value == 1))
             e->cursor_adjacency = (int)value;
         else if (n == "alias_hub_grid" && value >= 0 && value <= 4096)
@@ -703,20 +874,7 @@ kk_status kk_walk_into(kk_engine *e, const kk_walk_opts *opts, uint32_t *h_lengt
     if (!e || !h_length || !h_offset || !h_vertices)
         return KK_ERR_INVALID_CONFIG;
     return guard(e, [&] {
-        uint64_t base = 0;
-        uint64_t steps = walk_epochs(e, opts, nullptr, [&](uint32_t done, uint32_t num, const uint32_t *d_len,
-                                                  const uint64_t *d_off, const uint32_t *d_verts, uint64_t total) {
-            if (base + total > vertices_capacity)
-                fail(KK_ERR_PATH_CAPACITY, "vertices buffer too small");
-            KK_CUDA_CHECK(cudaMemcpyAsync(h_length + done, d_len, (size_t)num * 4, cudaMemcpyDeviceToHost, e->stream));
-            KK_CUDA_CHECK(cudaMemcpyAsync(h_offset + done, d_off, (size_t)num * 8, cudaMemcpyDeviceToHost, e->stream));
-            KK_CUDA_CHECK(cudaMemcpyAsync(h_vertices + base, d_verts, total * 4, cudaMemcpyDeviceToHost, e->stream));
-            KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
-            if (base != 0)
-                for (uint32_t i = 0; i < num; i++)
-                    h_offset[done + i] += base;
-            base += total;
-        });
+        const uint64_t steps = walk_into_chunked(e, opts, h_length, h_offset, h_vertices, vertices_capacity);
         if (total_steps)
             *total_steps = steps;
     });

@@ -31,12 +31,17 @@
 namespace kk
 {
 
-void exclusive_scan_u64(kk_engine *e, const uint64_t *in, uint64_t *out, uint64_t n)
+void exclusive_scan_u64(kk_engine *e, const uint64_t *in, uint64_t *out, uint64_t n, cudaStream_t st, DevBuf &tmpb)
 {
     size_t bytes = 0;
-    KK_CUDA_CHECK(cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, out, (int64_t)n, e->stream));
-    void *tmp = e->cub_tmp.ensure(bytes);
-    KK_CUDA_CHECK(cub::DeviceScan::ExclusiveSum(tmp, bytes, in, out, (int64_t)n, e->stream));
+    KK_CUDA_CHECK(cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, out, (int64_t)n, st));
+    void *tmp = tmpb.ensure(bytes);
+    KK_CUDA_CHECK(cub::DeviceScan::ExclusiveSum(tmp, bytes, in, out, (int64_t)n, st));
+}
+
+void exclusive_scan_u64(kk_engine *e, const uint64_t *in, uint64_t *out, uint64_t n)
+{
+    exclusive_scan_u64(e, in, out, n, e->stream, e->cub_tmp);
 }
 
 namespace

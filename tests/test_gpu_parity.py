@@ -269,6 +269,10 @@ def test_invalid_configs_raise(kk, engine):
         engine.walk("metapath", 10, schemes=[[1]])
     with pytest.raises(kk.KKError):
         engine.walk("ppr", 10, terminate_prob=0.0)
+    with pytest.raises(kk.KKError, match="start vertex"):
+        engine.walk("deepwalk", 10, start=[0, 3, 50])
+    # the engine stays usable after the failed call
+    assert engine.walk("deepwalk", 10, start=[0, 3, 49]).total_steps > 0
 
 
 def _compare_alias(engine, oracle_lib, V, off, nbr, w):

@@ -1,0 +1,82 @@
+"""kk_walk_into in walker chunks: chunk c + 1 walks while chunk c's paths are
+packed and copied out.  Whatever the chunking, the lengths, offsets and
+vertices in the caller's buffers are the paths kk_walk returns (which the
+parity tests pin to the reference)."""
+
+import numpy as np
+import pytest
+
+from oracle import graphs as G
+
+pytestmark = pytest.mark.gpu
+
+N = 600_000  # > 2 x 2^18 walkers: several chunks
+
+
+@pytest.fixture(scope="module")
+def engine():
+    import knightking_gb300 as kk
+    e = kk.WalkEngine(0)
+    yield e
+    e.close()
+
+
+def _load(engine, seed, weighted, types=False):
+    g = G.random_undirected(400, 5000, seed=seed, weight="unif" if weighted else None,
+                            types="uniform" if types else None)
+    csr = G.csr_file_order(400, g["src"], g["dst"], w=g.get("w"), type=g.get("type"))
+    engine.load_arrays(400, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
+
+
+def _into(engine, app, n, cap, **kw):
+    h_len = np.zeros(n, np.uint32)
+    h_off = np.zeros(n, np.uint64)
+    h_vert = np.zeros(cap, np.uint32)
+    steps = engine.walk_into(app, n, h_len.ctypes.data, h_off.ctypes.data, h_vert.ctypes.data, cap, **kw)
+    return steps, h_len, h_off, h_vert
+
+
+CASES = [
+    ("deepwalk", True, False, dict(walk_length=10, seed=3)),
+    ("deepwalk", False, False, dict(walk_length=7, seed=4, walker_begin=1000)),
+    ("ppr", False, False, dict(terminate_prob=0.15, seed=5)),
+    ("node2vec", True, False, dict(walk_length=6, p=2.0, q=0.5, seed=6)),
+    ("metapath", True, True, dict(walk_length=6, schemes=[[1, 2, 4, 8], [2, 8, 2, 16]], seed=7)),
+]
+
+
+@pytest.mark.parametrize("chunks,cursor", [(1, 0), (4, 1), (3, 0)])
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_walk_into_equals_walk(engine, case, chunks, cursor):
+    app, weighted, types, kw = CASES[case]
+    _load(engine, 20 + case, weighted, types)
+    ref = engine.walk(app, N, weighted=weighted, **kw)
+    engine.set_option("into_chunks", chunks)
+    engine.set_option("cursor_adjacency", cursor)
+    try:
+        steps, h_len, h_off, h_vert = _into(engine, app, N, len(ref.vertices) + 16, weighted=weighted, **kw)
+    finally:
+        engine.set_option("into_chunks", 4)
+        engine.set_option("cursor_adjacency", 0)
+    assert steps == ref.total_steps
+    np.testing.assert_array_equal(h_len, ref.path_length)
+    total = int(h_len.sum(dtype=np.uint64))
+    assert total == len(ref.vertices)
+    np.testing.assert_array_equal(h_vert[:total], ref.vertices)
+    np.testing.assert_array_equal(h_off[1:], np.cumsum(h_len.astype(np.uint64))[:-1])
+    assert h_off[0] == 0
+
+
+def test_walk_into_epochs_and_small_capacity(engine):
+    """Epochs (rate 0.5) in chunks, and a buffer one vertex short fails cleanly."""
+    import knightking_gb300 as kk
+    _load(engine, 31, True)
+    kw = dict(walk_length=9, seed=11, rate=0.5)
+    ref = engine.walk("deepwalk", N, weighted=True, **kw)
+    total = len(ref.vertices)
+    steps, h_len, h_off, h_vert = _into(engine, "deepwalk", N, total, weighted=True, **kw)
+    assert steps == ref.total_steps
+    np.testing.assert_array_equal(h_len, ref.path_length)
+    np.testing.assert_array_equal(h_vert, ref.vertices)
+    with pytest.raises(kk.KKError):
+        _into(engine, "deepwalk", N, total - 1, weighted=True, **kw)

@@ -116,7 +116,7 @@ kk_status kk_engine_set_stream(kk_engine *e, void *stream);
  *   "walk_multi"         walkers per thread (1, 2, 4) of first-order walks without a dynamic component
  *   "alias_hub_grid"     blocks of the hub alias kernel (0: one per SM)
  *   "into_chunks"        kk_walk_into walks in up to this many walker chunks (>= 2^18 walkers each),
- *                        copying each chunk's paths out while the next chunk walks (default 4; 1 = whole)
+ *                        copying each chunk's paths out while the next chunk walks (default 6; 1 = whole)
  *   "cursor_adjacency"   1 uniform picks read a per-graph adjacency copy holding each neighbour's
  *                        position (16 B/edge, built on first use): one dependent read per step */
 kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value);

@@ -91,6 +91,7 @@ struct WalkResult
     uint32_t cap = 0;
     uint32_t *path = nullptr;
     uint64_t total_steps = 0;
+    bool packed = false; /* path_off holds the exact lengths: path is packed */
 };
 
 /* Stream, events and buffers one batch runs on: the engine's own (for the
@@ -221,6 +222,12 @@ struct RunSpec
     uint32_t cap = 1;        /* vertices per walker, fixed_cap */
     float const_ext = 0.0f;  /* !fixed_cap: constant extension probability */
     bool want_paths = true;
+    /* the walk ends only by its extension or on an isolated start vertex
+     * (built-in DeepWalk, PPR, node2vec): on a graph where no walker can
+     * reach a dead end, every path length is known before the walk, and
+     * the walk writes its paths packed */
+    bool exact = false;
+    bool packed_out = false; /* the caller packs the paths (or wants them packed) */
 };
 
 } // namespace kk
@@ -261,13 +268,16 @@ struct kk_engine
      * into the other output set (walk_set) while chunk c is packed and copied
      * to the caller's buffers on copy_stream */
     int walk_set = 0;
-    int into_chunks = 4;
-    kk::DevBuf path_b, length_b, path_off_b, caps_b;
-    kk::DevBuf into_lens[2], into_off[2], into_offb[2], into_verts[2], into_cub[2];
+    int into_chunks = 6;
+    kk::DevBuf path_x[2], length_x[2], path_off_x[2], caps_x[2]; /* output sets 1 and 2 */
+    kk::DevBuf into_lens[3], into_off[3], into_offb[3], into_verts[3], into_cub[3];
     cudaStream_t copy_stream = nullptr;
     void *h_status = nullptr;      /* mapped pinned words for the walks' status and capacity reads */
     void *d_status_host = nullptr; /* the device address of h_status */
-    cudaEvent_t ev_walked[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
+    cudaEvent_t ev_walked[3] = {nullptr, nullptr, nullptr}, ev_copied[3] = {nullptr, nullptr, nullptr};
+    /* no walker can reach a vertex without out-edges except by starting on
+     * one (every edge's target has out-edges); cached per graph */
+    bool no_dead_ends = false, dead_ends_valid = false;
     /* kernels this library has launched on the engine's streams (CUDA-graph
      * replays not counted; kk_engine_launch_count) */
     std::atomic<uint64_t> launches{0};
@@ -407,6 +417,8 @@ const uint32_t *vertex_order(kk_engine *e);
 const uint64_t *vertex_cursors(kk_engine *e);
 /* The cursor adjacency of the loaded graph (built once per graph). */
 const uint4 *cursor_adjacency_of(kk_engine *e);
+/* Whether no edge leads to a vertex without out-edges (cached per graph). */
+bool graph_no_dead_ends(kk_engine *e);
 
 /* The edge set the node2vec adjacency test reads (cached per graph), or an
  * empty view when the engine's node2vec_adjacency option asks for binary
@@ -617,11 +629,13 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
     L.stats = e->walk_stats ? (unsigned long long *)((char *)d_status + 24) : nullptr;
     /* the walk's output set (two sets let a chunked kk_walk_into walk one
      * chunk while the previous one is packed and copied out) */
-    kk::DevBuf &b_length = e->walk_set ? e->length_b : e->length, &b_caps = e->walk_set ? e->caps_b : e->caps;
-    kk::DevBuf &b_off = e->walk_set ? e->path_off_b : e->path_off, &b_path = e->walk_set ? e->path_b : e->path;
+    const int ws = e->walk_set;
+    kk::DevBuf &b_length = ws ? e->length_x[ws - 1] : e->length, &b_caps = ws ? e->caps_x[ws - 1] : e->caps;
+    kk::DevBuf &b_off = ws ? e->path_off_x[ws - 1] : e->path_off, &b_path = ws ? e->path_x[ws - 1] : e->path;
     L.length = b_length.as<uint32_t>(n);
     uint64_t total_cap;
-    if (rs.fixed_cap)
+    const bool exact = rs.exact && rs.packed_out && rs.want_paths && graph_no_dead_ends(e);
+    if (rs.fixed_cap && !exact)
     {
         L.path_off = nullptr;
         L.cap = rs.cap;
@@ -632,10 +646,22 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
         uint64_t *caps = b_caps.as<uint64_t>((uint64_t)n + 1);
         uint64_t *off = b_off.as<uint64_t>((uint64_t)n + 1);
         KK_CUDA_CHECK(cudaMemsetAsync(caps + n, 0, sizeof(uint64_t), e->stream));
-        constant_extension_bound_kernel<<<grid_for(e, (uint64_t)n * 32, 256), 256, 0, e->stream>>>(
-            rs.seed, rs.walker_begin, n, rs.const_ext, 1u << 24, caps, d_status);
-        count_launch(e);
-        KK_CUDA_CHECK(cudaGetLastError());
+        if (!rs.fixed_cap)
+        {
+            constant_extension_bound_kernel<<<grid_for(e, (uint64_t)n * 32, 256), 256, 0, e->stream>>>(
+                rs.seed, rs.walker_begin, n, rs.const_ext, 1u << 24, caps, d_status);
+            count_launch(e);
+            KK_CUDA_CHECK(cudaGetLastError());
+        }
+        if (exact)
+        {
+            /* the full capacity (fixed length) or the extension bound, and one
+             * vertex for a walker on an isolated start */
+            exact_caps_kernel<<<grid_for(e, n, 256), 256, 0, e->stream>>>(g, rs.d_start, rs.n_start, rs.walker_begin,
+                                                                          n, rs.fixed_cap ? rs.cap : 0u, caps);
+            count_launch(e);
+            KK_CUDA_CHECK(cudaGetLastError());
+        }
         exclusive_scan_u64(e, caps, off, (uint64_t)n + 1);
         words_to_host(e, (const uint32_t *)(off + n), 32, 2); /* host words 32, 33 of the 64 */
         KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
@@ -691,15 +717,16 @@ launched:
     memcpy(e->last_stats, (char *)h_small + 24, sizeof(e->last_stats));
     KK_CUDA_CHECK(cudaEventElapsedTime(&e->alias_ms, e->ev[0], e->ev[1]));
     KK_CUDA_CHECK(cudaEventElapsedTime(&e->walk_ms, e->ev[1], e->ev[2]));
-    if (h_small[0] == KK_STATUS_TRIAL_LIMIT)
-        fail(KK_ERR_TRIAL_LIMIT, "a walker exceeded the rejection-trial limit");
-    if (h_small[0] == KK_STATUS_PATH_CAPACITY)
-        fail(KK_ERR_PATH_CAPACITY, "a walk exceeded its path capacity");
-    if (h_small[0] == KK_STATUS_BAD_START)
+    if (h_small[0] & KK_STATUS_BAD_START) /* first: it can cause the others */
         fail(KK_ERR_INVALID_CONFIG, "start vertex >= v_num");
+    if (h_small[0] & KK_STATUS_TRIAL_LIMIT)
+        fail(KK_ERR_TRIAL_LIMIT, "a walker exceeded the rejection-trial limit");
+    if (h_small[0] & KK_STATUS_PATH_CAPACITY)
+        fail(KK_ERR_PATH_CAPACITY, "a walk exceeded its path capacity");
     unsigned long long steps;
     memcpy(&steps, (char *)h_small + 16, sizeof(steps));
     res.walker_num = n;
+    res.packed = exact;
     res.length = L.length;
     res.path_off = L.path_off;
     res.cap = L.cap;

@@ -259,6 +259,37 @@ static __global__ void vertex_cursor_kernel(GraphView g, uint64_t *cur)
         cur[v] = make_cursor(g.off[v], (uint32_t)(g.off[v + 1] - g.off[v]));
 }
 
+/* Dead ends: flag set when some edge's target has no out-edges. */
+static __global__ void dead_end_kernel(GraphView g, int *flag)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < g.E; e += (uint64_t)gridDim.x * blockDim.x)
+    {
+        const uint32_t v = g.nbr[e];
+        if (__ldg(g.off + v + 1) == __ldg(g.off + v))
+            *flag = 1;
+    }
+}
+
+/* Exact path capacities of walks that end only by their extension: cap
+ * vertices (fixed length; cap 0 keeps the extension bound already in caps),
+ * one for a walker whose start vertex is isolated.  The start vertex is the
+ * walk's (start list, or walker id mod V); an out-of-range one gets 1 (the
+ * walk fails the call on it). */
+static __global__ void exact_caps_kernel(GraphView g, const uint32_t *start, uint32_t n_start, walker_id_t begin,
+                                         uint32_t n, uint32_t cap, uint64_t *caps)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const walker_id_t id = begin + i;
+        const uint32_t v = start != nullptr ? start[id % n_start] : (uint32_t)(id % g.V);
+        const bool alive = v < g.V && g.off[v + 1] > g.off[v];
+        if (!alive)
+            caps[i] = 1;
+        else if (cap != 0)
+            caps[i] = cap;
+    }
+}
+
 /* cursor adjacency: every edge's neighbour with that neighbour's cursor */
 static __global__ void adj_cursor_kernel(GraphView g, const uint64_t *cur, uint4 *adjc)
 {
@@ -1145,6 +1176,7 @@ __global__ void regular_area_kernel(GraphView g, TC tc, const float *sum, float 
 
 /* ---- walk kernels -------------------------------------------------------- */
 
+/* walk status words: an OR of these flags */
 #define KK_STATUS_OK 0
 #define KK_STATUS_TRIAL_LIMIT 4
 #define KK_STATUS_PATH_CAPACITY 8
@@ -1190,7 +1222,7 @@ __device__ __forceinline__ vertex_id_t walker_start(const GraphView &g, const WC
     {
         /* a start vertex outside the graph fails the call (the host reads
          * the status); the walker stands on vertex 0 meanwhile */
-        atomicExch(L.status, KK_STATUS_BAD_START);
+        atomicOr(L.status, KK_STATUS_BAD_START);
         v = 0;
     }
     if constexpr (is_hook<decltype(wc.walker_init_state)>())
@@ -1419,7 +1451,7 @@ __device__ __forceinline__ bool walk_trial(const GraphView &g, const WC &wc, con
         {
             if (run.len >= run.cap)
             {
-                atomicExch(L.status, KK_STATUS_PATH_CAPACITY);
+                atomicOr(L.status, KK_STATUS_PATH_CAPACITY);
                 return false;
             }
             run.out[run.len] = ac.nbr;
@@ -1461,7 +1493,7 @@ __device__ __forceinline__ bool walk_trial(const GraphView &g, const WC &wc, con
     }
     if (++run.step_trials > L.trial_limit)
     {
-        atomicExch(L.status, KK_STATUS_TRIAL_LIMIT);
+        atomicOr(L.status, KK_STATUS_TRIAL_LIMIT);
         run.trials += run.step_trials;
         return false;
     }
@@ -1593,7 +1625,7 @@ __device__ __forceinline__ bool walk_trial(const GraphView &g, const WC &wc, con
     {
         if (run.len >= run.cap)
         {
-            atomicExch(L.status, KK_STATUS_PATH_CAPACITY);
+            atomicOr(L.status, KK_STATUS_PATH_CAPACITY);
             return false;
         }
         run.out[run.len] = ac.nbr;
@@ -1781,7 +1813,7 @@ __global__ void __launch_bounds__(256, 4) walk_multi_kernel(GraphView g, WC wc, 
             {
                 if (r.len >= r.cap)
                 {
-                    atomicExch(L.status, KK_STATUS_PATH_CAPACITY);
+                    atomicOr(L.status, KK_STATUS_PATH_CAPACITY);
                     over = true;
                 }
                 else
@@ -2060,7 +2092,7 @@ static __global__ void constant_extension_bound_kernel(uint64_t seed, walker_id_
         if (lane == 0)
         {
             if (stop == max_steps)
-                atomicExch(status, KK_STATUS_PATH_CAPACITY);
+                atomicOr(status, KK_STATUS_PATH_CAPACITY);
             cap_out[i] = (uint64_t)stop + 1;
         }
     }

@@ -24,6 +24,7 @@ void run_deepwalk(kk_engine *e, const kk_walk_opts &o, RunSpec rs, WalkResult &r
 {
     rs.fixed_cap = true;
     rs.cap = o.walk_length + 1;
+    rs.exact = true; /* ends only after walk_length steps or on an isolated start */
     FixedLengthExt<EmptyData> ext{o.walk_length};
     if (o.weighted)
     {
@@ -49,6 +50,7 @@ void run_ppr(kk_engine *e, const kk_walk_opts &o, RunSpec rs, WalkResult &res)
         fail(KK_ERR_INVALID_CONFIG, "PPR needs 0 < terminate_prob <= 1");
     rs.fixed_cap = false;
     rs.const_ext = ext;
+    rs.exact = true; /* ends only by the extension draw or on an isolated start */
     ConstantExt cext{ext};
     if (o.weighted)
     {

@@ -54,6 +54,7 @@ void run_app_node2vec(kk_engine *e, const kk_walk_opts &o, const RunSpec &rs0, W
     RunSpec rs = rs0;
     rs.fixed_cap = true;
     rs.cap = o.walk_length + 1;
+    rs.exact = true; /* ends only after walk_length steps or on an isolated start */
     Node2vecConstants c = Node2vecConstants::make(o.p, o.q);
     const EdgeSetView set = node2vec_edge_set(e);
     if (o.weighted)

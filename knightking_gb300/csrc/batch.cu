@@ -342,9 +342,9 @@ static uint64_t run_batch_graph(kk_engine *e, BatchPlan &plan, BatchSlot &slot)
     KK_CUDA_CHECK(cudaStreamSynchronize(slot.stream));
     slot.alias_ms = 0.0f;
     KK_CUDA_CHECK(cudaEventElapsedTime(&slot.walk_ms, slot.ev[1], slot.ev[2]));
-    if (h.status[0] == KK_STATUS_TRIAL_LIMIT)
+    if (h.status[0] & KK_STATUS_TRIAL_LIMIT)
         fail(KK_ERR_TRIAL_LIMIT, "a walker exceeded the rejection-trial limit");
-    if (h.status[0] == KK_STATUS_PATH_CAPACITY)
+    if (h.status[0] & KK_STATUS_PATH_CAPACITY)
         fail(KK_ERR_PATH_CAPACITY, "a walk exceeded its path capacity");
     unsigned long long steps;
     memcpy(&steps, (char *)h.status + 16, sizeof(steps));
@@ -392,9 +392,9 @@ uint64_t run_batch(kk_engine *e, BatchPlan &plan, BatchSlot &slot, bool want_pat
         memcpy(e->last_stats, (char *)h_small + 24, sizeof(e->last_stats));
     KK_CUDA_CHECK(cudaEventElapsedTime(&slot.alias_ms, slot.ev[0], slot.ev[1]));
     KK_CUDA_CHECK(cudaEventElapsedTime(&slot.walk_ms, slot.ev[1], slot.ev[2]));
-    if (h_small[0] == KK_STATUS_TRIAL_LIMIT)
+    if (h_small[0] & KK_STATUS_TRIAL_LIMIT)
         fail(KK_ERR_TRIAL_LIMIT, "a walker exceeded the rejection-trial limit");
-    if (h_small[0] == KK_STATUS_PATH_CAPACITY)
+    if (h_small[0] & KK_STATUS_PATH_CAPACITY)
         fail(KK_ERR_PATH_CAPACITY, "a walk exceeded its path capacity");
     unsigned long long steps;
     memcpy(&steps, (char *)h_small + 16, sizeof(steps));

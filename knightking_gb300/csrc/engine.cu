@@ -40,6 +40,7 @@ void kk_engine::free_graph()
     vcur_valid = false;
     edge_set_valid = false;
     adjc_valid = false;
+    dead_ends_valid = false;
     alias_cached = -1;
     n_hub = n_nz = 0;
     memset(tier, 0, sizeof(tier));
@@ -195,7 +196,7 @@ const uint32_t *upload_start(kk_engine *e, const kk_walk_opts *o)
 }
 
 void run_epoch(kk_engine *e, const kk_walk_opts *o, const uint32_t *d_start, uint32_t begin, uint32_t num,
-               bool want_paths, WalkResult &res)
+               bool want_paths, WalkResult &res, bool packed_out = true)
 {
     RunSpec rs;
     rs.seed = o->seed;
@@ -204,6 +205,7 @@ void run_epoch(kk_engine *e, const kk_walk_opts *o, const uint32_t *d_start, uin
     rs.d_start = d_start;
     rs.n_start = o->n_start;
     rs.want_paths = want_paths;
+    rs.packed_out = packed_out;
     if (o->app == KK_APP_NODE2VEC)
         run_app_node2vec(e, *o, rs, res);
     else
@@ -214,6 +216,13 @@ void run_epoch(kk_engine *e, const kk_walk_opts *o, const uint32_t *d_start, uin
 uint64_t pack_paths(kk_engine *e, const WalkResult &r, uint64_t **d_off_out, uint32_t **d_verts_out)
 {
     uint32_t n = r.walker_num;
+    if (r.packed)
+    {
+        /* the walk wrote its paths at their packed offsets */
+        *d_off_out = const_cast<uint64_t *>(r.path_off);
+        *d_verts_out = r.path;
+        return r.total_steps + n;
+    }
     uint64_t *lens64 = e->caps.as<uint64_t>((uint64_t)n + 1);
     uint64_t *off = e->packed_off.as<uint64_t>((uint64_t)n + 1);
     length_to_u64_kernel<<<grid_for(e, (uint64_t)n + 1, 256), 256, 0, e->stream>>>(r.length, lens64, n);
@@ -240,6 +249,15 @@ uint64_t pack_paths_on(kk_engine *e, const WalkResult &r, cudaStream_t st, int s
     const uint32_t n = r.walker_num;
     const uint64_t total = r.total_steps + n;
     uint64_t *ob = e->into_offb[s].as<uint64_t>((uint64_t)n + 1);
+    if (r.packed)
+    {
+        offsets_plus_base_kernel<<<grid_for(e, n, 256), 256, 0, st>>>(r.path_off, 0, base, n, ob);
+        count_launch(e);
+        KK_CUDA_CHECK(cudaGetLastError());
+        *offb = ob;
+        *verts = r.path;
+        return total;
+    }
     if (r.path_off == nullptr && total == (uint64_t)n * r.cap)
     {
         offsets_plus_base_kernel<<<grid_for(e, n, 256), 256, 0, st>>>(nullptr, r.cap, base, n, ob);
@@ -267,9 +285,10 @@ uint64_t pack_paths_on(kk_engine *e, const WalkResult &r, cudaStream_t st, int s
 }
 
 /* kk_walk_into for the built-in apps: the walkers of each epoch in chunks
- * (the into_chunks option; chunks of at least kIntoMinChunk walkers).  Chunk
- * c + 1 walks into the other output set while chunk c's lengths, packed
- * offsets and vertices go to the caller's buffers on the copy stream.  The
+ * (the into_chunks option; about kIntoMinChunk walkers at least).  Chunks
+ * rotate over three output sets: chunk c + 1 walks while chunk c's lengths,
+ * packed offsets and vertices go to the caller's buffers on the copy stream,
+ * and chunk c + 3 waits only for chunk c's copies.  The
  * alias tables are built once per call, by the first chunk (the same tables
  * every chunk would build), unless the alias_cache option keeps them across
  * calls anyway. */
@@ -287,7 +306,7 @@ uint64_t walk_into_chunked(kk_engine *e, const kk_walk_opts *o, uint32_t *h_leng
         int lo = 0, hi = 0;
         KK_CUDA_CHECK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
         KK_CUDA_CHECK(cudaStreamCreateWithPriority(&e->copy_stream, cudaStreamNonBlocking, hi));
-        for (int i = 0; i < 2; i++)
+        for (int i = 0; i < 3; i++)
         {
             KK_CUDA_CHECK(cudaEventCreateWithFlags(&e->ev_walked[i], cudaEventDisableTiming));
             KK_CUDA_CHECK(cudaEventCreateWithFlags(&e->ev_copied[i], cudaEventDisableTiming));
@@ -316,12 +335,23 @@ uint64_t walk_into_chunked(kk_engine *e, const kk_walk_opts *o, uint32_t *h_leng
         uint32_t nch = e->into_chunks > 1 ? (uint32_t)e->into_chunks : 1u;
         if (nch > epoch_n / kIntoMinChunk)
             nch = epoch_n / kIntoMinChunk > 1 ? epoch_n / kIntoMinChunk : 1u;
-        for (uint32_t k = 0; k < nch; k++, chunk++)
+        /* chunk k holds a share 0.8^k of the epoch: each chunk's copy (~0.8 of
+         * its walk time on GB300) hides under the next, smaller chunk's walk,
+         * and the last copy, which nothing hides, is the smallest */
+        double wsum = 0.0, wk = 1.0;
+        for (uint32_t k = 0; k < nch; k++, wk *= 0.8)
+            wsum += wk;
+        double acc = 0.0;
+        wk = 1.0;
+        for (uint32_t k = 0; k < nch; k++, chunk++, wk *= 0.8)
         {
-            const uint32_t cb = done + (uint32_t)((uint64_t)epoch_n * k / nch);
-            const uint32_t ce = done + (uint32_t)((uint64_t)epoch_n * (k + 1) / nch);
+            const uint32_t cb = done + (uint32_t)((double)epoch_n * (acc / wsum));
+            acc += wk;
+            const uint32_t ce = k + 1 == nch ? done + epoch_n : done + (uint32_t)((double)epoch_n * (acc / wsum));
+            if (ce <= cb)
+                continue;
             const uint32_t num = ce - cb;
-            const int s = (int)(chunk & 1u);
+            const int s = (int)(chunk % 3u);
             /* the set's previous chunk must be out before this walk overwrites it */
             KK_CUDA_CHECK(cudaStreamWaitEvent(e->stream, e->ev_copied[s], 0));
             e->walk_set = s;
@@ -504,16 +534,20 @@ void kk_engine_destroy(kk_engine *e)
     {
         cudaStreamSynchronize(e->copy_stream);
         cudaStreamDestroy(e->copy_stream);
-        for (int i = 0; i < 2; i++)
+        for (int i = 0; i < 3; i++)
         {
             cudaEventDestroy(e->ev_walked[i]);
             cudaEventDestroy(e->ev_copied[i]);
         }
     }
-    kk::DevBuf *into_bufs[] = {&e->path_b, &e->length_b, &e->path_off_b, &e->caps_b};
-    for (kk::DevBuf *b : into_bufs)
-        b->release();
     for (int i = 0; i < 2; i++)
+    {
+        e->path_x[i].release();
+        e->length_x[i].release();
+        e->path_off_x[i].release();
+        e->caps_x[i].release();
+    }
+    for (int i = 0; i < 3; i++)
     {
         e->into_lens[i].release();
         e->into_off[i].release();
@@ -889,7 +923,8 @@ kk_status kk_walk_device(kk_engine *e, const kk_walk_opts *opts, uint64_t *total
         validate_opts(e, opts, true);
         const uint32_t *d_start = upload_start(e, opts);
         WalkResult r;
-        run_epoch(e, opts, d_start, opts->walker_begin, opts->walker_num, d_vertices != nullptr, r);
+        run_epoch(e, opts, d_start, opts->walker_begin, opts->walker_num, d_vertices != nullptr, r,
+                  d_offset != nullptr);
         if (total_steps)
             *total_steps = r.total_steps;
         if (d_length)

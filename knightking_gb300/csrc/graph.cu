@@ -219,6 +219,23 @@ const uint64_t *vertex_cursors(kk_engine *e)
     return cur;
 }
 
+bool graph_no_dead_ends(kk_engine *e)
+{
+    if (!e->dead_ends_valid)
+    {
+        int *flag = (int *)e->small.ensure(64) + 12; /* a word the walks' status does not use */
+        KK_CUDA_CHECK(cudaMemsetAsync(flag, 0, sizeof(int), e->stream));
+        dead_end_kernel<<<grid_for(e, e->E, 256), 256, 0, e->stream>>>(e->view(), flag);
+        count_launch(e);
+        KK_CUDA_CHECK(cudaGetLastError());
+        words_to_host(e, (const uint32_t *)flag, 40, 1);
+        KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+        e->no_dead_ends = ((volatile uint32_t *)e->h_status)[40] == 0;
+        e->dead_ends_valid = true;
+    }
+    return e->no_dead_ends;
+}
+
 const uint4 *cursor_adjacency_of(kk_engine *e)
 {
     if (!e->adjc_valid)

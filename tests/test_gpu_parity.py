@@ -155,6 +155,48 @@ def test_fresh_walks_match_oracle(engine, oracle_lib, i, seed, schedule, layout)
     assert ps.total_steps == steps
 
 
+@pytest.mark.parametrize("app", ["deepwalk", "ppr", "node2vec"])
+def test_dead_ends_and_isolated_starts_match_oracle(kk, engine, oracle_lib, app):
+    """A directed graph with dead ends (vertices without out-edges that walks
+    reach) and isolated start vertices: paths end early there, so the engine
+    cannot know their lengths before the walk and packs them afterwards; on
+    the same graph made undirected (isolated starts only) the walk writes
+    them packed.  Both match the oracle, through kk_walk and kk_walk_into."""
+    rng = np.random.default_rng(5)
+    V = 300
+    src = rng.integers(0, V, size=2400)
+    dst = rng.integers(0, V, size=2400)
+    keep = (src % 7 != 0) & (src != dst)  # sources divisible by 7 have no out-edges
+    for directed in (True, False):
+        s, d = src[keep], dst[keep]
+        if not directed:
+            s, d = np.concatenate([s, d]), np.concatenate([d, s])
+            iso = (s % 11 == 5) | (d % 11 == 5)  # these vertices end up isolated
+            s, d = s[~iso], d[~iso]
+        pairs = np.unique(np.stack([s, d], 1), axis=0)
+        csr = G.csr_file_order(V, pairs[:, 0].astype(np.uint32), pairs[:, 1].astype(np.uint32))
+        engine.load_arrays(V, csr["off"], csr["nbr"])
+        kw = dict(walk_length=12) if app != "ppr" else dict(terminate_prob=0.1)
+        if app == "node2vec":
+            kw.update(p=2.0, q=0.5)
+        n = 2000
+        ps = engine.walk(app, n, seed=9, **kw)
+        ocsr = oracle_lib.CSR(V, csr["off"], csr["nbr"])
+        if app == "node2vec":
+            ocsr = ocsr.sorted_copy()
+        prm = oracle_lib.make_params(app, seed=9, walker_num=n, weighted=False, **kw)
+        lens, verts, steps = oracle_lib.walk(ocsr, prm, cap=4096)
+        np.testing.assert_array_equal(ps.path_length, lens)
+        np.testing.assert_array_equal(ps.vertices, verts)
+        h_len = np.zeros(n, np.uint32)
+        h_off = np.zeros(n, np.uint64)
+        h_vert = np.zeros(len(verts), np.uint32)
+        assert engine.walk_into(app, n, h_len.ctypes.data, h_off.ctypes.data, h_vert.ctypes.data, len(verts),
+                                seed=9, **kw) == steps
+        np.testing.assert_array_equal(h_len, lens)
+        np.testing.assert_array_equal(h_vert, verts)
+
+
 @pytest.mark.parametrize("multi", [2, 4])
 @pytest.mark.parametrize("i", [0, 1, 2, 3])
 def test_multi_walker_kernel_matches_oracle(engine, oracle_lib, i, multi):

@@ -56,7 +56,7 @@ def test_walk_into_equals_walk(engine, case, chunks, cursor):
     try:
         steps, h_len, h_off, h_vert = _into(engine, app, N, len(ref.vertices) + 16, weighted=weighted, **kw)
     finally:
-        engine.set_option("into_chunks", 4)
+        engine.set_option("into_chunks", 6)
         engine.set_option("cursor_adjacency", 0)
     assert steps == ref.total_steps
     np.testing.assert_array_equal(h_len, ref.path_length)

@@ -114,7 +114,7 @@ kk_status kk_engine_set_stream(kk_engine *e, void *stream);
  *                        lives: 32, 64, 128, or 0 for the value found (restored on destroy)
  *   "walk_stats"         1 counts trials, queries and probes (kk_last_walk_stats)
  *   "walk_multi"         walkers per thread (1, 2, 4) of first-order walks without a dynamic component
- *   "alias_hub_grid"     blocks of the hub alias kernel (0: one per SM)
+ *   "alias_hub_grid"     blocks of the hub alias kernel (0: one per two SMs)
  *   "into_chunks"        kk_walk_into walks in up to this many walker chunks (>= 2^18 walkers each),
  *                        copying each chunk's paths out while the next chunk walks (default 6; 1 = whole)
  *   "cursor_adjacency"   1 uniform picks read a per-graph adjacency copy holding each neighbour's

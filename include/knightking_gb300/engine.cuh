@@ -329,8 +329,8 @@ struct kk_engine
      * e->alias hold (0 cursor, 1 index), -1 none. */
     int alias_cache = 0;
     int alias_cached = -1;
-    /* alias_hub_grid (option): blocks of the hub alias kernel (0: one per SM);
-     * fewer leave more of the SMs to the classes on the main stream */
+    /* alias_hub_grid (option): blocks of the hub alias kernel (0: one per two
+     * SMs); fewer leave more of the SMs to the classes on the main stream */
     int alias_hub_grid = 0;
     /* l2_fetch_bytes (option): the context's cudaLimitMaxL2FetchGranularity
      * hint while the engine lives (0: left as found); the value found is put
@@ -533,7 +533,10 @@ void build_alias(kk_engine *e, const TC &tc)
         /* hubs first, largest first, on the side stream so they start at once */
         KK_CUDA_CHECK(cudaEventRecord(e->ev_fork, e->stream));
         KK_CUDA_CHECK(cudaStreamWaitEvent(e->side, e->ev_fork, 0));
-        const uint32_t cap = e->alias_hub_grid > 0 ? (uint32_t)e->alias_hub_grid : (uint32_t)e->sm_count;
+        /* half the SMs by default: the hubs' serial sums and short batches use
+         * few lanes, and the classes on the main stream get the other half */
+        const uint32_t cap =
+            e->alias_hub_grid > 0 ? (uint32_t)e->alias_hub_grid : (uint32_t)(e->sm_count > 1 ? e->sm_count / 2 : 1);
         const unsigned grid = e->n_hub < cap ? e->n_hub : cap;
         alias_build_hub_kernel<TC, Bucket><<<grid, 1024, 0, e->side>>>(g, tc, alias, vcur, sum, scratch, order, 0,
                                                                        e->n_hub, next);

@@ -182,6 +182,14 @@ def allreduce(world, value, op):
     return float(t.item())
 
 
+def rank_walkers(rank, walkers):
+    """Walker ids of a rank: every rank walks `walkers` walkers (weak scaling),
+    rank r the global ids [r * walkers, (r + 1) * walkers).  The stream is
+    keyed by the global id, so the ranks' paths together are the paths of one
+    walk over all of them."""
+    return rank * walkers, walkers
+
+
 def walk_kwargs(wl):
     kw = {}
     for k in ("walk_length", "terminate_prob", "p", "q", "schemes", "scheme_round_robin"):
@@ -570,7 +578,7 @@ def run_ours(args, wl, world, rank, local):
     engine.generate_rmat(wl["scale"], 16, seed=wl["scale"], weights=wl["weights"], types=wl["types"])
     V, E, _, _ = engine.info()
     walkers = V if not (wl["app"] == "node2vec" and wl["scale"] == 16) else 65536
-    walker_begin = rank * walkers
+    walker_begin, walkers = rank_walkers(rank, walkers)
     kw = walk_kwargs(wl)
     stream = torch.cuda.Stream()
     engine.set_stream(stream.cuda_stream)

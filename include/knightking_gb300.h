@@ -115,8 +115,13 @@ kk_status kk_engine_set_stream(kk_engine *e, void *stream);
  *   "walk_stats"         1 counts trials, queries and probes (kk_last_walk_stats)
  *   "walk_multi"         walkers per thread (1, 2, 4) of first-order walks without a dynamic component
  *   "alias_hub_grid"     blocks of the hub alias kernel (0: one per two SMs)
- *   "into_chunks"        kk_walk_into walks in up to this many walker chunks (>= 2^18 walkers each),
- *                        copying each chunk's paths out while the next chunk walks (default 6; 1 = whole)
+ *   "into_stream"        1 (default): kk_walk_into walks whose path lengths are known before they
+ *                        run (DeepWalk, PPR, node2vec on graphs without reachable dead ends) in one
+ *                        launch per epoch and copies each segment of walkers out as soon as its
+ *                        last walker finishes; 0: walker chunks for every walk (into_chunks)
+ *   "into_chunks"        kk_walk_into walks that are not streamed run in up to this many walker
+ *                        chunks (>= 2^18 walkers each), copying each chunk's paths out while the
+ *                        next chunk walks (default 6; 1 = whole)
  *   "cursor_adjacency"   1 uniform picks read a per-graph adjacency copy holding each neighbour's
  *                        position (16 B/edge, built on first use): one dependent read per step */
 kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value);
@@ -208,7 +213,9 @@ kk_status kk_walk_metapath(kk_engine *e, const kk_walk_opts *opts, kk_paths **ou
 /* Same walk into caller-owned host buffers (pinned memory gives full copy
  * bandwidth): h_length[walker_num], h_offset[walker_num], and h_vertices with
  * room for vertices_capacity vertices (KK_ERR_PATH_CAPACITY if too small).
- * The output is PathSet-equivalent (include/path.hpp:46-84) in walker-id order. */
+ * The output is PathSet-equivalent (include/path.hpp:46-84) in walker-id order.
+ * The copies to the caller's buffers overlap the walk (options into_stream,
+ * into_chunks); the call returns when every path is in host memory. */
 kk_status kk_walk_into(kk_engine *e, const kk_walk_opts *opts, uint32_t *h_length, uint64_t *h_offset,
                        uint32_t *h_vertices, uint64_t vertices_capacity, uint64_t *total_steps);
 

@@ -211,6 +211,30 @@ struct PooledPaths
     size_t cls;
 };
 
+/* kk_walk_into's streamed copy-out of one walk whose path offsets are known
+ * before it runs.  The walk counts finished walkers per segment of
+ * 2^shift walkers (at most kMaxSegments segments); the host copies each
+ * segment's lengths and paths out as soon as its flag is set, while the rest
+ * of the walk goes on, instead of splitting the walk into launches (each of
+ * which pays its own tail). */
+constexpr uint32_t kMaxSegments = 256;
+constexpr size_t kStatusBytes = 8192;  /* the mapped status block */
+constexpr size_t kSegFlagAt = 1024;    /* segment flags: kMaxSegments words */
+constexpr size_t kSegBoundAt = 2048;   /* segment path offsets: kMaxSegments + 1 */
+struct SegmentSink
+{
+    /* the walk's path offsets d_off (n + 1, total vertices total) are final;
+     * the walk is not launched yet */
+    std::function<void(const uint64_t *d_off, uint32_t n, uint64_t total)> before;
+    /* the walk is launched (event walked after it): copies every segment out
+     * as it finishes, and whatever is left once walked has completed;
+     * bound[k] = the path offset of segment k's first walker */
+    std::function<void(const uint32_t *d_len, const uint32_t *d_path, uint32_t n, uint32_t shift, uint32_t nseg,
+                       const volatile uint32_t *flag, const volatile uint64_t *bound, cudaEvent_t walked)>
+        during;
+    bool used = false;
+};
+
 struct RunSpec
 {
     uint64_t seed = 1;
@@ -274,6 +298,11 @@ struct kk_engine
     cudaStream_t copy_stream = nullptr;
     void *h_status = nullptr;      /* mapped pinned words for the walks' status and capacity reads */
     void *d_status_host = nullptr; /* the device address of h_status */
+    /* streamed copy-out of the running walk (kk_walk_into; nullptr: none) and
+     * its per-segment walker counters */
+    kk::SegmentSink *seg_sink = nullptr;
+    int into_stream = 1; /* option into_stream: 0 keeps the walker chunks */
+    kk::DevBuf seg_count;
     cudaEvent_t ev_walked[3] = {nullptr, nullptr, nullptr}, ev_copied[3] = {nullptr, nullptr, nullptr};
     /* no walker can reach a vertex without out-edges except by starting on
      * one (every edge's target has out-edges); cached per graph */
@@ -351,6 +380,9 @@ inline void count_launch(kk_engine *e) { e->launches.fetch_add(1, std::memory_or
 /* n 32-bit words from src to the engine's mapped host words at word `at`,
  * written by a kernel on the engine's stream (no copy engine involved). */
 void words_to_host(kk_engine *e, const uint32_t *src, int at, int n);
+/* The path offsets of segments 0..nseg (walker k << shift, the last one n)
+ * into the mapped status block at kSegBoundAt, on the engine's stream. */
+void segment_bounds_to_host(kk_engine *e, const uint64_t *off, uint32_t n, uint32_t shift, uint32_t nseg);
 
 /* Runs f, turning the exceptions inside the engine into a status and the
  * engine's last-error message (no exception crosses the C-ABI). */
@@ -638,6 +670,7 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
     L.length = b_length.as<uint32_t>(n);
     uint64_t total_cap;
     const bool exact = rs.exact && rs.packed_out && rs.want_paths && graph_no_dead_ends(e);
+    uint32_t seg_shift = 0, nseg = 0, *seg_count = nullptr;
     if (rs.fixed_cap && !exact)
     {
         L.path_off = nullptr;
@@ -667,10 +700,30 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
         }
         exclusive_scan_u64(e, caps, off, (uint64_t)n + 1);
         words_to_host(e, (const uint32_t *)(off + n), 32, 2); /* host words 32, 33 of the 64 */
+        if (exact && e->seg_sink != nullptr && n > 0)
+        {
+            /* streamed copy-out: segments of 2^shift >= 4096 walkers, at most
+             * kMaxSegments of them; flags cleared before the walk can set any */
+            seg_shift = 12;
+            while ((((uint64_t)n + (1ull << seg_shift) - 1) >> seg_shift) > kMaxSegments)
+                seg_shift++;
+            nseg = (uint32_t)(((uint64_t)n + (1ull << seg_shift) - 1) >> seg_shift);
+            memset((char *)e->h_status + kSegFlagAt, 0, (size_t)nseg * 4);
+            seg_count = e->seg_count.as<uint32_t>(kMaxSegments);
+            KK_CUDA_CHECK(cudaMemsetAsync(seg_count, 0, (size_t)nseg * 4, e->stream));
+            segment_bounds_to_host(e, off, n, seg_shift, nseg);
+        }
         KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
         total_cap = ((volatile uint64_t *)e->h_status)[16];
         L.path_off = off;
         L.cap = 0;
+        if (nseg > 0)
+        {
+            e->seg_sink->before(off, n, total_cap);
+            L.seg_count = seg_count;
+            L.seg_flag = (volatile uint32_t *)((char *)e->d_status_host + kSegFlagAt);
+            L.seg_shift = seg_shift;
+        }
     }
     L.path = rs.want_paths ? b_path.as<uint32_t>(total_cap) : nullptr;
     KK_CUDA_CHECK(cudaEventRecord(e->ev[1], e->stream));
@@ -713,6 +766,13 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
 launched:
     KK_CUDA_CHECK(cudaGetLastError());
     KK_CUDA_CHECK(cudaEventRecord(e->ev[2], e->stream));
+    if (nseg > 0)
+    {
+        e->seg_sink->used = true;
+        e->seg_sink->during(L.length, L.path, n, seg_shift, nseg,
+                            (const volatile uint32_t *)((const char *)e->h_status + kSegFlagAt),
+                            (const volatile uint64_t *)((const char *)e->h_status + kSegBoundAt), e->ev[2]);
+    }
     words_to_host(e, (const uint32_t *)d_status, 0, 16);
     KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
     int h_small[16];

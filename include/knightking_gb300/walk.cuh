@@ -1198,7 +1198,47 @@ struct WalkLaunch
     int *status;
     uint32_t trial_limit;
     unsigned long long *stats; /* trials, queries, probes of the launch, or nullptr */
+    /* streamed copy-out (kk_walk_into): finished walkers counted per segment
+     * of 2^seg_shift walkers; the segment's last walker sets its flag in
+     * mapped host memory, and the host copies the segment's paths out while
+     * the walk goes on.  seg_count == nullptr: no counting. */
+    uint32_t *seg_count = nullptr;
+    volatile uint32_t *seg_flag = nullptr;
+    uint32_t seg_shift = 0;
 };
+
+/* Walker i has written its whole path and its length.  The lanes that end a
+ * walker of the same segment together are counted by one of them (a counter
+ * per walker serialises the resident threads on the few segments they are
+ * all finishing: +40% walk time at 4 M walkers).  The warp barrier orders the
+ * lanes' writes before that lane's release add (performed in device memory
+ * no later than the count; no acquire, so the SM's L1 keeps its lines).  The
+ * segment's last count is followed by an acquire-release fence at device
+ * scope, which orders every counted walker's writes before the flag's store
+ * to host memory.  The host issues the segment's copy on seeing the flag, and
+ * the copy engine reads device memory through the same L2, so it reads
+ * finished paths; no system-scope fence is needed (the data never goes to
+ * the host by any other route). */
+__device__ __forceinline__ void segment_done(const WalkLaunch &L, uint32_t i)
+{
+    if (L.seg_count == nullptr)
+        return;
+    const uint32_t s = i >> L.seg_shift;
+    const unsigned peers = __match_any_sync(__activemask(), s);
+    __syncwarp(peers);
+    if ((int)(threadIdx.x & 31) != __ffs(peers) - 1)
+        return;
+    const uint32_t left = L.walker_num - (s << L.seg_shift);
+    const uint32_t size = left < (1u << L.seg_shift) ? left : (1u << L.seg_shift);
+    const uint32_t add = (uint32_t)__popc(peers);
+    uint32_t old;
+    asm volatile("atom.release.gpu.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(L.seg_count + s), "r"(add) : "memory");
+    if (old + add == size)
+    {
+        asm volatile("fence.acq_rel.gpu;" ::: "memory");
+        asm volatile("st.relaxed.sys.u32 [%0], 1;" ::"l"(L.seg_flag + s) : "memory");
+    }
+}
 
 template <typename S, typename WC>
 __device__ __forceinline__ vertex_id_t walker_start(const GraphView &g, const WC &wc, const WalkLaunch &L,
@@ -1663,6 +1703,7 @@ __global__ void __launch_bounds__(256, 4) walk_static_kernel(GraphView g, WC wc,
             {
             }
             L.length[i] = run.len;
+            segment_done(L, i);
             my_steps += run.len - 1;
             counts.add(run);
         }
@@ -1748,6 +1789,7 @@ __global__ void __launch_bounds__(256, 4) walk_multi_kernel(GraphView g, WC wc, 
             if (ends)
             {
                 L.length[idx[k]] = run[k].len;
+                segment_done(L, idx[k]);
                 my_steps += run[k].len - 1;
                 counts.add(run[k]);
                 act[k] = next < L.walker_num;
@@ -1824,6 +1866,7 @@ __global__ void __launch_bounds__(256, 4) walk_multi_kernel(GraphView g, WC wc, 
             if (over)
             {
                 L.length[idx[k]] = r.len;
+                segment_done(L, idx[k]);
                 my_steps += r.len - 1;
                 counts.add(r);
                 act[k] = false;
@@ -1871,6 +1914,7 @@ __global__ void __launch_bounds__(256) walk_pool_kernel(GraphView g, WC wc, TC t
         if (have && !walk_trial<S>(g, wc, tc, alias, ra, L, run, rng))
         {
             L.length[i] = run.len;
+            segment_done(L, i);
             my_steps += run.len - 1;
             counts.add(run);
             i = atomicAdd(&s_next, 1u);

@@ -14,6 +14,7 @@
 
 #include <cub/cub.cuh>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "knightking_gb300/engine.cuh"
@@ -90,6 +91,19 @@ __global__ void words_to_host_kernel(const uint32_t *src, volatile uint32_t *dst
 {
     if (threadIdx.x < (unsigned)n)
         dst[threadIdx.x] = src[threadIdx.x];
+}
+
+/* Path offsets of the streamed segments: bound[k] = off[min(k << shift, n)]
+ * for k = 0..nseg, written to mapped host memory. */
+__global__ void segment_bounds_kernel(const uint64_t *off, uint32_t n, uint32_t shift, uint32_t nseg,
+                                      volatile uint64_t *bound)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k <= nseg)
+    {
+        const uint64_t w = (uint64_t)k << shift;
+        bound[k] = off[w < n ? w : n];
+    }
 }
 
 /* Host-side path offsets of a chunk: its packed offsets plus the chunk's base
@@ -321,9 +335,13 @@ uint64_t walk_into_chunked(kk_engine *e, const kk_walk_opts *o, uint32_t *h_leng
         {
             e->alias_cache = cache;
             e->walk_set = 0;
+            e->seg_sink = nullptr;
             cudaStreamSynchronize(e->copy_stream);
         }
     } restore{e, user_cache};
+    /* a walk whose path lengths are known before it runs streams its
+     * segments out as they finish: one launch per epoch, no chunk tails */
+    const bool streamed = e->into_stream && o->app != KK_APP_METAPATH && graph_no_dead_ends(e);
     if (!user_cache)
         e->alias_cached = -1; /* this call builds its own tables */
     const uint32_t per = epoch_walkers(o);
@@ -332,7 +350,7 @@ uint64_t walk_into_chunked(kk_engine *e, const kk_walk_opts *o, uint32_t *h_leng
     while (done < o->walker_num)
     {
         const uint32_t epoch_n = o->walker_num - done < per ? o->walker_num - done : per;
-        uint32_t nch = e->into_chunks > 1 ? (uint32_t)e->into_chunks : 1u;
+        uint32_t nch = e->into_chunks > 1 && !streamed ? (uint32_t)e->into_chunks : 1u;
         if (nch > epoch_n / kIntoMinChunk)
             nch = epoch_n / kIntoMinChunk > 1 ? epoch_n / kIntoMinChunk : 1u;
         /* chunk k holds a share 0.8^k of the epoch: each chunk's copy (~0.8 of
@@ -355,15 +373,84 @@ uint64_t walk_into_chunked(kk_engine *e, const kk_walk_opts *o, uint32_t *h_leng
             /* the set's previous chunk must be out before this walk overwrites it */
             KK_CUDA_CHECK(cudaStreamWaitEvent(e->stream, e->ev_copied[s], 0));
             e->walk_set = s;
+            cudaStream_t cs = e->copy_stream;
+            SegmentSink sink;
+            if (streamed)
+            {
+                sink.before = [&](const uint64_t *d_off, uint32_t n, uint64_t total) {
+                    if (base + total > capacity)
+                        fail(KK_ERR_PATH_CAPACITY, "vertices buffer too small");
+                    /* the offsets are final (the engine's stream has been
+                     * synchronised): out at once, beside the walk */
+                    uint64_t *ob = e->into_offb[s].as<uint64_t>((uint64_t)n + 1);
+                    offsets_plus_base_kernel<<<grid_for(e, n, 256), 256, 0, cs>>>(d_off, 0, base, n, ob);
+                    count_launch(e);
+                    KK_CUDA_CHECK(cudaGetLastError());
+                    KK_CUDA_CHECK(cudaMemcpyAsync(h_offset + cb, ob, (size_t)n * 8, cudaMemcpyDeviceToHost, cs));
+                };
+                sink.during = [&](const uint32_t *d_len, const uint32_t *d_path, uint32_t n, uint32_t shift,
+                                  uint32_t nseg, const volatile uint32_t *flag, const volatile uint64_t *bound,
+                                  cudaEvent_t walked) {
+                    std::vector<char> out(nseg, 0);
+                    uint32_t left = nseg;
+                    bool all = false;
+                    while (left > 0)
+                    {
+                        if (!all)
+                        {
+                            /* once the walk has ended every segment is final,
+                             * whether or not its flag has arrived */
+                            const cudaError_t q = cudaEventQuery(walked);
+                            if (q == cudaSuccess)
+                                all = true;
+                            else if (q != cudaErrorNotReady)
+                                KK_CUDA_CHECK(q);
+                        }
+                        bool issued = false;
+                        for (uint32_t a = 0; a < nseg;)
+                        {
+                            if (out[a] || !(all || flag[a]))
+                            {
+                                a++;
+                                continue;
+                            }
+                            uint32_t b = a;
+                            while (b < nseg && !out[b] && (all || flag[b]))
+                                out[b++] = 1;
+                            const uint32_t wa = a << shift;
+                            const uint32_t wb = (uint64_t)b << shift < n ? b << shift : n;
+                            const uint64_t va = bound[a], vb = bound[b];
+                            KK_CUDA_CHECK(cudaMemcpyAsync(h_length + cb + wa, d_len + wa, (size_t)(wb - wa) * 4,
+                                                          cudaMemcpyDeviceToHost, cs));
+                            if (vb > va)
+                                KK_CUDA_CHECK(cudaMemcpyAsync(h_vertices + base + va, d_path + va,
+                                                              (size_t)(vb - va) * 4, cudaMemcpyDeviceToHost, cs));
+                            left -= b - a;
+                            issued = true;
+                            a = b;
+                        }
+                        if (!issued && !all)
+                            std::this_thread::yield();
+                    }
+                };
+                e->seg_sink = &sink;
+            }
             WalkResult r;
             run_epoch(e, o, d_start, o->walker_begin + cb, num, true, r);
+            e->seg_sink = nullptr;
             e->alias_cache = 1;
             steps += r.total_steps;
             const uint64_t total = r.total_steps + num;
             if (base + total > capacity)
                 fail(KK_ERR_PATH_CAPACITY, "vertices buffer too small");
+            if (sink.used)
+            {
+                /* every segment's copies are queued on the copy stream */
+                KK_CUDA_CHECK(cudaEventRecord(e->ev_copied[s], cs));
+                base += total;
+                continue;
+            }
             KK_CUDA_CHECK(cudaEventRecord(e->ev_walked[s], e->stream));
-            cudaStream_t cs = e->copy_stream;
             KK_CUDA_CHECK(cudaStreamWaitEvent(cs, e->ev_walked[s], 0));
             const uint64_t *offb;
             const uint32_t *verts;
@@ -421,6 +508,14 @@ uint64_t walk_epochs(kk_engine *e, const kk_walk_opts *o, const EpochRunner *cus
 }
 
 } // namespace
+
+void segment_bounds_to_host(kk_engine *e, const uint64_t *off, uint32_t n, uint32_t shift, uint32_t nseg)
+{
+    segment_bounds_kernel<<<(nseg + 256) / 256, 256, 0, e->stream>>>(
+        off, n, shift, nseg, (volatile uint64_t *)((char *)e->d_status_host + kSegBoundAt));
+    count_launch(e);
+    KK_CUDA_CHECK(cudaGetLastError());
+}
 
 void words_to_host(kk_engine *e, const uint32_t *src, int at, int n)
 {
@@ -489,7 +584,7 @@ kk_status kk_engine_create(kk_engine **out, int device)
         /* mapped pinned words the walks' status and capacity reads land in:
          * a kernel writes them (kk::words_to_host), so the host read waits on
          * the engine's stream only, never on copies queued on other streams */
-        KK_CUDA_CHECK(cudaHostAlloc(&e->h_status, 256, cudaHostAllocMapped));
+        KK_CUDA_CHECK(cudaHostAlloc(&e->h_status, kk::kStatusBytes, cudaHostAllocMapped));
         KK_CUDA_CHECK(cudaHostGetDevicePointer(&e->d_status_host, e->h_status, 0));
     });
     if (s != KK_OK)
@@ -556,6 +651,7 @@ void kk_engine_destroy(kk_engine *e)
         e->into_cub[i].release();
     }
     e->alias_next.release();
+    e->seg_count.release();
     e->vcur.release();
     e->edge_set.release();
     e->edge_pos.release();
@@ -606,6 +702,8 @@ kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value)
             e->walk_stats = (int)value;
         else if (n == "into_chunks" && value >= 1 && value <= 64)
             e->into_chunks = (int)value;
+        else if (n == "into_stream" && (value == 0 || value == 1))
+            e->into_stream = (int)value;
         else if (n == "cursor_adjacency" && (value == 0 || value == 1))
             e->cursor_adjacency = (int)value;
         else if (n == "alias_hub_grid" && value >= 0 && value <= 4096)

@@ -1,7 +1,10 @@
-"""kk_walk_into in walker chunks: chunk c + 1 walks while chunk c's paths are
-packed and copied out.  Whatever the chunking, the lengths, offsets and
-vertices in the caller's buffers are the paths kk_walk returns (which the
-parity tests pin to the reference)."""
+"""kk_walk_into's two copy-out modes.  Streamed (walks whose path lengths are
+known before they run): one launch per epoch, every segment of walkers copied
+out as soon as its last walker finishes.  Chunked (into_stream 0, metapath,
+graphs with dead ends): chunk c + 1 walks while chunk c's paths are packed and
+copied out.  Whatever the mode, the lengths, offsets and vertices in the
+caller's buffers are the paths kk_walk returns (which the parity tests pin to
+the reference)."""
 
 import numpy as np
 import pytest
@@ -45,19 +48,21 @@ CASES = [
 ]
 
 
-@pytest.mark.parametrize("chunks,cursor", [(1, 0), (4, 1), (3, 0)])
+@pytest.mark.parametrize("chunks,cursor,stream", [(1, 0, 1), (4, 1, 1), (3, 0, 0), (4, 1, 0)])
 @pytest.mark.parametrize("case", range(len(CASES)))
-def test_walk_into_equals_walk(engine, case, chunks, cursor):
+def test_walk_into_equals_walk(engine, case, chunks, cursor, stream):
     app, weighted, types, kw = CASES[case]
     _load(engine, 20 + case, weighted, types)
     ref = engine.walk(app, N, weighted=weighted, **kw)
     engine.set_option("into_chunks", chunks)
     engine.set_option("cursor_adjacency", cursor)
+    engine.set_option("into_stream", stream)
     try:
         steps, h_len, h_off, h_vert = _into(engine, app, N, len(ref.vertices) + 16, weighted=weighted, **kw)
     finally:
         engine.set_option("into_chunks", 6)
         engine.set_option("cursor_adjacency", 0)
+        engine.set_option("into_stream", 1)
     assert steps == ref.total_steps
     np.testing.assert_array_equal(h_len, ref.path_length)
     total = int(h_len.sum(dtype=np.uint64))
@@ -67,16 +72,41 @@ def test_walk_into_equals_walk(engine, case, chunks, cursor):
     assert h_off[0] == 0
 
 
-def test_walk_into_epochs_and_small_capacity(engine):
-    """Epochs (rate 0.5) in chunks, and a buffer one vertex short fails cleanly."""
+@pytest.mark.parametrize("stream", [1, 0])
+def test_walk_into_epochs_and_small_capacity(engine, stream):
+    """Epochs (rate 0.5), streamed or in chunks, and a buffer one vertex short
+    fails cleanly (before any copy in the streamed mode)."""
     import knightking_gb300 as kk
     _load(engine, 31, True)
     kw = dict(walk_length=9, seed=11, rate=0.5)
     ref = engine.walk("deepwalk", N, weighted=True, **kw)
     total = len(ref.vertices)
-    steps, h_len, h_off, h_vert = _into(engine, "deepwalk", N, total, weighted=True, **kw)
+    engine.set_option("into_stream", stream)
+    try:
+        steps, h_len, h_off, h_vert = _into(engine, "deepwalk", N, total, weighted=True, **kw)
+        assert steps == ref.total_steps
+        np.testing.assert_array_equal(h_len, ref.path_length)
+        np.testing.assert_array_equal(h_vert, ref.vertices)
+        with pytest.raises(kk.KKError):
+            _into(engine, "deepwalk", N, total - 1, weighted=True, **kw)
+        # the engine stays usable after the refused call
+        steps2, h_len2, _, h_vert2 = _into(engine, "deepwalk", N, total, weighted=True, **kw)
+        np.testing.assert_array_equal(h_vert2, ref.vertices)
+    finally:
+        engine.set_option("into_stream", 1)
+
+
+def test_walk_into_streamed_large_walk(engine):
+    """A walk of 2^21 walkers over a graph with isolated vertices: 256
+    segments of 8192 walkers, some holding only one-vertex paths."""
+    g = G.random_undirected(3000, 20000, seed=41, weight="unif")
+    csr = G.csr_file_order(4000, g["src"], g["dst"], w=g.get("w"))  # vertices 3000.. are isolated
+    engine.load_arrays(4000, csr["off"], csr["nbr"], csr.get("w"))
+    n = 1 << 21
+    kw = dict(walk_length=5, seed=13)
+    ref = engine.walk("deepwalk", n, weighted=True, **kw)
+    steps, h_len, h_off, h_vert = _into(engine, "deepwalk", n, len(ref.vertices), weighted=True, **kw)
     assert steps == ref.total_steps
     np.testing.assert_array_equal(h_len, ref.path_length)
     np.testing.assert_array_equal(h_vert, ref.vertices)
-    with pytest.raises(kk.KKError):
-        _into(engine, "deepwalk", N, total - 1, weighted=True, **kw)
+    np.testing.assert_array_equal(h_off[1:], np.cumsum(h_len.astype(np.uint64))[:-1])

@@ -203,6 +203,10 @@ struct HostPool
     void release() { put(nullptr, 0); }
 };
 
+/* Pinned bytes the pool of kk_batch_walk's results keeps for reuse once the
+ * caller has returned them (kk_paths_free). */
+constexpr size_t kBatchPoolCache = (size_t)4 << 30;
+
 /* Owner record of a kk_paths whose arrays live in one pooled block. */
 struct PooledPaths
 {
@@ -303,6 +307,11 @@ struct kk_engine
     kk::SegmentSink *seg_sink = nullptr;
     int into_stream = 1; /* option into_stream: 0 keeps the walker chunks */
     kk::DevBuf seg_count;
+    /* kk_batch_walk: the jobs' packed offsets and first vertices, and the
+     * pooled pinned blocks its results are handed out in (created on first
+     * use; kk_paths_free returns a block) */
+    kk::DevBuf batch_small, batch_rel;
+    kk::HostPool *host_pool = nullptr;
     cudaEvent_t ev_walked[3] = {nullptr, nullptr, nullptr}, ev_copied[3] = {nullptr, nullptr, nullptr};
     /* no walker can reach a vertex without out-edges except by starting on
      * one (every edge's target has out-edges); cached per graph */
@@ -474,6 +483,16 @@ struct BatchPlan
 
 /* Checks the jobs and lays out the batch (fails on mixed apps or weighting). */
 BatchPlan plan_batch(kk_engine *e, const kk_walk_opts *jobs, int n);
+
+/* Packs a finished batch's paths (job j's walker i at path[path_base_j + i *
+ * cap_j], its length at length[first_task_j + i]; d_jobs the job table on the
+ * device) into one buffer in job order, on the engine's stream (engine.cu):
+ * *d_verts the packed vertices, *d_rel each walker's offset counted from its
+ * job's first vertex, job_begin (host, one entry per job and one past the
+ * last) the position of each job's first vertex in *d_verts. */
+void pack_batch_paths(kk_engine *e, const BatchPlan &plan, const BatchJob *d_jobs, const uint32_t *length,
+                      const uint32_t *path, const uint64_t **d_rel, const uint32_t **d_verts,
+                      std::vector<uint64_t> &job_begin);
 
 /* Everything a batch of the plan's app reads besides the graph, on the
  * engine's stream: the sorted adjacency (node2vec), the vertex type masks

@@ -249,16 +249,24 @@ class WalkEngine:
             ctypes.memmove(ctypes.byref(arr[i]), ctypes.byref(o), ctypes.sizeof(o))
         return arr, keep
 
-    def batch_walk(self, app, jobs):
+    def batch_walk(self, app, jobs, keep_paths=True):
         """Many jobs of one app in one launch (kk_batch_walk); jobs are dicts of
-        make_opts keywords with walker_num.  Returns one PathSet per job."""
+        make_opts keywords with walker_num.  Returns one PathSet per job, or
+        with keep_paths=False, per job a dict of walker_num, total_steps and
+        vertices, the paths (in pinned host memory when the call returns)
+        handed back to the library's pool without a copy."""
         arr, keep = self._job_array(app, jobs)
         outs = (ctypes.POINTER(_capi.KKPaths) * len(jobs))()
         self._check(self._lib.kk_batch_walk(self._h, arr, len(jobs), outs))
         res = []
         try:
             for p in outs:
-                res.append(PathSet(*_capi.paths_to_numpy(p.contents)))
+                if keep_paths:
+                    res.append(PathSet(*_capi.paths_to_numpy(p.contents)))
+                else:
+                    c = p.contents
+                    res.append({"walker_num": int(c.walker_num), "total_steps": int(c.total_steps),
+                                "vertices": int(c.total_steps) + int(c.walker_num)})
         finally:
             for p in outs:
                 if p:

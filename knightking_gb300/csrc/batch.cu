@@ -444,45 +444,56 @@ kk_status kk_batch_walk(kk_engine *e, const kk_walk_opts *jobs, int n_jobs, kk_p
         e->alias_ms = slot.alias_ms;
         e->walk_ms = slot.walk_ms;
         const uint32_t *len = (const uint32_t *)slot.length.p, *path = (const uint32_t *)slot.path.p;
-        std::vector<uint32_t> h_len(plan.total + 1);
-        KK_CUDA_CHECK(cudaMemcpy(h_len.data(), len, (size_t)plan.total * 4, cudaMemcpyDeviceToHost));
+        /* all jobs packed in one pass, then every job's lengths, offsets and
+         * vertices copied straight into a pooled pinned block, one wait */
+        std::vector<uint64_t> jb;
+        const uint64_t *d_rel = nullptr;
+        const uint32_t *d_verts = nullptr;
+        pack_batch_paths(e, plan, (const BatchJob *)slot.jobs.p, len, path, &d_rel, &d_verts, jb);
+        if (e->host_pool == nullptr)
+        {
+            e->host_pool = new HostPool();
+            e->host_pool->limit = kBatchPoolCache;
+        }
         for (int j = 0; j < n_jobs; j++)
         {
             const BatchJob &b = plan.jobs[j];
+            const uint32_t n = b.walker_num;
+            const uint64_t total = jb[j + 1] - jb[j];
+            const size_t len_bytes = ((size_t)n * 4 + 15) & ~(size_t)15;
+            const size_t off_bytes = ((size_t)n * 8 + 15) & ~(size_t)15;
             kk_paths *p = (kk_paths *)calloc(1, sizeof(kk_paths));
-            if (!p)
+            PooledPaths *o = new (std::nothrow) PooledPaths();
+            size_t cls = 0;
+            char *blk = (p && o) ? (char *)e->host_pool->get(len_bytes + off_bytes + total * 4 + 16, &cls) : nullptr;
+            if (!blk)
+            {
+                free(p);
+                delete o;
                 fail(KK_ERR_OOM, "host allocation failed");
+            }
+            o->pool = e->host_pool;
+            o->block = blk;
+            o->cls = cls;
+            p->owner = o;
             out[j] = p;
-            p->walker_num = b.walker_num;
+            p->walker_num = n;
             p->walker_begin = b.walker_begin;
-            p->epoch_walkers = b.walker_num;
-            uint64_t total = 0;
-            for (uint32_t i = 0; i < b.walker_num; i++)
-                total += h_len[b.first_task + i];
-            p->total_steps = total - b.walker_num;
-            p->length = (uint32_t *)malloc((size_t)b.walker_num * 4 + 4);
-            p->offset = (uint64_t *)malloc((size_t)b.walker_num * 8 + 8);
-            p->vertices = (uint32_t *)malloc(total * 4 + 4);
-            if (!p->length || !p->offset || !p->vertices)
-                fail(KK_ERR_OOM, "host allocation failed");
-            memcpy(p->length, h_len.data() + b.first_task, (size_t)b.walker_num * 4);
-            if (b.walker_num == 0)
+            p->epoch_walkers = n;
+            p->total_steps = total - n;
+            p->length = (uint32_t *)blk;
+            p->offset = (uint64_t *)(blk + len_bytes);
+            p->vertices = (uint32_t *)(blk + len_bytes + off_bytes);
+            if (n == 0)
                 continue;
-            WalkResult r;
-            r.walker_num = b.walker_num;
-            r.length = const_cast<uint32_t *>(len) + b.first_task;
-            r.path_off = nullptr;
-            r.cap = b.cap;
-            r.path = const_cast<uint32_t *>(path) + b.path_base;
-            r.total_steps = p->total_steps;
-            uint64_t *d_off;
-            uint32_t *d_verts;
-            pack_walk_paths(e, r, &d_off, &d_verts);
-            KK_CUDA_CHECK(cudaMemcpyAsync(p->offset, d_off, (size_t)b.walker_num * 8, cudaMemcpyDeviceToHost,
+            KK_CUDA_CHECK(cudaMemcpyAsync(p->length, len + b.first_task, (size_t)n * 4, cudaMemcpyDeviceToHost,
                                           e->stream));
-            KK_CUDA_CHECK(cudaMemcpyAsync(p->vertices, d_verts, total * 4, cudaMemcpyDeviceToHost, e->stream));
-            KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+            KK_CUDA_CHECK(cudaMemcpyAsync(p->offset, d_rel + b.first_task, (size_t)n * 8, cudaMemcpyDeviceToHost,
+                                          e->stream));
+            KK_CUDA_CHECK(cudaMemcpyAsync(p->vertices, d_verts + jb[j], total * 4, cudaMemcpyDeviceToHost,
+                                          e->stream));
         }
+        KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
     });
     if (s != KK_OK)
     {

@@ -93,6 +93,46 @@ __global__ void words_to_host_kernel(const uint32_t *src, volatile uint32_t *dst
         dst[threadIdx.x] = src[threadIdx.x];
 }
 
+/* Position of each batch job's first vertex in the packed output:
+ * out[j] = off[first_task_j], out[nj] = off[total]. */
+__global__ void job_begin_kernel(const BatchJob *jobs, uint32_t nj, uint32_t total, const uint64_t *off,
+                                 uint64_t *out)
+{
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j <= nj; j += gridDim.x * blockDim.x)
+        out[j] = off[j < nj ? jobs[j].first_task : total];
+}
+
+/* One warp per walker of a batch: finds the walker's job (binary search over
+ * the jobs' first positions), copies its path from the batch layout (job
+ * base + i * cap) to its packed offset, and writes the offset counted from
+ * the job's first vertex. */
+__global__ void pack_batch_kernel(const BatchJob *jobs, uint32_t nj, uint32_t total, const uint32_t *length,
+                                  const uint32_t *path, const uint64_t *off, uint32_t *out, uint64_t *rel)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < total; t += nwarps)
+    {
+        uint32_t lo = 0, hi = nj;
+        while (hi - lo > 1)
+        {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (jobs[mid].first_task <= t)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        const BatchJob &b = jobs[lo];
+        const uint64_t s = b.path_base + (uint64_t)(t - b.first_task) * b.cap;
+        const uint64_t d = off[t];
+        const uint32_t len = length[t];
+        for (uint32_t k = lane; k < len; k += 32)
+            out[d + k] = path[s + k];
+        if (lane == 0)
+            rel[t] = d - off[b.first_task];
+    }
+}
+
 /* Path offsets of the streamed segments: bound[k] = off[min(k << shift, n)]
  * for k = 0..nseg, written to mapped host memory. */
 __global__ void segment_bounds_kernel(const uint64_t *off, uint32_t n, uint32_t shift, uint32_t nseg,
@@ -524,6 +564,37 @@ void words_to_host(kk_engine *e, const uint32_t *src, int at, int n)
     KK_CUDA_CHECK(cudaGetLastError());
 }
 
+void pack_batch_paths(kk_engine *e, const BatchPlan &plan, const BatchJob *d_jobs, const uint32_t *length,
+                      const uint32_t *path, const uint64_t **d_rel, const uint32_t **d_verts,
+                      std::vector<uint64_t> &job_begin)
+{
+    const uint32_t n = plan.total;
+    const uint32_t nj = (uint32_t)plan.jobs.size();
+    uint64_t *lens64 = e->caps.as<uint64_t>((uint64_t)n + 1);
+    uint64_t *off = e->packed_off.as<uint64_t>((uint64_t)n + 1);
+    length_to_u64_kernel<<<grid_for(e, (uint64_t)n + 1, 256), 256, 0, e->stream>>>(length, lens64, n);
+    count_launch(e);
+    exclusive_scan_u64(e, lens64, off, (uint64_t)n + 1);
+    uint64_t *jb = e->batch_small.as<uint64_t>((uint64_t)nj + 1);
+    job_begin_kernel<<<1, 256, 0, e->stream>>>(d_jobs, nj, n, off, jb);
+    count_launch(e);
+    KK_CUDA_CHECK(cudaGetLastError());
+    job_begin.assign((size_t)nj + 1, 0);
+    KK_CUDA_CHECK(cudaMemcpyAsync(job_begin.data(), jb, ((size_t)nj + 1) * 8, cudaMemcpyDeviceToHost, e->stream));
+    KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+    uint32_t *verts = e->packed.as<uint32_t>(job_begin[nj]);
+    uint64_t *rel = e->batch_rel.as<uint64_t>(n);
+    if (n > 0)
+    {
+        pack_batch_kernel<<<grid_for(e, (uint64_t)n * 32, 256), 256, 0, e->stream>>>(d_jobs, nj, n, length, path, off,
+                                                                                    verts, rel);
+        count_launch(e);
+        KK_CUDA_CHECK(cudaGetLastError());
+    }
+    *d_rel = rel;
+    *d_verts = verts;
+}
+
 uint64_t pack_walk_paths(kk_engine *e, const WalkResult &r, uint64_t **d_off, uint32_t **d_verts)
 {
     return pack_paths(e, r, d_off, d_verts);
@@ -652,6 +723,10 @@ void kk_engine_destroy(kk_engine *e)
     }
     e->alias_next.release();
     e->seg_count.release();
+    e->batch_small.release();
+    e->batch_rel.release();
+    if (e->host_pool)
+        e->host_pool->release();
     e->vcur.release();
     e->edge_set.release();
     e->edge_pos.release();

@@ -94,3 +94,21 @@ def test_batch_rejects_mixed_apps_and_ppr(engine):
         engine.batch_walk("deepwalk", [dict(walker_num=3, weighted=True), dict(walker_num=3, weighted=False)])
     with pytest.raises(kk.KKError):
         engine.batch_walk("ppr", [dict(walker_num=3, terminate_prob=0.1)])
+
+
+def test_batch_results_from_pooled_blocks_across_calls(engine):
+    """kk_batch_walk hands its results out in pooled pinned blocks: blocks
+    returned by one call (kk_paths_free) carry the next call's paths, and the
+    counts-only form frees them without reading."""
+    _load(engine, 7, True)
+    jobs = [dict(walker_num=n, seed=s, walk_length=l, weighted=True, walker_begin=b)
+            for n, s, l, b in ((5000, 11, 40, 0), (0, 12, 9, 0), (777, 13, 3, 123), (1, 14, 100, 9))]
+    first = engine.batch_walk("deepwalk", jobs)
+    counts = engine.batch_walk("deepwalk", jobs, keep_paths=False)
+    again = engine.batch_walk("deepwalk", jobs)
+    for a, b, c, job in zip(first, again, counts, jobs):
+        np.testing.assert_array_equal(a.path_length, b.path_length)
+        np.testing.assert_array_equal(a.vertices, b.vertices)
+        assert c["walker_num"] == job["walker_num"] == a.path_num
+        assert c["total_steps"] == a.total_steps
+        assert c["vertices"] == len(a.vertices)

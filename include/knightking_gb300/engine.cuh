@@ -370,6 +370,10 @@ struct kk_engine
     /* alias_hub_grid (option): blocks of the hub alias kernel (0: one per two
      * SMs); fewer leave more of the SMs to the classes on the main stream */
     int alias_hub_grid = 0;
+    /* alias_streams (option): 1 every class but the hubs on the main stream,
+     * 2 the classes of degree <= 128 after the hubs on the side stream, 3 the
+     * classes of degree <= 512 (default: S22 lognormal build 2.69 -> 2.50 ms) */
+    int alias_streams = 3;
     /* l2_fetch_bytes (option): the context's cudaLimitMaxL2FetchGranularity
      * hint while the engine lives (0: left as found); the value found is put
      * back when the option returns to 0 and when the engine is destroyed. */
@@ -556,7 +560,8 @@ void launch_alias_class(kk_engine *e, K kern, unsigned nt, size_t smem, uint32_t
 
 /* Builds alias tables in the Bucket layout into e->alias/e->sum for a
  * static functor: hubs on the side stream, the other classes in turn on the
- * main stream, every class largest vertex first from its own counter. */
+ * main stream or (alias_streams) the small-row classes after the hubs on the
+ * side stream, every class largest vertex first from its own counter. */
 template <typename TC, typename Bucket = IndexBucket>
 void build_alias(kk_engine *e, const TC &tc)
 {
@@ -593,7 +598,6 @@ void build_alias(kk_engine *e, const TC &tc)
                                                                        e->n_hub, next);
         count_launch(e);
         KK_CUDA_CHECK(cudaGetLastError());
-        KK_CUDA_CHECK(cudaEventRecord(e->ev_join, e->side));
     }
     /* 4097..16384: the hub kernel in 256-thread blocks */
     {
@@ -616,21 +620,40 @@ void build_alias(kk_engine *e, const TC &tc)
                            });
     }
     /* 1..2048: lane groups, 32/G vertices per warp */
-    auto group = [&](auto kern, uint32_t G, size_t smem, int c, int &res) {
+    auto group = [&](auto kern, uint32_t G, size_t smem, int c, int &res, cudaStream_t s) {
         launch_alias_class(e, kern, 32, smem, 32 / G, t[c - 1], t[c], res, [&](unsigned grid) {
-            kern<<<grid, 32, smem, st>>>(g, tc, alias, vcur, sum, rows, t[c - 1], t[c], next + c);
+            kern<<<grid, 32, smem, s>>>(g, tc, alias, vcur, sum, rows, t[c - 1], t[c], next + c);
             count_launch(e);
         });
     };
+    /* alias_streams 2: the classes of degree <= 128 (2.5 to 5 KB of shared
+     * memory per warp) follow the hubs on the side stream and share the SMs
+     * with the classes of large rows (10 to 48 KB per warp or block); 3: the
+     * class 129..512 with them */
+    const bool split = e->alias_streams >= 2;
+    cudaStream_t light = st;
+    if (split)
+    {
+        if (!e->n_hub)
+        {
+            KK_CUDA_CHECK(cudaEventRecord(e->ev_fork, e->stream));
+            KK_CUDA_CHECK(cudaStreamWaitEvent(e->side, e->ev_fork, 0));
+        }
+        light = e->side;
+    }
     static int r3 = 0, r4 = 0, r5 = 0, r6 = 0, r7 = 0, r8 = 0;
-    group(alias_group_kernel<TC, Bucket, 32, 2048>, 32, alias_group_smem_per_warp<32, 2048>(), 3, r3);
-    group(alias_group_kernel<TC, Bucket, 32, 1024>, 32, alias_group_smem_per_warp<32, 1024>(), 4, r4);
-    group(alias_group_kernel<TC, Bucket, 16, 512>, 16, alias_group_smem_per_warp<16, 512>(), 5, r5);
-    group(alias_group_kernel<TC, Bucket, 8, 128>, 8, alias_group_smem_per_warp<8, 128>(), 6, r6);
-    group(alias_group_kernel<TC, Bucket, 4, 32>, 4, alias_group_smem_per_warp<4, 32>(), 7, r7);
-    group(alias_group_kernel<TC, Bucket, 2, 16>, 2, alias_group_smem_per_warp<2, 16>(), 8, r8);
-    if (e->n_hub)
+    group(alias_group_kernel<TC, Bucket, 32, 2048>, 32, alias_group_smem_per_warp<32, 2048>(), 3, r3, st);
+    group(alias_group_kernel<TC, Bucket, 32, 1024>, 32, alias_group_smem_per_warp<32, 1024>(), 4, r4, st);
+    group(alias_group_kernel<TC, Bucket, 16, 512>, 16, alias_group_smem_per_warp<16, 512>(), 5, r5,
+          e->alias_streams == 3 ? light : st);
+    group(alias_group_kernel<TC, Bucket, 8, 128>, 8, alias_group_smem_per_warp<8, 128>(), 6, r6, light);
+    group(alias_group_kernel<TC, Bucket, 4, 32>, 4, alias_group_smem_per_warp<4, 32>(), 7, r7, light);
+    group(alias_group_kernel<TC, Bucket, 2, 16>, 2, alias_group_smem_per_warp<2, 16>(), 8, r8, light);
+    if (e->n_hub || split)
+    {
+        KK_CUDA_CHECK(cudaEventRecord(e->ev_join, e->side));
         KK_CUDA_CHECK(cudaStreamWaitEvent(e->stream, e->ev_join, 0));
+    }
     if constexpr (weight_tables)
     {
         if (tc.static_comp.w == e->d_w)

@@ -783,6 +783,8 @@ kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value)
             e->cursor_adjacency = (int)value;
         else if (n == "alias_hub_grid" && value >= 0 && value <= 4096)
             e->alias_hub_grid = (int)value;
+        else if (n == "alias_streams" && value >= 1 && value <= 3)
+            e->alias_streams = (int)value;
         else if (n == "walk_multi" && (value == 1 || value == 2 || value == 4))
             e->walk_multi = (int)value;
         else

@@ -1,7 +1,8 @@
 """Autotuner of the engine's speed options.
 
 The options (kk_engine_set_option) never change a path, only how fast it is
-produced: alias-table layout, node2vec adjacency test, walk block size,
+produced: alias-table layout, the alias build's stream split, node2vec
+adjacency test, walk block size,
 walkers per thread, the context's L2 fetch-granularity hint, the walk schedule
 and the cursor adjacency of uniform walks.  The tuner runs a
 caller-supplied step (one walk call on the real workload) under candidate
@@ -12,6 +13,7 @@ descent: each option in turn, the others held at their best so far).
 
 DEFAULT_SPACE = (
     ("alias_layout", (0, 1)),
+    ("alias_streams", (3, 2, 1)),
     ("node2vec_adjacency", (0, 1)),
     ("walk_block", (256, 128, 64)),
     ("walk_multi", (1, 2, 4)),
@@ -26,7 +28,7 @@ def space_for(app, weighted):
     alias tables, the adjacency test only for node2vec."""
     out = []
     for name, vals in DEFAULT_SPACE:
-        if name == "alias_layout" and not weighted:
+        if name in ("alias_layout", "alias_streams") and not weighted:
             continue
         if name == "node2vec_adjacency" and app != "node2vec":
             continue

@@ -326,16 +326,23 @@ def _compare_alias(engine, oracle_lib, V, off, nbr, w):
     np.testing.assert_array_equal(s.view(np.uint32), osum.view(np.uint32))
 
 
+@pytest.mark.parametrize("streams", [1, 2, 3])
 @pytest.mark.parametrize("weights", [1, 2])
-def test_alias_tables_match_oracle_rmat16(engine, oracle_lib, weights):
+def test_alias_tables_match_oracle_rmat16(engine, oracle_lib, weights, streams):
+    """R-MAT scale 16 has no hub above degree 16384: with alias_streams 2 the
+    side stream runs the light classes alone."""
     engine.generate_rmat(16, 16, seed=3, weights=weights)
     g = engine.download_graph()
-    _compare_alias(engine, oracle_lib, g["V"], g["off"], g["nbr"], g["w"])
+    engine.set_option("alias_streams", streams)
+    try:
+        _compare_alias(engine, oracle_lib, g["V"], g["off"], g["nbr"], g["w"])
+    finally:
+        engine.set_option("alias_streams", 3)
 
 
-@pytest.mark.parametrize("hub_grid", [0, 2])
+@pytest.mark.parametrize("hub_grid,streams", [(0, 1), (2, 1), (0, 2), (0, 3), (2, 3)])
 @pytest.mark.parametrize("dist", ["lognormal", "pareto", "uniform", "equal", "twovalue"])
-def test_alias_tables_match_oracle_hubs(engine, oracle_lib, dist, hub_grid):
+def test_alias_tables_match_oracle_hubs(engine, oracle_lib, dist, hub_grid, streams):
     """Every build class and both sides of every class boundary: hubs (40000,
     20000, 16385), 4097..16384 (block per vertex, queues in the scratch),
     2049..4096 (block per vertex, shared memory), 1..2048 (lane groups of 32,
@@ -364,7 +371,9 @@ def test_alias_tables_match_oracle_hubs(engine, oracle_lib, dist, hub_grid):
     w = w.astype(np.float32)
     engine.load_arrays(V, off, nbr, w)
     engine.set_option("alias_hub_grid", hub_grid)
+    engine.set_option("alias_streams", streams)
     try:
         _compare_alias(engine, oracle_lib, V, off, nbr, w)
     finally:
         engine.set_option("alias_hub_grid", 0)
+        engine.set_option("alias_streams", 3)

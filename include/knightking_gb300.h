@@ -114,6 +114,10 @@ kk_status kk_engine_set_stream(kk_engine *e, void *stream);
  *                        lives: 32, 64, 128, or 0 for the value found (restored on destroy)
  *   "walk_stats"         1 counts trials, queries and probes (kk_last_walk_stats)
  *   "walk_multi"         walkers per thread (1, 2, 4) of first-order walks without a dynamic component
+ *   "walk_park"          first-order walks with a dynamic component (rejection trials), one walker per
+ *                        thread: once fewer than this many lanes of a warp are walking, its walkers stop
+ *                        at their next step boundary and later launches resume them 32 to a warp
+ *                        (0 off, 1..32; default 20)
  *   "alias_hub_grid"     blocks of the hub alias kernel (0: one per two SMs)
  *   "alias_streams"      1 the alias classes of degree <= 16384 in turn on the engine's stream,
  *                        2 those of degree <= 128 after the hubs on a second stream, beside the rest,
@@ -122,9 +126,9 @@ kk_status kk_engine_set_stream(kk_engine *e, void *stream);
  *                        run (DeepWalk, PPR, node2vec on graphs without reachable dead ends) in one
  *                        launch per epoch and copies each segment of walkers out as soon as its
  *                        last walker finishes; 0: walker chunks for every walk (into_chunks)
- *   "into_chunks"        kk_walk_into walks that are not streamed run in up to this many walker
- *                        chunks (>= 2^18 walkers each), copying each chunk's paths out while the
- *                        next chunk walks (default 6; 1 = whole)
+ *   "into_chunks"        kk_walk_into walks that are not streamed (metapath excepted: one chunk) run in
+ *                        up to this many walker chunks (>= 2^18 walkers each), copying each chunk's
+ *                        paths out while the next chunk walks (default 6; 1 = whole)
  *   "cursor_adjacency"   1 uniform picks read a per-graph adjacency copy holding each neighbour's
  *                        position (16 B/edge, built on first use): one dependent read per step */
 kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value);

@@ -1205,7 +1205,19 @@ struct WalkLaunch
     uint32_t *seg_count = nullptr;
     volatile uint32_t *seg_flag = nullptr;
     uint32_t seg_shift = 0;
+    /* parking (first-order walks with rejection trials): once fewer than
+     * park_below of a warp's lanes are still walking, each of them stops at
+     * its next step boundary and is appended to park (a ParkedWalker<S>
+     * array, park_count entries), so that the warp ends and a later launch
+     * resumes the stragglers 32 to a warp.  park == nullptr: no parking. */
+    void *park = nullptr;
+    uint32_t *park_count = nullptr;
+    uint32_t park_below = 0;
 };
+
+/* Trials each lane runs on its own between a parking warp's ballots (metapath
+ * S22: 1 -> 16.8 ms, 8 -> 13.6 ms, 16 -> 13.7 ms per walk). */
+constexpr uint32_t kParkCheck = 8;
 
 /* Walker i has written its whole path and its length.  The lanes that end a
  * walker of the same segment together are counted by one of them (a counter
@@ -1681,6 +1693,133 @@ __device__ __forceinline__ bool walk_trial(const GraphView &g, const WC &wc, con
     return true;
 }
 
+/* A walker stopped at a step boundary between launches (first-order walks):
+ * its position i in the launch, the vertex it stands on, its step, its path
+ * length so far and its state.  The stream is keyed by (walker, step), so
+ * a walk resumed from this record draws and writes what it would have. */
+template <typename S>
+struct ParkedWalker
+{
+    uint32_t i;
+    vertex_id_t v;
+    step_t step;
+    uint32_t len;
+    S data;
+};
+
+/* Walks that park: first order with rejection trials (a step takes a
+ * geometric number of trials and a walk may end at any step, so the lanes
+ * of a warp finish far apart). */
+template <typename TC>
+constexpr bool parks()
+{
+    return TC::order == 1 && TC::has_dynamic;
+}
+
+/* Ends walker i's record in the launch: its length, its segment count, its
+ * steps and access counts. */
+template <typename S>
+__device__ __forceinline__ void walk_finish(const WalkLaunch &L, uint32_t i, const WalkerRun<S> &run,
+                                            unsigned long long &my_steps, WalkCounts &counts)
+{
+    L.length[i] = run.len;
+    segment_done(L, i);
+    my_steps += run.len - 1;
+    counts.add(run);
+}
+
+/* Restores parked walker i (its record pw) of launch L at its step boundary. */
+template <typename S>
+__device__ __forceinline__ void resume_run(const WalkLaunch &L, uint32_t i, const ParkedWalker<S> &pw,
+                                           WalkerRun<S> &run)
+{
+    run.w.id = L.walker_begin + i;
+    run.w.step = pw.step;
+    run.w.data = pw.data;
+    run.v = pw.v;
+    run.pos = Pos{-1, 0};
+    run.pv = kNone;
+    run.ppos = Pos{-1, 0};
+    const uint64_t pbase = L.path_off ? L.path_off[i] : (uint64_t)i * L.cap;
+    run.cap = L.path_off ? (uint32_t)(L.path_off[i + 1] - pbase) : L.cap;
+    run.out = L.path ? L.path + pbase : nullptr;
+    run.len = pw.len;
+    run.in_step = run.need_ext = run.ob_known = false;
+    run.step_trials = 0;
+    run.ob_c = 0.0f;
+    run.on_c = 0;
+    run.trials = run.queries = run.probes = 0;
+}
+
+/* Runs the warp's walkers (alive: lane holds walker i) to their ends, or,
+ * with parking on, until fewer than L.park_below lanes are walking; then each
+ * lane still walking finishes its step and parks (record under park_id),
+ * once it has taken a step in this launch (so every launch moves every walker
+ * it holds).  Every lane of the warp calls it with the same L.park and
+ * L.park_below (the ballots take the full warp). */
+template <typename S, typename WC, typename TC, typename Bucket>
+__device__ __forceinline__ void walk_lanes(const GraphView &g, const WC &wc, const TC &tc, const Bucket *alias,
+                                           const float *ra, const WalkLaunch &L, bool alive, uint32_t i,
+                                           WalkerRun<S> &run, Sampler &rng, unsigned long long &my_steps,
+                                           WalkCounts &counts, uint32_t park_id)
+{
+    /* between the warp's ballots each lane runs up to kParkCheck trials on
+     * its own, so lanes in different phases of a step overlap their reads (a
+     * ballot per trial forces the warp to reconverge every trial: 16.8 vs
+     * 13.6 ms); a lane that may park stops at its step boundary.  Without
+     * parking one pass runs every walk to its end. */
+    const uint32_t check = L.park != nullptr ? kParkCheck : 0xffffffffu;
+    bool parking = false;
+    const step_t step0 = alive ? run.w.step : 0;
+    for (;;)
+    {
+        const unsigned live = __ballot_sync(kFullMask, alive);
+        if (live == 0)
+            return;
+        if (L.park != nullptr)
+        {
+            if ((unsigned)__popc(live) < L.park_below)
+                parking = true;
+            const bool stop = alive && parking && !run.in_step && run.w.step != step0;
+            const unsigned stops = __ballot_sync(kFullMask, stop);
+            if (stops != 0)
+            {
+                const unsigned lane = threadIdx.x & 31;
+                uint32_t base = 0;
+                if (lane == (unsigned)(__ffs(stops) - 1))
+                    base = atomicAdd(L.park_count, (uint32_t)__popc(stops));
+                base = __shfl_sync(kFullMask, base, __ffs(stops) - 1);
+                if (stop)
+                {
+                    ParkedWalker<S> *q = (ParkedWalker<S> *)L.park;
+                    q[base + __popc(stops & ((1u << lane) - 1u))] = ParkedWalker<S>{park_id, run.v, run.w.step,
+                                                                                   run.len, run.w.data};
+                    counts.add(run);
+                    alive = false;
+                }
+            }
+        }
+        bool ended = false;
+        for (uint32_t k = 0; alive && k < check; k++)
+        {
+            if (parking && !run.in_step && run.w.step != step0)
+                break;
+            if (!walk_trial<S>(g, wc, tc, alias, ra, L, run, rng))
+            {
+                ended = true;
+                break;
+            }
+        }
+        /* outside the divergent loop: walk_finish's segment count synchronises
+         * lanes (inside it the walk took 25 instead of 19 ms) */
+        if (ended)
+        {
+            walk_finish<S>(L, i, run, my_steps, counts);
+            alive = false;
+        }
+    }
+}
+
 /* One thread per walker for its whole walk, walker state in registers. */
 template <typename S, typename WC, typename TC, typename Bucket>
 __global__ void __launch_bounds__(256, 4) walk_static_kernel(GraphView g, WC wc, TC tc, const Bucket *alias,
@@ -1693,7 +1832,20 @@ __global__ void __launch_bounds__(256, 4) walk_static_kernel(GraphView g, WC wc,
     for (uint32_t it = 0; it < n_iter; it++)
     {
         const uint32_t i = (it * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
-        if (i < L.walker_num)
+        if constexpr (parks<TC>())
+        {
+            /* every lane takes part in walk_lanes' ballots */
+            const bool alive = i < L.walker_num;
+            Sampler rng;
+            WalkerRun<S> run;
+            if (alive)
+            {
+                rng.init(L.seed);
+                walk_begin<S>(g, wc, L, i, run, rng);
+            }
+            walk_lanes<S>(g, wc, tc, alias, ra, L, alive, i, run, rng, my_steps, counts, i);
+        }
+        else if (i < L.walker_num)
         {
             Sampler rng;
             rng.init(L.seed);
@@ -1702,11 +1854,39 @@ __global__ void __launch_bounds__(256, 4) walk_static_kernel(GraphView g, WC wc,
             while (walk_trial<S>(g, wc, tc, alias, ra, L, run, rng))
             {
             }
-            L.length[i] = run.len;
-            segment_done(L, i);
-            my_steps += run.len - 1;
-            counts.add(run);
+            walk_finish<S>(L, i, run, my_steps, counts);
         }
+    }
+    flush_steps(L.total_steps, my_steps);
+    counts.flush(L.stats);
+}
+
+/* Resumes the walkers parked by the previous launch (*in_count of them),
+ * 32 to a warp, parking again into L.park (or running them to their ends
+ * when L.park is nullptr). */
+template <typename S, typename WC, typename TC, typename Bucket>
+__global__ void __launch_bounds__(256, 4) walk_resume_kernel(GraphView g, WC wc, TC tc, const Bucket *alias,
+                                                          const float *ra, WalkLaunch L,
+                                                          const ParkedWalker<S> *in, const uint32_t *in_count)
+{
+    unsigned long long my_steps = 0;
+    WalkCounts counts;
+    const uint32_t n = *in_count;
+    for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x)
+    {
+        const uint32_t k = b + threadIdx.x;
+        const bool alive = k < n;
+        uint32_t i = 0;
+        Sampler rng;
+        WalkerRun<S> run;
+        if (alive)
+        {
+            const ParkedWalker<S> pw = in[k];
+            i = pw.i;
+            rng.init(L.seed);
+            resume_run<S>(L, i, pw, run);
+        }
+        walk_lanes<S>(g, wc, tc, alias, ra, L, alive, i, run, rng, my_steps, counts, i);
     }
     flush_steps(L.total_steps, my_steps);
     counts.flush(L.stats);
@@ -1954,14 +2134,12 @@ struct BatchJob
  * App::make(job, wc, tc) builds the job's WalkerConfig / TransitionConfig. */
 /* Walker t of a batch: its job (binary search over the jobs' first positions
  * in shared memory), the job's hooks and launch record, the walker started. */
-template <typename S, typename App>
-__device__ __forceinline__ uint32_t batch_walker_begin(const GraphView &g, const App &app, const BatchJob *jobs,
-                                                       const uint32_t *s_first, uint32_t njobs, uint32_t t,
-                                                       const float *alias_sum, uint32_t *path, uint32_t *length,
-                                                       unsigned long long *total_steps, int *status,
-                                                       uint32_t trial_limit, typename App::WC &wc,
-                                                       typename App::TC &tc, WalkLaunch &L, WalkerRun<S> &run,
-                                                       Sampler &rng)
+template <typename App>
+__device__ __forceinline__ uint32_t batch_launch(const App &app, const BatchJob *jobs, const uint32_t *s_first,
+                                                 uint32_t njobs, uint32_t t, const float *alias_sum, uint32_t *path,
+                                                 uint32_t *length, unsigned long long *total_steps, int *status,
+                                                 uint32_t trial_limit, typename App::WC &wc, typename App::TC &tc,
+                                                 WalkLaunch &L)
 {
     uint32_t lo = 0, hi = njobs;
     while (hi - lo > 1)
@@ -1988,11 +2166,34 @@ __device__ __forceinline__ uint32_t batch_walker_begin(const GraphView &g, const
     L.status = status;
     L.trial_limit = trial_limit;
     L.stats = nullptr;
-    const uint32_t i = t - job.first_task;
+    return t - job.first_task;
+}
+
+/* Walker t of a batch started: its job, hooks and launch record, then its walk. */
+template <typename S, typename App>
+__device__ __forceinline__ uint32_t batch_walker_begin(const GraphView &g, const App &app, const BatchJob *jobs,
+                                                       const uint32_t *s_first, uint32_t njobs, uint32_t t,
+                                                       const float *alias_sum, uint32_t *path, uint32_t *length,
+                                                       unsigned long long *total_steps, int *status,
+                                                       uint32_t trial_limit, typename App::WC &wc,
+                                                       typename App::TC &tc, WalkLaunch &L, WalkerRun<S> &run,
+                                                       Sampler &rng)
+{
+    const uint32_t i = batch_launch(app, jobs, s_first, njobs, t, alias_sum, path, length, total_steps, status,
+                                    trial_limit, wc, tc, L);
     rng.init(L.seed);
     walk_begin<S>(g, wc, L, i, run, rng);
     return i;
 }
+
+/* Parking of a batch launch (first-order rejection walks): the queue the
+ * stragglers go to and the lane threshold; out == nullptr: none. */
+struct BatchPark
+{
+    void *out = nullptr;
+    uint32_t *count = nullptr;
+    uint32_t below = 0;
+};
 
 /* One thread per walker over the concatenated walkers of all jobs.
  * App::make(job, wc, tc) builds the job's WalkerConfig / TransitionConfig. */
@@ -2002,7 +2203,7 @@ __global__ void __launch_bounds__(256, 4) walk_batch_kernel(GraphView g, App app
                                                          const float *alias_sum, uint32_t *path, uint32_t *length,
                                                          unsigned long long *total_steps, int *status,
                                                          uint32_t trial_limit, unsigned long long *stats,
-                                                         const uint32_t *hdr)
+                                                         const uint32_t *hdr, BatchPark bp)
 {
     __shared__ uint32_t s_first[kMaxBatchJobs];
     if (hdr != nullptr)
@@ -2021,7 +2222,26 @@ __global__ void __launch_bounds__(256, 4) walk_batch_kernel(GraphView g, App app
     for (uint32_t it = 0; it < n_iter; it++)
     {
         const uint32_t t = (it * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
-        if (t < total)
+        if constexpr (parks<typename App::TC>())
+        {
+            /* every lane takes part in walk_lanes' ballots, with the same
+             * parking fields */
+            typename App::WC wc;
+            typename App::TC tc;
+            WalkLaunch L;
+            L.park = bp.out;
+            L.park_count = bp.count;
+            L.park_below = bp.below;
+            WalkerRun<S> run;
+            Sampler rng;
+            const bool alive = t < total;
+            uint32_t i = 0;
+            if (alive)
+                i = batch_walker_begin<S>(g, app, jobs, s_first, njobs, t, alias_sum, path, length, total_steps,
+                                          status, trial_limit, wc, tc, L, run, rng);
+            walk_lanes<S>(g, wc, tc, alias, nullptr, L, alive, i, run, rng, my_steps, counts, t);
+        }
+        else if (t < total)
         {
             typename App::WC wc;
             typename App::TC tc;
@@ -2037,6 +2257,55 @@ __global__ void __launch_bounds__(256, 4) walk_batch_kernel(GraphView g, App app
             my_steps += run.len - 1;
             counts.add(run);
         }
+    }
+    flush_steps(total_steps, my_steps);
+    counts.flush(stats);
+}
+
+/* Resumes the batch walkers parked by the previous launch (*in_count of
+ * them; a record holds the walker's position t in the batch), 32 to a warp,
+ * parking again into bp (or running them to their ends when bp.out is
+ * nullptr). */
+template <typename S, typename App, typename Bucket>
+__global__ void __launch_bounds__(256, 4) walk_batch_resume_kernel(GraphView g, App app, const BatchJob *jobs,
+                                                                uint32_t njobs, const Bucket *alias,
+                                                                const float *alias_sum, uint32_t *path,
+                                                                uint32_t *length, unsigned long long *total_steps,
+                                                                int *status, uint32_t trial_limit,
+                                                                unsigned long long *stats,
+                                                                const ParkedWalker<S> *in, const uint32_t *in_count,
+                                                                BatchPark bp)
+{
+    __shared__ uint32_t s_first[kMaxBatchJobs];
+    for (uint32_t j = threadIdx.x; j < njobs; j += blockDim.x)
+        s_first[j] = jobs[j].first_task;
+    __syncthreads();
+    unsigned long long my_steps = 0;
+    WalkCounts counts;
+    const uint32_t n = *in_count;
+    for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x)
+    {
+        const uint32_t k = b + threadIdx.x;
+        typename App::WC wc;
+        typename App::TC tc;
+        WalkLaunch L;
+        L.park = bp.out;
+        L.park_count = bp.count;
+        L.park_below = bp.below;
+        WalkerRun<S> run;
+        Sampler rng;
+        const bool alive = k < n;
+        uint32_t i = 0, t = 0;
+        if (alive)
+        {
+            const ParkedWalker<S> pw = in[k];
+            t = pw.i;
+            i = batch_launch(app, jobs, s_first, njobs, t, alias_sum, path, length, total_steps, status, trial_limit,
+                             wc, tc, L);
+            rng.init(L.seed);
+            resume_run<S>(L, i, pw, run);
+        }
+        walk_lanes<S>(g, wc, tc, alias, nullptr, L, alive, i, run, rng, my_steps, counts, t);
     }
     flush_steps(total_steps, my_steps);
     counts.flush(stats);

@@ -119,10 +119,48 @@ void launch_batch_with(kk_engine *e, const App &app, const BatchPlan &plan, Batc
         unsigned grid = grid_for(e, walkers, bs);
         if (hdr && grid > 64u * (unsigned)e->sm_count)
             grid = 64u * (unsigned)e->sm_count; /* grid-stride over whatever the header holds */
+        /* parking (first-order rejection walks) on the engine's own batch
+         * slot only: serving slots replay captured launches and run side by
+         * side, and the queues are the engine's */
+        BatchPark bp;
+        typedef ParkedWalker<typename App::S> PW;
+        PW *q[2] = {nullptr, nullptr};
+        uint32_t *cnt = nullptr;
+        const bool park = parks<TC>() && e->walk_park > 0 && hdr == nullptr && &slot == &e->bslot && plan.total > 0;
+        if (park)
+        {
+            q[0] = e->park[0].as<PW>(plan.total);
+            q[1] = e->park[1].as<PW>(plan.total);
+            cnt = e->park_count.as<uint32_t>(2);
+            KK_CUDA_CHECK(cudaMemsetAsync(cnt, 0, 2 * sizeof(uint32_t), slot.stream));
+            bp.out = q[0];
+            bp.count = cnt;
+            bp.below = (uint32_t)e->walk_park;
+        }
         walk_batch_kernel<typename App::S, App, Bucket><<<grid, bs, 0, slot.stream>>>(
             gv, app, d_jobs, nj, plan.total, alias, (const float *)e->sum.p, *path, length, steps, status,
-            e->trial_limit, st, hdr);
+            e->trial_limit, st, hdr, bp);
         count_launch(e);
+        if (park)
+        {
+            const unsigned rgrid = (unsigned)e->sm_count * (1024u / bs);
+            for (int r = 0; r < kParkRounds; r++)
+            {
+                const int cur = r & 1, nxt = cur ^ 1;
+                KK_CUDA_CHECK(cudaMemsetAsync(cnt + nxt, 0, sizeof(uint32_t), slot.stream));
+                BatchPark br;
+                if (r + 1 < kParkRounds)
+                {
+                    br.out = q[nxt];
+                    br.count = cnt + nxt;
+                    br.below = (uint32_t)e->walk_park;
+                }
+                walk_batch_resume_kernel<typename App::S, App, Bucket><<<rgrid, bs, 0, slot.stream>>>(
+                    gv, app, d_jobs, nj, alias, (const float *)e->sum.p, *path, length, steps, status,
+                    e->trial_limit, st, q[cur], cnt + cur, br);
+                count_launch(e);
+            }
+        }
     }
     else
     {

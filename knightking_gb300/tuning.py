@@ -2,7 +2,7 @@
 
 The options (kk_engine_set_option) never change a path, only how fast it is
 produced: alias-table layout, the alias build's stream split, node2vec
-adjacency test, walk block size,
+adjacency test, walk block size, the parking threshold of rejection walks,
 walkers per thread, the context's L2 fetch-granularity hint, the walk schedule
 and the cursor adjacency of uniform walks.  The tuner runs a
 caller-supplied step (one walk call on the real workload) under candidate
@@ -17,6 +17,7 @@ DEFAULT_SPACE = (
     ("node2vec_adjacency", (0, 1)),
     ("walk_block", (256, 128, 64)),
     ("walk_multi", (1, 2, 4)),
+    ("walk_park", (20, 0, 12, 28)),
     ("l2_fetch_bytes", (0, 64)),
     ("walk_schedule", (0, 1)),
     ("cursor_adjacency", (0, 1)),
@@ -33,6 +34,8 @@ def space_for(app, weighted):
         if name == "node2vec_adjacency" and app != "node2vec":
             continue
         if name == "walk_multi" and app not in ("deepwalk", "ppr"):
+            continue
+        if name == "walk_park" and app != "metapath":
             continue
         if name == "cursor_adjacency" and weighted:
             continue

@@ -377,3 +377,51 @@ def test_alias_tables_match_oracle_hubs(engine, oracle_lib, dist, hub_grid, stre
     finally:
         engine.set_option("alias_hub_grid", 0)
         engine.set_option("alias_streams", 3)
+
+
+@pytest.mark.parametrize("park", [8, 31, 32])
+@pytest.mark.parametrize("i", [7, 8])
+def test_parked_walks_match_oracle(engine, oracle_lib, i, park):
+    """Parking (walk_park): walkers of thinned-out warps stop at a step
+    boundary and later launches resume them; paths, steps and the trial
+    count equal the oracle's and the unparked walk's.  park 32 parks a
+    walker as soon as any lane of its warp has ended."""
+    app, gkw, wkw = FRESH[i]
+    g = G.random_undirected(500, 6000, seed=300 + i, **gkw)
+    csr = G.csr_file_order(500, g["src"], g["dst"], w=g.get("w"), type=g.get("type"))
+    engine.load_arrays(500, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
+    weighted = "w" in csr
+    n = 20000
+    engine.set_option("walk_stats", 1)
+    try:
+        engine.set_option("walk_park", 0)
+        plain = engine.walk(app, n, seed=21, weighted=weighted, **wkw)
+        t_plain = engine.last_stats()[0]
+        engine.set_option("walk_park", park)
+        ps = engine.walk(app, n, seed=21, weighted=weighted, **wkw)
+        t_park = engine.last_stats()[0]
+    finally:
+        engine.set_option("walk_park", 20)
+        engine.set_option("walk_stats", 0)
+    ocsr = oracle_lib.CSR(500, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
+    prm = oracle_lib.make_params(app, seed=21, walker_begin=0, walker_num=n, weighted=weighted, **wkw)
+    lens, verts, steps = oracle_lib.walk(ocsr, prm, cap=4096)
+    np.testing.assert_array_equal(ps.path_length, lens)
+    np.testing.assert_array_equal(ps.vertices, verts)
+    assert ps.total_steps == steps == plain.total_steps
+    assert t_park == t_plain
+
+
+@pytest.mark.parametrize("name", APP_CASES)
+def test_paths_match_reference_parked(engine, name):
+    """The reference's own paths with parking on (metapath parks; the other
+    apps have no rejection trials of the first order and do not)."""
+    case = Case(name)
+    load_case(engine, case)
+    engine.set_option("walk_park", 24)
+    try:
+        ps = gpu_walk(engine, case)
+    finally:
+        engine.set_option("walk_park", 20)
+    np.testing.assert_array_equal(ps.path_length, case.lens)
+    np.testing.assert_array_equal(ps.vertices, case.verts)

@@ -45,8 +45,11 @@ def engine(kk):
     e.close()
 
 
+@pytest.mark.parametrize("park", [0, 20])
 @pytest.mark.parametrize("name", case_ids("case_t200"))
-def test_tagwalk_hooks_match_reference(kk, example, engine, name):
+def test_tagwalk_hooks_match_reference(kk, example, engine, name, park):
+    """park 20: first-order tag walks (rejection trials) park the walkers of
+    thinned-out warps and resume them in later launches (walk_park)."""
     from knightking_gb300 import _capi
     case = Case(name)
     g = case.graph()
@@ -56,9 +59,13 @@ def test_tagwalk_hooks_match_reference(kk, example, engine, name):
                             weighted=kw["weighted"])
     vtag = np.ascontiguousarray(kw["vertex_tag"], dtype=np.int32)
     out = ctypes.POINTER(_capi.KKPaths)()
-    st = example.kk_example_tagwalk(engine._h, ctypes.byref(opts), vtag.ctypes.data, kw["tag_num"],
-                                    kw["vertex_tag_weight"], kw["outlier_amplifier"], kw["order"],
-                                    int(kw["outlier"]), ctypes.byref(out))
+    engine.set_option("walk_park", park)
+    try:
+        st = example.kk_example_tagwalk(engine._h, ctypes.byref(opts), vtag.ctypes.data, kw["tag_num"],
+                                        kw["vertex_tag_weight"], kw["outlier_amplifier"], kw["order"],
+                                        int(kw["outlier"]), ctypes.byref(out))
+    finally:
+        engine.set_option("walk_park", 20)
     assert st == 0, _capi.lib().kk_last_error(engine._h)
     try:
         _, _, lens, _, verts, steps = _capi.paths_to_numpy(out.contents)

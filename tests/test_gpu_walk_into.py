@@ -1,6 +1,7 @@
 """kk_walk_into's two copy-out modes.  Streamed (walks whose path lengths are
 known before they run): one launch per epoch, every segment of walkers copied
-out as soon as its last walker finishes.  Chunked (into_stream 0, metapath,
+out as soon as its last walker finishes.  Metapath: one launch, then packed and
+copied out.  Chunked (into_stream 0,
 graphs with dead ends): chunk c + 1 walks while chunk c's paths are packed and
 copied out.  Whatever the mode, the lengths, offsets and vertices in the
 caller's buffers are the paths kk_walk returns (which the parity tests pin to

@@ -35,3 +35,10 @@ def test_space_for_apps():
     assert "alias_layout" not in names(tuning.space_for("ppr", False))
     assert "node2vec_adjacency" in names(tuning.space_for("node2vec", True))
     assert "node2vec_adjacency" not in names(tuning.space_for("deepwalk", True))
+    # parking applies to first-order rejection walks (metapath), alias stream
+    # splits only to walks with alias tables
+    assert "walk_park" in names(tuning.space_for("metapath", True))
+    assert "walk_park" not in names(tuning.space_for("node2vec", True))
+    assert "walk_park" not in names(tuning.space_for("deepwalk", True))
+    assert "alias_streams" in names(tuning.space_for("deepwalk", True))
+    assert "alias_streams" not in names(tuning.space_for("ppr", False))

@@ -83,11 +83,21 @@ def batch_jobs(wl):
 # 4 B path write is merged by L2 into full sectors (4 B).
 #   alias DeepWalk: 40 + 40 + 32 + 4 = 116;  unweighted PPR: 40 + 32 + 4 = 76.
 B_STEP = {"deepwalk": 40 + 40 + 32 + 4, "ppr": 40 + 32 + 4}
-# Bytes this engine's layout touches per step: alias DeepWalk reads one 32 B
-# cursor bucket (candidate, neighbour and the neighbour's adjacency position)
-# plus the path write; unweighted PPR reads the offset pair, the neighbour id
-# and writes the path.
-DESIGN_B_STEP = {"deepwalk": 32 + 4, "ppr": 40 + 32 + 4}
+
+
+def design_bytes_per_step(app, best):
+    """Bytes this engine's layout touches per step, at 32 B sectors, under the
+    tuned options.  Alias DeepWalk: a cursor bucket (layout 0) carries the next
+    vertex and its adjacency position, so a step reads one 32 B sector; index
+    or 16 B neighbour buckets (layouts 1, 2) add the next vertex's offset pair
+    (40 B, in L2 while the offsets fit).  Unweighted PPR: a cursor-adjacency
+    entry (one sector) or the offset pair and the neighbour id.  Each adds the
+    4 B path write."""
+    if app == "deepwalk":
+        return 32 + 4 if best.get("alias_layout", 2) == 0 else 32 + 40 + 4
+    if app == "ppr":
+        return 32 + 4 if best.get("cursor_adjacency", 0) else 40 + 32 + 4
+    return None
 
 
 def load_peaks():
@@ -658,7 +668,7 @@ def run_ours(args, wl, world, rank, local):
     peak, peak_kind = load_peaks()
     steps_per_launch = total_steps / args.steps
     b_step = B_STEP.get(app)
-    design_b = DESIGN_B_STEP.get(app)
+    design_b = design_bytes_per_step(app, best)
     counts = None
     if app in ("node2vec", "metapath"):
         # one counted walk after the timed region (same paths): trials per step

@@ -105,7 +105,8 @@ kk_status kk_engine_set_stream(kk_engine *e, void *stream);
  *   "walk_block"         threads per block of the walk kernels, 32..256 step 32 (default 256)
  *   "trial_limit"        rejection trials per step before KK_ERR_TRIAL_LIMIT (default 2^24)
  *   "alias_layout"       0 cursor buckets where no hook reads the taken edge's index
- *                        (a step reads one 32 B bucket), 1 index buckets always
+ *                        (a step reads one 32 B bucket), 1 index buckets always, 2 (default) 16 B
+ *                        neighbour buckets where no hook reads the edge index (half the bytes to build)
  *   "alias_cache"        1 keeps the built-in apps' edge-weight alias tables across calls
  *                        (the reference rebuilds them per call; the tables are the same)
  *   "node2vec_adjacency" 0 edge-set lookup (built once per graph), 1 binary search of the

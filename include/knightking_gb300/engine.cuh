@@ -365,8 +365,9 @@ struct kk_engine
     int walk_stats = 0;
     uint64_t last_stats[3] = {0, 0, 0};
     /* alias-table layout: 0 cursor buckets where the hooks allow them, 1 index
-     * buckets always */
-    int alias_layout = 0;
+     * buckets always, 2 (default) 16 B neighbour buckets where the hooks allow
+     * them (DeepWalk S22: build 2.50 -> 2.25 ms, walk 5.71 -> 5.06 ms) */
+    int alias_layout = 2;
     /* alias_cache (option): keep the edge-weight alias tables of the built-in
      * apps across calls instead of rebuilding them per call as the reference
      * does (same tables either way).  alias_cached: layout the tables in
@@ -575,7 +576,7 @@ template <typename TC, typename Bucket = IndexBucket>
 void build_alias(kk_engine *e, const TC &tc)
 {
     constexpr bool weight_tables = std::is_same<typename TC::static_type, apps::WeightStatic>::value;
-    const int layout = Bucket::cursor ? 0 : 1;
+    const int layout = Bucket::cursor ? 0 : (Bucket::compact ? 2 : 1);
     if constexpr (weight_tables)
     {
         if (e->alias_cache && e->alias_cached == layout && tc.static_comp.w == e->d_w)
@@ -887,7 +888,8 @@ launched:
 }
 
 /* Runs a walk with the alias-table layout the engine's alias_layout option
- * picks: cursor buckets where the hooks allow them (auto), or index buckets. */
+ * picks: where no hook reads the taken edge's index, cursor buckets (0) or
+ * 16 B neighbour buckets (2); else index buckets. */
 template <typename S, typename WC, typename TC>
 void run_walk(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, WalkResult &res)
 {
@@ -896,6 +898,11 @@ void run_walk(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, WalkR
         if (e->alias_layout == 0)
         {
             run_walk_with<S, WC, TC, CursorBucket>(e, wc, tc, rs, res);
+            return;
+        }
+        if (e->alias_layout == 2)
+        {
+            run_walk_with<S, WC, TC, NeighbourBucket>(e, wc, tc, rs, res);
             return;
         }
     }

@@ -302,7 +302,7 @@ static __global__ void adj_cursor_kernel(GraphView g, const uint64_t *cur, uint4
 }
 
 /* One alias bucket (AliasBucket, include/walk.hpp:52-57), in one of two 32 B
- * layouts (one DRAM sector each):
+ * layouts (one DRAM sector each) or a 16 B one:
  *
  * IndexBucket: p, p_idx, q_idx (indices local to the vertex's adjacency;
  *   q_idx == kNone is the reference's q_ptr == nullptr) and the two edges'
@@ -310,7 +310,10 @@ static __global__ void adj_cursor_kernel(GraphView g, const uint64_t *cur, uint4
  *   dependent gather.  Used when a hook reads the taken edge's index.
  * CursorBucket: p, the two neighbours (q_nbr == kNone: no alias) and their
  *   vertex cursors; used when no hook reads the edge index, so one 32 B read
- *   per step gives the next vertex and its adjacency position. */
+ *   per step gives the next vertex and its adjacency position.
+ * NeighbourBucket: p and the two neighbours, 16 B; used when no hook reads
+ *   the edge index.  The build writes half the bytes, and a step reads the
+ *   next vertex's offsets (in L2 while they fit) besides the bucket. */
 struct __align__(32) IndexBucket
 {
     float p;
@@ -323,6 +326,7 @@ struct __align__(32) IndexBucket
     uint32_t pad2;
 
     static constexpr bool cursor = false;
+    static constexpr bool compact = false;
     /* pn, qn: the neighbours of edges pi, qi (qn unused when qi == kNone);
      * ty: the row's edge types, stored as type | 0x100 in pad1 / pad2 so a
      * pick also knows its candidate's type (nullptr: no types) */
@@ -355,6 +359,7 @@ struct __align__(32) CursorBucket
     uint64_t q_cur;
 
     static constexpr bool cursor = true;
+    static constexpr bool compact = false;
     __device__ __forceinline__ static CursorBucket make_n(float p, uint32_t, uint32_t qi, uint32_t pn, uint32_t qn,
                                                           const uint64_t *vcur, const uint8_t *)
     {
@@ -368,7 +373,28 @@ struct __align__(32) CursorBucket
         return make_n(p, pi, qi, nb[pi], qi == kNone ? kNone : nb[qi], vcur, ty);
     }
 };
+struct __align__(16) NeighbourBucket
+{
+    float p;
+    uint32_t p_nbr;
+    uint32_t q_nbr;
+    uint32_t pad0;
+
+    static constexpr bool cursor = false;
+    static constexpr bool compact = true;
+    __device__ __forceinline__ static NeighbourBucket make_n(float p, uint32_t, uint32_t qi, uint32_t pn, uint32_t qn,
+                                                             const uint64_t *, const uint8_t *)
+    {
+        return NeighbourBucket{p, pn, qi == kNone ? kNone : qn, 0};
+    }
+    __device__ __forceinline__ static NeighbourBucket make(float p, uint32_t pi, uint32_t qi, const uint32_t *nb,
+                                                           const uint64_t *vcur, const uint8_t *ty)
+    {
+        return make_n(p, pi, qi, nb[pi], qi == kNone ? kNone : nb[qi], vcur, ty);
+    }
+};
 static_assert(sizeof(IndexBucket) == 32 && sizeof(CursorBucket) == 32, "one sector per bucket");
+static_assert(sizeof(NeighbourBucket) == 16, "two buckets per sector");
 typedef IndexBucket AliasBucket;
 
 /* Whether a hook reads the index of the edge it is given: hooks declare
@@ -1322,7 +1348,15 @@ struct Cand
 template <typename TC, typename Bucket>
 __device__ __forceinline__ Cand pick_candidate(const GraphView &g, const Bucket *alias, const Pos &pos, Sampler &rng)
 {
-    if constexpr (TC::has_static)
+    if constexpr (TC::has_static && Bucket::compact)
+    {
+        /* b = {p, p_nbr, q_nbr, -} */
+        const uint4 b = gather(reinterpret_cast<const uint4 *>(alias + pos.e0 + rng.gen(pos.deg)));
+        if (b.z == kNone || rng.gen_float(1.0f) < __uint_as_float(b.x))
+            return Cand{kNone, b.y, 0, false, 0};
+        return Cand{kNone, b.z, 0, false, 0};
+    }
+    else if constexpr (TC::has_static)
     {
         const uint4 *b4 = reinterpret_cast<const uint4 *>(alias + pos.e0 + rng.gen(pos.deg));
         const uint4 lo = gather(b4), hi = gather(b4 + 1);
@@ -1988,7 +2022,8 @@ __global__ void __launch_bounds__(256, 4) walk_multi_kernel(GraphView g, WC wc, 
             {
                 const uint4 *b4 = reinterpret_cast<const uint4 *>(alias + pos.e0 + c[k]);
                 lo[k] = gather(b4);
-                hi[k] = gather(b4 + 1);
+                if constexpr (!Bucket::compact)
+                    hi[k] = gather(b4 + 1);
             }
             else
             {
@@ -2004,7 +2039,14 @@ __global__ void __launch_bounds__(256, 4) walk_multi_kernel(GraphView g, WC wc, 
             Cand ac;
             if constexpr (TC::has_static)
             {
-                if constexpr (Bucket::cursor)
+                if constexpr (Bucket::compact)
+                {
+                    if (lo[k].z == kNone || rng[k].gen_float(1.0f) < __uint_as_float(lo[k].x))
+                        ac = Cand{kNone, lo[k].y, 0, false, 0};
+                    else
+                        ac = Cand{kNone, lo[k].z, 0, false, 0};
+                }
+                else if constexpr (Bucket::cursor)
                 {
                     if (lo[k].z == kNone || rng[k].gen_float(1.0f) < __uint_as_float(lo[k].x))
                         ac = Cand{kNone, lo[k].y, ((uint64_t)hi[k].y << 32) | hi[k].x, true, 0};

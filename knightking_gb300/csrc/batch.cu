@@ -181,11 +181,14 @@ void launch_batch_with(kk_engine *e, const App &app, const BatchPlan &plan, Batc
 }
 
 /* The alias layout the engine's alias_layout option picks for the app:
- * cursor buckets where the app's hooks allow them, else index buckets. */
+ * where the app's hooks allow them, cursor (0) or 16 B neighbour (2)
+ * buckets; else index buckets (1). */
 template <typename App>
-bool app_uses_cursor(const kk_engine *e)
+int app_layout(const kk_engine *e)
 {
-    return use_cursor_buckets<typename App::WC, typename App::TC>() && e->alias_layout == 0;
+    if (use_cursor_buckets<typename App::WC, typename App::TC>() && e->alias_layout != 1)
+        return e->alias_layout;
+    return 1;
 }
 
 template <typename App>
@@ -195,10 +198,16 @@ void launch_batch(kk_engine *e, const App &app, const BatchPlan &plan, BatchSlot
 {
     if constexpr (use_cursor_buckets<typename App::WC, typename App::TC>())
     {
-        if (app_uses_cursor<App>(e))
+        if (app_layout<App>(e) == 0)
         {
             launch_batch_with<App, CursorBucket>(e, app, plan, slot, d_jobs, length, path, steps, status,
                                                  want_paths, prepared, hdr);
+            return;
+        }
+        if (app_layout<App>(e) == 2)
+        {
+            launch_batch_with<App, NeighbourBucket>(e, app, plan, slot, d_jobs, length, path, steps, status,
+                                                    want_paths, prepared, hdr);
             return;
         }
     }
@@ -255,8 +264,11 @@ void prepare_tables(kk_engine *e)
 {
     TransitionConfig<EmptyData, FixedLengthExt<EmptyData>, WeightStatic> stc;
     stc.static_comp = WeightStatic{e->d_w};
-    if (app_uses_cursor<App>(e))
+    const int layout = app_layout<App>(e);
+    if (layout == 0)
         build_alias<decltype(stc), CursorBucket>(e, stc);
+    else if (layout == 2)
+        build_alias<decltype(stc), NeighbourBucket>(e, stc);
     else
         build_alias<decltype(stc), IndexBucket>(e, stc);
 }

@@ -769,7 +769,7 @@ kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value)
             e->walk_blocks_per_sm = (int)value;
         else if (n == "trial_limit" && value >= 1 && value <= 0xffffffffLL)
             e->trial_limit = (uint32_t)value;
-        else if (n == "alias_layout" && (value == 0 || value == 1))
+        else if (n == "alias_layout" && value >= 0 && value <= 2)
             e->alias_layout = (int)value;
         else if (n == "alias_cache" && (value == 0 || value == 1))
             e->alias_cache = (int)value;

@@ -79,12 +79,17 @@ def test_metapath_batch_equals_single_jobs(engine, weighted):
     _check(engine, "metapath", jobs)
 
 
-@pytest.mark.parametrize("weighted", [True, False])
-def test_deepwalk_batch_equals_single_jobs(engine, weighted):
+@pytest.mark.parametrize("weighted,layout", [(True, 2), (True, 0), (True, 1), (False, 2)])
+def test_deepwalk_batch_equals_single_jobs(engine, weighted, layout):
+    """Every alias layout: 16 B neighbour buckets (the default), cursor and index buckets."""
     _load(engine, 5, weighted)
     jobs = [dict(walker_num=n, seed=s, walk_length=l, weighted=weighted, walker_begin=b)
             for n, s, l, b in ((1, 1, 80, 0), (1024, 2, 5, 10), (333, 3, 200, 5000), (2048, 4, 17, 0))]
-    _check(engine, "deepwalk", jobs)
+    engine.set_option("alias_layout", layout)
+    try:
+        _check(engine, "deepwalk", jobs)
+    finally:
+        engine.set_option("alias_layout", 2)
 
 
 def test_batch_rejects_mixed_apps_and_ppr(engine):

@@ -142,7 +142,7 @@ def test_fresh_walks_match_oracle(engine, oracle_lib, i, seed, schedule, layout)
         ps = engine.walk(app, n, seed=seed, weighted=weighted, walker_begin=77, **wkw)
     finally:
         engine.set_option("walk_schedule", 0)
-        engine.set_option("alias_layout", 0)
+        engine.set_option("alias_layout", 2)
         engine.set_option("node2vec_adjacency", 0)
         engine.set_option("cursor_adjacency", 0)
     ocsr = oracle_lib.CSR(500, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
@@ -221,7 +221,7 @@ def test_multi_walker_kernel_matches_oracle(engine, oracle_lib, i, multi):
             assert ps.total_steps == steps
     finally:
         engine.set_option("walk_multi", 1)
-        engine.set_option("alias_layout", 0)
+        engine.set_option("alias_layout", 2)
         engine.set_option("cursor_adjacency", 0)
 
 
@@ -425,3 +425,33 @@ def test_paths_match_reference_parked(engine, name):
         engine.set_option("walk_park", 20)
     np.testing.assert_array_equal(ps.path_length, case.lens)
     np.testing.assert_array_equal(ps.vertices, case.verts)
+
+
+@pytest.mark.parametrize("multi,schedule", [(1, 0), (2, 0), (4, 0), (1, 1)])
+@pytest.mark.parametrize("i", [0, 2, 4])
+def test_neighbour_buckets_match_oracle(engine, oracle_lib, i, multi, schedule):
+    """alias_layout 2 (16 B buckets holding p and the two neighbours) in the
+    one-walker, multi-walker and pool kernels: weighted DeepWalk, PPR and
+    node2vec (whose hooks need index buckets where they read the edge)."""
+    app, gkw, wkw = FRESH[i]
+    g = G.random_undirected(500, 6000, seed=400 + i, **gkw)
+    csr = G.csr_file_order(500, g["src"], g["dst"], w=g.get("w"), type=g.get("type"))
+    engine.load_arrays(500, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
+    n = 3000
+    engine.set_option("alias_layout", 2)
+    engine.set_option("walk_multi", multi)
+    engine.set_option("walk_schedule", schedule)
+    try:
+        ps = engine.walk(app, n, seed=31, weighted=True, walker_begin=5, **wkw)
+    finally:
+        engine.set_option("alias_layout", 2)
+        engine.set_option("walk_multi", 1)
+        engine.set_option("walk_schedule", 0)
+    ocsr = oracle_lib.CSR(500, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
+    if app == "node2vec":
+        ocsr = ocsr.sorted_copy()
+    prm = oracle_lib.make_params(app, seed=31, walker_begin=5, walker_num=n, weighted=True, **wkw)
+    lens, verts, steps = oracle_lib.walk(ocsr, prm, cap=4096)
+    np.testing.assert_array_equal(ps.path_length, lens)
+    np.testing.assert_array_equal(ps.vertices, verts)
+    assert ps.total_steps == steps

@@ -97,16 +97,22 @@ def test_walk_into_epochs_and_small_capacity(engine, stream):
         engine.set_option("into_stream", 1)
 
 
-def test_walk_into_streamed_large_walk(engine):
+@pytest.mark.parametrize("layout", [0, 2])
+def test_walk_into_streamed_large_walk(engine, layout):
     """A walk of 2^21 walkers over a graph with isolated vertices: 256
-    segments of 8192 walkers, some holding only one-vertex paths."""
+    segments of 8192 walkers, some holding only one-vertex paths; cursor and
+    16 B neighbour buckets."""
     g = G.random_undirected(3000, 20000, seed=41, weight="unif")
     csr = G.csr_file_order(4000, g["src"], g["dst"], w=g.get("w"))  # vertices 3000.. are isolated
     engine.load_arrays(4000, csr["off"], csr["nbr"], csr.get("w"))
     n = 1 << 21
     kw = dict(walk_length=5, seed=13)
     ref = engine.walk("deepwalk", n, weighted=True, **kw)
-    steps, h_len, h_off, h_vert = _into(engine, "deepwalk", n, len(ref.vertices), weighted=True, **kw)
+    engine.set_option("alias_layout", layout)
+    try:
+        steps, h_len, h_off, h_vert = _into(engine, "deepwalk", n, len(ref.vertices), weighted=True, **kw)
+    finally:
+        engine.set_option("alias_layout", 2)
     assert steps == ref.total_steps
     np.testing.assert_array_equal(h_len, ref.path_length)
     np.testing.assert_array_equal(h_vert, ref.vertices)

@@ -257,6 +257,10 @@ struct MetapathExt
 /* dynamic_comp: 1 if the edge's type is allowed in the current state, else 0 (metapath.hpp:107-116) */
 struct MetapathDyn
 {
+    /* the type comes from the bucket's tag (index and neighbour buckets carry
+     * it); the edge index is read only where no tag is held */
+    static constexpr bool reads_edge_index = false;
+    static constexpr bool needs_type_tag = true;
     const uint8_t *type;
     const MetaSchemes *sc;
     __device__ __forceinline__ real_t operator()(const Walker<MetapathState> &w, vertex_id_t, const AdjUnit &e) const
@@ -282,6 +286,7 @@ struct MetapathInitState
 /* update: state = (state + 1) % len(scheme) (metapath.hpp:96-99) */
 struct MetapathUpdate
 {
+    static constexpr bool reads_edge_index = false;
     const MetaSchemes *sc;
     __device__ __forceinline__ void operator()(Walker<MetapathState> &w, vertex_id_t, const AdjUnit &) const
     {

@@ -900,6 +900,9 @@ void run_walk(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, WalkR
             run_walk_with<S, WC, TC, CursorBucket>(e, wc, tc, rs, res);
             return;
         }
+    }
+    if constexpr (use_neighbour_buckets<WC, TC>())
+    {
         if (e->alias_layout == 2)
         {
             run_walk_with<S, WC, TC, NeighbourBucket>(e, wc, tc, rs, res);

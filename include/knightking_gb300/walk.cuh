@@ -311,9 +311,11 @@ static __global__ void adj_cursor_kernel(GraphView g, const uint64_t *cur, uint4
  * CursorBucket: p, the two neighbours (q_nbr == kNone: no alias) and their
  *   vertex cursors; used when no hook reads the edge index, so one 32 B read
  *   per step gives the next vertex and its adjacency position.
- * NeighbourBucket: p and the two neighbours, 16 B; used when no hook reads
- *   the edge index.  The build writes half the bytes, and a step reads the
- *   next vertex's offsets (in L2 while they fit) besides the bucket. */
+ * NeighbourBucket: p, the two neighbours and their edge types (type | 0x100
+ *   in the low and high halves of the last word, 0 without types), 16 B;
+ *   used when no hook reads the edge index.  The build writes half the
+ *   bytes, and a step reads the next vertex's offsets (in L2 while they fit)
+ *   besides the bucket. */
 struct __align__(32) IndexBucket
 {
     float p;
@@ -378,14 +380,21 @@ struct __align__(16) NeighbourBucket
     float p;
     uint32_t p_nbr;
     uint32_t q_nbr;
-    uint32_t pad0;
+    uint32_t types;
 
     static constexpr bool cursor = false;
     static constexpr bool compact = true;
-    __device__ __forceinline__ static NeighbourBucket make_n(float p, uint32_t, uint32_t qi, uint32_t pn, uint32_t qn,
-                                                             const uint64_t *, const uint8_t *)
+    __device__ __forceinline__ static NeighbourBucket make_n(float p, uint32_t pi, uint32_t qi, uint32_t pn,
+                                                             uint32_t qn, const uint64_t *, const uint8_t *ty)
     {
-        return NeighbourBucket{p, pn, qi == kNone ? kNone : qn, 0};
+        uint32_t t = 0;
+        if (ty != nullptr)
+        {
+            t = 0x100u | ty[pi];
+            if (qi != kNone)
+                t |= (0x100u | ty[qi]) << 16;
+        }
+        return NeighbourBucket{p, pn, qi == kNone ? kNone : qn, t};
     }
     __device__ __forceinline__ static NeighbourBucket make(float p, uint32_t pi, uint32_t qi, const uint32_t *nb,
                                                            const uint64_t *vcur, const uint8_t *ty)
@@ -411,14 +420,36 @@ struct hook_reads_index<F, std::void_t<decltype(F::reads_edge_index)>>
     static constexpr bool value = F::reads_edge_index;
 };
 
-/* The walk of (WC, TC) may use cursor buckets: it samples by alias tables and
- * none of the hooks that see the picked edge reads its index. */
+/* Whether a hook reads the picked edge's type from the bucket's type tag
+ * (`static constexpr bool needs_type_tag = true`): index and neighbour
+ * buckets carry the tags, cursor buckets do not. */
+template <typename F, typename = void>
+struct hook_needs_type_tag
+{
+    static constexpr bool value = false;
+};
+template <typename F>
+struct hook_needs_type_tag<F, std::void_t<decltype(F::needs_type_tag)>>
+{
+    static constexpr bool value = F::needs_type_tag;
+};
+
+/* The walk of (WC, TC) may use neighbour buckets: it samples by alias tables
+ * and none of the hooks that see the picked edge reads its index. */
 template <typename WC, typename TC>
-constexpr bool use_cursor_buckets()
+constexpr bool use_neighbour_buckets()
 {
     return TC::has_static && !hook_reads_index<typename TC::dyn_type>::value &&
            !hook_reads_index<typename TC::post_query_type>::value &&
            !hook_reads_index<decltype(WC::walker_update_state)>::value;
+}
+
+/* The walk of (WC, TC) may use cursor buckets: neighbour buckets may, and no
+ * hook needs the edge's type tag. */
+template <typename WC, typename TC>
+constexpr bool use_cursor_buckets()
+{
+    return use_neighbour_buckets<WC, TC>() && !hook_needs_type_tag<typename TC::dyn_type>::value;
 }
 
 /* ---- alias-table build (init_alias_tables, include/walk.hpp:538-652) -------
@@ -1350,11 +1381,11 @@ __device__ __forceinline__ Cand pick_candidate(const GraphView &g, const Bucket 
 {
     if constexpr (TC::has_static && Bucket::compact)
     {
-        /* b = {p, p_nbr, q_nbr, -} */
+        /* b = {p, p_nbr, q_nbr, p_type tag | q_type tag << 16} */
         const uint4 b = gather(reinterpret_cast<const uint4 *>(alias + pos.e0 + rng.gen(pos.deg)));
         if (b.z == kNone || rng.gen_float(1.0f) < __uint_as_float(b.x))
-            return Cand{kNone, b.y, 0, false, 0};
-        return Cand{kNone, b.z, 0, false, 0};
+            return Cand{kNone, b.y, 0, false, b.w & 0xffffu};
+        return Cand{kNone, b.z, 0, false, b.w >> 16};
     }
     else if constexpr (TC::has_static)
     {
@@ -2042,9 +2073,9 @@ __global__ void __launch_bounds__(256, 4) walk_multi_kernel(GraphView g, WC wc, 
                 if constexpr (Bucket::compact)
                 {
                     if (lo[k].z == kNone || rng[k].gen_float(1.0f) < __uint_as_float(lo[k].x))
-                        ac = Cand{kNone, lo[k].y, 0, false, 0};
+                        ac = Cand{kNone, lo[k].y, 0, false, lo[k].w & 0xffffu};
                     else
-                        ac = Cand{kNone, lo[k].z, 0, false, 0};
+                        ac = Cand{kNone, lo[k].z, 0, false, lo[k].w >> 16};
                 }
                 else if constexpr (Bucket::cursor)
                 {

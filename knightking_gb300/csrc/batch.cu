@@ -186,8 +186,10 @@ void launch_batch_with(kk_engine *e, const App &app, const BatchPlan &plan, Batc
 template <typename App>
 int app_layout(const kk_engine *e)
 {
-    if (use_cursor_buckets<typename App::WC, typename App::TC>() && e->alias_layout != 1)
-        return e->alias_layout;
+    if (e->alias_layout == 0 && use_cursor_buckets<typename App::WC, typename App::TC>())
+        return 0;
+    if (e->alias_layout == 2 && use_neighbour_buckets<typename App::WC, typename App::TC>())
+        return 2;
     return 1;
 }
 
@@ -204,6 +206,9 @@ void launch_batch(kk_engine *e, const App &app, const BatchPlan &plan, BatchSlot
                                                  want_paths, prepared, hdr);
             return;
         }
+    }
+    if constexpr (use_neighbour_buckets<typename App::WC, typename App::TC>())
+    {
         if (app_layout<App>(e) == 2)
         {
             launch_batch_with<App, NeighbourBucket>(e, app, plan, slot, d_jobs, length, path, steps, status,

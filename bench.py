@@ -655,9 +655,12 @@ def run_ours(args, wl, world, rank, local):
     barrier(world)
     t0 = time.perf_counter()
     d2h = 0
+    call_ms = []
     for _ in range(e2e_runs):
+        tc = time.perf_counter()
         st = engine.walk_into(app, walkers, h_len.data_ptr(), h_off.data_ptr(), h_vert.data_ptr(), cap_vertices,
                               seed=1, walker_begin=walker_begin, start=start, **kw)
+        call_ms.append(round((time.perf_counter() - tc) * 1e3, 3))
         e2e_steps += st
         d2h += walkers * 4 + walkers * 8 + (st + walkers) * 4
     e2e_s = time.perf_counter() - t0
@@ -755,7 +758,7 @@ def run_ours(args, wl, world, rank, local):
                        "tuned": best,
                        "tuning_ms": [[cfg, ms] for cfg, ms in tune_table]},
             "e2e": {"value": e2e_value, "unit": "walker-steps/s", "h2d_bytes_per_step": walkers * 4 + 256,
-                    "d2h_bytes_per_step": d2h // e2e_runs},
+                    "d2h_bytes_per_step": d2h // e2e_runs, "call_ms": call_ms},
             "gpu_launches": launches,
             "roofline": roof,
             "cpu_baseline": cpu,

@@ -14,7 +14,6 @@
 
 #include <cub/cub.cuh>
 #include <string>
-#include <thread>
 #include <vector>
 
 #include "knightking_gb300/engine.cuh"
@@ -472,8 +471,9 @@ uint64_t walk_into_chunked(kk_engine *e, const kk_walk_opts *o, uint32_t *h_leng
                             issued = true;
                             a = b;
                         }
-                        if (!issued && !all)
-                            std::this_thread::yield();
+                        /* no yield: the thread keeps its core, so a finished
+                         * segment waits microseconds, not a time slice */
+                        (void)issued;
                     }
                 };
                 e->seg_sink = &sink;

@@ -11,7 +11,8 @@ value : walker-steps/s with the graph resident in HBM and paths written to HBM
         (kk_walk_device), device time from CUDA events on the engine's stream.
 e2e   : the same walk through the public C-ABI call kk_walk_into: the start-vertex
         list is copied host->device and every path is copied device->host into
-        pinned host memory, inside the timed region.
+        pinned host memory, inside the timed region; K calls (the device loop's
+        K), each call's time recorded in e2e.call_ms.
 roofline: the walk kernel's bytes touched per walker-step at 32-byte sector
         granularity (sampling part only) over its CUDA-event duration, against
         the measured HBM copy bandwidth.
@@ -545,7 +546,7 @@ def run_batch_bench(args, wl, world, rank, local):
     t0 = time.perf_counter()
     e_steps = 0
     d2h = 0
-    e2e_runs = max(1, min(args.steps, 3))
+    e2e_runs = max(1, args.steps)  # the same K as the device-timed loop
     for _ in range(e2e_runs):
         res = engine.batch_walk(app, jobs, keep_paths=False)
         e_steps += sum(r["total_steps"] for r in res)
@@ -649,7 +650,7 @@ def run_ours(args, wl, world, rank, local):
     h_off = torch.empty(walkers, dtype=torch.int64, pin_memory=True)
     h_vert = torch.empty(cap_vertices, dtype=torch.int32, pin_memory=True)
     e2e_steps = 0
-    e2e_runs = max(1, min(args.steps, 3))
+    e2e_runs = max(1, args.steps)  # the same K as the device-timed loop
     engine.walk_into(app, walkers, h_len.data_ptr(), h_off.data_ptr(), h_vert.data_ptr(), cap_vertices, seed=1,
                      walker_begin=walker_begin, start=start, **kw)
     barrier(world)

@@ -209,7 +209,10 @@ kk_status kk_alias_build_noalloc(uint32_t v_num, const int64_t *d_off, const flo
 /* ---- walks (WalkEngine::random_walk, include/walk.hpp:423-436) ---------- */
 
 /* Runs one walk job and returns its paths in host memory (free with
- * kk_paths_free).  Epochs (opts->rate < 1) run one after the other. */
+ * kk_paths_free).  Epochs (opts->rate < 1) run one after the other.  The
+ * paths come in a pinned block from the engine's pool (one epoch, or epochs of
+ * walks bounded by walk_length + 1 vertices), copied straight from the device;
+ * kk_paths_free returns the block. */
 kk_status kk_walk(kk_engine *e, const kk_walk_opts *opts, kk_paths **out);
 
 /* The apps' entry points: set opts->app and call kk_walk. */

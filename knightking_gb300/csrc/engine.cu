@@ -1008,6 +1008,69 @@ kk_status walk_to_host(kk_engine *e, const kk_walk_opts *opts, kk_paths **out, c
         p->walker_num = n;
         p->walker_begin = opts->walker_begin;
         p->epoch_walkers = epoch_walkers(opts);
+        /* one epoch, or epochs of walks no longer than walk_length + 1 vertices
+         * (DeepWalk, node2vec, user hooks): lengths, offsets and vertices
+         * straight from the device into one pooled pinned block (kk_paths_free
+         * returns it), sized by the epoch's total or by that bound */
+        const bool one_epoch = n > 0 && p->epoch_walkers >= n;
+        const bool bounded = n > 0 && (custom != nullptr || opts->app == KK_APP_DEEPWALK ||
+                                       opts->app == KK_APP_NODE2VEC);
+        if (one_epoch || bounded)
+        {
+            uint64_t base = 0, vcap = 0;
+            p->total_steps = walk_epochs(e, opts, custom, [&](uint32_t done, uint32_t num, const uint32_t *d_len,
+                                                              const uint64_t *d_off, const uint32_t *d_verts,
+                                                              uint64_t total) {
+                const size_t len_bytes = ((size_t)n * 4 + 15) & ~(size_t)15;
+                const size_t off_bytes = ((size_t)n * 8 + 15) & ~(size_t)15;
+                if (p->owner == nullptr)
+                {
+                    if (e->host_pool == nullptr)
+                    {
+                        e->host_pool = new HostPool();
+                        e->host_pool->limit = kBatchPoolCache;
+                    }
+                    vcap = one_epoch ? total : (uint64_t)n * ((uint64_t)opts->walk_length + 1);
+                    PooledPaths *o = new (std::nothrow) PooledPaths();
+                    size_t cls = 0;
+                    char *blk = o ? (char *)e->host_pool->get(len_bytes + off_bytes + vcap * 4 + 16, &cls) : nullptr;
+                    if (!blk)
+                    {
+                        delete o;
+                        fail(KK_ERR_OOM, "host allocation failed");
+                    }
+                    o->pool = e->host_pool;
+                    o->block = blk;
+                    o->cls = cls;
+                    p->owner = o;
+                    p->length = (uint32_t *)blk;
+                    p->offset = (uint64_t *)(blk + len_bytes);
+                    p->vertices = (uint32_t *)(blk + len_bytes + off_bytes);
+                }
+                if (base + total > vcap)
+                    fail(KK_ERR_PATH_CAPACITY, "a walk exceeded its path capacity");
+                const uint64_t *src_off = d_off;
+                if (base != 0)
+                {
+                    /* the epoch's offsets count from the caller's first vertex */
+                    uint64_t *ob = e->into_offb[0].as<uint64_t>((uint64_t)num + 1);
+                    offsets_plus_base_kernel<<<grid_for(e, num, 256), 256, 0, e->stream>>>(d_off, 0, base, num, ob);
+                    count_launch(e);
+                    KK_CUDA_CHECK(cudaGetLastError());
+                    src_off = ob;
+                }
+                KK_CUDA_CHECK(cudaMemcpyAsync(p->length + done, d_len, (size_t)num * 4, cudaMemcpyDeviceToHost,
+                                              e->stream));
+                KK_CUDA_CHECK(cudaMemcpyAsync(p->offset + done, src_off, (size_t)num * 8, cudaMemcpyDeviceToHost,
+                                              e->stream));
+                KK_CUDA_CHECK(cudaMemcpyAsync(p->vertices + base, d_verts, total * 4, cudaMemcpyDeviceToHost,
+                                              e->stream));
+                /* the next epoch reuses the device buffers */
+                KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+                base += total;
+            });
+            return;
+        }
         p->length = (uint32_t *)malloc((size_t)n * 4 + 4);
         p->offset = (uint64_t *)malloc((size_t)n * 8 + 8);
         if (!p->length || !p->offset)

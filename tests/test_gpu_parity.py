@@ -455,3 +455,23 @@ def test_neighbour_buckets_match_oracle(engine, oracle_lib, i, multi, schedule):
     np.testing.assert_array_equal(ps.path_length, lens)
     np.testing.assert_array_equal(ps.vertices, verts)
     assert ps.total_steps == steps
+
+
+@pytest.mark.parametrize("i", [0, 2, 4, 7])
+def test_epoch_split_matches_single_epoch(engine, i):
+    """kk_walk with epochs (rate 0.37): DeepWalk and node2vec into one pooled
+    block sized by walk_length + 1, PPR and metapath through per-epoch host
+    chunks; every path equals the single-epoch walk's."""
+    app, gkw, wkw = FRESH[i]
+    g = G.random_undirected(500, 6000, seed=500 + i, **gkw)
+    csr = G.csr_file_order(500, g["src"], g["dst"], w=g.get("w"), type=g.get("type"))
+    engine.load_arrays(500, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
+    weighted = "w" in csr
+    one = engine.walk(app, 5000, seed=17, weighted=weighted, **wkw)
+    import knightking_gb300 as kk
+    conf = kk.WalkConfig()
+    conf.set_walk_rate(0.37)
+    many = engine.walk(app, 5000, walk_conf=conf, seed=17, weighted=weighted, **wkw)
+    np.testing.assert_array_equal(many.path_length, one.path_length)
+    np.testing.assert_array_equal(many.vertices, one.vertices)
+    assert many.total_steps == one.total_steps

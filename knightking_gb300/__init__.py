@@ -227,11 +227,8 @@ class WalkEngine:
         opts = self.make_opts(app, walker_num, **kw)
         out = ctypes.POINTER(_capi.KKPaths)()
         self._check(self._lib.kk_walk(self._h, ctypes.byref(opts), ctypes.byref(out)))
-        try:
-            ps = _capi.paths_to_numpy(out.contents)
-        finally:
-            self._lib.kk_paths_free(out)
-        paths = PathSet(*ps)
+        # the arrays view the library's pinned block and return it when dropped
+        paths = PathSet(*_capi.paths_to_numpy_owned(out))
         if walk_conf is not None:
             if walk_conf.output_file_flag:
                 paths.dump(walk_conf.output_path_prefix + ".0", "w", walk_conf.print_with_head_info, self.seg_num)
@@ -259,17 +256,20 @@ class WalkEngine:
         outs = (ctypes.POINTER(_capi.KKPaths) * len(jobs))()
         self._check(self._lib.kk_batch_walk(self._h, arr, len(jobs), outs))
         res = []
+        owned = [False] * len(jobs)
         try:
-            for p in outs:
+            for k, p in enumerate(outs):
                 if keep_paths:
-                    res.append(PathSet(*_capi.paths_to_numpy(p.contents)))
+                    # views of the pinned block, returned when the arrays are dropped
+                    res.append(PathSet(*_capi.paths_to_numpy_owned(p)))
+                    owned[k] = True
                 else:
                     c = p.contents
                     res.append({"walker_num": int(c.walker_num), "total_steps": int(c.total_steps),
                                 "vertices": int(c.total_steps) + int(c.walker_num)})
         finally:
-            for p in outs:
-                if p:
+            for k, p in enumerate(outs):
+                if p and not owned[k]:
                     self._lib.kk_paths_free(p)
         return res
 

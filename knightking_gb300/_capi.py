@@ -5,6 +5,7 @@ knightking_gb300/build.py).  If it is missing or cannot be loaded this module
 raises: there is no CPU fallback.
 """
 
+import atexit
 import ctypes
 import os
 
@@ -220,6 +221,65 @@ def make_opts(app, walker_num, seed, walker_begin, walk_length, terminate_prob, 
         o.n_start = len(st)
     o.rate = float(rate)
     return o
+
+
+_exiting = False
+
+
+def _mark_exit():
+    global _exiting
+    _exiting = True
+
+
+atexit.register(_mark_exit)
+
+
+class _PathsOwner:
+    """Owns a kk_paths: returns it to the library (kk_paths_free) once the last
+    numpy array viewing it is gone.  At interpreter exit it leaves the memory
+    alone: the library may already be unloading."""
+
+    def __init__(self, ptr):
+        self.ptr = ptr
+
+    def __del__(self):
+        if not _exiting and self.ptr:
+            lib().kk_paths_free(self.ptr)
+            self.ptr = None
+
+
+def _view(addr, ctype, count, owner, dtype):
+    """A numpy array over count elements at addr, keeping owner alive."""
+    if count == 0:
+        return np.zeros(0, dtype)
+    buf = (ctype * count).from_address(addr)
+    buf._owner = owner
+    return np.frombuffer(buf, dtype=dtype)
+
+
+def paths_to_numpy_owned(pp):
+    """Like paths_to_numpy for a POINTER(KKPaths) whose ownership passes to
+    the result: packed paths (every kk_walk and kk_batch_walk result) are
+    returned as views of the library's pinned block, freed when the last view
+    is gone; other layouts are copied and freed at once."""
+    p = pp.contents
+    n = int(p.walker_num)
+    total = int(p.total_steps) + n
+    owner = _PathsOwner(pp)
+    length = _view(ctypes.addressof(p.length.contents), ctypes.c_uint32, n, owner, np.uint32) if n else \
+        np.zeros(0, np.uint32)
+    offset = _view(ctypes.addressof(p.offset.contents), ctypes.c_uint64, n, owner, np.uint64) if n else \
+        np.zeros(0, np.uint64)
+    # the library hands out packed paths or fixed-capacity slots (offset i *
+    # cap); of those layouts, only packed paths end at total with offset 0 first
+    packed = n == 0 or (int(offset[0]) == 0 and int(offset[n - 1]) + int(length[n - 1]) == total)
+    if packed:
+        verts = _view(ctypes.addressof(p.vertices.contents), ctypes.c_uint32, total, owner, np.uint32) if total \
+            else np.zeros(0, np.uint32)
+        return int(p.walker_begin), int(p.epoch_walkers), length, offset, verts, int(p.total_steps)
+    out = paths_to_numpy(p)
+    del length, offset
+    return out
 
 
 def paths_to_numpy(p):

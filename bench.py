@@ -1,24 +1,33 @@
 #!/usr/bin/env python3
 """Walker-step benchmark (one JSON line on rank 0).
 
-Default workload: weighted DeepWalk (static alias sampling), walk length 80,
-4,194,304 walkers (one per vertex) on a seeded R-MAT scale-22 graph (edge
-factor 16, a/b/c = 0.57/0.19/0.19, undirected, lognormal(0,1) float32
-weights); every step rebuilds the alias tables on the GPU and walks all
-walkers (the reference includes the alias build in its timings).
+Default workload (node2vec-serve-s24): a served node2vec request stream on a
+resident R-MAT scale-24 weighted graph (edge factor 16, a/b/c = 0.57/0.19/0.19,
+undirected, uniform [1,5) float32 weights): 3000 requests, per request p and q
+log-uniform in [0.25, 4], length uniform in [5, 200], walkers lognormal (median
+4096) clipped to [1, 2^20].  A step is one pass of the whole stream.
 
-value : walker-steps/s with the graph resident in HBM and paths written to HBM
-        (kk_walk_device), device time from CUDA events on the engine's stream.
-e2e   : the same walk through the public C-ABI call kk_walk_into: the start-vertex
-        list is copied host->device and every path is copied device->host into
-        pinned host memory, inside the timed region; K calls (the device loop's
-        K), each call's time recorded in e2e.call_ms.
+value : walker-steps/s of the stream through the batched kernel
+        (kk_batch_walk_device, 1024 requests per launch, paths in HBM), device
+        time from CUDA events on the engine's stream; the plain
+        one-launch-per-request kernel is timed beside it (batched_over_plain).
+e2e   : the same stream through the serving C-ABI (kk_serve_submit/poll): job
+        records host->device, every path device->host into pinned memory,
+        inside the timed region (served_over_plain); p50/p99 latency of an
+        open-loop Poisson stream at 70% of that rate.
 roofline: the walk kernel's bytes touched per walker-step at 32-byte sector
-        granularity (sampling part only) over its CUDA-event duration, against
-        the measured HBM copy bandwidth.
-cpu_baseline / --impl reference: the CPU restatement of the reference's path
-        (oracle/kk_oracle.c, pinned bit-for-bit to the reference) on all host
-        cores, over a bounded sample of the same workload.
+        granularity (the reference's access pattern) over its CUDA-event
+        duration per launch, against the measured HBM copy bandwidth; beside it
+        the fraction of the measured random-gather ceiling.
+parity: the benchmarked walks' paths against the oracle (the C restatement,
+        pinned bit for bit to the reference), walker for walker, on the
+        benchmarked graph.
+cpu_baseline / --impl reference: the oracle on all host cores over a bounded
+        sample of the same workload.
+
+The default run also measures weighted DeepWalk on R-MAT scale 22 (alias build
+inside every step; e2e through kk_walk_into) and reports it under "also".
+Other workloads: --workload.
 
 Multi-GPU (torchrun): weak scaling, each rank walks its own walker-id range on
 its own replica of the graph; no collective on the data path.
@@ -32,6 +41,8 @@ import subprocess
 import sys
 import threading
 import time
+
+import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -209,24 +220,101 @@ def walk_kwargs(wl):
     return kw
 
 
-def cpu_sample(g, wl, walkers, threads, seed, target_s=10.0, chunks=16):
-    """Times the oracle (CPU restatement) on a bounded sample of the workload,
-    about target_s seconds of walking on `threads` host threads.
+def oracle_cap(app, wl, gpu_lens=None):
+    """Path capacity (vertices per walker) for an oracle walk of the workload."""
+    if "walk_length" in wl:
+        return wl["walk_length"] + 1
+    return int(gpu_lens.max()) + 1 if gpu_lens is not None and len(gpu_lens) else 4096
 
-    Alias tables (weighted) are built once for the whole graph and their time
-    is charged per walker (t_alias * sample/walkers); the walk runs `chunks`
-    contiguous walker-id ranges spread over the id space, sized from a short
-    calibration walk.
+
+def host_graph(engine, app, threads):
+    """The engine's graph on the host for the oracle (bit-identical to the
+    device's: the same seeded generator, downloaded), with the weight alias
+    tables built once by the oracle.  Returns (csr, alias, alias_seconds)."""
+    from oracle import pyoracle
+    g = engine.download_graph()
+    csr = pyoracle.CSR(g["V"], g["off"], g["nbr"], g.get("w"), g.get("type"))
+    alias, t_alias = None, 0.0
+    if csr.w is not None:
+        t0 = time.perf_counter()
+        alias = pyoracle.alias_build(csr, threads=threads)
+        t_alias = time.perf_counter() - t0
+    return csr, alias, t_alias
+
+
+def count_mismatches(lens_a, verts_a, lens_b, verts_b):
+    """Walkers whose paths differ between two packed path sets of the same walkers."""
+    lens_a = np.asarray(lens_a, np.int64)
+    lens_b = np.asarray(lens_b, np.int64)
+    if len(lens_a) != len(lens_b):
+        return max(len(lens_a), len(lens_b))
+    oa = np.zeros(len(lens_a) + 1, np.int64)
+    ob = np.zeros(len(lens_b) + 1, np.int64)
+    np.cumsum(lens_a, out=oa[1:])
+    np.cumsum(lens_b, out=ob[1:])
+    if np.array_equal(lens_a, lens_b) and len(verts_a) == len(verts_b):
+        diff = np.asarray(verts_a) != np.asarray(verts_b)
+        if not diff.any():
+            return 0
+        per = np.add.reduceat(diff.astype(np.int64), oa[:-1]) if len(diff) else np.zeros(0)
+        return int(((per > 0) & (lens_a > 0)).sum())
+    bad = 0
+    for i in range(len(lens_a)):
+        if lens_a[i] != lens_b[i] or not np.array_equal(verts_a[oa[i]:oa[i + 1]], verts_b[ob[i]:ob[i + 1]]):
+            bad += 1
+    return bad
+
+
+def oracle_paths(csr, alias, app, threads, cap, **prm_kw):
+    """The oracle's paths (lens, flat vertices, steps) of one walk; a path
+    longer than cap raises."""
+    from oracle import pyoracle
+    prm = pyoracle.make_params(app, **prm_kw)
+    return pyoracle.walk(csr, prm, cap=cap, threads=threads, alias=alias)
+
+
+def parity_ranges(engine, csr, alias, wl, walkers, threads, chunks=16, per=8192):
+    """Bit-for-bit parity of the benchmarked walk on the benchmarked graph:
+    `chunks` walker-id ranges of `per` walkers spread over the id space, each
+    walked by the engine (kk_walk, paths to the host) and by the oracle."""
+    app = wl["app"]
+    kw = walk_kwargs(wl)
+    weighted = csr.w is not None
+    checked = mism = steps = 0
+    for c in range(chunks):
+        begin = (walkers // chunks) * c
+        n = min(per, walkers - begin)
+        if n <= 0:
+            continue
+        ps = engine.walk(app, n, seed=1, walker_begin=begin, weighted=weighted, **kw)
+        try:
+            lens, verts, st = oracle_paths(csr, alias, app, threads, oracle_cap(app, wl, ps.path_length), seed=1,
+                                           walker_begin=begin, walker_num=n, weighted=weighted, **kw)
+            mism += count_mismatches(ps.path_length, ps.vertices, lens, verts)
+        except RuntimeError:
+            mism += n
+            st = 0
+        checked += n
+        steps += st
+        del ps
+    return {"walkers_checked": checked, "mismatches": mism, "steps_checked": steps,
+            "what": "%d walker-id ranges of %d walkers spread over %d: kk_walk paths vs the oracle (pinned to "
+                    "the reference), bit for bit" % (chunks, per, walkers)}
+
+
+def cpu_sample(csr, alias, t_alias, wl, walkers, threads, seed, target_s=10.0, chunks=16):
+    """Times the oracle (CPU restatement) on a bounded sample of the workload,
+    about target_s seconds of walking on `threads` host threads, without path
+    output (the reference's pure-performance mode).
+
+    Alias tables (weighted) are built once for the whole graph (t_alias) and
+    their time is charged per walker (t_alias * sample/walkers); the walk runs
+    `chunks` contiguous walker-id ranges spread over the id space, sized from
+    a short calibration walk.
     """
     from oracle import pyoracle
-    csr = pyoracle.CSR(g["V"], g["off"], g["nbr"], g.get("w"), g.get("type"))
-    weighted = g.get("w") is not None
+    weighted = csr.w is not None
     kw = walk_kwargs(wl)
-    t_alias = 0.0
-    if weighted:
-        t0 = time.perf_counter()
-        pyoracle.alias_build(csr, threads=threads)
-        t_alias = time.perf_counter() - t0
 
     def run(n_per_chunk):
         steps, t_walk, n_done = 0, 0.0, 0
@@ -234,7 +322,7 @@ def cpu_sample(g, wl, walkers, threads, seed, target_s=10.0, chunks=16):
             begin = (walkers // chunks) * c
             prm = pyoracle.make_params(wl["app"], seed=seed, walker_begin=begin, walker_num=n_per_chunk,
                                        weighted=weighted, **kw)
-            _, _, st = pyoracle.walk(csr, prm, cap=1, threads=threads, with_paths=False)
+            _, _, st = pyoracle.walk(csr, prm, cap=1, threads=threads, with_paths=False, alias=alias)
             steps += st
             t_walk += pyoracle.last_timing()[1]
             n_done += n_per_chunk
@@ -256,6 +344,40 @@ def cpu_sample(g, wl, walkers, threads, seed, target_s=10.0, chunks=16):
     }
 
 
+def cpu_sample_requests(csr, alias, t_alias, reqs, first, threads, target_s=10.0):
+    """Times the oracle on a bounded sample of the served request stream: the
+    requests from position `first` on, each as one plain node2vec() call
+    (src/apps/node2vec.hpp:108-202) run one after the other, until about
+    target_s seconds of walking.  The reference's random_walk rebuilds the
+    whole graph's alias tables in every call (include/walk.hpp:538-652); here
+    they are built once and charged to the sample pro rata by walker-steps
+    against the whole stream (a CPU baseline favourable to the CPU)."""
+    from oracle import pyoracle
+    steps, t_walk, n = 0, 0.0, 0
+    i = first
+    while t_walk < target_s and n < len(reqs):
+        r = reqs[i % len(reqs)]
+        prm = pyoracle.make_params("node2vec", seed=r["seed"], walker_begin=r["walker_begin"],
+                                   walker_num=r["walker_num"], walk_length=r["walk_length"], p=r["p"], q=r["q"],
+                                   weighted=r["weighted"])
+        _, _, st = pyoracle.walk(csr, prm, cap=1, threads=threads, with_paths=False, alias=alias)
+        steps += st
+        t_walk += pyoracle.last_timing()[1]
+        n += 1
+        i += 1
+    stream_cap = sum(r["walker_num"] * r["walk_length"] for r in reqs)
+    charged = t_alias * min(1.0, steps / max(stream_cap, 1))
+    t_total = t_walk + charged
+    return {
+        "value": steps / t_total, "unit": "walker-steps/s", "cores": threads, "kind": "port",
+        "seconds": t_total,
+        "sample": "%d requests of the stream from request %d, each one node2vec() call in turn (%d steps, %.2f s "
+                  "walking); alias build over the full graph %.2f s, charged %.3f s pro rata by steps (the "
+                  "reference rebuilds it in every call)" % (n, first, steps, t_walk, t_alias, charged),
+        "alias_build_s_per_call": t_alias,
+    }, i
+
+
 def walk_kernel_name(app, best):
     """The walk kernel the engine launches under the tuned options."""
     if best.get("walk_schedule", 0) == 1:
@@ -266,37 +388,60 @@ def walk_kernel_name(app, best):
 
 
 def run_reference(args, wl, world, rank, local):
-    """The reference's CPU path (its C restatement, pinned to the reference) on all host cores."""
+    """The reference's CPU path (its C restatement, pinned to the reference)
+    on all host cores, on the workload's graph generated on the CPU."""
     if rank != 0:
         return
     from oracle import pyoracle
     pyoracle.build()
-    g = pyoracle.rmat_graph(wl["scale"], 16, seed=wl["scale"], weights=wl["weights"], types=wl["types"])
-    walkers = g["V"] if wl["app"] != "node2vec" or wl["scale"] != 16 else 65536
     threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    g = pyoracle.rmat_graph(wl["scale"], 16, seed=wl["scale"], weights=wl["weights"], types=wl["types"],
+                            threads=threads)
+    csr = pyoracle.CSR(g["V"], g["off"], g["nbr"], g.get("w"), g.get("type"))
+    del g
+    t_gen = time.perf_counter() - t0
+    alias, t_alias = None, 0.0
+    if csr.w is not None:
+        t0 = time.perf_counter()
+        alias = pyoracle.alias_build(csr, threads=threads)
+        t_alias = time.perf_counter() - t0
     vals = []
-    # each step: a bounded sample of ~2 s of walking, so the whole run stays
-    # within a few minutes
-    for _ in range(args.warmup):
-        cpu_sample(g, wl, walkers, threads, seed=1, target_s=0.5, chunks=4)
-    for _ in range(args.steps):
-        vals.append(cpu_sample(g, wl, walkers, threads, seed=1, target_s=2.0))
+    if "serve" in wl:
+        reqs = serve_requests(wl, csr.V)
+        pos = 0
+        for _ in range(args.warmup):
+            _, pos = cpu_sample_requests(csr, alias, t_alias, reqs, pos, threads, target_s=0.3)
+        for _ in range(args.steps):
+            v, pos = cpu_sample_requests(csr, alias, t_alias, reqs, pos, threads, target_s=2.0)
+            vals.append(v)
+        walkers = None
+    else:
+        walkers = csr.V if wl["app"] != "node2vec" or wl["scale"] != 16 else 65536
+        # each step: a bounded sample of ~2 s of walking, so the whole run stays
+        # within a few minutes
+        for _ in range(args.warmup):
+            cpu_sample(csr, alias, t_alias, wl, walkers, threads, seed=1, target_s=0.5, chunks=4)
+        for _ in range(args.steps):
+            vals.append(cpu_sample(csr, alias, t_alias, wl, walkers, threads, seed=1, target_s=2.0))
     value = statistics.median(v["value"] for v in vals)
     line = {
         "impl": "reference", "metric": "walker-steps/s", "value": value, "unit": "walker-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * statistics.median(v["seconds"] for v in vals), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded R-MAT)",
-        "config": {"workload": args.workload, "desc": wl["desc"], "walkers": walkers},
+        "config": {"workload": args.workload, "desc": wl["desc"], "vertices": csr.V, "edges": csr.E,
+                   "graph_generation_s": t_gen},
         "cpu_baseline": dict(vals[-1], value=value),
         "e2e": {"value": value, "unit": "walker-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if walkers is not None:
+        line["config"]["walkers"] = walkers
     print(json.dumps(line), flush=True)
 
 
 def serve_requests(wl, V, seed=5):
     """The served workload's request stream (seeded)."""
-    import numpy as np
     rng = np.random.default_rng(seed)
     reqs = []
     for i in range(wl["serve"]):
@@ -308,16 +453,39 @@ def serve_requests(wl, V, seed=5):
     return reqs
 
 
-def run_serve_bench(args, wl, world, rank, local):
-    """Served request stream (continuous batching on two slots) against plain
-    per-request launches and device-side batches of the same requests.
+def parity_requests(results, csr, alias, reqs, threads, what):
+    """Each served (or batched) request's paths against the oracle's node2vec
+    walk of the same request; results[i] is (lens, verts) of reqs[i]."""
+    checked = mism = steps = 0
+    for (lens_g, verts_g), r in zip(results, reqs):
+        lens, verts, st = oracle_paths(csr, alias, "node2vec", threads, r["walk_length"] + 1, seed=r["seed"],
+                                       walker_begin=r["walker_begin"], walker_num=r["walker_num"],
+                                       walk_length=r["walk_length"], p=r["p"], q=r["q"], weighted=r["weighted"])
+        mism += count_mismatches(lens_g, verts_g, lens, verts)
+        checked += r["walker_num"]
+        steps += st
+    return {"requests": len(reqs), "walkers_checked": checked, "mismatches": mism, "steps_checked": steps,
+            "what": what}
 
-    value = saturated serving throughput: every request submitted at once,
-    walker-steps over first submit -> last paths on the host.  Latency: an
-    open-loop Poisson stream at 70% of that throughput, p50/p99 of submit ->
-    paths on the host.  plain: one kk_walk_device per request (alias tables
-    kept, or rebuilt per call as the reference's random_walk does)."""
-    import numpy as np
+
+SERVE_JOB_BYTES = 72  # one BatchJob record (walk.cuh), uploaded per job slot of a batch
+
+
+def run_serve_bench(args, wl, world, rank, local):
+    """North-star workload: the served node2vec request stream on a resident
+    R-MAT scale-24 weighted graph.
+
+    value  : K passes of the whole stream through kk_batch_walk_device (1024
+             requests per launch, paths in HBM), CUDA events on the engine's
+             stream; the plain one-launch-per-request kernel is timed beside it.
+    e2e    : K passes through the serving API (kk_serve_submit / kk_serve_poll):
+             every request of a pass submitted at once, its job record copied
+             to the device and its paths copied back into pinned host memory;
+             submit of the first -> paths of the last on the host.
+    latency: an open-loop Poisson stream at 70% of the saturated rate, p50/p99
+             of submit -> paths on the host.
+    parity : the first requests' served paths (and their kk_batch_walk paths)
+             against the oracle, walker for walker."""
     import torch
 
     import knightking_gb300 as kk
@@ -328,19 +496,18 @@ def run_serve_bench(args, wl, world, rank, local):
     V, E, _, _ = engine.info()
     app = wl["app"]
     reqs = serve_requests(wl, V)
-    total_req_steps_cap = sum(r["walker_num"] * r["walk_length"] for r in reqs)
+    stream_cap = sum(r["walker_num"] * r["walk_length"] for r in reqs)
     stream = torch.cuda.Stream()
     engine.set_stream(stream.cuda_stream)
+    kernel_ms = []
 
-    def timed(fn):
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        steps = fn()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        return steps, e0.elapsed_time(e1)
+    def batched(rs, record=False):
+        steps = 0
+        for k in range(0, len(rs), 1024):
+            steps += engine.batch_walk_device(app, rs[k:k + 1024], paths=True)
+            if record:
+                kernel_ms.append((engine.last_timing()[1], steps))
+        return steps
 
     def plain(rs):
         steps = 0
@@ -349,11 +516,15 @@ def run_serve_bench(args, wl, world, rank, local):
             steps += engine.walk_device(app, kw.pop("walker_num"), paths="unpacked", **kw)[0]
         return steps
 
-    def batched(rs):
-        steps = 0
-        for k in range(0, len(rs), 1024):
-            steps += engine.batch_walk_device(app, rs[k:k + 1024], paths=True)
-        return steps
+    def timed(fn, k=1):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        steps = sum(fn() for _ in range(k))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return steps, e0.elapsed_time(e1)
 
     # tables resident (sorted adjacency, edge set, alias tables), then tune the
     # batch kernel on the whole stream
@@ -362,35 +533,40 @@ def run_serve_bench(args, wl, world, rank, local):
     best, tune_table = tuning.autotune(engine, lambda: batched(reqs), tuning.space_for(app, bool(wl["weights"])),
                                       repeats=1)
     for _ in range(args.warmup):
-        batched(reqs[:64])
-        plain(reqs[:8])
+        batched(reqs)
+    plain(reqs[:8])
     barrier(world)
     n_plain = min(len(reqs), 300)
+    srv = engine.serve(app, slots=2, max_jobs=256, slot_bytes=2 << 30)
+    for t in [srv.submit(**r) for r in reqs]:  # fills the server's pinned result pool
+        srv.poll(t, keep_paths=False)
     with ClockSampler(local) as clocks:
         time.sleep(0.5)
-        b_steps, b_ms = timed(lambda: batched(reqs))
+        l0 = engine.launch_count()
+        kernel_ms.clear()
+        b_steps, b_ms = timed(lambda: batched(reqs, record=True), args.steps)
+        launches = engine.launch_count() - l0
         p_steps, p_ms = timed(lambda: plain(reqs[:n_plain]))
         engine.set_option("alias_cache", 0)
         r_steps, r_ms = timed(lambda: plain(reqs[:12]))
         engine.set_option("alias_cache", 1)
-        # saturated serving (after one untimed pass that fills the server's
-        # pinned result pool)
-        srv = engine.serve(app, slots=2, max_jobs=256, slot_bytes=2 << 30)
-        for t in [srv.submit(**r) for r in reqs]:
-            srv.poll(t, keep_paths=False)
+        # e2e: K saturated passes through the server
         srv.reset_stats()
-        t0 = time.perf_counter()
-        tickets = [srv.submit(**r) for r in reqs]
         s_steps = 0
-        for t in tickets:
-            res = srv.poll(t, keep_paths=False)
-            assert res.status == 0
-            s_steps += res.total_steps
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            tickets = [srv.submit(**r) for r in reqs]
+            for t in tickets:
+                res = srv.poll(t, keep_paths=False)
+                assert res.status == 0
+                s_steps += res.total_steps
         s_s = time.perf_counter() - t0
         sat = srv.stats()
-    served_value = s_steps / s_s
+    b_ms = allreduce(world, b_ms, "max")
+    value = allreduce(world, float(b_steps), "sum") / (b_ms / 1e3)
+    served_value = allreduce(world, float(s_steps), "sum") / allreduce(world, s_s, "max")
     # latency under an open-loop Poisson stream at 70% of the saturated rate
-    rate = 0.7 * served_value / (s_steps / len(reqs))
+    rate = 0.7 * served_value / (s_steps / args.steps / len(reqs))
     rng = np.random.default_rng(11)
     gaps = rng.exponential(1.0 / rate, len(reqs))
     srv.reset_stats()
@@ -400,7 +576,6 @@ def run_serve_bench(args, wl, world, rank, local):
         for i, t in ts:
             results[i] = srv.poll(t, keep_paths=False)
 
-    import threading
     t_start = time.perf_counter()
     due = t_start
     pending = []
@@ -424,8 +599,21 @@ def run_serve_bench(args, wl, world, rank, local):
         th.join()
     open_s = time.perf_counter() - t_start
     lat = srv.stats()
-    srv.stop()
     open_steps = sum(r.total_steps for r in results)
+    # the parity sample: the stream's first requests up to >= 131072 walkers,
+    # served with their paths kept, and the same requests through kk_batch_walk
+    n_par, acc = 0, 0
+    while n_par < len(reqs) and acc < 131072:
+        acc += reqs[n_par]["walker_num"]
+        n_par += 1
+    par_reqs = reqs[:n_par]
+    served_paths = []
+    for t in [srv.submit(**r) for r in par_reqs]:
+        res = srv.poll(t, keep_paths=True)
+        assert res.status == 0
+        served_paths.append((np.array(res.paths.path_length), np.array(res.paths.vertices)))
+    srv.stop()
+    batch_paths = [(np.array(ps.path_length), np.array(ps.vertices)) for ps in engine.batch_walk(app, par_reqs)]
 
     # access counts of the stream (binary-search probe counts), for the byte model
     engine.set_option("walk_stats", 1)
@@ -438,53 +626,109 @@ def run_serve_bench(args, wl, world, rank, local):
     b_step = 40 + T * (40 + 32) + P * 32 + 4
     design_b = 40 + T * 32 + Q * 32 + 4
     peak, peak_kind = load_peaks()
-    batched_value = b_steps / (b_ms / 1e3)
     plain_value = p_steps / (p_ms / 1e3)
     rebuild_value = r_steps / (r_ms / 1e3)
-    achieved = batched_value * b_step / 1e9
+    # the walk kernel's own launches: steps and CUDA-event time per launch
+    launch_steps = []
+    prev = 0
+    for ms, cum in kernel_ms:
+        if cum < prev:
+            prev = 0
+        launch_steps.append((ms, cum - prev))
+        prev = cum
+    k_ms = sum(ms for ms, _ in launch_steps)
+    k_steps = sum(st for _, st in launch_steps)
+    mean_launch_ms = k_ms / len(launch_steps)
+    steps_per_launch = k_steps / len(launch_steps)
+    achieved = steps_per_launch * b_step / (mean_launch_ms / 1e3) / 1e9
+    kernel_rate = k_steps / (k_ms / 1e3)
     ceiling = engine.gather_ceiling(4 << 30)
+    traffic = traffic_for(args.workload, "walk_batch_kernel", steps_per_launch)
+
+    parity = cpu = None
     if rank == 0:
-        line = {
-            "metric": "walker-steps/s", "value": served_value, "unit": "walker-steps/s", "n_gpus": world,
-            "steps": 1, "warmup": args.warmup, "ms_per_step": s_s * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded R-MAT generated on the GPU, seeded request stream)",
-            "config": {"workload": args.workload, "desc": wl["desc"], "vertices": V, "edges": E,
-                       "requests": len(reqs), "walker_step_capacity": total_req_steps_cap,
-                       "parallelism": "replicas", "l2": "inputs larger than L2", "slots": 2, "max_jobs": 256,
-                       "tuned": best, "tuning_ms": [[c, ms] for c, ms in tune_table]},
-            "served": {"value": served_value, "what": "all requests submitted at once; submit -> paths on host",
-                       "batches": sat["batches"], "mean_batch_jobs": sat["mean_batch_jobs"],
-                       "slot_time_ms": {"walk": sat["walk_ms"], "copy_to_pinned": sat["copy_ms"],
-                                        "per_request_copies": sat["host_ms"]}},
-            "latency": {"offered_rate_req_s": rate, "p50_ms": lat["p50_ms"], "p99_ms": lat["p99_ms"],
-                        "mean_ms": lat["mean_ms"], "throughput": open_steps / open_s,
-                        "what": "open-loop Poisson arrivals at 70% of the saturated rate"},
-            "batched": {"value": batched_value, "unit": "walker-steps/s", "ms": b_ms,
-                        "what": "kk_batch_walk_device, 1024 requests per launch, paths in HBM"},
-            "plain": {"value": plain_value, "unit": "walker-steps/s", "requests": n_plain,
-                      "what": "one kk_walk_device launch per request, alias tables kept"},
-            "plain_rebuild": {"value": rebuild_value, "unit": "walker-steps/s", "requests": 12,
-                              "what": "one launch per request, alias tables rebuilt per call (reference)"},
-            "served_over_plain": served_value / plain_value,
-            "batched_over_plain": batched_value / plain_value,
-            "e2e": {"value": served_value, "unit": "walker-steps/s",
-                    "h2d_bytes_per_step": len(reqs) * 120, "d2h_bytes_per_step": 4 * (s_steps + sum(
-                        r["walker_num"] for r in reqs))},
-            "gpu_launches": sat["batches"],
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
-                         "bytes_per_step": b_step, "design_bytes_per_step": design_b,
-                         "access_counts": {"trials_per_step": T, "queries_per_step": Q, "probes_per_step": P},
-                         "kernel": "walk_batch_kernel (second order), from the batched throughput",
-                         "gather": {"ceiling_reads_per_s": ceiling, "reads_per_step": T + Q,
-                                    "achieved_reads_per_s": batched_value * (T + Q),
-                                    "frac": batched_value * (T + Q) / ceiling,
-                                    "what": "alias buckets + edge-set sectors per step (batched throughput) vs "
-                                            "kk_gather_ceiling (4 GiB, this GPU, this run)"}},
-            "cpu_baseline": None, "clocks": clocks.summary(),
+        threads = os.cpu_count() or 1
+        csr, alias, t_alias = host_graph(engine, app, threads)
+        parity = {
+            "served": parity_requests(served_paths, csr, alias, par_reqs, threads,
+                                      "served paths (kk_serve_poll) of the stream's first requests vs the oracle's "
+                                      "node2vec walks of the same requests, bit for bit"),
+            "batched": parity_requests(batch_paths, csr, alias, par_reqs, threads,
+                                       "the same requests through kk_batch_walk vs the oracle"),
         }
-        print(json.dumps(line))
+        parity["walkers_checked"] = parity["served"]["walkers_checked"] + parity["batched"]["walkers_checked"]
+        parity["mismatches"] = parity["served"]["mismatches"] + parity["batched"]["mismatches"]
+        if not args.no_cpu:
+            cpu, _ = cpu_sample_requests(csr, alias, t_alias, reqs, n_par, threads)
+        del csr, alias
+    engine.close()
+    if rank != 0:
+        return None
+    d2h = 0
+    for r in reqs:
+        d2h += r["walker_num"] * (4 + 8 + 4)
+    d2h = args.steps * d2h + 4 * s_steps
+    line = {
+        "metric": "walker-steps/s", "value": value, "unit": "walker-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": b_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded R-MAT generated on the GPU, seeded request stream)",
+        "config": {"workload": args.workload, "desc": wl["desc"], "vertices": V, "edges": E,
+                   "requests": len(reqs), "walker_step_capacity": stream_cap,
+                   "walker_steps_per_step": b_steps / args.steps,
+                   "step": "one pass of the whole request stream",
+                   "parallelism": "replicas", "l2": "inputs larger than L2 (graph, alias tables, edge set)",
+                   "slots": 2, "max_jobs": 256, "tuned": best,
+                   "tuning_ms": [[c, ms] for c, ms in tune_table]},
+        "batched": {"value": value, "unit": "walker-steps/s", "ms_per_pass": b_ms / args.steps,
+                    "what": "kk_batch_walk_device, 1024 requests per launch, paths in HBM (the line's value)"},
+        "plain": {"value": plain_value, "unit": "walker-steps/s", "requests": n_plain,
+                  "what": "one kk_walk_device launch per request, alias tables kept"},
+        "plain_rebuild": {"value": rebuild_value, "unit": "walker-steps/s", "requests": 12,
+                          "what": "one launch per request, alias tables rebuilt per call (as the reference's "
+                                  "random_walk does)"},
+        "served": {"value": served_value, "unit": "walker-steps/s",
+                   "what": "kk_serve_*, every request of a pass submitted at once; submit -> paths on the host "
+                           "(the line's e2e)",
+                   "batches": sat["batches"], "mean_batch_jobs": sat["mean_batch_jobs"],
+                   "slot_time_ms": {"walk": sat["walk_ms"], "copy_to_pinned": sat["copy_ms"],
+                                    "per_request_copies": sat["host_ms"]}},
+        "batched_over_plain": value / plain_value,
+        "served_over_plain": served_value / plain_value,
+        "latency": {"offered_rate_req_s": rate, "p50_ms": lat["p50_ms"], "p99_ms": lat["p99_ms"],
+                    "mean_ms": lat["mean_ms"], "throughput": open_steps / open_s,
+                    "what": "open-loop Poisson arrivals at 70% of the saturated rate; submit -> paths on the host"},
+        "e2e": {"value": served_value, "unit": "walker-steps/s",
+                "h2d_bytes_per_step": (sat["batches"] // max(args.steps, 1)) * 1024 * SERVE_JOB_BYTES,
+                "d2h_bytes_per_step": d2h // args.steps},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "bytes_per_step": b_step, "design_bytes_per_step": design_b,
+                     "access_counts": {"trials_per_step": T, "queries_per_step": Q, "probes_per_step": P},
+                     "kernel": "walk_batch_kernel (second order)", "kernel_ms": mean_launch_ms,
+                     "launches": len(launch_steps), "steps_per_launch": steps_per_launch,
+                     "gather": {"ceiling_reads_per_s": ceiling, "reads_per_step": T + Q,
+                                "achieved_reads_per_s": kernel_rate * (T + Q),
+                                "frac": kernel_rate * (T + Q) / ceiling,
+                                "what": "alias buckets + edge-set sectors per step of the walk kernel's launches vs "
+                                        "kk_gather_ceiling (4 GiB, this GPU, this run)"}},
+        "parity": parity,
+        "cpu_baseline": cpu, "clocks": clocks.summary(),
+    }
+    return line
+
+
+def traffic_for(workload, kernel, steps_per_launch):
+    """ncu's DRAM bytes per walker-step of `kernel` (profiles/traffic_<workload>.json,
+    captured on a smaller case of the same kernel) scaled to a full launch."""
+    tf = os.path.join(ROOT, "profiles", "traffic_%s.json" % workload.split("@")[0])
+    if not os.path.exists(tf):
+        return None
+    with open(tf) as f:
+        per_kernel = json.load(f)["dram_bytes_per_step"]
+    b = per_kernel.get(kernel) if isinstance(per_kernel, dict) else per_kernel
+    return b * steps_per_launch if b is not None else None
 
 
 def run_batch_bench(args, wl, world, rank, local):
@@ -553,11 +797,16 @@ def run_batch_bench(args, wl, world, rank, local):
         d2h += sum(r["walker_num"] * 12 + r["vertices"] * 4 for r in res)
     e2e_s = allreduce(world, time.perf_counter() - t0, "max")
     e2e_value = allreduce(world, float(e_steps), "sum") / e2e_s
-    cpu = None
-    if rank == 0 and not args.no_cpu:
-        g = engine.download_graph()
-        cpu = cpu_sample(g, dict(wl, walk_length=max(j["walk_length"] for j in jobs)), V, os.cpu_count() or 1,
-                         seed=1)
+    cpu = parity = None
+    if rank == 0:
+        threads = os.cpu_count() or 1
+        csr, alias, t_alias = host_graph(engine, app, threads)
+        parity = parity_jobs(engine, csr, alias, app, jobs, threads)
+        if not args.no_cpu:
+            cpu = cpu_sample(csr, alias, t_alias, dict(wl, walk_length=max(j["walk_length"] for j in jobs)), V,
+                             threads, seed=1)
+        del csr, alias
+    engine.close()
     if rank == 0:
         line = {
             "metric": "walker-steps/s", "value": value, "unit": "walker-steps/s", "n_gpus": world,
@@ -574,15 +823,35 @@ def run_batch_bench(args, wl, world, rank, local):
             "e2e": {"value": e2e_value, "unit": "walker-steps/s", "h2d_bytes_per_step": 64 * len(jobs),
                     "d2h_bytes_per_step": d2h // e2e_runs},
             "gpu_launches": b_launches,
+            "parity": parity,
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
         }
-        print(json.dumps(line), flush=True)
-    engine.close()
+        return line
+    return None
+
+
+def parity_jobs(engine, csr, alias, app, jobs, threads, per=8192):
+    """Every job of a batch through kk_batch_walk (paths to the host) against
+    the oracle's walk of the same job, on each job's first `per` walkers."""
+    res = engine.batch_walk(app, jobs)
+    checked = mism = 0
+    weighted = csr.w is not None
+    for ps, j in zip(res, jobs):
+        n = min(per, j["walker_num"])
+        kw = {k: j[k] for k in ("walk_length", "terminate_prob", "p", "q", "schemes", "scheme_round_robin") if k in j}
+        lens, verts, _ = oracle_paths(csr, alias, app, threads, j.get("walk_length", 4095) + 1, seed=j["seed"],
+                                      walker_begin=j.get("walker_begin", 0), walker_num=n, weighted=weighted, **kw)
+        tot = int(np.asarray(ps.path_length[:n], np.int64).sum())
+        mism += count_mismatches(ps.path_length[:n], ps.vertices[:tot], lens, verts)
+        checked += n
+    del res
+    return {"jobs": len(jobs), "walkers_checked": checked, "mismatches": mism,
+            "what": "each job's first %d walkers through kk_batch_walk vs the oracle's walk of the job, bit for "
+                    "bit" % per}
 
 
 def run_ours(args, wl, world, rank, local):
-    import numpy as np
     import torch
 
     import knightking_gb300 as kk
@@ -703,14 +972,8 @@ def run_ours(args, wl, world, rank, local):
     roof = None
     if b_step is not None:
         achieved = steps_per_launch * b_step / (mean_walk_ms / 1e3) / 1e9
-        traffic = None
-        tf = os.path.join(ROOT, "profiles", "traffic_%s.json" % args.workload)
-        if os.path.exists(tf):
-            with open(tf) as f:
-                per_kernel = json.load(f)["dram_bytes_per_step"]
-            # ncu's DRAM bytes per step of the kernel this run launched
-            b = per_kernel.get(walk_kernel_name(app, best)) if isinstance(per_kernel, dict) else per_kernel
-            traffic = b * steps_per_launch if b is not None else None
+        # ncu's DRAM bytes per step of the kernel this run launched
+        traffic = traffic_for(args.workload, walk_kernel_name(app, best), steps_per_launch)
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_kind": peak_kind, "bytes_per_step": b_step,
                 "design_bytes_per_step": design_b, "access_counts": counts,
@@ -741,10 +1004,15 @@ def run_ours(args, wl, world, rank, local):
     if roof is not None:
         roof["gather"] = gather
 
-    cpu = None
-    if rank == 0 and not args.no_cpu:
-        g = engine.download_graph()
-        cpu = cpu_sample(g, wl, walkers, os.cpu_count() or 1, seed=1)
+    cpu = parity = None
+    if rank == 0:
+        threads = os.cpu_count() or 1
+        csr, alias, t_alias = host_graph(engine, app, threads)
+        parity = parity_ranges(engine, csr, alias, wl, walkers, threads)
+        if not args.no_cpu:
+            cpu = cpu_sample(csr, alias, t_alias, wl, walkers, threads, seed=1)
+        del csr, alias
+    engine.close()
 
     if rank == 0:
         line = {
@@ -762,11 +1030,24 @@ def run_ours(args, wl, world, rank, local):
                     "d2h_bytes_per_step": d2h // e2e_runs, "call_ms": call_ms},
             "gpu_launches": launches,
             "roofline": roof,
+            "parity": parity,
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
         }
-        print(json.dumps(line), flush=True)
-    engine.close()
+        return line
+    return None
+
+
+DEFAULT_WORKLOAD = "node2vec-serve-s24"
+SECOND_WORKLOAD = "deepwalk-s22"
+
+
+def run_workload(args, wl, world, rank, local):
+    if "batch" in wl:
+        return run_batch_bench(args, wl, world, rank, local)
+    if "serve" in wl:
+        return run_serve_bench(args, wl, world, rank, local)
+    return run_ours(args, wl, world, rank, local)
 
 
 def main():
@@ -775,12 +1056,16 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="deepwalk-s22", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=None, choices=sorted(WORKLOADS),
+                    help="default: %s, with %s measured in the same run under the key 'also'"
+                         % (DEFAULT_WORKLOAD, SECOND_WORKLOAD))
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--scale", type=int, default=None, help="override the R-MAT scale (profiling on a small case)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    default_run = args.workload is None and args.scale is None
+    args.workload = args.workload or DEFAULT_WORKLOAD
     wl = dict(WORKLOADS[args.workload])
     if args.scale is not None:
         wl["scale"] = args.scale
@@ -789,12 +1074,18 @@ def main():
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, wl, world, rank, local)
-    elif "batch" in wl:
-        run_batch_bench(args, wl, world, rank, local)
-    elif "serve" in wl:
-        run_serve_bench(args, wl, world, rank, local)
     else:
-        run_ours(args, wl, world, rank, local)
+        line = run_workload(args, wl, world, rank, local)
+        if default_run and args.impl == "ours":
+            # the second workload (weighted DeepWalk, alias build in every step)
+            # in the same run, reported inside the same line
+            a2 = argparse.Namespace(**vars(args))
+            a2.workload = SECOND_WORKLOAD
+            second = run_workload(a2, dict(WORKLOADS[SECOND_WORKLOAD]), world, rank, local)
+            if line is not None:
+                line["also"] = {SECOND_WORKLOAD: second}
+        if rank == 0 and line is not None:
+            print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

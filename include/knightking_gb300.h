@@ -330,6 +330,13 @@ kk_status kk_last_walk_timing(const kk_engine *e, float *alias_ms, float *walk_m
  * allocates and frees `bytes` of device memory. */
 kk_status kk_gather_ceiling(kk_engine *e, uint64_t bytes, double *reads_per_s);
 
+/* n blocks of the walk's generator, Philox4x32-10, computed by a device
+ * kernel on the current device: host arrays ctr[4n] in and out[4n] out, key =
+ * seed (low 32 bits k0, high 32 bits k1).  For known-answer checks of the
+ * random stream that replaces StdRandNumGenerator (include/util.hpp:45-70);
+ * allocates and frees 32n bytes of device memory and synchronises. */
+kk_status kk_philox_blocks(uint64_t seed, uint32_t n, const uint32_t *ctr, uint32_t *out);
+
 /* Kernels this library has launched on the engine's streams since the engine
  * was created (alias builds, walks, batches, graph loading; the replays of a
  * serving slot's captured CUDA graph are not counted). */

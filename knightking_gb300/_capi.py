@@ -142,6 +142,7 @@ _SIGS = {
     "kk_engine_launch_count": (ctypes.c_int, [_P, _P]),
     "kk_gather_ceiling": (ctypes.c_int, [_P, ctypes.c_uint64, _P]),
     "kk_last_walk_stats": (ctypes.c_int, [_P, _P, _P, _P]),
+    "kk_philox_blocks": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint32, _P, _P]),
     "kk_serve_start": (ctypes.c_int, [_P, _P, _P]),
     "kk_serve_submit": (ctypes.c_int, [_P, _P, _P]),
     "kk_serve_poll": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.c_int, _P]),

@@ -167,7 +167,9 @@ __global__ void __launch_bounds__(256) noalloc_alias_kernel(const int64_t *off, 
 
 std::mutex g_setup_lock;
 uint2 *g_scratch_ptr[128] = {};
-bool g_smem_attr_set = false;
+/* cudaFuncSetAttribute applies to the current device only, so the shared-memory
+ * opt-in is recorded per device like the scratch address */
+bool g_smem_attr_set[128] = {};
 
 } // namespace
 
@@ -194,12 +196,12 @@ extern "C" kk_status kk_alias_build_noalloc(uint32_t v_num, const int64_t *d_off
                 return KK_ERR_CUDA;
             }
         }
-        if (!g_smem_attr_set)
+        if (!g_smem_attr_set[dev])
         {
             if (cudaFuncSetAttribute(noalloc_alias_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)kNoAllocSmem) != cudaSuccess)
                 return KK_ERR_CUDA;
-            g_smem_attr_set = true;
+            g_smem_attr_set[dev] = true;
         }
         scratch = g_scratch_ptr[dev];
     }
@@ -221,8 +223,9 @@ extern "C" kk_status kk_alias_build_noalloc(uint32_t v_num, const int64_t *d_off
     unsigned int warp_blocks = (v_num + 7) / 8 < 3u * sms ? (v_num + 7) / 8 : 3u * sms;
     noalloc_alias_kernel<<<warp_blocks, 256, kNoAllocSmem, st>>>(d_off, d_w, v_num, d_p, d_p_idx, d_q_idx, d_sum,
                                                                  scratch, 0);
-    noalloc_alias_kernel<<<kNoAllocSlots / 8, 256, kNoAllocSmem, st>>>(d_off, d_w, v_num, d_p, d_p_idx, d_q_idx,
-                                                                       d_sum, scratch, 1);
+    /* the large-degree pass keeps its queues in the scratch slices: no shared memory */
+    noalloc_alias_kernel<<<kNoAllocSlots / 8, 256, 0, st>>>(d_off, d_w, v_num, d_p, d_p_idx, d_q_idx, d_sum, scratch,
+                                                            1);
     if (cudaGetLastError() != cudaSuccess)
         return KK_ERR_CUDA;
     return KK_OK;

@@ -1238,6 +1238,34 @@ kk_status kk_gather_ceiling(kk_engine *e, uint64_t bytes, double *reads_per_s)
     });
 }
 
+static __global__ void philox_blocks_kernel(uint32_t k0, uint32_t k1, uint32_t n, const uint4 *ctr, uint4 *out)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        out[i] = kk::philox4x32_10(ctr[i], k0, k1);
+}
+
+kk_status kk_philox_blocks(uint64_t seed, uint32_t n, const uint32_t *ctr, uint32_t *out)
+{
+    if (n == 0 || !ctr || !out)
+        return KK_ERR_INVALID_CONFIG;
+    uint4 *d = nullptr;
+    if (cudaMalloc(&d, (size_t)n * 32) != cudaSuccess)
+        return KK_ERR_OOM;
+    kk_status st = KK_OK;
+    if (cudaMemcpy(d, ctr, (size_t)n * 16, cudaMemcpyHostToDevice) != cudaSuccess)
+        st = KK_ERR_CUDA;
+    if (st == KK_OK)
+    {
+        philox_blocks_kernel<<<(n + 255) / 256, 256>>>((uint32_t)seed, (uint32_t)(seed >> 32), n, d, d + n);
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpy(out, d + n, (size_t)n * 16, cudaMemcpyDeviceToHost) != cudaSuccess)
+            st = KK_ERR_CUDA;
+    }
+    cudaFree(d);
+    return st;
+}
+
 kk_status kk_engine_launch_count(const kk_engine *e, uint64_t *count)
 {
     if (!e || !count)

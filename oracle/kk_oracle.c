@@ -616,6 +616,13 @@ static int ko_walk_one(const ko_ctx *c, uint32_t id, uint32_t cap, uint32_t *len
 int ko_walk(const ko_graph *g, const ko_walk_params *p, uint32_t cap, uint32_t *out_len, uint32_t *out_path, int threads,
             uint64_t *total_steps)
 {
+    return ko_walk_alias(g, p, cap, out_len, out_path, threads, total_steps, NULL, NULL, NULL, NULL);
+}
+
+int ko_walk_alias(const ko_graph *g, const ko_walk_params *p, uint32_t cap, uint32_t *out_len, uint32_t *out_path,
+                  int threads, uint64_t *total_steps, const float *alias_p, const uint32_t *alias_pi,
+                  const uint32_t *alias_qi, const float *alias_sum)
+{
     ko_ctx c;
     memset(&c, 0, sizeof(c));
     c.g = g;
@@ -705,13 +712,22 @@ int ko_walk(const ko_graph *g, const ko_walk_params *p, uint32_t cap, uint32_t *
         }
     }
     double t0 = ko_now();
-    if (p->weighted)
+    const int own_alias = p->weighted && alias_p == NULL;
+    if (own_alias)
     {
         c.ap = (float *)malloc(sizeof(float) * g->E);
         c.api = (uint32_t *)malloc(sizeof(uint32_t) * g->E);
         c.aqi = (uint32_t *)malloc(sizeof(uint32_t) * g->E);
         c.sum = (float *)calloc(V, sizeof(float));
         ko_alias_build(g, c.ap, c.api, c.aqi, c.sum, threads);
+    }
+    else if (p->weighted)
+    {
+        /* tables the caller built with ko_alias_build on this graph */
+        c.ap = (float *)alias_p;
+        c.api = (uint32_t *)alias_pi;
+        c.aqi = (uint32_t *)alias_qi;
+        c.sum = (float *)alias_sum;
     }
     if (c.outlier)
     {
@@ -748,10 +764,13 @@ int ko_walk(const ko_graph *g, const ko_walk_params *p, uint32_t cap, uint32_t *
     g_walk_seconds = t2 - t1;
     if (total_steps)
         *total_steps = steps;
-    free(c.ap);
-    free(c.api);
-    free(c.aqi);
-    free(c.sum);
+    if (own_alias)
+    {
+        free(c.ap);
+        free(c.api);
+        free(c.aqi);
+        free(c.sum);
+    }
     free(c.ub);
     free(c.lb);
     free(c.ra);
@@ -862,4 +881,10 @@ void ko_radix_sort_u64(uint64_t n, uint64_t *keys, uint64_t *tmp, int bits, int 
     if (src != keys)
         memcpy(keys, src, n * sizeof(uint64_t));
     free(hist);
+}
+
+void ko_philox_blocks(uint64_t seed, uint64_t n, const uint32_t *ctr, uint32_t *out)
+{
+    for (uint64_t i = 0; i < n; i++)
+        kko_philox4x32_10(ctr + 4 * i, seed, out + 4 * i);
 }

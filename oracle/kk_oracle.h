@@ -84,6 +84,14 @@ void ko_sort_adjacency(uint32_t V, const int64_t *off, uint32_t *nbr, float *w, 
 int ko_walk(const ko_graph *g, const ko_walk_params *prm, uint32_t cap, uint32_t *out_len, uint32_t *out_path,
             int threads, uint64_t *total_steps);
 
+/* ko_walk with the weight alias tables (and sums) of this graph built
+ * beforehand by ko_alias_build, instead of building them in the call as the
+ * reference's random_walk does (include/walk.hpp:538-652); NULL tables build
+ * them as ko_walk does.  For many calls on one large graph. */
+int ko_walk_alias(const ko_graph *g, const ko_walk_params *prm, uint32_t cap, uint32_t *out_len, uint32_t *out_path,
+                  int threads, uint64_t *total_steps, const float *alias_p, const uint32_t *alias_pi,
+                  const uint32_t *alias_qi, const float *alias_sum);
+
 /* Seconds spent in the alias build and in the walk by the last ko_walk call. */
 void ko_last_timing(double *alias_seconds, double *walk_seconds);
 
@@ -94,6 +102,10 @@ void ko_rmat_draw(uint32_t scale, uint64_t m, uint64_t ta, uint64_t tab, uint64_
 void ko_radix_sort_u64(uint64_t n, uint64_t *keys, uint64_t *tmp, int bits, int threads);
 void ko_pair_data(uint64_t n, const uint32_t *src, const uint32_t *dst, uint64_t seed, int weights, uint32_t types,
                   float *w, uint8_t *t, int threads);
+
+/* n Philox4x32-10 blocks of the oracle's generator: ctr[4i..4i+3] in,
+ * out[4i..4i+3] out, key = seed (low word k0, high word k1). */
+void ko_philox_blocks(uint64_t seed, uint64_t n, const uint32_t *ctr, uint32_t *out);
 
 #ifdef __cplusplus
 }

@@ -62,10 +62,17 @@ _lib = None
 
 
 def build(force=False):
-    """Compile liboracle.so with its Makefile (gcc only)."""
-    if force or not os.path.exists(LIB_PATH):
-        subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    """Compile liboracle.so with its Makefile (gcc only; make rebuilds it when
+    a source is newer)."""
+    subprocess.run(["make", "-s", "-C", HERE] + (["-B"] if force else []) + ["liboracle.so"], check=True)
     return LIB_PATH
+
+
+def ref_root():
+    """Where the reference's sources lie: the oracle Makefile's REF_ROOT
+    (environment variable KK_REFERENCE_ROOT, else the recipe's default)."""
+    r = subprocess.run(["make", "-s", "-C", HERE, "ref-root"], capture_output=True, text=True)
+    return r.stdout.strip() if r.returncode == 0 else ""
 
 
 def build_ref():
@@ -82,6 +89,10 @@ def lib():
         _lib.ko_walk.restype = ctypes.c_int
         _lib.ko_walk.argtypes = [ctypes.POINTER(Graph), ctypes.POINTER(WalkParams), ctypes.c_uint32,
                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_uint64)]
+        _lib.ko_walk_alias.restype = ctypes.c_int
+        _lib.ko_walk_alias.argtypes = [ctypes.POINTER(Graph), ctypes.POINTER(WalkParams), ctypes.c_uint32,
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_uint64),
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         _lib.ko_alias_build.restype = None
         _lib.ko_alias_build.argtypes = [ctypes.POINTER(Graph), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_int]
@@ -173,14 +184,18 @@ def make_params(app, seed=1, walker_begin=0, walker_num=0, walk_length=80, termi
     return prm
 
 
-def walk(csr, prm, cap, threads=0, with_paths=True):
-    """Returns (lens, flat_paths, total_steps); flat_paths concatenates each walker's path."""
+def walk(csr, prm, cap, threads=0, with_paths=True, alias=None):
+    """Returns (lens, flat_paths, total_steps); flat_paths concatenates each walker's path.
+    alias: the (p, p_idx, q_idx, sum) of alias_build(csr), reused instead of
+    building the tables in the call."""
     n = prm.walker_num
     lens = np.zeros(n, np.uint32)
     buf = np.zeros(n * cap, np.uint32) if with_paths else None
     steps = ctypes.c_uint64(0)
     g = csr.c()
-    st = lib().ko_walk(ctypes.byref(g), ctypes.byref(prm), cap, _ptr(lens), _ptr(buf), threads, ctypes.byref(steps))
+    a = [None] * 4 if alias is None else [_ptr(x) for x in alias]
+    st = lib().ko_walk_alias(ctypes.byref(g), ctypes.byref(prm), cap, _ptr(lens), _ptr(buf), threads,
+                             ctypes.byref(steps), *a)
     if st != 0:
         raise RuntimeError("ko_walk failed with status %d" % st)
     if not with_paths:

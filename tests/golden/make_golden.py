@@ -33,7 +33,7 @@ from oracle import graphs as G  # noqa: E402
 from oracle import pyoracle as O  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
-KARATE = "/root/reference/dataset/karate.txt"
+KARATE = os.path.join(O.ref_root(), "dataset", "karate.txt")  # the oracle recipe's REF_ROOT
 
 SCHEMES = [  # 3 schemes x 4 states over 5 edge types, as type masks
     [0b00001, 0b00010, 0b00100, 0b01000],

@@ -468,6 +468,14 @@ def parity_requests(results, csr, alias, reqs, threads, what):
             "what": what}
 
 
+def n2v_outlier(p, q):
+    """Whether node2vec (p, q) is in the outlier regime: the overflow
+    1/p - max(1, 1/q), computed in double and rounded to float as
+    src/apps/node2vec.hpp:126-139 does, is positive."""
+    ub = np.float32(max(1.0 / float(np.float32(q)), 1.0))
+    return float(np.float32(1.0 / float(np.float32(p)) - float(ub))) > 0.0
+
+
 SERVE_JOB_BYTES = 72  # one BatchJob record (walk.cuh), uploaded per job slot of a batch
 
 
@@ -623,8 +631,13 @@ def run_serve_bench(args, wl, world, rank, local):
     engine.set_option("walk_stats", 0)
     engine.set_option("node2vec_adjacency", best.get("node2vec_adjacency", 0))
     T, Q, P = trials / c_steps, queries / c_steps, probes / c_steps
+    # return-edge lookups of the outlier bound: one per step of a request in
+    # the outlier regime (1/p > max(1, 1/q)), from the requests' own step counts
+    per_job = engine.batch_walk(app, reqs[:1024], keep_paths=False)
+    r_steps = sum(res["total_steps"] for res, r in zip(per_job, reqs[:1024]) if n2v_outlier(r["p"], r["q"]))
+    R = r_steps / max(1, sum(res["total_steps"] for res in per_job))
     b_step = 40 + T * (40 + 32) + P * 32 + 4
-    design_b = 40 + T * 32 + Q * 32 + 4
+    design_b = 40 + T * 32 + Q * 32 + R * 64 + 4
     peak, peak_kind = load_peaks()
     plain_value = p_steps / (p_ms / 1e3)
     rebuild_value = r_steps / (r_ms / 1e3)
@@ -705,13 +718,15 @@ def run_serve_bench(args, wl, world, rank, local):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "bytes_per_step": b_step, "design_bytes_per_step": design_b,
-                     "access_counts": {"trials_per_step": T, "queries_per_step": Q, "probes_per_step": P},
+                     "access_counts": {"trials_per_step": T, "queries_per_step": Q, "probes_per_step": P,
+                                       "return_edge_lookups_per_step": R},
                      "kernel": "walk_batch_kernel (second order)", "kernel_ms": mean_launch_ms,
                      "launches": len(launch_steps), "steps_per_launch": steps_per_launch,
-                     "gather": {"ceiling_reads_per_s": ceiling, "reads_per_step": T + Q,
-                                "achieved_reads_per_s": kernel_rate * (T + Q),
-                                "frac": kernel_rate * (T + Q) / ceiling,
-                                "what": "alias buckets + edge-set sectors per step of the walk kernel's launches vs "
+                     "gather": {"ceiling_reads_per_s": ceiling, "reads_per_step": T + Q + R,
+                                "achieved_reads_per_s": kernel_rate * (T + Q + R),
+                                "frac": kernel_rate * (T + Q + R) / ceiling,
+                                "what": "alias buckets + edge-set sectors of the adjacency queries + return-edge "
+                                        "lookups of the outlier bound, per step of the walk kernel's launches, vs "
                                         "kk_gather_ceiling (4 GiB, this GPU, this run)"}},
         "parity": parity,
         "cpu_baseline": cpu, "clocks": clocks.summary(),

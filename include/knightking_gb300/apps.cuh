@@ -141,18 +141,38 @@ struct Node2vecDyn
  * overflow * w(return edge) (weighted), one outlier.  Where the previous
  * vertex is not a neighbour (directed graphs) the reference reads past the
  * adjacency; here the area is empty. */
-/* The position std::lower_bound(N(v), x) of node2vec.hpp:71-78 / :91-97: from
- * the edge set when x is a neighbour (its smallest index), else by search. */
-__device__ __forceinline__ uint32_t n2v_lower_bound(const uint32_t *nbr, const EdgeSetView &set, vertex_id_t v,
-                                                    const AdjList &adj, vertex_id_t x)
+/* The return edge std::lower_bound(N(v), x) of node2vec.hpp:71-78 / :91-97:
+ * its local index i (deg if none) and, when want_weight, its weight.  x = 0
+ * (the value-initialised state of step 0) is at or below every neighbour, so
+ * its position is 0 with no lookup; a neighbour x comes from the edge set,
+ * index and weight in one access; anything else by binary search. */
+__device__ __forceinline__ uint32_t n2v_return_edge(const uint32_t *nbr, const float *w, const EdgeSetView &set,
+                                                    vertex_id_t v, const AdjList &adj, vertex_id_t x, bool want_weight,
+                                                    float &weight, bool &is_x)
 {
-    if (set.keys != nullptr)
+    const uint32_t deg = adj.degree();
+    uint32_t i;
+    is_x = false;
+    if (x == 0)
     {
-        const uint64_t slot = edge_set_slot(set, v, x);
-        if (slot != ~0ull)
-            return __ldg(set.pos + slot);
+        i = 0;
     }
-    return lower_bound_adj(nbr, adj.begin, adj.degree(), x);
+    else
+    {
+        if (set.keys != nullptr)
+        {
+            uint32_t pos;
+            if (edge_set_find(set, v, x, pos, weight))
+            {
+                is_x = true; /* the edge at pos leads to x */
+                return pos;
+            }
+        }
+        i = lower_bound_adj(nbr, adj.begin, deg, x);
+    }
+    if (want_weight && i < deg)
+        weight = gather(w + adj.begin + i);
+    return i;
 }
 
 template <bool Weighted>
@@ -175,9 +195,10 @@ struct Node2vecOutlierUB
                 area = overflow;
                 return;
             }
-            uint32_t deg = adj.degree();
-            uint32_t i = n2v_lower_bound(nbr, set, v, adj, wk.data.previous_vertex);
-            area = i < deg ? fmul(gather(w + adj.begin + i), overflow) : 0.0f;
+            float rw = 0.0f;
+            bool is_x;
+            const uint32_t i = n2v_return_edge(nbr, w, set, v, adj, wk.data.previous_vertex, true, rw, is_x);
+            area = i < adj.degree() ? fmul(rw, overflow) : 0.0f;
         }
         else
         {
@@ -194,11 +215,13 @@ struct Node2vecOutlierSearch
     __device__ __forceinline__ bool operator()(const Walker<Node2vecState> &wk, vertex_id_t v, const AdjList &adj,
                                                vertex_id_t, AdjUnit &out) const
     {
-        uint32_t deg = adj.degree();
-        uint32_t i = n2v_lower_bound(nbr, set, v, adj, wk.data.previous_vertex);
-        if (i >= deg)
+        float unused = 0.0f;
+        bool is_x;
+        const vertex_id_t x = wk.data.previous_vertex;
+        const uint32_t i = n2v_return_edge(nbr, nullptr, set, v, adj, x, false, unused, is_x);
+        if (i >= adj.degree())
             return false;
-        out = AdjUnit{gather(nbr + adj.begin + i), adj.begin + i};
+        out = AdjUnit{is_x ? x : gather(nbr + adj.begin + i), adj.begin + i};
         return true;
     }
 };

@@ -332,7 +332,7 @@ struct kk_engine
     /* node2vec adjacency test: 0 edge set (built once per graph), 1 binary
      * search of the sorted adjacency (option node2vec_adjacency) */
     int n2v_adjacency = 0;
-    kk::DevBuf edge_set, edge_pos;
+    kk::DevBuf edge_set;
     uint64_t edge_set_nb = 0;
     bool edge_set_valid = false;
     kk::DevBuf schemes;    /* metapath schemes of the running job */

@@ -108,23 +108,24 @@ struct SecondOrderTransitionConfig
 };
 
 /* ---- edge set ---------------------------------------------------------------
- * Exact lookup of directed edges (u, v): open addressing over 32 B buckets of
- * four 64-bit keys u << 32 | v (one sector), linear probing bucket by bucket
- * from bucket mulhi(mix(key), nbuckets), 4 * nbuckets >= 4E so the load is at
- * most 1/4 and a lookup rarely leaves its first bucket.
- * Beside each key slot a 32-bit position: the smallest index of (u, v) within
- * u's adjacency, which for a sorted adjacency is std::lower_bound's position
- * of v in N(u).  Keys only go from empty to filled and an insert moves past a
- * bucket only when all four of its slots hold other keys, so a lookup that
- * meets an empty slot may stop.  A membership test reads one 32 B sector in
- * the common case, where a binary search of a sorted adjacency reads about
- * log2(degree) dependent sectors. */
+ * Exact lookup of directed edges (u, v): open addressing over 64 B buckets,
+ * linear probing bucket by bucket from bucket mulhi(mix(key), nbuckets), with
+ * 4 * nbuckets >= 4E slots so the load is at most 1/4 and a lookup rarely
+ * leaves its first bucket.  A bucket is eight 64-bit words: four keys
+ * u << 32 | v (one 32 B sector), then per slot (pos << 32 | weight bits):
+ * the smallest index of (u, v) within u's adjacency, which for a sorted
+ * adjacency is std::lower_bound's position of v in N(u), and the weight of
+ * that edge (0 without weights).  A membership test reads the key sector; the
+ * return-edge lookup of node2vec's outlier bound reads the whole bucket and
+ * has the edge's position and weight in the same access.  Keys only go from
+ * empty to filled and an insert moves past a bucket only when all four of its
+ * slots hold other keys, so a lookup that meets an empty slot may stop. */
 constexpr uint64_t kEdgeSetEmpty = ~0ull;
+constexpr uint32_t kEdgeSetWords = 8; /* 64-bit words per bucket */
 
 struct EdgeSetView
 {
-    const uint64_t *keys; /* 4 per bucket; nullptr: no set */
-    const uint32_t *pos;  /* position within the source's adjacency, per key slot */
+    const uint64_t *keys; /* nbuckets buckets of kEdgeSetWords words; nullptr: no set */
     uint64_t nbuckets;
 };
 
@@ -139,14 +140,14 @@ __host__ __device__ __forceinline__ uint64_t mix64(uint64_t x)
     return x;
 }
 
-/* The slot of edge (u, v), or ~0 when (u, v) is not an edge. */
+/* The slot (bucket * 4 + j) of edge (u, v), or ~0 when (u, v) is not an edge. */
 __device__ __forceinline__ uint64_t edge_set_slot(const EdgeSetView &s, vertex_id_t u, vertex_id_t v)
 {
     const uint64_t key = ((uint64_t)u << 32) | v;
     uint64_t b = __umul64hi(mix64(key), s.nbuckets);
     for (uint64_t probe = 0; probe < s.nbuckets; probe++)
     {
-        const uint4 *p = reinterpret_cast<const uint4 *>(s.keys + b * 4);
+        const uint4 *p = reinterpret_cast<const uint4 *>(s.keys + b * kEdgeSetWords);
         uint4 q[2];
 #pragma unroll
         for (int j = 0; j < 2; j++)
@@ -167,8 +168,45 @@ __device__ __forceinline__ uint64_t edge_set_slot(const EdgeSetView &s, vertex_i
     return ~0ull;
 }
 
-__device__ __forceinline__ void edge_set_insert(uint64_t *keys, uint32_t *pos, uint64_t nbuckets, vertex_id_t u,
-                                                vertex_id_t v, uint32_t local)
+/* Edge (u, v)'s first position in N(u) and its weight, read with the keys in
+ * one access per bucket probed; false when (u, v) is not an edge. */
+__device__ __forceinline__ bool edge_set_find(const EdgeSetView &s, vertex_id_t u, vertex_id_t v, uint32_t &pos,
+                                              float &weight)
+{
+    const uint64_t key = ((uint64_t)u << 32) | v;
+    uint64_t b = __umul64hi(mix64(key), s.nbuckets);
+    for (uint64_t probe = 0; probe < s.nbuckets; probe++)
+    {
+        const uint4 *p = reinterpret_cast<const uint4 *>(s.keys + b * kEdgeSetWords);
+        uint4 q[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            q[j] = __ldg(p + j);
+        const uint64_t k[4] = {((uint64_t)q[0].y << 32) | q[0].x, ((uint64_t)q[0].w << 32) | q[0].z,
+                               ((uint64_t)q[1].y << 32) | q[1].x, ((uint64_t)q[1].w << 32) | q[1].z};
+        const uint32_t pw[8] = {q[2].x, q[2].y, q[2].z, q[2].w, q[3].x, q[3].y, q[3].z, q[3].w};
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+        {
+            if (k[j] == key)
+            {
+                weight = __uint_as_float(pw[2 * j]);
+                pos = pw[2 * j + 1];
+                return true;
+            }
+            if (k[j] == kEdgeSetEmpty)
+                return false;
+        }
+        b = b + 1 == s.nbuckets ? 0 : b + 1;
+    }
+    return false;
+}
+
+/* Adds edge (u, v) at local index `local` of N(u), weight wt: the smallest
+ * index of the key wins, with its weight (one 64-bit atomicMin on
+ * local << 32 | weight bits). */
+__device__ __forceinline__ void edge_set_insert(uint64_t *buckets, uint64_t nbuckets, vertex_id_t u, vertex_id_t v,
+                                                uint32_t local, float wt)
 {
     const uint64_t key = ((uint64_t)u << 32) | v;
     uint64_t b = __umul64hi(mix64(key), nbuckets);
@@ -176,11 +214,12 @@ __device__ __forceinline__ void edge_set_insert(uint64_t *keys, uint32_t *pos, u
     {
         for (int j = 0; j < 4; j++)
         {
-            unsigned long long *k = reinterpret_cast<unsigned long long *>(keys + b * 4 + j);
+            unsigned long long *k = reinterpret_cast<unsigned long long *>(buckets + b * kEdgeSetWords + j);
             const unsigned long long old = atomicCAS(k, (unsigned long long)kEdgeSetEmpty, (unsigned long long)key);
             if (old == kEdgeSetEmpty || old == key)
             {
-                atomicMin(pos + b * 4 + j, local);
+                atomicMin(reinterpret_cast<unsigned long long *>(buckets + b * kEdgeSetWords + 4 + j),
+                          ((unsigned long long)local << 32) | __float_as_uint(wt));
                 return;
             }
         }
@@ -190,7 +229,7 @@ __device__ __forceinline__ void edge_set_insert(uint64_t *keys, uint32_t *pos, u
 
 /* Inserts the out-edges of the vertices order[lo, hi): a block per vertex
  * (hubs) or a warp per vertex. */
-static __global__ void edge_set_block_kernel(GraphView g, uint64_t *keys, uint32_t *pos, uint64_t nbuckets,
+static __global__ void edge_set_block_kernel(GraphView g, uint64_t *buckets, uint64_t nbuckets,
                                              const uint32_t *order, uint32_t lo, uint32_t hi)
 {
     for (uint32_t k = lo + blockIdx.x; k < hi; k += gridDim.x)
@@ -198,11 +237,11 @@ static __global__ void edge_set_block_kernel(GraphView g, uint64_t *keys, uint32
         const uint32_t v = order[k];
         const int64_t e0 = g.off[v];
         for (int64_t e = e0 + threadIdx.x; e < g.off[v + 1]; e += blockDim.x)
-            edge_set_insert(keys, pos, nbuckets, v, g.nbr[e], (uint32_t)(e - e0));
+            edge_set_insert(buckets, nbuckets, v, g.nbr[e], (uint32_t)(e - e0), g.w ? g.w[e] : 0.0f);
     }
 }
 
-static __global__ void edge_set_warp_kernel(GraphView g, uint64_t *keys, uint32_t *pos, uint64_t nbuckets,
+static __global__ void edge_set_warp_kernel(GraphView g, uint64_t *buckets, uint64_t nbuckets,
                                             const uint32_t *order, uint32_t lo, uint32_t hi)
 {
     const uint32_t lane = threadIdx.x & 31;
@@ -212,7 +251,7 @@ static __global__ void edge_set_warp_kernel(GraphView g, uint64_t *keys, uint32_
         const uint32_t v = order[k];
         const int64_t e0 = g.off[v];
         for (int64_t e = e0 + lane; e < g.off[v + 1]; e += 32)
-            edge_set_insert(keys, pos, nbuckets, v, g.nbr[e], (uint32_t)(e - e0));
+            edge_set_insert(buckets, nbuckets, v, g.nbr[e], (uint32_t)(e - e0), g.w ? g.w[e] : 0.0f);
     }
 }
 

@@ -238,10 +238,9 @@ void launch_app_batch(kk_engine *e, const BatchPlan &plan, BatchSlot &slot, cons
     }
     else if (plan.app == KK_APP_NODE2VEC)
     {
-        const EdgeSetView set = p ? e->n2v_adjacency == 0 ? EdgeSetView{(const uint64_t *)e->edge_set.p,
-                                                                         (const uint32_t *)e->edge_pos.p,
-                                                                         e->edge_set_nb}
-                                                           : EdgeSetView{nullptr, nullptr, 0}
+        const EdgeSetView set = p ? e->n2v_adjacency == 0
+                                        ? EdgeSetView{(const uint64_t *)e->edge_set.p, e->edge_set_nb}
+                                        : EdgeSetView{nullptr, 0}
                                   : node2vec_edge_set(e);
         if (plan.weighted)
             launch_batch(e, Node2vecBatch<true>{g.nbr, e->d_w, set}, plan, slot, d_jobs, length, path, d_steps,

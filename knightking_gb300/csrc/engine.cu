@@ -735,7 +735,6 @@ void kk_engine_destroy(kk_engine *e)
         e->host_pool->release();
     e->vcur.release();
     e->edge_set.release();
-    e->edge_pos.release();
     e->bslot.release();
     if (e->side)
     {

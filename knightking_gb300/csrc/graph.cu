@@ -257,34 +257,33 @@ const uint4 *cursor_adjacency_of(kk_engine *e)
 EdgeSetView node2vec_edge_set(kk_engine *e)
 {
     if (e->n2v_adjacency != 0)
-        return EdgeSetView{nullptr, nullptr, 0};
+        return EdgeSetView{nullptr, 0};
     if (!e->edge_set_valid)
     {
         const uint64_t nb = e->E > 0 ? e->E : 1; /* four slots per bucket: load <= 1/4 */
-        uint64_t *keys = e->edge_set.as<uint64_t>(nb * 4);
-        uint32_t *pos = e->edge_pos.as<uint32_t>(nb * 4);
-        KK_CUDA_CHECK(cudaMemsetAsync(keys, 0xff, nb * 4 * sizeof(uint64_t), e->stream));
-        KK_CUDA_CHECK(cudaMemsetAsync(pos, 0xff, nb * 4 * sizeof(uint32_t), e->stream));
+        uint64_t *buckets = e->edge_set.as<uint64_t>(nb * kEdgeSetWords);
+        /* empty keys and (pos, weight) words at their maximum for atomicMin */
+        KK_CUDA_CHECK(cudaMemsetAsync(buckets, 0xff, nb * kEdgeSetWords * sizeof(uint64_t), e->stream));
         const uint32_t *order = vertex_order(e);
         const GraphView g = e->view();
         if (e->n_hub)
         {
             const unsigned grid = e->n_hub < 4u * e->sm_count ? e->n_hub : 4u * e->sm_count;
-            edge_set_block_kernel<<<grid, 1024, 0, e->stream>>>(g, keys, pos, nb, order, 0, e->n_hub);
+            edge_set_block_kernel<<<grid, 1024, 0, e->stream>>>(g, buckets, nb, order, 0, e->n_hub);
             count_launch(e);
             KK_CUDA_CHECK(cudaGetLastError());
         }
         if (e->n_nz > e->n_hub)
         {
             edge_set_warp_kernel<<<grid_for(e, (uint64_t)(e->n_nz - e->n_hub) * 32, 256), 256, 0, e->stream>>>(
-                g, keys, pos, nb, order, e->n_hub, e->n_nz);
+                g, buckets, nb, order, e->n_hub, e->n_nz);
             count_launch(e);
             KK_CUDA_CHECK(cudaGetLastError());
         }
         e->edge_set_nb = nb;
         e->edge_set_valid = true;
     }
-    return EdgeSetView{(const uint64_t *)e->edge_set.p, (const uint32_t *)e->edge_pos.p, e->edge_set_nb};
+    return EdgeSetView{(const uint64_t *)e->edge_set.p, e->edge_set_nb};
 }
 
 const uint8_t *metapath_vertex_masks(kk_engine *e)

@@ -22,7 +22,8 @@ LIB = os.path.join(LIBDIR, "libknightking_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["engine.cu", "graph.cu", "apps_first.cu", "apps_node2vec.cu", "alias_noalloc.cu", "batch.cu", "serve.cu"]
-EXAMPLES = ["tagwalk.cu"]  # knightking_gb300/examples/, each built into lib/libkk_example_<name>.so
+# knightking_gb300/examples/, each built into lib/libkk_example_<name>.so
+EXAMPLES = ["tagwalk.cu", "dynamic_walk.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",

@@ -223,7 +223,7 @@ typedef struct
 
 typedef struct
 {
-    uint32_t a; /* node2vec: previous vertex; metapath: scheme id; tagwalk: tag */
+    uint32_t a; /* node2vec: previous vertex; metapath: scheme id; tagwalk: tag; dynwalk: last vertex */
     uint32_t b; /* metapath: state; tagwalk: previous vertex */
 } ko_state;
 
@@ -338,6 +338,13 @@ static inline float ko_dyn1(const ko_ctx *c, const ko_state *s, uint32_t step, u
         uint8_t t = c->g->etype[e];
         return ((p->scheme_mask[s->a][s->b] >> t) & 1u) ? 1.0f : 0.0f;
     }
+    if (p->app == KO_APP_DYNWALK)
+    {
+        /* src/examples/dynamic_walk.cpp:72-88: 1 at step 0, 2 back to the last vertex, else 1 */
+        if (step == 0)
+            return 1.0f;
+        return c->g->nbr[e] == s->a ? 2.0f : 1.0f;
+    }
     /* tag walk */
     int T = p->tag_num;
     if (step == 0)
@@ -413,6 +420,9 @@ static inline void ko_update(const ko_ctx *c, ko_state *s, uint32_t v)
         s->a = (s->a + 1) % (uint32_t)c->prm->tag_num;
         s->b = v;
         break;
+    case KO_APP_DYNWALK:
+        s->a = v; /* dynamic_walk.cpp:62-65 */
+        break;
     default:
         break;
     }
@@ -464,6 +474,10 @@ static int ko_walk_one(const ko_ctx *c, uint32_t id, uint32_t cap, uint32_t *len
     else if (p->app == KO_APP_TAGWALK)
     {
         s.a = id % (uint32_t)p->tag_num;
+    }
+    else if (p->app == KO_APP_DYNWALK)
+    {
+        s.a = 0xffffffffu; /* dynamic_walk.cpp:57-61: no last vertex yet */
     }
     uint32_t step = 0;
     uint32_t len = 1;
@@ -654,6 +668,10 @@ int ko_walk_alias(const ko_graph *g, const ko_walk_params *p, uint32_t cap, uint
         c.has_lb = 1;
         c.outlier = c.n2v_overflow > 0.0f;
     }
+    else if (p->app == KO_APP_DYNWALK)
+    {
+        c.dynamic = 1; /* upper bound 2, no lower bound, no outlier (dynamic_walk.cpp:89-92) */
+    }
     else if (p->app == KO_APP_METAPATH)
     {
         c.dynamic = 1;
@@ -697,6 +715,11 @@ int ko_walk_alias(const ko_graph *g, const ko_walk_params *p, uint32_t cap, uint
             else if (p->app == KO_APP_METAPATH)
             {
                 c.ub[v] = 1.0f;
+                c.lb[v] = 0.0f;
+            }
+            else if (p->app == KO_APP_DYNWALK)
+            {
+                c.ub[v] = 2.0f;
                 c.lb[v] = 0.0f;
             }
             else if (p->outlier)

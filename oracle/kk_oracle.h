@@ -23,6 +23,7 @@ extern "C" {
 #define KO_APP_NODE2VEC 2
 #define KO_APP_METAPATH 3
 #define KO_APP_TAGWALK 4
+#define KO_APP_DYNWALK 5 /* the return-edge-doubling walk of src/examples/dynamic_walk.cpp:52-93 */
 
 #define KO_MAX_SCHEMES 16
 #define KO_MAX_SCHEME_LEN 16

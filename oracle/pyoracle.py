@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_BIN = os.path.join(HERE, "_ref", "kk_ref")
 REF_STOCK_BIN = os.path.join(HERE, "_ref", "kk_ref_stock")
 
-APP = {"deepwalk": 0, "ppr": 1, "node2vec": 2, "metapath": 3, "tagwalk": 4}
+APP = {"deepwalk": 0, "ppr": 1, "node2vec": 2, "metapath": 3, "tagwalk": 4, "dynwalk": 5}
 MAX_SCHEMES = 16
 MAX_SCHEME_LEN = 16
 

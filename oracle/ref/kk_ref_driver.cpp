@@ -14,7 +14,7 @@
  * that build is only used to time the reference.
  *
  * Usage: kk_ref <cmd> --graph FILE --v V --kind KIND [options] --out FILE
- *   cmd  = alias | deepwalk | ppr | node2vec | metapath | tagwalk
+ *   cmd  = alias | deepwalk | ppr | node2vec | metapath | tagwalk | dynwalk
  *   kind = none | f32 | meta | meta_f32 | tag | tag_f32
  * Output files are little-endian binary, read by tests/golden/make_golden.py:
  *   paths: "KKP1", u32 n, u32 len[n], u32 vertices[sum(len)] (walker id order)
@@ -323,6 +323,51 @@ void kk_tagwalk(WalkEngine<E, KKTagState> *graph, KKTagConf conf, std::vector<in
     }
 }
 
+/* ---- Dynamic walk: the configuration of src/examples/dynamic_walk.cpp:52-93 ----
+ * Weighted first-order walk whose dynamic component doubles the return edge:
+ * the walker remembers the vertex it came from (UINT_MAX before its first
+ * step), dynamic_comp is 1 at step 0, 2 for an edge back to that vertex and 1
+ * otherwise, with upper bound 2.  The lambdas are the example's, with its
+ * fixed walker count made a parameter. */
+struct KKDynWalkState
+{
+    vertex_id_t last_vertex;
+};
+
+template <typename E>
+void kk_dynwalk(WalkEngine<E, KKDynWalkState> *graph, walker_id_t walker_num, step_t walk_length,
+                WalkConfig *walk_conf)
+{
+    auto init_walker_func = [&](Walker<KKDynWalkState> &walker, vertex_id_t start_vertex) {
+        walker.data.last_vertex = UINT_MAX;
+    };
+    auto update_walker_func = [&](Walker<KKDynWalkState> &walker, vertex_id_t current_v, AdjUnit<E> *edge) {
+        walker.data.last_vertex = current_v;
+    };
+    WalkerConfig<E, KKDynWalkState> walker_conf(walker_num, init_walker_func, update_walker_func);
+    auto extension_comp = [&](Walker<KKDynWalkState> &walker, vertex_id_t current_v) {
+        return walker.step >= walk_length ? 0.0 : 1.0;
+    };
+    auto static_comp = [&](vertex_id_t v, AdjUnit<E> *edge) { return edge->data; };
+    auto dynamic_comp = [&](Walker<KKDynWalkState> &walker, vertex_id_t current_v, AdjUnit<E> *edge) {
+        if (walker.step == 0)
+        {
+            return 1.0;
+        }
+        else if (edge->neighbour == walker.data.last_vertex)
+        {
+            return 2.0;
+        }
+        else
+        {
+            return 1.0;
+        }
+    };
+    auto dynamic_comp_upperbound = [&](vertex_id_t v_id, AdjList<E> *adj_lists) { return 2.0; };
+    TransitionConfig<E, KKDynWalkState> tr_conf(extension_comp, static_comp, dynamic_comp, dynamic_comp_upperbound);
+    graph->random_walk(&walker_conf, &tr_conf, walk_conf);
+}
+
 /* ---- Hooked random_walk ------------------------------------------------
  * Explicit specialisations of WalkEngine::random_walk (include/walk.hpp:423-436)
  * for every (edge, state, transition config) the apps use.  Each one wraps
@@ -409,6 +454,7 @@ typedef TransitionConfig<KKTag, KKTagState> kk_tc_ut1;
 typedef TransitionConfig<KKWeightedTag, KKTagState> kk_tc_wt1;
 typedef SecondOrderTransitionConfig<KKTag, KKTagState, EmptyData, int> kk_tc_ut2;
 typedef SecondOrderTransitionConfig<KKWeightedTag, KKTagState, EmptyData, int> kk_tc_wt2;
+typedef TransitionConfig<real_t, KKDynWalkState> kk_tc_dyn;
 
 KK_HOOKED_RANDOM_WALK(EmptyData, EmptyData, kk_tc_ue)
 KK_HOOKED_RANDOM_WALK(real_t, EmptyData, kk_tc_we)
@@ -420,6 +466,7 @@ KK_HOOKED_RANDOM_WALK(KKTag, KKTagState, kk_tc_ut1)
 KK_HOOKED_RANDOM_WALK(KKWeightedTag, KKTagState, kk_tc_wt1)
 KK_HOOKED_RANDOM_WALK(KKTag, KKTagState, kk_tc_ut2)
 KK_HOOKED_RANDOM_WALK(KKWeightedTag, KKTagState, kk_tc_wt2)
+KK_HOOKED_RANDOM_WALK(real_t, KKDynWalkState, kk_tc_dyn)
 #else
 namespace kkhook
 {
@@ -443,7 +490,7 @@ struct Args
 
 static void usage()
 {
-    fprintf(stderr, "usage: kk_ref <alias|deepwalk|ppr|node2vec|metapath|tagwalk> --graph F --v V --kind K [opts] --out F\n");
+    fprintf(stderr, "usage: kk_ref <alias|deepwalk|ppr|node2vec|metapath|tagwalk|dynwalk> --graph F --v V --kind K [opts] --out F\n");
     exit(2);
 }
 
@@ -714,6 +761,14 @@ int main(int argc, char **argv)
         if (k == "meta_f32")
             return run_walk<WeightedMetaData, MetapathState>(a, [&](WalkEngine<WeightedMetaData, MetapathState> &g, walker_id_t n, WalkConfig *wc) {
                 metapath(&g, schemes, n, a.len, wc);
+            });
+        usage();
+    }
+    if (a.cmd == "dynwalk")
+    {
+        if (k == "f32")
+            return run_walk<real_t, KKDynWalkState>(a, [&](WalkEngine<real_t, KKDynWalkState> &g, walker_id_t n, WalkConfig *wc) {
+                kk_dynwalk<real_t>(&g, n, a.len, wc);
             });
         usage();
     }

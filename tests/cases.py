@@ -67,7 +67,7 @@ def walk_kwargs(case):
     p = case.params
     app = case.cmd
     kw = dict(seed=int(p["seed"]), walker_num=int(p["walkers"]), weighted=case.weighted)
-    if app in ("deepwalk", "node2vec", "metapath", "tagwalk"):
+    if app in ("deepwalk", "node2vec", "metapath", "tagwalk", "dynwalk"):
         kw["walk_length"] = int(p["len"])
     if app == "ppr":
         kw["terminate_prob"] = float(np.float32(p["term"]))

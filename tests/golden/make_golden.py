@@ -165,6 +165,12 @@ def small_cases(tmp):
         ("case_t200_outlier_o2_u", gtu, "tag", "tagwalk", dict(seed=57, order=2, variant="outlier", **base)),
         ("case_t200_outlier_o2_w", gtw, "tag_f32", "tagwalk", dict(seed=58, order=2, variant="outlier", **base)),
     ]
+    # the dynamic walk of src/examples/dynamic_walk.cpp:52-93 (return edge
+    # doubled): the example's own 34 walkers on karate, and a random graph
+    cases += [
+        ("case_dyn_karate", kar, "f32", "dynwalk", dict(seed=8, walkers=34, len=80)),
+        ("case_dyn_f200", gf, "f32", "dynwalk", dict(seed=35, walkers=400, len=25)),
+    ]
     # edge cases: isolated and degree-1 vertices, walkers not a multiple of V,
     # a single walker, zero length, immediate termination
     gs = G.random_undirected(400, 500, seed=61, weight="int5")

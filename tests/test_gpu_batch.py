@@ -1,5 +1,6 @@
 """Batched walks (kk_batch_walk): every job of a batch has exactly the paths it
-has when run alone through kk_walk, which the other tests pin to the reference.
+has when run alone through kk_walk and the oracle's paths (the C restatement
+pinned to the reference).
 
 Jobs in one batch differ in seed, walker range, walk length, node2vec (p, q)
 (in and out of the outlier regime) and metapath schemes."""
@@ -25,9 +26,10 @@ def _load(engine, seed, weighted, types=False):
                             types="uniform" if types else None)
     csr = G.csr_file_order(400, g["src"], g["dst"], w=g.get("w"), type=g.get("type"))
     engine.load_arrays(400, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
+    return csr
 
 
-def _check(engine, app, jobs):
+def _check(engine, app, jobs, oracle_lib=None, csr=None):
     """Both batch schedules (one walker per thread, the persistent pool) and
     uniform picks with and without the cursor adjacency."""
     batch = engine.batch_walk(app, jobs)
@@ -55,39 +57,47 @@ def _check(engine, app, jobs):
         np.testing.assert_array_equal(got.vertices, alone.vertices)
         assert got.walker_begin == alone.walker_begin
         assert got.total_steps == alone.total_steps
+        if oracle_lib is not None:
+            ocsr = oracle_lib.CSR(400, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
+            if app == "node2vec":
+                ocsr = ocsr.sorted_copy()
+            prm = oracle_lib.make_params(app, walker_num=n, **kw)
+            lens, verts, steps = oracle_lib.walk(ocsr, prm, cap=kw["walk_length"] + 1)
+            np.testing.assert_array_equal(got.path_length, lens)
+            np.testing.assert_array_equal(got.vertices, verts)
 
 
 @pytest.mark.parametrize("weighted", [True, False])
-def test_node2vec_batch_equals_single_jobs(engine, weighted):
-    _load(engine, 3, weighted)
+def test_node2vec_batch_equals_single_jobs(engine, oracle_lib, weighted):
+    csr = _load(engine, 3, weighted)
     jobs = [dict(walker_num=300, seed=1, walk_length=20, p=2.0, q=0.5, weighted=weighted),
             dict(walker_num=7, seed=2, walk_length=50, p=0.25, q=4.0, weighted=weighted, walker_begin=1000),
             dict(walker_num=0, seed=3, walk_length=10, p=1.0, q=1.0, weighted=weighted),
             dict(walker_num=513, seed=4, walk_length=5, p=0.5, q=2.0, weighted=weighted),
             dict(walker_num=64, seed=5, walk_length=33, p=3.0, q=0.3, weighted=weighted, walker_begin=77)]
-    _check(engine, "node2vec", jobs)
+    _check(engine, "node2vec", jobs, oracle_lib, csr)
 
 
 @pytest.mark.parametrize("weighted", [True, False])
-def test_metapath_batch_equals_single_jobs(engine, weighted):
-    _load(engine, 4, weighted, types=True)
+def test_metapath_batch_equals_single_jobs(engine, oracle_lib, weighted):
+    csr = _load(engine, 4, weighted, types=True)
     jobs = [dict(walker_num=400, seed=7, walk_length=30, weighted=weighted, schemes=[[1, 2, 4, 8], [2, 8, 2, 16]]),
             dict(walker_num=129, seed=8, walk_length=12, weighted=weighted, schemes=[[3, 12]],
                  scheme_round_robin=True),
             dict(walker_num=1000, seed=9, walk_length=60, weighted=weighted,
                  schemes=[[31], [1, 2], [4, 16, 8]], scheme_round_robin=True)]
-    _check(engine, "metapath", jobs)
+    _check(engine, "metapath", jobs, oracle_lib, csr)
 
 
 @pytest.mark.parametrize("weighted,layout", [(True, 2), (True, 0), (True, 1), (False, 2)])
-def test_deepwalk_batch_equals_single_jobs(engine, weighted, layout):
+def test_deepwalk_batch_equals_single_jobs(engine, oracle_lib, weighted, layout):
     """Every alias layout: 16 B neighbour buckets (the default), cursor and index buckets."""
-    _load(engine, 5, weighted)
+    csr = _load(engine, 5, weighted)
     jobs = [dict(walker_num=n, seed=s, walk_length=l, weighted=weighted, walker_begin=b)
             for n, s, l, b in ((1, 1, 80, 0), (1024, 2, 5, 10), (333, 3, 200, 5000), (2048, 4, 17, 0))]
     engine.set_option("alias_layout", layout)
     try:
-        _check(engine, "deepwalk", jobs)
+        _check(engine, "deepwalk", jobs, oracle_lib, csr)
     finally:
         engine.set_option("alias_layout", 2)
 

@@ -1,7 +1,8 @@
 """Serving (kk_serve_*): continuous batching of requests from several client
 threads on two slots.  Every request's paths equal those of the same request
 run alone through kk_walk (bit-identical), whatever else shared its batch and
-whichever slot ran it; the server reports its latency statistics."""
+whichever slot ran it, and equal the oracle's (the C restatement pinned to the
+reference); the server reports its latency statistics."""
 
 import threading
 
@@ -25,6 +26,16 @@ def _load(engine, seed, types=False):
     g = G.random_undirected(600, 8000, seed=seed, weight="unif", types="uniform" if types else None)
     csr = G.csr_file_order(600, g["src"], g["dst"], w=g.get("w"), type=g.get("type"))
     engine.load_arrays(600, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
+    return csr
+
+
+def _oracle(oracle_lib, csr, app, r):
+    ocsr = oracle_lib.CSR(600, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
+    if app == "node2vec":
+        ocsr = ocsr.sorted_copy()
+    kw = dict(r)
+    prm = oracle_lib.make_params(app, weighted=True, **kw)
+    return oracle_lib.walk(ocsr, prm, cap=r["walk_length"] + 1)
 
 
 def _requests(app, n, seed):
@@ -63,9 +74,9 @@ def _serve_all(engine, app, reqs, clients=4, **server_kw):
 
 @pytest.mark.parametrize("graphs", [True, False])
 @pytest.mark.parametrize("app", ["node2vec", "deepwalk", "metapath"])
-def test_served_requests_equal_alone(engine, app, graphs):
+def test_served_requests_equal_alone(engine, oracle_lib, app, graphs):
     """Slots replaying captured CUDA graphs, and slots launching on their streams."""
-    _load(engine, 11, types=app == "metapath")
+    csr = _load(engine, 11, types=app == "metapath")
     reqs = _requests(app, 60, seed=5)
     results, stats = _serve_all(engine, app, reqs, slots=2, max_jobs=16, slot_bytes=8 << 20, graphs=graphs)
     assert stats["completed"] == len(reqs) and stats["failed"] == 0
@@ -79,6 +90,10 @@ def test_served_requests_equal_alone(engine, app, graphs):
         np.testing.assert_array_equal(res.paths.vertices, alone.vertices)
         assert res.paths.total_steps == alone.total_steps
         assert res.latency_ms >= res.queue_ms >= 0
+        if graphs:
+            lens, verts, steps = _oracle(oracle_lib, csr, app, r)
+            np.testing.assert_array_equal(res.paths.path_length, lens)
+            np.testing.assert_array_equal(res.paths.vertices, verts)
 
 
 def test_server_refuses_bad_requests(engine):

@@ -4,8 +4,8 @@ out as soon as its last walker finishes.  Metapath: one launch, then packed and
 copied out.  Chunked (into_stream 0,
 graphs with dead ends): chunk c + 1 walks while chunk c's paths are packed and
 copied out.  Whatever the mode, the lengths, offsets and vertices in the
-caller's buffers are the paths kk_walk returns (which the parity tests pin to
-the reference)."""
+caller's buffers are the paths kk_walk returns, and both equal the oracle's
+(the C restatement pinned to the reference), walker for walker."""
 
 import numpy as np
 import pytest
@@ -30,6 +30,18 @@ def _load(engine, seed, weighted, types=False):
                             types="uniform" if types else None)
     csr = G.csr_file_order(400, g["src"], g["dst"], w=g.get("w"), type=g.get("type"))
     engine.load_arrays(400, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
+    return csr
+
+
+def _oracle(oracle_lib, csr, app, n, weighted, kw):
+    """The oracle's walk of the same walkers (lengths, packed vertices, steps)."""
+    V = len(csr["off"]) - 1
+    ocsr = oracle_lib.CSR(V, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
+    if app == "node2vec":
+        ocsr = ocsr.sorted_copy()
+    kw = {k: v for k, v in kw.items() if k != "rate"}
+    prm = oracle_lib.make_params(app, walker_num=n, weighted=weighted, **kw)
+    return oracle_lib.walk(ocsr, prm, cap=kw.get("walk_length", 400) + 1)
 
 
 def _into(engine, app, n, cap, **kw):
@@ -51,10 +63,14 @@ CASES = [
 
 @pytest.mark.parametrize("chunks,cursor,stream", [(1, 0, 1), (4, 1, 1), (3, 0, 0), (4, 1, 0)])
 @pytest.mark.parametrize("case", range(len(CASES)))
-def test_walk_into_equals_walk(engine, case, chunks, cursor, stream):
+def test_walk_into_equals_walk(engine, oracle_lib, case, chunks, cursor, stream):
     app, weighted, types, kw = CASES[case]
-    _load(engine, 20 + case, weighted, types)
+    csr = _load(engine, 20 + case, weighted, types)
     ref = engine.walk(app, N, weighted=weighted, **kw)
+    if chunks == 1:
+        lens, verts, steps = _oracle(oracle_lib, csr, app, N, weighted, kw)
+        np.testing.assert_array_equal(ref.path_length, lens)
+        np.testing.assert_array_equal(ref.vertices, verts)
     engine.set_option("into_chunks", chunks)
     engine.set_option("cursor_adjacency", cursor)
     engine.set_option("into_stream", stream)
@@ -74,13 +90,16 @@ def test_walk_into_equals_walk(engine, case, chunks, cursor, stream):
 
 
 @pytest.mark.parametrize("stream", [1, 0])
-def test_walk_into_epochs_and_small_capacity(engine, stream):
+def test_walk_into_epochs_and_small_capacity(engine, oracle_lib, stream):
     """Epochs (rate 0.5), streamed or in chunks, and a buffer one vertex short
     fails cleanly (before any copy in the streamed mode)."""
     import knightking_gb300 as kk
-    _load(engine, 31, True)
+    csr = _load(engine, 31, True)
     kw = dict(walk_length=9, seed=11, rate=0.5)
     ref = engine.walk("deepwalk", N, weighted=True, **kw)
+    lens, verts, _ = _oracle(oracle_lib, csr, "deepwalk", N, True, kw)
+    np.testing.assert_array_equal(ref.path_length, lens)
+    np.testing.assert_array_equal(ref.vertices, verts)
     total = len(ref.vertices)
     engine.set_option("into_stream", stream)
     try:
@@ -98,7 +117,7 @@ def test_walk_into_epochs_and_small_capacity(engine, stream):
 
 
 @pytest.mark.parametrize("layout", [0, 2])
-def test_walk_into_streamed_large_walk(engine, layout):
+def test_walk_into_streamed_large_walk(engine, oracle_lib, layout):
     """A walk of 2^21 walkers over a graph with isolated vertices: 256
     segments of 8192 walkers, some holding only one-vertex paths; cursor and
     16 B neighbour buckets."""
@@ -108,6 +127,10 @@ def test_walk_into_streamed_large_walk(engine, layout):
     n = 1 << 21
     kw = dict(walk_length=5, seed=13)
     ref = engine.walk("deepwalk", n, weighted=True, **kw)
+    if layout == 0:
+        lens, verts, _ = _oracle(oracle_lib, csr, "deepwalk", n, True, kw)
+        np.testing.assert_array_equal(ref.path_length, lens)
+        np.testing.assert_array_equal(ref.vertices, verts)
     engine.set_option("alias_layout", layout)
     try:
         steps, h_len, h_off, h_vert = _into(engine, "deepwalk", n, len(ref.vertices), weighted=True, **kw)

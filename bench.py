@@ -538,7 +538,8 @@ def run_serve_bench(args, wl, world, rank, local):
     # batch kernel on the whole stream
     engine.set_option("alias_cache", 1)
     from knightking_gb300 import tuning
-    best, tune_table = tuning.autotune(engine, lambda: batched(reqs), tuning.space_for(app, bool(wl["weights"])),
+    best, tune_table = tuning.autotune(engine, lambda: batched(reqs),
+                                      tuning.space_for(app, bool(wl["weights"]), batch=True),
                                       repeats=1)
     for _ in range(args.warmup):
         batched(reqs)

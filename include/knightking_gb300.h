@@ -131,7 +131,10 @@ kk_status kk_engine_set_stream(kk_engine *e, void *stream);
  *                        up to this many walker chunks (>= 2^18 walkers each), copying each chunk's
  *                        paths out while the next chunk walks (default 6; 1 = whole)
  *   "cursor_adjacency"   1 uniform picks read a per-graph adjacency copy holding each neighbour's
- *                        position (16 B/edge, built on first use): one dependent read per step */
+ *                        position (16 B/edge, built on first use): one dependent read per step
+ *   "regroup_interval"   0 (default) off; k > 0: single-job walks of the one-walker-per-thread schedule
+ *                        that do not park run in phases of k steps, and each phase takes its walkers
+ *                        sorted by the vertex they stand on (0..4096) */
 kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value);
 /* Message of the last failed call on this engine ("" if none). */
 const char *kk_last_error(const kk_engine *e);

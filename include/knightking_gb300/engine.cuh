@@ -360,6 +360,12 @@ struct kk_engine
      * metapath S22 walk 19.3 -> 13.6 ms) */
     int walk_park = 20;
     kk::DevBuf park[2], park_count;
+    /* regroup_interval (option): 0 off; k > 0 runs the walks of walk_static
+     * scheduling that do not park in phases of k steps, each phase's walkers
+     * sorted by the vertex they stand on (walk_regroup_kernel): records,
+     * sort keys in and out, sort values, the sorted order, the counts */
+    int regroup = 0;
+    kk::DevBuf regroup_rec[2], regroup_key[2], regroup_val, regroup_perm, regroup_count;
     /* walk_stats (option): count trials, queries and binary-search probes of
      * the walks (kk_last_walk_stats) */
     int walk_stats = 0;
@@ -464,6 +470,11 @@ void exclusive_scan_u64(kk_engine *e, const uint64_t *in, uint64_t *out, uint64_
 /* The same on stream st with temporary storage tmp. */
 void exclusive_scan_u64(kk_engine *e, const uint64_t *in, uint64_t *out, uint64_t n, cudaStream_t st,
                         kk::DevBuf &tmp);
+
+/* Sorts n (key, value) pairs by the low `bits` bits of the key (stable), on
+ * the engine's stream: the regrouped walk's records by vertex. */
+void sort_pairs_u32(kk_engine *e, const uint32_t *keys_in, uint32_t *keys_out, const uint32_t *vals_in,
+                    uint32_t *vals_out, uint32_t n, int bits);
 
 /* Vertices sorted by degree, descending, with the alias tiers (cached per graph). */
 const uint32_t *vertex_order(kk_engine *e);
@@ -671,6 +682,47 @@ void build_alias(kk_engine *e, const TC &tc)
     }
 }
 
+/* A regrouped walk (option regroup_interval = k): phases of k steps, each
+ * phase's walkers in the order of the vertices they stand on
+ * (walk_regroup_kernel).  After each phase the host reads how many walkers
+ * are still walking (through the mapped status words, no copy engine) and
+ * sorts exactly those records by vertex.  Every phase moves each walker it
+ * holds by at least k steps or ends it, and a walk ends within its path
+ * capacity or its trial limit, so the phases are bounded. */
+template <typename S, typename WC, typename TC, typename Bucket>
+void walk_regrouped(kk_engine *e, const GraphView &g, const WC &wc, const TC &tc, const Bucket *alias,
+                    const float *ra, const WalkLaunch &L)
+{
+    typedef ParkedWalker<S> PW;
+    const uint32_t n = L.walker_num;
+    PW *rec[2] = {e->regroup_rec[0].as<PW>(n), e->regroup_rec[1].as<PW>(n)};
+    uint32_t *key = e->regroup_key[0].as<uint32_t>(n), *key_sorted = e->regroup_key[1].as<uint32_t>(n);
+    uint32_t *val = e->regroup_val.as<uint32_t>(n), *perm = e->regroup_perm.as<uint32_t>(n);
+    uint32_t *cnt = e->regroup_count.as<uint32_t>(2);
+    int bits = 1;
+    while (bits < 32 && ((uint64_t)1 << bits) < (uint64_t)g.V)
+        bits++;
+    const unsigned bs = (unsigned)e->walk_block;
+    const uint32_t k = (uint32_t)e->regroup;
+    const PW *in = nullptr;
+    uint32_t left = n;
+    for (int ph = 0; left > 0; ph++)
+    {
+        const int o = ph & 1;
+        KK_CUDA_CHECK(cudaMemsetAsync(cnt + o, 0, sizeof(uint32_t), e->stream));
+        walk_regroup_kernel<S, WC, TC, Bucket><<<grid_for(e, left, bs), bs, 0, e->stream>>>(
+            g, wc, tc, alias, ra, L, in, perm, cnt + (o ^ 1), rec[o], key, val, cnt + o, k);
+        count_launch(e);
+        KK_CUDA_CHECK(cudaGetLastError());
+        words_to_host(e, cnt + o, 44, 1);
+        KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+        left = ((volatile uint32_t *)e->h_status)[44];
+        if (left > 0)
+            sort_pairs_u32(e, key, key_sorted, val, perm, left, bits);
+        in = rec[o];
+    }
+}
+
 /* One walk over walkers [rs.walker_begin, + rs.walker_num): alias tables,
  * regular area, path capacity, the walk kernel.  Events: ev0 before the alias
  * build, ev1 before the walk, ev2 after. */
@@ -781,7 +833,7 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
     KK_CUDA_CHECK(cudaEventRecord(e->ev[1], e->stream));
     if constexpr (TC::order == 1 && !TC::has_dynamic)
     {
-        if (e->walk_schedule == 0 && e->walk_multi > 1)
+        if (e->walk_schedule == 0 && e->walk_multi > 1 && e->regroup == 0)
         {
             /* W walkers per thread, gathers of all W in flight together */
             const unsigned bs = (unsigned)e->walk_block;
@@ -795,6 +847,11 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
             count_launch(e);
             goto launched;
         }
+    }
+    if (e->walk_schedule == 0 && e->regroup > 0 && !(parks<TC>() && e->walk_park > 0) && n > 0)
+    {
+        walk_regrouped<S, WC, TC, Bucket>(e, g, wc, tc, alias, ra, L);
+        goto launched;
     }
     if (e->walk_schedule == 0)
     {

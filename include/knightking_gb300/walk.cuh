@@ -1996,6 +1996,87 @@ __global__ void __launch_bounds__(256, 4) walk_resume_kernel(GraphView g, WC wc,
     counts.flush(L.stats);
 }
 
+/* Regrouping walkers by the vertex they stand on (option regroup_interval =
+ * k > 0).  The walk runs in phases of k steps.  A phase takes its walkers in
+ * the order of the previous phase's records sorted by vertex (in[perm[t]],
+ * *in_count of them; the first phase starts walkers 0..n-1 in id order), runs
+ * each to its first step boundary at or past k more steps, and records every
+ * walker still walking in out (a ParkedWalker<S>: node2vec's previous vertex
+ * is in its state) with its vertex as the next phase's sort key and its
+ * record index as the sort value.  Lanes of a warp then start on the same or
+ * nearby vertices, so their offset and first bucket reads share sectors.  The
+ * stream is keyed by (walker, step), so the paths are those of one walk. */
+template <typename S, typename WC, typename TC, typename Bucket>
+__global__ void __launch_bounds__(256, 4) walk_regroup_kernel(GraphView g, WC wc, TC tc, const Bucket *alias,
+                                                           const float *ra, WalkLaunch L,
+                                                           const ParkedWalker<S> *in, const uint32_t *perm,
+                                                           const uint32_t *in_count, ParkedWalker<S> *out,
+                                                           uint32_t *out_keys, uint32_t *out_vals,
+                                                           uint32_t *out_count, uint32_t k)
+{
+    unsigned long long my_steps = 0;
+    WalkCounts counts;
+    const uint32_t n = in != nullptr ? *in_count : L.walker_num;
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x)
+    {
+        const uint32_t t = b + threadIdx.x;
+        bool park = false, ended = false;
+        uint32_t i = 0;
+        Sampler rng;
+        WalkerRun<S> run;
+        if (t < n)
+        {
+            rng.init(L.seed);
+            if (in != nullptr)
+            {
+                const ParkedWalker<S> pw = in[perm[t]];
+                i = pw.i;
+                resume_run<S>(L, i, pw, run);
+            }
+            else
+            {
+                i = t;
+                walk_begin<S>(g, wc, L, i, run, rng);
+            }
+            const step_t end = run.w.step + k;
+            for (;;)
+            {
+                if (!run.in_step && run.w.step >= end)
+                {
+                    park = true;
+                    break;
+                }
+                if (!walk_trial<S>(g, wc, tc, alias, ra, L, run, rng))
+                {
+                    ended = true;
+                    break;
+                }
+            }
+        }
+        if (ended)
+            walk_finish<S>(L, i, run, my_steps, counts);
+        const unsigned pm = __ballot_sync(kFullMask, park);
+        if (pm != 0)
+        {
+            uint32_t base = 0;
+            if (lane == (unsigned)(__ffs(pm) - 1))
+                base = atomicAdd(out_count, (uint32_t)__popc(pm));
+            base = __shfl_sync(kFullMask, base, __ffs(pm) - 1);
+            if (park)
+            {
+                const uint32_t slot = base + __popc(pm & ((1u << lane) - 1u));
+                out[slot] = ParkedWalker<S>{i, run.v, run.w.step, run.len, run.w.data};
+                out_keys[slot] = run.v;
+                out_vals[slot] = slot;
+                counts.add(run);
+            }
+        }
+    }
+    flush_steps(L.total_steps, my_steps);
+    counts.flush(L.stats);
+}
+
 /* Several walkers per thread for walks whose every trial is accepted (first
  * order without a dynamic component: DeepWalk, PPR).  A step is two dependent
  * gathers (the adjacency position, when the bucket did not carry it, then the

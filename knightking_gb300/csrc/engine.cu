@@ -731,6 +731,14 @@ void kk_engine_destroy(kk_engine *e)
     e->park[0].release();
     e->park[1].release();
     e->park_count.release();
+    for (int i = 0; i < 2; i++)
+    {
+        e->regroup_rec[i].release();
+        e->regroup_key[i].release();
+    }
+    e->regroup_val.release();
+    e->regroup_perm.release();
+    e->regroup_count.release();
     if (e->host_pool)
         e->host_pool->release();
     e->vcur.release();
@@ -794,6 +802,8 @@ kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value)
             e->alias_streams = (int)value;
         else if (n == "walk_multi" && (value == 1 || value == 2 || value == 4))
             e->walk_multi = (int)value;
+        else if (n == "regroup_interval" && value >= 0 && value <= 4096)
+            e->regroup = (int)value;
         else
             fail(KK_ERR_INVALID_CONFIG, "unknown option or value out of range: " + n);
     });

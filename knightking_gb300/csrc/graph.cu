@@ -44,6 +44,16 @@ void exclusive_scan_u64(kk_engine *e, const uint64_t *in, uint64_t *out, uint64_
     exclusive_scan_u64(e, in, out, n, e->stream, e->cub_tmp);
 }
 
+void sort_pairs_u32(kk_engine *e, const uint32_t *keys_in, uint32_t *keys_out, const uint32_t *vals_in,
+                    uint32_t *vals_out, uint32_t n, int bits)
+{
+    size_t bytes = 0;
+    KK_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(nullptr, bytes, keys_in, keys_out, vals_in, vals_out, (int64_t)n, 0,
+                                                  bits, e->stream));
+    KK_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(e->cub_tmp.ensure(bytes), bytes, keys_in, keys_out, vals_in,
+                                                  vals_out, (int64_t)n, 0, bits, e->stream));
+}
+
 namespace
 {
 

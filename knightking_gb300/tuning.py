@@ -3,8 +3,9 @@
 The options (kk_engine_set_option) never change a path, only how fast it is
 produced: alias-table layout, the alias build's stream split, node2vec
 adjacency test, walk block size, the parking threshold of rejection walks,
-walkers per thread, the context's L2 fetch-granularity hint, the walk schedule
-and the cursor adjacency of uniform walks.  The tuner runs a
+walkers per thread, the context's L2 fetch-granularity hint, the walk schedule,
+the cursor adjacency of uniform walks and the regroup interval (walkers sorted
+by the vertex they stand on every k steps).  The tuner runs a
 caller-supplied step (one walk call on the real workload) under candidate
 settings and keeps, option by option, the value with the shortest alias-build
 plus walk time as the engine's CUDA events measure it (greedy coordinate
@@ -21,14 +22,18 @@ DEFAULT_SPACE = (
     ("l2_fetch_bytes", (0, 64)),
     ("walk_schedule", (0, 1)),
     ("cursor_adjacency", (0, 1)),
+    ("regroup_interval", (0, 16, 4)),
 )
 
 
-def space_for(app, weighted):
+def space_for(app, weighted, batch=False):
     """The options that matter for a built-in app: the alias layout only with
-    alias tables, the adjacency test only for node2vec."""
+    alias tables, the adjacency test only for node2vec; batched walks
+    (walk_batch_kernel) neither regroup nor run several walkers per thread."""
     out = []
     for name, vals in DEFAULT_SPACE:
+        if name in ("regroup_interval", "walk_multi") and batch:
+            continue
         if name in ("alias_layout", "alias_streams") and not weighted:
             continue
         if name == "node2vec_adjacency" and app != "node2vec":

@@ -42,3 +42,13 @@ def test_space_for_apps():
     assert "walk_park" not in names(tuning.space_for("deepwalk", True))
     assert "alias_streams" in names(tuning.space_for("deepwalk", True))
     assert "alias_streams" not in names(tuning.space_for("ppr", False))
+
+
+def test_space_for_batches_leaves_out_single_walk_options():
+    names = lambda sp: [n for n, _ in sp]
+    assert "regroup_interval" in names(tuning.space_for("deepwalk", True))
+    assert "regroup_interval" in names(tuning.space_for("node2vec", True))
+    assert "regroup_interval" not in names(tuning.space_for("node2vec", True, batch=True))
+    assert "walk_multi" not in names(tuning.space_for("deepwalk", True, batch=True))
+    # the first value of every option is the engine's default (off for regrouping)
+    assert dict(tuning.space_for("ppr", False))["regroup_interval"][0] == 0

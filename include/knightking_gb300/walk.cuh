@@ -658,12 +658,295 @@ __device__ __forceinline__ void block_rank2(bool a, bool b, uint32_t &ra, uint32
     tb = sb[32];
 }
 
-/* Pairing loop of a block: block-wide batches while both queues are long,
- * warp 0 alone for short stretches; then the q leftovers (:631-638). */
-template <typename Bucket>
-__device__ __forceinline__ void block_pairing(uint2 *P, uint2 *Q, uint32_t pt, uint32_t qt, float ave, Bucket *ob,
-                                              const uint32_t *nb, const uint64_t *vcur, const uint8_t *ty,
-                                              uint32_t *sa, uint32_t *sb, uint32_t *s_state)
+/* ---- a row's sum, exact and in parallel ------------------------------------
+ *
+ * The alias build needs each row's sum as the reference adds it: one float
+ * rounding per term, in edge order (include/walk.hpp:579-584).  As a serial
+ * FADD chain it costs one thread several cycles per edge (a 163,585-edge hub
+ * row: ~0.4 ms while the rest of its block waits).  For non-negative finite
+ * terms the partial sums never decrease, so they pass through each binade
+ * [2^e, 2^(e+1)) once.  Inside one binade every partial sum is a multiple of
+ * u = 2^(e-23), and s + x rounds to s + m*u or s + (m+1)*u with m = floor(x/u):
+ * to the nearest, a tie to the even significand, which depends only on the
+ * parity of S = s/u.  So each term acts on the significand as a map
+ * S -> S + a[S & 1], and such maps compose:
+ *     (f then g)[p] = f[p] + g[(p + f[p]) & 1].
+ * A block scan of the maps over a window of terms gives every partial sum of
+ * the window at once.  The first term whose partial sum would reach 2^(e+1)
+ * is added with a real FADD to the exact partial sum before it, and the next
+ * window starts after it in the new binade.  Partial sums below 2^-103 and
+ * rows with a negative, negative-zero or non-finite term take the serial
+ * chain.  The result is the serial chain's, bit for bit. */
+struct SumMap
+{
+    uint32_t a0, a1; /* increments of S, in units of u, for S even / odd */
+};
+constexpr uint32_t kSumSat = 1u << 26; /* saturation: past any binade */
+
+__device__ __forceinline__ SumMap summap_then(SumMap f, SumMap g)
+{
+    const uint32_t c0 = f.a0 + ((f.a0 & 1u) ? g.a1 : g.a0);
+    const uint32_t c1 = f.a1 + ((f.a1 & 1u) ? g.a0 : g.a1);
+    return SumMap{min(c0, kSumSat), min(c1, kSumSat)};
+}
+
+/* The map of adding term x, scale = 1/u (a power of two). */
+__device__ __forceinline__ SumMap summap_term(float x, float scale)
+{
+    const float xs = fmul(x, scale); /* exact: a power-of-two scaling */
+    if (!(xs < 33554432.0f))         /* 2^25 (and inf): past the binade */
+        return SumMap{kSumSat, kSumSat};
+    const uint32_t m = __float2uint_rz(xs);
+    const float fr = fsub(xs, u2f(m)); /* exact */
+    if (fr > 0.5f)
+        return SumMap{m + 1u, m + 1u};
+    if (fr < 0.5f)
+        return SumMap{m, m};
+    return SumMap{m + (m & 1u), m + ((m + 1u) & 1u)};
+}
+
+/* Inclusive and exclusive scans of the block's maps in thread order.
+ * s_maps: 33 SumMaps of shared memory. */
+__device__ __forceinline__ void block_scan_maps(SumMap mine, SumMap &inc, SumMap &exc, SumMap *s_maps)
+{
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    inc = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const SumMap prev{__shfl_up_sync(kFullMask, inc.a0, o), __shfl_up_sync(kFullMask, inc.a1, o)};
+        if (lane >= (uint32_t)o)
+            inc = summap_then(prev, inc);
+    }
+    SumMap wexc{__shfl_up_sync(kFullMask, inc.a0, 1), __shfl_up_sync(kFullMask, inc.a1, 1)};
+    if (lane == 0)
+        wexc = SumMap{0u, 0u};
+    if (lane == 31)
+        s_maps[wid] = inc;
+    __syncthreads();
+    if (wid == 0)
+    {
+        SumMap t = lane < nw ? s_maps[lane] : SumMap{0u, 0u};
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const SumMap prev{__shfl_up_sync(kFullMask, t.a0, o), __shfl_up_sync(kFullMask, t.a1, o)};
+            if (lane >= (uint32_t)o)
+                t = summap_then(prev, t);
+        }
+        SumMap te{__shfl_up_sync(kFullMask, t.a0, 1), __shfl_up_sync(kFullMask, t.a1, 1)};
+        if (lane == 0)
+            te = SumMap{0u, 0u};
+        if (lane < nw)
+            s_maps[lane] = te; /* the maps of the warps before `lane` */
+    }
+    __syncthreads();
+    const SumMap before = s_maps[wid];
+    inc = summap_then(before, inc);
+    exc = summap_then(before, wexc);
+    __syncthreads(); /* s_maps is free again */
+}
+
+/* The row's sum (every thread of the block gets it): terms load(0..deg), K
+ * per thread per window after a serial head of 2 * blockDim.x terms.
+ * s_maps: 33 SumMaps, s_f: 1 float, s_u: 1 word of shared memory. */
+template <uint32_t K, typename Load>
+__device__ float block_exact_sum(Load load, uint32_t deg, SumMap *s_maps, float *s_f, uint32_t *s_u)
+{
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    /* the first terms on one thread: the partial sums double every few
+     * terms there, which would end a window every few terms */
+    if (tid == 0)
+    {
+        float s = 0.0f;
+        uint32_t i = 0;
+        const uint32_t head = deg < 2u * nt ? deg : 2u * nt;
+        for (; i + 4 <= head; i += 4)
+            s = fadd(fadd(fadd(fadd(s, load(i)), load(i + 1)), load(i + 2)), load(i + 3));
+        for (; i < head; i++)
+            s = fadd(s, load(i));
+        *s_f = s;
+        *s_u = i;
+    }
+    __syncthreads();
+    float s = *s_f;
+    uint32_t pos = *s_u;
+    __syncthreads();
+    while (pos < deg)
+    {
+        const uint32_t bits = __float_as_uint(s), ex = (bits >> 23) & 0xFFu;
+        const uint32_t base = pos + tid * K;
+        float xk[K];
+        /* sums below 2^-103, inf, NaN and negative sums take the serial chain */
+        bool odd = !(ex >= 24u && ex < 255u) || bits >= 0x80000000u;
+        SumMap m{0u, 0u};
+        const float scale = __uint_as_float((277u - (ex < 24u ? 24u : ex > 254u ? 254u : ex)) << 23);
+#pragma unroll
+        for (uint32_t j = 0; j < K; j++)
+        {
+            const float x = base + j < deg ? load(base + j) : 0.0f;
+            xk[j] = x;
+            odd = odd || __float_as_uint(x) >= 0x7F800000u; /* negative (incl. -0), inf, NaN */
+            m = summap_then(m, summap_term(x, scale));
+        }
+        if (__syncthreads_or(odd))
+        {
+            /* the serial chain for the rest of the row */
+            if (tid == 0)
+            {
+                for (uint32_t i = pos; i < deg; i++)
+                    s = fadd(s, load(i));
+                *s_f = s;
+            }
+            __syncthreads();
+            s = *s_f;
+            __syncthreads();
+            break;
+        }
+        const uint32_t S = (bits & 0x7FFFFFu) | 0x800000u, p0 = S & 1u;
+        const float u = __uint_as_float((ex - 23u) << 23);
+        SumMap inc, exc;
+        block_scan_maps(m, inc, exc, s_maps);
+        const uint32_t end = S + (p0 ? inc.a1 : inc.a0);
+        /* partial sums never decrease, so the threads whose terms stay in
+         * the binade come first */
+        const uint32_t stay = (uint32_t)__syncthreads_count(end < (1u << 24));
+        if (stay == nt)
+        {
+            if (tid == nt - 1)
+                *s_f = fmul(u2f(end), u);
+            __syncthreads();
+            s = *s_f;
+            pos += nt * K;
+            __syncthreads();
+            continue;
+        }
+        if (tid == stay)
+        {
+            uint32_t Sj = S + (p0 ? exc.a1 : exc.a0);
+            bool found = false;
+#pragma unroll
+            for (uint32_t j = 0; j < K; j++)
+            {
+                const SumMap t = summap_term(xk[j], scale);
+                const uint32_t a = (Sj & 1u) ? t.a1 : t.a0;
+                if (!found && Sj + a >= (1u << 24))
+                {
+                    *s_f = fadd(fmul(u2f(Sj), u), xk[j]);
+                    *s_u = base + j + 1;
+                    found = true;
+                }
+                Sj += a;
+            }
+            if (!found)
+            {
+                /* unreachable by the argument above; should it ever be
+                 * reached, the serial chain finishes the row exactly */
+                float r = fmul(u2f(S + (p0 ? exc.a1 : exc.a0)), u);
+                for (uint32_t i = base; i < deg; i++)
+                    r = fadd(r, load(i));
+                *s_f = r;
+                *s_u = deg;
+            }
+        }
+        __syncthreads();
+        s = *s_f;
+        pos = *s_u;
+        __syncthreads();
+    }
+    return s;
+}
+
+/* Block-wide exclusive scan of two counts packed as a | b << 16 (each total
+ * below 2^16): exclusive prefix and total.  s_w: 33 words of shared memory. */
+__device__ __forceinline__ uint32_t block_scan_packed(uint32_t x, uint32_t &total, uint32_t *s_w)
+{
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t inc = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const uint32_t y = __shfl_up_sync(kFullMask, inc, o);
+        if (lane >= (uint32_t)o)
+            inc += y;
+    }
+    if (lane == 31)
+        s_w[wid] = inc;
+    __syncthreads();
+    if (wid == 0)
+    {
+        const uint32_t t = lane < nw ? s_w[lane] : 0u;
+        uint32_t ti = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t y = __shfl_up_sync(kFullMask, ti, o);
+            if (lane >= (uint32_t)o)
+                ti += y;
+        }
+        if (lane < nw)
+            s_w[lane] = ti - t;
+        if (lane == 31)
+            s_w[32] = ti;
+    }
+    __syncthreads();
+    const uint32_t ex = s_w[wid] + inc - x;
+    total = s_w[32];
+    __syncthreads();
+    return ex;
+}
+
+/* Stable block-wide split, K consecutive terms per thread per pass: terms
+ * below ave to the p queue, the rest to the q queue, in edge order
+ * (:593-602). */
+template <uint32_t K, typename Load>
+__device__ __forceinline__ void block_split_wide(Load load, uint32_t deg, float ave, uint2 *P, uint2 *Q,
+                                                 uint32_t &pt, uint32_t &qt, uint32_t *s_w)
+{
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    pt = 0;
+    qt = 0;
+    for (uint32_t base = 0; base < deg; base += nt * K)
+    {
+        const uint32_t i0 = base + tid * K;
+        float xk[K];
+        uint32_t cs = 0, cb = 0;
+#pragma unroll
+        for (uint32_t j = 0; j < K; j++)
+        {
+            const bool valid = i0 + j < deg;
+            xk[j] = valid ? load(i0 + j) : 0.0f;
+            cs += valid && xk[j] < ave;
+            cb += valid && !(xk[j] < ave);
+        }
+        uint32_t tot;
+        const uint32_t ex = block_scan_packed(cs | (cb << 16), tot, s_w);
+        uint32_t ps = pt + (ex & 0xFFFFu), qs = qt + (ex >> 16);
+#pragma unroll
+        for (uint32_t j = 0; j < K; j++)
+        {
+            if (i0 + j < deg)
+            {
+                const uint2 ent = make_uint2(i0 + j, __float_as_uint(xk[j]));
+                if (xk[j] < ave)
+                    P[ps++] = ent;
+                else
+                    Q[qs++] = ent;
+            }
+        }
+        pt += tot & 0xFFFFu;
+        qt += tot >> 16;
+    }
+    __syncthreads();
+}
+
+/* Pairing loop of a block (:603-638) with K iterations per thread per batch:
+ * batches of up to nt * K iterations while both queues are long, warp 0
+ * alone for short stretches; then the q leftovers. */
+template <uint32_t K, typename Bucket>
+__device__ __forceinline__ void block_pairing_wide(uint2 *P, uint2 *Q, uint32_t pt, uint32_t qt, float ave,
+                                                   Bucket *ob, const uint32_t *nb, const uint64_t *vcur,
+                                                   const uint8_t *ty, uint32_t *s_w, uint32_t *s_state)
 {
     const uint32_t tid = threadIdx.x, nt = blockDim.x;
     uint32_t ph = 0, qh = 0;
@@ -677,7 +960,7 @@ __device__ __forceinline__ void block_pairing(uint2 *P, uint2 *Q, uint32_t pt, u
             ph = pt;
             break;
         }
-        const uint32_t b = min(min(lp, lq), nt);
+        const uint32_t b = min(min(lp, lq), nt * K);
         if (b <= 64)
         {
             if (tid < 32)
@@ -699,62 +982,56 @@ __device__ __forceinline__ void block_pairing(uint2 *P, uint2 *Q, uint32_t pt, u
             __syncthreads();
             continue;
         }
-        const bool act = tid < b;
-        bool conv = false;
-        uint2 ne = make_uint2(0, 0);
-        if (act)
+        /* iterations tid*K .. tid*K + K - 1 of the batch */
+        const uint32_t i0 = tid * K;
+        uint2 ne[K];
+        uint32_t convm = 0, nc = 0, ns = 0;
+#pragma unroll
+        for (uint32_t j = 0; j < K; j++)
         {
-            const uint2 pe = P[ph + tid], qe = Q[qh + tid];
-            const float pv = __uint_as_float(pe.y), qv = __uint_as_float(qe.y);
-            ob[ph + tid] = Bucket::make(fdiv(pv, ave), pe.x, qe.x, nb, vcur, ty);
-            const float r = fsub(qv, fsub(ave, pv));
-            conv = r < ave;
-            ne = make_uint2(qe.x, __float_as_uint(r));
+            const uint32_t i = i0 + j;
+            ne[j] = make_uint2(0u, 0u);
+            if (i < b)
+            {
+                const uint2 pe = P[ph + i], qe = Q[qh + i];
+                const float pv = __uint_as_float(pe.y), qv = __uint_as_float(qe.y);
+                ob[ph + i] = Bucket::make(fdiv(pv, ave), pe.x, qe.x, nb, vcur, ty);
+                const float r = fsub(qv, fsub(ave, pv));
+                ne[j] = make_uint2(qe.x, __float_as_uint(r));
+                if (r < ave)
+                {
+                    convm |= 1u << j;
+                    nc++;
+                }
+                else
+                {
+                    ns++;
+                }
+            }
         }
-        uint32_t rc, rs, tcn, tsn;
-        block_rank2(act && conv, act && !conv, rc, rs, tcn, tsn, sa, sb);
-        if (act)
+        uint32_t tot;
+        const uint32_t ex = block_scan_packed(nc | (ns << 16), tot, s_w);
+        uint32_t pc = pt + (ex & 0xFFFFu), qs = qt + (ex >> 16);
+#pragma unroll
+        for (uint32_t j = 0; j < K; j++)
         {
-            if (conv)
-                P[pt + rc] = ne;
-            else
-                Q[qt + rs] = ne;
+            if (i0 + j < b)
+            {
+                if (convm & (1u << j))
+                    P[pc++] = ne[j];
+                else
+                    Q[qs++] = ne[j];
+            }
         }
         __syncthreads();
         ph += b;
         qh += b;
-        pt += tcn;
-        qt += tsn;
+        pt += tot & 0xFFFFu;
+        qt += tot >> 16;
     }
     for (uint32_t i = tid; i < qt - qh; i += nt)
         ob[pt + i] = Bucket::make(1.0f, Q[qh + i].x, kNone, nb, vcur, ty);
     __syncthreads();
-}
-
-/* Stable block-wide split of the staged values into the p and q queues. */
-template <typename Load>
-__device__ __forceinline__ void block_split(Load load, uint32_t deg, float ave, uint2 *P, uint2 *Q, uint32_t &pt,
-                                            uint32_t &qt, uint32_t *sa, uint32_t *sb)
-{
-    const uint32_t tid = threadIdx.x, nt = blockDim.x;
-    pt = 0;
-    qt = 0;
-    for (uint32_t base = 0; base < deg; base += nt)
-    {
-        const bool valid = base + tid < deg;
-        const float x = valid ? load(base + tid) : 0.0f;
-        const bool sm = valid && x < ave, bg = valid && !(x < ave);
-        uint32_t rs, rq, ts, tq;
-        block_rank2(sm, bg, rs, rq, ts, tq, sa, sb);
-        const uint2 ent = make_uint2(base + tid, __float_as_uint(x));
-        if (sm)
-            P[pt + rs] = ent;
-        if (bg)
-            Q[qt + rq] = ent;
-        pt += ts;
-        qt += tq;
-        __syncthreads();
-    }
 }
 
 /* Group tiers: a group of G lanes per vertex of degree <= DMAX, 32/G vertices
@@ -975,7 +1252,9 @@ __global__ void __launch_bounds__(NT) alias_block_row_kernel(GraphView g, TC tc,
     static_assert(NT % 32 == 0 && NT <= 1024 && DMAX % 8 == 0 && DMAX <= 65535, "block-row tier shape");
     extern __shared__ uint32_t smem[];
     __shared__ uint32_t sa[33], sb[33], s_row[4];
-    __shared__ float s_ave;
+    __shared__ SumMap s_maps[33];
+    __shared__ float s_f;
+    __shared__ uint32_t s_u;
     float *F = reinterpret_cast<float *>(smem);
     uint32_t *N = smem + DMAX;
     uint16_t *P = reinterpret_cast<uint16_t *>(smem + 2 * DMAX);
@@ -999,24 +1278,11 @@ __global__ void __launch_bounds__(NT) alias_block_row_kernel(GraphView g, TC tc,
             N[i] = g.nbr[e0 + i];
         }
         __syncthreads();
-        /* the sum in edge order (:579-584) by thread 0 */
-        if (tid == 0)
-        {
-            float sum = 0.0f;
-            uint32_t i = 0;
-            for (; i + 8 <= deg; i += 8)
-                sum = fadd(fadd(fadd(fadd(fadd(fadd(fadd(fadd(sum, F[i]), F[i + 1]), F[i + 2]), F[i + 3]), F[i + 4]),
-                                     F[i + 5]),
-                                F[i + 6]),
-                           F[i + 7]);
-            for (; i < deg; i++)
-                sum = fadd(sum, F[i]);
-            if (sum_out != nullptr)
-                sum_out[v] = sum;
-            s_ave = fdiv(sum, u2f(deg));
-        }
-        __syncthreads();
-        const float ave = s_ave;
+        /* the sum in edge order (:579-584), exact block scan */
+        const float sum = block_exact_sum<4>([&](uint32_t i) { return F[i]; }, deg, s_maps, &s_f, &s_u);
+        if (tid == 0 && sum_out != nullptr)
+            sum_out[v] = sum;
+        const float ave = fdiv(sum, u2f(deg));
         /* stable split in edge order (:593-602) */
         uint32_t pt = 0, qt = 0;
         for (uint32_t base = 0; base < deg; base += NT)
@@ -1141,17 +1407,21 @@ __global__ void __launch_bounds__(NT) alias_block_row_kernel(GraphView g, TC tc,
     }
 }
 
-/* Hub tier: a 1024-thread block per vertex, queues in global scratch. */
+/* Hub tier: a 1024-thread block per vertex (256 threads for 4097..16384),
+ * queues in global scratch at 2 * off[v].  The row's sum by the exact block
+ * scan (block_exact_sum), then the split and the pairing with four terms or
+ * iterations per thread per pass, so a 163,585-edge row takes ~40 passes of
+ * each instead of one thread's FADD chain and ~160 barrier rounds. */
 template <typename TC, typename Bucket>
 __global__ void __launch_bounds__(1024) alias_build_hub_kernel(GraphView g, TC tc, Bucket *out, const uint64_t *vcur,
                                                                float *sum_out, uint2 *scratch, const uint32_t *order,
                                                                uint32_t lo, uint32_t hi, uint32_t *next)
 {
-    __shared__ float chunk[2][1024];
-    __shared__ uint32_t sa[33], sb[33], s_state[4];
-    __shared__ float s_ave;
-    __shared__ uint32_t s_k;
-    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    __shared__ SumMap s_maps[33];
+    __shared__ uint32_t s_w[33], s_state[4];
+    __shared__ float s_f;
+    __shared__ uint32_t s_u, s_k;
+    const uint32_t tid = threadIdx.x;
     for (;;)
     {
         /* vertices from *next, largest first */
@@ -1165,51 +1435,17 @@ __global__ void __launch_bounds__(1024) alias_build_hub_kernel(GraphView g, TC t
         const uint32_t v = order[k];
         const int64_t e0 = g.off[v];
         const uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
-        /* the sum in edge order (:579-584) by thread 0, double-buffered: the
-         * block loads chunk c + 1 while thread 0 adds chunk c */
-        float sum = 0.0f;
-        if (tid < deg)
-            chunk[0][tid] = static_at(g, tc, v, e0 + tid);
-        __syncthreads();
-        for (uint32_t base = 0, c = 0; base < deg; base += nt, c ^= 1u)
-        {
-            const uint32_t nx = base + nt + tid;
-            const bool more = nx < deg;
-            float x = 0.0f;
-            if (more)
-                x = static_at(g, tc, v, e0 + nx);
-            if (tid == 0)
-            {
-                const uint32_t n = min(nt, deg - base);
-                const float *cc = chunk[c];
-                uint32_t j = 0;
-                for (; j + 8 <= n; j += 8)
-                    sum = fadd(fadd(fadd(fadd(fadd(fadd(fadd(fadd(sum, cc[j]), cc[j + 1]), cc[j + 2]), cc[j + 3]),
-                                                   cc[j + 4]),
-                                              cc[j + 5]),
-                                         cc[j + 6]),
-                                    cc[j + 7]);
-                for (; j < n; j++)
-                    sum = fadd(sum, cc[j]);
-            }
-            if (more)
-                chunk[c ^ 1u][tid] = x;
-            __syncthreads();
-        }
-        if (tid == 0)
-        {
-            s_ave = fdiv(sum, u2f(deg));
-            if (sum_out != nullptr)
-                sum_out[v] = sum;
-        }
-        __syncthreads();
-        const float ave = s_ave;
+        auto load = [&](uint32_t i) { return static_at(g, tc, v, e0 + i); };
+        const float sum = block_exact_sum<4>(load, deg, s_maps, &s_f, &s_u);
+        const float ave = fdiv(sum, u2f(deg));
+        if (tid == 0 && sum_out != nullptr)
+            sum_out[v] = sum;
         uint2 *P = scratch + 2 * e0;
         uint2 *Q = P + deg;
         uint32_t pt, qt;
-        block_split([&](uint32_t i) { return static_at(g, tc, v, e0 + i); }, deg, ave, P, Q, pt, qt, sa, sb);
-        block_pairing(P, Q, pt, qt, ave, out + e0, g.nbr + e0, vcur, g.type != nullptr ? g.type + e0 : nullptr, sa,
-                      sb, s_state);
+        block_split_wide<4>(load, deg, ave, P, Q, pt, qt, s_w);
+        block_pairing_wide<4>(P, Q, pt, qt, ave, out + e0, g.nbr + e0, vcur, g.type != nullptr ? g.type + e0 : nullptr,
+                              s_w, s_state);
     }
 }
 

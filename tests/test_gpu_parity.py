@@ -342,12 +342,17 @@ def test_alias_tables_match_oracle_rmat16(engine, oracle_lib, weights, streams):
 
 
 @pytest.mark.parametrize("hub_grid,streams", [(0, 1), (2, 1), (0, 2), (0, 3), (2, 3)])
-@pytest.mark.parametrize("dist", ["lognormal", "pareto", "uniform", "equal", "twovalue"])
+@pytest.mark.parametrize("dist", ["lognormal", "pareto", "uniform", "equal", "twovalue", "halves", "wide", "tiny",
+                                  "zeros"])
 def test_alias_tables_match_oracle_hubs(engine, oracle_lib, dist, hub_grid, streams):
     """Every build class and both sides of every class boundary: hubs (40000,
     20000, 16385), 4097..16384 (block per vertex, queues in the scratch),
     2049..4096 (block per vertex, shared memory), 1..2048 (lane groups of 32,
-    16, 8, 4 and 2), with rows of unequal degree side by side in a warp."""
+    16, 8, 4 and 2), with rows of unequal degree side by side in a warp.
+    The large rows' sums take the exact block scan; these weights exercise
+    its rounding: halves (exact ties at every binade), wide (lognormal sigma
+    4: terms far above and below the running sum), tiny (sums below 2^-103,
+    the serial chain) and zeros (half the terms +0)."""
     rng = np.random.default_rng(17)
     degs = [40000, 20000, 16385, 16384, 12000, 5000, 4097, 4096, 3000, 2049, 2048, 1500, 1025, 1024, 600, 513, 512,
             300, 129, 128, 100, 33, 32, 31, 17, 16, 7, 1]
@@ -367,8 +372,17 @@ def test_alias_tables_match_oracle_hubs(engine, oracle_lib, dist, hub_grid, stre
         w = 1.0 + 4.0 * rng.random(E)
     elif dist == "equal":
         w = np.full(E, 0.3)
-    else:
+    elif dist == "twovalue":
         w = np.where(rng.random(E) < 0.9, 1.0, 50.0)
+    elif dist == "halves":
+        w = 0.5 * rng.integers(1, 9, size=E)
+    elif dist == "wide":
+        w = rng.lognormal(0.0, 4.0, size=E)
+    elif dist == "tiny":
+        w = 1e-33 * rng.lognormal(0.0, 1.0, size=E)
+    else:
+        w = np.where(rng.random(E) < 0.5, 0.0, rng.lognormal(0.0, 1.0, size=E))
+        w[off[:-1][degs > 0]] = 1.0  # no all-zero row (its 0/0 average is NaN)
     w = w.astype(np.float32)
     engine.load_arrays(V, off, nbr, w)
     engine.set_option("alias_hub_grid", hub_grid)

@@ -122,7 +122,8 @@ kk_status kk_engine_set_stream(kk_engine *e, void *stream);
  *   "alias_hub_grid"     blocks of the hub alias kernel (0: one per two SMs)
  *   "alias_streams"      1 the alias classes of degree <= 16384 in turn on the engine's stream,
  *                        2 those of degree <= 128 after the hubs on a second stream, beside the rest,
- *                        3 (default) those of degree <= 512
+ *                        3 (default) those of degree <= 512, 4 those of degree <= 512 on the second
+ *                        stream from the start and the hubs alone on a third
  *   "into_stream"        1 (default): kk_walk_into walks whose path lengths are known before they
  *                        run (DeepWalk, PPR, node2vec on graphs without reachable dead ends) in one
  *                        launch per epoch and copies each segment of walkers out as soon as its

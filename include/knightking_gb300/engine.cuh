@@ -283,6 +283,8 @@ struct kk_engine
 
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     cudaStream_t side = nullptr; /* hub alias builds run here, joined by events */
+    cudaStream_t hub = nullptr;  /* alias_streams 4: the hubs alone on this stream */
+    cudaEvent_t ev_hub_join = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     /* vertices by degree, descending (cached per graph), and the alias-build
      * classes: tier[k] = number of vertices of degree > kAliasClassMax[k]
@@ -385,7 +387,10 @@ struct kk_engine
     int alias_hub_grid = 0;
     /* alias_streams (option): 1 every class but the hubs on the main stream,
      * 2 the classes of degree <= 128 after the hubs on the side stream, 3 the
-     * classes of degree <= 512 (default: S22 lognormal build 2.69 -> 2.50 ms) */
+     * classes of degree <= 512 (S22 lognormal build 2.69 -> 2.50 ms); 4 the
+     * hubs alone on a third stream, the classes of degree <= 512 on the side
+     * stream from the start (a hub row's pairing is a long chain of rounds
+     * that the small classes need not wait for) */
     int alias_streams = 3;
     /* l2_fetch_bytes (option): the context's cudaLimitMaxL2FetchGranularity
      * hint while the engine lives (0: left as found); the value found is put
@@ -605,18 +610,20 @@ void build_alias(kk_engine *e, const TC &tc)
     KK_CUDA_CHECK(cudaMemsetAsync(next, 0, 16 * sizeof(uint32_t), e->stream));
     const uint32_t *t = e->tier;
     cudaStream_t st = e->stream;
+    const bool hub_alone = e->alias_streams == 4 && e->n_hub;
+    cudaStream_t hub_st = hub_alone ? e->hub : e->side;
+    KK_CUDA_CHECK(cudaEventRecord(e->ev_fork, e->stream));
     if (e->n_hub)
     {
-        /* hubs first, largest first, on the side stream so they start at once */
-        KK_CUDA_CHECK(cudaEventRecord(e->ev_fork, e->stream));
-        KK_CUDA_CHECK(cudaStreamWaitEvent(e->side, e->ev_fork, 0));
+        /* hubs first, largest first, on their own stream so they start at once */
+        KK_CUDA_CHECK(cudaStreamWaitEvent(hub_st, e->ev_fork, 0));
         /* half the SMs by default: the hubs' serial sums and short batches use
          * few lanes, and the classes on the main stream get the other half */
         const uint32_t cap =
             e->alias_hub_grid > 0 ? (uint32_t)e->alias_hub_grid : (uint32_t)(e->sm_count > 1 ? e->sm_count / 2 : 1);
         const unsigned grid = e->n_hub < cap ? e->n_hub : cap;
-        alias_build_hub_kernel<TC, Bucket><<<grid, 1024, 0, e->side>>>(g, tc, alias, vcur, sum, scratch, order, 0,
-                                                                       e->n_hub, next);
+        alias_build_hub_kernel<TC, Bucket><<<grid, 1024, 0, hub_st>>>(g, tc, alias, vcur, sum, scratch, order, 0,
+                                                                      e->n_hub, next);
         count_launch(e);
         KK_CUDA_CHECK(cudaGetLastError());
     }
@@ -655,18 +662,15 @@ void build_alias(kk_engine *e, const TC &tc)
     cudaStream_t light = st;
     if (split)
     {
-        if (!e->n_hub)
-        {
-            KK_CUDA_CHECK(cudaEventRecord(e->ev_fork, e->stream));
+        if (!e->n_hub || hub_alone)
             KK_CUDA_CHECK(cudaStreamWaitEvent(e->side, e->ev_fork, 0));
-        }
         light = e->side;
     }
     static int r3 = 0, r4 = 0, r5 = 0, r6 = 0, r7 = 0, r8 = 0;
     group(alias_group_kernel<TC, Bucket, 32, 2048>, 32, alias_group_smem_per_warp<32, 2048>(), 3, r3, st);
     group(alias_group_kernel<TC, Bucket, 32, 1024>, 32, alias_group_smem_per_warp<32, 1024>(), 4, r4, st);
     group(alias_group_kernel<TC, Bucket, 16, 512>, 16, alias_group_smem_per_warp<16, 512>(), 5, r5,
-          e->alias_streams == 3 ? light : st);
+          e->alias_streams >= 3 ? light : st);
     group(alias_group_kernel<TC, Bucket, 8, 128>, 8, alias_group_smem_per_warp<8, 128>(), 6, r6, light);
     group(alias_group_kernel<TC, Bucket, 4, 32>, 4, alias_group_smem_per_warp<4, 32>(), 7, r7, light);
     group(alias_group_kernel<TC, Bucket, 2, 16>, 2, alias_group_smem_per_warp<2, 16>(), 8, r8, light);
@@ -674,6 +678,11 @@ void build_alias(kk_engine *e, const TC &tc)
     {
         KK_CUDA_CHECK(cudaEventRecord(e->ev_join, e->side));
         KK_CUDA_CHECK(cudaStreamWaitEvent(e->stream, e->ev_join, 0));
+    }
+    if (hub_alone)
+    {
+        KK_CUDA_CHECK(cudaEventRecord(e->ev_hub_join, e->hub));
+        KK_CUDA_CHECK(cudaStreamWaitEvent(e->stream, e->ev_hub_join, 0));
     }
     if constexpr (weight_tables)
     {

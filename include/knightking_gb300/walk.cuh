@@ -562,26 +562,40 @@ __device__ __forceinline__ float static_at(const GraphView &g, const TC &tc, uin
     return tc.static_comp(v, AdjUnit{g.nbr[e], (edge_id_t)e});
 }
 
-/* One warp runs pairing batches of at most 32 iterations until the pairing
- * ends or both queues again hold more than stop_above live entries. */
-template <typename Bucket>
-__device__ __forceinline__ void warp_pairing(uint2 *P, uint2 *Q, uint32_t &ph, uint32_t &pt, uint32_t &qh,
-                                             uint32_t &qt, float ave, Bucket *ob, const uint32_t *nb,
-                                             const uint64_t *vcur, const uint8_t *ty, uint32_t stop_above)
+/* One warp runs pairing batches of at most 32 iterations, with the short
+ * queue in a shared-memory ring: while one queue holds few entries, each
+ * batch consumes entries the previous batch appended, and a global-memory
+ * queue turns every batch into an L2 round trip.  The short queue (Q when QRing, else P) is copied into R (kRingSize
+ * entries, index j at R[j % kRingSize]) on entry and back on exit; the long
+ * queue stays in global memory, where its reads are far from its appends.
+ * The warp leaves when both queues are long again (stop_above), when the
+ * ring is nearly full, or when the pairing ends. */
+constexpr uint32_t kRingSize = 512;
+template <bool QRing, typename Bucket>
+__device__ __forceinline__ void warp_pairing_ring(uint2 *P, uint2 *Q, uint2 *R, uint32_t &ph, uint32_t &pt,
+                                                  uint32_t &qh, uint32_t &qt, float ave, Bucket *ob,
+                                                  const uint32_t *nb, const uint64_t *vcur, const uint8_t *ty,
+                                                  uint32_t stop_above)
 {
     const uint32_t lane = threadIdx.x & 31, lt = lanemask_lt();
+    constexpr uint32_t M = kRingSize - 1;
+    uint2 *G = QRing ? Q : P;
+    const uint32_t h0 = QRing ? qh : ph, t0 = QRing ? qt : pt;
+    for (uint32_t j = h0 + lane; j < t0; j += 32)
+        R[j & M] = G[j];
+    __syncwarp();
     while (ph < pt)
     {
         const uint32_t lp = pt - ph, lq = qt - qh;
         if (lq == 0)
         {
             for (uint32_t i = lane; i < lp; i += 32)
-                ob[ph + i] = Bucket::make(1.0f, P[ph + i].x, kNone, nb, vcur, ty);
+                ob[ph + i] = Bucket::make(1.0f, (QRing ? P[ph + i] : R[(ph + i) & M]).x, kNone, nb, vcur, ty);
             ph = pt;
             break;
         }
         uint32_t b = min(lp, lq);
-        if (b > stop_above)
+        if (b > stop_above || (QRing ? lq : lp) > kRingSize - 64)
             break;
         if (b > 32)
             b = 32;
@@ -590,7 +604,8 @@ __device__ __forceinline__ void warp_pairing(uint2 *P, uint2 *Q, uint32_t &ph, u
         uint2 ne = make_uint2(0, 0);
         if (act)
         {
-            const uint2 pe = P[ph + lane], qe = Q[qh + lane];
+            const uint2 pe = QRing ? P[ph + lane] : R[(ph + lane) & M];
+            const uint2 qe = QRing ? R[(qh + lane) & M] : Q[qh + lane];
             const float pv = __uint_as_float(pe.y), qv = __uint_as_float(qe.y);
             ob[ph + lane] = Bucket::make(fdiv(pv, ave), pe.x, qe.x, nb, vcur, ty);
             const float r = fsub(qv, fsub(ave, pv));
@@ -598,12 +613,25 @@ __device__ __forceinline__ void warp_pairing(uint2 *P, uint2 *Q, uint32_t &ph, u
             ne = make_uint2(qe.x, __float_as_uint(r));
         }
         const uint32_t mc = __ballot_sync(kFullMask, act && conv), ms = __ballot_sync(kFullMask, act && !conv);
+        __syncwarp(); /* every lane has read its ring entries before any append lands */
         if (act)
         {
             if (conv)
-                P[pt + __popc(mc & lt)] = ne;
+            {
+                const uint32_t j = pt + __popc(mc & lt);
+                if (QRing)
+                    P[j] = ne;
+                else
+                    R[j & M] = ne;
+            }
             else
-                Q[qt + __popc(ms & lt)] = ne;
+            {
+                const uint32_t j = qt + __popc(ms & lt);
+                if (QRing)
+                    R[j & M] = ne;
+                else
+                    Q[j] = ne;
+            }
         }
         __syncwarp();
         ph += b;
@@ -611,6 +639,10 @@ __device__ __forceinline__ void warp_pairing(uint2 *P, uint2 *Q, uint32_t &ph, u
         pt += __popc(mc);
         qt += __popc(ms);
     }
+    const uint32_t h1 = QRing ? qh : ph, t1 = QRing ? qt : pt;
+    for (uint32_t j = h1 + lane; j < t1; j += 32)
+        G[j] = R[j & M];
+    __syncwarp();
 }
 
 /* Block-wide stable ranks of two predicates (a, b): exclusive ranks in thread
@@ -946,7 +978,7 @@ __device__ __forceinline__ void block_split_wide(Load load, uint32_t deg, float 
 template <uint32_t K, typename Bucket>
 __device__ __forceinline__ void block_pairing_wide(uint2 *P, uint2 *Q, uint32_t pt, uint32_t qt, float ave,
                                                    Bucket *ob, const uint32_t *nb, const uint64_t *vcur,
-                                                   const uint8_t *ty, uint32_t *s_w, uint32_t *s_state)
+                                                   const uint8_t *ty, uint32_t *s_w, uint32_t *s_state, uint2 *ring)
 {
     const uint32_t tid = threadIdx.x, nt = blockDim.x;
     uint32_t ph = 0, qh = 0;
@@ -965,7 +997,10 @@ __device__ __forceinline__ void block_pairing_wide(uint2 *P, uint2 *Q, uint32_t 
         {
             if (tid < 32)
             {
-                warp_pairing(P, Q, ph, pt, qh, qt, ave, ob, nb, vcur, ty, 128);
+                if (lq <= lp)
+                    warp_pairing_ring<true>(P, Q, ring, ph, pt, qh, qt, ave, ob, nb, vcur, ty, 128);
+                else
+                    warp_pairing_ring<false>(P, Q, ring, ph, pt, qh, qt, ave, ob, nb, vcur, ty, 128);
                 if (tid == 0)
                 {
                     s_state[0] = ph;
@@ -1421,6 +1456,7 @@ __global__ void __launch_bounds__(1024) alias_build_hub_kernel(GraphView g, TC t
     __shared__ uint32_t s_w[33], s_state[4];
     __shared__ float s_f;
     __shared__ uint32_t s_u, s_k;
+    __shared__ uint2 s_ring[kRingSize];
     const uint32_t tid = threadIdx.x;
     for (;;)
     {
@@ -1445,7 +1481,7 @@ __global__ void __launch_bounds__(1024) alias_build_hub_kernel(GraphView g, TC t
         uint32_t pt, qt;
         block_split_wide<4>(load, deg, ave, P, Q, pt, qt, s_w);
         block_pairing_wide<4>(P, Q, pt, qt, ave, out + e0, g.nbr + e0, vcur, g.type != nullptr ? g.type + e0 : nullptr,
-                              s_w, s_state);
+                              s_w, s_state, s_ring);
     }
 }
 
@@ -2543,6 +2579,11 @@ __global__ void __launch_bounds__(256) walk_pool_kernel(GraphView g, WC wc, TC t
  * seed and the walker's id and the job's hooks are rebuilt per walker. */
 
 constexpr uint32_t kMaxBatchJobs = 1024;
+/* resident blocks of 256 threads per SM the batch kernels are compiled for
+ * (the register budget: 4 -> 64 registers a thread) */
+#ifndef KK_BATCH_MINB
+#define KK_BATCH_MINB 4
+#endif
 
 struct BatchJob
 {
@@ -2627,7 +2668,7 @@ struct BatchPark
 /* One thread per walker over the concatenated walkers of all jobs.
  * App::make(job, wc, tc) builds the job's WalkerConfig / TransitionConfig. */
 template <typename S, typename App, typename Bucket>
-__global__ void __launch_bounds__(256, 4) walk_batch_kernel(GraphView g, App app, const BatchJob *jobs, uint32_t njobs,
+__global__ void __launch_bounds__(256, KK_BATCH_MINB) walk_batch_kernel(GraphView g, App app, const BatchJob *jobs, uint32_t njobs,
                                                          uint32_t total, const Bucket *alias,
                                                          const float *alias_sum, uint32_t *path, uint32_t *length,
                                                          unsigned long long *total_steps, int *status,

@@ -651,10 +651,12 @@ kk_status kk_engine_create(kk_engine **out, int device)
         KK_CUDA_CHECK(cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking));
         e->stream = e->own_stream;
         KK_CUDA_CHECK(cudaStreamCreateWithFlags(&e->side, cudaStreamNonBlocking));
+        KK_CUDA_CHECK(cudaStreamCreateWithFlags(&e->hub, cudaStreamNonBlocking));
         for (int i = 0; i < 3; i++)
             KK_CUDA_CHECK(cudaEventCreate(&e->ev[i]));
         KK_CUDA_CHECK(cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming));
         KK_CUDA_CHECK(cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming));
+        KK_CUDA_CHECK(cudaEventCreateWithFlags(&e->ev_hub_join, cudaEventDisableTiming));
         /* mapped pinned words the walks' status and capacity reads land in:
          * a kernel writes them (kk::words_to_host), so the host read waits on
          * the engine's stream only, never on copies queued on other streams */
@@ -694,6 +696,8 @@ void kk_engine_destroy(kk_engine *e)
         cudaEventDestroy(e->ev_fork);
     if (e->ev_join)
         cudaEventDestroy(e->ev_join);
+    if (e->ev_hub_join)
+        cudaEventDestroy(e->ev_hub_join);
     e->order.release();
     e->rows.release();
     e->adjc.release();
@@ -744,6 +748,11 @@ void kk_engine_destroy(kk_engine *e)
     e->vcur.release();
     e->edge_set.release();
     e->bslot.release();
+    if (e->hub)
+    {
+        cudaStreamSynchronize(e->hub);
+        cudaStreamDestroy(e->hub);
+    }
     if (e->side)
     {
         cudaStreamSynchronize(e->side);
@@ -798,7 +807,7 @@ kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value)
             e->alias_hub_grid = (int)value;
         else if (n == "walk_park" && value >= 0 && value <= 32)
             e->walk_park = (int)value;
-        else if (n == "alias_streams" && value >= 1 && value <= 3)
+        else if (n == "alias_streams" && value >= 1 && value <= 4)
             e->alias_streams = (int)value;
         else if (n == "walk_multi" && (value == 1 || value == 2 || value == 4))
             e->walk_multi = (int)value;

@@ -14,7 +14,7 @@ descent: each option in turn, the others held at their best so far).
 
 DEFAULT_SPACE = (
     ("alias_layout", (2, 0, 1)),
-    ("alias_streams", (3, 2, 1)),
+    ("alias_streams", (3, 4, 2, 1)),
     ("node2vec_adjacency", (0, 1)),
     ("walk_block", (256, 128, 64)),
     ("walk_multi", (1, 2, 4)),

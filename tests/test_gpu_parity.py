@@ -341,7 +341,7 @@ def test_alias_tables_match_oracle_rmat16(engine, oracle_lib, weights, streams):
         engine.set_option("alias_streams", 3)
 
 
-@pytest.mark.parametrize("hub_grid,streams", [(0, 1), (2, 1), (0, 2), (0, 3), (2, 3)])
+@pytest.mark.parametrize("hub_grid,streams", [(0, 1), (2, 1), (0, 2), (0, 3), (2, 3), (0, 4), (2, 4)])
 @pytest.mark.parametrize("dist", ["lognormal", "pareto", "uniform", "equal", "twovalue", "halves", "wide", "tiny",
                                   "zeros"])
 def test_alias_tables_match_oracle_hubs(engine, oracle_lib, dist, hub_grid, streams):

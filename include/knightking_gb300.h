@@ -124,6 +124,8 @@ kk_status kk_engine_set_stream(kk_engine *e, void *stream);
  *                        2 those of degree <= 128 after the hubs on a second stream, beside the rest,
  *                        3 (default) those of degree <= 512, 4 those of degree <= 512 on the second
  *                        stream from the start and the hubs alone on a third
+ *   "alias_small_lanes"  0 (default) lane groups of 4 and 2 per row for the alias rows of degree
+ *                        17..32 and 1..16; 1 groups of 2 and 1
  *   "into_stream"        1 (default): kk_walk_into walks whose path lengths are known before they
  *                        run (DeepWalk, PPR, node2vec on graphs without reachable dead ends) in one
  *                        launch per epoch and copies each segment of walkers out as soon as its

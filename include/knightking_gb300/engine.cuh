@@ -392,6 +392,9 @@ struct kk_engine
      * stream from the start (a hub row's pairing is a long chain of rounds
      * that the small classes need not wait for) */
     int alias_streams = 3;
+    /* alias_small_lanes (option): 0 lane groups of 4 (degree 17..32) and 2
+     * (1..16) per row; 1 groups of 2 and 1 */
+    int alias_small_lanes = 0;
     /* l2_fetch_bytes (option): the context's cudaLimitMaxL2FetchGranularity
      * hint while the engine lives (0: left as found); the value found is put
      * back when the option returns to 0 and when the engine is destroyed. */
@@ -672,8 +675,18 @@ void build_alias(kk_engine *e, const TC &tc)
     group(alias_group_kernel<TC, Bucket, 16, 512>, 16, alias_group_smem_per_warp<16, 512>(), 5, r5,
           e->alias_streams >= 3 ? light : st);
     group(alias_group_kernel<TC, Bucket, 8, 128>, 8, alias_group_smem_per_warp<8, 128>(), 6, r6, light);
-    group(alias_group_kernel<TC, Bucket, 4, 32>, 4, alias_group_smem_per_warp<4, 32>(), 7, r7, light);
-    group(alias_group_kernel<TC, Bucket, 2, 16>, 2, alias_group_smem_per_warp<2, 16>(), 8, r8, light);
+    if (e->alias_small_lanes == 0)
+    {
+        group(alias_group_kernel<TC, Bucket, 4, 32>, 4, alias_group_smem_per_warp<4, 32>(), 7, r7, light);
+        group(alias_group_kernel<TC, Bucket, 2, 16>, 2, alias_group_smem_per_warp<2, 16>(), 8, r8, light);
+    }
+    else
+    {
+        /* half the lanes per row: more rows per warp, each row's sum on its own lane */
+        static int r7h = 0, r8h = 0;
+        group(alias_group_kernel<TC, Bucket, 2, 32>, 2, alias_group_smem_per_warp<2, 32>(), 7, r7h, light);
+        group(alias_group_kernel<TC, Bucket, 1, 16>, 1, alias_group_smem_per_warp<1, 16>(), 8, r8h, light);
+    }
     if (e->n_hub || split)
     {
         KK_CUDA_CHECK(cudaEventRecord(e->ev_join, e->side));

@@ -809,6 +809,8 @@ kk_status kk_engine_set_option(kk_engine *e, const char *name, int64_t value)
             e->walk_park = (int)value;
         else if (n == "alias_streams" && value >= 1 && value <= 4)
             e->alias_streams = (int)value;
+        else if (n == "alias_small_lanes" && (value == 0 || value == 1))
+            e->alias_small_lanes = (int)value;
         else if (n == "walk_multi" && (value == 1 || value == 2 || value == 4))
             e->walk_multi = (int)value;
         else if (n == "regroup_interval" && value >= 0 && value <= 4096)

@@ -15,6 +15,7 @@ descent: each option in turn, the others held at their best so far).
 DEFAULT_SPACE = (
     ("alias_layout", (2, 0, 1)),
     ("alias_streams", (3, 4, 2, 1)),
+    ("alias_small_lanes", (0, 1)),
     ("node2vec_adjacency", (0, 1)),
     ("walk_block", (256, 128, 64)),
     ("walk_multi", (1, 2, 4)),
@@ -34,7 +35,7 @@ def space_for(app, weighted, batch=False):
     for name, vals in DEFAULT_SPACE:
         if name in ("regroup_interval", "walk_multi") and batch:
             continue
-        if name in ("alias_layout", "alias_streams") and not weighted:
+        if name in ("alias_layout", "alias_streams", "alias_small_lanes") and not weighted:
             continue
         if name == "node2vec_adjacency" and app != "node2vec":
             continue

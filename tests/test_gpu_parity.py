@@ -387,11 +387,13 @@ def test_alias_tables_match_oracle_hubs(engine, oracle_lib, dist, hub_grid, stre
     engine.load_arrays(V, off, nbr, w)
     engine.set_option("alias_hub_grid", hub_grid)
     engine.set_option("alias_streams", streams)
+    engine.set_option("alias_small_lanes", int(streams == 4))
     try:
         _compare_alias(engine, oracle_lib, V, off, nbr, w)
     finally:
         engine.set_option("alias_hub_grid", 0)
         engine.set_option("alias_streams", 3)
+        engine.set_option("alias_small_lanes", 0)
 
 
 @pytest.mark.parametrize("park", [8, 31, 32])

@@ -781,22 +781,45 @@ __device__ __forceinline__ void block_scan_maps(SumMap mine, SumMap &inc, SumMap
 
 /* The row's sum (every thread of the block gets it): terms load(0..deg), K
  * per thread per window after a serial head of 2 * blockDim.x terms.
- * s_maps: 33 SumMaps, s_f: 1 float, s_u: 1 word of shared memory. */
+ * s_maps: 33 SumMaps, s_f: 1 float, s_u: 1 word of shared memory; s_head:
+ * 2 * blockDim.x floats of shared memory the block stages the head in (so
+ * that the serial chain reads shared memory, not one global load after
+ * another), or nullptr when load() already reads shared memory. */
 template <uint32_t K, typename Load>
-__device__ float block_exact_sum(Load load, uint32_t deg, SumMap *s_maps, float *s_f, uint32_t *s_u)
+__device__ float block_exact_sum(Load load, uint32_t deg, SumMap *s_maps, float *s_f, uint32_t *s_u,
+                                 float *s_head)
 {
     const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    const uint32_t head = deg < 2u * nt ? deg : 2u * nt;
+    if (s_head != nullptr)
+    {
+        for (uint32_t i = tid; i < head; i += nt)
+            s_head[i] = load(i);
+        __syncthreads();
+    }
     /* the first terms on one thread: the partial sums double every few
      * terms there, which would end a window every few terms */
     if (tid == 0)
     {
         float s = 0.0f;
         uint32_t i = 0;
-        const uint32_t head = deg < 2u * nt ? deg : 2u * nt;
-        for (; i + 4 <= head; i += 4)
-            s = fadd(fadd(fadd(fadd(s, load(i)), load(i + 1)), load(i + 2)), load(i + 3));
-        for (; i < head; i++)
-            s = fadd(s, load(i));
+        if (s_head != nullptr)
+        {
+            for (; i + 8 <= head; i += 8)
+                s = fadd(fadd(fadd(fadd(fadd(fadd(fadd(fadd(s, s_head[i]), s_head[i + 1]), s_head[i + 2]),
+                                                 s_head[i + 3]),
+                                            s_head[i + 4]),
+                                       s_head[i + 5]),
+                                  s_head[i + 6]),
+                             s_head[i + 7]);
+            for (; i < head; i++)
+                s = fadd(s, s_head[i]);
+        }
+        else
+        {
+            for (; i < head; i++)
+                s = fadd(s, load(i));
+        }
         *s_f = s;
         *s_u = i;
     }
@@ -938,6 +961,12 @@ __device__ __forceinline__ void block_split_wide(Load load, uint32_t deg, float 
     const uint32_t tid = threadIdx.x, nt = blockDim.x;
     pt = 0;
     qt = 0;
+    /* the next pass's terms are loaded before this pass's scan, so their
+     * latency hides behind its barriers */
+    float nx[K];
+#pragma unroll
+    for (uint32_t j = 0; j < K; j++)
+        nx[j] = tid * K + j < deg ? load(tid * K + j) : 0.0f;
     for (uint32_t base = 0; base < deg; base += nt * K)
     {
         const uint32_t i0 = base + tid * K;
@@ -947,10 +976,13 @@ __device__ __forceinline__ void block_split_wide(Load load, uint32_t deg, float 
         for (uint32_t j = 0; j < K; j++)
         {
             const bool valid = i0 + j < deg;
-            xk[j] = valid ? load(i0 + j) : 0.0f;
+            xk[j] = nx[j];
             cs += valid && xk[j] < ave;
             cb += valid && !(xk[j] < ave);
         }
+#pragma unroll
+        for (uint32_t j = 0; j < K; j++)
+            nx[j] = i0 + nt * K + j < deg ? load(i0 + nt * K + j) : 0.0f;
         uint32_t tot;
         const uint32_t ex = block_scan_packed(cs | (cb << 16), tot, s_w);
         uint32_t ps = pt + (ex & 0xFFFFu), qs = qt + (ex >> 16);
@@ -1314,7 +1346,7 @@ __global__ void __launch_bounds__(NT) alias_block_row_kernel(GraphView g, TC tc,
         }
         __syncthreads();
         /* the sum in edge order (:579-584), exact block scan */
-        const float sum = block_exact_sum<4>([&](uint32_t i) { return F[i]; }, deg, s_maps, &s_f, &s_u);
+        const float sum = block_exact_sum<4>([&](uint32_t i) { return F[i]; }, deg, s_maps, &s_f, &s_u, nullptr);
         if (tid == 0 && sum_out != nullptr)
             sum_out[v] = sum;
         const float ave = fdiv(sum, u2f(deg));
@@ -1457,6 +1489,7 @@ __global__ void __launch_bounds__(1024) alias_build_hub_kernel(GraphView g, TC t
     __shared__ float s_f;
     __shared__ uint32_t s_u, s_k;
     __shared__ uint2 s_ring[kRingSize];
+    __shared__ float s_head[2048];
     const uint32_t tid = threadIdx.x;
     for (;;)
     {
@@ -1472,7 +1505,7 @@ __global__ void __launch_bounds__(1024) alias_build_hub_kernel(GraphView g, TC t
         const int64_t e0 = g.off[v];
         const uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
         auto load = [&](uint32_t i) { return static_at(g, tc, v, e0 + i); };
-        const float sum = block_exact_sum<4>(load, deg, s_maps, &s_f, &s_u);
+        const float sum = block_exact_sum<4>(load, deg, s_maps, &s_f, &s_u, s_head);
         const float ave = fdiv(sum, u2f(deg));
         if (tid == 0 && sum_out != nullptr)
             sum_out[v] = sum;

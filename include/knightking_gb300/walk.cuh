@@ -571,11 +571,9 @@ __device__ __forceinline__ float static_at(const GraphView &g, const TC &tc, uin
  * The warp leaves when both queues are long again (stop_above), when the
  * ring is nearly full, or when the pairing ends. */
 constexpr uint32_t kRingSize = 512;
-template <bool QRing, typename Bucket>
+template <bool QRing>
 __device__ __forceinline__ void warp_pairing_ring(uint2 *P, uint2 *Q, uint2 *R, uint32_t &ph, uint32_t &pt,
-                                                  uint32_t &qh, uint32_t &qt, float ave, Bucket *ob,
-                                                  const uint32_t *nb, const uint64_t *vcur, const uint8_t *ty,
-                                                  uint32_t stop_above)
+                                                  uint32_t &qh, uint32_t &qt, float ave, uint32_t stop_above)
 {
     const uint32_t lane = threadIdx.x & 31, lt = lanemask_lt();
     constexpr uint32_t M = kRingSize - 1;
@@ -588,12 +586,7 @@ __device__ __forceinline__ void warp_pairing_ring(uint2 *P, uint2 *Q, uint2 *R, 
     {
         const uint32_t lp = pt - ph, lq = qt - qh;
         if (lq == 0)
-        {
-            for (uint32_t i = lane; i < lp; i += 32)
-                ob[ph + i] = Bucket::make(1.0f, (QRing ? P[ph + i] : R[(ph + i) & M]).x, kNone, nb, vcur, ty);
-            ph = pt;
-            break;
-        }
+            break; /* the p leftovers: written by the caller's bucket pass */
         uint32_t b = min(lp, lq);
         if (b > stop_above || (QRing ? lq : lp) > kRingSize - 64)
             break;
@@ -606,8 +599,13 @@ __device__ __forceinline__ void warp_pairing_ring(uint2 *P, uint2 *Q, uint2 *R, 
         {
             const uint2 pe = QRing ? P[ph + lane] : R[(ph + lane) & M];
             const uint2 qe = QRing ? R[(qh + lane) & M] : Q[qh + lane];
+            /* the popped ring entry goes to its place in the global queue,
+             * the record the bucket pass reads */
+            if (QRing)
+                Q[qh + lane] = qe;
+            else
+                P[ph + lane] = pe;
             const float pv = __uint_as_float(pe.y), qv = __uint_as_float(qe.y);
-            ob[ph + lane] = Bucket::make(fdiv(pv, ave), pe.x, qe.x, nb, vcur, ty);
             const float r = fsub(qv, fsub(ave, pv));
             conv = r < ave;
             ne = make_uint2(qe.x, __float_as_uint(r));
@@ -1013,26 +1011,22 @@ __device__ __forceinline__ void block_pairing_wide(uint2 *P, uint2 *Q, uint32_t 
                                                    const uint8_t *ty, uint32_t *s_w, uint32_t *s_state, uint2 *ring)
 {
     const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    const uint32_t deg = pt + qt;
     uint32_t ph = 0, qh = 0;
     while (ph < pt)
     {
         const uint32_t lp = pt - ph, lq = qt - qh;
         if (lq == 0)
-        {
-            for (uint32_t i = tid; i < lp; i += nt)
-                ob[ph + i] = Bucket::make(1.0f, P[ph + i].x, kNone, nb, vcur, ty);
-            ph = pt;
             break;
-        }
         const uint32_t b = min(min(lp, lq), nt * K);
         if (b <= 64)
         {
             if (tid < 32)
             {
                 if (lq <= lp)
-                    warp_pairing_ring<true>(P, Q, ring, ph, pt, qh, qt, ave, ob, nb, vcur, ty, 128);
+                    warp_pairing_ring<true>(P, Q, ring, ph, pt, qh, qt, ave, 128);
                 else
-                    warp_pairing_ring<false>(P, Q, ring, ph, pt, qh, qt, ave, ob, nb, vcur, ty, 128);
+                    warp_pairing_ring<false>(P, Q, ring, ph, pt, qh, qt, ave, 128);
                 if (tid == 0)
                 {
                     s_state[0] = ph;
@@ -1062,7 +1056,6 @@ __device__ __forceinline__ void block_pairing_wide(uint2 *P, uint2 *Q, uint32_t 
             {
                 const uint2 pe = P[ph + i], qe = Q[qh + i];
                 const float pv = __uint_as_float(pe.y), qv = __uint_as_float(qe.y);
-                ob[ph + i] = Bucket::make(fdiv(pv, ave), pe.x, qe.x, nb, vcur, ty);
                 const float r = fsub(qv, fsub(ave, pv));
                 ne[j] = make_uint2(qe.x, __float_as_uint(r));
                 if (r < ave)
@@ -1096,28 +1089,43 @@ __device__ __forceinline__ void block_pairing_wide(uint2 *P, uint2 *Q, uint32_t 
         pt += tot & 0xFFFFu;
         qt += tot >> 16;
     }
-    for (uint32_t i = tid; i < qt - qh; i += nt)
-        ob[pt + i] = Bucket::make(1.0f, Q[qh + i].x, kNone, nb, vcur, ty);
+    /* the buckets in pop order: iteration k popped P[k] and Q[k] (both kept
+     * in the linear queues; a p entry's value is final when pushed), then
+     * the leftovers of whichever queue is non-empty with p = 1 (:623-638) */
+    for (uint32_t k = tid; k < deg; k += nt)
+    {
+        if (k < ph)
+        {
+            const uint2 pe = P[k], qe = Q[k];
+            ob[k] = Bucket::make(fdiv(__uint_as_float(pe.y), ave), pe.x, qe.x, nb, vcur, ty);
+        }
+        else
+        {
+            const uint32_t x = k < pt ? P[k].x : Q[qh + (k - pt)].x;
+            ob[k] = Bucket::make(1.0f, x, kNone, nb, vcur, ty);
+        }
+    }
     __syncthreads();
 }
 
 /* Group tiers: a group of G lanes per vertex of degree <= DMAX, 32/G vertices
- * per warp side by side, each row staged in shared memory at 10 B/edge:
- *   F[i]  its probability (static_comp), then its residual (prob[] of :582,
- *         updated in place as :613 does);
- *   N[i]  its neighbour;
- *   Q[s]  the two queues as 16-bit edge indices: the p queue a ring over the
- *         first S0 slots, the q queue a ring over the last B0 slots counted
- *         from the end (neither queue outgrows its start).
+ * per warp side by side, each row staged in shared memory at 12 B/edge:
+ *   F[i]   its probability (static_comp), then its residual (prob[] of :582,
+ *          updated in place as :613 does);
+ *   N[i]   its neighbour;
+ *   Pq, Qq the two queues as linear arrays of 16-bit edge indices (each
+ *          receives at most deg entries), which also record every pairing:
+ *          iteration k pops Pq[k] and Qq[k].
  * A pairing batch is min(lp, lq, G) iterations on the group's lanes, so a
  * vertex whose batches are short shares its warp with other vertices instead
- * of idling 32 - b lanes.  Vertices are taken from *next in degree-descending
+ * of idling 32 - b lanes.  The pairing loop only moves queue entries and
+ * residuals; the buckets are written after it in one converged pass.  Vertices are taken from *next in degree-descending
  * order, 32/G consecutive ones per warp (vertices of similar degree side by
  * side). */
 template <uint32_t G, uint32_t DMAX>
 constexpr size_t alias_group_smem_per_warp()
 {
-    return (size_t)(32 / G) * DMAX * 10;
+    return (size_t)(32 / G) * DMAX * 12;
 }
 
 template <typename TC, typename Bucket, uint32_t G, uint32_t DMAX>
@@ -1134,7 +1142,8 @@ __global__ void __launch_bounds__(32) alias_group_kernel(GraphView g, TC tc, Buc
     const uint32_t glt = (1u << gl) - 1u;
     float *F = reinterpret_cast<float *>(smem) + (size_t)grp * DMAX;
     uint32_t *N = smem + (size_t)RPW * DMAX + (size_t)grp * DMAX;
-    uint16_t *Qs = reinterpret_cast<uint16_t *>(smem + (size_t)2 * RPW * DMAX) + (size_t)grp * DMAX;
+    uint16_t *Pq = reinterpret_cast<uint16_t *>(smem + (size_t)2 * RPW * DMAX) + (size_t)grp * 2 * DMAX;
+    uint16_t *Qq = Pq + DMAX;
     /* every loop below runs to the warp's maximum with per-group predicates,
      * so the groups stay converged and share each instruction.  The next
      * vertices' counter value and row descriptors are fetched while the
@@ -1205,8 +1214,11 @@ __global__ void __launch_bounds__(32) alias_group_kernel(GraphView g, TC tc, Buc
         }
         sum = __shfl_sync(kFullMask, sum, gsh);
         const float ave = fdiv(sum, u2f(deg));
-        /* split in edge order (:593-602): p queue from the front, q queue from the back */
-        uint32_t S0 = 0, B0 = 0;
+        /* split in edge order (:593-602) into two linear queues of 16-bit
+         * edge indices, P from the front of its array, Q from the front of
+         * its own (each queue gets at most deg entries over the whole
+         * pairing: the q tail is B + I - C <= deg) */
+        uint32_t pt = 0, qt = 0;
         for (uint32_t base = 0; base < wdeg; base += G)
         {
             const uint32_t i = base + gl;
@@ -1216,35 +1228,35 @@ __global__ void __launch_bounds__(32) alias_group_kernel(GraphView g, TC tc, Buc
             const uint32_t mp = (__ballot_sync(kFullMask, sm) >> gsh) & gbits;
             const uint32_t mq = (__ballot_sync(kFullMask, bg) >> gsh) & gbits;
             if (sm)
-                Qs[S0 + __popc(mp & glt)] = (uint16_t)i;
+                Pq[pt + __popc(mp & glt)] = (uint16_t)i;
             if (bg)
-                Qs[deg - 1 - (B0 + __popc(mq & glt))] = (uint16_t)i;
-            S0 += __popc(mp);
-            B0 += __popc(mq);
+                Qq[qt + __popc(mq & glt)] = (uint16_t)i;
+            pt += __popc(mp);
+            qt += __popc(mq);
         }
         __syncwarp();
-        /* pairing (:603-630) in batches of at most G iterations; a batch of
-         * b = 0 leaves a finished group's state unchanged */
-        Bucket *ob = out + e0;
-        const uint8_t *ty = g.type != nullptr ? g.type + e0 : nullptr;
-        uint32_t ph = 0, pt = 0, lp = S0, qh = 0, qt = 0, lq = B0, npop = 0;
+        /* pairing (:603-630) in batches of at most G iterations, queue
+         * mechanics and residuals only: iteration k pops P[k] and Q[k], so
+         * the queues themselves record every pairing, and the buckets are
+         * written afterwards in one converged pass.  A p entry's value is
+         * final when it is popped (only popped q entries change), so the
+         * pass reads the same F[P[k]] the iteration saw.  A batch of b = 0
+         * leaves a finished group's state unchanged. */
+        uint32_t ph = 0, qh = 0;
         for (;;)
         {
-            const bool live = lp != 0 && lq != 0;
+            const bool live = ph < pt && qh < qt;
             if (!__any_sync(kFullMask, live))
                 break;
-            const uint32_t b = live ? min(min(lp, lq), G) : 0;
+            const uint32_t b = live ? min(min(pt - ph, qt - qh), G) : 0;
             const bool act = gl < b;
             bool conv = false;
             uint32_t qi = 0;
             if (act)
             {
-                const uint32_t ps = ph + gl, qs = qh + gl;
-                const uint32_t pi = Qs[ps >= S0 ? ps - S0 : ps];
-                qi = Qs[deg - 1 - (qs >= B0 ? qs - B0 : qs)];
-                const float pv = F[pi], qv = F[qi];
-                ob[npop + gl] = Bucket::make_n(fdiv(pv, ave), pi, qi, N[pi], N[qi], vcur, ty);
-                const float r = fsub(qv, fsub(ave, pv));
+                const uint32_t pi = Pq[ph + gl];
+                qi = Qq[qh + gl];
+                const float r = fsub(F[qi], fsub(ave, F[pi]));
                 F[qi] = r;
                 conv = r < ave;
             }
@@ -1253,42 +1265,37 @@ __global__ void __launch_bounds__(32) alias_group_kernel(GraphView g, TC tc, Buc
             if (act)
             {
                 if (conv)
+                    Pq[pt + __popc(mc & glt)] = (uint16_t)qi;
+                else
+                    Qq[qt + __popc(ms & glt)] = (uint16_t)qi;
+            }
+            __syncwarp();
+            ph += b;
+            qh += b;
+            pt += __popc(mc);
+            qt += __popc(ms);
+        }
+        /* the buckets in pop order: pairs (P[k], Q[k]) for k < ph (= qh),
+         * then the leftovers of whichever queue is non-empty with p = 1
+         * (:623-638) */
+        Bucket *ob = out + e0;
+        const uint8_t *ty = g.type != nullptr ? g.type + e0 : nullptr;
+#pragma unroll 2
+        for (uint32_t base = 0; base < wdeg; base += G)
+        {
+            const uint32_t k = base + gl;
+            if (k < deg)
+            {
+                if (k < ph)
                 {
-                    const uint32_t s = pt + __popc(mc & glt);
-                    Qs[s >= S0 ? s - S0 : s] = (uint16_t)qi;
+                    const uint32_t pi = Pq[k], qi = Qq[k];
+                    ob[k] = Bucket::make_n(fdiv(F[pi], ave), pi, qi, N[pi], N[qi], vcur, ty);
                 }
                 else
                 {
-                    const uint32_t s = qt + __popc(ms & glt);
-                    Qs[deg - 1 - (s >= B0 ? s - B0 : s)] = (uint16_t)qi;
+                    const uint32_t x = k - ph < pt - ph ? Pq[k] : Qq[qh + (k - pt)];
+                    ob[k] = Bucket::make_n(1.0f, x, kNone, N[x], 0, vcur, ty);
                 }
-            }
-            __syncwarp();
-            const uint32_t nc = __popc(mc), ns = __popc(ms);
-            ph = ph + b >= S0 ? ph + b - S0 : ph + b;
-            qh = qh + b >= B0 ? qh + b - B0 : qh + b;
-            pt = pt + nc >= S0 ? pt + nc - S0 : pt + nc;
-            qt = qt + ns >= B0 ? qt + ns - B0 : qt + ns;
-            lp = lp - b + nc;
-            lq = lq - b + ns;
-            npop += b;
-        }
-        /* leftovers (:623-638): the rest of whichever queue is non-empty */
-        const uint32_t wleft = __reduce_max_sync(kFullMask, lp + lq);
-        for (uint32_t i = gl; i < wleft; i += G)
-        {
-            if (i < lp)
-            {
-                const uint32_t s = ph + i >= S0 ? ph + i - S0 : ph + i;
-                const uint32_t x = Qs[s];
-                ob[npop + i] = Bucket::make_n(1.0f, x, kNone, N[x], 0, vcur, ty);
-            }
-            else if (i < lp + lq)
-            {
-                const uint32_t j = i - lp;
-                const uint32_t s = qh + j >= B0 ? qh + j - B0 : qh + j;
-                const uint32_t x = Qs[deg - 1 - s];
-                ob[npop + i] = Bucket::make_n(1.0f, x, kNone, N[x], 0, vcur, ty);
             }
         }
         __syncwarp();
@@ -1394,9 +1401,7 @@ __global__ void __launch_bounds__(NT) alias_block_row_kernel(GraphView g, TC tc,
                         {
                             const uint32_t pi = P[wph + lane];
                             qi = Q[wqh + lane];
-                            const float pv = F[pi], qv = F[qi];
-                            ob[wph + lane] = Bucket::make_n(fdiv(pv, ave), pi, qi, N[pi], N[qi], vcur, ty);
-                            const float r = fsub(qv, fsub(ave, pv));
+                            const float r = fsub(F[qi], fsub(ave, F[pi]));
                             F[qi] = r;
                             conv = r < ave;
                         }
@@ -1438,9 +1443,7 @@ __global__ void __launch_bounds__(NT) alias_block_row_kernel(GraphView g, TC tc,
             {
                 const uint32_t pi = P[ph + tid];
                 qi = Q[qh + tid];
-                const float pv = F[pi], qv = F[qi];
-                ob[ph + tid] = Bucket::make_n(fdiv(pv, ave), pi, qi, N[pi], N[qi], vcur, ty);
-                const float r = fsub(qv, fsub(ave, pv));
+                const float r = fsub(F[qi], fsub(ave, F[pi]));
                 F[qi] = r;
                 conv = r < ave;
             }
@@ -1459,16 +1462,21 @@ __global__ void __launch_bounds__(NT) alias_block_row_kernel(GraphView g, TC tc,
             pt += tcn;
             qt += tsn;
         }
-        /* leftovers (:623-638): p entries with no q left, then q entries */
-        for (uint32_t i = tid; i < pt - ph; i += NT)
+        /* the buckets in pop order (iteration k popped P[k] and Q[k]; a p
+         * entry's value is final once popped), then the leftovers of
+         * whichever queue is non-empty with p = 1 (:623-638) */
+        for (uint32_t k2 = tid; k2 < deg; k2 += NT)
         {
-            const uint32_t x = P[ph + i];
-            ob[ph + i] = Bucket::make_n(1.0f, x, kNone, N[x], 0, vcur, ty);
-        }
-        for (uint32_t i = tid; i < qt - qh; i += NT)
-        {
-            const uint32_t x = Q[qh + i];
-            ob[pt + i] = Bucket::make_n(1.0f, x, kNone, N[x], 0, vcur, ty);
+            if (k2 < ph)
+            {
+                const uint32_t pi = P[k2], qi2 = Q[k2];
+                ob[k2] = Bucket::make_n(fdiv(F[pi], ave), pi, qi2, N[pi], N[qi2], vcur, ty);
+            }
+            else
+            {
+                const uint32_t x = k2 < pt ? P[k2] : Q[qh + (k2 - pt)];
+                ob[k2] = Bucket::make_n(1.0f, x, kNone, N[x], 0, vcur, ty);
+            }
         }
         __syncthreads();
     }

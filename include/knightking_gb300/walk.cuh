@@ -1109,23 +1109,24 @@ __device__ __forceinline__ void block_pairing_wide(uint2 *P, uint2 *Q, uint32_t 
 }
 
 /* Group tiers: a group of G lanes per vertex of degree <= DMAX, 32/G vertices
- * per warp side by side, each row staged in shared memory at 12 B/edge:
+ * per warp side by side, each row staged in shared memory at 8 B/edge:
  *   F[i]   its probability (static_comp), then its residual (prob[] of :582,
  *          updated in place as :613 does);
- *   N[i]   its neighbour;
  *   Pq, Qq the two queues as linear arrays of 16-bit edge indices (each
  *          receives at most deg entries), which also record every pairing:
  *          iteration k pops Pq[k] and Qq[k].
  * A pairing batch is min(lp, lq, G) iterations on the group's lanes, so a
  * vertex whose batches are short shares its warp with other vertices instead
  * of idling 32 - b lanes.  The pairing loop only moves queue entries and
- * residuals; the buckets are written after it in one converged pass.  Vertices are taken from *next in degree-descending
- * order, 32/G consecutive ones per warp (vertices of similar degree side by
- * side). */
+ * residuals; the buckets are written after it in one converged pass, which
+ * reads the candidates' neighbours from the row in global memory (keeping
+ * them out of shared memory lets more warps share an SM).  Vertices are
+ * taken from *next in degree-descending order, 32/G consecutive ones per
+ * warp (vertices of similar degree side by side). */
 template <uint32_t G, uint32_t DMAX>
 constexpr size_t alias_group_smem_per_warp()
 {
-    return (size_t)(32 / G) * DMAX * 12;
+    return (size_t)(32 / G) * DMAX * 8;
 }
 
 template <typename TC, typename Bucket, uint32_t G, uint32_t DMAX>
@@ -1141,8 +1142,7 @@ __global__ void __launch_bounds__(32) alias_group_kernel(GraphView g, TC tc, Buc
     const uint32_t lane = threadIdx.x & 31, grp = lane / G, gl = lane % G, gsh = grp * G;
     const uint32_t glt = (1u << gl) - 1u;
     float *F = reinterpret_cast<float *>(smem) + (size_t)grp * DMAX;
-    uint32_t *N = smem + (size_t)RPW * DMAX + (size_t)grp * DMAX;
-    uint16_t *Pq = reinterpret_cast<uint16_t *>(smem + (size_t)2 * RPW * DMAX) + (size_t)grp * 2 * DMAX;
+    uint16_t *Pq = reinterpret_cast<uint16_t *>(smem + (size_t)RPW * DMAX) + (size_t)grp * 2 * DMAX;
     uint16_t *Qq = Pq + DMAX;
     /* every loop below runs to the warp's maximum with per-group predicates,
      * so the groups stay converged and share each instruction.  The next
@@ -1164,14 +1164,11 @@ __global__ void __launch_bounds__(32) alias_group_kernel(GraphView g, TC tc, Buc
         const uint32_t v = d.v, deg = d.deg;
         const int64_t e0 = d.e0;
         const uint32_t wdeg = __reduce_max_sync(kFullMask, deg);
-        /* stage the rows: probabilities and neighbours, G consecutive edges per load */
+        /* stage the rows' probabilities, G consecutive edges per load */
 #pragma unroll 4
         for (uint32_t i = gl; i < wdeg; i += G)
             if (i < deg)
-            {
                 F[i] = static_at(g, tc, v, e0 + i);
-                N[i] = g.nbr[e0 + i];
-            }
         __syncwarp();
         tn = __shfl_sync(kFullMask, tn, 0);
         RowDesc dn{0, 0, 0};
@@ -1280,6 +1277,7 @@ __global__ void __launch_bounds__(32) alias_group_kernel(GraphView g, TC tc, Buc
          * (:623-638) */
         Bucket *ob = out + e0;
         const uint8_t *ty = g.type != nullptr ? g.type + e0 : nullptr;
+        const uint32_t *N = g.nbr + e0; /* the row's neighbours, read from the L1-cached row */
 #pragma unroll 2
         for (uint32_t base = 0; base < wdeg; base += G)
         {

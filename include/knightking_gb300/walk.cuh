@@ -572,15 +572,21 @@ __device__ __forceinline__ float static_at(const GraphView &g, const TC &tc, uin
  * ring is nearly full, or when the pairing ends. */
 constexpr uint32_t kRingSize = 512;
 template <bool QRing>
-__device__ __forceinline__ void warp_pairing_ring(uint2 *P, uint2 *Q, uint2 *R, uint32_t &ph, uint32_t &pt,
+__device__ __forceinline__ void warp_pairing_ring(uint2 *P, uint2 *Q, uint2 *R, uint2 *Lr, uint32_t &ph, uint32_t &pt,
                                                   uint32_t &qh, uint32_t &qt, float ave, uint32_t stop_above)
 {
     const uint32_t lane = threadIdx.x & 31, lt = lanemask_lt();
     constexpr uint32_t M = kRingSize - 1;
     uint2 *G = QRing ? Q : P;
+    uint2 *GL = QRing ? P : Q; /* the long queue */
     const uint32_t h0 = QRing ? qh : ph, t0 = QRing ? qt : pt;
     for (uint32_t j = h0 + lane; j < t0; j += 32)
         R[j & M] = G[j];
+    /* the long queue's head is staged in Lr, refilled up to kRingSize
+     * entries ahead whenever a batch would pass the staged end (one L2 round
+     * trip per refill instead of one per batch); its appends go to global
+     * memory, where a later refill finds them */
+    uint32_t le = QRing ? ph : qh;
     __syncwarp();
     while (ph < pt)
     {
@@ -592,13 +598,22 @@ __device__ __forceinline__ void warp_pairing_ring(uint2 *P, uint2 *Q, uint2 *R, 
             break;
         if (b > 32)
             b = 32;
+        const uint32_t lh = QRing ? ph : qh, ltail = QRing ? pt : qt;
+        if (lh + b > le)
+        {
+            const uint32_t to = min(ltail, lh + kRingSize);
+            for (uint32_t j = le + lane; j < to; j += 32)
+                Lr[j & M] = GL[j];
+            __syncwarp();
+            le = to;
+        }
         const bool act = lane < b;
         bool conv = false;
         uint2 ne = make_uint2(0, 0);
         if (act)
         {
-            const uint2 pe = QRing ? P[ph + lane] : R[(ph + lane) & M];
-            const uint2 qe = QRing ? R[(qh + lane) & M] : Q[qh + lane];
+            const uint2 pe = QRing ? Lr[(ph + lane) & M] : R[(ph + lane) & M];
+            const uint2 qe = QRing ? R[(qh + lane) & M] : Lr[(qh + lane) & M];
             /* the popped ring entry goes to its place in the global queue,
              * the record the bucket pass reads */
             if (QRing)
@@ -641,51 +656,6 @@ __device__ __forceinline__ void warp_pairing_ring(uint2 *P, uint2 *Q, uint2 *R, 
     for (uint32_t j = h1 + lane; j < t1; j += 32)
         G[j] = R[j & M];
     __syncwarp();
-}
-
-/* Block-wide stable ranks of two predicates (a, b): exclusive ranks in thread
- * order and the totals.  sa, sb: 33 words of shared memory each. */
-__device__ __forceinline__ void block_rank2(bool a, bool b, uint32_t &ra, uint32_t &rb, uint32_t &ta, uint32_t &tb,
-                                            uint32_t *sa, uint32_t *sb)
-{
-    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const uint32_t lt = lanemask_lt();
-    const uint32_t ma = __ballot_sync(kFullMask, a), mb = __ballot_sync(kFullMask, b);
-    if (lane == 0)
-    {
-        sa[wid] = __popc(ma);
-        sb[wid] = __popc(mb);
-    }
-    __syncthreads();
-    if (wid == 0)
-    {
-        uint32_t xa = lane < nw ? sa[lane] : 0, xb = lane < nw ? sb[lane] : 0;
-        uint32_t ia = xa, ib = xb;
-        for (int o = 1; o < 32; o <<= 1)
-        {
-            uint32_t ya = __shfl_up_sync(kFullMask, ia, o), yb = __shfl_up_sync(kFullMask, ib, o);
-            if (lane >= (uint32_t)o)
-            {
-                ia += ya;
-                ib += yb;
-            }
-        }
-        if (lane < nw)
-        {
-            sa[lane] = ia - xa;
-            sb[lane] = ib - xb;
-        }
-        if (lane == 31)
-        {
-            sa[32] = ia;
-            sb[32] = ib;
-        }
-    }
-    __syncthreads();
-    ra = sa[wid] + __popc(ma & lt);
-    rb = sb[wid] + __popc(mb & lt);
-    ta = sa[32];
-    tb = sb[32];
 }
 
 /* ---- a row's sum, exact and in parallel ------------------------------------
@@ -1024,9 +994,9 @@ __device__ __forceinline__ void block_pairing_wide(uint2 *P, uint2 *Q, uint32_t 
             if (tid < 32)
             {
                 if (lq <= lp)
-                    warp_pairing_ring<true>(P, Q, ring, ph, pt, qh, qt, ave, 128);
+                    warp_pairing_ring<true>(P, Q, ring, ring + kRingSize, ph, pt, qh, qt, ave, 128);
                 else
-                    warp_pairing_ring<false>(P, Q, ring, ph, pt, qh, qt, ave, 128);
+                    warp_pairing_ring<false>(P, Q, ring, ring + kRingSize, ph, pt, qh, qt, ave, 128);
                 if (tid == 0)
                 {
                     s_state[0] = ph;
@@ -1303,17 +1273,19 @@ __global__ void __launch_bounds__(32) alias_group_kernel(GraphView g, TC tc, Buc
 }
 
 /* Block-row tier: one NT-thread block per vertex of degree <= DMAX, the row
- * staged in shared memory (12 B/edge): F[i] its probability then residual,
- * N[i] its neighbour, and the p and q queues as linear arrays of 16-bit edge
- * indices (each holds at most deg entries over the whole pairing).  Pairing
- * batches span the block (b = min(lp, lq, NT) iterations, one per thread,
- * conversions and survivors appended by block-wide stable ranks) while both
- * queues are long, and warp 0 alone runs them in batches of 32 while one is
- * short.  Vertices come from *next, largest first. */
+ * staged in shared memory (8 B/edge): F[i] its probability then residual,
+ * and the p and q queues as linear arrays of 16-bit edge indices (each holds
+ * at most deg entries over the whole pairing, and iteration k pops P[k] and
+ * Q[k]).  The split and the pairing batches take four terms or iterations
+ * per thread per pass (b = min(lp, lq, 4 NT), conversions and survivors
+ * appended by a block-wide scan of per-thread counts) while both queues are
+ * long, and warp 0 alone runs them in batches of 32 while one is short.  The
+ * buckets are written after the pairing in one pass.  Vertices come from
+ * *next, largest first. */
 template <uint32_t DMAX>
 constexpr size_t alias_block_row_smem()
 {
-    return (size_t)DMAX * 12;
+    return (size_t)DMAX * 8;
 }
 
 template <typename TC, typename Bucket, uint32_t NT, uint32_t DMAX>
@@ -1323,13 +1295,13 @@ __global__ void __launch_bounds__(NT) alias_block_row_kernel(GraphView g, TC tc,
 {
     static_assert(NT % 32 == 0 && NT <= 1024 && DMAX % 8 == 0 && DMAX <= 65535, "block-row tier shape");
     extern __shared__ uint32_t smem[];
-    __shared__ uint32_t sa[33], sb[33], s_row[4];
+    constexpr uint32_t K = 4; /* terms or iterations per thread per pass */
+    __shared__ uint32_t s_w[33], s_row[4];
     __shared__ SumMap s_maps[33];
     __shared__ float s_f;
     __shared__ uint32_t s_u;
     float *F = reinterpret_cast<float *>(smem);
-    uint32_t *N = smem + DMAX;
-    uint16_t *P = reinterpret_cast<uint16_t *>(smem + 2 * DMAX);
+    uint16_t *P = reinterpret_cast<uint16_t *>(smem + DMAX);
     uint16_t *Q = P + DMAX;
     const uint32_t tid = threadIdx.x, lane = tid & 31;
     for (;;)
@@ -1345,41 +1317,53 @@ __global__ void __launch_bounds__(NT) alias_block_row_kernel(GraphView g, TC tc,
         const uint32_t deg = (uint32_t)(g.off[v + 1] - e0);
 #pragma unroll 4
         for (uint32_t i = tid; i < deg; i += NT)
-        {
             F[i] = static_at(g, tc, v, e0 + i);
-            N[i] = g.nbr[e0 + i];
-        }
         __syncthreads();
         /* the sum in edge order (:579-584), exact block scan */
         const float sum = block_exact_sum<4>([&](uint32_t i) { return F[i]; }, deg, s_maps, &s_f, &s_u, nullptr);
         if (tid == 0 && sum_out != nullptr)
             sum_out[v] = sum;
         const float ave = fdiv(sum, u2f(deg));
-        /* stable split in edge order (:593-602) */
+        /* stable split in edge order (:593-602), K consecutive terms per
+         * thread per pass */
         uint32_t pt = 0, qt = 0;
-        for (uint32_t base = 0; base < deg; base += NT)
+        for (uint32_t base = 0; base < deg; base += NT * K)
         {
-            const uint32_t i = base + tid;
-            const bool valid = i < deg;
-            const float x = valid ? F[i] : 0.0f;
-            const bool sm = valid && x < ave, bg = valid && !(x < ave);
-            uint32_t rs, rq, ts, tq;
-            block_rank2(sm, bg, rs, rq, ts, tq, sa, sb);
-            if (sm)
-                P[pt + rs] = (uint16_t)i;
-            if (bg)
-                Q[qt + rq] = (uint16_t)i;
-            pt += ts;
-            qt += tq;
-            __syncthreads();
+            const uint32_t i0 = base + tid * K;
+            uint32_t cs = 0, cb = 0;
+#pragma unroll
+            for (uint32_t j = 0; j < K; j++)
+            {
+                const bool valid = i0 + j < deg;
+                const bool sm = valid && F[i0 + j] < ave;
+                cs += sm;
+                cb += valid && !sm;
+            }
+            uint32_t tot;
+            const uint32_t ex = block_scan_packed(cs | (cb << 16), tot, s_w);
+            uint32_t ps = pt + (ex & 0xFFFFu), qs = qt + (ex >> 16);
+#pragma unroll
+            for (uint32_t j = 0; j < K; j++)
+            {
+                if (i0 + j < deg)
+                {
+                    if (F[i0 + j] < ave)
+                        P[ps++] = (uint16_t)(i0 + j);
+                    else
+                        Q[qs++] = (uint16_t)(i0 + j);
+                }
+            }
+            pt += tot & 0xFFFFu;
+            qt += tot >> 16;
         }
+        __syncthreads();
         /* pairing (:603-630); bucket k is the k-th p pop */
         Bucket *ob = out + e0;
         const uint8_t *ty = g.type != nullptr ? g.type + e0 : nullptr;
         uint32_t ph = 0, qh = 0;
         while (ph < pt && qh < qt)
         {
-            const uint32_t b = min(min(pt - ph, qt - qh), NT);
+            const uint32_t b = min(min(pt - ph, qt - qh), NT * K);
             if (b <= 64)
             {
                 /* warp 0 alone until the pairing ends or both queues are long again */
@@ -1434,35 +1418,54 @@ __global__ void __launch_bounds__(NT) alias_block_row_kernel(GraphView g, TC tc,
                 __syncthreads();
                 continue;
             }
-            const bool act = tid < b;
-            bool conv = false;
-            uint32_t qi = 0;
-            if (act)
+            /* iterations tid*K .. tid*K + K - 1 of the batch */
+            const uint32_t i0 = tid * K;
+            uint32_t qk[K], convm = 0, nc = 0, ns = 0;
+#pragma unroll
+            for (uint32_t j = 0; j < K; j++)
             {
-                const uint32_t pi = P[ph + tid];
-                qi = Q[qh + tid];
-                const float r = fsub(F[qi], fsub(ave, F[pi]));
-                F[qi] = r;
-                conv = r < ave;
+                qk[j] = 0;
+                if (i0 + j < b)
+                {
+                    const uint32_t pi = P[ph + i0 + j];
+                    qk[j] = Q[qh + i0 + j];
+                    const float r = fsub(F[qk[j]], fsub(ave, F[pi]));
+                    F[qk[j]] = r;
+                    if (r < ave)
+                    {
+                        convm |= 1u << j;
+                        nc++;
+                    }
+                    else
+                    {
+                        ns++;
+                    }
+                }
             }
-            uint32_t rc, rs, tcn, tsn;
-            block_rank2(act && conv, act && !conv, rc, rs, tcn, tsn, sa, sb);
-            if (act)
+            uint32_t tot;
+            const uint32_t ex = block_scan_packed(nc | (ns << 16), tot, s_w);
+            uint32_t pc = pt + (ex & 0xFFFFu), qs = qt + (ex >> 16);
+#pragma unroll
+            for (uint32_t j = 0; j < K; j++)
             {
-                if (conv)
-                    P[pt + rc] = (uint16_t)qi;
-                else
-                    Q[qt + rs] = (uint16_t)qi;
+                if (i0 + j < b)
+                {
+                    if (convm & (1u << j))
+                        P[pc++] = (uint16_t)qk[j];
+                    else
+                        Q[qs++] = (uint16_t)qk[j];
+                }
             }
             __syncthreads();
             ph += b;
             qh += b;
-            pt += tcn;
-            qt += tsn;
+            pt += tot & 0xFFFFu;
+            qt += tot >> 16;
         }
         /* the buckets in pop order (iteration k popped P[k] and Q[k]; a p
          * entry's value is final once popped), then the leftovers of
          * whichever queue is non-empty with p = 1 (:623-638) */
+        const uint32_t *N = g.nbr + e0; /* the row's neighbours, from global memory */
         for (uint32_t k2 = tid; k2 < deg; k2 += NT)
         {
             if (k2 < ph)
@@ -1494,7 +1497,7 @@ __global__ void __launch_bounds__(1024) alias_build_hub_kernel(GraphView g, TC t
     __shared__ uint32_t s_w[33], s_state[4];
     __shared__ float s_f;
     __shared__ uint32_t s_u, s_k;
-    __shared__ uint2 s_ring[kRingSize];
+    __shared__ uint2 s_ring[2 * kRingSize]; /* the short queue's ring, the long queue's staged head */
     __shared__ float s_head[2048];
     const uint32_t tid = threadIdx.x;
     for (;;)

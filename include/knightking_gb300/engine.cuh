@@ -651,9 +651,11 @@ void build_alias(kk_engine *e, const TC &tc)
                            });
     }
     /* 1..2048: lane groups, 32/G vertices per warp */
-    auto group = [&](auto kern, uint32_t G, size_t smem, int c, int &res, cudaStream_t s) {
-        launch_alias_class(e, kern, 32, smem, 32 / G, t[c - 1], t[c], res, [&](unsigned grid) {
-            kern<<<grid, 32, smem, s>>>(g, tc, alias, vcur, sum, rows, t[c - 1], t[c], next + c);
+    auto group = [&](auto kern, uint32_t G, size_t smem_warp, int c, int &res, cudaStream_t s) {
+        constexpr unsigned W = kAliasGroupWarps;
+        const size_t smem = smem_warp * W;
+        launch_alias_class(e, kern, 32 * W, smem, W * (32 / G), t[c - 1], t[c], res, [&](unsigned grid) {
+            kern<<<grid, 32 * W, smem, s>>>(g, tc, alias, vcur, sum, rows, t[c - 1], t[c], next + c);
             count_launch(e);
         });
     };

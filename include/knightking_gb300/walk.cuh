@@ -880,6 +880,99 @@ __device__ float block_exact_sum(Load load, uint32_t deg, SumMap *s_maps, float 
     return s;
 }
 
+/* The same exact sum for one row in shared memory on one warp (every lane
+ * gets it): a serial head of 64 terms on lane 0, then windows of 32 K terms
+ * scanned across the lanes. */
+template <uint32_t K>
+__device__ float warp_exact_sum(const float *F, uint32_t deg)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t head = deg < 64u ? deg : 64u;
+    float s = 0.0f;
+    if (lane == 0)
+        for (uint32_t i = 0; i < head; i++)
+            s = fadd(s, F[i]);
+    s = __shfl_sync(kFullMask, s, 0);
+    uint32_t pos = head;
+    while (pos < deg)
+    {
+        const uint32_t bits = __float_as_uint(s), ex = (bits >> 23) & 0xFFu;
+        const uint32_t base = pos + lane * K;
+        float xk[K];
+        bool odd = !(ex >= 24u && ex < 255u) || bits >= 0x80000000u;
+        SumMap m{0u, 0u};
+        const float scale = __uint_as_float((277u - (ex < 24u ? 24u : ex > 254u ? 254u : ex)) << 23);
+#pragma unroll
+        for (uint32_t j = 0; j < K; j++)
+        {
+            const float x = base + j < deg ? F[base + j] : 0.0f;
+            xk[j] = x;
+            odd = odd || __float_as_uint(x) >= 0x7F800000u;
+            m = summap_then(m, summap_term(x, scale));
+        }
+        if (__any_sync(kFullMask, odd))
+        {
+            if (lane == 0)
+                for (uint32_t i = pos; i < deg; i++)
+                    s = fadd(s, F[i]);
+            s = __shfl_sync(kFullMask, s, 0);
+            break;
+        }
+        const uint32_t S = (bits & 0x7FFFFFu) | 0x800000u, p0 = S & 1u;
+        const float u = __uint_as_float((ex - 23u) << 23);
+        SumMap inc = m;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const SumMap prev{__shfl_up_sync(kFullMask, inc.a0, o), __shfl_up_sync(kFullMask, inc.a1, o)};
+            if (lane >= (uint32_t)o)
+                inc = summap_then(prev, inc);
+        }
+        SumMap exc{__shfl_up_sync(kFullMask, inc.a0, 1), __shfl_up_sync(kFullMask, inc.a1, 1)};
+        if (lane == 0)
+            exc = SumMap{0u, 0u};
+        const uint32_t end = S + (p0 ? inc.a1 : inc.a0);
+        const uint32_t stay = (uint32_t)__popc(__ballot_sync(kFullMask, end < (1u << 24)));
+        if (stay == 32u)
+        {
+            s = fmul(u2f(__shfl_sync(kFullMask, end, 31)), u);
+            pos += 32u * K;
+            continue;
+        }
+        float ns = 0.0f;
+        uint32_t np = 0;
+        if (lane == stay)
+        {
+            uint32_t Sj = S + (p0 ? exc.a1 : exc.a0);
+            bool found = false;
+#pragma unroll
+            for (uint32_t j = 0; j < K; j++)
+            {
+                const SumMap t = summap_term(xk[j], scale);
+                const uint32_t a = (Sj & 1u) ? t.a1 : t.a0;
+                if (!found && Sj + a >= (1u << 24))
+                {
+                    ns = fadd(fmul(u2f(Sj), u), xk[j]);
+                    np = base + j + 1;
+                    found = true;
+                }
+                Sj += a;
+            }
+            if (!found)
+            {
+                /* unreachable (see block_exact_sum); the serial chain if not */
+                ns = fmul(u2f(S + (p0 ? exc.a1 : exc.a0)), u);
+                for (uint32_t i = base; i < deg; i++)
+                    ns = fadd(ns, F[i]);
+                np = deg;
+            }
+        }
+        s = __shfl_sync(kFullMask, ns, stay);
+        pos = __shfl_sync(kFullMask, np, stay);
+    }
+    return s;
+}
+
 /* Block-wide exclusive scan of two counts packed as a | b << 16 (each total
  * below 2^16): exclusive prefix and total.  s_w: 33 words of shared memory. */
 __device__ __forceinline__ uint32_t block_scan_packed(uint32_t x, uint32_t &total, uint32_t *s_w)
@@ -1099,16 +1192,24 @@ constexpr size_t alias_group_smem_per_warp()
     return (size_t)(32 / G) * DMAX * 8;
 }
 
+/* Warps per block of the lane-group kernels: each warp works alone (its own
+ * rows, its own slice of shared memory), several to a block because an SM
+ * holds at most 32 blocks, so one-warp blocks would cap it at 32 warps. */
+constexpr uint32_t kAliasGroupWarps = 4;
+
 template <typename TC, typename Bucket, uint32_t G, uint32_t DMAX>
-__global__ void __launch_bounds__(32) alias_group_kernel(GraphView g, TC tc, Bucket *out, const uint64_t *vcur,
-                                                         float *sum_out, const RowDesc *rows, uint32_t lo,
-                                                         uint32_t hi, uint32_t *next)
+__global__ void __launch_bounds__(32 * kAliasGroupWarps) alias_group_kernel(GraphView g, TC tc, Bucket *out,
+                                                                          const uint64_t *vcur, float *sum_out,
+                                                                          const RowDesc *rows, uint32_t lo,
+                                                                          uint32_t hi, uint32_t *next)
 {
     static_assert(G == 1 || G == 2 || G == 4 || G == 8 || G == 16 || G == 32, "group of 1 to 32 lanes");
     static_assert(DMAX % 4 == 0 && DMAX <= 65535, "16-bit queue entries");
     constexpr uint32_t RPW = 32 / G;
     constexpr uint32_t gbits = G == 32 ? kFullMask : (1u << G) - 1u;
-    extern __shared__ uint32_t smem[];
+    extern __shared__ uint32_t smem_all[];
+    /* this warp's slice: 8 B per edge of its RPW rows */
+    uint32_t *smem = smem_all + (size_t)(threadIdx.x >> 5) * RPW * DMAX * 2;
     const uint32_t lane = threadIdx.x & 31, grp = lane / G, gl = lane % G, gsh = grp * G;
     const uint32_t glt = (1u << gl) - 1u;
     float *F = reinterpret_cast<float *>(smem) + (size_t)grp * DMAX;
@@ -1148,20 +1249,10 @@ __global__ void __launch_bounds__(32) alias_group_kernel(GraphView g, TC tc, Buc
         float sum = 0.0f;
         if constexpr (RPW == 1)
         {
-            if (lane == 0)
-            {
-                uint32_t i = 0;
-                for (; i + 8 <= deg; i += 8)
-                    sum = fadd(fadd(fadd(fadd(fadd(fadd(fadd(fadd(sum, F[i]), F[i + 1]), F[i + 2]), F[i + 3]),
-                                                   F[i + 4]),
-                                              F[i + 5]),
-                                         F[i + 6]),
-                                    F[i + 7]);
-                for (; i < deg; i++)
-                    sum = fadd(sum, F[i]);
-                if (deg != 0 && sum_out != nullptr)
-                    sum_out[v] = sum;
-            }
+            /* rows of 513..2048 edges: the exact warp scan */
+            sum = warp_exact_sum<8>(F, deg);
+            if (lane == 0 && deg != 0 && sum_out != nullptr)
+                sum_out[v] = sum;
         }
         else if (gl == 0)
         {

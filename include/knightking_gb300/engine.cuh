@@ -812,17 +812,20 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
         KK_CUDA_CHECK(cudaMemsetAsync(caps + n, 0, sizeof(uint64_t), e->stream));
         if (!rs.fixed_cap)
         {
-            constant_extension_bound_kernel<<<grid_for(e, (uint64_t)n * 32, 256), 256, 0, e->stream>>>(
-                rs.seed, rs.walker_begin, n, rs.const_ext, 1u << 24, caps, d_status);
+            /* the extension bound; exact capacities also give a walker on an
+             * isolated start its one vertex here, with no draws */
+            constant_extension_bound_kernel<<<grid_for(e, n, 256), 256, 0, e->stream>>>(
+                g, exact, rs.d_start, rs.n_start, rs.seed, rs.walker_begin, n, rs.const_ext, 1u << 24, caps,
+                d_status);
             count_launch(e);
             KK_CUDA_CHECK(cudaGetLastError());
         }
-        if (exact)
+        if (exact && rs.fixed_cap)
         {
-            /* the full capacity (fixed length) or the extension bound, and one
-             * vertex for a walker on an isolated start */
+            /* the full capacity, and one vertex for a walker on an isolated
+             * start */
             exact_caps_kernel<<<grid_for(e, n, 256), 256, 0, e->stream>>>(g, rs.d_start, rs.n_start, rs.walker_begin,
-                                                                          n, rs.fixed_cap ? rs.cap : 0u, caps);
+                                                                          n, rs.cap, caps);
             count_launch(e);
             KK_CUDA_CHECK(cudaGetLastError());
         }

@@ -309,11 +309,10 @@ static __global__ void dead_end_kernel(GraphView g, int *flag)
     }
 }
 
-/* Exact path capacities of walks that end only by their extension: cap
- * vertices (fixed length; cap 0 keeps the extension bound already in caps),
- * one for a walker whose start vertex is isolated.  The start vertex is the
- * walk's (start list, or walker id mod V); an out-of-range one gets 1 (the
- * walk fails the call on it). */
+/* Exact path capacities of fixed-length walks that end only by their
+ * extension: cap vertices, one for a walker whose start vertex is isolated.
+ * The start vertex is the walk's (start list, or walker id mod V); an
+ * out-of-range one gets 1 (the walk fails the call on it). */
 static __global__ void exact_caps_kernel(GraphView g, const uint32_t *start, uint32_t n_start, walker_id_t begin,
                                          uint32_t n, uint32_t cap, uint64_t *caps)
 {
@@ -322,10 +321,7 @@ static __global__ void exact_caps_kernel(GraphView g, const uint32_t *start, uin
         const walker_id_t id = begin + i;
         const uint32_t v = start != nullptr ? start[id % n_start] : (uint32_t)(id % g.V);
         const bool alive = v < g.V && g.off[v + 1] > g.off[v];
-        if (!alive)
-            caps[i] = 1;
-        else if (cap != 0)
-            caps[i] = cap;
+        caps[i] = alive ? cap : 1;
     }
 }
 
@@ -1193,9 +1189,10 @@ constexpr size_t alias_group_smem_per_warp()
 }
 
 /* Warps per block of the lane-group kernels: each warp works alone (its own
- * rows, its own slice of shared memory), several to a block because an SM
- * holds at most 32 blocks, so one-warp blocks would cap it at 32 warps. */
-constexpr uint32_t kAliasGroupWarps = 4;
+ * rows, its own slice of shared memory).  Four to a block measured slower
+ * on every class at scale 22 (residency is held by registers and shared
+ * memory before the limit of 32 blocks per SM), so a block is one warp. */
+constexpr uint32_t kAliasGroupWarps = 1;
 
 template <typename TC, typename Bucket, uint32_t G, uint32_t DMAX>
 __global__ void __launch_bounds__(32 * kAliasGroupWarps) alias_group_kernel(GraphView g, TC tc, Bucket *out,
@@ -2976,40 +2973,62 @@ __global__ void __launch_bounds__(256, 4) walk_batch_pool_kernel(GraphView g, Ap
  * probability ext in (0,1) (PPR, src/apps/ppr.hpp:55-58): the walk cannot pass
  * the first step whose first draw (the extension draw, draw 0) says stop.
  * cap[i] = that step + 1 vertices; fails when no stop comes within max_steps.
- * A warp per walker tests 32 consecutive steps at a time and takes the first
- * stop by ballot, so geometric lengths leave no lane waiting on the longest
- * walk of its warp. */
-static __global__ void constant_extension_bound_kernel(uint64_t seed, walker_id_t walker_begin, uint32_t walker_num,
-                                                       float ext, uint32_t max_steps, uint64_t *cap_out, int *status)
+ * A warp takes 32 walkers at a time: with check_starts, each lane first reads
+ * its walker's start vertex (start list, or walker id mod V) and gives a
+ * walker on an isolated or out-of-range start one vertex with no draws (its
+ * walk ends there, or fails the call); the warp then tests 32 consecutive
+ * steps of one live walker at a time and takes the first stop by ballot, so
+ * geometric lengths leave no lane waiting on the longest walk of its warp. */
+static __global__ void constant_extension_bound_kernel(GraphView g, bool check_starts, const uint32_t *start,
+                                                       uint32_t n_start, uint64_t seed, walker_id_t walker_begin,
+                                                       uint32_t walker_num, float ext, uint32_t max_steps,
+                                                       uint64_t *cap_out, int *status)
 {
     const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    for (uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < walker_num; i += nwarps)
+    for (uint64_t base = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; base < walker_num;
+         base += nwarps * 32)
     {
-        const walker_id_t id = walker_begin + (uint32_t)i;
-        uint32_t stop = max_steps;
-        for (uint32_t base = 0; base < max_steps; base += 32)
+        const uint64_t mine = base + lane;
+        bool live = mine < walker_num;
+        if (live && check_starts)
         {
-            const uint32_t s = base + lane;
-            bool says_stop = false;
-            if (s < max_steps)
-            {
-                const uint4 b = philox4x32_10(make_uint4(id, s, 0, 0), k0, k1);
-                says_stop = map_gen_float(b.x, 1.0f) > ext;
-            }
-            const uint32_t m = __ballot_sync(kFullMask, says_stop);
-            if (m != 0)
-            {
-                stop = base + __ffs(m) - 1;
-                break;
-            }
+            const walker_id_t id = walker_begin + (uint32_t)mine;
+            const uint32_t v = start != nullptr ? start[id % n_start] : (uint32_t)(id % g.V);
+            live = v < g.V && g.off[v + 1] > g.off[v];
+            if (!live)
+                cap_out[mine] = 1;
         }
-        if (lane == 0)
+        uint32_t todo = __ballot_sync(kFullMask, live);
+        while (todo != 0)
         {
-            if (stop == max_steps)
-                atomicOr(status, KK_STATUS_PATH_CAPACITY);
-            cap_out[i] = (uint64_t)stop + 1;
+            const uint32_t j = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const walker_id_t id = walker_begin + (uint32_t)(base + j);
+            uint32_t stop = max_steps;
+            for (uint32_t s0 = 0; s0 < max_steps; s0 += 32)
+            {
+                const uint32_t s = s0 + lane;
+                bool says_stop = false;
+                if (s < max_steps)
+                {
+                    const uint4 b = philox4x32_10(make_uint4(id, s, 0, 0), k0, k1);
+                    says_stop = map_gen_float(b.x, 1.0f) > ext;
+                }
+                const uint32_t m = __ballot_sync(kFullMask, says_stop);
+                if (m != 0)
+                {
+                    stop = s0 + __ffs(m) - 1;
+                    break;
+                }
+            }
+            if (lane == 0)
+            {
+                if (stop == max_steps)
+                    atomicOr(status, KK_STATUS_PATH_CAPACITY);
+                cap_out[base + j] = (uint64_t)stop + 1;
+            }
         }
     }
 }

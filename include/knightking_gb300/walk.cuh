@@ -1182,6 +1182,82 @@ __device__ __forceinline__ void block_pairing_wide(uint2 *P, uint2 *Q, uint32_t 
  * them out of shared memory lets more warps share an SM).  Vertices are
  * taken from *next in degree-descending order, 32/G consecutive ones per
  * warp (vertices of similar degree side by side). */
+/* The end of a pairing whose q queue holds one entry q, the usual way a FIFO
+ * pairing ends (one heavy edge left, include/walk.hpp:603-630).  Every
+ * iteration then pops the next p and the same q: r -= ave - prob[p], and q
+ * goes back to the q tail while r >= ave.  The pairing ends at the first
+ * r < ave (q to the p tail, the q queue empty) or when the p queue runs out
+ * (q left in the q queue).  A group runs those iterations as one chain of
+ * subtractions with the reference's roundings in its order, G pops at a
+ * time: lane j of the group computes ave - prob[P[ph + j]] and every lane of
+ * the group folds the differences in turn from shuffles, at a few
+ * instructions per iteration instead of a batch's ballots and compaction.
+ * Q[k] = q records each pop for the bucket pass.  Groups in any other state
+ * run empty chains, so the warp stays converged. */
+template <uint32_t G>
+__device__ __forceinline__ void alias_q1_chain(float *F, uint16_t *Pq, uint16_t *Qq, uint32_t &ph, uint32_t &pt,
+                                               uint32_t &qh, uint32_t &qt, float ave, uint32_t gl, uint32_t gsh)
+{
+    bool chain = ph < pt && qt - qh == 1;
+    if (!__any_sync(kFullMask, chain))
+        return;
+    const uint32_t q = chain ? Qq[qh] : 0u;
+    float r = chain ? F[q] : 0.0f;
+    while (__any_sync(kFullMask, chain))
+    {
+        const uint32_t avail = chain ? min(pt - ph, G) : 0u;
+        const float dj = gl < avail ? fsub(ave, F[Pq[ph + gl]]) : 0.0f;
+        const uint32_t wmax = __reduce_max_sync(kFullMask, avail);
+        uint32_t n = avail;
+        bool conv = false;
+        for (uint32_t j = 0; j < wmax; j++)
+        {
+            const float d = __shfl_sync(kFullMask, dj, gsh + j);
+            if (j < n)
+            {
+                r = fsub(r, d);
+                if (r < ave)
+                {
+                    conv = true;
+                    n = j + 1;
+                }
+            }
+        }
+        if (gl < n)
+            Qq[qh + gl] = (uint16_t)q;
+        ph += n;
+        qh += n;
+        if (chain)
+        {
+            if (conv)
+            {
+                if (gl == 0)
+                {
+                    Pq[pt] = (uint16_t)q;
+                    F[q] = r;
+                }
+                pt += 1;
+                qt = qh;
+                chain = false;
+            }
+            else
+            {
+                qt = qh + 1;
+                if (ph == pt)
+                {
+                    if (gl == 0)
+                    {
+                        Qq[qh] = (uint16_t)q;
+                        F[q] = r;
+                    }
+                    chain = false;
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
 template <uint32_t G, uint32_t DMAX>
 constexpr size_t alias_group_smem_per_warp()
 {
@@ -1296,11 +1372,12 @@ __global__ void __launch_bounds__(32 * kAliasGroupWarps) alias_group_kernel(Grap
          * written afterwards in one converged pass.  A p entry's value is
          * final when it is popped (only popped q entries change), so the
          * pass reads the same F[P[k]] the iteration saw.  A batch of b = 0
-         * leaves a finished group's state unchanged. */
+         * leaves a finished group's state unchanged.  A group whose q queue
+         * holds a single entry leaves the batches for the chain below. */
         uint32_t ph = 0, qh = 0;
         for (;;)
         {
-            const bool live = ph < pt && qh < qt;
+            const bool live = ph < pt && qt - qh > 1;
             if (!__any_sync(kFullMask, live))
                 break;
             const uint32_t b = live ? min(min(pt - ph, qt - qh), G) : 0;
@@ -1330,6 +1407,7 @@ __global__ void __launch_bounds__(32 * kAliasGroupWarps) alias_group_kernel(Grap
             pt += __popc(mc);
             qt += __popc(ms);
         }
+        alias_q1_chain<G>(F, Pq, Qq, ph, pt, qh, qt, ave, gl, gsh);
         /* the buckets in pop order: pairs (P[k], Q[k]) for k < ph (= qh),
          * then the leftovers of whichever queue is non-empty with p = 1
          * (:623-638) */

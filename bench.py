@@ -11,10 +11,11 @@ value : walker-steps/s of the stream through the batched kernel
         (kk_batch_walk_device, 1024 requests per launch, paths in HBM), device
         time from CUDA events on the engine's stream; the plain
         one-launch-per-request kernel is timed beside it (batched_over_plain).
-e2e   : the same stream through the serving C-ABI (kk_serve_submit/poll): job
-        records host->device, every path device->host into pinned memory,
-        inside the timed region (served_over_plain); p50/p99 latency of an
-        open-loop Poisson stream at 70% of that rate.
+e2e   : the same stream through the serving C-ABI (kk_serve_submit/poll,
+        driven by the library's own client kk_serve_replay): job records
+        host->device, every path device->host into pinned memory, inside the
+        timed region (served_over_plain); p50/p99 latency of open-loop Poisson
+        streams at 30%, 50% and 70% of that rate.
 roofline: the walk kernel's bytes touched per walker-step at 32-byte sector
         granularity (the reference's access pattern) over its CUDA-event
         duration per launch, against the measured HBM copy bandwidth; beside it
@@ -477,6 +478,8 @@ def n2v_outlier(p, q):
 
 
 SERVE_JOB_BYTES = 72  # one BatchJob record (walk.cuh), uploaded per job slot of a batch
+LATENCY_LOADS = (0.3, 0.5, 0.7)  # open-loop offered load, fraction of the saturated served rate
+LATENCY_HEAD = 0.5  # the load of the line's headline p50/p99
 
 
 def run_serve_bench(args, wl, world, rank, local):
@@ -486,12 +489,14 @@ def run_serve_bench(args, wl, world, rank, local):
     value  : K passes of the whole stream through kk_batch_walk_device (1024
              requests per launch, paths in HBM), CUDA events on the engine's
              stream; the plain one-launch-per-request kernel is timed beside it.
-    e2e    : K passes through the serving API (kk_serve_submit / kk_serve_poll):
-             every request of a pass submitted at once, its job record copied
-             to the device and its paths copied back into pinned host memory;
-             submit of the first -> paths of the last on the host.
-    latency: an open-loop Poisson stream at 70% of the saturated rate, p50/p99
-             of submit -> paths on the host.
+    e2e    : K passes through the serving API (kk_serve_submit / kk_serve_poll
+             from kk_serve_replay, the library's client): every request of a
+             pass submitted at once, its job record copied to the device and
+             its paths copied back into pinned host memory; submit of the
+             first -> paths of the last on the host.  One pass driven request
+             by request from Python is reported beside it.
+    latency: open-loop Poisson streams at 30%, 50% and 70% of the saturated
+             rate, p50/p99 of submit -> paths on the host.
     parity : the first requests' served paths (and their kk_batch_walk paths)
              against the oracle, walker for walker."""
     import torch
@@ -559,56 +564,45 @@ def run_serve_bench(args, wl, world, rank, local):
         engine.set_option("alias_cache", 0)
         r_steps, r_ms = timed(lambda: plain(reqs[:12]))
         engine.set_option("alias_cache", 1)
-        # e2e: K saturated passes through the server
+        # e2e: K saturated passes through the server, every request of a
+        # pass submitted at once by the library's own client (kk_serve_replay:
+        # kk_serve_submit from one host thread, kk_serve_poll and
+        # kk_paths_free of every result from another)
         srv.reset_stats()
-        s_steps = 0
-        t0 = time.perf_counter()
+        s_steps, s_s = 0, 0.0
         for _ in range(args.steps):
-            tickets = [srv.submit(**r) for r in reqs]
-            for t in tickets:
-                res = srv.poll(t, keep_paths=False)
-                assert res.status == 0
-                s_steps += res.total_steps
-        s_s = time.perf_counter() - t0
+            _, st_k, el_k = srv.replay(reqs, np.zeros(len(reqs)))
+            s_steps += st_k
+            s_s += el_k
         sat = srv.stats()
+        # one pass driven from Python (submit and poll per request through ctypes)
+        t0 = time.perf_counter()
+        py_steps = 0
+        for t in [srv.submit(**r) for r in reqs]:
+            res = srv.poll(t, keep_paths=False)
+            assert res.status == 0
+            py_steps += res.total_steps
+        py_s = time.perf_counter() - t0
     b_ms = allreduce(world, b_ms, "max")
     value = allreduce(world, float(b_steps), "sum") / (b_ms / 1e3)
     served_value = allreduce(world, float(s_steps), "sum") / allreduce(world, s_s, "max")
-    # latency under an open-loop Poisson stream at 70% of the saturated rate
-    rate = 0.7 * served_value / (s_steps / args.steps / len(reqs))
-    rng = np.random.default_rng(11)
-    gaps = rng.exponential(1.0 / rate, len(reqs))
-    srv.reset_stats()
-    results = [None] * len(reqs)
-
-    def poller(ts):
-        for i, t in ts:
-            results[i] = srv.poll(t, keep_paths=False)
-
-    t_start = time.perf_counter()
-    due = t_start
-    pending = []
-    pollers = []
-    for i, r in enumerate(reqs):
-        due += gaps[i]
-        d = due - time.perf_counter()
-        if d > 0:
-            time.sleep(d)
-        pending.append((i, srv.submit(**r)))
-        if len(pending) == 64:
-            th = threading.Thread(target=poller, args=(pending,))
-            th.start()
-            pollers.append(th)
-            pending = []
-    if pending:
-        th = threading.Thread(target=poller, args=(pending,))
-        th.start()
-        pollers.append(th)
-    for th in pollers:
-        th.join()
-    open_s = time.perf_counter() - t_start
-    lat = srv.stats()
-    open_steps = sum(r.total_steps for r in results)
+    # latency under open-loop Poisson streams at 30%, 50% and 70% of the
+    # saturated served rate, three passes of the stream each (the first pass
+    # warms the server up and is not counted), kk_serve_replay keeping the
+    # arrival schedule
+    steps_per_req = s_steps / args.steps / len(reqs)
+    curve = []
+    for frac in LATENCY_LOADS:
+        rate = frac * served_value / steps_per_req
+        rng = np.random.default_rng(11)
+        n_open = 3 * len(reqs)
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, n_open))
+        lat_ms, o_steps, o_s = srv.replay([reqs[i % len(reqs)] for i in range(n_open)], arrivals)
+        kept = lat_ms[len(reqs):]
+        curve.append({"load": frac, "offered_req_s": rate, "offered_steps_s": rate * steps_per_req,
+                      "p50_ms": float(np.percentile(kept, 50)), "p99_ms": float(np.percentile(kept, 99)),
+                      "mean_ms": float(kept.mean()), "throughput": o_steps / o_s, "requests": int(len(kept))})
+    head = next(c for c in curve if c["load"] == LATENCY_HEAD)
     # the parity sample: the stream's first requests up to >= 131072 walkers,
     # served with their paths kept, and the same requests through kk_batch_walk
     n_par, acc = 0, 0
@@ -635,8 +629,8 @@ def run_serve_bench(args, wl, world, rank, local):
     # return-edge lookups of the outlier bound: one per step of a request in
     # the outlier regime (1/p > max(1, 1/q)), from the requests' own step counts
     per_job = engine.batch_walk(app, reqs[:1024], keep_paths=False)
-    r_steps = sum(res["total_steps"] for res, r in zip(per_job, reqs[:1024]) if n2v_outlier(r["p"], r["q"]))
-    R = r_steps / max(1, sum(res["total_steps"] for res in per_job))
+    out_steps = sum(res["total_steps"] for res, r in zip(per_job, reqs[:1024]) if n2v_outlier(r["p"], r["q"]))
+    R = out_steps / max(1, sum(res["total_steps"] for res in per_job))
     b_step = 40 + T * (40 + 32) + P * 32 + 4
     design_b = 40 + T * 32 + Q * 32 + R * 64 + 4
     peak, peak_kind = load_peaks()
@@ -704,14 +698,22 @@ def run_serve_bench(args, wl, world, rank, local):
         "served": {"value": served_value, "unit": "walker-steps/s",
                    "what": "kk_serve_*, every request of a pass submitted at once; submit -> paths on the host "
                            "(the line's e2e)",
+                   "client": "kk_serve_replay (the library's client: submit from one host thread, poll and "
+                             "free from another)",
+                   "python_client": {"value": py_steps / py_s, "unit": "walker-steps/s",
+                                     "what": "one pass submitted and polled request by request from Python "
+                                             "through ctypes"},
                    "batches": sat["batches"], "mean_batch_jobs": sat["mean_batch_jobs"],
                    "slot_time_ms": {"walk": sat["walk_ms"], "copy_to_pinned": sat["copy_ms"],
                                     "per_request_copies": sat["host_ms"]}},
         "batched_over_plain": value / plain_value,
         "served_over_plain": served_value / plain_value,
-        "latency": {"offered_rate_req_s": rate, "p50_ms": lat["p50_ms"], "p99_ms": lat["p99_ms"],
-                    "mean_ms": lat["mean_ms"], "throughput": open_steps / open_s,
-                    "what": "open-loop Poisson arrivals at 70% of the saturated rate; submit -> paths on the host"},
+        "latency": {"load": head["load"], "offered_rate_req_s": head["offered_req_s"], "p50_ms": head["p50_ms"],
+                    "p99_ms": head["p99_ms"], "mean_ms": head["mean_ms"], "throughput": head["throughput"],
+                    "curve": curve,
+                    "what": "open-loop Poisson arrivals (kk_serve_replay) at a stated fraction of the saturated "
+                            "served rate; submit -> paths on the host; the headline fields at load %.1f, the curve "
+                            "at every load" % LATENCY_HEAD},
         "e2e": {"value": served_value, "unit": "walker-steps/s",
                 "h2d_bytes_per_step": (sat["batches"] // max(args.steps, 1)) * 1024 * SERVE_JOB_BYTES,
                 "d2h_bytes_per_step": d2h // args.steps},

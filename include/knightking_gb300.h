@@ -318,6 +318,17 @@ kk_status kk_serve_stats_reset(kk_server *s);
 /* Finishes the queued requests, stops the slots and frees the server (results
  * not yet polled are freed). */
 kk_status kk_serve_stop(kk_server *s);
+/* Open-loop client for measuring a server: submits reqs[i] through
+ * kk_serve_submit at arrival_s[i] seconds (non-decreasing) after the call
+ * starts, from the calling thread, while a second host thread polls every
+ * request in order and frees its paths.  latency_ms[i] (may be NULL) receives
+ * request i's submit-to-host latency, *total_steps the walker-steps of all
+ * requests and *elapsed_s the time from the call's start to the last result.
+ * A client driven from an interpreter adds its own per-call overhead to the
+ * arrivals; this one keeps the schedule.  Returns the first failed submit's or
+ * request's status (the requests submitted before it still finish). */
+kk_status kk_serve_replay(kk_server *s, const kk_walk_opts *reqs, const double *arrival_s, uint32_t n,
+                          double *latency_ms, uint64_t *total_steps, double *elapsed_s);
 
 /* Access counts of the last walk call's last epoch when the walk_stats option
  * is on (zeros otherwise): rejection trials, second-order queries, and the

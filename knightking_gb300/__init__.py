@@ -478,6 +478,26 @@ class Server:
         res.total_steps = int(total_steps)
         return res
 
+    def replay(self, requests, arrival_s):
+        """Open-loop client in the library (kk_serve_replay): request i (a dict
+        of submit() keywords) is submitted arrival_s[i] seconds after the
+        call starts while a library thread polls and frees every result.
+        Returns (latency_ms per request, walker-steps, elapsed seconds)."""
+        requests = [dict(r, weighted=r.get("weighted", self.weighted)) for r in requests]
+        arr, keep = self._engine._job_array(self.app, requests)
+        arrival = np.ascontiguousarray(arrival_s, dtype=np.float64)
+        if len(arrival) != len(requests):
+            raise ValueError("one arrival time per request")
+        lat = np.zeros(len(requests), np.float64)
+        steps = ctypes.c_uint64()
+        elapsed = ctypes.c_double()
+        st = self._lib.kk_serve_replay(self._h, arr, arrival.ctypes.data, len(requests), lat.ctypes.data,
+                                       ctypes.byref(steps), ctypes.byref(elapsed))
+        del keep
+        if st != _capi.KK_OK:
+            raise KKError(st, "replay failed")
+        return lat, int(steps.value), float(elapsed.value)
+
     def stats(self):
         s = _capi.KKServeStats()
         self._lib.kk_serve_stats_get(self._h, ctypes.byref(s))

@@ -149,6 +149,7 @@ _SIGS = {
     "kk_serve_stats_get": (ctypes.c_int, [_P, _P]),
     "kk_serve_stats_reset": (ctypes.c_int, [_P]),
     "kk_serve_stop": (ctypes.c_int, [_P]),
+    "kk_serve_replay": (ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, _P, _P, _P]),
     "kk_paths_free": (None, [_P]),
     "kk_paths_dump": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]),
 }

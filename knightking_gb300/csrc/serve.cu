@@ -400,6 +400,89 @@ kk_status kk_serve_stats_reset(kk_server *s)
     return KK_OK;
 }
 
+kk_status kk_serve_replay(kk_server *s, const kk_walk_opts *reqs, const double *arrival_s, uint32_t n,
+                          double *latency_ms, uint64_t *total_steps, double *elapsed_s)
+{
+    if (!s || !reqs || !arrival_s || n == 0)
+        return KK_ERR_INVALID_CONFIG;
+    for (uint32_t i = 1; i < n; i++)
+        if (!(arrival_s[i] >= arrival_s[i - 1]))
+            return KK_ERR_INVALID_CONFIG;
+    std::vector<uint64_t> tickets(n, 0);
+    std::mutex m;
+    std::condition_variable cv;
+    uint32_t n_sub = 0;      /* tickets[0, n_sub) are valid */
+    bool sub_done = false;   /* no more submissions */
+    kk_status sub_st = KK_OK, res_st = KK_OK;
+    uint64_t steps = 0;
+    const Clock::time_point t0 = Clock::now();
+    std::thread poller([&] {
+        for (uint32_t i = 0;; i++)
+        {
+            {
+                std::unique_lock<std::mutex> lk(m);
+                cv.wait(lk, [&] { return i < n_sub || sub_done; });
+                if (i >= n_sub)
+                    return;
+            }
+            kk_serve_result r;
+            const kk_status st = kk_serve_poll(s, tickets[i], -1, &r);
+            if (st != KK_OK || r.status != KK_OK)
+            {
+                if (res_st == KK_OK)
+                    res_st = st != KK_OK ? st : r.status;
+                if (latency_ms)
+                    latency_ms[i] = -1.0;
+            }
+            else if (latency_ms)
+            {
+                latency_ms[i] = r.latency_ms;
+            }
+            if (st == KK_OK && r.paths)
+            {
+                steps += r.paths->total_steps;
+                kk_paths_free(r.paths);
+            }
+        }
+    });
+    for (uint32_t i = 0; i < n; i++)
+    {
+        /* sleep until shortly before the arrival, then spin to it */
+        const Clock::time_point due =
+            t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(arrival_s[i]));
+        if (due - Clock::now() > std::chrono::microseconds(200))
+            std::this_thread::sleep_until(due - std::chrono::microseconds(100));
+        while (Clock::now() < due)
+        {
+        }
+        const kk_status st = kk_serve_submit(s, &reqs[i], &tickets[i]);
+        if (st != KK_OK)
+        {
+            sub_st = st;
+            if (latency_ms)
+                for (uint32_t j = i; j < n; j++)
+                    latency_ms[j] = -1.0;
+            break;
+        }
+        {
+            std::lock_guard<std::mutex> lk(m);
+            n_sub = i + 1;
+        }
+        cv.notify_one();
+    }
+    {
+        std::lock_guard<std::mutex> lk(m);
+        sub_done = true;
+    }
+    cv.notify_one();
+    poller.join();
+    if (total_steps)
+        *total_steps = steps;
+    if (elapsed_s)
+        *elapsed_s = std::chrono::duration<double>(Clock::now() - t0).count();
+    return sub_st != KK_OK ? sub_st : res_st;
+}
+
 kk_status kk_serve_stop(kk_server *s)
 {
     if (!s)

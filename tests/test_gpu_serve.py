@@ -108,3 +108,32 @@ def test_server_refuses_bad_requests(engine):
         assert srv.poll(t).status == 0
         with pytest.raises(kk.KKError):
             srv.poll(t)                                             # handed out once
+
+
+def test_replay_client_keeps_schedule_and_counts_every_step(engine):
+    """kk_serve_replay (the library's open-loop client): every request
+    completes with a latency, the walker-steps equal those of the same
+    requests run alone, an arrival schedule that spreads the requests over
+    0.2 s is kept (the call lasts at least that long), and a schedule that
+    runs backwards or a refused request is reported."""
+    import knightking_gb300 as kk
+    _load(engine, 13)
+    reqs = _requests("node2vec", 80, seed=9)
+    alone = sum(engine.walk("node2vec", dict(r)["walker_num"], **{k: v for k, v in r.items() if k != "walker_num"})
+                .total_steps for r in reqs)
+    with engine.serve("node2vec", slots=2, max_jobs=16, slot_bytes=8 << 20) as srv:
+        lat, steps, elapsed = srv.replay(reqs, np.zeros(len(reqs)))
+        assert steps == alone
+        assert np.all(lat > 0)
+        arrivals = np.linspace(0.0, 0.2, len(reqs))
+        lat, steps, elapsed = srv.replay(reqs, arrivals)
+        assert steps == alone and np.all(lat > 0)
+        assert elapsed >= 0.2
+        with pytest.raises(kk.KKError):
+            srv.replay(reqs[:3], [0.0, 0.2, 0.1])
+        bad = [dict(reqs[0]), dict(reqs[1], p=0.0), dict(reqs[2])]
+        with pytest.raises(kk.KKError):
+            srv.replay(bad, np.zeros(3))
+        # the server still serves after the refused request
+        lat, steps, _ = srv.replay(reqs[:4], np.zeros(4))
+        assert np.all(lat > 0)

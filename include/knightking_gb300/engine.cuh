@@ -300,7 +300,7 @@ struct kk_engine
     int walk_set = 0;
     int into_chunks = 6;
     kk::DevBuf path_x[2], length_x[2], path_off_x[2], caps_x[2]; /* output sets 1 and 2 */
-    kk::DevBuf into_lens[3], into_off[3], into_offb[3], into_verts[3], into_cub[3];
+    kk::DevBuf into_lens[3], into_off[3], into_offb[3], into_lenb[3], into_verts[3], into_cub[3];
     cudaStream_t copy_stream = nullptr;
     void *h_status = nullptr;      /* mapped pinned words for the walks' status and capacity reads */
     void *d_status_host = nullptr; /* the device address of h_status */

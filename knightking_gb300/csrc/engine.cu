@@ -153,6 +153,20 @@ __global__ void offsets_plus_base_kernel(const uint64_t *off, uint32_t cap, uint
         out[i] = (off ? off[i] : (uint64_t)i * cap) + base;
 }
 
+/* A streamed walk's host-side offsets (packed offsets plus the chunk's base)
+ * and path lengths, from its exact path offsets: walker i's length is
+ * off[i + 1] - off[i], the capacity the walk fills exactly. */
+__global__ void offsets_lengths_kernel(const uint64_t *off, uint64_t base, uint32_t n, uint64_t *out_off,
+                                       uint32_t *out_len)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const uint64_t a = off[i];
+        out_off[i] = a + base;
+        out_len[i] = (uint32_t)(off[i + 1] - a);
+    }
+}
+
 /* Gather-ceiling probe: every thread follows two dependent chains of random
  * 32 B-aligned reads over n sectors (the access a walk step makes: the next
  * address depends on the value read). */
@@ -346,6 +360,7 @@ uint64_t pack_paths_on(kk_engine *e, const WalkResult &r, cudaStream_t st, int s
  * every chunk would build), unless the alias_cache option keeps them across
  * calls anyway. */
 constexpr uint32_t kIntoMinChunk = 1u << 18;
+constexpr uint32_t kIntoMinRun = 4; /* streamed segments per copy while the walk runs */
 
 uint64_t walk_into_chunked(kk_engine *e, const kk_walk_opts *o, uint32_t *h_length, uint64_t *h_offset,
                            uint32_t *h_vertices, uint64_t capacity)
@@ -423,12 +438,16 @@ uint64_t walk_into_chunked(kk_engine *e, const kk_walk_opts *o, uint32_t *h_leng
                     if (base + total > capacity)
                         fail(KK_ERR_PATH_CAPACITY, "vertices buffer too small");
                     /* the offsets are final (the engine's stream has been
-                     * synchronised): out at once, beside the walk */
+                     * synchronised), and so are the lengths, which the walk
+                     * fills exactly: both out at once, while the walk's first
+                     * segments are still walking */
                     uint64_t *ob = e->into_offb[s].as<uint64_t>((uint64_t)n + 1);
-                    offsets_plus_base_kernel<<<grid_for(e, n, 256), 256, 0, cs>>>(d_off, 0, base, n, ob);
+                    uint32_t *lb = e->into_lenb[s].as<uint32_t>((uint64_t)n + 1);
+                    offsets_lengths_kernel<<<grid_for(e, n, 256), 256, 0, cs>>>(d_off, base, n, ob, lb);
                     count_launch(e);
                     KK_CUDA_CHECK(cudaGetLastError());
                     KK_CUDA_CHECK(cudaMemcpyAsync(h_offset + cb, ob, (size_t)n * 8, cudaMemcpyDeviceToHost, cs));
+                    KK_CUDA_CHECK(cudaMemcpyAsync(h_length + cb, lb, (size_t)n * 4, cudaMemcpyDeviceToHost, cs));
                 };
                 sink.during = [&](const uint32_t *d_len, const uint32_t *d_path, uint32_t n, uint32_t shift,
                                   uint32_t nseg, const volatile uint32_t *flag, const volatile uint64_t *bound,
@@ -448,7 +467,6 @@ uint64_t walk_into_chunked(kk_engine *e, const kk_walk_opts *o, uint32_t *h_leng
                             else if (q != cudaErrorNotReady)
                                 KK_CUDA_CHECK(q);
                         }
-                        bool issued = false;
                         for (uint32_t a = 0; a < nseg;)
                         {
                             if (out[a] || !(all || flag[a]))
@@ -458,22 +476,26 @@ uint64_t walk_into_chunked(kk_engine *e, const kk_walk_opts *o, uint32_t *h_leng
                             }
                             uint32_t b = a;
                             while (b < nseg && !out[b] && (all || flag[b]))
-                                out[b++] = 1;
-                            const uint32_t wa = a << shift;
-                            const uint32_t wb = (uint64_t)b << shift < n ? b << shift : n;
+                                b++;
+                            /* finished segments go out in runs of at least
+                             * kIntoMinRun (the copy engine moves fewer, larger
+                             * copies faster), the last ones as they come */
+                            if (!all && b - a < kIntoMinRun && b < nseg)
+                            {
+                                a = b;
+                                continue;
+                            }
+                            for (uint32_t k = a; k < b; k++)
+                                out[k] = 1;
                             const uint64_t va = bound[a], vb = bound[b];
-                            KK_CUDA_CHECK(cudaMemcpyAsync(h_length + cb + wa, d_len + wa, (size_t)(wb - wa) * 4,
-                                                          cudaMemcpyDeviceToHost, cs));
                             if (vb > va)
                                 KK_CUDA_CHECK(cudaMemcpyAsync(h_vertices + base + va, d_path + va,
                                                               (size_t)(vb - va) * 4, cudaMemcpyDeviceToHost, cs));
                             left -= b - a;
-                            issued = true;
                             a = b;
                         }
                         /* no yield: the thread keeps its core, so a finished
                          * segment waits microseconds, not a time slice */
-                        (void)issued;
                     }
                 };
                 e->seg_sink = &sink;
@@ -725,6 +747,7 @@ void kk_engine_destroy(kk_engine *e)
         e->into_lens[i].release();
         e->into_off[i].release();
         e->into_offb[i].release();
+        e->into_lenb[i].release();
         e->into_verts[i].release();
         e->into_cub[i].release();
     }

@@ -315,6 +315,7 @@ struct kk_engine
     kk::DevBuf batch_small, batch_rel;
     kk::HostPool *host_pool = nullptr;
     cudaEvent_t ev_walked[3] = {nullptr, nullptr, nullptr}, ev_copied[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t ev_seg_copy = nullptr; /* after the last streamed segment copy issued */
     /* no walker can reach a vertex without out-edges except by starting on
      * one (every edge's target has out-edges); cached per graph */
     bool no_dead_ends = false, dead_ends_valid = false;
@@ -812,10 +813,11 @@ void run_walk_with(kk_engine *e, const WC &wc, const TC &tc, const RunSpec &rs, 
         KK_CUDA_CHECK(cudaMemsetAsync(caps + n, 0, sizeof(uint64_t), e->stream));
         if (!rs.fixed_cap)
         {
-            /* the extension bound; exact capacities also give a walker on an
-             * isolated start its one vertex here, with no draws */
+            /* the extension bound; a walker on an isolated start gets its one
+             * vertex here, with no draws (its walk ends there at once: a bound
+             * that is exact, packed paths or not) */
             constant_extension_bound_kernel<<<grid_for(e, n, 256), 256, 0, e->stream>>>(
-                g, exact, rs.d_start, rs.n_start, rs.seed, rs.walker_begin, n, rs.const_ext, 1u << 24, caps,
+                g, true, rs.d_start, rs.n_start, rs.seed, rs.walker_begin, n, rs.const_ext, 1u << 24, caps,
                 d_status);
             count_launch(e);
             KK_CUDA_CHECK(cudaGetLastError());

@@ -379,6 +379,7 @@ uint64_t walk_into_chunked(kk_engine *e, const kk_walk_opts *o, uint32_t *h_leng
             KK_CUDA_CHECK(cudaEventCreateWithFlags(&e->ev_walked[i], cudaEventDisableTiming));
             KK_CUDA_CHECK(cudaEventCreateWithFlags(&e->ev_copied[i], cudaEventDisableTiming));
         }
+        KK_CUDA_CHECK(cudaEventCreateWithFlags(&e->ev_seg_copy, cudaEventDisableTiming));
     }
     const int user_cache = e->alias_cache;
     struct Restore
@@ -454,7 +455,7 @@ uint64_t walk_into_chunked(kk_engine *e, const kk_walk_opts *o, uint32_t *h_leng
                                   cudaEvent_t walked) {
                     std::vector<char> out(nseg, 0);
                     uint32_t left = nseg;
-                    bool all = false;
+                    bool all = false, issued_any = false;
                     while (left > 0)
                     {
                         if (!all)
@@ -477,13 +478,20 @@ uint64_t walk_into_chunked(kk_engine *e, const kk_walk_opts *o, uint32_t *h_leng
                             uint32_t b = a;
                             while (b < nseg && !out[b] && (all || flag[b]))
                                 b++;
-                            /* finished segments go out in runs of at least
-                             * kIntoMinRun (the copy engine moves fewer, larger
-                             * copies faster), the last ones as they come */
-                            if (!all && b - a < kIntoMinRun && b < nseg)
+                            /* while the copy engine has work queued, finished
+                             * segments wait to go out in runs of at least
+                             * kIntoMinRun (it moves fewer, larger copies
+                             * faster); an idle engine takes whatever is ready */
+                            if (!all && b - a < kIntoMinRun && b < nseg && issued_any)
                             {
-                                a = b;
-                                continue;
+                                const cudaError_t q = cudaEventQuery(e->ev_seg_copy);
+                                if (q == cudaErrorNotReady)
+                                {
+                                    a = b;
+                                    continue;
+                                }
+                                if (q != cudaSuccess)
+                                    KK_CUDA_CHECK(q);
                             }
                             for (uint32_t k = a; k < b; k++)
                                 out[k] = 1;
@@ -491,6 +499,8 @@ uint64_t walk_into_chunked(kk_engine *e, const kk_walk_opts *o, uint32_t *h_leng
                             if (vb > va)
                                 KK_CUDA_CHECK(cudaMemcpyAsync(h_vertices + base + va, d_path + va,
                                                               (size_t)(vb - va) * 4, cudaMemcpyDeviceToHost, cs));
+                            KK_CUDA_CHECK(cudaEventRecord(e->ev_seg_copy, cs));
+                            issued_any = true;
                             left -= b - a;
                             a = b;
                         }
@@ -734,6 +744,8 @@ void kk_engine_destroy(kk_engine *e)
             cudaEventDestroy(e->ev_walked[i]);
             cudaEventDestroy(e->ev_copied[i]);
         }
+        if (e->ev_seg_copy)
+            cudaEventDestroy(e->ev_seg_copy);
     }
     for (int i = 0; i < 2; i++)
     {

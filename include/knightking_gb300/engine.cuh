@@ -112,11 +112,32 @@ struct BatchSlot
     uint64_t max_cap = 0;
     cudaGraphExec_t exec = nullptr;
     char *h_stage = nullptr; /* pinned: jobs | schemes | header | status */
+    /* per-request completion (serving): counters and status words on the
+     * device, flags in mapped host memory (notify.count == nullptr: off); the
+     * slot's requests are copied out on `copy`, one event per request */
+    BatchNotify notify;
+    DevBuf notify_dev;        /* count[kMaxBatchJobs] | status[kMaxBatchJobs] */
+    uint32_t *h_flag = nullptr;
+    cudaStream_t copy = nullptr;
+    std::vector<cudaEvent_t> job_ev;
     void release()
     {
-        DevBuf *b[] = {&jobs, &small, &length, &path, &schemes};
+        DevBuf *b[] = {&jobs, &small, &length, &path, &schemes, &notify_dev};
         for (DevBuf *x : b)
             x->release();
+        if (copy)
+        {
+            cudaStreamSynchronize(copy);
+            cudaStreamDestroy(copy);
+        }
+        copy = nullptr;
+        for (cudaEvent_t ev_j : job_ev)
+            cudaEventDestroy(ev_j);
+        job_ev.clear();
+        if (h_flag)
+            cudaFreeHost(h_flag);
+        h_flag = nullptr;
+        notify = BatchNotify{};
         for (int i = 0; i < 3; i++)
             if (ev[i])
                 cudaEventDestroy(ev[i]);
@@ -543,6 +564,19 @@ uint64_t run_batch(kk_engine *e, BatchPlan &plan, BatchSlot &slot, bool want_pat
  * max_cap path vertices (batch_prepare must have run: the graph reads the
  * shared tables). */
 void batch_slot_graph_mode(kk_engine *e, BatchSlot &slot, uint32_t max_walkers, uint64_t max_cap);
+
+/* Gives a slot per-request completion (BatchNotify): each job of its batches
+ * raises its own flag, with its own status, as its last walker ends.  Call
+ * before the slot's first batch (a graph-mode slot captures the counters'
+ * reset with its launch). */
+void batch_slot_notify_mode(BatchSlot &slot);
+
+/* run_batch in two halves for a prepared engine: batch_launch_async queues
+ * the batch on the slot's stream (its end recorded in slot.ev[2]);
+ * batch_finish waits for it and returns the walker-steps.  With per-request
+ * completion, a failed walk is reported per job in its flag, not here. */
+void batch_launch_async(kk_engine *e, BatchPlan &plan, BatchSlot &slot);
+uint64_t batch_finish(kk_engine *e, BatchSlot &slot);
 
 /* Metapath schemes of one job as per-state type masks, checked. */
 inline apps::MetaSchemes make_schemes(const kk_walk_opts &o)

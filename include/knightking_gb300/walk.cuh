@@ -1781,6 +1781,10 @@ struct WalkLaunch
     uint32_t *seg_count = nullptr;
     volatile uint32_t *seg_flag = nullptr;
     uint32_t seg_shift = 0;
+    /* a segment's status word (batches of served requests: each request is a
+     * segment with its own status), reported in its flag as 1 + status;
+     * nullptr: the flag is 1 */
+    const int *seg_status = nullptr;
     /* parking (first-order walks with rejection trials): once fewer than
      * park_below of a warp's lanes are still walking, each of them stops at
      * its next step boundary and is appended to park (a ParkedWalker<S>
@@ -1812,7 +1816,9 @@ __device__ __forceinline__ void segment_done(const WalkLaunch &L, uint32_t i)
     if (L.seg_count == nullptr)
         return;
     const uint32_t s = i >> L.seg_shift;
-    const unsigned peers = __match_any_sync(__activemask(), s);
+    /* lanes of one warp may walk for different launches' segments (the jobs
+     * of a batch): they count together only on the same counter */
+    const unsigned peers = __match_any_sync(__activemask(), (unsigned long long)(L.seg_count + s));
     __syncwarp(peers);
     if ((int)(threadIdx.x & 31) != __ffs(peers) - 1)
         return;
@@ -1824,7 +1830,10 @@ __device__ __forceinline__ void segment_done(const WalkLaunch &L, uint32_t i)
     if (old + add == size)
     {
         asm volatile("fence.acq_rel.gpu;" ::: "memory");
-        asm volatile("st.relaxed.sys.u32 [%0], 1;" ::"l"(L.seg_flag + s) : "memory");
+        /* every walker of the segment released its status update before its
+         * count: the status word is final here */
+        const uint32_t f = L.seg_status != nullptr ? 1u + (uint32_t)*(const volatile int *)L.seg_status : 1u;
+        asm volatile("st.relaxed.sys.u32 [%0], %1;" ::"l"(L.seg_flag + s), "r"(f) : "memory");
     }
 }
 
@@ -2807,9 +2816,19 @@ struct BatchJob
     const void *param;     /* metapath: the job's schemes (device) */
 };
 
-/* One thread per walker over the concatenated walkers of all jobs; the job of
- * a walker by binary search over the jobs' first positions (shared memory).
- * App::make(job, wc, tc) builds the job's WalkerConfig / TransitionConfig. */
+/* Per-job completion of a batch (serving): the walkers of job j count
+ * themselves done on count[j], and the job's last walker writes flag[j] =
+ * 1 + status[j] in mapped host memory, status[j] being the job's own status
+ * word (its walkers' trial-limit and capacity failures), so the host hands
+ * each request out as soon as it is walked, with its own outcome.
+ * count == nullptr: the batch reports one status when it ends. */
+struct BatchNotify
+{
+    uint32_t *count = nullptr;
+    volatile uint32_t *flag = nullptr;
+    int *status = nullptr;
+};
+
 /* Walker t of a batch: its job (binary search over the jobs' first positions
  * in shared memory), the job's hooks and launch record, the walker started. */
 template <typename App>
@@ -2817,7 +2836,7 @@ __device__ __forceinline__ uint32_t batch_launch(const App &app, const BatchJob 
                                                  uint32_t njobs, uint32_t t, const float *alias_sum, uint32_t *path,
                                                  uint32_t *length, unsigned long long *total_steps, int *status,
                                                  uint32_t trial_limit, typename App::WC &wc, typename App::TC &tc,
-                                                 WalkLaunch &L)
+                                                 WalkLaunch &L, const BatchNotify &nt)
 {
     uint32_t lo = 0, hi = njobs;
     while (hi - lo > 1)
@@ -2844,6 +2863,15 @@ __device__ __forceinline__ uint32_t batch_launch(const App &app, const BatchJob 
     L.status = status;
     L.trial_limit = trial_limit;
     L.stats = nullptr;
+    if (nt.count != nullptr)
+    {
+        /* the job is one segment of its own */
+        L.seg_count = nt.count + lo;
+        L.seg_flag = nt.flag + lo;
+        L.seg_shift = 31;
+        L.status = nt.status + lo;
+        L.seg_status = nt.status + lo;
+    }
     return t - job.first_task;
 }
 
@@ -2855,10 +2883,10 @@ __device__ __forceinline__ uint32_t batch_walker_begin(const GraphView &g, const
                                                        unsigned long long *total_steps, int *status,
                                                        uint32_t trial_limit, typename App::WC &wc,
                                                        typename App::TC &tc, WalkLaunch &L, WalkerRun<S> &run,
-                                                       Sampler &rng)
+                                                       Sampler &rng, const BatchNotify &nt)
 {
     const uint32_t i = batch_launch(app, jobs, s_first, njobs, t, alias_sum, path, length, total_steps, status,
-                                    trial_limit, wc, tc, L);
+                                    trial_limit, wc, tc, L, nt);
     rng.init(L.seed);
     walk_begin<S>(g, wc, L, i, run, rng);
     return i;
@@ -2881,7 +2909,7 @@ __global__ void __launch_bounds__(256, KK_BATCH_MINB) walk_batch_kernel(GraphVie
                                                          const float *alias_sum, uint32_t *path, uint32_t *length,
                                                          unsigned long long *total_steps, int *status,
                                                          uint32_t trial_limit, unsigned long long *stats,
-                                                         const uint32_t *hdr, BatchPark bp)
+                                                         const uint32_t *hdr, BatchPark bp, BatchNotify nt)
 {
     __shared__ uint32_t s_first[kMaxBatchJobs];
     if (hdr != nullptr)
@@ -2916,7 +2944,7 @@ __global__ void __launch_bounds__(256, KK_BATCH_MINB) walk_batch_kernel(GraphVie
             uint32_t i = 0;
             if (alive)
                 i = batch_walker_begin<S>(g, app, jobs, s_first, njobs, t, alias_sum, path, length, total_steps,
-                                          status, trial_limit, wc, tc, L, run, rng);
+                                          status, trial_limit, wc, tc, L, run, rng, nt);
             walk_lanes<S>(g, wc, tc, alias, nullptr, L, alive, i, run, rng, my_steps, counts, t);
         }
         else if (t < total)
@@ -2927,11 +2955,12 @@ __global__ void __launch_bounds__(256, KK_BATCH_MINB) walk_batch_kernel(GraphVie
             WalkerRun<S> run;
             Sampler rng;
             const uint32_t i = batch_walker_begin<S>(g, app, jobs, s_first, njobs, t, alias_sum, path, length,
-                                                     total_steps, status, trial_limit, wc, tc, L, run, rng);
+                                                     total_steps, status, trial_limit, wc, tc, L, run, rng, nt);
             while (walk_trial<S>(g, wc, tc, alias, nullptr, L, run, rng))
             {
             }
             L.length[i] = run.len;
+            segment_done(L, i);
             my_steps += run.len - 1;
             counts.add(run);
         }
@@ -2979,7 +3008,7 @@ __global__ void __launch_bounds__(256, 4) walk_batch_resume_kernel(GraphView g, 
             const ParkedWalker<S> pw = in[k];
             t = pw.i;
             i = batch_launch(app, jobs, s_first, njobs, t, alias_sum, path, length, total_steps, status, trial_limit,
-                             wc, tc, L);
+                             wc, tc, L, BatchNotify{});
             rng.init(L.seed);
             resume_run<S>(L, i, pw, run);
         }
@@ -3000,7 +3029,8 @@ __global__ void __launch_bounds__(256, 4) walk_batch_pool_kernel(GraphView g, Ap
                                                               const float *alias_sum, uint32_t *path,
                                                               uint32_t *length, unsigned long long *total_steps,
                                                               int *status, uint32_t trial_limit,
-                                                              unsigned long long *stats, const uint32_t *hdr)
+                                                              unsigned long long *stats, const uint32_t *hdr,
+                                                              BatchNotify nt)
 {
     __shared__ uint32_t s_first[kMaxBatchJobs];
     __shared__ uint32_t s_next;
@@ -3028,19 +3058,20 @@ __global__ void __launch_bounds__(256, 4) walk_batch_pool_kernel(GraphView g, Ap
     bool have = t < hi;
     if (have)
         i = batch_walker_begin<S>(g, app, jobs, s_first, njobs, t, alias_sum, path, length, total_steps, status,
-                                  trial_limit, wc, tc, L, run, rng);
+                                  trial_limit, wc, tc, L, run, rng, nt);
     while (__any_sync(kFullMask, have))
     {
         if (have && !walk_trial<S>(g, wc, tc, alias, nullptr, L, run, rng))
         {
             L.length[i] = run.len;
+            segment_done(L, i);
             my_steps += run.len - 1;
             counts.add(run);
             t = atomicAdd(&s_next, 1u);
             have = t < hi;
             if (have)
                 i = batch_walker_begin<S>(g, app, jobs, s_first, njobs, t, alias_sum, path, length, total_steps,
-                                          status, trial_limit, wc, tc, L, run, rng);
+                                          status, trial_limit, wc, tc, L, run, rng, nt);
         }
     }
     flush_steps(total_steps, my_steps);

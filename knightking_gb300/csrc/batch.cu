@@ -139,7 +139,7 @@ void launch_batch_with(kk_engine *e, const App &app, const BatchPlan &plan, Batc
         }
         walk_batch_kernel<typename App::S, App, Bucket><<<grid, bs, 0, slot.stream>>>(
             gv, app, d_jobs, nj, plan.total, alias, (const float *)e->sum.p, *path, length, steps, status,
-            e->trial_limit, st, hdr, bp);
+            e->trial_limit, st, hdr, bp, slot.notify);
         count_launch(e);
         if (park)
         {
@@ -174,7 +174,7 @@ void launch_batch_with(kk_engine *e, const App &app, const BatchPlan &plan, Batc
         const unsigned grid = (unsigned)(want < need ? want : (need ? need : 1));
         walk_batch_pool_kernel<typename App::S, App, Bucket><<<grid, bs, 0, slot.stream>>>(
             gv, app, d_jobs, nj, plan.total, alias, (const float *)e->sum.p, *path, length, steps, status,
-            e->trial_limit, st, hdr);
+            e->trial_limit, st, hdr, slot.notify);
         count_launch(e);
     }
     KK_CUDA_CHECK(cudaGetLastError());
@@ -340,9 +340,32 @@ void batch_slot_graph_mode(kk_engine *e, BatchSlot &slot, uint32_t max_walkers, 
     (void)e;
 }
 
+void batch_slot_notify_mode(BatchSlot &slot)
+{
+    if (slot.notify.count != nullptr)
+        return;
+    uint32_t *d = slot.notify_dev.as<uint32_t>(2 * kMaxBatchJobs);
+    KK_CUDA_CHECK(cudaHostAlloc((void **)&slot.h_flag, kMaxBatchJobs * sizeof(uint32_t), cudaHostAllocMapped));
+    memset(slot.h_flag, 0, kMaxBatchJobs * sizeof(uint32_t));
+    uint32_t *d_flag = nullptr;
+    KK_CUDA_CHECK(cudaHostGetDevicePointer((void **)&d_flag, slot.h_flag, 0));
+    KK_CUDA_CHECK(cudaStreamCreateWithFlags(&slot.copy, cudaStreamNonBlocking));
+    slot.notify.count = d;
+    slot.notify.status = (int *)(d + kMaxBatchJobs);
+    slot.notify.flag = d_flag;
+}
+
+/* The per-request counters and status words start at zero for every batch. */
+static void reset_notify(const BatchSlot &slot)
+{
+    if (slot.notify.count != nullptr)
+        KK_CUDA_CHECK(cudaMemsetAsync(slot.notify.count, 0, 2 * kMaxBatchJobs * sizeof(uint32_t), slot.stream));
+}
+
 /* One graph-mode batch: stage the job table and counts, replay (capturing it
- * on first use) the slot's graph, read the status back. */
-static uint64_t run_batch_graph(kk_engine *e, BatchPlan &plan, BatchSlot &slot)
+ * on first use) the slot's graph; the status read-back lands in the staging
+ * block when the graph ends. */
+static void launch_batch_graph(kk_engine *e, BatchPlan &plan, BatchSlot &slot)
 {
     if (plan.total > slot.max_walkers || plan.total_cap > slot.max_cap)
         fail(KK_ERR_INVALID_CONFIG, "batch larger than the slot");
@@ -373,6 +396,7 @@ static uint64_t run_batch_graph(kk_engine *e, BatchPlan &plan, BatchSlot &slot)
                                               cudaMemcpyHostToDevice, slot.stream));
             KK_CUDA_CHECK(cudaMemcpyAsync((void *)d_hdr, h.hdr, 16, cudaMemcpyHostToDevice, slot.stream));
             KK_CUDA_CHECK(cudaMemsetAsync(d_status, 0, 64, slot.stream));
+            reset_notify(slot);
             uint32_t *path = nullptr;
             launch_app_batch(e, plan, slot, d_jobs, (uint32_t *)slot.length.p, &path, d_steps, d_status, true, true,
                              d_hdr);
@@ -393,6 +417,13 @@ static uint64_t run_batch_graph(kk_engine *e, BatchPlan &plan, BatchSlot &slot)
     KK_CUDA_CHECK(cudaEventRecord(slot.ev[1], slot.stream));
     KK_CUDA_CHECK(cudaGraphLaunch(slot.exec, slot.stream));
     KK_CUDA_CHECK(cudaEventRecord(slot.ev[2], slot.stream));
+}
+
+/* Waits for a graph-mode batch; its status (the batch's, or none with
+ * per-request completion) and walker-steps from the staging block. */
+static uint64_t finish_batch_graph(BatchSlot &slot)
+{
+    const GraphStage h = graph_stage(slot);
     KK_CUDA_CHECK(cudaStreamSynchronize(slot.stream));
     slot.alias_ms = 0.0f;
     KK_CUDA_CHECK(cudaEventElapsedTime(&slot.walk_ms, slot.ev[1], slot.ev[2]));
@@ -402,6 +433,64 @@ static uint64_t run_batch_graph(kk_engine *e, BatchPlan &plan, BatchSlot &slot)
         fail(KK_ERR_PATH_CAPACITY, "a walk exceeded its path capacity");
     unsigned long long steps;
     memcpy(&steps, (char *)h.status + 16, sizeof(steps));
+    return steps;
+}
+
+static uint64_t run_batch_graph(kk_engine *e, BatchPlan &plan, BatchSlot &slot)
+{
+    launch_batch_graph(e, plan, slot);
+    return finish_batch_graph(slot);
+}
+
+void batch_launch_async(kk_engine *e, BatchPlan &plan, BatchSlot &slot)
+{
+    if (slot.graph_mode)
+    {
+        launch_batch_graph(e, plan, slot);
+        return;
+    }
+    for (int i = 0; i < 3; i++)
+        if (slot.ev[i] == nullptr)
+            KK_CUDA_CHECK(cudaEventCreate(&slot.ev[i]));
+    if (plan.app == KK_APP_METAPATH)
+    {
+        MetaSchemes *d_sc = slot.schemes.as<MetaSchemes>(plan.schemes.size());
+        KK_CUDA_CHECK(cudaMemcpyAsync(d_sc, plan.schemes.data(), plan.schemes.size() * sizeof(MetaSchemes),
+                                      cudaMemcpyHostToDevice, slot.stream));
+        for (size_t j = 0; j < plan.jobs.size(); j++)
+            plan.jobs[j].param = d_sc + j;
+    }
+    BatchJob *d_jobs = slot.jobs.as<BatchJob>(plan.jobs.size());
+    KK_CUDA_CHECK(cudaMemcpyAsync(d_jobs, plan.jobs.data(), plan.jobs.size() * sizeof(BatchJob),
+                                  cudaMemcpyHostToDevice, slot.stream));
+    int *d_status = (int *)slot.small.ensure(64);
+    unsigned long long *d_steps = (unsigned long long *)((char *)d_status + 16);
+    KK_CUDA_CHECK(cudaMemsetAsync(d_status, 0, 64, slot.stream));
+    reset_notify(slot);
+    KK_CUDA_CHECK(cudaEventRecord(slot.ev[0], slot.stream));
+    KK_CUDA_CHECK(cudaEventRecord(slot.ev[1], slot.stream));
+    uint32_t *length = slot.length.as<uint32_t>(plan.total);
+    uint32_t *path = nullptr;
+    launch_app_batch(e, plan, slot, d_jobs, length, &path, d_steps, d_status, true, true, nullptr);
+    KK_CUDA_CHECK(cudaEventRecord(slot.ev[2], slot.stream));
+}
+
+uint64_t batch_finish(kk_engine *e, BatchSlot &slot)
+{
+    (void)e;
+    if (slot.graph_mode)
+        return finish_batch_graph(slot);
+    KK_CUDA_CHECK(cudaStreamSynchronize(slot.stream));
+    int h_small[16];
+    KK_CUDA_CHECK(cudaMemcpy(h_small, slot.small.p, sizeof(h_small), cudaMemcpyDeviceToHost));
+    KK_CUDA_CHECK(cudaEventElapsedTime(&slot.alias_ms, slot.ev[0], slot.ev[1]));
+    KK_CUDA_CHECK(cudaEventElapsedTime(&slot.walk_ms, slot.ev[1], slot.ev[2]));
+    if (h_small[0] & KK_STATUS_TRIAL_LIMIT)
+        fail(KK_ERR_TRIAL_LIMIT, "a walker exceeded the rejection-trial limit");
+    if (h_small[0] & KK_STATUS_PATH_CAPACITY)
+        fail(KK_ERR_PATH_CAPACITY, "a walk exceeded its path capacity");
+    unsigned long long steps;
+    memcpy(&steps, (char *)h_small + 16, sizeof(steps));
     return steps;
 }
 

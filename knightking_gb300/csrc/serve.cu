@@ -52,10 +52,11 @@ uint64_t request_bytes(const kk_walk_opts &o)
     return (uint64_t)o.walker_num * (((uint64_t)o.walk_length + 1) * 4 + 4);
 }
 
-/* One job's paths from a finished batch, in a pooled pinned block: lengths,
- * offsets (walker i at i * (walk_length + 1)) and the vertices, copied
- * straight from the slot's path buffer (asynchronously on the slot's stream). */
-kk_paths *job_paths(HostPool *pool, const BatchJob &b, const uint32_t *h_len_all, const uint32_t *d_path,
+/* One job's paths in a pooled pinned block: lengths and vertices copied
+ * straight from the slot's buffers on stream st (asynchronously: the caller
+ * waits for st before reading them), offsets i * (walk_length + 1) written
+ * here.  total_steps is set once the lengths have arrived (finish_paths). */
+kk_paths *job_paths(HostPool *pool, const BatchJob &b, const uint32_t *d_len_all, const uint32_t *d_path,
                     cudaStream_t st)
 {
     const uint32_t n = b.walker_num;
@@ -82,18 +83,14 @@ kk_paths *job_paths(HostPool *pool, const BatchJob &b, const uint32_t *h_len_all
     p->length = (uint32_t *)blk;
     p->offset = (uint64_t *)(blk + len_bytes);
     p->vertices = (uint32_t *)(blk + len_bytes + off_bytes);
-    uint64_t total = 0;
     for (uint32_t i = 0; i < n; i++)
-    {
-        p->length[i] = h_len_all[b.first_task + i];
         p->offset[i] = (uint64_t)i * b.cap;
-        total += p->length[i];
-    }
-    p->total_steps = total - n;
     if (n != 0)
     {
-        const cudaError_t err = cudaMemcpyAsync(p->vertices, d_path + b.path_base, vert_bytes,
-                                                cudaMemcpyDeviceToHost, st);
+        cudaError_t err = cudaMemcpyAsync(p->length, d_len_all + b.first_task, (size_t)n * 4,
+                                          cudaMemcpyDeviceToHost, st);
+        if (err == cudaSuccess)
+            err = cudaMemcpyAsync(p->vertices, d_path + b.path_base, vert_bytes, cudaMemcpyDeviceToHost, st);
         if (err != cudaSuccess)
         {
             kk_paths_free(p);
@@ -101,6 +98,25 @@ kk_paths *job_paths(HostPool *pool, const BatchJob &b, const uint32_t *h_len_all
         }
     }
     return p;
+}
+
+/* A job's paths once their copies are done: the walker-steps from the lengths. */
+void finish_paths(kk_paths *p)
+{
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < p->walker_num; i++)
+        total += p->length[i];
+    p->total_steps = total - p->walker_num;
+}
+
+/* The status of a request from its walkers' status word. */
+kk_status job_status_of(uint32_t word)
+{
+    if (word & KK_STATUS_TRIAL_LIMIT)
+        return KK_ERR_TRIAL_LIMIT;
+    if (word & KK_STATUS_PATH_CAPACITY)
+        return KK_ERR_PATH_CAPACITY;
+    return word ? KK_ERR_CUDA : KK_OK;
 }
 
 } // namespace
@@ -129,7 +145,33 @@ struct kk_server
 namespace
 {
 
-/* One slot's loop: take a batch of queued requests, run it, hand out results. */
+/* Hands request j of a batch out (the caller holds s->m). */
+void hand_out(kk_server *s, const Request &r, kk_status st, kk_paths *paths, Clock::time_point t_launch,
+              Clock::time_point t_done, size_t n)
+{
+    kk_serve_result res;
+    res.status = st;
+    res.paths = st == KK_OK ? paths : nullptr;
+    res.queue_ms = ms_between(r.t_submit, t_launch);
+    res.latency_ms = ms_between(r.t_submit, t_done);
+    res.batch_jobs = (uint32_t)n;
+    s->done[r.ticket] = res;
+    if (st == KK_OK)
+    {
+        s->completed++;
+        s->latencies.push_back(res.latency_ms);
+    }
+    else
+    {
+        kk_paths_free(paths);
+        s->failed++;
+    }
+}
+
+/* One slot's loop: take a batch of queued requests, launch it, and hand each
+ * request out as soon as its own walkers have ended (its flag, raised by the
+ * last of them with the request's status) and its paths have reached pinned
+ * host memory, while the rest of the batch is still walking. */
 void slot_loop(kk_server *s, int k)
 {
     cudaSetDevice(s->e->device);
@@ -159,23 +201,99 @@ void slot_loop(kk_server *s, int k)
         for (size_t j = 0; j < n; j++)
             jobs[j] = batch[j].opts;
         std::vector<kk_paths *> paths(n, nullptr);
+        std::vector<kk_status> job_st(n, KK_OK);
+        std::vector<char> handed(n, 0);
         kk_status st = KK_OK;
         uint64_t steps = 0;
         Clock::time_point t_walked = t_launch, t_copied = t_launch;
         try
         {
             BatchPlan plan = plan_batch(s->e, jobs.data(), (int)n);
-            steps = run_batch(s->e, plan, slot, true, true);
-            t_walked = Clock::now();
-            std::vector<uint32_t> h_len(plan.total + 1);
-            KK_CUDA_CHECK(cudaMemcpyAsync(h_len.data(), slot.length.p, (size_t)plan.total * 4,
-                                          cudaMemcpyDeviceToHost, slot.stream));
-            KK_CUDA_CHECK(cudaStreamSynchronize(slot.stream));
+            while (slot.job_ev.size() < n)
+            {
+                cudaEvent_t ev_j = nullptr;
+                KK_CUDA_CHECK(cudaEventCreateWithFlags(&ev_j, cudaEventDisableTiming));
+                slot.job_ev.push_back(ev_j);
+            }
+            /* the slot's previous batch has ended: no walker writes a flag */
+            volatile uint32_t *flag = slot.h_flag;
             for (size_t j = 0; j < n; j++)
-                paths[j] = job_paths(s->pool, plan.jobs[j], h_len.data(), (const uint32_t *)slot.path.p,
-                                     slot.stream);
-            KK_CUDA_CHECK(cudaStreamSynchronize(slot.stream));
+                flag[j] = 0;
+            batch_launch_async(s->e, plan, slot);
+            std::vector<uint32_t> order; /* requests in the order their copies were issued */
+            order.reserve(n);
+            size_t fin = 0;
+            bool walked = false;
+            while (fin < n)
+            {
+                if (!walked)
+                {
+                    const cudaError_t q = cudaEventQuery(slot.ev[2]);
+                    if (q == cudaSuccess)
+                    {
+                        walked = true;
+                        t_walked = Clock::now();
+                    }
+                    else if (q != cudaErrorNotReady)
+                    {
+                        KK_CUDA_CHECK(q);
+                    }
+                }
+                for (size_t j = 0; j < n && order.size() < n; j++)
+                {
+                    if (paths[j] != nullptr || handed[j])
+                        continue;
+                    /* a request of no walkers has nothing to walk */
+                    const uint32_t f = plan.jobs[j].walker_num == 0 ? 1u : flag[j];
+                    if (f == 0)
+                    {
+                        /* the batch has ended and visibly so: a request whose
+                         * walkers never all counted themselves done */
+                        if (walked && flag[j] == 0)
+                            fail(KK_ERR_CUDA, "a request of the batch did not complete");
+                        continue;
+                    }
+                    job_st[j] = job_status_of(f - 1);
+                    paths[j] = job_paths(s->pool, plan.jobs[j], (const uint32_t *)slot.length.p,
+                                         (const uint32_t *)slot.path.p, slot.copy);
+                    KK_CUDA_CHECK(cudaEventRecord(slot.job_ev[j], slot.copy));
+                    order.push_back((uint32_t)j);
+                }
+                /* the requests whose copies are done, in issue order */
+                size_t ready = fin;
+                while (ready < order.size())
+                {
+                    const cudaError_t q = cudaEventQuery(slot.job_ev[order[ready]]);
+                    if (q == cudaErrorNotReady)
+                        break;
+                    KK_CUDA_CHECK(q);
+                    ready++;
+                }
+                if (ready > fin)
+                {
+                    const Clock::time_point t_done = Clock::now();
+                    for (size_t x = fin; x < ready; x++)
+                        finish_paths(paths[order[x]]);
+                    {
+                        std::lock_guard<std::mutex> lk(s->m);
+                        for (size_t x = fin; x < ready; x++)
+                        {
+                            const uint32_t j = order[x];
+                            hand_out(s, batch[j], job_st[j], paths[j], t_launch, t_done, n);
+                            handed[j] = 1;
+                            paths[j] = nullptr;
+                        }
+                    }
+                    s->cv_done.notify_all();
+                    fin = ready;
+                }
+                else
+                {
+                    std::this_thread::yield();
+                }
+            }
             t_copied = Clock::now();
+            steps = batch_finish(s->e, slot);
         }
         catch (const Error &x)
         {
@@ -190,33 +308,18 @@ void slot_loop(kk_server *s, int k)
             st = KK_ERR_CUDA;
         }
         if (st != KK_OK)
-            for (size_t j = 0; j < n; j++)
-            {
-                kk_paths_free(paths[j]);
-                paths[j] = nullptr;
-            }
+        {
+            /* copies in flight land in blocks about to go back to the pool */
+            if (slot.copy)
+                cudaStreamSynchronize(slot.copy);
+            cudaStreamSynchronize(slot.stream);
+        }
         const Clock::time_point t_done = Clock::now();
         {
             std::lock_guard<std::mutex> lk(s->m);
             for (size_t j = 0; j < n; j++)
-            {
-                kk_serve_result r;
-                r.status = st;
-                r.paths = paths[j];
-                r.queue_ms = ms_between(batch[j].t_submit, t_launch);
-                r.latency_ms = ms_between(batch[j].t_submit, t_done);
-                r.batch_jobs = (uint32_t)n;
-                s->done[batch[j].ticket] = r;
-                if (st == KK_OK)
-                {
-                    s->completed++;
-                    s->latencies.push_back(r.latency_ms);
-                }
-                else
-                {
-                    s->failed++;
-                }
-            }
+                if (!handed[j])
+                    hand_out(s, batch[j], st, paths[j], t_launch, t_done, n);
             s->batches++;
             s->batch_jobs_sum += n;
             s->steps += steps;
@@ -274,6 +377,7 @@ kk_status kk_serve_start(kk_engine *e, const kk_serve_opts *opts, kk_server **ou
             if (o.launch_mode == 0)
                 batch_slot_graph_mode(e, s->slots[k], (uint32_t)std::min<uint64_t>(o.slot_bytes / 8, 0x80000000ull),
                                       o.slot_bytes / 4);
+            batch_slot_notify_mode(s->slots[k]);
         }
         s->pool = new HostPool();
         s->pool->limit = (size_t)o.slots * 2 * o.slot_bytes;

@@ -137,3 +137,39 @@ def test_replay_client_keeps_schedule_and_counts_every_step(engine):
         # the server still serves after the refused request
         lat, steps, _ = srv.replay(reqs[:4], np.zeros(4))
         assert np.all(lat > 0)
+
+
+@pytest.mark.parametrize("graphs", [True, False])
+def test_failed_request_fails_alone(engine, oracle_lib, graphs):
+    """Each request of a batch is handed out with its own outcome as soon as
+    its own walkers end: with a trial limit of 1, requests whose scheme
+    allows one edge type per step (most steps need more trials) fail with
+    KK_ERR_TRIAL_LIMIT, while the requests that shared their batches, whose
+    scheme allows every type (every trial accepted), come back with the
+    oracle's paths."""
+    csr = _load(engine, 14, types=True)
+    good = [dict(walker_num=40 + i, seed=100 + i, walk_length=12 + i, walker_begin=50 * i, schemes=[[31, 31, 31]])
+            for i in range(24)]
+    bad = [dict(walker_num=30 + i, seed=300 + i, walk_length=15, walker_begin=2000 + 50 * i, schemes=[[1], [2]])
+           for i in range(8)]
+    reqs = []
+    for i in range(8):
+        reqs += good[3 * i:3 * i + 3] + [bad[i]]
+    engine.set_option("trial_limit", 1)
+    try:
+        results, stats = _serve_all(engine, "metapath", reqs, clients=2, slots=2, max_jobs=16,
+                                    slot_bytes=8 << 20, graphs=graphs)
+    finally:
+        engine.set_option("trial_limit", 1 << 24)
+    assert stats["completed"] == len(good) and stats["failed"] == len(bad)
+    for r, res in zip(reqs, results):
+        if r["schemes"] == [[1], [2]]:
+            assert res.status == 4 and res.paths is None  # KK_ERR_TRIAL_LIMIT
+        else:
+            assert res.status == 0
+            lens, verts, steps = _oracle(oracle_lib, csr, "metapath", r)
+            np.testing.assert_array_equal(res.paths.path_length, lens)
+            np.testing.assert_array_equal(res.paths.vertices, verts)
+    # the server's engine serves again at the usual limit
+    results, stats = _serve_all(engine, "metapath", bad[:2], clients=1, slots=1, max_jobs=4, slot_bytes=8 << 20)
+    assert all(res.status == 0 for res in results)

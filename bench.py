@@ -477,7 +477,7 @@ def n2v_outlier(p, q):
     return float(np.float32(1.0 / float(np.float32(p)) - float(ub))) > 0.0
 
 
-SERVE_JOB_BYTES = 72  # one BatchJob record (walk.cuh), uploaded per job slot of a batch
+SERVE_JOB_BYTES = 80  # one BatchJob record (walk.cuh), uploaded per job slot of a batch
 LATENCY_LOADS = (0.3, 0.5, 0.7)  # open-loop offered load, fraction of the saturated served rate
 LATENCY_HEAD = 0.5  # the load of the line's headline p50/p99
 

@@ -536,8 +536,11 @@ struct BatchPlan
     bool weighted = false;
 };
 
-/* Checks the jobs and lays out the batch (fails on mixed apps or weighting). */
-BatchPlan plan_batch(kk_engine *e, const kk_walk_opts *jobs, int n);
+/* Checks the jobs and lays out the batch (fails on mixed apps or weighting).
+ * longest_first: the launch takes the jobs longest walk first (the shortest
+ * makespan for a batch whose results are used together); else in job order
+ * (served requests, each handed out as it ends). */
+BatchPlan plan_batch(kk_engine *e, const kk_walk_opts *jobs, int n, bool longest_first = true);
 
 /* Packs a finished batch's paths (job j's walker i at path[path_base_j + i *
  * cap_j], its length at length[first_task_j + i]; d_jobs the job table on the

@@ -2813,7 +2813,12 @@ struct BatchJob
     uint32_t walk_length;
     int32_t flag;          /* metapath: round-robin scheme assignment */
     float c[5];            /* node2vec: upperbound, lowerbound, overflow, 1/p, 1/q */
+    /* the launch order: the walkers of the launch's k-th job (the jobs by
+     * walk length, longest first) are the launch's walkers launch_first
+     * onwards of entry k, and that job is entry launch_job of this table */
+    uint32_t launch_first;
     const void *param;     /* metapath: the job's schemes (device) */
+    uint32_t launch_job;
 };
 
 /* Per-job completion of a batch (serving): the walkers of job j count
@@ -2838,15 +2843,18 @@ __device__ __forceinline__ uint32_t batch_launch(const App &app, const BatchJob 
                                                  uint32_t trial_limit, typename App::WC &wc, typename App::TC &tc,
                                                  WalkLaunch &L, const BatchNotify &nt)
 {
-    uint32_t lo = 0, hi = njobs;
-    while (hi - lo > 1)
+    /* s_first: the launch order's first walkers, then the table entry of
+     * each (kMaxBatchJobs on) */
+    uint32_t k = 0, hi = njobs;
+    while (hi - k > 1)
     {
-        const uint32_t mid = (lo + hi) >> 1;
+        const uint32_t mid = (k + hi) >> 1;
         if (s_first[mid] <= t)
-            lo = mid;
+            k = mid;
         else
             hi = mid;
     }
+    const uint32_t lo = s_first[kMaxBatchJobs + k];
     const BatchJob job = jobs[lo];
     app.make(job, wc, tc);
     L.seed = job.seed;
@@ -2872,7 +2880,7 @@ __device__ __forceinline__ uint32_t batch_launch(const App &app, const BatchJob 
         L.status = nt.status + lo;
         L.seg_status = nt.status + lo;
     }
-    return t - job.first_task;
+    return t - s_first[k];
 }
 
 /* Walker t of a batch started: its job, hooks and launch record, then its walk. */
@@ -2911,7 +2919,7 @@ __global__ void __launch_bounds__(256, KK_BATCH_MINB) walk_batch_kernel(GraphVie
                                                          uint32_t trial_limit, unsigned long long *stats,
                                                          const uint32_t *hdr, BatchPark bp, BatchNotify nt)
 {
-    __shared__ uint32_t s_first[kMaxBatchJobs];
+    __shared__ uint32_t s_first[2 * kMaxBatchJobs];
     if (hdr != nullptr)
     {
         /* counts from device memory: one captured launch serves every batch */
@@ -2919,7 +2927,10 @@ __global__ void __launch_bounds__(256, KK_BATCH_MINB) walk_batch_kernel(GraphVie
         total = hdr[1];
     }
     for (uint32_t j = threadIdx.x; j < njobs; j += blockDim.x)
-        s_first[j] = jobs[j].first_task;
+    {
+        s_first[j] = jobs[j].launch_first;
+        s_first[kMaxBatchJobs + j] = jobs[j].launch_job;
+    }
     __syncthreads();
     unsigned long long my_steps = 0;
     WalkCounts counts;
@@ -2983,9 +2994,12 @@ __global__ void __launch_bounds__(256, 4) walk_batch_resume_kernel(GraphView g, 
                                                                 const ParkedWalker<S> *in, const uint32_t *in_count,
                                                                 BatchPark bp)
 {
-    __shared__ uint32_t s_first[kMaxBatchJobs];
+    __shared__ uint32_t s_first[2 * kMaxBatchJobs];
     for (uint32_t j = threadIdx.x; j < njobs; j += blockDim.x)
-        s_first[j] = jobs[j].first_task;
+    {
+        s_first[j] = jobs[j].launch_first;
+        s_first[kMaxBatchJobs + j] = jobs[j].launch_job;
+    }
     __syncthreads();
     unsigned long long my_steps = 0;
     WalkCounts counts;
@@ -3032,7 +3046,7 @@ __global__ void __launch_bounds__(256, 4) walk_batch_pool_kernel(GraphView g, Ap
                                                               unsigned long long *stats, const uint32_t *hdr,
                                                               BatchNotify nt)
 {
-    __shared__ uint32_t s_first[kMaxBatchJobs];
+    __shared__ uint32_t s_first[2 * kMaxBatchJobs];
     __shared__ uint32_t s_next;
     if (hdr != nullptr)
     {
@@ -3040,7 +3054,10 @@ __global__ void __launch_bounds__(256, 4) walk_batch_pool_kernel(GraphView g, Ap
         total = hdr[1];
     }
     for (uint32_t j = threadIdx.x; j < njobs; j += blockDim.x)
-        s_first[j] = jobs[j].first_task;
+    {
+        s_first[j] = jobs[j].launch_first;
+        s_first[kMaxBatchJobs + j] = jobs[j].launch_job;
+    }
     const uint32_t per = (uint32_t)(((uint64_t)total + gridDim.x - 1) / gridDim.x);
     const uint32_t lo = (uint32_t)min((uint64_t)blockIdx.x * per, (uint64_t)total);
     const uint32_t hi = (uint32_t)min((uint64_t)lo + per, (uint64_t)total);

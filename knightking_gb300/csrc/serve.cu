@@ -208,7 +208,9 @@ void slot_loop(kk_server *s, int k)
         Clock::time_point t_walked = t_launch, t_copied = t_launch;
         try
         {
-            BatchPlan plan = plan_batch(s->e, jobs.data(), (int)n);
+            /* in arrival order: a request is handed out as soon as it ends,
+             * and the long ones of the batch need not all start first */
+            BatchPlan plan = plan_batch(s->e, jobs.data(), (int)n, false);
             while (slot.job_ev.size() < n)
             {
                 cudaEvent_t ev_j = nullptr;

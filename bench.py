@@ -490,11 +490,11 @@ def run_serve_bench(args, wl, world, rank, local):
              requests per launch, paths in HBM), CUDA events on the engine's
              stream; the plain one-launch-per-request kernel is timed beside it.
     e2e    : K passes through the serving API (kk_serve_submit / kk_serve_poll
-             from kk_serve_replay, the library's client): every request of a
-             pass submitted at once, its job record copied to the device and
-             its paths copied back into pinned host memory; submit of the
-             first -> paths of the last on the host.  One pass driven request
-             by request from Python is reported beside it.
+             from kk_serve_replay, the library's client): the K passes' requests
+             submitted at once as one stream, each job record copied to the
+             device and its paths copied back into pinned host memory; submit
+             of the first -> paths of the last on the host.  One pass driven
+             request by request from Python is reported beside it.
     latency: open-loop Poisson streams at 30%, 50% and 70% of the saturated
              rate, p50/p99 of submit -> paths on the host.
     parity : the first requests' served paths (and their kk_batch_walk paths)
@@ -568,12 +568,10 @@ def run_serve_bench(args, wl, world, rank, local):
         # pass submitted at once by the library's own client (kk_serve_replay:
         # kk_serve_submit from one host thread, kk_serve_poll and
         # kk_paths_free of every result from another)
+        # the K passes go in as one stream (K x 3000 requests, all at once),
+        # so the server stays saturated across pass boundaries
         srv.reset_stats()
-        s_steps, s_s = 0, 0.0
-        for _ in range(args.steps):
-            _, st_k, el_k = srv.replay(reqs, np.zeros(len(reqs)))
-            s_steps += st_k
-            s_s += el_k
+        _, s_steps, s_s = srv.replay(reqs * args.steps, np.zeros(len(reqs) * args.steps))
         sat = srv.stats()
         # one pass driven from Python (submit and poll per request through ctypes)
         t0 = time.perf_counter()
@@ -696,8 +694,8 @@ def run_serve_bench(args, wl, world, rank, local):
                           "what": "one launch per request, alias tables rebuilt per call (as the reference's "
                                   "random_walk does)"},
         "served": {"value": served_value, "unit": "walker-steps/s",
-                   "what": "kk_serve_*, every request of a pass submitted at once; submit -> paths on the host "
-                           "(the line's e2e)",
+                   "what": "kk_serve_*, the K passes' requests submitted at once as one stream; submit -> paths "
+                           "on the host (the line's e2e)",
                    "client": "kk_serve_replay (the library's client: submit from one host thread, poll and "
                              "free from another)",
                    "python_client": {"value": py_steps / py_s, "unit": "walker-steps/s",

@@ -173,3 +173,19 @@ def test_failed_request_fails_alone(engine, oracle_lib, graphs):
     # the server's engine serves again at the usual limit
     results, stats = _serve_all(engine, "metapath", bad[:2], clients=1, slots=1, max_jobs=4, slot_bytes=8 << 20)
     assert all(res.status == 0 for res in results)
+
+
+def test_request_of_no_walkers_is_served(engine):
+    """A request of zero walkers shares a batch with others and comes back at
+    once, empty; the others keep their paths."""
+    _load(engine, 15)
+    reqs = _requests("node2vec", 12, seed=21)
+    reqs.insert(5, dict(walker_num=0, seed=7, walk_length=30, walker_begin=3, p=1.0, q=2.0))
+    results, stats = _serve_all(engine, "node2vec", reqs, clients=1, slots=1, max_jobs=32, slot_bytes=8 << 20)
+    assert stats["completed"] == len(reqs) and stats["failed"] == 0
+    assert results[5].status == 0 and results[5].paths.path_num == 0
+    for r, res in zip(reqs, results):
+        if r["walker_num"]:
+            kw = dict(r)
+            alone = engine.walk("node2vec", kw.pop("walker_num"), **kw)
+            np.testing.assert_array_equal(res.paths.vertices, alone.vertices)

@@ -236,7 +236,16 @@ class WalkEngine:
                 walk_conf.output_consumer_func(paths)
         return paths
 
+    def job_table(self, app, jobs):
+        """The kk_walk_opts array of a batch, built once (batch_walk_device and
+        batch_walk take it in place of the list of job dicts)."""
+        return JobTable(app, *self._job_array(app, jobs))
+
     def _job_array(self, app, jobs):
+        if isinstance(jobs, JobTable):
+            if jobs.app != app:
+                raise ValueError("job table built for another app")
+            return jobs.arr, jobs.keep
         arr = (_capi.KKWalkOpts * len(jobs))()
         keep = []
         for i, job in enumerate(jobs):
@@ -283,10 +292,12 @@ class WalkEngine:
                                                    ctypes.byref(dv) if paths else None))
         return steps.value
 
-    def walk_device(self, app, walker_num, paths=True, **kw):
+    def walk_device(self, app, walker_num, paths=True, opts=None, **kw):
         """Walk with results left in HBM; returns (total_steps, d_length, d_offset, d_vertices) pointers.
-        paths: True packed, "unpacked" as the walk wrote them (no compaction pass), False not stored."""
-        opts = self.make_opts(app, walker_num, **kw)
+        paths: True packed, "unpacked" as the walk wrote them (no compaction pass), False not stored.
+        opts: a kk_walk_opts from make_opts, used as it is (walker_num and kw are then ignored)."""
+        if opts is None:
+            opts = self.make_opts(app, walker_num, **kw)
         steps = ctypes.c_uint64()
         dl = ctypes.c_void_p()
         do = ctypes.c_void_p()
@@ -421,6 +432,18 @@ class ServeResult:
         self.queue_ms = queue_ms
         self.latency_ms = latency_ms
         self.batch_jobs = batch_jobs
+
+
+class JobTable:
+    """A batch's job records in the C-ABI's layout (WalkEngine.job_table)."""
+
+    def __init__(self, app, arr, keep):
+        self.app = app
+        self.arr = arr
+        self.keep = keep
+
+    def __len__(self):
+        return len(self.arr)
 
 
 class Server:

@@ -255,6 +255,17 @@ kk_status kk_walk_device(kk_engine *e, const kk_walk_opts *opts, uint64_t *total
  * start list and no epochs.  out[j] receives job j's paths (kk_paths_free each). */
 kk_status kk_batch_walk(kk_engine *e, const kk_walk_opts *jobs, int n_jobs, kk_paths **out);
 
+/* The same batch without waiting: kk_batch_submit checks the jobs, builds
+ * what the walk reads and queues the batch on the engine's stream, then
+ * returns; kk_batch_wait waits for it and hands out out[j] for job j (as
+ * kk_batch_walk does) and frees the handle.  The calling thread is free
+ * meanwhile.  Until the wait, the engine takes no other call
+ * (KK_ERR_INVALID_CONFIG); destroy the engine only after the wait.  No
+ * counterpart in the reference, whose random_walk() call blocks. */
+typedef struct kk_batch kk_batch;
+kk_status kk_batch_submit(kk_engine *e, const kk_walk_opts *jobs, int n_jobs, kk_batch **out);
+kk_status kk_batch_wait(kk_batch *b, kk_paths **out);
+
 /* Same with paths left in HBM in the batch layout (job after job, walker i of a
  * job at i * (walk_length + 1)); valid until the next walk call. */
 kk_status kk_batch_walk_device(kk_engine *e, const kk_walk_opts *jobs, int n_jobs, uint64_t *total_steps,

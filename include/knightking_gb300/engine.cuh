@@ -393,6 +393,9 @@ struct kk_engine
     /* walk_stats (option): count trials, queries and binary-search probes of
      * the walks (kk_last_walk_stats) */
     int walk_stats = 0;
+    /* kk_batch_submit: a batch is on the engine's batch slot until
+     * kk_batch_wait (batch_wait: the wait itself is running) */
+    bool batch_out = false, batch_wait = false;
     uint64_t last_stats[3] = {0, 0, 0};
     /* alias-table layout: 0 cursor buckets where the hooks allow them, 1 index
      * buckets always, 2 (default) 16 B neighbour buckets where the hooks allow
@@ -451,7 +454,11 @@ kk_status guard(kk_engine *e, F f)
     try
     {
         if (e)
+        {
             e->err.clear();
+            if (e->batch_out && !e->batch_wait)
+                fail(KK_ERR_INVALID_CONFIG, "a submitted batch is outstanding (kk_batch_wait first)");
+        }
         f();
         return KK_OK;
     }

@@ -282,6 +282,15 @@ class WalkEngine:
                     self._lib.kk_paths_free(p)
         return res
 
+    def batch_submit(self, app, jobs):
+        """kk_batch_submit: queues the batch and returns at once; the returned
+        handle's wait() gives what batch_walk would have returned.  The engine
+        takes no other call until then."""
+        arr, keep = self._job_array(app, jobs)
+        h = ctypes.c_void_p()
+        self._check(self._lib.kk_batch_submit(self._h, arr, len(jobs), ctypes.byref(h)))
+        return SubmittedBatch(self, h, len(jobs), keep)
+
     def batch_walk_device(self, app, jobs, paths=True):
         """kk_batch_walk_device: paths stay in HBM; returns the total walker-steps."""
         arr, keep = self._job_array(app, jobs)
@@ -432,6 +441,36 @@ class ServeResult:
         self.queue_ms = queue_ms
         self.latency_ms = latency_ms
         self.batch_jobs = batch_jobs
+
+
+class SubmittedBatch:
+    """A batch queued by WalkEngine.batch_submit."""
+
+    def __init__(self, engine, handle, n, keep):
+        self._engine = engine
+        self._h = handle
+        self._n = n
+        self._keep = keep
+
+    def wait(self):
+        """kk_batch_wait: one PathSet per job, in job order."""
+        if self._h is None:
+            raise ValueError("batch already waited for")
+        lib = self._engine._lib
+        outs = (ctypes.POINTER(_capi.KKPaths) * self._n)()
+        st = lib.kk_batch_wait(self._h, outs)
+        self._h = None
+        self._engine._check(st)
+        res, owned = [], [False] * self._n
+        try:
+            for k, p in enumerate(outs):
+                res.append(PathSet(*_capi.paths_to_numpy_owned(p)))
+                owned[k] = True
+        finally:
+            for k, p in enumerate(outs):
+                if p and not owned[k]:
+                    lib.kk_paths_free(p)
+        return res
 
 
 class JobTable:

@@ -137,6 +137,8 @@ _SIGS = {
     "kk_walk_into": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.c_uint64, _P]),
     "kk_batch_walk": (ctypes.c_int, [_P, _P, ctypes.c_int, _P]),
     "kk_batch_walk_device": (ctypes.c_int, [_P, _P, ctypes.c_int, _P, _P, _P]),
+    "kk_batch_submit": (ctypes.c_int, [_P, _P, ctypes.c_int, _P]),
+    "kk_batch_wait": (ctypes.c_int, [_P, _P]),
     "kk_walk_device": (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
     "kk_last_walk_timing": (ctypes.c_int, [_P, _P, _P]),
     "kk_engine_launch_count": (ctypes.c_int, [_P, _P]),

@@ -595,19 +595,18 @@ kk_status kk_batch_walk_device(kk_engine *e, const kk_walk_opts *jobs, int n_job
     });
 }
 
-kk_status kk_batch_walk(kk_engine *e, const kk_walk_opts *jobs, int n_jobs, kk_paths **out)
+} /* extern "C" */
+
+namespace
 {
-    if (!e || !out)
-        return KK_ERR_INVALID_CONFIG;
-    for (int j = 0; j < n_jobs; j++)
-        out[j] = nullptr;
-    kk_status s = guard(e, [&] {
-        BatchPlan plan = plan_batch(e, jobs, n_jobs);
-        BatchSlot &slot = e->bslot;
-        slot.stream = e->stream;
-        run_batch(e, plan, slot, true, false);
-        e->alias_ms = slot.alias_ms;
-        e->walk_ms = slot.walk_ms;
+
+/* A walked batch's paths out: all jobs packed in one pass, then every job's
+ * lengths, offsets and vertices copied straight into a pooled pinned block,
+ * one wait. */
+void batch_paths_out(kk_engine *e, const BatchPlan &plan, BatchSlot &slot, kk_paths **out)
+{
+    const int n_jobs = (int)plan.jobs.size();
+    {
         const uint32_t *len = (const uint32_t *)slot.length.p, *path = (const uint32_t *)slot.path.p;
         /* all jobs packed in one pass, then every job's lengths, offsets and
          * vertices copied straight into a pooled pinned block, one wait */
@@ -659,15 +658,95 @@ kk_status kk_batch_walk(kk_engine *e, const kk_walk_opts *jobs, int n_jobs, kk_p
                                           e->stream));
         }
         KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+    }
+}
+
+void free_outs(kk_paths **out, int n)
+{
+    for (int j = 0; j < n; j++)
+    {
+        kk_paths_free(out[j]);
+        out[j] = nullptr;
+    }
+}
+
+} // namespace
+
+/* A submitted batch: its plan, on the engine's batch slot. */
+struct kk_batch
+{
+    kk_engine *e = nullptr;
+    BatchPlan plan;
+};
+
+extern "C" {
+
+kk_status kk_batch_walk(kk_engine *e, const kk_walk_opts *jobs, int n_jobs, kk_paths **out)
+{
+    if (!e || !out)
+        return KK_ERR_INVALID_CONFIG;
+    for (int j = 0; j < n_jobs; j++)
+        out[j] = nullptr;
+    kk_status s = guard(e, [&] {
+        BatchPlan plan = plan_batch(e, jobs, n_jobs);
+        BatchSlot &slot = e->bslot;
+        slot.stream = e->stream;
+        run_batch(e, plan, slot, true, false);
+        e->alias_ms = slot.alias_ms;
+        e->walk_ms = slot.walk_ms;
+        batch_paths_out(e, plan, slot, out);
+    });
+    if (s != KK_OK)
+        free_outs(out, n_jobs);
+    return s;
+}
+
+kk_status kk_batch_submit(kk_engine *e, const kk_walk_opts *jobs, int n_jobs, kk_batch **out)
+{
+    if (!e || !out)
+        return KK_ERR_INVALID_CONFIG;
+    *out = nullptr;
+    kk_batch *b = new (std::nothrow) kk_batch();
+    if (!b)
+        return KK_ERR_OOM;
+    kk_status s = guard(e, [&] {
+        b->e = e;
+        b->plan = plan_batch(e, jobs, n_jobs);
+        BatchSlot &slot = e->bslot;
+        slot.stream = e->stream;
+        batch_prepare(e, b->plan); /* the tables the walk reads, on the engine's stream */
+        batch_launch_async(e, b->plan, slot);
     });
     if (s != KK_OK)
     {
-        for (int j = 0; j < n_jobs; j++)
-        {
-            kk_paths_free(out[j]);
-            out[j] = nullptr;
-        }
+        delete b;
+        return s;
     }
+    e->batch_out = true;
+    *out = b;
+    return KK_OK;
+}
+
+kk_status kk_batch_wait(kk_batch *b, kk_paths **out)
+{
+    if (!b || !out)
+        return KK_ERR_INVALID_CONFIG;
+    kk_engine *e = b->e;
+    const int n_jobs = (int)b->plan.jobs.size();
+    for (int j = 0; j < n_jobs; j++)
+        out[j] = nullptr;
+    e->batch_wait = true;
+    kk_status s = guard(e, [&] {
+        BatchSlot &slot = e->bslot;
+        batch_finish(e, slot);
+        e->alias_ms = slot.alias_ms;
+        e->walk_ms = slot.walk_ms;
+        batch_paths_out(e, b->plan, slot, out);
+    });
+    if (s != KK_OK)
+        free_outs(out, n_jobs);
+    e->batch_out = e->batch_wait = false;
+    delete b;
     return s;
 }
 

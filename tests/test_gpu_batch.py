@@ -127,3 +127,45 @@ def test_batch_results_from_pooled_blocks_across_calls(engine):
         assert c["walker_num"] == job["walker_num"] == a.path_num
         assert c["total_steps"] == a.total_steps
         assert c["vertices"] == len(a.vertices)
+
+
+@pytest.mark.parametrize("app", ["node2vec", "metapath"])
+def test_submitted_batch_equals_batch_walk(engine, oracle_lib, app):
+    """kk_batch_submit / kk_batch_wait: the engine refuses other calls while
+    the batch is outstanding, and the waited-for paths equal kk_batch_walk's
+    and the oracle's; metapath runs with parking, as kk_batch_walk does."""
+    import knightking_gb300 as kk
+    csr = _load(engine, 8, True, types=app == "metapath")
+    if app == "node2vec":
+        jobs = [dict(walker_num=n, seed=s, walk_length=l, p=p, q=q, weighted=True, walker_begin=b)
+                for n, s, l, p, q, b in ((300, 1, 20, 2.0, 0.5, 0), (0, 2, 10, 1.0, 1.0, 0),
+                                         (900, 3, 60, 0.25, 4.0, 50), (17, 4, 5, 0.5, 0.5, 333))]
+    else:
+        jobs = [dict(walker_num=700, seed=7, walk_length=30, weighted=True, schemes=[[1, 2, 4, 8], [2, 8, 2, 16]]),
+                dict(walker_num=64, seed=8, walk_length=12, weighted=True, schemes=[[3, 12]],
+                     scheme_round_robin=True)]
+    ref = engine.batch_walk(app, jobs)
+    b = engine.batch_submit(app, jobs)
+    with pytest.raises(kk.KKError):
+        engine.walk(app, 4, **{k: v for k, v in jobs[0].items() if k != "walker_num"})
+    with pytest.raises(kk.KKError):
+        engine.batch_submit(app, jobs)
+    got = b.wait()
+    with pytest.raises(ValueError):
+        b.wait()
+    assert len(got) == len(jobs)
+    for job, g, r in zip(jobs, got, ref):
+        np.testing.assert_array_equal(g.path_length, r.path_length)
+        np.testing.assert_array_equal(g.vertices, r.vertices)
+        assert g.total_steps == r.total_steps
+        kw = dict(job)
+        n = kw.pop("walker_num")
+        ocsr = oracle_lib.CSR(400, csr["off"], csr["nbr"], csr.get("w"), csr.get("type"))
+        if app == "node2vec":
+            ocsr = ocsr.sorted_copy()
+        lens, verts, _ = oracle_lib.walk(ocsr, oracle_lib.make_params(app, walker_num=n, **kw),
+                                         cap=kw["walk_length"] + 1)
+        np.testing.assert_array_equal(g.path_length, lens)
+        np.testing.assert_array_equal(g.vertices, verts)
+    # the engine serves calls again
+    assert engine.walk(app, 4, **{k: v for k, v in jobs[0].items() if k != "walker_num"}).total_steps >= 0

@@ -8,9 +8,10 @@ log-uniform in [0.25, 4], length uniform in [5, 200], walkers lognormal (median
 4096) clipped to [1, 2^20].  A step is one pass of the whole stream.
 
 value : walker-steps/s of the stream through the batched kernel
-        (kk_batch_walk_device, 1024 requests per launch, paths in HBM), device
-        time from CUDA events on the engine's stream; the plain
-        one-launch-per-request kernel is timed beside it (batched_over_plain).
+        (kk_batch_walk_device, 1024 requests per launch from request tables
+        built before the timed region, paths in HBM), device time from CUDA
+        events on the engine's stream; the plain one-launch-per-request kernel
+        is timed beside it (batched_over_plain).
 e2e   : the same stream through the serving C-ABI (kk_serve_submit/poll,
         driven by the library's own client kk_serve_replay): job records
         host->device, every path device->host into pinned memory, inside the

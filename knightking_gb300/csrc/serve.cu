@@ -291,6 +291,9 @@ void slot_loop(kk_server *s, int k)
                 }
                 else
                 {
+                    /* the slot's thread polls while its batch is on the GPU
+                     * (a core per busy slot), so a finished request is seen
+                     * within microseconds rather than a timer tick */
                     std::this_thread::yield();
                 }
             }

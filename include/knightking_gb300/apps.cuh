@@ -84,6 +84,10 @@ struct Node2vecUpdate
 struct Node2vecPostQuery
 {
     static constexpr bool reads_edge_index = false;
+    /* min(1, 1/q) as floats: a dart at or below it is accepted whether the
+     * candidate is a neighbour of the previous vertex (dynamic component 1)
+     * or not (1/q) */
+    real_t sure_below = 0.0f;
     __device__ __forceinline__ bool operator()(const Walker<Node2vecState> &w, vertex_id_t, const AdjUnit &cand,
                                                vertex_id_t &target, vertex_id_t &query) const
     {
@@ -92,6 +96,16 @@ struct Node2vecPostQuery
         target = w.data.previous_vertex;
         query = cand.neighbour;
         return true;
+    }
+    /* Whether the answer can change the trial's outcome: not for the return
+     * edge (its dynamic component is 1/p either way), nor for a dart at or
+     * below sure_below.  The reference asks in both cases (node2vec.hpp:150-
+     * 158); skipping the question leaves every decision, and so every path,
+     * as it is. */
+    __device__ __forceinline__ bool query_matters(const Walker<Node2vecState> &w, const AdjUnit &cand,
+                                                  real_t dart) const
+    {
+        return !(w.data.previous_vertex == cand.neighbour || dart <= sure_below);
     }
 };
 
@@ -372,7 +386,7 @@ struct Node2vecBatch
         tc.extension_comp = FixedLengthExt<Node2vecState>{j.walk_length};
         if constexpr (Weighted)
             tc.static_comp = WeightStatic{w};
-        tc.post_query = Node2vecPostQuery{};
+        tc.post_query = Node2vecPostQuery{j.c[4] < 1.0f ? j.c[4] : 1.0f};
         tc.respond_query = Node2vecRespond{nbr, set};
         tc.dynamic_comp = Node2vecDyn{j.c[0], j.c[3], j.c[4]};
         tc.dcomp_upperbound = ConstBound{j.c[0]};

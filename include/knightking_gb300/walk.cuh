@@ -1889,6 +1889,19 @@ __device__ __forceinline__ bool respond_needs_adjacency(const F &f)
         return true;
 }
 
+/* Whether a post_query hook offers query_matters(walker, candidate, dart). */
+template <typename F, typename S, typename = void>
+struct has_query_matters : std::false_type
+{
+};
+template <typename F, typename S>
+struct has_query_matters<F, S,
+                         std::void_t<decltype(std::declval<const F &>().query_matters(
+                             std::declval<const Walker<S> &>(), std::declval<const AdjUnit &>(), 0.0f))>>
+    : std::true_type
+{
+};
+
 /* A picked candidate: index local to the adjacency (kNone when the bucket
  * does not carry it), neighbour, and the neighbour's cursor when the bucket
  * carries one (has_cur). */
@@ -2237,7 +2250,13 @@ __device__ __forceinline__ bool walk_trial(const GraphView &g, const WC &wc, con
             R resp{};
             Q query{};
             vertex_id_t target = 0;
-            if (tc.post_query(w, v, cu, target, query))
+            /* a post_query hook that can tell when its answer cannot change
+             * the outcome skips the question; a launch counting accesses asks
+             * as the reference does */
+            bool ask = true;
+            if constexpr (has_query_matters<decltype(tc.post_query), S>::value)
+                ask = L.stats != nullptr || tc.post_query.query_matters(w, cu, randval);
+            if (ask && tc.post_query(w, v, cu, target, query))
             {
                 AdjList tadj{0, 0};
                 run.queries++;
@@ -2956,6 +2975,7 @@ __global__ void __launch_bounds__(256, KK_BATCH_MINB) walk_batch_kernel(GraphVie
             if (alive)
                 i = batch_walker_begin<S>(g, app, jobs, s_first, njobs, t, alias_sum, path, length, total_steps,
                                           status, trial_limit, wc, tc, L, run, rng, nt);
+            L.stats = stats;
             walk_lanes<S>(g, wc, tc, alias, nullptr, L, alive, i, run, rng, my_steps, counts, t);
         }
         else if (t < total)
@@ -2967,6 +2987,7 @@ __global__ void __launch_bounds__(256, KK_BATCH_MINB) walk_batch_kernel(GraphVie
             Sampler rng;
             const uint32_t i = batch_walker_begin<S>(g, app, jobs, s_first, njobs, t, alias_sum, path, length,
                                                      total_steps, status, trial_limit, wc, tc, L, run, rng, nt);
+            L.stats = stats;
             while (walk_trial<S>(g, wc, tc, alias, nullptr, L, run, rng))
             {
             }
@@ -3026,6 +3047,7 @@ __global__ void __launch_bounds__(256, 4) walk_batch_resume_kernel(GraphView g, 
             rng.init(L.seed);
             resume_run<S>(L, i, pw, run);
         }
+        L.stats = stats;
         walk_lanes<S>(g, wc, tc, alias, nullptr, L, alive, i, run, rng, my_steps, counts, t);
     }
     flush_steps(total_steps, my_steps);
@@ -3076,6 +3098,7 @@ __global__ void __launch_bounds__(256, 4) walk_batch_pool_kernel(GraphView g, Ap
     if (have)
         i = batch_walker_begin<S>(g, app, jobs, s_first, njobs, t, alias_sum, path, length, total_steps, status,
                                   trial_limit, wc, tc, L, run, rng, nt);
+    L.stats = stats;
     while (__any_sync(kFullMask, have))
     {
         if (have && !walk_trial<S>(g, wc, tc, alias, nullptr, L, run, rng))
@@ -3089,6 +3112,7 @@ __global__ void __launch_bounds__(256, 4) walk_batch_pool_kernel(GraphView g, Ap
             if (have)
                 i = batch_walker_begin<S>(g, app, jobs, s_first, njobs, t, alias_sum, path, length, total_steps,
                                           status, trial_limit, wc, tc, L, run, rng, nt);
+            L.stats = stats;
         }
     }
     flush_steps(total_steps, my_steps);

@@ -27,7 +27,7 @@ void run_n2v(kk_engine *e, const kk_walk_opts &o, const Node2vecConstants &c, co
     tc.extension_comp = FixedLengthExt<Node2vecState>{o.walk_length};
     if constexpr (Weighted)
         tc.static_comp = WeightStatic{e->d_w};
-    tc.post_query = Node2vecPostQuery{};
+    tc.post_query = Node2vecPostQuery{c.inv_q < 1.0f ? c.inv_q : 1.0f};
     tc.respond_query = Node2vecRespond{e->d_nbr, set};
     tc.dynamic_comp = Node2vecDyn{c.upperbound, c.inv_p, c.inv_q};
     tc.dcomp_upperbound = ConstBound{c.upperbound};

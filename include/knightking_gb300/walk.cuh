@@ -2250,23 +2250,33 @@ __device__ __forceinline__ bool walk_trial(const GraphView &g, const WC &wc, con
             R resp{};
             Q query{};
             vertex_id_t target = 0;
-            /* a post_query hook that can tell when its answer cannot change
-             * the outcome skips the question; a launch counting accesses asks
-             * as the reference does */
-            bool ask = true;
-            if constexpr (has_query_matters<decltype(tc.post_query), S>::value)
-                ask = L.stats != nullptr || tc.post_query.query_matters(w, cu, randval);
-            if (ask && tc.post_query(w, v, cu, target, query))
+            if (tc.post_query(w, v, cu, target, query))
             {
-                AdjList tadj{0, 0};
-                run.queries++;
-                if (respond_needs_adjacency(tc.respond_query))
+                /* the reference asks here; a post_query hook that can tell
+                 * when the answer cannot change the outcome skips the
+                 * question.  Counts: queries this engine asks, and the binary
+                 * search probes of every question the reference asks (a
+                 * launch counting accesses tallies those of skipped ones
+                 * too) */
+                bool ask = true;
+                if constexpr (has_query_matters<decltype(tc.post_query), S>::value)
+                    ask = tc.post_query.query_matters(w, cu, randval);
+                if (ask || L.stats != nullptr)
                 {
-                    const Pos tp = (target == run.pv && run.ppos.e0 >= 0) ? run.ppos : pos_from_offsets(g, target);
-                    tadj = AdjList{(edge_id_t)tp.e0, (edge_id_t)(tp.e0 + tp.deg)};
-                    run.probes += 32 - __clz(tp.deg);
+                    AdjList tadj{0, 0};
+                    if (respond_needs_adjacency(tc.respond_query))
+                    {
+                        const Pos tp =
+                            (target == run.pv && run.ppos.e0 >= 0) ? run.ppos : pos_from_offsets(g, target);
+                        tadj = AdjList{(edge_id_t)tp.e0, (edge_id_t)(tp.e0 + tp.deg)};
+                        run.probes += 32 - __clz(tp.deg);
+                    }
+                    if (ask)
+                    {
+                        run.queries++;
+                        tc.respond_query(target, query, tadj, resp);
+                    }
                 }
-                tc.respond_query(target, query, tadj, resp);
             }
             accepted = randval <= tc.dynamic_comp(w, resp, v, cu);
         }

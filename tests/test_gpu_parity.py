@@ -492,3 +492,34 @@ def test_epoch_split_matches_single_epoch(engine, i):
     np.testing.assert_array_equal(many.path_length, one.path_length)
     np.testing.assert_array_equal(many.vertices, one.vertices)
     assert many.total_steps == one.total_steps
+
+
+@pytest.mark.parametrize("p,q,lo,hi", [(2.0, 0.5, 0.35, 0.56), (0.5, 2.0, 0.35, 0.56)])
+def test_node2vec_asks_only_queries_that_can_matter(engine, oracle_lib, p, q, lo, hi):
+    """The adjacency question is skipped for the return edge and for darts at
+    or below min(1, 1/q), where either answer accepts.  With p = 2, q = 0.5
+    the reference asks for darts above lb = 0.5 of ub = 2 (3/4 of the trials)
+    and this engine for darts above 1 (1/2); with p = 0.5, q = 2 both ask for
+    darts above 0.5 of ub = 1 (1/2).  Paths are the same with the access
+    counts on and off, and equal the oracle's; the counted binary-search
+    probes cover every question the reference asks."""
+    g = G.random_undirected(400, 6000, seed=77, weight="unif")
+    csr = G.csr_file_order(400, g["src"], g["dst"], w=g["w"])
+    engine.load_arrays(400, csr["off"], csr["nbr"], csr["w"])
+    n, L = 20000, 20
+    a = engine.walk("node2vec", n, seed=5, walk_length=L, p=p, q=q, weighted=True)
+    engine.set_option("walk_stats", 1)
+    engine.set_option("node2vec_adjacency", 1)
+    try:
+        b = engine.walk("node2vec", n, seed=5, walk_length=L, p=p, q=q, weighted=True)
+        trials, queries, probes = engine.last_stats()
+    finally:
+        engine.set_option("walk_stats", 0)
+        engine.set_option("node2vec_adjacency", 0)
+    np.testing.assert_array_equal(a.vertices, b.vertices)
+    ocsr = oracle_lib.CSR(400, csr["off"], csr["nbr"], csr["w"]).sorted_copy()
+    prm = oracle_lib.make_params("node2vec", seed=5, walker_num=n, walk_length=L, p=p, q=q, weighted=True)
+    lens, verts, steps = oracle_lib.walk(ocsr, prm, cap=L + 1)
+    np.testing.assert_array_equal(a.vertices, verts)
+    assert lo < queries / trials < hi
+    assert probes > queries

@@ -308,11 +308,13 @@ typedef struct
 typedef struct
 {
     uint64_t completed, failed, batches;
-    uint64_t walker_steps;
+    uint64_t walker_steps;          /* of the completed requests */
     double p50_ms, p99_ms, mean_ms; /* latency of the completed requests */
     double mean_batch_jobs;
-    double walk_ms, copy_ms, host_ms; /* summed over batches: the batch on the GPU (launch to
-                                         status), its paths to pinned memory, the per-request copies */
+    double walk_ms, copy_ms, host_ms; /* summed over batches: launch to the batch's walk seen
+                                         ended (0 when its last request was out first), from
+                                         there to its last request out, then the slot's own
+                                         hand-out of failed requests */
 } kk_serve_stats;
 
 kk_status kk_serve_start(kk_engine *e, const kk_serve_opts *opts, kk_server **out);

@@ -422,7 +422,11 @@ static void launch_batch_graph(kk_engine *e, BatchPlan &plan, BatchSlot &slot)
             uint32_t *path = nullptr;
             launch_app_batch(e, plan, slot, d_jobs, (uint32_t *)slot.length.p, &path, d_steps, d_status, true, true,
                              d_hdr);
-            KK_CUDA_CHECK(cudaMemcpyAsync(h.status, d_status, 64, cudaMemcpyDeviceToHost, slot.stream));
+            /* with per-request completion each request's status comes with
+             * its flag and its steps with its paths: no read-back, which
+             * would wait on a copy engine behind the other slots' paths */
+            if (slot.notify.count == nullptr)
+                KK_CUDA_CHECK(cudaMemcpyAsync(h.status, d_status, 64, cudaMemcpyDeviceToHost, slot.stream));
         }
         catch (...)
         {
@@ -441,12 +445,15 @@ static void launch_batch_graph(kk_engine *e, BatchPlan &plan, BatchSlot &slot)
     KK_CUDA_CHECK(cudaEventRecord(slot.ev[2], slot.stream));
 }
 
-/* Waits for a graph-mode batch; its status (the batch's, or none with
- * per-request completion) and walker-steps from the staging block. */
+/* Waits for a graph-mode batch; its status and walker-steps from the staging
+ * block (a slot with per-request completion reads neither: see
+ * launch_batch_graph). */
 static uint64_t finish_batch_graph(BatchSlot &slot)
 {
     const GraphStage h = graph_stage(slot);
     KK_CUDA_CHECK(cudaStreamSynchronize(slot.stream));
+    if (slot.notify.count != nullptr)
+        fail(KK_ERR_INVALID_CONFIG, "a slot with per-request completion has no batch count");
     slot.alias_ms = 0.0f;
     KK_CUDA_CHECK(cudaEventElapsedTime(&slot.walk_ms, slot.ev[1], slot.ev[2]));
     if (h.status[0] & KK_STATUS_TRIAL_LIMIT)

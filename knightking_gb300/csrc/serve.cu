@@ -281,6 +281,8 @@ void slot_loop(kk_server *s, int k)
                         for (size_t x = fin; x < ready; x++)
                         {
                             const uint32_t j = order[x];
+                            if (job_st[j] == KK_OK)
+                                steps += paths[j]->total_steps;
                             hand_out(s, batch[j], job_st[j], paths[j], t_launch, t_done, n);
                             handed[j] = 1;
                             paths[j] = nullptr;
@@ -297,8 +299,12 @@ void slot_loop(kk_server *s, int k)
                     std::this_thread::yield();
                 }
             }
+            /* every request is out: the slot takes its next batch without
+             * waiting for this one's last blocks to leave the GPU, since the
+             * next launch is ordered behind them on the slot's stream and
+             * nothing of this batch is read any more (a fault would surface
+             * at that launch or its event) */
             t_copied = Clock::now();
-            steps = batch_finish(s->e, slot);
         }
         catch (const Error &x)
         {

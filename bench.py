@@ -722,8 +722,8 @@ def run_serve_bench(args, wl, world, rank, local):
                                      "what": "one pass submitted and polled request by request from Python "
                                              "through ctypes"},
                    "batches": sat["batches"], "mean_batch_jobs": sat["mean_batch_jobs"],
-                   "slot_time_ms": {"walk_seen_ended": sat["walk_ms"], "then_last_request_out": sat["copy_ms"],
-                                    "after_last_request_out": sat["host_ms"]}},
+                   "slot_time_ms": {"walk_seen_ended": sat["walk_ms"], "then_last_copies_issued": sat["copy_ms"],
+                                    "after_last_copies_issued": sat["host_ms"]}},
         "batched_over_plain": value / plain_value,
         "served_over_plain": served_value / plain_value,
         "latency": {"load": head["load"], "offered_rate_req_s": head["offered_req_s"], "p50_ms": head["p50_ms"],

@@ -312,8 +312,9 @@ typedef struct
     double p50_ms, p99_ms, mean_ms; /* latency of the completed requests */
     double mean_batch_jobs;
     double walk_ms, copy_ms, host_ms; /* summed over batches: launch to the batch's walk seen
-                                         ended (0 when its last request was out first), from
-                                         there to its last request out, then the slot's own
+                                         ended (0 when its last copies were issued first), from
+                                         there to its last request's copies issued (the slot
+                                         then takes its next batch), then the slot's own
                                          hand-out of failed requests */
 } kk_serve_stats;
 

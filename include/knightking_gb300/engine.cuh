@@ -114,7 +114,8 @@ struct BatchSlot
     char *h_stage = nullptr; /* pinned: jobs | schemes | header | status */
     /* per-request completion (serving): counters and status words on the
      * device, flags in mapped host memory (notify.count == nullptr: off); the
-     * slot's requests are copied out on `copy`, one event per request */
+     * slot's requests are copied out on `copy`; job_ev holds the events the
+     * slot's thread created (one per request in flight, reused) */
     BatchNotify notify;
     DevBuf notify_dev;        /* count[kMaxBatchJobs] | status[kMaxBatchJobs] */
     uint32_t *h_flag = nullptr;

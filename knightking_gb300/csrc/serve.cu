@@ -168,22 +168,135 @@ void hand_out(kk_server *s, const Request &r, kk_status st, kk_paths *paths, Clo
     }
 }
 
+/* A request whose paths are on their way to its pinned block. */
+struct InFlight
+{
+    Request r;
+    kk_status st;
+    kk_paths *paths;
+    cudaEvent_t ev; /* recorded on the slot's copy stream after its copies */
+    Clock::time_point t_launch;
+    size_t n; /* requests in its batch */
+};
+
+/* The status of a failure caught in a slot's loop. */
+kk_status caught_status()
+{
+    try
+    {
+        throw;
+    }
+    catch (const Error &x)
+    {
+        return x.status;
+    }
+    catch (const std::bad_alloc &)
+    {
+        return KK_ERR_OOM;
+    }
+    catch (...)
+    {
+        return KK_ERR_CUDA;
+    }
+}
+
 /* One slot's loop: take a batch of queued requests, launch it, and hand each
  * request out as soon as its own walkers have ended (its flag, raised by the
  * last of them with the request's status) and its paths have reached pinned
- * host memory, while the rest of the batch is still walking. */
+ * host memory, while the rest of the batch is still walking.  Once the last
+ * request's copies are issued the slot takes its next batch: that walk waits
+ * on the GPU for the copies (an event on the copy stream), and the requests
+ * still in flight are handed out while it runs. */
 void slot_loop(kk_server *s, int k)
 {
     cudaSetDevice(s->e->device);
     BatchSlot &slot = s->slots[k];
+    std::deque<InFlight> out;         /* copies issued, in issue order */
+    std::vector<cudaEvent_t> free_ev; /* events of requests handed out */
+    cudaEvent_t copies_ev = nullptr;  /* after the last copy issued */
+
+    auto new_event = [&]() {
+        if (!free_ev.empty())
+        {
+            cudaEvent_t ev = free_ev.back();
+            free_ev.pop_back();
+            return ev;
+        }
+        cudaEvent_t ev = nullptr;
+        KK_CUDA_CHECK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        slot.job_ev.push_back(ev); /* destroyed with the slot */
+        return ev;
+    };
+    /* hands out the requests whose copies are done, in issue order */
+    auto hand_out_ready = [&]() {
+        size_t ready = 0;
+        while (ready < out.size())
+        {
+            const cudaError_t q = cudaEventQuery(out[ready].ev);
+            if (q == cudaErrorNotReady)
+                break;
+            KK_CUDA_CHECK(q);
+            ready++;
+        }
+        if (ready == 0)
+            return false;
+        const Clock::time_point t_done = Clock::now();
+        for (size_t x = 0; x < ready; x++)
+            finish_paths(out[x].paths);
+        {
+            std::lock_guard<std::mutex> lk(s->m);
+            for (size_t x = 0; x < ready; x++)
+            {
+                InFlight &f = out.front();
+                if (f.st == KK_OK)
+                    s->steps += f.paths->total_steps;
+                hand_out(s, f.r, f.st, f.paths, f.t_launch, t_done, f.n);
+                free_ev.push_back(f.ev);
+                out.pop_front();
+            }
+        }
+        s->cv_done.notify_all();
+        return true;
+    };
+    /* after a failure: the requests in flight go out once their copies have
+     * landed, with their own status if the copies did, else with st */
+    auto drain_after_failure = [&](kk_status st) {
+        const bool copied = slot.copy == nullptr || cudaStreamSynchronize(slot.copy) == cudaSuccess;
+        const Clock::time_point t_done = Clock::now();
+        std::lock_guard<std::mutex> lk(s->m);
+        for (InFlight &f : out)
+        {
+            if (copied)
+                finish_paths(f.paths);
+            hand_out(s, f.r, copied ? f.st : st, f.paths, f.t_launch, t_done, f.n);
+            free_ev.push_back(f.ev);
+        }
+        out.clear();
+    };
+
     for (;;)
     {
         std::vector<Request> batch;
+        try
         {
             std::unique_lock<std::mutex> lk(s->m);
-            s->cv_work.wait(lk, [&] { return s->stopping || !s->queue.empty(); });
-            if (s->queue.empty())
-                return; /* stopping, queue drained */
+            for (;;)
+            {
+                if (!s->queue.empty())
+                    break;
+                if (out.empty())
+                {
+                    s->cv_work.wait(lk, [&] { return s->stopping || !s->queue.empty(); });
+                    if (s->queue.empty())
+                        return; /* stopping, queue drained, nothing in flight */
+                    break;
+                }
+                /* requests in flight: hand them out while waiting for work */
+                lk.unlock();
+                if (!hand_out_ready())
+                    std::this_thread::yield();
+                lk.lock();
+            }
             uint64_t bytes = 0;
             while (!s->queue.empty() && batch.size() < s->o.max_jobs)
             {
@@ -195,38 +308,38 @@ void slot_loop(kk_server *s, int k)
                 s->queue.pop_front();
             }
         }
+        catch (...)
+        {
+            drain_after_failure(caught_status());
+            s->cv_done.notify_all();
+            continue;
+        }
         const Clock::time_point t_launch = Clock::now();
         const size_t n = batch.size();
         std::vector<kk_walk_opts> jobs(n);
         for (size_t j = 0; j < n; j++)
             jobs[j] = batch[j].opts;
-        std::vector<kk_paths *> paths(n, nullptr);
-        std::vector<kk_status> job_st(n, KK_OK);
-        std::vector<char> handed(n, 0);
+        std::vector<char> issued(n, 0);
         kk_status st = KK_OK;
-        uint64_t steps = 0;
         Clock::time_point t_walked = t_launch, t_copied = t_launch;
         try
         {
             /* in arrival order: a request is handed out as soon as it ends,
              * and the long ones of the batch need not all start first */
             BatchPlan plan = plan_batch(s->e, jobs.data(), (int)n, false);
-            while (slot.job_ev.size() < n)
-            {
-                cudaEvent_t ev_j = nullptr;
-                KK_CUDA_CHECK(cudaEventCreateWithFlags(&ev_j, cudaEventDisableTiming));
-                slot.job_ev.push_back(ev_j);
-            }
-            /* the slot's previous batch has ended: no walker writes a flag */
+            /* every flag of the slot's previous batch has been read: no
+             * walker of it writes one any more */
             volatile uint32_t *flag = slot.h_flag;
             for (size_t j = 0; j < n; j++)
                 flag[j] = 0;
+            /* the walk overwrites the slot's buffers the previous batch's
+             * copies read from */
+            if (copies_ev != nullptr)
+                KK_CUDA_CHECK(cudaStreamWaitEvent(slot.stream, copies_ev, 0));
             batch_launch_async(s->e, plan, slot);
-            std::vector<uint32_t> order; /* requests in the order their copies were issued */
-            order.reserve(n);
-            size_t fin = 0;
+            size_t n_issued = 0;
             bool walked = false;
-            while (fin < n)
+            while (n_issued < n)
             {
                 if (!walked)
                 {
@@ -241,9 +354,10 @@ void slot_loop(kk_server *s, int k)
                         KK_CUDA_CHECK(q);
                     }
                 }
-                for (size_t j = 0; j < n && order.size() < n; j++)
+                bool any = false;
+                for (size_t j = 0; j < n && n_issued < n; j++)
                 {
-                    if (paths[j] != nullptr || handed[j])
+                    if (issued[j])
                         continue;
                     /* a request of no walkers has nothing to walk */
                     const uint32_t f = plan.jobs[j].walker_num == 0 ? 1u : flag[j];
@@ -255,43 +369,28 @@ void slot_loop(kk_server *s, int k)
                             fail(KK_ERR_CUDA, "a request of the batch did not complete");
                         continue;
                     }
-                    job_st[j] = job_status_of(f - 1);
-                    paths[j] = job_paths(s->pool, plan.jobs[j], (const uint32_t *)slot.length.p,
-                                         (const uint32_t *)slot.path.p, slot.copy);
-                    KK_CUDA_CHECK(cudaEventRecord(slot.job_ev[j], slot.copy));
-                    order.push_back((uint32_t)j);
-                }
-                /* the requests whose copies are done, in issue order */
-                size_t ready = fin;
-                while (ready < order.size())
-                {
-                    const cudaError_t q = cudaEventQuery(slot.job_ev[order[ready]]);
-                    if (q == cudaErrorNotReady)
-                        break;
-                    KK_CUDA_CHECK(q);
-                    ready++;
-                }
-                if (ready > fin)
-                {
-                    const Clock::time_point t_done = Clock::now();
-                    for (size_t x = fin; x < ready; x++)
-                        finish_paths(paths[order[x]]);
+                    kk_paths *pj = job_paths(s->pool, plan.jobs[j], (const uint32_t *)slot.length.p,
+                                             (const uint32_t *)slot.path.p, slot.copy);
+                    cudaEvent_t ev = nullptr;
+                    try
                     {
-                        std::lock_guard<std::mutex> lk(s->m);
-                        for (size_t x = fin; x < ready; x++)
-                        {
-                            const uint32_t j = order[x];
-                            if (job_st[j] == KK_OK)
-                                steps += paths[j]->total_steps;
-                            hand_out(s, batch[j], job_st[j], paths[j], t_launch, t_done, n);
-                            handed[j] = 1;
-                            paths[j] = nullptr;
-                        }
+                        ev = new_event();
+                        out.push_back(InFlight{batch[j], job_status_of(f - 1), pj, ev, t_launch, n});
                     }
-                    s->cv_done.notify_all();
-                    fin = ready;
+                    catch (...)
+                    {
+                        cudaStreamSynchronize(slot.copy);
+                        kk_paths_free(pj);
+                        throw;
+                    }
+                    issued[j] = 1;
+                    n_issued++;
+                    KK_CUDA_CHECK(cudaEventRecord(ev, slot.copy));
+                    any = true;
                 }
-                else
+                if (hand_out_ready())
+                    any = true;
+                if (!any)
                 {
                     /* the slot's thread polls while its batch is on the GPU
                      * (a core per busy slot), so a finished request is seen
@@ -299,41 +398,32 @@ void slot_loop(kk_server *s, int k)
                     std::this_thread::yield();
                 }
             }
-            /* every request is out: the slot takes its next batch without
-             * waiting for this one's last blocks to leave the GPU, since the
-             * next launch is ordered behind them on the slot's stream and
-             * nothing of this batch is read any more (a fault would surface
-             * at that launch or its event) */
+            if (copies_ev == nullptr)
+                copies_ev = new_event();
+            KK_CUDA_CHECK(cudaEventRecord(copies_ev, slot.copy));
+            /* nothing of this batch is read back: its last blocks leave the
+             * GPU ahead of the slot's next walk on the same stream (a fault
+             * would surface at that launch or its event) */
             t_copied = Clock::now();
-        }
-        catch (const Error &x)
-        {
-            st = x.status;
-        }
-        catch (const std::bad_alloc &)
-        {
-            st = KK_ERR_OOM;
         }
         catch (...)
         {
-            st = KK_ERR_CUDA;
+            st = caught_status();
         }
         if (st != KK_OK)
         {
             /* copies in flight land in blocks about to go back to the pool */
-            if (slot.copy)
-                cudaStreamSynchronize(slot.copy);
+            drain_after_failure(st);
             cudaStreamSynchronize(slot.stream);
         }
         const Clock::time_point t_done = Clock::now();
         {
             std::lock_guard<std::mutex> lk(s->m);
             for (size_t j = 0; j < n; j++)
-                if (!handed[j])
-                    hand_out(s, batch[j], st, paths[j], t_launch, t_done, n);
+                if (!issued[j])
+                    hand_out(s, batch[j], st, nullptr, t_launch, t_done, n);
             s->batches++;
             s->batch_jobs_sum += n;
-            s->steps += steps;
             s->walk_ms += ms_between(t_launch, t_walked);
             s->copy_ms += ms_between(t_walked, t_copied);
             s->host_ms += ms_between(t_copied, t_done);

@@ -205,9 +205,10 @@ kk_status kk_alias_build(kk_engine *e, float *p, uint32_t *p_idx, uint32_t *q_id
  * values bit for bit.  Its queue scratch is a fixed 32 MiB device array inside
  * the library that every GPU which loads the library keeps until the process
  * exits; a vertex degree above 16384 is rejected with KK_ERR_INVALID_CONFIG.
- * The first call on a device looks up that array's address (make it before
- * any stream capture); the work is queued on `stream` (a cudaStream_t, NULL =
- * default stream) after a short degree check that synchronises the stream.
+ * The first call on a device looks up that array's address; the work is
+ * queued on `stream` (a cudaStream_t, NULL = default stream) after a short
+ * degree check that synchronises the stream, so no call can be made while its
+ * stream is being captured into a CUDA graph.
  * Calls share the scratch: calls that overlap on the GPU race. */
 kk_status kk_alias_build_noalloc(uint32_t v_num, const int64_t *d_off, const float *d_w, float *d_p,
                                  uint32_t *d_p_idx, uint32_t *d_q_idx, float *d_sum, void *stream);

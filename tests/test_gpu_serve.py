@@ -113,9 +113,11 @@ def test_server_refuses_bad_requests(engine):
 def test_replay_client_keeps_schedule_and_counts_every_step(engine):
     """kk_serve_replay (the library's open-loop client): every request
     completes with a latency, the walker-steps equal those of the same
-    requests run alone, an arrival schedule that spreads the requests over
-    0.2 s is kept (the call lasts at least that long), and a schedule that
-    runs backwards or a refused request is reported."""
+    requests run alone (and so do the server's own statistics, which count
+    the completed requests' steps from their paths), an arrival schedule that
+    spreads the requests over 0.2 s is kept (the call lasts at least that
+    long), and a schedule that runs backwards or a refused request is
+    reported."""
     import knightking_gb300 as kk
     _load(engine, 13)
     reqs = _requests("node2vec", 80, seed=9)
@@ -125,6 +127,8 @@ def test_replay_client_keeps_schedule_and_counts_every_step(engine):
         lat, steps, elapsed = srv.replay(reqs, np.zeros(len(reqs)))
         assert steps == alone
         assert np.all(lat > 0)
+        st = srv.stats()
+        assert st["walker_steps"] == alone and st["completed"] == len(reqs) and st["failed"] == 0
         arrivals = np.linspace(0.0, 0.2, len(reqs))
         lat, steps, elapsed = srv.replay(reqs, arrivals)
         assert steps == alone and np.all(lat > 0)

@@ -68,6 +68,10 @@ WORKLOADS = {
                                     "graph: per request p, q log-uniform [0.25, 4], length uniform [5, 200], "
                                     "walkers lognormal (median 4096, sigma 1) clipped to [1, 2^20], each request "
                                     "its own seed and walker-id range"),
+    "ingest-s22": dict(app=None, scale=22, weights=1, types=0, ingest=True,
+                       desc="graph ingestion: binary Edge<float> file (src u32, dst u32, weight f32 per record) of "
+                            "the R-MAT scale 22 ef16 uniform[1,5) graph, each undirected edge once in a seeded "
+                            "shuffled order, loaded with --make-undirected into a CSR in HBM"),
     "metapath-batch-s22": dict(app="metapath", scale=22, weights=1, types=5, batch=16,
                                schemes=[[1, 2, 4, 8], [2, 8, 2, 16], [4, 1, 16, 4]], scheme_round_robin=True,
                                desc="16 metapath jobs (walkers 2^10..2^22, lengths 5..200, 3 schemes of 4 one-hot "
@@ -397,6 +401,8 @@ def run_reference(args, wl, world, rank, local):
     from oracle import pyoracle
     pyoracle.build()
     threads = os.cpu_count() or 1
+    if "ingest" in wl:
+        return run_reference_ingest(args, wl, world, threads)
     t0 = time.perf_counter()
     g = pyoracle.rmat_graph(wl["scale"], 16, seed=wl["scale"], weights=wl["weights"], types=wl["types"],
                             threads=threads)
@@ -439,6 +445,43 @@ def run_reference(args, wl, world, rank, local):
     }
     if walkers is not None:
         line["config"]["walkers"] = walkers
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_ingest(args, wl, world, threads):
+    """The reference's loader restated on the CPU (ingest_oracle) on the same
+    file as the GPU arm's, a few whole-file steps (each takes seconds)."""
+    import tempfile
+
+    from oracle import pyoracle
+    g = pyoracle.rmat_graph(wl["scale"], 16, seed=wl["scale"], weights=wl["weights"], types=0, threads=threads)
+    V = g["V"]
+    rec = ingest_records(V, g["off"], g["nbr"], g["w"])
+    del g
+    path = os.path.join(tempfile.gettempdir(), "kk_ingest_ref_s%d_%d.bin" % (wl["scale"], os.getpid()))
+    rec.tofile(path)
+    E = 2 * len(rec)
+    del rec
+    steps = min(args.steps, 3)
+    try:
+        ingest_oracle(V, path)
+        secs = []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            ingest_oracle(V, path)
+            secs.append(time.perf_counter() - t0)
+    finally:
+        os.unlink(path)
+    value = E / statistics.median(secs)
+    line = {
+        "impl": "reference", "metric": "edges/s", "value": value, "unit": "edges/s", "n_gpus": world,
+        "steps": steps, "warmup": 1, "ms_per_step": 1e3 * statistics.median(secs), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded R-MAT)",
+        "config": {"workload": args.workload, "desc": wl["desc"], "vertices": V, "edges": E},
+        "cpu_baseline": {"value": value, "unit": "edges/s", "cores": 1, "kind": "port",
+                         "sample": "the whole file: read, mirror, stable sort by source, offsets (numpy)"},
+        "e2e": {"value": value, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
     print(json.dumps(line), flush=True)
 
 
@@ -1078,7 +1121,125 @@ DEFAULT_WORKLOAD = "node2vec-serve-s24"
 SECOND_WORKLOAD = "deepwalk-s22"
 
 
+INGEST_RECORD = np.dtype([("src", "<u4"), ("dst", "<u4"), ("w", "<f4")])
+
+
+def ingest_records(V, off, nbr, w, seed=7):
+    """The ingestion file's records: each undirected edge of a symmetric CSR
+    once (source < destination), in a seeded shuffled order."""
+    src = np.repeat(np.arange(V, dtype=np.uint32), np.diff(off))
+    keep = src < nbr
+    perm = np.random.default_rng(seed).permutation(int(keep.sum()))
+    rec = np.empty(len(perm), dtype=INGEST_RECORD)
+    rec["src"] = src[keep][perm]
+    rec["dst"] = nbr[keep][perm]
+    rec["w"] = w[keep][perm]
+    return rec
+
+
+def ingest_oracle(V, path):
+    """The reference's loader (include/graph.hpp:408-530, --make-undirected at
+    :430-443) restated on the CPU: read the records, follow each by its mirror,
+    stable sort by source (file order within a source), offsets by counting."""
+    from oracle import graphs
+    rec = np.fromfile(path, dtype=INGEST_RECORD)
+    src = np.empty(2 * len(rec), np.uint32)
+    dst = np.empty(2 * len(rec), np.uint32)
+    src[0::2], src[1::2] = rec["src"], rec["dst"]
+    dst[0::2], dst[1::2] = rec["dst"], rec["src"]
+    return graphs.csr_file_order(V, src, dst, w=np.repeat(rec["w"], 2))
+
+
+def run_ingest_bench(args, wl, world, rank, local):
+    """Graph ingestion, the step before the walk: kk_graph_load_binary of a
+    binary Edge<float> file with --make-undirected into a CSR in HBM.
+
+    value : CSR edges per second of the call's device part (the edge columns
+            copied to HBM, the stable radix sort by source, offsets, permutes;
+            kk_graph_load_timing), K calls.
+    e2e   : CSR edges per second of the whole call, file (in the page cache)
+            to CSR in HBM.
+    parity: the loaded CSR (offsets, neighbours, weights) against the oracle's
+            restatement of the reference's loader, array for array.
+    cpu_baseline: that restatement (numpy, one core) timed on the same file."""
+    import tempfile
+
+    import torch
+
+    import knightking_gb300 as kk
+
+    torch.cuda.set_device(local)
+    engine = kk.WalkEngine(local)
+    engine.generate_rmat(wl["scale"], 16, seed=wl["scale"], weights=wl["weights"])
+    V, _, _, _ = engine.info()
+    g = engine.download_graph()
+    rec = ingest_records(V, g["off"], g["nbr"], g["w"])
+    del g
+    path = os.path.join(tempfile.gettempdir(), "kk_ingest_s%d_r%d_%d.bin" % (wl["scale"], rank, os.getpid()))
+    rec.tofile(path)
+    file_bytes = rec.nbytes
+    del rec
+    steps = min(args.steps, 5)  # a call takes about a second
+    try:
+        for _ in range(args.warmup):
+            engine.load_graph(V, path, load_as_undirected=True, kind="f32")
+        barrier(world)
+        total_s, device_s = [], []
+        with ClockSampler(local) as clocks:
+            l0 = engine.launch_count()
+            for _ in range(steps):
+                t0 = time.perf_counter()
+                engine.load_graph(V, path, load_as_undirected=True, kind="f32")
+                total_s.append(time.perf_counter() - t0)
+                device_s.append(engine.load_timing()[1] / 1e3)
+            launches = engine.launch_count() - l0
+        _, E, _, _ = engine.info()
+        t_all = allreduce(world, sum(total_s), "max")
+        t_dev = allreduce(world, sum(device_s), "max")
+        value = allreduce(world, float(E * steps), "sum") / t_dev
+        e2e_value = allreduce(world, float(E * steps), "sum") / t_all
+        parity = cpu = None
+        if rank == 0:
+            got = engine.download_graph()
+            t0 = time.perf_counter()
+            ref = ingest_oracle(V, path)
+            t_cpu = time.perf_counter() - t0
+            parity = {"edges": int(E),
+                      "mismatches": int(np.count_nonzero(ref["off"] != got["off"])
+                                        + np.count_nonzero(ref["nbr"].view(np.uint32) != got["nbr"])
+                                        + np.count_nonzero(ref["w"].view(np.uint32) != got["w"].view(np.uint32))),
+                      "what": "offsets, neighbours and weights of the loaded CSR vs the oracle's restatement of "
+                              "the reference's loader, bit for bit"}
+            cpu = {"value": E / t_cpu, "unit": "edges/s", "cores": 1, "kind": "port", "seconds": t_cpu,
+                   "sample": "the whole file: read, mirror, stable sort by source, offsets (numpy)"}
+    finally:
+        os.unlink(path)
+    engine.close()
+    if rank != 0:
+        return None
+    return {
+        "metric": "edges/s", "value": value, "unit": "edges/s", "n_gpus": world, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_all / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded R-MAT generated on the GPU, written as "
+                                                     "a binary edge file)",
+        "config": {"workload": args.workload, "desc": wl["desc"], "vertices": V, "edges": E,
+                   "file_records": E // 2, "file_bytes": file_bytes, "parallelism": "replicas",
+                   "l2": "inputs larger than L2"},
+        "device": {"ms_per_call": 1e3 * t_dev / steps,
+                   "what": "edge columns to HBM, stable radix sort by source, offsets, permutes"},
+        "e2e": {"value": e2e_value, "unit": "edges/s", "h2d_bytes_per_step": E * 12, "d2h_bytes_per_step": 0,
+                "what": "the whole kk_graph_load_binary call: file (page cache) -> CSR in HBM"},
+        "gpu_launches": launches,
+        "roofline": None,
+        "parity": parity,
+        "cpu_baseline": cpu,
+        "clocks": clocks.summary(),
+    }
+
+
 def run_workload(args, wl, world, rank, local):
+    if "ingest" in wl:
+        return run_ingest_bench(args, wl, world, rank, local)
     if "batch" in wl:
         return run_batch_bench(args, wl, world, rank, local)
     if "serve" in wl:

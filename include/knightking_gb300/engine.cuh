@@ -292,6 +292,9 @@ struct kk_engine
 
     /* graph */
     bool has_graph = false;
+    /* the last file load: the whole call and its device part (edge columns
+     * to the device, sort, offsets, permutes), host clocks in ms */
+    double load_total_ms = 0.0, load_device_ms = 0.0;
     uint32_t V = 0;
     uint64_t E = 0;
     int64_t *d_off = nullptr;

@@ -162,6 +162,14 @@ class WalkEngine:
         self._check(self._lib.kk_graph_load_binary(self._h, int(v_num), str(graph_path).encode(),
                                                    EDGE_KINDS[kind], int(bool(load_as_undirected))))
 
+    def load_timing(self):
+        """(total_ms, device_ms) of the last load_graph from a file: the whole
+        call and its device part (columns to HBM, sort by source, offsets)."""
+        total = ctypes.c_double()
+        dev = ctypes.c_double()
+        self._check(self._lib.kk_graph_load_timing(self._h, ctypes.byref(total), ctypes.byref(dev)))
+        return total.value, dev.value
+
     def load_arrays(self, v_num, off, nbr, w=None, etype=None):
         off = np.ascontiguousarray(off, dtype=np.int64)
         nbr = np.ascontiguousarray(nbr, dtype=np.uint32)

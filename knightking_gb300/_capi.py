@@ -120,6 +120,7 @@ _SIGS = {
     "kk_graph_load_binary": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]),
     "kk_graph_load_arrays": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_uint64, _P, _P, _P, _P]),
     "kk_graph_load_text": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]),
+    "kk_graph_load_timing": (ctypes.c_int, [_P, _P, _P]),
     "kk_text_to_binary": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, _P]),
     "kk_read_metapath_schemes": (ctypes.c_int, [ctypes.c_char_p, _P]),
     "kk_graph_generate_rmat": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, ctypes.c_double,

@@ -12,6 +12,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <chrono>
 #include <cub/cub.cuh>
 #include <string>
 #include <vector>
@@ -867,7 +868,9 @@ kk_status kk_graph_load_binary(kk_engine *e, uint32_t v_num, const char *path, i
     return guard(e, [&] {
         if (path == nullptr)
             fail(KK_ERR_INVALID_CONFIG, "path is NULL");
+        const auto t0 = std::chrono::steady_clock::now();
         graph_load_binary(e, v_num, path, edge_kind, make_undirected);
+        e->load_total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     });
 }
 
@@ -878,8 +881,19 @@ kk_status kk_graph_load_text(kk_engine *e, uint32_t v_num, const char *path, int
     return guard(e, [&] {
         if (path == nullptr)
             fail(KK_ERR_INVALID_CONFIG, "path is NULL");
+        const auto t0 = std::chrono::steady_clock::now();
         graph_load_text(e, v_num, path, weighted, make_undirected);
+        e->load_total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     });
+}
+
+kk_status kk_graph_load_timing(const kk_engine *e, double *total_ms, double *device_ms)
+{
+    if (!e || !total_ms || !device_ms)
+        return KK_ERR_INVALID_CONFIG;
+    *total_ms = e->load_total_ms;
+    *device_ms = e->load_device_ms;
+    return KK_OK;
 }
 
 kk_status kk_text_to_binary(const char *text_path, const char *binary_path, int weighted, uint64_t *edges)

@@ -15,13 +15,18 @@
  *     word0 -> uniform [1,5) weight 1 + 4*(w0>>8)*2^-24, or (words 2,3) a
  *     lognormal(0,1) weight by Box-Muller; word1 -> type floor(w1*types/2^32).
  */
+#include <fcntl.h>
 #include <stdio.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cub/cub.cuh>
+#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
@@ -449,6 +454,7 @@ void csr_from_edges(kk_engine *e, uint32_t V, uint64_t m, const uint32_t *h_src,
 {
     if (m >= 0xffffffffull)
         fail(KK_ERR_INVALID_CONFIG, "edge lists are limited to 2^32 - 1 edges");
+    const auto t0 = std::chrono::steady_clock::now();
     e->free_graph();
     struct Temps
     {
@@ -511,6 +517,7 @@ void csr_from_edges(kk_engine *e, uint32_t V, uint64_t m, const uint32_t *h_src,
     e->E = m;
     e->has_graph = true;
     e->sorted = -1;
+    e->load_device_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
 /* Text edge lists (read_edge_txt, include/storage.hpp:107-115): "src dst" or
@@ -673,61 +680,139 @@ void graph_load_binary(kk_engine *e, uint32_t V, const char *path, int kind, int
     }
     if (V == 0)
         fail(KK_ERR_INVALID_CONFIG, "v_num must be > 0");
-    FILE *f = fopen(path, "rb");
-    if (!f)
-        fail(KK_ERR_IO, std::string("cannot open ") + path);
-    fseek(f, 0, SEEK_END);
-    size_t bytes = (size_t)ftell(f);
-    fseek(f, 0, SEEK_SET);
-    size_t n = bytes / rec;
-    std::vector<unsigned char> raw(n * rec + 1);
-    size_t got = n ? fread(raw.data(), rec, n, f) : 0;
-    fclose(f);
-    if (got != n)
-        fail(KK_ERR_IO, std::string("short read from ") + path);
-    bool has_w = kind == KK_EDGE_F32 || kind == KK_EDGE_META_F32;
-    bool has_t = kind == KK_EDGE_META || kind == KK_EDGE_META_F32;
-    uint64_t m = undirected ? 2 * (uint64_t)n : n;
-    std::vector<uint32_t> src(m), dst(m);
-    std::vector<float> w(has_w ? m : 0);
-    std::vector<uint8_t> t(has_t ? m : 0);
-    for (size_t i = 0; i < n; i++)
+    struct File
     {
-        const unsigned char *r = raw.data() + i * rec;
-        uint32_t s, d;
-        memcpy(&s, r, 4);
-        memcpy(&d, r + 4, 4);
-        if (s >= V || d >= V)
-            fail(KK_ERR_INVALID_CONFIG, "edge endpoint >= v_num");
-        float wt = 0.0f;
-        int32_t ty = 0;
-        if (kind == KK_EDGE_F32 || kind == KK_EDGE_META_F32)
-            memcpy(&wt, r + 8, 4);
-        if (kind == KK_EDGE_META)
-            memcpy(&ty, r + 8, 4);
-        if (kind == KK_EDGE_META_F32)
-            memcpy(&ty, r + 12, 4);
-        if (has_t && (ty < 0 || ty >= 8))
-            fail(KK_ERR_INVALID_CONFIG, "edge types must be in [0, 8)");
-        size_t j = undirected ? 2 * i : i;
-        src[j] = s;
-        dst[j] = d;
-        if (has_w)
-            w[j] = wt;
-        if (has_t)
-            t[j] = (uint8_t)ty;
-        if (undirected)
+        int fd;
+        ~File()
         {
-            src[j + 1] = d;
-            dst[j + 1] = s;
-            if (has_w)
-                w[j + 1] = wt;
-            if (has_t)
-                t[j + 1] = (uint8_t)ty;
+            if (fd >= 0)
+                close(fd);
         }
+    } file{open(path, O_RDONLY)};
+    const int fd = file.fd;
+    if (fd < 0)
+        fail(KK_ERR_IO, std::string("cannot open ") + path);
+    struct stat sb;
+    if (fstat(fd, &sb) != 0)
+        fail(KK_ERR_IO, std::string("cannot stat ") + path);
+    const size_t n = (size_t)sb.st_size / rec;
+    const bool has_w = kind == KK_EDGE_F32 || kind == KK_EDGE_META_F32;
+    const bool has_t = kind == KK_EDGE_META || kind == KK_EDGE_META_F32;
+    const uint64_t m = undirected ? 2 * (uint64_t)n : n;
+    /* the columns, left uninitialised: every slot is written below */
+    std::unique_ptr<uint32_t[]> src(new uint32_t[m + 1]), dst(new uint32_t[m + 1]);
+    std::unique_ptr<float[]> w(has_w ? new float[m] : nullptr);
+    std::unique_ptr<uint8_t[]> t(has_t ? new uint8_t[m] : nullptr);
+    /* the records split among the host threads, each reading its share
+     * with pread in blocks and writing its columns' slots */
+    unsigned nt = std::thread::hardware_concurrency();
+    nt = nt == 0 ? 1 : nt > 32 ? 32 : nt;
+    if (n < (1u << 16))
+        nt = 1;
+    enum : int
+    {
+        kOk = 0,
+        kShort,
+        kEndpoint,
+        kType,
+        kAlloc
+    };
+    std::vector<int> err(nt, kOk);
+    auto split = [&](unsigned th) {
+        const size_t lo = n / nt * th + (th < n % nt ? th : n % nt);
+        const size_t hi = lo + n / nt + (th < n % nt ? 1 : 0);
+        const size_t block = ((size_t)4 << 20) / rec;
+        std::unique_ptr<unsigned char[]> buf(new unsigned char[block * rec]);
+        for (size_t b = lo; b < hi; b += block)
+        {
+            const size_t cnt = hi - b < block ? hi - b : block;
+            size_t done = 0;
+            while (done < cnt * rec)
+            {
+                const ssize_t r = pread(fd, buf.get() + done, cnt * rec - done, (off_t)(b * rec + done));
+                if (r <= 0)
+                {
+                    err[th] = kShort;
+                    return;
+                }
+                done += (size_t)r;
+            }
+            for (size_t k = 0; k < cnt; k++)
+            {
+                const unsigned char *r = buf.get() + k * rec;
+                uint32_t s, d;
+                memcpy(&s, r, 4);
+                memcpy(&d, r + 4, 4);
+                if (s >= V || d >= V)
+                {
+                    err[th] = kEndpoint;
+                    return;
+                }
+                float wt = 0.0f;
+                int32_t ty = 0;
+                if (kind == KK_EDGE_F32 || kind == KK_EDGE_META_F32)
+                    memcpy(&wt, r + 8, 4);
+                if (kind == KK_EDGE_META)
+                    memcpy(&ty, r + 8, 4);
+                if (kind == KK_EDGE_META_F32)
+                    memcpy(&ty, r + 12, 4);
+                if (has_t && (ty < 0 || ty >= 8))
+                {
+                    err[th] = kType;
+                    return;
+                }
+                const size_t i = b + k;
+                const size_t j = undirected ? 2 * i : i;
+                src[j] = s;
+                dst[j] = d;
+                if (has_w)
+                    w[j] = wt;
+                if (has_t)
+                    t[j] = (uint8_t)ty;
+                if (undirected)
+                {
+                    /* --make-undirected: each edge followed by its mirror */
+                    src[j + 1] = d;
+                    dst[j + 1] = s;
+                    if (has_w)
+                        w[j + 1] = wt;
+                    if (has_t)
+                        t[j + 1] = (uint8_t)ty;
+                }
+            }
+        }
+    };
+    auto work = [&](unsigned th) {
+        try
+        {
+            split(th);
+        }
+        catch (...)
+        {
+            err[th] = kAlloc;
+        }
+    };
+    {
+        std::vector<std::thread> pool;
+        for (unsigned th = 1; th < nt; th++)
+            pool.emplace_back(work, th);
+        work(0);
+        for (std::thread &x : pool)
+            x.join();
+    }
+    for (int x : err)
+    {
+        if (x == kAlloc)
+            fail(KK_ERR_OOM, "host allocation failed");
+        if (x == kShort)
+            fail(KK_ERR_IO, std::string("short read from ") + path);
+        if (x == kEndpoint)
+            fail(KK_ERR_INVALID_CONFIG, "edge endpoint >= v_num");
+        if (x == kType)
+            fail(KK_ERR_INVALID_CONFIG, "edge types must be in [0, 8)");
     }
     /* file order within a source, sorted on the device */
-    csr_from_edges(e, V, m, src.data(), dst.data(), has_w ? w.data() : nullptr, has_t ? t.data() : nullptr);
+    csr_from_edges(e, V, m, src.get(), dst.get(), w.get(), t.get());
 }
 
 void graph_generate_rmat(kk_engine *e, uint32_t scale, uint32_t ef, double a, double b, double c, uint64_t seed,

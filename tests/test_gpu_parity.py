@@ -273,6 +273,52 @@ def test_binary_file_load_matches_file_order(kk, engine, tmp_path):
     engine.load_graph(200, f, load_as_undirected=True, kind="f32")
     dg2 = engine.download_graph()
     np.testing.assert_array_equal(dg2["nbr"], csr["nbr"])
+    # the call's timing: the whole call, and the device part inside it
+    total_ms, device_ms = engine.load_timing()
+    assert 0.0 < device_ms <= total_ms
+
+
+def test_binary_file_load_in_parallel_and_refusals(kk, engine, tmp_path):
+    """A file of more than 2^16 records is read and split by several host
+    threads: the CSR still keeps file order within each source, with and
+    without --make-undirected (include/graph.hpp:309-330, :430-443).  A record
+    whose endpoint is >= v_num, or in a typed file whose type is outside
+    [0, 8), is refused, and the engine loads the next file."""
+    rng = np.random.default_rng(5)
+    V, n = 5000, 300_000
+    g = {"V": V, "src": rng.integers(0, V, n).astype(np.uint32), "dst": rng.integers(0, V, n).astype(np.uint32),
+         "w": rng.random(n, dtype=np.float32)}
+    f = tmp_path / "big.bin"
+    G.write_edge_file(f, g, "f32")
+    engine.load_graph(V, f, kind="f32")
+    dg = engine.download_graph()
+    csr = G.csr_file_order(V, g["src"], g["dst"], w=g["w"])
+    np.testing.assert_array_equal(dg["off"], csr["off"])
+    np.testing.assert_array_equal(dg["nbr"], csr["nbr"])
+    np.testing.assert_array_equal(dg["w"], csr["w"])
+    engine.load_graph(V, f, load_as_undirected=True, kind="f32")
+    dg2 = engine.download_graph()
+    s2 = np.empty(2 * n, np.uint32)
+    d2 = np.empty(2 * n, np.uint32)
+    s2[0::2], s2[1::2] = g["src"], g["dst"]
+    d2[0::2], d2[1::2] = g["dst"], g["src"]
+    csr2 = G.csr_file_order(V, s2, d2, w=np.repeat(g["w"], 2))
+    np.testing.assert_array_equal(dg2["off"], csr2["off"])
+    np.testing.assert_array_equal(dg2["nbr"], csr2["nbr"])
+    np.testing.assert_array_equal(dg2["w"], csr2["w"])
+    bad = dict(g, dst=g["dst"].copy())
+    bad["dst"][n - 7] = V
+    G.write_edge_file(f, bad, "f32")
+    with pytest.raises(kk.KKError):
+        engine.load_graph(V, f, kind="f32")
+    typed = dict(g, type=rng.integers(0, 8, n).astype(np.int32))
+    typed["type"][n // 3] = 9
+    G.write_edge_file(f, typed, "meta")
+    with pytest.raises(kk.KKError):
+        engine.load_graph(V, f, kind="meta")
+    G.write_edge_file(f, g, "f32")
+    engine.load_graph(V, f, kind="f32")
+    np.testing.assert_array_equal(engine.download_graph()["nbr"], csr["nbr"])
 
 
 @pytest.mark.parametrize("undirected", [False, True])

@@ -29,7 +29,8 @@ cpu_baseline / --impl reference: the oracle on all host cores over a bounded
 
 The default run also measures weighted DeepWalk on R-MAT scale 22 (alias build
 inside every step; e2e through kk_walk_into) and reports it under "also".
-Other workloads: --workload.
+Other workloads: --workload (single walks, batches of jobs, and ingest-s22, the
+load of a binary edge file into a CSR in HBM, in edges/s).
 
 Multi-GPU (torchrun): weak scaling, each rank walks its own walker-id range on
 its own replica of the graph; no collective on the data path.

@@ -444,7 +444,125 @@ __global__ void permute_kernel(const T *in, const uint32_t *perm, T *out, uint64
         out[i] = in[perm[i]];
 }
 
+/* One record of a binary edge file (words 32-bit words: src, dst[, weight])
+ * per thread: the source as the sort key, the destination and the weight's
+ * bits as the value; with --make-undirected the record at 2i and its mirror
+ * at 2i + 1.  An endpoint >= V sets *bad. */
+__global__ void split_records_kernel(const uint32_t *rec, uint32_t words, uint64_t n, uint32_t V, bool weighted,
+                                     bool undirected, uint32_t *key, uint64_t *val, uint32_t *bad)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    {
+        const uint32_t *r = rec + i * words;
+        const uint32_t s = r[0], d = r[1];
+        const uint64_t wb = weighted ? (uint64_t)r[2] << 32 : 0;
+        if (s >= V || d >= V)
+            atomicOr(bad, 1u);
+        const uint64_t j = undirected ? 2 * i : i;
+        key[j] = s;
+        val[j] = d | wb;
+        if (undirected)
+        {
+            key[j + 1] = d;
+            val[j + 1] = s | wb;
+        }
+    }
+}
+
+/* Offsets from the sorted sources: off[v] is the first position whose source
+ * is >= v (off[V] = m), written once per v by the position where the source
+ * steps past it. */
+__global__ void offsets_from_sorted_kernel(const uint32_t *s, uint64_t m, uint32_t V, int64_t *off)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i <= m; i += (uint64_t)gridDim.x * blockDim.x)
+    {
+        const int64_t lo = i == 0 ? -1 : (int64_t)s[i - 1];
+        const int64_t hi = i == m ? (int64_t)V : (int64_t)s[i];
+        for (int64_t v = lo + 1; v <= hi; v++)
+            off[v] = (int64_t)i;
+    }
+}
+
+__global__ void unpack_values_kernel(const uint64_t *val, uint64_t m, uint32_t *nbr, float *w)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x)
+    {
+        const uint64_t x = val[i];
+        nbr[i] = (uint32_t)x;
+        if (w != nullptr)
+            w[i] = __uint_as_float((uint32_t)(x >> 32));
+    }
+}
+
 } // namespace
+
+/* CSR in HBM from the raw records of an untyped binary edge file (8-byte
+ * src/dst or 12-byte src/dst/weight, include/storage.hpp:35-55) in host
+ * memory: the records go to the device as they are, are split (and mirrored,
+ * include/graph.hpp:430-443) there, and a stable radix sort of the sources
+ * carrying each edge's destination and weight keeps file order within each
+ * source (include/graph.hpp:309-330); the offsets come from the sorted
+ * sources.  The CSR equals csr_from_edges' of the same edges. */
+void csr_from_records(kk_engine *e, uint32_t V, uint64_t n, const unsigned char *h_rec, size_t rec, bool undirected)
+{
+    const uint64_t m = undirected ? 2 * n : n;
+    if (m >= 0xffffffffull)
+        fail(KK_ERR_INVALID_CONFIG, "edge lists are limited to 2^32 - 1 edges");
+    const auto t0 = std::chrono::steady_clock::now();
+    const bool weighted = rec == 12;
+    struct Temps
+    {
+        DevBuf raw, key, key2, val, val2;
+        ~Temps()
+        {
+            DevBuf *b[] = {&raw, &key, &key2, &val, &val2};
+            for (DevBuf *x : b)
+                x->release();
+        }
+    } tmp;
+    uint32_t *d_raw = tmp.raw.as<uint32_t>(n * (rec / 4) + 1);
+    uint32_t *d_key = tmp.key.as<uint32_t>(m + 1), *d_key2 = tmp.key2.as<uint32_t>(m + 1);
+    uint64_t *d_val = tmp.val.as<uint64_t>(m + 1), *d_val2 = tmp.val2.as<uint64_t>(m + 1);
+    uint32_t *bad = (uint32_t *)e->small.ensure(64) + 13; /* a word the walks' status does not use */
+    KK_CUDA_CHECK(cudaMemsetAsync(bad, 0, sizeof(uint32_t), e->stream));
+    if (n)
+        KK_CUDA_CHECK(cudaMemcpyAsync(d_raw, h_rec, n * rec, cudaMemcpyHostToDevice, e->stream));
+    split_records_kernel<<<grid_for(e, n ? n : 1, 256), 256, 0, e->stream>>>(d_raw, (uint32_t)(rec / 4), n, V, weighted,
+                                                                             undirected, d_key, d_val, bad);
+    count_launch(e);
+    KK_CUDA_CHECK(cudaGetLastError());
+    words_to_host(e, bad, 41, 1);
+    KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+    if (((volatile uint32_t *)e->h_status)[41] != 0)
+        fail(KK_ERR_INVALID_CONFIG, "edge endpoint >= v_num"); /* the engine keeps its graph */
+    tmp.raw.release();
+    e->free_graph();
+    int bits = 1;
+    while (bits < 32 && ((uint64_t)1 << bits) < V)
+        bits++;
+    size_t bytes = 0;
+    KK_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(nullptr, bytes, d_key, d_key2, d_val, d_val2, (int64_t)m, 0, bits,
+                                                  e->stream));
+    KK_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(e->cub_tmp.ensure(bytes), bytes, d_key, d_key2, d_val, d_val2,
+                                                  (int64_t)m, 0, bits, e->stream));
+    KK_CUDA_CHECK(cudaMalloc(&e->d_off, ((uint64_t)V + 1) * sizeof(int64_t)));
+    offsets_from_sorted_kernel<<<grid_for(e, m + 1, 256), 256, 0, e->stream>>>(d_key2, m, V, e->d_off);
+    count_launch(e);
+    KK_CUDA_CHECK(cudaGetLastError());
+    KK_CUDA_CHECK(cudaMalloc(&e->d_nbr, m * 4 + 4));
+    if (weighted)
+        KK_CUDA_CHECK(cudaMalloc(&e->d_w, m * 4 + 4));
+    unpack_values_kernel<<<grid_for(e, m ? m : 1, 256), 256, 0, e->stream>>>(d_val2, m, e->d_nbr,
+                                                                             weighted ? e->d_w : nullptr);
+    count_launch(e);
+    KK_CUDA_CHECK(cudaGetLastError());
+    KK_CUDA_CHECK(cudaStreamSynchronize(e->stream));
+    e->V = V;
+    e->E = m;
+    e->has_graph = true;
+    e->sorted = -1;
+    e->load_device_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
 
 /* CSR in HBM from an edge list in file order (include/graph.hpp:309-330):
  * a stable radix sort of the edge positions by source keeps file order within
@@ -699,16 +817,51 @@ void graph_load_binary(kk_engine *e, uint32_t V, const char *path, int kind, int
     const bool has_w = kind == KK_EDGE_F32 || kind == KK_EDGE_META_F32;
     const bool has_t = kind == KK_EDGE_META || kind == KK_EDGE_META_F32;
     const uint64_t m = undirected ? 2 * (uint64_t)n : n;
+    unsigned nt = std::thread::hardware_concurrency();
+    nt = nt == 0 ? 1 : nt > 32 ? 32 : nt;
+    if (n < (1u << 16))
+        nt = 1;
+    if (!has_t)
+    {
+        /* untyped records go to the device as read (all host threads, each
+         * its share with pread) and are split there */
+        std::unique_ptr<unsigned char[]> raw(new unsigned char[n * rec + 1]);
+        std::vector<char> short_read(nt, 0);
+        auto read_share = [&](unsigned th) {
+            const size_t total = n * rec;
+            size_t lo = total / nt * th, hi = th + 1 == nt ? total : total / nt * (th + 1);
+            while (lo < hi)
+            {
+                const ssize_t r = pread(fd, raw.get() + lo, hi - lo, (off_t)lo);
+                if (r <= 0)
+                {
+                    short_read[th] = 1;
+                    return;
+                }
+                lo += (size_t)r;
+            }
+        };
+        {
+            std::vector<std::thread> pool;
+            for (unsigned th = 1; th < nt; th++)
+                pool.emplace_back(read_share, th);
+            read_share(0);
+            for (std::thread &x : pool)
+                x.join();
+        }
+        for (char x : short_read)
+            if (x)
+                fail(KK_ERR_IO, std::string("short read from ") + path);
+        csr_from_records(e, V, n, raw.get(), rec, undirected);
+        return;
+    }
+    /* typed records: split into columns on the host */
     /* the columns, left uninitialised: every slot is written below */
     std::unique_ptr<uint32_t[]> src(new uint32_t[m + 1]), dst(new uint32_t[m + 1]);
     std::unique_ptr<float[]> w(has_w ? new float[m] : nullptr);
     std::unique_ptr<uint8_t[]> t(has_t ? new uint8_t[m] : nullptr);
     /* the records split among the host threads, each reading its share
      * with pread in blocks and writing its columns' slots */
-    unsigned nt = std::thread::hardware_concurrency();
-    nt = nt == 0 ? 1 : nt > 32 ? 32 : nt;
-    if (n < (1u << 16))
-        nt = 1;
     enum : int
     {
         kOk = 0,

@@ -283,7 +283,9 @@ def test_binary_file_load_in_parallel_and_refusals(kk, engine, tmp_path):
     threads: the CSR still keeps file order within each source, with and
     without --make-undirected (include/graph.hpp:309-330, :430-443).  A record
     whose endpoint is >= v_num, or in a typed file whose type is outside
-    [0, 8), is refused, and the engine loads the next file."""
+    [0, 8), is refused; the engine keeps its graph and loads the next file.
+    Untyped records are split on the device, typed ones on the host: both
+    paths are covered, unweighted too."""
     rng = np.random.default_rng(5)
     V, n = 5000, 300_000
     g = {"V": V, "src": rng.integers(0, V, n).astype(np.uint32), "dst": rng.integers(0, V, n).astype(np.uint32),
@@ -316,9 +318,25 @@ def test_binary_file_load_in_parallel_and_refusals(kk, engine, tmp_path):
     G.write_edge_file(f, typed, "meta")
     with pytest.raises(kk.KKError):
         engine.load_graph(V, f, kind="meta")
+    # a refused file leaves the engine's graph as it was
+    np.testing.assert_array_equal(engine.download_graph()["nbr"], csr2["nbr"])
     G.write_edge_file(f, g, "f32")
     engine.load_graph(V, f, kind="f32")
     np.testing.assert_array_equal(engine.download_graph()["nbr"], csr["nbr"])
+    # unweighted records, and typed ones (split on the host), in file order
+    G.write_edge_file(f, g, "none")
+    engine.load_graph(V, f, load_as_undirected=True, kind="unweighted")
+    dg3 = engine.download_graph()
+    np.testing.assert_array_equal(dg3["off"], csr2["off"])
+    np.testing.assert_array_equal(dg3["nbr"], csr2["nbr"])
+    assert dg3["w"] is None
+    typed["type"][n // 3] = 4
+    G.write_edge_file(f, typed, "meta")
+    engine.load_graph(V, f, kind="meta")
+    dg4 = engine.download_graph()
+    csr4 = G.csr_file_order(V, g["src"], g["dst"], type=typed["type"])
+    np.testing.assert_array_equal(dg4["nbr"], csr4["nbr"])
+    np.testing.assert_array_equal(dg4["type"], csr4["type"])
 
 
 @pytest.mark.parametrize("undirected", [False, True])

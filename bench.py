@@ -1155,10 +1155,11 @@ def run_ingest_bench(args, wl, world, rank, local):
     """Graph ingestion, the step before the walk: kk_graph_load_binary of a
     binary Edge<float> file with --make-undirected into a CSR in HBM.
 
-    value : CSR edges per second of the call's device part (the file's
-            records copied to HBM and split there, mirrored, the stable radix
-            sort by source carrying each edge's destination and weight,
-            offsets from the sorted sources; kk_graph_load_timing), K calls.
+    value : CSR edges per second of the call's device part, from the file's
+            records in HBM (read and copied in overlapped blocks) to the CSR:
+            split and mirror, the stable radix sort by source carrying each
+            edge's destination and weight, offsets from the sorted sources,
+            unpack (kk_graph_load_timing), K calls.
     e2e   : CSR edges per second of the whole call, file (in the page cache)
             to CSR in HBM.
     parity: the loaded CSR (offsets, neighbours, weights) against the oracle's
@@ -1228,8 +1229,8 @@ def run_ingest_bench(args, wl, world, rank, local):
                    "file_records": E // 2, "file_bytes": file_bytes, "parallelism": "replicas",
                    "l2": "inputs larger than L2"},
         "device": {"ms_per_call": 1e3 * t_dev / steps,
-                   "what": "records to HBM, split and mirrored there, stable radix sort by source carrying "
-                           "destination and weight, offsets from the sorted sources"},
+                   "what": "from the records in HBM: split and mirror, stable radix sort by source carrying "
+                           "destination and weight, offsets from the sorted sources, unpack"},
         "e2e": {"value": e2e_value, "unit": "edges/s", "h2d_bytes_per_step": E * 12, "d2h_bytes_per_step": 0,
                 "what": "the whole kk_graph_load_binary call: file (page cache) -> CSR in HBM"},
         "gpu_launches": launches,

@@ -158,11 +158,12 @@ kk_status kk_graph_load_binary(kk_engine *e, uint32_t v_num, const char *path, i
  * as kk_graph_load_binary. */
 kk_status kk_graph_load_text(kk_engine *e, uint32_t v_num, const char *path, int weighted, int make_undirected);
 /* Timing of the engine's last kk_graph_load_binary / kk_graph_load_text call
- * (host clocks, ms): the whole call, and its device part (from the edges'
- * copy to the device to the CSR in HBM: split and mirror of untyped binary
- * records, stable sort by source, offsets, per-edge data in sorted order);
- * the rest is the file read (and, for text and typed files, the split into
- * columns) on the host.  No counterpart in the reference. */
+ * (host clocks, ms): the whole call, and its device part.  For untyped binary
+ * files the records are read and copied to the device in overlapped blocks,
+ * and the device part runs from the records in HBM to the CSR (split and
+ * mirror, stable sort by source, offsets, unpack); for text and typed files
+ * the host splits the edges into columns, and the device part runs from their
+ * copy to the device to the CSR.  No counterpart in the reference. */
 kk_status kk_graph_load_timing(const kk_engine *e, double *total_ms, double *device_ms);
 
 /* gconverter (src/tools/gconverter.cpp:69-100): a text edge list to the

@@ -292,9 +292,16 @@ struct kk_engine
 
     /* graph */
     bool has_graph = false;
-    /* the last file load: the whole call and its device part (edge columns
-     * to the device, sort, offsets, permutes), host clocks in ms */
+    /* the last file load: the whole call and its device part, host clocks
+     * in ms */
     double load_total_ms = 0.0, load_device_ms = 0.0;
+    /* the binary loader's readers: per reader two pinned blocks, a stream
+     * and two events, made on the first untyped file load and kept */
+    static constexpr int kReaders = 16;
+    static constexpr size_t kReadBlock = (size_t)4 << 20;
+    unsigned char *read_pinned = nullptr; /* kReaders x 2 x kReadBlock */
+    cudaStream_t read_st[kReaders] = {};
+    cudaEvent_t read_ev[kReaders][2] = {};
     uint32_t V = 0;
     uint64_t E = 0;
     int64_t *d_off = nullptr;

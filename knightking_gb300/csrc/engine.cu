@@ -736,6 +736,19 @@ void kk_engine_destroy(kk_engine *e)
     e->adjc.release();
     if (e->h_status)
         cudaFreeHost(e->h_status);
+    for (int r = 0; r < kk_engine::kReaders; r++)
+    {
+        if (e->read_st[r])
+        {
+            cudaStreamSynchronize(e->read_st[r]);
+            cudaStreamDestroy(e->read_st[r]);
+        }
+        for (int b = 0; b < 2; b++)
+            if (e->read_ev[r][b])
+                cudaEventDestroy(e->read_ev[r][b]);
+    }
+    if (e->read_pinned)
+        cudaFreeHost(e->read_pinned);
     if (e->copy_stream)
     {
         cudaStreamSynchronize(e->copy_stream);

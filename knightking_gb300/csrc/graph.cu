@@ -497,18 +497,18 @@ __global__ void unpack_values_kernel(const uint64_t *val, uint64_t m, uint32_t *
 } // namespace
 
 /* CSR in HBM from the raw records of an untyped binary edge file (8-byte
- * src/dst or 12-byte src/dst/weight, include/storage.hpp:35-55) in host
- * memory: the records go to the device as they are, are split (and mirrored,
+ * src/dst or 12-byte src/dst/weight, include/storage.hpp:35-55), which
+ * fill(d) puts into device memory at d as they are; they are split (and mirrored,
  * include/graph.hpp:430-443) there, and a stable radix sort of the sources
  * carrying each edge's destination and weight keeps file order within each
  * source (include/graph.hpp:309-330); the offsets come from the sorted
  * sources.  The CSR equals csr_from_edges' of the same edges. */
-void csr_from_records(kk_engine *e, uint32_t V, uint64_t n, const unsigned char *h_rec, size_t rec, bool undirected)
+template <typename Fill>
+void csr_from_records(kk_engine *e, uint32_t V, uint64_t n, size_t rec, bool undirected, Fill fill)
 {
     const uint64_t m = undirected ? 2 * n : n;
     if (m >= 0xffffffffull)
         fail(KK_ERR_INVALID_CONFIG, "edge lists are limited to 2^32 - 1 edges");
-    const auto t0 = std::chrono::steady_clock::now();
     const bool weighted = rec == 12;
     struct Temps
     {
@@ -524,9 +524,11 @@ void csr_from_records(kk_engine *e, uint32_t V, uint64_t n, const unsigned char 
     uint32_t *d_key = tmp.key.as<uint32_t>(m + 1), *d_key2 = tmp.key2.as<uint32_t>(m + 1);
     uint64_t *d_val = tmp.val.as<uint64_t>(m + 1), *d_val2 = tmp.val2.as<uint64_t>(m + 1);
     uint32_t *bad = (uint32_t *)e->small.ensure(64) + 13; /* a word the walks' status does not use */
+    /* the records in HBM, as read (fill returns once they have arrived) */
+    fill((unsigned char *)d_raw);
+    /* the device part: from the records in HBM to the CSR */
+    const auto t0 = std::chrono::steady_clock::now();
     KK_CUDA_CHECK(cudaMemsetAsync(bad, 0, sizeof(uint32_t), e->stream));
-    if (n)
-        KK_CUDA_CHECK(cudaMemcpyAsync(d_raw, h_rec, n * rec, cudaMemcpyHostToDevice, e->stream));
     split_records_kernel<<<grid_for(e, n ? n : 1, 256), 256, 0, e->stream>>>(d_raw, (uint32_t)(rec / 4), n, V, weighted,
                                                                              undirected, d_key, d_val, bad);
     count_launch(e);
@@ -823,36 +825,83 @@ void graph_load_binary(kk_engine *e, uint32_t V, const char *path, int kind, int
         nt = 1;
     if (!has_t)
     {
-        /* untyped records go to the device as read (all host threads, each
-         * its share with pread) and are split there */
-        std::unique_ptr<unsigned char[]> raw(new unsigned char[n * rec + 1]);
-        std::vector<char> short_read(nt, 0);
-        auto read_share = [&](unsigned th) {
-            const size_t total = n * rec;
-            size_t lo = total / nt * th, hi = th + 1 == nt ? total : total / nt * (th + 1);
-            while (lo < hi)
+        /* untyped records go to the device as read and are split there:
+         * each reader thread takes its share of the file in blocks, reading
+         * one block into a pinned buffer while the copy of the previous one
+         * (its other buffer) runs on its own stream */
+        const unsigned nr = nt < (unsigned)kk_engine::kReaders ? nt : (unsigned)kk_engine::kReaders;
+        const size_t blk = kk_engine::kReadBlock;
+        if (e->read_pinned == nullptr)
+        {
+            KK_CUDA_CHECK(cudaHostAlloc((void **)&e->read_pinned, (size_t)kk_engine::kReaders * 2 * blk,
+                                        cudaHostAllocDefault));
+            for (int r = 0; r < kk_engine::kReaders; r++)
             {
-                const ssize_t r = pread(fd, raw.get() + lo, hi - lo, (off_t)lo);
-                if (r <= 0)
+                KK_CUDA_CHECK(cudaStreamCreateWithFlags(&e->read_st[r], cudaStreamNonBlocking));
+                for (int b = 0; b < 2; b++)
+                    KK_CUDA_CHECK(cudaEventCreateWithFlags(&e->read_ev[r][b], cudaEventDisableTiming));
+            }
+        }
+        auto fill = [&](unsigned char *d_raw) {
+            const size_t total = n * rec;
+            std::vector<int> failed(nr, 0); /* 1: short read, 2: CUDA */
+            auto read_share = [&](unsigned th) {
+                size_t pos = total / nr * th;
+                const size_t hi = th + 1 == nr ? total : total / nr * (th + 1);
+                unsigned char *buf[2] = {e->read_pinned + (size_t)th * 2 * blk,
+                                         e->read_pinned + ((size_t)th * 2 + 1) * blk};
+                for (unsigned k = 0; pos < hi; k++)
                 {
-                    short_read[th] = 1;
-                    return;
+                    const size_t len = hi - pos < blk ? hi - pos : blk;
+                    /* the buffer's previous copy has left it */
+                    if (k >= 2 && cudaEventSynchronize(e->read_ev[th][k & 1]) != cudaSuccess)
+                    {
+                        failed[th] = 2;
+                        return;
+                    }
+                    size_t got = 0;
+                    while (got < len)
+                    {
+                        const ssize_t r = pread(fd, buf[k & 1] + got, len - got, (off_t)(pos + got));
+                        if (r <= 0)
+                        {
+                            failed[th] = 1;
+                            return;
+                        }
+                        got += (size_t)r;
+                    }
+                    if (cudaMemcpyAsync(d_raw + pos, buf[k & 1], len, cudaMemcpyHostToDevice, e->read_st[th]) !=
+                            cudaSuccess ||
+                        cudaEventRecord(e->read_ev[th][k & 1], e->read_st[th]) != cudaSuccess)
+                    {
+                        failed[th] = 2;
+                        return;
+                    }
+                    pos += len;
                 }
-                lo += (size_t)r;
+            };
+            {
+                std::vector<std::thread> pool;
+                for (unsigned th = 1; th < nr; th++)
+                    pool.emplace_back(read_share, th);
+                read_share(0);
+                for (std::thread &x : pool)
+                    x.join();
+            }
+            /* every copy issued has landed before the buffers are reused or
+             * the records are read */
+            for (unsigned th = 0; th < nr; th++)
+                if (cudaStreamSynchronize(e->read_st[th]) != cudaSuccess)
+                    failed[th] = 2;
+            for (int x : failed)
+            {
+                if (x == 1)
+                    fail(KK_ERR_IO, std::string("short read from ") + path);
+                if (x == 2)
+                    fail(KK_ERR_CUDA, "copy of the edge records to the device");
             }
         };
-        {
-            std::vector<std::thread> pool;
-            for (unsigned th = 1; th < nt; th++)
-                pool.emplace_back(read_share, th);
-            read_share(0);
-            for (std::thread &x : pool)
-                x.join();
-        }
-        for (char x : short_read)
-            if (x)
-                fail(KK_ERR_IO, std::string("short read from ") + path);
-        csr_from_records(e, V, n, raw.get(), rec, undirected);
+        csr_from_records(e, V, n, rec, undirected, fill);
         return;
     }
     /* typed records: split into columns on the host */

@@ -149,7 +149,11 @@ const char *kk_status_string(kk_status s);
 /* Reads the reference's binary edge-list file (include/storage.hpp:35-55),
  * optionally mirrors every edge (--make-undirected, include/graph.hpp:430-443),
  * and builds the CSR in HBM with file order kept per source
- * (include/graph.hpp:309-330). */
+ * (include/graph.hpp:309-330).  Untyped files are streamed to the device by
+ * up to 16 host threads; the engine's first such load allocates 128 MiB of
+ * pinned host memory for them (two 4 MiB buffers per thread), kept until
+ * kk_engine_destroy.  A refused file (an endpoint >= v_num, a type outside
+ * [0, 8)) leaves the engine's graph as it was. */
 kk_status kk_graph_load_binary(kk_engine *e, uint32_t v_num, const char *path, int edge_kind, int make_undirected);
 
 /* Reads a text edge list (read_edge_txt, include/storage.hpp:107-115): one
